@@ -1,0 +1,1115 @@
+// wg_oracle.cpp -- CPU oracle for the WABBIT ACM block-level time-step hot path.
+//
+// TEST INFRASTRUCTURE ONLY. This file is a scalar, line-by-line restatement of
+// the reference's Fortran algorithms for the hot path, used by tests/, by
+// __graft_entry__.smoke() and by bench.py's cpu_baseline leg as the checker.
+// The product (wabbit_gb300/) never links, imports or calls it.
+//
+// It is compiled with -ffp-contract=off so that every floating-point
+// expression is evaluated with the reference's (x86-64, no FMA) rounding in the
+// reference's left-to-right order. Array indices in the patch-geometry code
+// are kept 1-based, as in the Fortran, and converted only at array access.
+//
+// Parity: pinned against the reference's committed regression files
+// (TESTING/acm/3vortices/3vorticesEquiFD4_CDF40, TESTING/acm/taylorGreen/
+// taylorGreenEqui_FD4_CDF40, TESTING/wavelets/adaptive_CDF4x) through fixtures
+// generated by tests/golden/make_fixtures.py.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/wabbit_gb300.h"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// wavelet filters: setup_wavelet (LIB/WAVELETS/module_wavelets.f90:1031-1561)
+// ---------------------------------------------------------------------------
+struct Filter {           // coefficients f(lo..hi)
+    int lo = 0, hi = -1;
+    std::vector<double> c;
+    double operator()(int i) const { return c[i - lo]; }
+    void init(int l, int h) { lo = l; hi = h; c.assign(h - l + 1, 0.0); }
+};
+
+// interpolation stencils with added zeros (module_wavelets.f90:14-22)
+static void stencil_int(int order, Filter &f) {
+    switch (order) {
+    case 2: f.init(-1, 1); { double v[] = {1, 2, 1}; for (int i = 0; i < 3; i++) f.c[i] = v[i] / 2.0; } break;
+    case 4: f.init(-3, 3); { double v[] = {-1, 0, 9, 16, 9, 0, -1}; for (int i = 0; i < 7; i++) f.c[i] = v[i] / 16.0; } break;
+    case 6: f.init(-5, 5); { double v[] = {3, 0, -25, 0, 150, 256, 150, 0, -25, 0, 3}; for (int i = 0; i < 11; i++) f.c[i] = v[i] / 256.0; } break;
+    case 8: f.init(-7, 7); { double v[] = {-5, 0, 49, 0, -245, 0, 1225, 2048, 1225, 0, -245, 0, 49, 0, -5}; for (int i = 0; i < 15; i++) f.c[i] = v[i] / 2048.0; } break;
+    default: f.init(0, -1);
+    }
+}
+
+struct Wavelet {
+    int X = 4, Y = 0;
+    bool lifted = false;
+    Filter HD, GD, HR, GR;
+    int order_predictor = 4;
+    int Nscl = 0, Nscr = 0, Nwcl = 0, Nwcr = 0;
+    std::string name;
+};
+
+static bool setup_wavelet(const char *name, int fd_max_size, Wavelet &w) {
+    w.name = name;
+    if (std::strncmp(name, "CDF", 3) != 0 || std::strlen(name) < 5) return false;
+    w.X = name[3] - '0';
+    w.Y = name[4] - '0';
+    if (w.X != 2 && w.X != 4 && w.X != 6 && w.X != 8) return false;
+    if (w.Y != 0 && w.Y != 2 && w.Y != 4 && w.Y != 6 && w.Y != 8) return false;
+    stencil_int(w.X, w.HR);
+    if (w.Y == 0) {
+        w.HD.init(0, 0);
+        w.HD.c[0] = 1.0;
+    } else if (w.X >= w.Y) {
+        Filter h;
+        stencil_int(w.Y, h);
+        h.c[0 - h.lo] = 0.0;
+        w.HD.init(w.HR.lo + h.lo, w.HR.hi + h.hi);
+        for (int i = w.HD.lo; i <= w.HD.hi; i++) {
+            double v = (i == 0) ? 1.0 : 0.0;
+            for (int j = w.HR.lo; j <= w.HR.hi; j++) {
+                if (i - j < h.lo || i - j > h.hi) continue;
+                // (-1.0_rk)**j * HR(j) * h_ntilde(i-j) / 2.0_rk
+                double sgn = (std::abs(j) % 2 == 0) ? 1.0 : -1.0;
+                v = v + sgn * w.HR(j) * h(i - j) / 2.0;
+            }
+            w.HD.c[i - w.HD.lo] = v;
+        }
+    } else {
+        return false;  // CDF24/26/28/46 not needed on this path
+    }
+    w.GD.init(w.HR.lo, w.HR.hi);
+    for (int i = w.GD.lo; i <= w.GD.hi; i++) w.GD.c[i - w.GD.lo] = ((std::abs(i) % 2 == 0) ? 1.0 : -1.0) * w.HR(i);
+    w.GR.init(w.HD.lo, w.HD.hi);
+    for (int i = w.GR.lo; i <= w.GR.hi; i++) w.GR.c[i - w.GR.lo] = ((std::abs(i) % 2 == 0) ? 1.0 : -1.0) * w.HD(i);
+    w.lifted = (w.Y != 0);
+    w.order_predictor = w.X;
+    // coarse-extension widths (module_wavelets.f90:1341-1375)
+    w.Nscl = std::max(std::abs(w.HD.lo) - 1, 0);
+    w.Nwcl = w.Nscl + std::abs(w.GD.lo);
+    w.Nscr = w.HD.hi;
+    w.Nwcr = w.Nscr + w.GD.hi;
+    int i2 = 2 * fd_max_size;
+    w.Nwcl += std::max(i2 - w.Nwcl, 0);
+    w.Nwcr += std::max(i2 - w.Nwcr, 0);
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// forest: blocks, levels, neighbour relations
+// ---------------------------------------------------------------------------
+struct Block {
+    int level;
+    int c[3];
+};
+
+static inline uint64_t key_of(int level, int x, int y, int z) {
+    return (uint64_t(level) << 60) | (uint64_t(x) << 40) | (uint64_t(y) << 20) | uint64_t(z);
+}
+
+struct Oracle {
+    wg_config cfg;
+    Wavelet wav;
+    int nx, ny, nz, nc, npts;       // block extents incl. ghosts
+    std::vector<Block> blocks;
+    std::vector<double> data;       // nblk * nc * npts
+    std::vector<double> mask;       // nblk * 6 * npts (optional)
+    std::vector<int> nb;            // nblk * 168
+    std::unordered_map<uint64_t, int> lookup;
+    // RK registers: slot 0 = u_n, 1..4 = k1..k4 (full blocks, as hvy_work)
+    std::vector<double> work;
+    int nthreads = 1;
+
+    double *blk(int b) { return data.data() + size_t(b) * nc * npts; }
+    const double *blk(int b) const { return data.data() + size_t(b) * nc * npts; }
+    // 1-based Fortran indexing into a block array
+    inline size_t at(int ix, int iy, int iz, int ic) const {
+        return ((size_t(ic - 1) * nz + (iz - 1)) * ny + (iy - 1)) * nx + (ix - 1);
+    }
+};
+
+// treecode digit of a block at its own level: bit0 = y, bit1 = x, bit2 = z
+// (LIB/TREE/module_treelib.f90 encoding_b/decoding_b, find_neighbors.f90:46)
+static inline int tc_last_digit(const Block &b) {
+    return 2 * (b.c[0] & 1) + (b.c[1] & 1) + 4 * (b.c[2] & 1);
+}
+
+static void rebuild_lookup(Oracle &o) {
+    o.lookup.clear();
+    for (int i = 0; i < (int)o.blocks.size(); i++) {
+        const Block &b = o.blocks[i];
+        o.lookup[key_of(b.level, b.c[0], b.c[1], b.c[2])] = i;
+    }
+}
+
+static int find_block(const Oracle &o, int level, const int c[3]) {
+    auto it = o.lookup.find(key_of(level, c[0], c[1], c[2]));
+    return it == o.lookup.end() ? -1 : it->second;
+}
+
+// adjacent block coordinates on `level` in direction d (periodic domain)
+static void adjacent(const int c[3], const int d[3], int level, int dim, int out[3]) {
+    int n = 1 << level;
+    for (int i = 0; i < 3; i++) {
+        if (i < dim) out[i] = ((c[i] + d[i]) % n + n) % n;
+        else out[i] = 0;
+    }
+}
+
+// find_neighbor (LIB/MESH/find_neighbors.f90:18-215) for one direction
+static void find_neighbor(Oracle &o, int ib, const int dir_dim[3]) {
+    const int dim = o.cfg.dim;
+    const Block &B = o.blocks[ib];
+    const int level = B.level;
+    int nzero = 0;
+    for (int i = 0; i < 3; i++) if (dir_dim[i] == 0) nzero++;
+    int dir_free = 1 << nzero;
+    if (dim == 2) dir_free /= 2;
+    int tcFiner[4] = {0, 0, 0, 0};
+    const int vary_tc[3] = {2, 1, 4};
+    int apply_free = 1;
+    for (int i = 0; i < dim; i++) {
+        if (dir_dim[i] == 0) {
+            for (int k = 0; k < 4; k++) tcFiner[k] += vary_tc[i] * ((k / apply_free) % 2);
+            apply_free++;
+        } else if (dir_dim[i] == 1) {
+            for (int k = 0; k < 4; k++) tcFiner[k] += vary_tc[i];
+        }
+    }
+    int same = -1;
+    if (nzero == 2) {
+        same = 1;
+        for (int i = 0; i < 3; i++) {
+            if (dir_dim[i] != 0) same += 8 * i;
+            if (dir_dim[i] == 1) same += 4;
+        }
+    } else if (nzero == 1) {
+        same = 25;
+        int af = 1;
+        for (int i = 0; i < 3; i++) {
+            if (dir_dim[i] == 0) same += 8 * (2 - i);
+            else if (dir_dim[i] == 1) { same += af * 2; af++; }
+            else af++;
+        }
+    } else {
+        same = 49;
+        for (int i = 0; i < 3; i++) if (dir_dim[i] == 1) same += 1 << i;
+    }
+    int coarser = -1;
+    const int tc_last = tc_last_digit(B);
+    for (int k = 0; k < dir_free; k++) if (tc_last == tcFiner[k]) coarser = same + k;
+
+    int *nbr = o.nb.data() + size_t(ib) * 168;
+    int d[3] = {dir_dim[0], dir_dim[1], dim == 3 ? dir_dim[2] : 0};
+    int cn[3];
+    if (level == 0) {
+        nbr[same - 1] = ib;
+        return;
+    }
+    adjacent(B.c, d, level, dim, cn);
+    int idn = find_block(o, level, cn);
+    if (idn >= 0) { nbr[same - 1] = idn; return; }
+    if (level < o.cfg.Jmax) {
+        for (int k = 0; k < dir_free; k++) {
+            int dig = tcFiner[k];
+            int vc[3] = {2 * B.c[0] + ((dig >> 1) & 1), 2 * B.c[1] + (dig & 1), 2 * B.c[2] + ((dig >> 2) & 1)};
+            if (dim == 2) vc[2] = 0;
+            int cf[3];
+            adjacent(vc, d, level + 1, dim, cf);
+            int idf = find_block(o, level + 1, cf);
+            if (idf >= 0) nbr[same + k - 1 + 2 * 56] = idf;
+            else break;
+            if (k == dir_free - 1) return;
+        }
+    }
+    if (coarser != -1 && level > o.cfg.Jmin) {
+        int cp[3] = {cn[0] >> 1, cn[1] >> 1, cn[2] >> 1};
+        if (dim == 2) cp[2] = 0;
+        int idc = find_block(o, level - 1, cp);
+        if (idc >= 0) nbr[coarser - 1 + 56] = idc;
+    }
+}
+
+static void update_neighbors(Oracle &o) {
+    rebuild_lookup(o);
+    const int nb = (int)o.blocks.size();
+    o.nb.assign(size_t(nb) * 168, -1);
+    const int dim = o.cfg.dim;
+    for (int ib = 0; ib < nb; ib++) {
+        for (int dz = (dim == 3 ? -1 : 0); dz <= (dim == 3 ? 1 : 0); dz++)
+            for (int dy = -1; dy <= 1; dy++)
+                for (int dx = -1; dx <= 1; dx++) {
+                    if (dx == 0 && dy == 0 && dz == 0) continue;
+                    int dd[3] = {dx, dy, dz};
+                    find_neighbor(o, ib, dd);
+                }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// patch geometry (LIB/TREE/neighborhood.f90, LIB/MPI/calc_data_bounds.f90)
+// idx(1:2,1:3) kept as idx[lr][dim] with 1-based values.
+// ---------------------------------------------------------------------------
+static bool in_list(int r, std::initializer_list<int> l) {
+    for (int v : l) if (v == r) return true;
+    return false;
+}
+
+// get_indices_of_modify_patch (neighborhood.f90:23-126)
+static void modify_patch(int dim, int relation, int idx[2][3], const int N[3], const int Ns[3], const int Ne[3],
+                         const int gm[3], const int gp[3], int lvlDiff) {
+    int r = relation > 56 ? (relation - 1) % 56 + 1 : relation;
+    for (int d = 0; d < 3; d++) { idx[0][d] = 1; idx[1][d] = 1; }
+    for (int d = 0; d < dim; d++) { idx[0][d] = 1 + gm[d]; idx[1][d] = N[d] - gp[d]; }
+    if (in_list(r, {1, 2, 3, 4, 25, 26, 29, 30, 33, 34, 37, 38, 49, 51, 53, 55})) idx[1][0] = Ns[0] + gm[0];
+    if (in_list(r, {5, 6, 7, 8, 27, 28, 31, 32, 35, 36, 39, 40, 50, 52, 54, 56})) idx[0][0] = N[0] - Ne[0] - gp[0] + 1;
+    if (in_list(r, {9, 10, 11, 12, 25, 26, 27, 28, 41, 42, 45, 46, 49, 50, 53, 54})) idx[1][1] = Ns[1] + gm[1];
+    if (in_list(r, {13, 14, 15, 16, 29, 30, 31, 32, 43, 44, 47, 48, 51, 52, 55, 56})) idx[0][1] = N[1] - Ne[1] - gp[1] + 1;
+    if (in_list(r, {17, 18, 19, 20, 33, 34, 35, 36, 41, 42, 43, 44, 49, 50, 51, 52})) idx[1][2] = Ns[2] + gm[2];
+    if (in_list(r, {21, 22, 23, 24, 37, 38, 39, 40, 45, 46, 47, 48, 53, 54, 55, 56})) idx[0][2] = N[2] - Ne[2] - gp[2] + 1;
+    if (lvlDiff == -1) {
+        if (in_list(r, {10, 12, 14, 16, 18, 20, 22, 24, 42, 44, 46, 48})) idx[0][0] = N[0] / 2 - Ne[0] + 2;
+        if (in_list(r, {9, 11, 13, 15, 17, 19, 21, 23, 41, 43, 45, 47})) idx[1][0] = N[0] / 2 + Ns[0];
+        if (in_list(r, {2, 4, 6, 8, 19, 20, 23, 24, 34, 36, 38, 40})) idx[0][1] = N[1] / 2 - Ne[1] + 2;
+        if (in_list(r, {1, 3, 5, 7, 17, 18, 21, 22, 33, 35, 37, 39})) idx[1][1] = N[1] / 2 + Ns[1];
+        if (dim == 3) {
+            if (in_list(r, {3, 4, 7, 8, 11, 12, 15, 16, 26, 28, 30, 32})) idx[0][2] = N[2] / 2 - Ne[2] + 2;
+            if (in_list(r, {1, 2, 5, 6, 9, 10, 13, 14, 25, 27, 29, 31})) idx[1][2] = N[2] / 2 + Ns[2];
+        }
+    }
+}
+
+// get_indices_of_ghost_patch (neighborhood.f90:158-327), neighbour relations only
+static void ghost_patch(const int Bs[3], int g, int dim, int relation, int idx[2][3], int gminus, int gplus, int lvl_diff) {
+    int r = relation > 56 ? (relation - 1) % 56 + 1 : relation;
+    for (int d = 0; d < 3; d++) { idx[0][d] = 1; idx[1][d] = 1; }
+    for (int d = 0; d < dim; d++) { idx[0][d] = g + 1; idx[1][d] = g + Bs[d]; }
+    if (in_list(r, {1, 2, 3, 4, 25, 26, 29, 30, 33, 34, 37, 38, 49, 51, 53, 55})) { idx[0][0] = g - gminus + 1; idx[1][0] = g; }
+    if (in_list(r, {5, 6, 7, 8, 27, 28, 31, 32, 35, 36, 39, 40, 50, 52, 54, 56})) { idx[0][0] = Bs[0] + g + 1; idx[1][0] = Bs[0] + g + gplus; }
+    if (in_list(r, {9, 10, 11, 12, 25, 26, 27, 28, 41, 42, 45, 46, 49, 50, 53, 54})) { idx[0][1] = g - gminus + 1; idx[1][1] = g; }
+    if (in_list(r, {13, 14, 15, 16, 29, 30, 31, 32, 43, 44, 47, 48, 51, 52, 55, 56})) { idx[0][1] = Bs[1] + g + 1; idx[1][1] = Bs[1] + g + gplus; }
+    if (in_list(r, {17, 18, 19, 20, 33, 34, 35, 36, 41, 42, 43, 44, 49, 50, 51, 52})) { idx[0][2] = g - gminus + 1; idx[1][2] = g; }
+    if (in_list(r, {21, 22, 23, 24, 37, 38, 39, 40, 45, 46, 47, 48, 53, 54, 55, 56})) { idx[0][2] = Bs[2] + g + 1; idx[1][2] = Bs[2] + g + gplus; }
+    if (in_list(r, {10, 12, 14, 16, 18, 20, 22, 24, 42, 44, 46, 48})) {
+        if (lvl_diff == +1) idx[0][0] = g - gminus + 1;
+        else if (lvl_diff == -1) idx[0][0] = g + Bs[0] / 2 + 1;
+        idx[1][0] = Bs[0] + g;
+    }
+    if (in_list(r, {9, 11, 13, 15, 17, 19, 21, 23, 41, 43, 45, 47})) {
+        idx[0][0] = g + 1;
+        if (lvl_diff == +1) idx[1][0] = Bs[0] + g + gplus;
+        else if (lvl_diff == -1) idx[1][0] = g + Bs[0] / 2;
+    }
+    if (in_list(r, {2, 4, 6, 8, 19, 20, 23, 24, 34, 36, 38, 40})) {
+        if (lvl_diff == +1) idx[0][1] = g - gminus + 1;
+        else if (lvl_diff == -1) idx[0][1] = g + Bs[1] / 2 + 1;
+        idx[1][1] = Bs[1] + g;
+    }
+    if (in_list(r, {1, 3, 5, 7, 17, 18, 21, 22, 33, 35, 37, 39})) {
+        idx[0][1] = g + 1;
+        if (lvl_diff == +1) idx[1][1] = Bs[1] + g + gplus;
+        else if (lvl_diff == -1) idx[1][1] = g + Bs[1] / 2;
+    }
+    if (dim == 3) {
+        if (in_list(r, {3, 4, 7, 8, 11, 12, 15, 16, 26, 28, 30, 32})) {
+            if (lvl_diff == +1) idx[0][2] = g - gminus + 1;
+            else if (lvl_diff == -1) idx[0][2] = g + Bs[2] / 2 + 1;
+            idx[1][2] = Bs[2] + g;
+        }
+        if (in_list(r, {1, 2, 5, 6, 9, 10, 13, 14, 25, 27, 29, 31})) {
+            idx[0][2] = g + 1;
+            if (lvl_diff == +1) idx[1][2] = Bs[2] + g + gplus;
+            else if (lvl_diff == -1) idx[1][2] = g + Bs[2] / 2;
+        }
+    }
+}
+
+// set_send_bounds (calc_data_bounds.f90:46-147)
+static void send_bounds(const wg_config &cfg, int order_predictor, int relation, int lvl_diff, int gminus, int gplus,
+                        int bounds[2][3], int buffer[2][3]) {
+    const int g = cfg.g, dim = cfg.dim;
+    int n[3] = {1, 1, 1};
+    for (int d = 0; d < dim; d++) n[d] = cfg.Bs[d] + 2 * g;
+    int a = order_predictor / 2 - 1;
+    for (int d = 0; d < 3; d++) { bounds[0][d] = bounds[1][d] = 1; buffer[0][d] = buffer[1][d] = 1; }
+    int gm3[3] = {g, g, g};
+    if (lvl_diff == 0) {
+        int Ns[3] = {gminus, gminus, gminus}, Ne[3] = {gplus, gplus, gplus};
+        modify_patch(dim, relation, bounds, n, Ns, Ne, gm3, gm3, 0);
+    } else if (lvl_diff == +1) {
+        int Ns[3] = {gminus * 2 - 1, gminus * 2 - 1, gminus * 2 - 1}, Ne[3] = {gplus * 2 - 1, gplus * 2 - 1, gplus * 2 - 1};
+        int gp[3] = {g + 1, g + 1, g + 1};
+        modify_patch(dim, relation, bounds, n, Ns, Ne, gm3, gp, +1);
+        for (int d = 0; d < dim; d++) {
+            int Nsender = bounds[1][d] - bounds[0][d] + 1;
+            buffer[1][d] = (Nsender + 1) / 2;
+        }
+    } else if (lvl_diff == -1) {
+        int Ns[3] = {gminus / 2 + 1, gminus / 2 + 1, gminus / 2 + 1};
+        int Ne[3] = {(gplus + 1) / 2 + 1, (gplus + 1) / 2 + 1, (gplus + 1) / 2 + 1};
+        int gp[3] = {g - 1, g - 1, g - 1};
+        modify_patch(dim, relation, bounds, n, Ns, Ne, gm3, gp, -1);
+        for (int d = 0; d < dim; d++) { bounds[0][d] -= a; bounds[1][d] += a; }
+        for (int d = 0; d < dim; d++) {
+            if (bounds[0][d] == g + 1 - a || gminus % 2 == 0) buffer[0][d] = 1 + a * 2;
+            else buffer[0][d] = 2 + a * 2;
+            buffer[1][d] = buffer[0][d] + gplus - 1;
+            if (bounds[1][d] - bounds[0][d] > g + a) buffer[1][d] += cfg.Bs[d];
+        }
+    }
+}
+
+// inverse_relation (neighborhood.f90:347-381)
+static int inverse_relation(int relation) {
+    int inv = (relation - 1) % 56 + 1;
+    if (relation > 56) inv += (3 - (relation - 1) / 56) * 56;
+    int m = (relation - 1) % 56;
+    for (int i_dim = 3; i_dim >= 3 - m / 24; i_dim--) {
+        int p = 1 << i_dim, h = 1 << (i_dim - 1);
+        if ((relation - 1) % p >= h) inv -= h;
+        else inv += h;
+    }
+    return inv;
+}
+
+// ---------------------------------------------------------------------------
+// prediction (module_wavelets.f90:96-284): coarse(n) -> fine(2n-1), in place
+// on a dense x-fastest array
+// ---------------------------------------------------------------------------
+static void prediction(const double *coarse, int cx, int cy, int cz, double *fine, int order) {
+    const int fx = 2 * cx - 1, fy = 2 * cy - 1, fz = 2 * cz - 1;
+    auto F = [&](int i, int j, int k) -> double & { return fine[((size_t)(k - 1) * fy + (j - 1)) * fx + (i - 1)]; };
+    double c[8];
+    int nc;
+    if (order == 2) { nc = 2; c[0] = 0.5; c[1] = 0.5; }
+    else if (order == 4) { nc = 4; c[0] = -1.0 / 16.0; c[1] = 9.0 / 16.0; c[2] = 9.0 / 16.0; c[3] = -1.0 / 16.0; }
+    else if (order == 6) { nc = 6; double v[] = {3, -25, 150, 150, -25, 3}; for (int i = 0; i < 6; i++) c[i] = v[i] / 256.0; }
+    else { nc = 8; double v[] = {-5, 49, -245, 1225, 1225, -245, 49, -5}; for (int i = 0; i < 8; i++) c[i] = v[i] / 2048.0; }
+    // ( -1.0_rk, 9.0_rk, 9.0_rk, -1.0_rk ) / 16.0_rk : elementwise division
+    for (int k = 1; k <= fz; k++) for (int j = 1; j <= fy; j++) for (int i = 1; i <= fx; i++)
+        if (i % 2 == 0 || j % 2 == 0 || k % 2 == 0) F(i, j, k) = 0.0;
+    for (int k = 1; k <= cz; k++) for (int j = 1; j <= cy; j++) for (int i = 1; i <= cx; i++)
+        F(2 * i - 1, 2 * j - 1, 2 * k - 1) = coarse[((size_t)(k - 1) * cy + (j - 1)) * cx + (i - 1)];
+    const int h = nc - 1;  // offsets -h,-h+2,...,+h
+    auto interp = [&](auto get) -> double {
+        double s = c[0] * get(-h);
+        for (int m = 1; m < nc; m++) s = s + c[m] * get(-h + 2 * m);
+        return s;
+    };
+    for (int k = 1; k <= fz; k += 2) {
+        for (int j = 1; j <= fy; j += 2)
+            for (int i = nc; i <= fx - (nc - 1); i += 2)
+                F(i, j, k) = interp([&](int o) { return F(i + o, j, k); });
+        for (int j = nc; j <= fy - (nc - 1); j += 2)
+            for (int i = 1; i <= fx; i++)
+                F(i, j, k) = interp([&](int o) { return F(i, j + o, k); });
+    }
+    for (int k = nc; k <= fz - (nc - 1); k += 2)
+        for (int j = 1; j <= fy; j++)
+            for (int i = 1; i <= fx; i++)
+                F(i, j, k) = interp([&](int o) { return F(i, j, k + o); });
+}
+
+// ---------------------------------------------------------------------------
+// ghost-node synchronisation: sync_ghosts_generic (synchronize_ghosts_generic.f90)
+// with unpack_ghostlayers_internal (xfer_block_data.f90:321-437), leaf-only grid.
+// The restriction is plain decimation (ignore_Filter, RHS sync) or, for
+// lifted wavelets without ignore_Filter, the HD-filtered variant.
+// ---------------------------------------------------------------------------
+static void hd_filter_block(const Oracle &o, int b, std::vector<double> &out);
+
+static void sync_ghosts(Oracle &o, int gminus, int gplus, bool ignore_filter) {
+    const wg_config &cfg = o.cfg;
+    const int dim = cfg.dim;
+    const int nstages = o.wav.lifted ? 3 : 2;
+    const int isUnlifted = o.wav.lifted ? 0 : 1;
+    const int nblk = (int)o.blocks.size();
+    std::vector<double> coarse, fine, filtered;
+    int filtered_id = -1;
+    for (int istage = 1; istage <= nstages; istage++) {
+        for (int ib = 0; ib < nblk; ib++) {
+            const int level = o.blocks[ib].level;
+            for (int i_n = 1; i_n <= 168; i_n++) {
+                const int in = o.nb[size_t(ib) * 168 + i_n - 1];
+                if (in < 0) continue;
+                const int lvl_diff = level - o.blocks[in].level;
+                bool send = (istage == 1 && lvl_diff == 0) || (istage == 2 - isUnlifted && lvl_diff == +1) ||
+                            (istage == 3 - isUnlifted && lvl_diff == -1);
+                if (!send) continue;
+                const int inv = inverse_relation(i_n);
+                int recv[2][3], sb[2][3], buf[2][3];
+                ghost_patch(cfg.Bs, cfg.g, dim, inv, recv, gminus, gplus, -lvl_diff);
+                send_bounds(cfg, o.wav.order_predictor, i_n, lvl_diff, gminus, gplus, sb, buf);
+                double *dst = o.blk(in);
+                const double *src = o.blk(ib);
+                if (lvl_diff == 0) {
+                    for (int c = 1; c <= o.nc; c++)
+                        for (int k = recv[0][2], ks = sb[0][2]; k <= recv[1][2]; k++, ks++)
+                            for (int j = recv[0][1], js = sb[0][1]; j <= recv[1][1]; j++, js++)
+                                for (int i = recv[0][0], is = sb[0][0]; i <= recv[1][0]; i++, is++)
+                                    dst[o.at(i, j, k, c)] = src[o.at(is, js, ks, c)];
+                } else if (lvl_diff == +1) {
+                    const double *srcf = src;
+                    if (!ignore_filter && o.wav.lifted) {
+                        if (filtered_id != ib) { hd_filter_block(o, ib, filtered); filtered_id = ib; }
+                        srcf = filtered.data();
+                    }
+                    // res_data(1:...) = src(ijk(1):ijk(2):2), then receiver takes res_data(buffer box)
+                    for (int c = 1; c <= o.nc; c++)
+                        for (int k = recv[0][2], kb = buf[0][2]; k <= recv[1][2]; k++, kb++)
+                            for (int j = recv[0][1], jb = buf[0][1]; j <= recv[1][1]; j++, jb++)
+                                for (int i = recv[0][0], ib2 = buf[0][0]; i <= recv[1][0]; i++, ib2++) {
+                                    int is = sb[0][0] + 2 * (ib2 - 1);
+                                    int js = sb[0][1] + 2 * (jb - 1);
+                                    int ks = (dim == 3) ? sb[0][2] + 2 * (kb - 1) : 1;
+                                    dst[o.at(i, j, k, c)] = srcf[o.at(is, js, ks, c)];
+                                }
+                } else {
+                    const int cx = sb[1][0] - sb[0][0] + 1, cy = sb[1][1] - sb[0][1] + 1, cz = sb[1][2] - sb[0][2] + 1;
+                    const int fx = 2 * cx - 1, fy = 2 * cy - 1;
+                    coarse.resize(size_t(cx) * cy * cz);
+                    fine.resize(size_t(fx) * fy * (2 * cz - 1));
+                    for (int c = 1; c <= o.nc; c++) {
+                        size_t p = 0;
+                        for (int k = sb[0][2]; k <= sb[1][2]; k++)
+                            for (int j = sb[0][1]; j <= sb[1][1]; j++)
+                                for (int i = sb[0][0]; i <= sb[1][0]; i++) coarse[p++] = src[o.at(i, j, k, c)];
+                        prediction(coarse.data(), cx, cy, cz, fine.data(), o.wav.order_predictor);
+                        for (int k = recv[0][2], kb = buf[0][2]; k <= recv[1][2]; k++, kb++)
+                            for (int j = recv[0][1], jb = buf[0][1]; j <= recv[1][1]; j++, jb++)
+                                for (int i = recv[0][0], ib2 = buf[0][0]; i <= recv[1][0]; i++, ib2++)
+                                    dst[o.at(i, j, k, c)] = fine[(size_t(kb - 1) * fy + (jb - 1)) * fx + (ib2 - 1)];
+                    }
+                }
+            }
+        }
+    }
+}
+
+// HD filter of a whole block (blockFilterXYZ_vct with do_restriction, used by
+// restrict_copy_at_CE for lifted wavelets). Filters x, then y, then z where the
+// filter support stays inside the block; other points keep the input values.
+static void hd_filter_block(const Oracle &o, int b, std::vector<double> &out) {
+    const Filter &HD = o.wav.HD;
+    const double *u = o.blk(b);
+    out.assign(u, u + size_t(o.nc) * o.npts);
+    std::vector<double> tmp(out);
+    const int dim = o.cfg.dim;
+    int n[3] = {o.nx, o.ny, o.nz};
+    for (int d = 0; d < dim; d++) {
+        tmp = out;
+        for (int c = 1; c <= o.nc; c++)
+            for (int k = 1; k <= n[2]; k++)
+                for (int j = 1; j <= n[1]; j++)
+                    for (int i = 1; i <= n[0]; i++) {
+                        int p[3] = {i, j, k};
+                        if (p[d] + HD.lo < 1 || p[d] + HD.hi > n[d]) continue;
+                        double s = 0.0;
+                        bool first = true;
+                        for (int m = HD.lo; m <= HD.hi; m++) {
+                            int q[3] = {i, j, k};
+                            q[d] += m;
+                            double v = HD(m) * tmp[o.at(q[0], q[1], q[2], c)];
+                            s = first ? v : s + v;
+                            first = false;
+                        }
+                        out[o.at(i, j, k, c)] = s;
+                    }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// ACM right-hand side, FD_4th_central (LIB/EQUATION/ACMnew/rhs_ACM.f90)
+// ---------------------------------------------------------------------------
+static const double a_FD4[5] = {1.0 / 12.0, -2.0 / 3.0, 0.0, 2.0 / 3.0, -1.0 / 12.0};
+static const double b_FD4[5] = {-1.0 / 12.0, 4.0 / 3.0, -5.0 / 2.0, 4.0 / 3.0, -1.0 / 12.0};
+#define A(i) a_FD4[(i) + 2]
+#define B(i) b_FD4[(i) + 2]
+
+static void rhs_2d(const Oracle &o, const double *phi, const double *mask, const double dx[3], double *rhs) {
+    const wg_config &p = o.cfg;
+    const int g = p.g, Bs0 = p.Bs[0], Bs1 = p.Bs[1];
+    const double dx_inv = 1.0 / dx[0], dy_inv = 1.0 / dx[1];
+    const double dx2_inv = 1.0 / (dx[0] * dx[0]), dy2_inv = 1.0 / (dx[1] * dx[1]);
+    const double c_0 = p.c0, nu = p.nu, gamma = p.gamma_p;
+    double Ceta_inv[8];
+    for (int i = 0; i < 8; i++) Ceta_inv[i] = 1.0 / p.C_eta;
+    Ceta_inv[0] = 0.0;
+    auto P = [&](int ix, int iy, int ic) { return phi[o.at(ix, iy, 1, ic)]; };
+    auto M = [&](int ix, int iy, int ic) { return mask ? mask[o.at(ix, iy, 1, ic)] : 0.0; };
+    for (int iy = g + 1; iy <= Bs1 + g; iy++)
+        for (int ix = g + 1; ix <= Bs0 + g; ix++) {
+            double u_dx = (A(-2) * P(ix - 2, iy, 1) + A(-1) * P(ix - 1, iy, 1) + A(1) * P(ix + 1, iy, 1) + A(2) * P(ix + 2, iy, 1)) * dx_inv;
+            double v_dx = (A(-2) * P(ix - 2, iy, 2) + A(-1) * P(ix - 1, iy, 2) + A(1) * P(ix + 1, iy, 2) + A(2) * P(ix + 2, iy, 2)) * dx_inv;
+            double p_dx = (A(-2) * P(ix - 2, iy, 3) + A(-1) * P(ix - 1, iy, 3) + A(1) * P(ix + 1, iy, 3) + A(2) * P(ix + 2, iy, 3)) * dx_inv;
+            double u_dy = (A(-2) * P(ix, iy - 2, 1) + A(-1) * P(ix, iy - 1, 1) + A(1) * P(ix, iy + 1, 1) + A(2) * P(ix, iy + 2, 1)) * dy_inv;
+            double v_dy = (A(-2) * P(ix, iy - 2, 2) + A(-1) * P(ix, iy - 1, 2) + A(1) * P(ix, iy + 1, 2) + A(2) * P(ix, iy + 2, 2)) * dy_inv;
+            double p_dy = (A(-2) * P(ix, iy - 2, 3) + A(-1) * P(ix, iy - 1, 3) + A(1) * P(ix, iy + 1, 3) + A(2) * P(ix, iy + 2, 3)) * dy_inv;
+            double u_dxdx = (B(-2) * P(ix - 2, iy, 1) + B(-1) * P(ix - 1, iy, 1) + B(0) * P(ix, iy, 1) + B(1) * P(ix + 1, iy, 1) + B(2) * P(ix + 2, iy, 1)) * dx2_inv;
+            double v_dxdx = (B(-2) * P(ix - 2, iy, 2) + B(-1) * P(ix - 1, iy, 2) + B(0) * P(ix, iy, 2) + B(1) * P(ix + 1, iy, 2) + B(2) * P(ix + 2, iy, 2)) * dx2_inv;
+            double u_dydy = (B(-2) * P(ix, iy - 2, 1) + B(-1) * P(ix, iy - 1, 1) + B(0) * P(ix, iy, 1) + B(1) * P(ix, iy + 1, 1) + B(2) * P(ix, iy + 2, 1)) * dy2_inv;
+            double v_dydy = (B(-2) * P(ix, iy - 2, 2) + B(-1) * P(ix, iy - 1, 2) + B(0) * P(ix, iy, 2) + B(1) * P(ix, iy + 1, 2) + B(2) * P(ix, iy + 2, 2)) * dy2_inv;
+            double div_U = u_dx + v_dy;
+            int color = (int)M(ix, iy, 5);
+            double penalx = -M(ix, iy, 1) * Ceta_inv[color] * (P(ix, iy, 1) - M(ix, iy, 2));
+            double penaly = -M(ix, iy, 1) * Ceta_inv[color] * (P(ix, iy, 2) - M(ix, iy, 3));
+            double r1, r2;
+            if (p.skew_symmetry) {
+                double uu_dx = (A(-2) * P(ix - 2, iy, 1) * P(ix - 2, iy, 1) + A(-1) * P(ix - 1, iy, 1) * P(ix - 1, iy, 1) + A(1) * P(ix + 1, iy, 1) * P(ix + 1, iy, 1) + A(2) * P(ix + 2, iy, 1) * P(ix + 2, iy, 1)) * dx_inv;
+                double uv_dy = (A(-2) * P(ix, iy - 2, 1) * P(ix, iy - 2, 2) + A(-1) * P(ix, iy - 1, 1) * P(ix, iy - 1, 2) + A(1) * P(ix, iy + 1, 1) * P(ix, iy + 1, 2) + A(2) * P(ix, iy + 2, 1) * P(ix, iy + 2, 2)) * dy_inv;
+                double vu_dx = (A(-2) * P(ix - 2, iy, 2) * P(ix - 2, iy, 1) + A(-1) * P(ix - 1, iy, 2) * P(ix - 1, iy, 1) + A(1) * P(ix + 1, iy, 2) * P(ix + 1, iy, 1) + A(2) * P(ix + 2, iy, 2) * P(ix + 2, iy, 1)) * dx_inv;
+                double vv_dy = (A(-2) * P(ix, iy - 2, 2) * P(ix, iy - 2, 2) + A(-1) * P(ix, iy - 1, 2) * P(ix, iy - 1, 2) + A(1) * P(ix, iy + 1, 2) * P(ix, iy + 1, 2) + A(2) * P(ix, iy + 2, 2) * P(ix, iy + 2, 2)) * dy_inv;
+                r1 = -0.5 * (uu_dx + uv_dy + P(ix, iy, 1) * u_dx + P(ix, iy, 2) * u_dy) - p_dx + nu * (u_dxdx + u_dydy) + penalx;
+                r2 = -0.5 * (vu_dx + vv_dy + P(ix, iy, 1) * v_dx + P(ix, iy, 2) * v_dy) - p_dy + nu * (v_dxdx + v_dydy) + penaly;
+            } else {
+                r1 = -P(ix, iy, 1) * u_dx - P(ix, iy, 2) * u_dy - p_dx + nu * (u_dxdx + u_dydy) + penalx;
+                r2 = -P(ix, iy, 1) * v_dx - P(ix, iy, 2) * v_dy - p_dy + nu * (v_dxdx + v_dydy) + penaly;
+            }
+            double r3 = -(c_0 * c_0) * div_U - gamma * P(ix, iy, 3);
+            if (p.use_sponge) {
+                double spo = M(ix, iy, 6) * (1.0 / p.C_sponge);
+                r1 = r1 - (P(ix, iy, 1) - p.u_mean_set[0]) * spo;
+                r2 = r2 - (P(ix, iy, 2) - p.u_mean_set[1]) * spo;
+                r3 = r3 - P(ix, iy, 3) * spo;
+            }
+            rhs[o.at(ix, iy, 1, 1)] = r1;
+            rhs[o.at(ix, iy, 1, 2)] = r2;
+            rhs[o.at(ix, iy, 1, 3)] = r3;
+        }
+}
+
+static void rhs_3d(const Oracle &o, const double *phi, const double *mask, const double dx[3], double *rhs) {
+    const wg_config &p = o.cfg;
+    const int g = p.g;
+    const double dx_inv = 1.0 / dx[0], dy_inv = 1.0 / dx[1], dz_inv = 1.0 / dx[2];
+    const double dx2_inv = 1.0 / (dx[0] * dx[0]), dy2_inv = 1.0 / (dx[1] * dx[1]), dz2_inv = 1.0 / (dx[2] * dx[2]);
+    const double c_0 = p.c0, nu = p.nu, gamma = p.gamma_p;
+    double Ceta_inv[8];
+    for (int i = 0; i < 8; i++) Ceta_inv[i] = 1.0 / p.C_eta;
+    Ceta_inv[0] = 0.0;
+    auto P = [&](int ix, int iy, int iz, int ic) { return phi[o.at(ix, iy, iz, ic)]; };
+    auto M = [&](int ix, int iy, int iz, int ic) { return mask ? mask[o.at(ix, iy, iz, ic)] : 0.0; };
+#define D1X(c) ((A(-2) * P(ix - 2, iy, iz, c) + A(-1) * P(ix - 1, iy, iz, c) + A(1) * P(ix + 1, iy, iz, c) + A(2) * P(ix + 2, iy, iz, c)) * dx_inv)
+#define D1Y(c) ((A(-2) * P(ix, iy - 2, iz, c) + A(-1) * P(ix, iy - 1, iz, c) + A(1) * P(ix, iy + 1, iz, c) + A(2) * P(ix, iy + 2, iz, c)) * dy_inv)
+#define D1Z(c) ((A(-2) * P(ix, iy, iz - 2, c) + A(-1) * P(ix, iy, iz - 1, c) + A(1) * P(ix, iy, iz + 1, c) + A(2) * P(ix, iy, iz + 2, c)) * dz_inv)
+#define D2X(c) ((B(-2) * P(ix - 2, iy, iz, c) + B(-1) * P(ix - 1, iy, iz, c) + B(0) * P(ix, iy, iz, c) + B(1) * P(ix + 1, iy, iz, c) + B(2) * P(ix + 2, iy, iz, c)) * dx2_inv)
+#define D2Y(c) ((B(-2) * P(ix, iy - 2, iz, c) + B(-1) * P(ix, iy - 1, iz, c) + B(0) * P(ix, iy, iz, c) + B(1) * P(ix, iy + 1, iz, c) + B(2) * P(ix, iy + 2, iz, c)) * dy2_inv)
+#define D2Z(c) ((B(-2) * P(ix, iy, iz - 2, c) + B(-1) * P(ix, iy, iz - 1, c) + B(0) * P(ix, iy, iz, c) + B(1) * P(ix, iy, iz + 1, c) + B(2) * P(ix, iy, iz + 2, c)) * dz2_inv)
+#define PX(a, b) ((A(-2) * P(ix - 2, iy, iz, a) * P(ix - 2, iy, iz, b) + A(-1) * P(ix - 1, iy, iz, a) * P(ix - 1, iy, iz, b) + A(1) * P(ix + 1, iy, iz, a) * P(ix + 1, iy, iz, b) + A(2) * P(ix + 2, iy, iz, a) * P(ix + 2, iy, iz, b)) * dx_inv)
+#define PY(a, b) ((A(-2) * P(ix, iy - 2, iz, a) * P(ix, iy - 2, iz, b) + A(-1) * P(ix, iy - 1, iz, a) * P(ix, iy - 1, iz, b) + A(1) * P(ix, iy + 1, iz, a) * P(ix, iy + 1, iz, b) + A(2) * P(ix, iy + 2, iz, a) * P(ix, iy + 2, iz, b)) * dy_inv)
+#define PZ(a, b) ((A(-2) * P(ix, iy, iz - 2, a) * P(ix, iy, iz - 2, b) + A(-1) * P(ix, iy, iz - 1, a) * P(ix, iy, iz - 1, b) + A(1) * P(ix, iy, iz + 1, a) * P(ix, iy, iz + 1, b) + A(2) * P(ix, iy, iz + 2, a) * P(ix, iy, iz + 2, b)) * dz_inv)
+    for (int iz = g + 1; iz <= p.Bs[2] + g; iz++)
+        for (int iy = g + 1; iy <= p.Bs[1] + g; iy++)
+            for (int ix = g + 1; ix <= p.Bs[0] + g; ix++) {
+                double u_dx = D1X(1), v_dx = D1X(2), w_dx = D1X(3), p_dx = D1X(4);
+                double u_dy = D1Y(1), v_dy = D1Y(2), w_dy = D1Y(3), p_dy = D1Y(4);
+                double u_dz = D1Z(1), v_dz = D1Z(2), w_dz = D1Z(3), p_dz = D1Z(4);
+                double u_dxdx = D2X(1), v_dxdx = D2X(2), w_dxdx = D2X(3);
+                double u_dydy = D2Y(1), v_dydy = D2Y(2), w_dydy = D2Y(3);
+                double u_dzdz = D2Z(1), v_dzdz = D2Z(2), w_dzdz = D2Z(3);
+                double u = P(ix, iy, iz, 1), v = P(ix, iy, iz, 2), w = P(ix, iy, iz, 3), pp = P(ix, iy, iz, 4);
+                double chi = M(ix, iy, iz, 1) * Ceta_inv[(int)M(ix, iy, iz, 5)];
+                double penalx = -chi * (u - M(ix, iy, iz, 2));
+                double penaly = -chi * (v - M(ix, iy, iz, 3));
+                double penalz = -chi * (w - M(ix, iy, iz, 4));
+                double r1, r2, r3;
+                if (p.skew_symmetry) {
+                    double uu_dx = PX(1, 1), uv_dy = PY(1, 2), uw_dz = PZ(1, 3);
+                    double vu_dx = PX(2, 1), vv_dy = PY(2, 2), vw_dz = PZ(2, 3);
+                    double wu_dx = PX(3, 1), wv_dy = PY(3, 2), ww_dz = PZ(3, 3);
+                    r1 = -0.5 * (uu_dx + uv_dy + uw_dz + u * u_dx + v * u_dy + w * u_dz) - p_dx + nu * (u_dxdx + u_dydy + u_dzdz) + penalx;
+                    r2 = -0.5 * (vu_dx + vv_dy + vw_dz + u * v_dx + v * v_dy + w * v_dz) - p_dy + nu * (v_dxdx + v_dydy + v_dzdz) + penaly;
+                    r3 = -0.5 * (wu_dx + wv_dy + ww_dz + u * w_dx + v * w_dy + w * w_dz) - p_dz + nu * (w_dxdx + w_dydy + w_dzdz) + penalz;
+                } else {
+                    r1 = (-u * u_dx - v * u_dy - w * u_dz) - p_dx + nu * (u_dxdx + u_dydy + u_dzdz) + penalx;
+                    r2 = (-u * v_dx - v * v_dy - w * v_dz) - p_dy + nu * (v_dxdx + v_dydy + v_dzdz) + penaly;
+                    r3 = (-u * w_dx - v * w_dy - w * w_dz) - p_dz + nu * (w_dxdx + w_dydy + w_dzdz) + penalz;
+                }
+                double r4 = -(c_0 * c_0) * (u_dx + v_dy + w_dz) - gamma * pp;
+                if (p.use_sponge) {
+                    double spo = M(ix, iy, iz, 6) * (1.0 / p.C_sponge);
+                    r1 = r1 - (u - p.u_mean_set[0]) * spo;
+                    r2 = r2 - (v - p.u_mean_set[1]) * spo;
+                    r3 = r3 - (w - p.u_mean_set[2]) * spo;
+                    r4 = r4 - pp * spo;
+                }
+                rhs[o.at(ix, iy, iz, 1)] = r1;
+                rhs[o.at(ix, iy, iz, 2)] = r2;
+                rhs[o.at(ix, iy, iz, 3)] = r3;
+                rhs[o.at(ix, iy, iz, 4)] = r4;
+            }
+#undef D1X
+#undef D1Y
+#undef D1Z
+#undef D2X
+#undef D2Y
+#undef D2Z
+#undef PX
+#undef PY
+#undef PZ
+}
+
+static void block_spacing(const Oracle &o, int b, double x0[3], double dx[3]) {
+    const Block &B = o.blocks[b];
+    for (int d = 0; d < 3; d++) {
+        x0[d] = 0.0;
+        dx[d] = 0.0;
+    }
+    for (int d = 0; d < o.cfg.dim; d++) {
+        dx[d] = std::pow(2.0, -B.level) * o.cfg.domain[d] / (double)o.cfg.Bs[d];
+        x0[d] = (double)(B.c[d] * o.cfg.Bs[d]) * dx[d];
+    }
+}
+
+// RHS_wrapper local stage over all blocks, result into rhs (full-block layout)
+static int rhs_all(Oracle &o, double *rhs) {
+    const int nblk = (int)o.blocks.size();
+    const size_t bs = size_t(o.nc) * o.npts;
+    // integral stage: divergence guard (rhs_ACM.f90:133-146)
+    for (int b = 0; b < nblk; b++) {
+        const double *u = o.blk(b);
+        for (int c = 1; c <= o.nc; c++)
+            for (int k = (o.cfg.dim == 3 ? o.cfg.g + 1 : 1); k <= (o.cfg.dim == 3 ? o.cfg.Bs[2] + o.cfg.g : 1); k++)
+                for (int j = o.cfg.g + 1; j <= o.cfg.Bs[1] + o.cfg.g; j++)
+                    for (int i = o.cfg.g + 1; i <= o.cfg.Bs[0] + o.cfg.g; i++)
+                        if (std::fabs(u[o.at(i, j, k, c)]) > 1.0e12) return WG_EDIVERGED;
+    }
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads) if (o.nthreads > 1)
+    for (int b = 0; b < nblk; b++) {
+        double x0[3], dx[3];
+        block_spacing(o, b, x0, dx);
+        const double *m = o.mask.empty() ? nullptr : o.mask.data() + size_t(b) * 6 * o.npts;
+        if (o.cfg.dim == 2) rhs_2d(o, o.blk(b), m, dx, rhs + b * bs);
+        else rhs_3d(o, o.blk(b), m, dx, rhs + b * bs);
+    }
+    return WG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// time step: calculate_time_step (LIB/TIME/calculate_time_step.f90:2-125) with
+// GET_DT_BLOCK_ACM (module_ACM.f90:617-691)
+// ---------------------------------------------------------------------------
+static double dt_block(const Oracle &o, int b) {
+    const wg_config &p = o.cfg;
+    double x0[3], dx[3];
+    block_spacing(o, b, x0, dx);
+    const double *u = o.blk(b);
+    const int g = p.g;
+    double u_mag = -HUGE_VAL;
+    for (int k = (p.dim == 3 ? g + 1 : 1); k <= (p.dim == 3 ? p.Bs[2] + g : 1); k++)
+        for (int j = g + 1; j <= p.Bs[1] + g; j++)
+            for (int i = g + 1; i <= p.Bs[0] + g; i++) {
+                double s;
+                if (p.dim == 2) {
+                    double a = u[o.at(i, j, k, 1)], bb = u[o.at(i, j, k, 2)];
+                    s = a * a + bb * bb;
+                } else {
+                    double a = u[o.at(i, j, k, 1)], bb = u[o.at(i, j, k, 2)], cc = u[o.at(i, j, k, 3)];
+                    s = a * a + bb * bb + cc * cc;
+                }
+                if (s > u_mag) u_mag = s;
+            }
+    double u_eigen = std::sqrt(u_mag) + std::sqrt(p.c0 * p.c0 + u_mag);
+    double dxmin = dx[0];
+    for (int d = 1; d < p.dim; d++) dxmin = std::min(dxmin, dx[d]);
+    double dt;
+    if (u_eigen >= 1.0e-6) dt = p.CFL * dxmin / u_eigen;
+    else dt = 1.0e-2;
+    if (p.nu > 1.0e-13) dt = std::min(dt, p.CFL_nu * (dxmin * dxmin) / p.nu);
+    if (p.gamma_p > 0) dt = std::min(dt, p.CFL_eta * p.gamma_p);
+    if (p.penalization) dt = std::min(dt, p.CFL_eta * p.C_eta);
+    if (p.use_sponge) dt = std::min(dt, p.CFL_eta * p.C_sponge);
+    return dt;
+}
+
+static double calc_dt(const Oracle &o, double time) {
+    const wg_config &p = o.cfg;
+    double dt = 9.0e9;
+    if (p.dt_fixed > 0.0) dt = p.dt_fixed;
+    else {
+        for (int b = 0; b < (int)o.blocks.size(); b++) dt = std::min(dt, dt_block(o, b));
+        if (p.dt_max > 0.0) dt = std::min(p.dt_max, dt);
+    }
+    if (p.write_time > 0.0) {
+        double wt = p.write_time;
+        if (std::fmod(time + dt, wt) < std::fmod(time + 1e-12, wt) && !(std::fabs(std::fmod(time, wt)) < 1e-12) && time + 1e-12 > 0.0)
+            dt = wt - std::fmod(time, wt);
+    }
+    if (p.tsave_stats > 0.0) {
+        double ts = p.tsave_stats;
+        if (std::fmod(time + dt, ts) < std::fmod(time + 1e-12, ts) && !(std::fabs(std::fmod(time, ts)) < 1e-12))
+            dt = ts - std::fmod(time, ts);
+    }
+    if (time + dt > p.time_max && time <= p.time_max) dt = p.time_max - time;
+    return dt;
+}
+
+// RungeKuttaGeneric with the default RK4 Butcher tableau
+// (LIB/TIME/runge_kutta_generic.f90:1-156, ini_file_to_params.f90:640-646)
+static int rk4_step(Oracle &o, double *time_inout, double *dt_out) {
+    const wg_config &p = o.cfg;
+    const int nblk = (int)o.blocks.size();
+    const size_t bs = size_t(o.nc) * o.npts;
+    static const double rk[5][5] = {
+        {0.0, 0.0, 0.0, 0.0, 0.0},
+        {0.5, 0.5, 0.0, 0.0, 0.0},
+        {0.5, 0.0, 0.5, 0.0, 0.0},
+        {1.0, 0.0, 0.0, 1.0, 0.0},
+        {0.0, 1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0}};
+    const double time = *time_inout;
+    const int grhs = p.g_rhs;
+    sync_ghosts(o, grhs, grhs, true);
+    double dt = calc_dt(o, time);
+    o.work.assign(bs * nblk * 5, 0.0);
+    auto W = [&](int slot, int b) { return o.work.data() + (size_t(slot) * nblk + b) * bs; };
+    const int g = p.g;
+    const int z1 = p.dim == 2 ? 1 : g + 1, z2 = p.dim == 2 ? 1 : p.Bs[2] + g;
+    auto interior = [&](auto fn) {
+        for (int b = 0; b < nblk; b++)
+            for (int c = 1; c <= o.nc; c++)
+                for (int k = z1; k <= z2; k++)
+                    for (int j = g + 1; j <= p.Bs[1] + g; j++)
+                        for (int i = g + 1; i <= p.Bs[0] + g; i++) fn(b, o.at(i, j, k, c));
+    };
+    interior([&](int b, size_t q) { W(0, b)[q] = o.blk(b)[q]; });
+    // stage 1
+    {
+        std::vector<double> r(bs * nblk, 0.0);
+        int st = rhs_all(o, r.data());
+        if (st) return st;
+        interior([&](int b, size_t q) { W(1, b)[q] = r[b * bs + q]; });
+    }
+    for (int j = 2; j <= 4; j++) {
+        interior([&](int b, size_t q) { o.blk(b)[q] = W(0, b)[q]; });
+        for (int l = 2; l <= j; l++) {
+            double a = rk[j - 1][l - 1];
+            if (std::fabs(a) < 1.0e-8) continue;
+            interior([&](int b, size_t q) { o.blk(b)[q] = o.blk(b)[q] + dt * a * W(l - 1, b)[q]; });
+        }
+        sync_ghosts(o, grhs, grhs, true);
+        std::vector<double> r(bs * nblk, 0.0);
+        int st = rhs_all(o, r.data());
+        if (st) return st;
+        interior([&](int b, size_t q) { W(j, b)[q] = r[b * bs + q]; });
+    }
+    interior([&](int b, size_t q) { o.blk(b)[q] = W(0, b)[q]; });
+    for (int j = 2; j <= 5; j++) {
+        double bj = rk[4][j - 1];
+        if (std::fabs(bj) < 1.0e-8) continue;
+        interior([&](int b, size_t q) { o.blk(b)[q] = o.blk(b)[q] + dt * bj * W(j - 1, b)[q]; });
+    }
+    *time_inout = time + dt;
+    *dt_out = dt;
+    return WG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// one-level FWT of a block, interior only, spaghetti order
+// (waveletDecomposition_optimized_block,
+//  LIB/WAVELETS/wavelet_decomposition_reconstruction.f90:23-389)
+// u and ud are full blocks (one component at a time), ud may equal u.
+// ---------------------------------------------------------------------------
+static void fwt_block(const Oracle &o, const double *u_in, double *u_d) {
+    const wg_config &p = o.cfg;
+    const Wavelet &w = o.wav;
+    const int dim = p.dim;
+    int g[3] = {p.g, p.g, dim == 3 ? p.g : 0};
+    int Bs[3] = {p.Bs[0], p.Bs[1], dim == 3 ? p.Bs[2] : 1};
+    int fmax = std::max(std::max(std::abs(w.HD.lo), std::abs(w.HD.hi)), std::max(std::abs(w.GD.lo), std::abs(w.GD.hi)));
+    fmax = std::max({w.HD.lo, w.HD.hi, w.GD.lo, w.GD.hi});
+    int fm[3] = {fmax, fmax, dim == 3 ? fmax : 0};
+    const int nmax = std::max(o.nx, std::max(o.ny, o.nz)) + 1;
+    std::vector<double> buf(nmax + 8);
+    auto U = [&](const double *a, int ix, int iy, int iz) { return a[((size_t)(iz - 1) * o.ny + (iy - 1)) * o.nx + (ix - 1)]; };
+    auto Ud = [&](int ix, int iy, int iz) -> double & { return u_d[((size_t)(iz - 1) * o.ny + (iy - 1)) * o.nx + (ix - 1)]; };
+    // a filter applied in the reference's explicit term order (non-zero taps in ascending offset)
+    auto apply = [&](const Filter &f, auto get, int at) {
+        double s = 0.0;
+        bool first = true;
+        for (int m = f.lo; m <= f.hi; m++) {
+            if (f(m) == 0.0 && !(m == 0)) continue;
+            double v = get(at + m) * f(m);
+            s = first ? v : s + v;
+            first = false;
+        }
+        return s;
+    };
+    const bool lazy = (w.Y == 0);  // CDFX0: SC copied, only odd points filtered
+    // X
+    for (int iz = g[2] + 1 - fm[2]; iz <= Bs[2] + g[2] + fm[2]; iz++)
+        for (int iy = g[1] + 1 - fm[1]; iy <= Bs[1] + g[1] + fm[1]; iy++) {
+            auto get = [&](int ix) { return U(u_in, ix, iy, iz); };
+            for (int ix = g[0] + 1; ix <= Bs[0] + g[0]; ix += 2) buf[ix] = lazy ? get(ix) : apply(w.HD, get, ix);
+            for (int ix = g[0] + 2; ix <= Bs[0] + g[0]; ix += 2) buf[ix] = apply(w.GD, get, ix);
+            for (int ix = g[0] + 1; ix <= Bs[0] + g[0]; ix++) Ud(ix, iy, iz) = buf[ix];
+        }
+    // Y
+    for (int iz = g[2] + 1 - fm[2]; iz <= Bs[2] + g[2] + fm[2]; iz++)
+        for (int ix = g[0] + 1; ix <= Bs[0] + g[0]; ix++) {
+            auto get = [&](int iy) { return Ud(ix, iy, iz); };
+            for (int iy = g[1] + 1; iy <= Bs[1] + g[1]; iy += 2) buf[iy] = lazy ? get(iy) : apply(w.HD, get, iy);
+            for (int iy = g[1] + 2; iy <= Bs[1] + g[1]; iy += 2) buf[iy] = apply(w.GD, get, iy);
+            for (int iy = g[1] + 1; iy <= Bs[1] + g[1]; iy++) Ud(ix, iy, iz) = buf[iy];
+        }
+    // Z
+    if (dim == 3) {
+        for (int iy = g[1] + 1; iy <= Bs[1] + g[1]; iy++)
+            for (int ix = g[0] + 1; ix <= Bs[0] + g[0]; ix++) {
+                auto get = [&](int iz) { return Ud(ix, iy, iz); };
+                for (int iz = g[2] + 1; iz <= Bs[2] + g[2]; iz += 2) buf[iz] = lazy ? get(iz) : apply(w.HD, get, iz);
+                for (int iz = g[2] + 2; iz <= Bs[2] + g[2]; iz += 2) buf[iz] = apply(w.GD, get, iz);
+                for (int iz = g[2] + 1; iz <= Bs[2] + g[2]; iz++) Ud(ix, iy, iz) = buf[iz];
+            }
+    }
+}
+
+// threshold_block (LIB/INDICATORS/threshold_block.f90) with Linfty renorm
+// (wavelet_renorm_block, module_wavelets.f90:1848-1960): details are the max
+// |WC| over the interior with scaling coefficients zeroed. Returns -1 (coarsen)
+// or 0 (stay) and writes per-component details.
+static int threshold_block(const Oracle &o, int b, const double *eps_use, double *detail_out) {
+    const wg_config &p = o.cfg;
+    std::vector<double> ud(size_t(o.npts));
+    double detail[8];
+    for (int c = 0; c < o.nc; c++) detail[c] = -1.0;
+    const int g = p.g;
+    const int z1 = p.dim == 2 ? 1 : g + 1, z2 = p.dim == 2 ? 1 : p.Bs[2] + g;
+    std::vector<double> compv(8, 0.0);
+    for (int c = 1; c <= o.nc; c++) {
+        const double *u = o.blk(b) + size_t(c - 1) * o.npts;
+        std::copy(u, u + o.npts, ud.begin());
+        fwt_block(o, u, ud.data());
+        double m = 0.0;
+        bool any = false;
+        for (int k = z1; k <= z2; k++)
+            for (int j = g + 1; j <= p.Bs[1] + g; j++)
+                for (int i = g + 1; i <= p.Bs[0] + g; i++) {
+                    bool sc = ((i - g - 1) % 2 == 0) && ((j - g - 1) % 2 == 0) && (p.dim == 2 || (k - g - 1) % 2 == 0);
+                    double v = sc ? 0.0 : std::fabs(ud[((size_t)(k - 1) * o.ny + (j - 1)) * o.nx + (i - 1)]);
+                    if (!any || v > m) { m = v; any = true; }
+                }
+        compv[c - 1] = m;
+    }
+    // threshold_state_vector_component: 1 = own component, 0 = ignore,
+    // l>=2 = vector group (max over sqrt(wc^2) of the group)
+    int maxgrp = 0;
+    for (int c = 0; c < o.nc; c++) maxgrp = std::max(maxgrp, p.threshold_state_vector_component[c]);
+    for (int l = 2; l <= maxgrp; l++) {
+        double m = 0.0;
+        for (int c = 0; c < o.nc; c++) if (p.threshold_state_vector_component[c] == l) m = std::max(m, compv[c]);
+        for (int c = 0; c < o.nc; c++) if (p.threshold_state_vector_component[c] == l) detail[c] = m;
+    }
+    for (int c = 0; c < o.nc; c++) {
+        if (p.threshold_state_vector_component[c] == 1) detail[c] = compv[c];
+        if (p.threshold_state_vector_component[c] == 0) detail[c] = 0.0;
+    }
+    bool all = true;
+    for (int c = 0; c < o.nc; c++) {
+        if (!(detail[c] <= eps_use[c])) all = false;
+        if (detail_out) detail_out[c] = detail[c];
+    }
+    return all ? -1 : 0;
+}
+
+// refineBlock (LIB/MESH/refinementExecute.f90:4-116): predict the whole block
+// (incl. ghosts) and cut the 2^d daughters out of the fine array.
+static void refine_everywhere(Oracle &o) {
+    const wg_config &p = o.cfg;
+    const int dim = p.dim, g = p.g;
+    const int nblk = (int)o.blocks.size();
+    const int nd = 1 << dim;
+    std::vector<Block> nbl;
+    std::vector<double> ndata(size_t(nblk) * nd * o.nc * o.npts, 0.0);
+    const int cx = o.nx, cy = o.ny, cz = o.nz;
+    const int fx = 2 * cx - 1, fy = 2 * cy - 1, fz = dim == 3 ? 2 * cz - 1 : 1;
+    std::vector<double> fine(size_t(fx) * fy * fz);
+    std::vector<double> coarse(size_t(o.npts));
+    // daughters are appended in (block, k_daughter) order
+    for (int b = 0; b < nblk; b++)
+        for (int k = 0; k < nd; k++) {
+            Block d;
+            d.level = o.blocks[b].level + 1;
+            int bx = (k / 2) % 2, by = k % 2, bz = k / 4;
+            d.c[0] = 2 * o.blocks[b].c[0] + bx;
+            d.c[1] = 2 * o.blocks[b].c[1] + by;
+            d.c[2] = dim == 3 ? 2 * o.blocks[b].c[2] + bz : 0;
+            nbl.push_back(d);
+        }
+    for (int b = 0; b < nblk; b++) {
+        for (int c = 1; c <= o.nc; c++) {
+            const double *u = o.blk(b) + size_t(c - 1) * o.npts;
+            std::copy(u, u + o.npts, coarse.begin());
+            prediction(coarse.data(), cx, cy, dim == 3 ? cz : 1, fine.data(), o.wav.order_predictor);
+            for (int k = 0; k < nd; k++) {
+                int i0 = g + 1 + p.Bs[0] * ((k / 2) % 2);
+                int j0 = g + 1 + p.Bs[1] * (k % 2);
+                int k0 = dim == 3 ? g + 1 + p.Bs[2] * (k / 4) : 1;
+                double *dst = ndata.data() + (size_t(b) * nd + k) * o.nc * o.npts + size_t(c - 1) * o.npts;
+                for (int kk = 0; kk < o.nz; kk++)
+                    for (int jj = 0; jj < o.ny; jj++)
+                        for (int ii = 0; ii < o.nx; ii++)
+                            dst[((size_t)kk * o.ny + jj) * o.nx + ii] = fine[((size_t)(k0 - 1 + kk) * fy + (j0 - 1 + jj)) * fx + (i0 - 1 + ii)];
+            }
+        }
+    }
+    o.blocks = nbl;
+    o.data.swap(ndata);
+    update_neighbors(o);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI for tests (ctypes)
+// ===========================================================================
+extern "C" {
+
+void *or_create(const wg_config *cfg) {
+    Oracle *o = new Oracle();
+    o->cfg = *cfg;
+    if (!setup_wavelet(cfg->wavelet, 2, o->wav)) { delete o; return nullptr; }
+    o->nx = cfg->Bs[0] + 2 * cfg->g;
+    o->ny = cfg->Bs[1] + 2 * cfg->g;
+    o->nz = cfg->dim == 3 ? cfg->Bs[2] + 2 * cfg->g : 1;
+    o->nc = cfg->neq;
+    o->npts = o->nx * o->ny * o->nz;
+    return o;
+}
+
+void or_destroy(void *h) { delete (Oracle *)h; }
+
+void or_set_threads(void *h, int n) { ((Oracle *)h)->nthreads = n < 1 ? 1 : n; }
+
+int or_set_grid(void *h, int nblk, const int *level, const int *coords, const double *data) {
+    Oracle &o = *(Oracle *)h;
+    o.blocks.resize(nblk);
+    for (int i = 0; i < nblk; i++) {
+        o.blocks[i].level = level[i];
+        for (int d = 0; d < 3; d++) o.blocks[i].c[d] = coords[3 * i + d];
+    }
+    o.data.assign(size_t(nblk) * o.nc * o.npts, 0.0);
+    if (data) std::memcpy(o.data.data(), data, o.data.size() * sizeof(double));
+    o.mask.clear();
+    update_neighbors(o);
+    return WG_OK;
+}
+
+int or_nblocks(void *h) { return (int)((Oracle *)h)->blocks.size(); }
+
+int or_get_grid(void *h, int *level, int *coords) {
+    Oracle &o = *(Oracle *)h;
+    for (size_t i = 0; i < o.blocks.size(); i++) {
+        level[i] = o.blocks[i].level;
+        for (int d = 0; d < 3; d++) coords[3 * i + d] = o.blocks[i].c[d];
+    }
+    return WG_OK;
+}
+
+int or_get_data(void *h, double *out) {
+    Oracle &o = *(Oracle *)h;
+    std::memcpy(out, o.data.data(), o.data.size() * sizeof(double));
+    return WG_OK;
+}
+
+int or_set_data(void *h, const double *in) {
+    Oracle &o = *(Oracle *)h;
+    std::memcpy(o.data.data(), in, o.data.size() * sizeof(double));
+    return WG_OK;
+}
+
+int or_set_mask(void *h, const double *mask) {
+    Oracle &o = *(Oracle *)h;
+    if (!mask) { o.mask.clear(); return WG_OK; }
+    o.mask.assign(mask, mask + o.blocks.size() * 6 * size_t(o.npts));
+    return WG_OK;
+}
+
+// neighbour table (nblk*168, -1 = none), 0-based block ids
+int or_get_neighbors(void *h, int *out) {
+    Oracle &o = *(Oracle *)h;
+    std::memcpy(out, o.nb.data(), o.nb.size() * sizeof(int));
+    return WG_OK;
+}
+
+int or_sync_ghosts(void *h, int gminus, int gplus, int ignore_filter) {
+    sync_ghosts(*(Oracle *)h, gminus, gplus, ignore_filter != 0);
+    return WG_OK;
+}
+
+// rhs for all blocks (no sync); out has full-block layout, interior written
+int or_rhs(void *h, double *out) {
+    Oracle &o = *(Oracle *)h;
+    std::memset(out, 0, o.data.size() * sizeof(double));
+    return rhs_all(o, out);
+}
+
+int or_dt(void *h, double time, double *dt) {
+    *dt = calc_dt(*(Oracle *)h, time);
+    return WG_OK;
+}
+
+int or_timestep(void *h, double *time, double *dt) { return rk4_step(*(Oracle *)h, time, dt); }
+
+// per-block coarsening flag (-1/0) from the FWT of the current data
+// (ghosts must have been synchronised); eps_use has neq entries
+int or_threshold_flags(void *h, const double *eps_use, int *flags, double *details) {
+    Oracle &o = *(Oracle *)h;
+    const int nblk = (int)o.blocks.size();
+#pragma omp parallel for schedule(dynamic) num_threads(o.nthreads) if (o.nthreads > 1)
+    for (int b = 0; b < nblk; b++) flags[b] = threshold_block(o, b, eps_use, details ? details + size_t(b) * o.nc : nullptr);
+    return WG_OK;
+}
+
+// FWT of every block (spaghetti order, interior), result into out (full layout)
+int or_fwt(void *h, double *out) {
+    Oracle &o = *(Oracle *)h;
+    std::memcpy(out, o.data.data(), o.data.size() * sizeof(double));
+    for (size_t b = 0; b < o.blocks.size(); b++)
+        for (int c = 0; c < o.nc; c++) {
+            const double *u = o.blk((int)b) + size_t(c) * o.npts;
+            fwt_block(o, u, out + (b * o.nc + c) * o.npts);
+        }
+    return WG_OK;
+}
+
+int or_refine_everywhere(void *h) {
+    refine_everywhere(*(Oracle *)h);
+    return WG_OK;
+}
+
+// wavelet filters for inspection: which = 0 HD, 1 GD, 2 HR, 3 GR; returns lo, hi
+int or_filter(void *h, int which, int *lo, int *hi, double *coef) {
+    Oracle &o = *(Oracle *)h;
+    const Filter *f = which == 0 ? &o.wav.HD : which == 1 ? &o.wav.GD : which == 2 ? &o.wav.HR : &o.wav.GR;
+    *lo = f->lo;
+    *hi = f->hi;
+    if (coef) std::memcpy(coef, f->c.data(), f->c.size() * sizeof(double));
+    return WG_OK;
+}
+
+// run nsteps RK4 steps, returns the per-step dt in dts (may be null)
+int or_run(void *h, int nsteps, double *time, double *dts) {
+    Oracle &o = *(Oracle *)h;
+    for (int s = 0; s < nsteps; s++) {
+        double dt;
+        int st = rk4_step(o, time, &dt);
+        if (st) return st;
+        if (dts) dts[s] = dt;
+        if (*time >= o.cfg.time_max - 1e-12 * std::max(1.0, std::fabs(o.cfg.time_max))) return s + 1;
+    }
+    return nsteps;
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures under tests/golden/ from the reference's own
+committed regression files (read-only reference checkout).
+
+Run once in a container that holds the reference checkout:
+
+    python tests/golden/make_fixtures.py /path/to/reference
+
+The fixtures are the reference's HDF5 field files converted to compact numpy
+archives, so that the tests (and the GPU machine, which has no reference) can
+compare against them:
+
+* vortex2d_equi.npz -- TESTING/acm/3vortices/3vorticesEquiFD4_CDF40: 2-D ACM,
+  FD_4th_central, skew-symmetric, Bs=32, 64 blocks on level 3, state at t=10
+  (input) and t=20 (output), the (iteration, time) pairs printed in the
+  reference's run log (log.original.txt), which pin the time-step sequence,
+  and the key/value pairs of its PARAMS_3vortices.ini.
+* tg3d_equi.npz -- TESTING/acm/taylorGreen/taylorGreenEqui_FD4_CDF40: 3-D ACM,
+  Bs=20, 8 blocks on level 1, state at t=0 (input) and t=10 (output).
+* wavelet_adaptive.npz -- TESTING/wavelets: a 2-D adaptive vorticity field
+  (112 blocks, levels 2-5, Bs=32), the reference's refine-everywhere result
+  with CDF40 (448 blocks) and its coarsen-everywhere results with CDF40 and
+  CDF44.
+
+Block data are stored as interiors only, shape (Nb, ncomp, [Bs,] Bs, Bs),
+x fastest; block geometry as level (Nb,) and integer coords (Nb, 3).
+"""
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from wabbit_gb300.h5io import read_wabbit  # noqa: E402
+
+
+def _interior(d):
+    """Drop the redundant +1 point the writer appends in every direction."""
+    b = d["blocks"]
+    if d["dim"] == 2:
+        return b[:, :-1, :-1]
+    return b[:, :-1, :-1, :-1]
+
+
+def _coords3(d):
+    c = np.zeros((len(d["level"]), 3), np.int32)
+    c[:, : d["dim"]] = d["coords"]
+    return c
+
+
+def _fields(folder, names, tag):
+    ds = [read_wabbit(os.path.join(folder, f"{n}_{tag}.h5")) for n in names]
+    for d in ds[1:]:
+        assert np.array_equal(d["level"], ds[0]["level"]) and np.array_equal(d["coords"], ds[0]["coords"])
+    data = np.stack([_interior(d) for d in ds], axis=1)
+    return ds[0], data
+
+
+def _sorted(d, data):
+    """Order blocks by (level, z, y, x) so files with different block orders compare."""
+    c = _coords3(d)
+    order = np.lexsort((c[:, 0], c[:, 1], c[:, 2], d["level"]))
+    return d["level"][order].astype(np.int32), c[order], data[order]
+
+
+def vortex2d(ref):
+    folder = os.path.join(ref, "TESTING/acm/3vortices/3vorticesEquiFD4_CDF40")
+    d0, u0 = _fields(folder, ["ux", "uy", "p"], "000010000000")
+    d1, u1 = _fields(folder, ["ux", "uy", "p"], "000020000000")
+    lv0, c0, u0 = _sorted(d0, u0)
+    lv1, c1, u1 = _sorted(d1, u1)
+    assert np.array_equal(lv0, lv1) and np.array_equal(c0, c1)
+    its, times = [], []
+    with open(os.path.join(folder, "log.original.txt"), errors="ignore") as f:
+        for line in f:
+            m = re.match(r"RUN: it=\s*(\d+) time=\s*([0-9.]+)", line)
+            if m:
+                its.append(int(m.group(1)))
+                times.append(float(m.group(2)))
+    from wabbit_gb300.config import _parse_ini
+    with open(os.path.join(folder, "PARAMS_3vortices.ini"), errors="ignore") as f:
+        kv = _parse_ini(f.read())
+    np.savez_compressed(
+        os.path.join(HERE, "vortex2d_equi.npz"),
+        ini_sec=np.array([k[0] for k in kv]), ini_key=np.array([k[1] for k in kv]),
+        ini_val=np.array(list(kv.values())),
+        level=lv0, coords=c0, u_in=u0, u_out=u1, t_in=d0["time"], t_out=d1["time"],
+        iteration_in=d0["iteration"], iteration_out=d1["iteration"],
+        log_it=np.array(its, np.int64), log_time=np.array(times), domain=d0["domain"], Bs=d0["Bs"])
+
+
+def tg3d(ref):
+    folder = os.path.join(ref, "TESTING/acm/taylorGreen/taylorGreenEqui_FD4_CDF40")
+    d0, u0 = _fields(folder, ["ux", "uy", "uz", "p"], "000000000000")
+    d1, u1 = _fields(folder, ["ux", "uy", "uz", "p"], "000010000000")
+    lv0, c0, u0 = _sorted(d0, u0)
+    lv1, c1, u1 = _sorted(d1, u1)
+    assert np.array_equal(lv0, lv1) and np.array_equal(c0, c1)
+    np.savez_compressed(
+        os.path.join(HERE, "tg3d_equi.npz"),
+        level=lv0, coords=c0, u_in=u0, u_out=u1, t_in=d0["time"], t_out=d1["time"],
+        iteration_out=d1["iteration"], domain=d0["domain"], Bs=d0["Bs"])
+
+
+def wavelets(ref):
+    folder = os.path.join(ref, "TESTING/wavelets")
+    out = {}
+    d = read_wabbit(os.path.join(folder, "vor_000020000000.h5"))
+    lv, c, u = _sorted(d, _interior(d)[:, None])
+    out.update(in_level=lv, in_coords=c, in_u=u, domain=d["domain"], Bs=d["Bs"])
+    d = read_wabbit(os.path.join(folder, "adaptive_CDF40", "vor_00100.h5"))
+    lv, c, u = _sorted(d, _interior(d)[:, None])
+    out.update(refined_level=lv, refined_coords=c, refined_u=u)
+    for w in ["CDF40", "CDF44"]:
+        d = read_wabbit(os.path.join(folder, f"adaptive_{w}", "vor_00200.h5"))
+        lv, c, u = _sorted(d, _interior(d)[:, None])
+        out.update({f"coarsened_{w}_level": lv, f"coarsened_{w}_coords": c, f"coarsened_{w}_u": u})
+    np.savez_compressed(os.path.join(HERE, "wavelet_adaptive.npz"), **out)
+
+
+if __name__ == "__main__":
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    vortex2d(ref)
+    tg3d(ref)
+    wavelets(ref)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))

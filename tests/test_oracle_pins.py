@@ -1,0 +1,149 @@
+"""The CPU oracle against the reference's own regression files.
+
+Fixtures come from TESTING/acm/3vortices/3vorticesEquiFD4_CDF40,
+TESTING/acm/taylorGreen/taylorGreenEqui_FD4_CDF40 and TESTING/wavelets
+(tests/golden/make_fixtures.py). The oracle must reproduce them bit for bit:
+it restates the reference's arithmetic in the reference's order without FMA.
+"""
+import numpy as np
+import pytest
+
+from pyoracle import Oracle, interior, pad_blocks
+from wabbit_gb300 import config
+
+INI_VORTEX = dict(dim=2, Bs=32, domain=6.283185307179586, wavelet="CDF40", c0=7.0, nu=5.0e-5,
+                  gamma_p=1.0, skew=1, penal=0, CFL=1.0, time_max=20.0, write_time=10.0, J=3)
+
+
+def vortex_cfg():
+    c = config.defaults(2)
+    c.Bs[0] = c.Bs[1] = 32
+    c.domain[0] = c.domain[1] = 6.283185307179586
+    c.wavelet = b"CDF40"
+    c.g, c.g_rhs = 3, 2
+    c.Jmin = c.Jmax = 3
+    c.c0, c.nu, c.gamma_p = 7.0, 5.0e-5, 1.0
+    c.skew_symmetry, c.penalization = 1, 0
+    c.CFL = 1.0
+    c.time_max, c.write_time = 20.0, 10.0
+    return c
+
+
+def tg_cfg():
+    c = config.defaults(3)
+    c.Bs[:] = (20, 20, 20)
+    c.domain[:] = (6.283185307179586,) * 3
+    c.wavelet = b"CDF40"
+    c.g, c.g_rhs = 3, 2
+    c.Jmin = c.Jmax = 1
+    c.c0, c.nu, c.gamma_p = 10.0, 3.125e-03, 0.0
+    c.skew_symmetry, c.penalization = 1, 0
+    c.CFL = 1.0
+    c.time_max, c.write_time, c.tsave_stats = 10.0, 10.0, 0.2
+    return c
+
+
+def test_ini_reader_matches_reference_defaults(golden, tmp_path):
+    """The .ini reader reproduces the values the reference printed in its log."""
+    z = golden("vortex2d_equi.npz")
+    lines, sec = [], None
+    for s_, k, v in zip(z["ini_sec"], z["ini_key"], z["ini_val"]):
+        if s_ != sec:
+            lines.append(f"[{s_}]")
+            sec = s_
+        lines.append(f"{k}={v};")
+    path = tmp_path / "params.ini"
+    path.write_text("\n".join(lines) + "\n")
+    c = config.from_ini(str(path))
+    assert (c.dim, c.Bs[0], c.g, c.g_rhs, c.Jmax) == (2, 32, 3, 2, 3)
+    # "CFL_nu=0.2485" in log.original.txt
+    assert abs(c.CFL_nu - 0.2485) < 1e-4
+    assert c.skew_symmetry == 1 and c.penalization == 0 and c.write_time == 10.0
+
+
+def test_vortex2d_dt_sequence_first_steps(golden):
+    """dt follows the reference log (9 printed decimals) for 300 steps."""
+    z = golden("vortex2d_equi.npz")
+    cfg = vortex_cfg()
+    o = Oracle(cfg, threads=4)
+    o.set_grid(z["level"], z["coords"], pad_blocks(cfg, z["u_in"]))
+    t, dts = o.run(300, float(z["t_in"]))
+    times = float(z["t_in"]) + np.cumsum(dts)
+    assert np.max(np.abs(times - z["log_time"][:300])) < 6e-10
+
+
+@pytest.mark.slow
+def test_vortex2d_golden_t20(golden):
+    """3073 RK4 steps t=10 -> t=20 reproduce the reference output exactly."""
+    z = golden("vortex2d_equi.npz")
+    cfg = vortex_cfg()
+    o = Oracle(cfg, threads=8)
+    o.set_grid(z["level"], z["coords"], pad_blocks(cfg, z["u_in"]))
+    t, dts = o.run(10000, float(z["t_in"]))
+    assert len(dts) == len(z["log_time"]) == int(z["iteration_out"] - z["iteration_in"])
+    assert t == 20.0
+    u = interior(cfg, o.data())
+    assert np.array_equal(u, z["u_out"])
+
+
+@pytest.mark.slow
+def test_tg3d_golden_t10(golden):
+    """3-D Taylor-Green, 713 RK4 steps, reproduces the reference output exactly."""
+    z = golden("tg3d_equi.npz")
+    cfg = tg_cfg()
+    o = Oracle(cfg, threads=8)
+    o.set_grid(z["level"], z["coords"], pad_blocks(cfg, z["u_in"]))
+    t, dts = o.run(10000, float(z["t_in"]))
+    assert len(dts) == int(z["iteration_out"])
+    u = interior(cfg, o.data())
+    assert np.array_equal(u, z["u_out"])
+
+
+def wavelet_cfg(w="CDF40", g=3):
+    c = config.defaults(2)
+    c.Bs[0] = c.Bs[1] = 32
+    c.domain[0] = c.domain[1] = 6.283185307179586
+    c.neq = 1
+    c.wavelet = w.encode()
+    c.g, c.g_rhs = g, 2
+    c.Jmin, c.Jmax = 1, 7
+    return c
+
+
+def test_refine_everywhere_golden(golden):
+    """Full ghost sync (g=3, levels 2-5) + refineBlock match the reference bit for bit."""
+    z = golden("wavelet_adaptive.npz")
+    cfg = wavelet_cfg()
+    o = Oracle(cfg)
+    o.set_grid(z["in_level"], z["in_coords"], pad_blocks(cfg, z["in_u"]))
+    o.sync(cfg.g, cfg.g, ignore_filter=False)
+    o.refine_everywhere()
+    lv, co = o.grid()
+    u = interior(cfg, o.data())
+    order = np.lexsort((co[:, 0], co[:, 1], co[:, 2], lv))
+    assert np.array_equal(lv[order], z["refined_level"])
+    assert np.array_equal(co[order], z["refined_coords"])
+    assert np.array_equal(u[order], z["refined_u"])
+
+
+@pytest.mark.parametrize("w", ["CDF20", "CDF40", "CDF44", "CDF60", "CDF62"])
+def test_wavelet_filter_sums(w):
+    """Filter-bank identities checked at start-up by the reference
+    (module_wavelets.f90:1551-1554): sum(HD)=1, sum(HR)=2, sum(GD)=0."""
+    g = {"CDF20": 1, "CDF40": 3, "CDF44": 6, "CDF60": 5, "CDF62": 6}[w]
+    o = Oracle(wavelet_cfg(w, g))
+    assert abs(o.filter(0)[1].sum() - 1.0) < 1e-15
+    assert abs(o.filter(1)[1].sum() - 0.0) < 1e-15
+    assert abs(o.filter(2)[1].sum() - 2.0) < 1e-15
+    # GR = (-1)^i HD: a delta for CDFX0, alternating-sum zero for lifted wavelets
+    assert abs(o.filter(3)[1].sum() - (1.0 if w.endswith("0") else 0.0)) < 1e-15
+
+
+def test_cdf40_filters_match_reference_log():
+    """Filters printed in log.original.txt for CDF40."""
+    o = Oracle(wavelet_cfg("CDF40", 3))
+    lo, gd = o.filter(1)
+    assert lo == -3
+    assert np.array_equal(gd, [6.25e-2, 0.0, -5.625e-1, 1.0, -5.625e-1, 0.0, 6.25e-2])
+    lo, hr = o.filter(2)
+    assert np.array_equal(hr, [-6.25e-2, 0.0, 5.625e-1, 1.0, 5.625e-1, 0.0, -6.25e-2])
