@@ -86,8 +86,92 @@ typedef struct wg_config {
 
 typedef struct wg_ctx wg_ctx;
 
-/* Fill *cfg with the reference defaults for a 2-D/3-D ACM run. */
+/* Fill *cfg with the reference defaults for a 2-D/3-D ACM run
+ * (ini_file_to_params.f90, READ_PARAMETERS_ACM module_ACM.f90:172-609). */
 int wg_config_defaults(wg_config *cfg, int dim);
+
+/* Message of the last failing call on this thread. */
+const char *wg_last_error(void);
+
+/* Device bytes one block slot needs (state, two RK stage buffers with
+ * g_rhs ghosts, interior RK accumulator, descriptor). Replaces the memory
+ * estimate of allocate_forest (LIB/MESH/allocate_forest.f90:122-147). */
+size_t wg_bytes_per_block(const wg_config *cfg);
+
+/* ---- context: a device arena for one block geometry -------------------
+ * Replaces allocate_forest / deallocate_forest
+ * (LIB/MESH/allocate_forest.f90:1-381): all heavy data lives in HBM for the
+ * lifetime of the context; max_blocks is the arena size. */
+int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **ctx);
+int wg_ctx_destroy(wg_ctx *ctx);
+/* 1: FMA stencil (default); 0: strict reference arithmetic (no FMA). */
+int wg_set_variant(wg_ctx *ctx, int fast);
+int wg_synchronize(wg_ctx *ctx);
+/* the context's CUDA stream (cudaStream_t) */
+void *wg_stream(wg_ctx *ctx);
+
+/* ---- trees: independent solves in one arena (the reference's tree_ID) -- */
+int wg_tree_create(wg_ctx *ctx, const wg_config *cfg, int *tree);
+int wg_tree_destroy(wg_ctx *ctx, int tree);
+
+/* Set the grid of a tree: level[nblk], coords[3*nblk] (see top of file).
+ * Runs the neighbour search (find_neighbor, LIB/MESH/find_neighbors.f90:18)
+ * and rejects grids that are not complete, periodic and graded. The state
+ * of the new blocks is undefined until wg_upload_state. */
+int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *coords);
+int wg_get_nblocks(wg_ctx *ctx, int tree, int *nblk);
+int wg_get_grid(wg_ctx *ctx, int tree, int cap, int *level, int *coords);
+
+/* Heavy data in the reference block layout (hvy_block, see top of file). */
+int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks);
+int wg_download_state(wg_ctx *ctx, int tree, double *host_blocks);
+/* Penalisation mask in the layout of hvy_mask (..., 1:6, Nb): chi, usx,
+ * usy, usz, colour, sponge (createMask_tree, LIB/MESH/createMask_tree.f90);
+ * NULL removes it. Only blocks with a non-zero mask keep a device copy. */
+int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask);
+
+int wg_set_time(wg_ctx *ctx, int tree, double time);
+int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);
+
+/* ---- the hot path ------------------------------------------------------ */
+/* sync_ghosts_RHS_tree / sync_ghosts_tree without the HD filter
+ * (LIB/MPI/synchronize_ghosts_generic.f90:121-174): fill gminus/gplus ghost
+ * layers of every block by copy, restriction and prediction. */
+int wg_sync_ghosts(wg_ctx *ctx, int tree, int gminus, int gplus);
+/* RHS_ACM "local_stage" of every block (LIB/EQUATION/ACMnew/rhs_ACM.f90:7;
+ * plugin entry RHS_META, LIB/EQUATION/module_physics_metamodule.f90:268)
+ * on the current synchronised state; host_rhs in the hvy_block layout. */
+int wg_rhs(wg_ctx *ctx, int tree, double *host_rhs);
+/* calculate_time_step + GET_DT_BLOCK_ACM (LIB/TIME/calculate_time_step.f90:2,
+ * LIB/EQUATION/ACMnew/module_ACM.f90:617) at the tree's current time. */
+int wg_compute_dt(wg_ctx *ctx, int tree, double *dt);
+/* timeStep_tree -> RungeKuttaGeneric, default RK4 tableau
+ * (LIB/TIME/timeStep_tree.f90:1, LIB/TIME/runge_kutta_generic.f90:1):
+ * sync, dt, four stages; the tree's time advances on the device. */
+int wg_rk4_step(wg_ctx *ctx, int tree, double *time, double *dt);
+/* nsteps RK4 steps of each listed tree, asynchronous; use_graph captures the
+ * launch sequence of one step of all trees in a CUDA graph and replays it. */
+int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph);
+/* coarseningIndicator_tree -> coarseningIndicator_block -> threshold_block
+ * (LIB/MESH/coarseningIndicator_tree.f90:4,
+ *  LIB/INDICATORS/threshold_block.f90:1): one-level FWT of every block and
+ * detail thresholding; flags[b] = -1 (may coarsen) or 0. eps_use holds the
+ * per-component threshold (eps * norm). Ghosts must hold g synced layers. */
+int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details);
+/* refine_tree(..., "everywhere") data part: refineBlock for every block
+ * (LIB/MESH/refinementExecute.f90:4-116). Block b becomes blocks
+ * 2^d*b .. 2^d*b+2^d-1. Ghosts must hold g synced layers. */
+int wg_refine_everywhere(wg_ctx *ctx, int tree);
+
+/* ---- inspection (tests, tooling) --------------------------------------- */
+/* ghost-patch table: returns the patch count; out receives 19 ints per
+ * patch: src, dst, op, stage, rlo[3], rhi[3], slo[3], shi[3], blo[3] */
+int wg_sync_table(wg_ctx *ctx, int tree, int gminus, int gplus, int thin, int cap, int *out);
+int wg_block_slot(wg_ctx *ctx, int tree, int b);
+/* the same table computed on the host alone (no device needed), with block
+ * indices in place of arena slots; thin != 0 gives the g_rhs-ghost layout */
+int wg_sync_table_host(const wg_config *cfg, int nblk, const int *level, const int *coords, int gminus,
+                       int gplus, int thin, int cap, int *out);
 
 #ifdef __cplusplus
 }

@@ -48,6 +48,7 @@ def lib():
         L.or_set_mask.argtypes = [ctypes.c_void_p, _dp]
         L.or_get_neighbors.argtypes = [ctypes.c_void_p, _ip]
         L.or_sync_ghosts.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.or_sync_ghosts.restype = ctypes.c_int
         L.or_rhs.argtypes = [ctypes.c_void_p, _dp]
         L.or_dt.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp]
         L.or_timestep.argtypes = [ctypes.c_void_p, _dp, _dp]
@@ -131,7 +132,8 @@ class Oracle:
     def sync(self, gminus=None, gplus=None, ignore_filter=True):
         gm = self.cfg.g_rhs if gminus is None else gminus
         gp = gm if gplus is None else gplus
-        self.L.or_sync_ghosts(self.h, gm, gp, 1 if ignore_filter else 0)
+        if self.L.or_sync_ghosts(self.h, gm, gp, 1 if ignore_filter else 0) != 0:
+            raise ValueError("oracle: ghost widths out of range")
 
     def rhs(self):
         out = np.zeros((self.nblocks,) + self.block_shape)

@@ -977,9 +977,17 @@ static void refine_everywhere(Oracle &o) {
 extern "C" {
 
 void *or_create(const wg_config *cfg) {
+    // ghost widths the oracle's loops rely on (the reference aborts likewise)
+    if (cfg->g < 2 || cfg->g_rhs < 2 || cfg->g_rhs > cfg->g) return nullptr;
     Oracle *o = new Oracle();
     o->cfg = *cfg;
     if (!setup_wavelet(cfg->wavelet, 2, o->wav)) { delete o; return nullptr; }
+    // every filter and the predictor stencil must fit into the ghost layer
+    {
+        const Wavelet &w = o->wav;
+        int need = std::max({std::abs(w.HD.lo), w.HD.hi, std::abs(w.GD.lo), w.GD.hi, w.X - 1});
+        if (cfg->g < need) { delete o; return nullptr; }
+    }
     o->nx = cfg->Bs[0] + 2 * cfg->g;
     o->ny = cfg->Bs[1] + 2 * cfg->g;
     o->nz = cfg->dim == 3 ? cfg->Bs[2] + 2 * cfg->g : 1;
@@ -1044,7 +1052,9 @@ int or_get_neighbors(void *h, int *out) {
 }
 
 int or_sync_ghosts(void *h, int gminus, int gplus, int ignore_filter) {
-    sync_ghosts(*(Oracle *)h, gminus, gplus, ignore_filter != 0);
+    Oracle &o = *(Oracle *)h;
+    if (gminus < 1 || gplus < 1 || gminus > o.cfg.g || gplus > o.cfg.g) return WG_EINVAL;
+    sync_ghosts(o, gminus, gplus, ignore_filter != 0);
     return WG_OK;
 }
 

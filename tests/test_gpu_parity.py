@@ -1,0 +1,218 @@
+"""GPU hot path against the CPU oracle and the reference's regression files.
+
+Bit-exactness bar: the sync, the dt, the strict-variant RHS/RK4 and the
+wavelet details are computed with the reference's rounding and must match
+bit for bit. The fast (FMA) variant must agree within relative L2 <= 1e-12
+per step (spec tolerance), and within 1e-10 after thousands of steps.
+"""
+import numpy as np
+import pytest
+
+from helpers import rel_l2, random_state, small_cfg, smooth_state, sphere_mask, vortex_cfg
+from pyoracle import Oracle, interior, pad_blocks
+from wabbit_gb300 import config, grids
+from wabbit_gb300.solver import Context
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def grids2d():
+    return grids.random_graded(2, 2, 5, seed=11, frac=0.3)
+
+
+@pytest.fixture(scope="module")
+def grids3d():
+    return grids.random_graded(3, 1, 3, seed=5, frac=0.3)
+
+
+@pytest.mark.parametrize("dim,wavelet", [(2, "CDF40"), (3, "CDF40"), (2, "CDF20"), (2, "CDF60")])
+@pytest.mark.parametrize("full", [False, True])
+def test_sync_bitexact(dim, wavelet, full, grids2d, grids3d):
+    g, _ = config.wavelet_ghosts(wavelet)
+    cfg = small_cfg(dim, wavelet, Bs=8 if 2 * g - 1 <= 8 else 16, jmin=1 if dim == 3 else 2, jmax=3 if dim == 3 else 5)
+    lv, co = grids2d if dim == 2 else grids3d
+    data = random_state(cfg, len(lv), 3)
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    gm = cfg.g if full else cfg.g_rhs
+    o.sync(gm, gm, ignore_filter=True)
+    with Context(cfg, len(lv) + 8) as ctx:
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(data)
+        if full:
+            f.sync_ghosts_tree()
+        else:
+            f.sync_ghosts_RHS_tree()
+        got = f.download()
+    assert np.array_equal(got, o.data())
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("skew", [0, 1])
+def test_rhs_strict_bitexact_fast_close(dim, skew, grids2d, grids3d):
+    cfg = small_cfg(dim, skew=skew, jmin=1 if dim == 3 else 2, jmax=3 if dim == 3 else 5)
+    lv, co = grids2d if dim == 2 else grids3d
+    data = smooth_state(cfg, lv, co, 7)
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    o.sync()
+    ref = interior(cfg, o.rhs())
+    with Context(cfg, len(lv) + 8) as ctx:
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(data)
+        f.sync_ghosts_RHS_tree()
+        ctx.set_variant(False)
+        strict = interior(cfg, f.RHS_ACM())
+        ctx.set_variant(True)
+        fast = interior(cfg, f.RHS_ACM())
+    assert np.array_equal(strict, ref)
+    assert rel_l2(fast, ref) < 1e-12
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("penal", [0, 1])
+def test_rk4_steps_strict_bitexact(dim, penal, grids2d, grids3d):
+    cfg = small_cfg(dim, skew=0, penal=penal, jmin=1 if dim == 3 else 2, jmax=3 if dim == 3 else 5)
+    cfg.C_eta = 1e-2
+    lv, co = grids2d if dim == 2 else grids3d
+    data = smooth_state(cfg, lv, co, 9)
+    mask = sphere_mask(cfg, lv, co, [0.5, 0.6, 0.7], 0.2) if penal else None
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    o.set_mask(mask)
+    with Context(cfg, len(lv) + 8) as ctx:
+        ctx.set_variant(False)
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(data)
+        f.set_mask(mask)
+        f.set_time(0.0)
+        t_ref = 0.0
+        for _ in range(3):
+            t_ref, dt_ref = o.step(t_ref)
+            t, dt = f.timeStep_tree()
+            assert dt == dt_ref and t == t_ref
+        got = interior(cfg, f.download())
+    assert np.array_equal(got, interior(cfg, o.data()))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_rk4_fast_within_tolerance(dim, grids2d, grids3d):
+    cfg = small_cfg(dim, skew=1, jmin=1 if dim == 3 else 2, jmax=3 if dim == 3 else 5)
+    lv, co = grids2d if dim == 2 else grids3d
+    data = smooth_state(cfg, lv, co, 13)
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    with Context(cfg, len(lv) + 8) as ctx:
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(data)
+        f.set_time(0.0)
+        t_ref = 0.0
+        for _ in range(5):
+            t_ref, _ = o.step(t_ref)
+            f.timeStep_tree()
+            err = rel_l2(interior(cfg, f.download()), interior(cfg, o.data()))
+            assert err < 1e-12
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_vortex2d_reference_golden(golden, fast):
+    """3073 RK4 steps of the reference's 3vorticesEquiFD4_CDF40 case on the GPU."""
+    z = golden("vortex2d_equi.npz")
+    cfg = vortex_cfg()
+    nsteps = len(z["log_time"])
+    with Context(cfg, 80) as ctx:
+        ctx.set_variant(fast)
+        f = ctx.forest()
+        f.set_grid(z["level"], z["coords"])
+        f.upload(pad_blocks(cfg, z["u_in"]))
+        f.set_time(float(z["t_in"]))
+        f.run(nsteps, use_graph=True)
+        t, dt = f.time()
+        u = interior(cfg, f.download())
+    assert t == 20.0
+    if fast:
+        assert rel_l2(u, z["u_out"]) < 1e-10
+    else:
+        assert np.array_equal(u, z["u_out"])
+
+
+def test_tg3d_reference_golden(golden):
+    z = golden("tg3d_equi.npz")
+    c = config.defaults(3)
+    c.Bs[:] = (20, 20, 20)
+    c.domain[:] = (6.283185307179586,) * 3
+    c.g, c.g_rhs = 3, 2
+    c.Jmin = c.Jmax = 1
+    c.c0, c.nu, c.gamma_p = 10.0, 3.125e-03, 0.0
+    c.skew_symmetry, c.penalization = 1, 0
+    c.CFL = 1.0
+    c.time_max, c.write_time, c.tsave_stats = 10.0, 10.0, 0.2
+    with Context(c, 8) as ctx:
+        ctx.set_variant(False)
+        f = ctx.forest()
+        f.set_grid(z["level"], z["coords"])
+        f.upload(pad_blocks(c, z["u_in"]))
+        f.set_time(0.0)
+        f.run(int(z["iteration_out"]), use_graph=False)
+        t, _ = f.time()
+        u = interior(c, f.download())
+    assert t == 10.0
+    assert np.array_equal(u, z["u_out"])
+
+
+def test_refine_everywhere_reference_golden(golden):
+    z = golden("wavelet_adaptive.npz")
+    c = config.defaults(2)
+    c.Bs[0] = c.Bs[1] = 32
+    c.domain[0] = c.domain[1] = 6.283185307179586
+    c.neq = 3  # the context needs dim+1 components: the field goes in component 0
+    c.wavelet = b"CDF40"
+    c.g, c.g_rhs = 3, 2
+    c.Jmin, c.Jmax = 1, 7
+    u = np.zeros((len(z["in_level"]), 3) + z["in_u"].shape[2:])
+    u[:, 0] = z["in_u"][:, 0]
+    with Context(c, 600) as ctx:
+        f = ctx.forest()
+        f.set_grid(z["in_level"], z["in_coords"])
+        f.upload(pad_blocks(c, u))
+        f.sync_ghosts_tree()
+        f.refine_everywhere()
+        lv, co = f.grid()
+        got = interior(c, f.download())[:, :1]
+    order = np.lexsort((co[:, 0], co[:, 1], co[:, 2], lv))
+    assert np.array_equal(lv[order], z["refined_level"])
+    assert np.array_equal(co[order], z["refined_coords"])
+    assert np.array_equal(got[order], z["refined_u"])
+
+
+@pytest.mark.parametrize("dim,wavelet", [(2, "CDF40"), (3, "CDF40"), (2, "CDF44"), (3, "CDF44"), (2, "CDF22")])
+def test_threshold_flags_bitexact(dim, wavelet, grids2d, grids3d):
+    g, _ = config.wavelet_ghosts(wavelet)
+    cfg = small_cfg(dim, wavelet, Bs=8 if 2 * g - 1 <= 8 else 12, jmin=1 if dim == 3 else 2, jmax=3 if dim == 3 else 5)
+    lv, co = grids2d if dim == 2 else grids3d
+    data = smooth_state(cfg, lv, co, 21)
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    o.sync(cfg.g, cfg.g, ignore_filter=True)
+    full = o.data()
+    # thresholds near the median detail so both decisions occur
+    _, det0 = o.flags(np.full(cfg.neq, 1.0))
+    eps = np.median(det0, axis=0)
+    fl_ref, det_ref = o.flags(eps)
+    with Context(cfg, len(lv) + 8) as ctx:
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(full)
+        fl, det = f.coarseningIndicator(eps)
+    assert np.array_equal(det, det_ref)
+    assert np.array_equal(fl, fl_ref)
+    assert (fl == -1).any() and (fl == 0).any()

@@ -66,15 +66,16 @@ class WgConfig(ctypes.Structure):
         return self.nx * (self.Bs[1] + 2 * self.g) * self.nz
 
 
-# wavelet -> minimal number of ghost nodes g_min and the RHS ghost width
-# (setup_wavelet, module_wavelets.f90:1327-1340, with FD_4th_central: FD size 2)
+# wavelet -> default number of ghost nodes g and the RHS ghost width g_rhs
+# (setup_wavelet, module_wavelets.f90:1327-1340; ini_file_to_params.f90:293-310
+# raises both to the FD_4th_central stencil half-width 2)
 def wavelet_ghosts(wavelet: str) -> tuple[int, int]:
     X, Y = int(wavelet[3]), int(wavelet[4])
     hr = X - 1                       # HR support -(X-1)..(X-1)
     hd = 0 if Y == 0 else (X - 1) + (Y - 1)
-    g_min = max(hr, hd)
+    g = max(hr, hd, 2)
     g_rhs = max(X // 2, 2)
-    return g_min, g_rhs
+    return g, g_rhs
 
 
 def defaults(dim: int = 2) -> WgConfig:

@@ -1,0 +1,912 @@
+// capi.cu -- the C ABI of the GB300 hot path (include/wabbit_gb300.h).
+//
+// A context is one device arena for a fixed block geometry (dim, Bs, g, neq)
+// holding up to max_blocks blocks. Blocks belong to trees: independent solves
+// with their own grid, physics constants, time and dt. The host keeps each
+// tree's grid (Forest) and derives flat ghost-patch tables from it whenever
+// the grid changes; the heavy data stays in HBM.
+//
+// Device buffers per block slot:
+//   A    full layout (ghost width g): the state u (hvy_block)
+//   B, C thin layout (ghost width g_rhs): RK stage inputs
+//   acc  interior only: u_n + dt*sum b_j k_j (the RK accumulator)
+//   mask interior only, 6 components, only for blocks that carry a mask
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/wabbit_gb300.h"
+#include "common.cuh"
+
+namespace wg {
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
+    return fail(WG_ECUDA, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+
+template <class T>
+struct DevArray {
+    T *p = nullptr;
+    size_t n = 0, cap = 0;
+    ~DevArray() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t upload(const T *h, size_t count, cudaStream_t s) {
+        if (count > cap) {
+            if (p) cudaFree(p);
+            p = nullptr;
+            cap = 0;
+            cudaError_t e = cudaMalloc(&p, sizeof(T) * (count ? count : 1));
+            if (e != cudaSuccess) return e;
+            cap = count;
+        }
+        n = count;
+        if (!count) return cudaSuccess;
+        return cudaMemcpyAsync(p, h, sizeof(T) * count, cudaMemcpyHostToDevice, s);
+    }
+};
+
+struct SyncPlan {
+    SyncTable table;
+    DevArray<Patch> d;
+};
+
+struct Tree {
+    bool live = false;
+    wg_config cfg;
+    TreeParams tp;
+    Forest forest;
+    std::vector<int> slots;            // block -> arena slot
+    std::vector<int> mask_slot;        // block -> mask slot or -1
+    DevArray<int> d_all, d_plain, d_masked;   // slot lists
+    int n_plain = 0, n_masked = 0;
+    std::map<long long, std::unique_ptr<SyncPlan>> sync;   // key: gm, gp, buffer
+    double time = 0.0;
+};
+
+}  // namespace wg
+
+using namespace wg;
+
+struct wg_ctx {
+    wg_config cfg;
+    Geometry geo;
+    WaveletInfo wav;
+    int max_blocks = 0;
+    BufGeo gA, gT;                      // full and thin layouts
+    long long nint = 0;                 // interior points per block
+    double *A = nullptr, *B = nullptr, *C = nullptr, *acc = nullptr;
+    double *mask = nullptr;
+    int mask_cap = 0;
+    std::vector<int> mask_free;
+    BlockDesc *d_desc = nullptr;
+    std::vector<BlockDesc> h_desc;
+    TreeParams *d_tp = nullptr;
+    TreeClock *d_clk = nullptr;
+    int max_trees = 64;
+    std::vector<Tree> trees;
+    std::vector<int> free_slots;
+    cudaStream_t stream = nullptr;
+    int variant_fast = 1;               // 1: FMA stencil, 0: strict reference arithmetic
+    DevArray<int> d_tree_ids;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<int> graph_trees;
+    int graph_version = -1;
+    int grid_version = 0;
+};
+
+namespace {
+
+int check_cfg(const wg_config *c) {
+    if (!c) return fail(WG_EINVAL, "null config");
+    if (c->dim != 2 && c->dim != 3) return fail(WG_EINVAL, "dim must be 2 or 3");
+    if (c->neq != c->dim + 1) return fail(WG_ENOTSUP, "neq must be dim+1 (ACM: velocity + pressure)");
+    for (int d = 0; d < c->dim; d++)
+        if (c->Bs[d] < 4 || (c->Bs[d] % 2) || c->Bs[d] > 64) return fail(WG_EINVAL, "Bs must be even, 4..64");
+    if (c->g_rhs < 2 || c->g < c->g_rhs) return fail(WG_EINVAL, "need g >= g_rhs >= 2 for FD_4th_central");
+    WaveletInfo w;
+    if (!make_wavelet(c->wavelet, w)) return fail(WG_EINVAL, "unknown wavelet '%s'", c->wavelet);
+    if (c->g < w.g_min) return fail(WG_EINVAL, "%s needs g >= %d", c->wavelet, w.g_min);
+    // a restriction takes 2g-1 fine points next to the interface; if that
+    // exceeds the block, it would read ghost nodes of the same sync stage
+    for (int d = 0; d < c->dim; d++)
+        if (2 * c->g - 1 > c->Bs[d]) return fail(WG_EINVAL, "Bs=%d too small for g=%d (need Bs >= 2g-1)", c->Bs[d], c->g);
+    if (c->Jmin < 0 || c->Jmax < c->Jmin || c->Jmax > 18) return fail(WG_EINVAL, "bad Jmin/Jmax");
+    return WG_OK;
+}
+
+TreeParams make_params(const wg_config &c) {
+    TreeParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.c0 = c.c0;
+    p.nu = c.nu;
+    p.gamma_p = c.gamma_p;
+    p.C_eta = c.C_eta;
+    p.C_eta_inv = 1.0 / c.C_eta;
+    p.C_sponge = c.C_sponge;
+    p.C_sponge_inv = 1.0 / c.C_sponge;
+    for (int i = 0; i < 3; i++) p.u_mean_set[i] = c.u_mean_set[i];
+    p.CFL = c.CFL;
+    p.CFL_nu = c.CFL_nu;
+    p.CFL_eta = c.CFL_eta;
+    p.dt_fixed = c.dt_fixed;
+    p.dt_max = c.dt_max;
+    p.time_max = c.time_max;
+    p.write_time = c.write_time;
+    p.tsave_stats = c.tsave_stats;
+    p.penalization = c.penalization;
+    p.use_sponge = c.use_sponge;
+    p.skew = c.skew_symmetry;
+    return p;
+}
+
+Tree *get_tree(wg_ctx *ctx, int t) {
+    if (!ctx || t < 0 || t >= (int)ctx->trees.size() || !ctx->trees[t].live) {
+        fail(WG_EINVAL, "invalid tree id %d", t);
+        return nullptr;
+    }
+    return &ctx->trees[t];
+}
+
+long long sync_key(int gm, int gp, int thin) { return ((long long)gm << 20) | ((long long)gp << 4) | thin; }
+
+int get_sync(wg_ctx *ctx, Tree &t, int gm, int gp, bool thin, SyncPlan **out) {
+    const long long key = sync_key(gm, gp, thin ? 1 : 0);
+    auto it = t.sync.find(key);
+    if (it == t.sync.end()) {
+        std::unique_ptr<SyncPlan> sp(new SyncPlan());
+        std::string err;
+        if (!make_sync_table(t.forest, ctx->geo, ctx->wav, gm, gp, thin ? ctx->gT.gb : ctx->gA.gb, 0, sp->table, err))
+            return fail(WG_EGRID, "sync table: %s", err.c_str());
+        for (auto &p : sp->table.patches) {
+            p.src = t.slots[p.src];
+            p.dst = t.slots[p.dst];
+        }
+        WG_CUDA_OK(sp->d.upload(sp->table.patches.data(), sp->table.patches.size(), ctx->stream));
+        it = t.sync.emplace(key, std::move(sp)).first;
+    }
+    *out = it->second.get();
+    return WG_OK;
+}
+
+int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp) {
+    SyncPlan *sp;
+    int st = get_sync(ctx, t, gm, gp, thin, &sp);
+    if (st) return st;
+    const BufGeo geo = thin ? ctx->gT : ctx->gA;
+    for (int s = 0; s < sp->table.nstages; s++) {
+        const int b = sp->table.stage_begin[s], e = sp->table.stage_begin[s + 1];
+        WG_CUDA_OK(launch_sync(sp->d.p + b, e - b, buf, geo, ctx->geo.nc, ctx->wav.order_predictor, ctx->stream));
+    }
+    return WG_OK;
+}
+
+void release_tree_blocks(wg_ctx *ctx, Tree &t) {
+    for (int s : t.slots) ctx->free_slots.push_back(s);
+    for (int m : t.mask_slot)
+        if (m >= 0) ctx->mask_free.push_back(m);
+    t.slots.clear();
+    t.mask_slot.clear();
+    t.sync.clear();
+    t.n_plain = t.n_masked = 0;
+}
+
+int upload_lists(wg_ctx *ctx, Tree &t) {
+    std::vector<int> plain, masked;
+    for (size_t b = 0; b < t.slots.size(); b++) (t.mask_slot[b] >= 0 ? masked : plain).push_back(t.slots[b]);
+    t.n_plain = (int)plain.size();
+    t.n_masked = (int)masked.size();
+    WG_CUDA_OK(t.d_all.upload(t.slots.data(), t.slots.size(), ctx->stream));
+    WG_CUDA_OK(t.d_plain.upload(plain.data(), plain.size(), ctx->stream));
+    WG_CUDA_OK(t.d_masked.upload(masked.data(), masked.size(), ctx->stream));
+    return WG_OK;
+}
+
+// (re)write the descriptors of a tree's blocks
+int upload_desc(wg_ctx *ctx, Tree &t, int tree_id) {
+    const wg_config &c = ctx->cfg;
+    for (size_t b = 0; b < t.slots.size(); b++) {
+        BlockDesc d;
+        std::memset(&d, 0, sizeof(d));
+        const int lv = t.forest.level[b];
+        for (int k = 0; k < 3; k++) d.dx[k] = k < c.dim ? std::pow(2.0, -lv) * c.domain[k] / (double)c.Bs[k] : 0.0;
+        d.tree = tree_id;
+        d.level = lv;
+        d.mask = t.mask_slot[b];
+        ctx->h_desc[t.slots[b]] = d;
+        WG_CUDA_OK(cudaMemcpyAsync(ctx->d_desc + t.slots[b], &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    return WG_OK;
+}
+
+int stage_launch(wg_ctx *ctx, Tree &t, int stage, const double *in, BufGeo gin, double *out, BufGeo gout) {
+    const int dim = ctx->cfg.dim;
+    const int base = (ctx->variant_fast ? 1 : 0) | (t.cfg.skew_symmetry ? 2 : 0);
+    const int *Bs = ctx->cfg.Bs;
+    WG_CUDA_OK(launch_acm_stage(base, dim, stage, t.d_plain.p, t.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
+                                gin, out, gout, ctx->A, ctx->gA, ctx->acc, ctx->mask, Bs[0], Bs[1], Bs[2],
+                                ctx->geo.nc, ctx->stream));
+    WG_CUDA_OK(launch_acm_stage(base | 4, dim, stage, t.d_masked.p, t.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk,
+                                in, gin, out, gout, ctx->A, ctx->gA, ctx->acc, ctx->mask, Bs[0], Bs[1], Bs[2],
+                                ctx->geo.nc, ctx->stream));
+    return WG_OK;
+}
+
+// one RK4 step of one tree, fully asynchronous on ctx->stream
+int rk4_enqueue(wg_ctx *ctx, int tree_id) {
+    Tree &t = ctx->trees[tree_id];
+    const int g_rhs = ctx->cfg.g_rhs;
+    const int *Bs = ctx->cfg.Bs;
+    int st;
+    if ((st = run_sync(ctx, t, ctx->A, false, g_rhs, g_rhs))) return st;
+    WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
+                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream));
+    if ((st = stage_launch(ctx, t, 1, ctx->A, ctx->gA, ctx->B, ctx->gT))) return st;
+    if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs))) return st;
+    if ((st = stage_launch(ctx, t, 2, ctx->B, ctx->gT, ctx->C, ctx->gT))) return st;
+    if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs))) return st;
+    if ((st = stage_launch(ctx, t, 3, ctx->C, ctx->gT, ctx->B, ctx->gT))) return st;
+    if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs))) return st;
+    if ((st = stage_launch(ctx, t, 4, ctx->B, ctx->gT, nullptr, ctx->gT))) return st;
+    WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
+    return WG_OK;
+}
+
+int read_clock(wg_ctx *ctx, int tree, TreeClock *out) {
+    WG_CUDA_OK(cudaMemcpyAsync(out, ctx->d_clk + tree, sizeof(TreeClock), cudaMemcpyDeviceToHost, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *wg_last_error(void) { return g_err.c_str(); }
+
+int wg_config_defaults(wg_config *c, int dim) {
+    if (!c || (dim != 2 && dim != 3)) return fail(WG_EINVAL, "bad arguments");
+    std::memset(c, 0, sizeof(*c));
+    c->dim = dim;
+    c->Bs[0] = c->Bs[1] = 16;
+    c->Bs[2] = dim == 3 ? 16 : 1;
+    std::strcpy(c->wavelet, "CDF40");
+    c->g = 3;
+    c->g_rhs = 2;
+    c->neq = dim + 1;
+    c->domain[0] = c->domain[1] = c->domain[2] = 1.0;
+    c->Jmin = 1;
+    c->Jmax = 1;
+    c->c0 = 10.0;
+    c->nu = 1e-1;
+    c->gamma_p = 1.0;
+    c->penalization = 1;
+    c->C_eta = 1.0;
+    c->C_sponge = 1e-2;
+    c->u_mean_set[0] = 1.0;
+    c->CFL = 1.0;
+    c->CFL_eta = 0.99;
+    c->CFL_nu = 0.95 * 2.79 / (5.333 * (double)dim);
+    c->time_max = 1.0;
+    c->eps = 1e-3;
+    for (int i = 0; i < 8; i++) c->threshold_state_vector_component[i] = 1;
+    return WG_OK;
+}
+
+size_t wg_bytes_per_block(const wg_config *c) {
+    if (!c) return 0;
+    const long long nA = (long long)(c->Bs[0] + 2 * c->g) * (c->Bs[1] + 2 * c->g) * (c->dim == 3 ? c->Bs[2] + 2 * c->g : 1);
+    const long long nT = (long long)(c->Bs[0] + 2 * c->g_rhs) * (c->Bs[1] + 2 * c->g_rhs) *
+                         (c->dim == 3 ? c->Bs[2] + 2 * c->g_rhs : 1);
+    const long long nI = (long long)c->Bs[0] * c->Bs[1] * (c->dim == 3 ? c->Bs[2] : 1);
+    return sizeof(double) * (size_t)c->neq * (size_t)(nA + 2 * nT + nI) + sizeof(BlockDesc);
+}
+
+int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
+    if (!out) return fail(WG_EINVAL, "null output");
+    *out = nullptr;
+    int st = check_cfg(cfg);
+    if (st) return st;
+    if (max_blocks <= 0) return fail(WG_EINVAL, "max_blocks must be positive");
+    std::unique_ptr<wg_ctx> ctx(new wg_ctx());
+    ctx->cfg = *cfg;
+    ctx->geo.dim = cfg->dim;
+    for (int d = 0; d < 3; d++) ctx->geo.Bs[d] = d < cfg->dim ? cfg->Bs[d] : 1;
+    ctx->geo.g = cfg->g;
+    ctx->geo.nc = cfg->neq;
+    make_wavelet(cfg->wavelet, ctx->wav);
+    ctx->max_blocks = max_blocks;
+    const int dim = cfg->dim;
+    ctx->gA = {cfg->Bs[0] + 2 * cfg->g, cfg->Bs[1] + 2 * cfg->g, dim == 3 ? cfg->Bs[2] + 2 * cfg->g : 1, cfg->g};
+    ctx->gT = {cfg->Bs[0] + 2 * cfg->g_rhs, cfg->Bs[1] + 2 * cfg->g_rhs, dim == 3 ? cfg->Bs[2] + 2 * cfg->g_rhs : 1,
+               cfg->g_rhs};
+    ctx->nint = (long long)cfg->Bs[0] * cfg->Bs[1] * (dim == 3 ? cfg->Bs[2] : 1);
+    const size_t nc = cfg->neq;
+    const size_t bytesA = sizeof(double) * nc * ctx->gA.npts() * max_blocks;
+    const size_t bytesT = sizeof(double) * nc * ctx->gT.npts() * max_blocks;
+    const size_t bytesI = sizeof(double) * nc * ctx->nint * max_blocks;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(WG_ECUDA, "cudaStreamCreate failed");
+    if (sync_init() != cudaSuccess || wavelet_init() != cudaSuccess) {
+        cudaStreamDestroy(ctx->stream);
+        return fail(WG_ECUDA, "constant-memory set-up failed");
+    }
+    auto alloc = [&](double **p, size_t n) { return cudaMalloc(p, n) == cudaSuccess; };
+    if (!alloc(&ctx->A, bytesA) || !alloc(&ctx->B, bytesT) || !alloc(&ctx->C, bytesT) || !alloc(&ctx->acc, bytesI)) {
+        cudaGetLastError();
+        wg_ctx_destroy(ctx.release());
+        return fail(WG_ENOMEM, "device allocation of %d blocks failed", max_blocks);
+    }
+    if (cudaMalloc(&ctx->d_desc, sizeof(BlockDesc) * max_blocks) != cudaSuccess ||
+        cudaMalloc(&ctx->d_tp, sizeof(TreeParams) * ctx->max_trees) != cudaSuccess ||
+        cudaMalloc(&ctx->d_clk, sizeof(TreeClock) * ctx->max_trees) != cudaSuccess) {
+        cudaGetLastError();
+        wg_ctx_destroy(ctx.release());
+        return fail(WG_ENOMEM, "device allocation of descriptors failed");
+    }
+    cudaMemsetAsync(ctx->A, 0, bytesA, ctx->stream);
+    cudaMemsetAsync(ctx->B, 0, bytesT, ctx->stream);
+    cudaMemsetAsync(ctx->C, 0, bytesT, ctx->stream);
+    cudaMemsetAsync(ctx->d_clk, 0, sizeof(TreeClock) * ctx->max_trees, ctx->stream);
+    ctx->h_desc.resize(max_blocks);
+    ctx->free_slots.reserve(max_blocks);
+    for (int i = max_blocks - 1; i >= 0; i--) ctx->free_slots.push_back(i);
+    ctx->trees.resize(ctx->max_trees);
+    std::vector<int> ids(ctx->max_trees);
+    for (int i = 0; i < ctx->max_trees; i++) ids[i] = i;
+    if (ctx->d_tree_ids.upload(ids.data(), ids.size(), ctx->stream) != cudaSuccess)
+        return fail(WG_ECUDA, "upload failed");
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return fail(WG_ECUDA, "stream sync failed");
+    *out = ctx.release();
+    return WG_OK;
+}
+
+int wg_ctx_destroy(wg_ctx *ctx) {
+    if (!ctx) return WG_OK;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->trees.clear();
+    cudaFree(ctx->A);
+    cudaFree(ctx->B);
+    cudaFree(ctx->C);
+    cudaFree(ctx->acc);
+    cudaFree(ctx->mask);
+    cudaFree(ctx->d_desc);
+    cudaFree(ctx->d_tp);
+    cudaFree(ctx->d_clk);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return WG_OK;
+}
+
+int wg_set_variant(wg_ctx *ctx, int fast) {
+    if (!ctx) return fail(WG_EINVAL, "null ctx");
+    ctx->variant_fast = fast ? 1 : 0;
+    return WG_OK;
+}
+
+int wg_tree_create(wg_ctx *ctx, const wg_config *cfg, int *tree) {
+    if (!ctx || !tree) return fail(WG_EINVAL, "null argument");
+    const wg_config *c = cfg ? cfg : &ctx->cfg;
+    if (c->dim != ctx->cfg.dim || c->g != ctx->cfg.g || c->g_rhs != ctx->cfg.g_rhs || c->neq != ctx->cfg.neq ||
+        std::memcmp(c->Bs, ctx->cfg.Bs, sizeof(c->Bs)) || std::strcmp(c->wavelet, ctx->cfg.wavelet))
+        return fail(WG_EINVAL, "tree geometry differs from the context's");
+    for (int i = 0; i < (int)ctx->trees.size(); i++) {
+        if (ctx->trees[i].live) continue;
+        Tree &t = ctx->trees[i];
+        t = Tree();
+        t.live = true;
+        t.cfg = *c;
+        t.tp = make_params(*c);
+        t.forest.dim = c->dim;
+        t.forest.Jmin = c->Jmin;
+        t.forest.Jmax = c->Jmax;
+        WG_CUDA_OK(cudaMemcpyAsync(ctx->d_tp + i, &t.tp, sizeof(TreeParams), cudaMemcpyHostToDevice, ctx->stream));
+        TreeClock clk;
+        std::memset(&clk, 0, sizeof(clk));
+        WG_CUDA_OK(cudaMemcpyAsync(ctx->d_clk + i, &clk, sizeof(clk), cudaMemcpyHostToDevice, ctx->stream));
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        *tree = i;
+        ctx->grid_version++;
+        return WG_OK;
+    }
+    return fail(WG_ENOMEM, "too many trees (max %d)", (int)ctx->trees.size());
+}
+
+int wg_tree_destroy(wg_ctx *ctx, int tree) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    cudaStreamSynchronize(ctx->stream);
+    release_tree_blocks(ctx, *t);
+    *t = Tree();
+    ctx->grid_version++;
+    return WG_OK;
+}
+
+int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *coords) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    if (nblk < 0 || (nblk && (!level || !coords))) return fail(WG_EINVAL, "bad grid arguments");
+    cudaStreamSynchronize(ctx->stream);
+    release_tree_blocks(ctx, *t);
+    if ((size_t)nblk > ctx->free_slots.size())
+        return fail(WG_ENOMEM, "grid of %d blocks does not fit (%zu free slots)", nblk, ctx->free_slots.size());
+    t->forest.set(nblk, level, coords);
+    std::string err;
+    if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "%s", err.c_str());
+    if (!t->forest.graded()) return fail(WG_EGRID, "grid is not graded (level jump > 1 between neighbours)");
+    t->slots.resize(nblk);
+    t->mask_slot.assign(nblk, -1);
+    for (int b = 0; b < nblk; b++) {
+        t->slots[b] = ctx->free_slots.back();
+        ctx->free_slots.pop_back();
+    }
+    int st;
+    if ((st = upload_desc(ctx, *t, tree))) return st;
+    if ((st = upload_lists(ctx, *t))) return st;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    ctx->grid_version++;
+    return WG_OK;
+}
+
+int wg_get_nblocks(wg_ctx *ctx, int tree, int *nblk) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !nblk) return WG_EINVAL;
+    *nblk = t->forest.size();
+    return WG_OK;
+}
+
+int wg_get_grid(wg_ctx *ctx, int tree, int cap, int *level, int *coords) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    const int n = t->forest.size();
+    if (cap < n) return fail(WG_EINVAL, "capacity %d < %d blocks", cap, n);
+    std::memcpy(level, t->forest.level.data(), sizeof(int) * n);
+    std::memcpy(coords, t->forest.coords.data(), sizeof(int) * 3 * n);
+    return WG_OK;
+}
+
+// host_blocks: nblk * neq * npts doubles in the reference block layout
+int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !host_blocks) return fail(WG_EINVAL, "bad arguments");
+    const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
+    for (size_t b = 0; b < t->slots.size(); b++)
+        WG_CUDA_OK(cudaMemcpyAsync((char *)ctx->A + per * t->slots[b], (const char *)host_blocks + per * b, per,
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+int wg_download_state(wg_ctx *ctx, int tree, double *host_blocks) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !host_blocks) return fail(WG_EINVAL, "bad arguments");
+    const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
+    for (size_t b = 0; b < t->slots.size(); b++)
+        WG_CUDA_OK(cudaMemcpyAsync((char *)host_blocks + per * b, (const char *)ctx->A + per * t->slots[b], per,
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+// host_mask: nblk * 6 * npts (reference layout hvy_mask) or NULL to drop
+// the mask. Blocks whose mask is zero everywhere get no device mask slot.
+int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    cudaStreamSynchronize(ctx->stream);
+    for (int &m : t->mask_slot) {
+        if (m >= 0) ctx->mask_free.push_back(m);
+        m = -1;
+    }
+    const int nb = t->forest.size();
+    const long long np = ctx->gA.npts();
+    const long long ni = ctx->nint;
+    const int g = ctx->cfg.g, dim = ctx->cfg.dim;
+    const int *Bs = ctx->cfg.Bs;
+    std::vector<double> packed;
+    std::vector<int> need;
+    if (host_mask) {
+        for (int b = 0; b < nb; b++) {
+            const double *m = host_mask + (size_t)b * 6 * np;
+            bool any = false;
+            std::vector<double> blk(6 * ni);
+            for (int c = 0; c < 6; c++)
+                for (int iz = 0; iz < (dim == 3 ? Bs[2] : 1); iz++)
+                    for (int iy = 0; iy < Bs[1]; iy++)
+                        for (int ix = 0; ix < Bs[0]; ix++) {
+                            const long long src = ((long long)(iz + (dim == 3 ? g : 0)) * ctx->gA.ny + iy + g) * ctx->gA.nx + ix + g;
+                            const double v = m[c * np + src];
+                            blk[c * ni + ((long long)iz * Bs[1] + iy) * Bs[0] + ix] = v;
+                            if (v != 0.0 && c != 4) any = true;
+                        }
+            if (any) {
+                need.push_back(b);
+                packed.insert(packed.end(), blk.begin(), blk.end());
+            }
+        }
+    }
+    // grow the pool if needed
+    int in_use = ctx->mask_cap - (int)ctx->mask_free.size();
+    int want = in_use + (int)need.size();
+    if (want > ctx->mask_cap) {
+        int ncap = std::max(want, ctx->mask_cap * 2);
+        double *nm = nullptr;
+        if (cudaMalloc(&nm, sizeof(double) * 6 * ni * (size_t)ncap) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(WG_ENOMEM, "mask pool of %d blocks does not fit", ncap);
+        }
+        if (ctx->mask) {
+            cudaMemcpyAsync(nm, ctx->mask, sizeof(double) * 6 * ni * (size_t)ctx->mask_cap, cudaMemcpyDeviceToDevice,
+                            ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->mask);
+        }
+        for (int i = ncap - 1; i >= ctx->mask_cap; i--) ctx->mask_free.push_back(i);
+        ctx->mask = nm;
+        ctx->mask_cap = ncap;
+    }
+    for (size_t k = 0; k < need.size(); k++) {
+        int slot = ctx->mask_free.back();
+        ctx->mask_free.pop_back();
+        t->mask_slot[need[k]] = slot;
+        WG_CUDA_OK(cudaMemcpyAsync(ctx->mask + (size_t)slot * 6 * ni, packed.data() + k * 6 * ni,
+                                   sizeof(double) * 6 * ni, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    int st;
+    if ((st = upload_desc(ctx, *t, tree))) return st;
+    if ((st = upload_lists(ctx, *t))) return st;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    ctx->grid_version++;
+    return WG_OK;
+}
+
+int wg_set_time(wg_ctx *ctx, int tree, double time) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    TreeClock c;
+    std::memset(&c, 0, sizeof(c));
+    c.time = time;
+    WG_CUDA_OK(cudaMemcpyAsync(ctx->d_clk + tree, &c, sizeof(c), cudaMemcpyHostToDevice, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    TreeClock c;
+    int st = read_clock(ctx, tree, &c);
+    if (st) return st;
+    if (time) *time = c.time;
+    if (dt) *dt = c.dt;
+    return c.diverged ? fail(WG_EDIVERGED, "ACM fail: very very large values in state vector") : WG_OK;
+}
+
+// sync_ghosts_RHS_tree / sync_ghosts_tree on the state (no HD filter)
+int wg_sync_ghosts(wg_ctx *ctx, int tree, int gminus, int gplus) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    if (gminus < 1 || gplus < 1 || gminus > ctx->cfg.g || gplus > ctx->cfg.g)
+        return fail(WG_EINVAL, "ghost widths must be in 1..g");
+    int st = run_sync(ctx, *t, ctx->A, false, gminus, gplus);
+    if (st) return st;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+// RHS_ACM local stage of every block on the current (synchronised) state;
+// host_rhs receives nblk*neq*npts doubles (reference layout, interior set)
+int wg_rhs(wg_ctx *ctx, int tree, double *host_rhs) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !host_rhs) return fail(WG_EINVAL, "bad arguments");
+    const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
+    double *d = nullptr;
+    WG_CUDA_OK(cudaMallocAsync(&d, per * ctx->max_blocks, ctx->stream));
+    cudaMemsetAsync(d, 0, per * ctx->max_blocks, ctx->stream);
+    const int base = (ctx->variant_fast ? 1 : 0) | (t->cfg.skew_symmetry ? 2 : 0);
+    const int *Bs = ctx->cfg.Bs;
+    cudaError_t e = launch_rhs_only(base, ctx->cfg.dim, t->d_plain.p, t->n_plain, ctx->d_desc, ctx->d_tp, ctx->A,
+                                    ctx->gA, d, ctx->mask, Bs[0], Bs[1], Bs[2], ctx->geo.nc, ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_rhs_only(base | 4, ctx->cfg.dim, t->d_masked.p, t->n_masked, ctx->d_desc, ctx->d_tp, ctx->A,
+                            ctx->gA, d, ctx->mask, Bs[0], Bs[1], Bs[2], ctx->geo.nc, ctx->stream);
+    for (size_t b = 0; e == cudaSuccess && b < t->slots.size(); b++)
+        e = cudaMemcpyAsync((char *)host_rhs + per * b, (const char *)d + per * t->slots[b], per,
+                            cudaMemcpyDeviceToHost, ctx->stream);
+    cudaFreeAsync(d, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "wg_rhs", __FILE__, __LINE__);
+    return WG_OK;
+}
+
+// calculate_time_step at the tree's current time (state must be synced)
+int wg_compute_dt(wg_ctx *ctx, int tree, double *dt) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    const int *Bs = ctx->cfg.Bs;
+    WG_CUDA_OK(launch_dt(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
+                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, ctx->stream));
+    TreeClock c;
+    int st = read_clock(ctx, tree, &c);
+    if (st) return st;
+    if (dt) *dt = c.dt;
+    return WG_OK;
+}
+
+// timeStep_tree: one RK4 step (sync, dt, four stages); time and dt are
+// returned when the pointers are non-NULL (which synchronises)
+int wg_rk4_step(wg_ctx *ctx, int tree, double *time, double *dt) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    int st = rk4_enqueue(ctx, tree);
+    if (st) return st;
+    if (time || dt) return wg_get_time(ctx, tree, time, dt);
+    return WG_OK;
+}
+
+// nsteps RK4 steps of each listed tree without host synchronisation; with
+// use_graph the per-step launch sequence is captured once and replayed
+int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph) {
+    if (!ctx || ntrees <= 0 || !trees || nsteps < 0) return fail(WG_EINVAL, "bad arguments");
+    for (int i = 0; i < ntrees; i++)
+        if (!get_tree(ctx, trees[i])) return WG_EINVAL;
+    if (!use_graph) {
+        for (int s = 0; s < nsteps; s++)
+            for (int i = 0; i < ntrees; i++) {
+                int st = rk4_enqueue(ctx, trees[i]);
+                if (st) return st;
+            }
+        return WG_OK;
+    }
+    const bool same = ctx->graph_exec && ctx->graph_version == ctx->grid_version &&
+                      ctx->graph_trees == std::vector<int>(trees, trees + ntrees);
+    if (!same) {
+        // tables are built (and uploaded) before capture
+        for (int i = 0; i < ntrees; i++) {
+            Tree &t = ctx->trees[trees[i]];
+            SyncPlan *sp;
+            int st;
+            if ((st = get_sync(ctx, t, ctx->cfg.g_rhs, ctx->cfg.g_rhs, false, &sp))) return st;
+            if ((st = get_sync(ctx, t, ctx->cfg.g_rhs, ctx->cfg.g_rhs, true, &sp))) return st;
+        }
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+        if (ctx->graph) cudaGraphDestroy(ctx->graph);
+        ctx->graph_exec = nullptr;
+        ctx->graph = nullptr;
+        WG_CUDA_OK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int st = WG_OK;
+        for (int i = 0; i < ntrees && !st; i++) st = rk4_enqueue(ctx, trees[i]);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (st) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __FILE__, __LINE__);
+        ctx->graph = g;
+        WG_CUDA_OK(cudaGraphInstantiate(&ctx->graph_exec, g, 0));
+        ctx->graph_trees.assign(trees, trees + ntrees);
+        ctx->graph_version = ctx->grid_version;
+    }
+    for (int s = 0; s < nsteps; s++) WG_CUDA_OK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    return WG_OK;
+}
+
+int wg_synchronize(wg_ctx *ctx) {
+    if (!ctx) return fail(WG_EINVAL, "null ctx");
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+// the context's stream, for callers that time or order work around it
+void *wg_stream(wg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+// coarseningIndicator for every block of the tree on the current state
+// (ghosts synchronised with g points first): flags[b] = -1 (may coarsen) or
+// 0; details (nblk*neq, may be NULL) receives the per-component details
+int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !eps_use || !flags) return fail(WG_EINVAL, "bad arguments");
+    const int nb = t->forest.size();
+    const int nc = ctx->geo.nc;
+    double *d_eps = nullptr, *d_det = nullptr;
+    int *d_tsvc = nullptr, *d_flags = nullptr;
+    cudaError_t e = cudaMallocAsync(&d_eps, sizeof(double) * nc, ctx->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_tsvc, sizeof(int) * nc, ctx->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_flags, sizeof(int) * (nb + 1), ctx->stream);
+    if (e == cudaSuccess) e = cudaMallocAsync(&d_det, sizeof(double) * (nb + 1) * nc, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_eps, eps_use, sizeof(double) * nc, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_tsvc, t->cfg.threshold_state_vector_component, sizeof(int) * nc, cudaMemcpyHostToDevice,
+                            ctx->stream);
+    const int *Bs = ctx->cfg.Bs;
+    if (e == cudaSuccess)
+        e = launch_fwt_flags(ctx->cfg.dim, t->d_all.p, nb, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], nc, ctx->wav.X,
+                             ctx->wav.Y, d_eps, d_tsvc, d_flags, d_det, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(flags, d_flags, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && details)
+        e = cudaMemcpyAsync(details, d_det, sizeof(double) * nb * nc, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaFreeAsync(d_eps, ctx->stream);
+    cudaFreeAsync(d_tsvc, ctx->stream);
+    cudaFreeAsync(d_flags, ctx->stream);
+    cudaFreeAsync(d_det, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "wg_threshold_flags", __FILE__, __LINE__);
+    return WG_OK;
+}
+
+// refine_tree(..., "everywhere") data part: every block is replaced by its
+// 2^d daughters (refineBlock); ghosts must be synchronised with g points.
+// Daughters of block b are blocks 2^d*b .. 2^d*b+2^d-1 of the new grid.
+int wg_refine_everywhere(wg_ctx *ctx, int tree) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    const int dim = ctx->cfg.dim, nd = 1 << dim;
+    const int nb = t->forest.size();
+    if ((size_t)nb * nd > ctx->free_slots.size()) return fail(WG_ENOMEM, "refinement needs %d free slots", nb * nd);
+    for (int b = 0; b < nb; b++)
+        if (t->forest.level[b] + 1 > t->cfg.Jmax) return fail(WG_EINVAL, "refinement beyond Jmax");
+    std::vector<int> lv(nb * nd), co(3 * nb * nd), slots(nb * nd), child_base(nb), parents(t->slots);
+    // daughters need consecutive slots: take them from the free list in runs
+    std::vector<int> fs = ctx->free_slots;
+    std::sort(fs.begin(), fs.end());
+    // consecutive run search
+    std::vector<int> used;
+    size_t i = 0;
+    for (int b = 0; b < nb; b++) {
+        while (i + nd <= fs.size() && fs[i + nd - 1] - fs[i] != nd - 1) i++;
+        if (i + nd > fs.size()) return fail(WG_ENOMEM, "no consecutive free slots for daughters");
+        child_base[b] = fs[i];
+        for (int k = 0; k < nd; k++) used.push_back(fs[i + k]);
+        i += nd;
+    }
+    for (int b = 0; b < nb; b++)
+        for (int k = 0; k < nd; k++) {
+            const int c = b * nd + k;
+            lv[c] = t->forest.level[b] + 1;
+            co[3 * c + 0] = 2 * t->forest.coords[3 * b + 0] + (k / 2) % 2;
+            co[3 * c + 1] = 2 * t->forest.coords[3 * b + 1] + k % 2;
+            co[3 * c + 2] = dim == 3 ? 2 * t->forest.coords[3 * b + 2] + k / 4 : 0;
+            slots[c] = child_base[b] + k;
+        }
+    DevArray<int> d_par, d_base;
+    WG_CUDA_OK(d_par.upload(parents.data(), nb, ctx->stream));
+    WG_CUDA_OK(d_base.upload(child_base.data(), nb, ctx->stream));
+    const int *Bs = ctx->cfg.Bs;
+    WG_CUDA_OK(launch_refine(dim, d_par.p, nb, d_base.p, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], ctx->geo.nc,
+                             ctx->wav.order_predictor, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    // swap the tree onto the daughters
+    std::sort(used.begin(), used.end());
+    std::vector<int> nf;
+    nf.reserve(ctx->free_slots.size());
+    for (int s : ctx->free_slots)
+        if (!std::binary_search(used.begin(), used.end(), s)) nf.push_back(s);
+    for (int s : parents) nf.push_back(s);
+    for (int m : t->mask_slot)
+        if (m >= 0) ctx->mask_free.push_back(m);
+    ctx->free_slots = nf;
+    t->slots = slots;
+    t->mask_slot.assign(nb * nd, -1);
+    t->sync.clear();
+    t->forest.set(nb * nd, lv.data(), co.data());
+    std::string err;
+    if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "%s", err.c_str());
+    int st;
+    if ((st = upload_desc(ctx, *t, tree))) return st;
+    if ((st = upload_lists(ctx, *t))) return st;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    ctx->grid_version++;
+    return WG_OK;
+}
+
+// patch table of the tree's ghost sync for inspection: returns the number of
+// patches; if out != NULL, writes 19 ints per patch
+// (src, dst, op, stage, rlo[3], rhi[3], slo[3], shi[3], blo[3])
+int wg_sync_table(wg_ctx *ctx, int tree, int gminus, int gplus, int thin, int cap, int *out) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    SyncPlan *sp;
+    int st = get_sync(ctx, *t, gminus, gplus, thin != 0, &sp);
+    if (st) return st;
+    const int n = (int)sp->table.patches.size();
+    if (out) {
+        if (cap < n) return fail(WG_EINVAL, "capacity too small");
+        for (int i = 0; i < n; i++) {
+            const Patch &p = sp->table.patches[i];
+            int *o = out + 19 * i;
+            o[0] = p.src;
+            o[1] = p.dst;
+            o[2] = p.op;
+            o[3] = p.stage;
+            for (int k = 0; k < 3; k++) {
+                o[4 + k] = p.rlo[k];
+                o[7 + k] = p.rhi[k];
+                o[10 + k] = p.slo[k];
+                o[13 + k] = p.shi[k];
+                o[16 + k] = p.blo[k];
+            }
+        }
+    }
+    return n;
+}
+
+// block slot of block b of a tree (for tests that inspect the arena)
+int wg_block_slot(wg_ctx *ctx, int tree, int b) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || b < 0 || b >= (int)t->slots.size()) return fail(WG_EINVAL, "bad block");
+    return t->slots[b];
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// Host-only ghost-patch table of a grid (no device needed): the same table
+// wg_sync_table returns, with block indices instead of arena slots.
+int wg_sync_table_host(const wg_config *cfg, int nblk, const int *level, const int *coords, int gminus, int gplus,
+                       int thin, int cap, int *out) {
+    int st = check_cfg(cfg);
+    if (st) return st;
+    Forest f;
+    f.dim = cfg->dim;
+    f.Jmin = cfg->Jmin;
+    f.Jmax = cfg->Jmax;
+    f.set(nblk, level, coords);
+    std::string err;
+    if (!f.update_neighbors(err)) return fail(WG_EGRID, "%s", err.c_str());
+    Geometry geo;
+    geo.dim = cfg->dim;
+    for (int d = 0; d < 3; d++) geo.Bs[d] = d < cfg->dim ? cfg->Bs[d] : 1;
+    geo.g = cfg->g;
+    geo.nc = cfg->neq;
+    WaveletInfo w;
+    make_wavelet(cfg->wavelet, w);
+    SyncTable t;
+    if (!make_sync_table(f, geo, w, gminus, gplus, thin ? cfg->g_rhs : cfg->g, 0, t, err))
+        return fail(WG_EGRID, "sync table: %s", err.c_str());
+    const int n = (int)t.patches.size();
+    if (out) {
+        if (cap < n) return fail(WG_EINVAL, "capacity too small");
+        for (int i = 0; i < n; i++) {
+            const Patch &p = t.patches[i];
+            int *o = out + 19 * i;
+            o[0] = p.src;
+            o[1] = p.dst;
+            o[2] = p.op;
+            o[3] = p.stage;
+            for (int k = 0; k < 3; k++) {
+                o[4 + k] = p.rlo[k];
+                o[7 + k] = p.rhi[k];
+                o[10 + k] = p.slo[k];
+                o[13 + k] = p.shi[k];
+                o[16 + k] = p.blo[k];
+            }
+        }
+    }
+    return n;
+}
+
+}  // extern "C"

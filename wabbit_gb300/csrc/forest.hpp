@@ -1,0 +1,89 @@
+// forest.hpp -- host-side tree bookkeeping of the GB300 hot path.
+//
+// The reference keeps the block tree as light data (lgt_block: level,
+// treecode) and recomputes neighbour relations and ghost-patch index boxes on
+// every synchronisation (LIB/MESH/find_neighbors.f90, LIB/TREE/neighborhood.f90,
+// LIB/MPI/calc_data_bounds.f90, synchronize_ghosts_generic.f90:352-694). Here
+// that integer work runs once per grid change and is flattened into patch
+// tables that the device sync kernel consumes; the heavy data never leaves HBM.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace wg {
+
+// neighbour-relation numbering of the reference (find_neighbors.f90:1-16):
+//   1- 56 same level, 57-112 coarser neighbour, 113-168 finer neighbour
+constexpr int kNumRelations = 168;
+
+struct WaveletInfo {
+    int X = 4, Y = 0;            // CDF X,Y
+    bool lifted = false;
+    int order_predictor = 4;     // 2,4,6,8
+    int g_min = 3;               // minimal ghost width
+    std::vector<double> HD, GD, HR, GR;  // coefficient arrays
+    int hd_lo = 0, gd_lo = 0, hr_lo = 0, gr_lo = 0;
+};
+bool make_wavelet(const char *name, WaveletInfo &w);
+
+struct Geometry {
+    int dim = 2;
+    int Bs[3] = {16, 16, 1};
+    int g = 4;                   // ghost width of the full-state layout
+    int nc = 3;
+    int n(int d) const { return d < dim ? Bs[d] + 2 * g : 1; }
+};
+
+class Forest {
+public:
+    int dim = 2, Jmin = 1, Jmax = 1;
+    std::vector<int> level;      // per block
+    std::vector<int> coords;     // 3 per block
+    std::vector<int> nbr;        // kNumRelations per block, -1 = none
+
+    int size() const { return (int)level.size(); }
+    void set(int nblk, const int *lv, const int *co);
+    int find(int lv, int x, int y, int z) const;
+    // neighbour search for all blocks; returns false and a message for an
+    // invalid grid (a face without any neighbour, overlapping blocks, ...)
+    bool update_neighbors(std::string &err);
+    // maximum level difference across any face/edge/corner is 1
+    bool graded() const;
+    uint64_t treecode(int b) const;  // reference bit layout (y bit0, x bit1, z bit2)
+
+private:
+    std::unordered_map<uint64_t, int> lookup_;
+};
+
+// One ghost patch: fill box [rlo,rhi] (0-based, inclusive) of block dst from
+// block src. op: 0 copy, 1 restriction (every 2nd point), 2 prediction.
+//   copy:     src index = slo + (r - rlo)
+//   restrict: src index = slo + 2*(blo + r - rlo)
+//   predict:  fine index f = blo + (r - rlo) into the (2n-1)-point fine array
+//             interpolated from the coarse box [slo,shi] of src
+struct Patch {
+    int32_t src, dst;
+    int16_t op, stage;
+    int16_t rlo[3], rhi[3];
+    int16_t slo[3], shi[3];
+    int16_t blo[3], pad;
+};
+static_assert(sizeof(Patch) == 44, "patch layout");
+
+struct SyncTable {
+    int nstages = 2;
+    std::vector<Patch> patches;        // sorted by stage
+    std::vector<int> stage_begin;      // nstages+1 offsets
+    int max_points = 0;                // largest receiver box
+};
+
+// Build the ghost-sync table of one forest for the reference's
+// sync_ghosts_RHS_tree / sync_ghosts_tree semantics on a leaf-only grid.
+// Boxes are expressed for a buffer with ghost width g_buf (<= geo.g): an
+// index i of the full layout maps to i - (geo.g - g_buf).
+bool make_sync_table(const Forest &f, const Geometry &geo, const WaveletInfo &w, int gminus, int gplus,
+                     int g_buf, int block_offset, SyncTable &out, std::string &err);
+
+}  // namespace wg

@@ -1,0 +1,166 @@
+// k_misc.cu -- time-step selection and stage dispatch.
+//
+// dt: GET_DT_BLOCK_ACM (LIB/EQUATION/ACMnew/module_ACM.f90:617-691) per block,
+// min over the blocks of each tree (the reference's MPI_Allreduce(MIN),
+// LIB/TIME/calculate_time_step.f90:28-48), then the output-time trimming of
+// calculate_time_step.f90:50-118 -- all on the device, so that a whole RK4
+// step can be captured in a CUDA graph.
+#include "common.cuh"
+
+namespace wg {
+
+// per-block max |u|^2 over the interior -> per-block dt -> atomic min per tree
+template <int DIM>
+__global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc *desc, const TreeParams *tp,
+                                                 TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1,
+                                                 int Bs2) {
+    const int b = blk[blockIdx.x];
+    const BlockDesc d = desc[b];
+    const long long np = geo.npts();
+    const int nint = Bs0 * Bs1 * (DIM == 3 ? Bs2 : 1);
+    const double *ub = u + (long long)b * (DIM + 1) * np;
+    double m = -1.0;
+    for (int q = threadIdx.x; q < nint; q += blockDim.x) {
+        const int ix = q % Bs0, iy = (q / Bs0) % Bs1, iz = DIM == 3 ? q / (Bs0 * Bs1) : 0;
+        const long long o = ((long long)(iz + (DIM == 3 ? geo.gb : 0)) * geo.ny + (iy + geo.gb)) * geo.nx + (ix + geo.gb);
+        const double a = ub[o], bb = ub[np + o];
+        double s = __dadd_rn(__dmul_rn(a, a), __dmul_rn(bb, bb));
+        if (DIM == 3) {
+            const double c = ub[2 * np + o];
+            s = __dadd_rn(s, __dmul_rn(c, c));
+        }
+        m = fmax(m, s);
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const TreeParams &p = tp[d.tree];
+        const double u_mag = red[0];
+        const double u_eigen = __dadd_rn(sqrt(u_mag), sqrt(__dadd_rn(__dmul_rn(p.c0, p.c0), u_mag)));
+        double dxmin = d.dx[0];
+        for (int k = 1; k < DIM; k++) dxmin = fmin(dxmin, d.dx[k]);
+        double dt = u_eigen >= 1.0e-6 ? __ddiv_rn(__dmul_rn(p.CFL, dxmin), u_eigen) : 1.0e-2;
+        if (p.nu > 1.0e-13) dt = fmin(dt, __ddiv_rn(__dmul_rn(p.CFL_nu, __dmul_rn(dxmin, dxmin)), p.nu));
+        if (p.gamma_p > 0) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.gamma_p));
+        if (p.penalization) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.C_eta));
+        if (p.use_sponge) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.C_sponge));
+        atomicMin(&clk[d.tree].dt_min_bits, (unsigned long long)__double_as_longlong(dt));
+    }
+}
+
+__global__ void dt_reset_kernel(TreeClock *clk, const int *trees, int ntrees) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ntrees) clk[trees[i]].dt_min_bits = (unsigned long long)__double_as_longlong(9.0e9);
+}
+
+// calculate_time_step.f90:28-118 after the MIN reduction
+__global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const int *trees, int ntrees) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntrees) return;
+    const int t = trees[i];
+    const TreeParams &p = tp[t];
+    TreeClock &c = clk[t];
+    const double time = c.time;
+    double dt;
+    if (p.dt_fixed > 0.0) dt = p.dt_fixed;
+    else {
+        dt = __longlong_as_double((long long)c.dt_min_bits);
+        if (p.dt_max > 0.0) dt = fmin(p.dt_max, dt);
+    }
+    if (p.write_time > 0.0) {
+        const double wt = p.write_time;
+        if (fmod(__dadd_rn(time, dt), wt) < fmod(__dadd_rn(time, 1e-12), wt) && !(fabs(fmod(time, wt)) < 1e-12) &&
+            __dadd_rn(time, 1e-12) > 0.0)
+            dt = __dsub_rn(wt, fmod(time, wt));
+    }
+    if (p.tsave_stats > 0.0) {
+        const double ts = p.tsave_stats;
+        if (fmod(__dadd_rn(time, dt), ts) < fmod(__dadd_rn(time, 1e-12), ts) && !(fabs(fmod(time, ts)) < 1e-12))
+            dt = __dsub_rn(ts, fmod(time, ts));
+    }
+    if (__dadd_rn(time, dt) > p.time_max && time <= p.time_max) dt = __dsub_rn(p.time_max, time);
+    c.dt = dt;
+}
+
+__global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntrees) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ntrees) {
+        TreeClock &c = clk[trees[i]];
+        c.time = __dadd_rn(c.time, c.dt);
+    }
+}
+
+cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
+                      TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
+                      const int *trees, cudaStream_t s) {
+    dt_reset_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
+    if (nblk > 0) {
+        if (dim == 2) dt_kernel<2><<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2);
+        else dt_kernel<3><<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2);
+    }
+    dt_finalize_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(tp, clk, trees, ntrees);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s) {
+    clock_advance_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
+    return cudaGetLastError();
+}
+
+static StageArgs make_args(const int *blk, const BlockDesc *desc, const TreeParams *tp,
+                                   const TreeClock *clk, const double *in, BufGeo gin, double *out, BufGeo gout,
+                                   double *un, BufGeo gun, double *acc, const double *mask, int Bs0, int Bs1,
+                                   int Bs2, int nc, int stage, int rhs_only) {
+    StageArgs a;
+    a.blk = blk;
+    a.desc = desc;
+    a.tp = tp;
+    a.clk = clk;
+    a.in = in;
+    a.gin = gin;
+    a.out = out;
+    a.gout = gout;
+    a.un = un;
+    a.gun = gun;
+    a.acc = acc;
+    a.mask = mask;
+    a.Bs0 = Bs0;
+    a.Bs1 = Bs1;
+    a.Bs2 = Bs2;
+    a.nc = nc;
+    a.stage = stage;
+    a.chunks = 1;
+    a.rhs_only = rhs_only;
+    return a;
+}
+
+// variant bit 0: 1 = fast (FMA); bit 1: skew-symmetric; bit 2: masked block list
+cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, int nblk, const BlockDesc *desc,
+                             const TreeParams *tp, const TreeClock *clk, const double *in, BufGeo gin,
+                             double *out, BufGeo gout, double *un, BufGeo gun, double *acc, const double *mask,
+                             int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    StageArgs a = make_args(blk, desc, tp, clk, in, gin, out, gout, un, gun, acc, mask, Bs0, Bs1, Bs2, nc,
+                                    stage, 0);
+    const bool skew = variant & 2, masked = variant & 4;
+    if (variant & 1) return fast::stage(dim, a, nblk, skew, masked, s);
+    return strict::stage(dim, a, nblk, skew, masked, s);
+}
+
+cudaError_t launch_rhs_only(int variant, int dim, const int *blk, int nblk, const BlockDesc *desc,
+                            const TreeParams *tp, const double *in, BufGeo gin, double *rhs, const double *mask,
+                            int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    StageArgs a = make_args(blk, desc, tp, nullptr, in, gin, rhs, gin, nullptr, gin, nullptr, mask, Bs0, Bs1,
+                                    Bs2, nc, 1, 1);
+    const bool skew = variant & 2, masked = variant & 4;
+    if (variant & 1) return fast::stage(dim, a, nblk, skew, masked, s);
+    return strict::stage(dim, a, nblk, skew, masked, s);
+}
+
+}  // namespace wg

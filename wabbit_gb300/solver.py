@@ -1,0 +1,181 @@
+"""Host-side mirror of the reference's tree-level interface for the hot path.
+
+The reference drives the time loop from Fortran (LIB/MAIN/main.f90:293-501)
+through tree-level routines: sync_ghosts_RHS_tree, calculate_time_step,
+timeStep_tree (-> RungeKuttaGeneric), coarseningIndicator_tree and
+refine_tree. ``Forest`` exposes the same operations, backed by the CUDA
+library; state lives on the device between calls.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+from .config import WgConfig
+
+
+def _p(a, t=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+class Context:
+    """A device arena for one block geometry (the reference's allocate_forest)."""
+
+    def __init__(self, cfg: WgConfig, max_blocks: int):
+        self.L = capi.load()
+        self.cfg = cfg.copy()
+        h = ctypes.c_void_p()
+        capi.check(self.L.wg_ctx_create(ctypes.byref(self.cfg), int(max_blocks), ctypes.byref(h)))
+        self.h = h
+        self.max_blocks = int(max_blocks)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.wg_ctx_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_variant(self, fast: bool):
+        capi.check(self.L.wg_set_variant(self.h, 1 if fast else 0))
+
+    def synchronize(self):
+        capi.check(self.L.wg_synchronize(self.h))
+
+    def forest(self, cfg: WgConfig | None = None) -> "Forest":
+        return Forest(self, cfg)
+
+    def run(self, forests, nsteps: int, use_graph: bool = True):
+        ids = np.array([f.tree for f in forests], np.int32)
+        capi.check(self.L.wg_run(self.h, len(ids), _p(ids, ctypes.c_int), int(nsteps), 1 if use_graph else 0))
+
+    @property
+    def stream(self) -> int:
+        return self.L.wg_stream(self.h)
+
+
+class Forest:
+    """One tree (independent solve) inside a Context."""
+
+    def __init__(self, ctx: Context, cfg: WgConfig | None = None):
+        self.ctx = ctx
+        self.L = ctx.L
+        self.cfg = (cfg or ctx.cfg).copy()
+        t = ctypes.c_int()
+        capi.check(self.L.wg_tree_create(ctx.h, ctypes.byref(self.cfg), ctypes.byref(t)))
+        self.tree = t.value
+
+    def destroy(self):
+        if self.tree >= 0 and self.ctx.h:
+            capi.check(self.L.wg_tree_destroy(self.ctx.h, self.tree))
+        self.tree = -1
+
+    # ---------------------------------------------------------------- layout
+    @property
+    def block_shape(self):
+        c = self.cfg
+        return (c.neq, c.nz, c.Bs[1] + 2 * c.g, c.nx)
+
+    @property
+    def nblocks(self) -> int:
+        n = ctypes.c_int()
+        capi.check(self.L.wg_get_nblocks(self.ctx.h, self.tree, ctypes.byref(n)))
+        return n.value
+
+    def set_grid(self, level, coords):
+        level = np.ascontiguousarray(level, np.int32)
+        coords = np.ascontiguousarray(coords, np.int32).reshape(-1, 3)
+        capi.check(self.L.wg_set_grid(self.ctx.h, self.tree, len(level), _p(level, ctypes.c_int),
+                                      _p(coords, ctypes.c_int)))
+
+    def grid(self):
+        n = self.nblocks
+        lv = np.zeros(n, np.int32)
+        co = np.zeros((n, 3), np.int32)
+        capi.check(self.L.wg_get_grid(self.ctx.h, self.tree, n, _p(lv, ctypes.c_int), _p(co, ctypes.c_int)))
+        return lv, co
+
+    def upload(self, data):
+        data = np.ascontiguousarray(data, np.float64)
+        if data.size != self.nblocks * int(np.prod(self.block_shape)):
+            raise ValueError("state has the wrong size for this grid")
+        capi.check(self.L.wg_upload_state(self.ctx.h, self.tree, _p(data)))
+
+    def download(self):
+        out = np.zeros((self.nblocks,) + self.block_shape)
+        capi.check(self.L.wg_download_state(self.ctx.h, self.tree, _p(out)))
+        return out
+
+    def set_mask(self, mask):
+        if mask is None:
+            capi.check(self.L.wg_set_mask(self.ctx.h, self.tree, None))
+            return
+        mask = np.ascontiguousarray(mask, np.float64)
+        c = self.cfg
+        if mask.size != self.nblocks * 6 * c.npts:
+            raise ValueError("mask has the wrong size")
+        capi.check(self.L.wg_set_mask(self.ctx.h, self.tree, _p(mask)))
+
+    # ------------------------------------------------------------------ time
+    def set_time(self, t: float):
+        capi.check(self.L.wg_set_time(self.ctx.h, self.tree, float(t)))
+
+    def time(self):
+        t, d = ctypes.c_double(), ctypes.c_double()
+        capi.check(self.L.wg_get_time(self.ctx.h, self.tree, ctypes.byref(t), ctypes.byref(d)))
+        return t.value, d.value
+
+    # -------------------------------------------------------- reference ops
+    def sync_ghosts_RHS_tree(self, g_minus=None, g_plus=None):
+        gm = self.cfg.g_rhs if g_minus is None else g_minus
+        gp = gm if g_plus is None else g_plus
+        capi.check(self.L.wg_sync_ghosts(self.ctx.h, self.tree, gm, gp))
+
+    def sync_ghosts_tree(self):
+        """Full ghost sync with g layers (CDFX0 wavelets: no HD filter)."""
+        capi.check(self.L.wg_sync_ghosts(self.ctx.h, self.tree, self.cfg.g, self.cfg.g))
+
+    def RHS_ACM(self):
+        out = np.zeros((self.nblocks,) + self.block_shape)
+        capi.check(self.L.wg_rhs(self.ctx.h, self.tree, _p(out)))
+        return out
+
+    def calculate_time_step(self) -> float:
+        d = ctypes.c_double()
+        capi.check(self.L.wg_compute_dt(self.ctx.h, self.tree, ctypes.byref(d)))
+        return d.value
+
+    def timeStep_tree(self):
+        """One RK4 step; returns (time, dt) after the step."""
+        t, d = ctypes.c_double(), ctypes.c_double()
+        capi.check(self.L.wg_rk4_step(self.ctx.h, self.tree, ctypes.byref(t), ctypes.byref(d)))
+        return t.value, d.value
+
+    def run(self, nsteps: int, use_graph: bool = True):
+        self.ctx.run([self], nsteps, use_graph)
+
+    def coarseningIndicator(self, eps_use):
+        eps_use = np.ascontiguousarray(np.broadcast_to(np.asarray(eps_use, np.float64), (self.cfg.neq,)))
+        n = self.nblocks
+        flags = np.zeros(n, np.int32)
+        det = np.zeros((n, self.cfg.neq))
+        capi.check(self.L.wg_threshold_flags(self.ctx.h, self.tree, _p(eps_use), _p(flags, ctypes.c_int), _p(det)))
+        return flags, det
+
+    def refine_everywhere(self):
+        capi.check(self.L.wg_refine_everywhere(self.ctx.h, self.tree))
+
+    def sync_table(self, gminus, gplus, thin=False):
+        n = capi.check(self.L.wg_sync_table(self.ctx.h, self.tree, gminus, gplus, 1 if thin else 0, 0, None))
+        out = np.zeros((n, 19), np.int32)
+        capi.check(self.L.wg_sync_table(self.ctx.h, self.tree, gminus, gplus, 1 if thin else 0, n,
+                                        _p(out, ctypes.c_int)))
+        return out
