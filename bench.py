@@ -1,0 +1,411 @@
+#!/usr/bin/env python3
+"""Benchmark of the ACM block-level time stepper (point-updates/s).
+
+A step is one RK4 time step (timeStep_tree: ghost sync, dt, four RHS+RK
+stages) over every block of the workload grid. The default workload is the
+3-D ACM channel with a penalised sphere (Bs=16^3, g=6, CDF4,4, Jmax=6, FP64,
+~4.2k blocks; see wabbit_gb300/workloads.py).
+
+value: point-updates/s with the state resident in HBM, K steps replayed from
+       a captured CUDA graph, timed with CUDA events on the solver's stream.
+e2e:   the same through the C ABI with host buffers: every step uploads the
+       interior state from pinned host memory, runs wg_rk4_step (which reads
+       back time and dt) and downloads the interior state.
+roofline: the RK-stage kernel timed alone (CUDA events, mean over launches)
+       against the measured HBM copy bandwidth, plus its FP64 rate against
+       the FP64 FMA peak measured in the same run (the kernel is FP64-ALU
+       bound on GB300).
+cpu_baseline: the CPU oracle (a scalar C++ restatement of the reference's
+       Fortran, OpenMP over blocks) on a bounded sample of the same physics.
+
+--impl reference runs only the CPU oracle (the reference is Fortran and
+cannot be built here; the oracle reproduces its regression outputs bit for
+bit) on the same metric.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic cost of one RK stage per interior point (FP64, fused ideal):
+# read stage input, u_n and the accumulator, write accumulator and next stage
+# input: 5 state vectors of neq doubles; masked blocks also read 6 mask words
+WORDS_PER_POINT_STAGE = 5
+MASK_WORDS = 6
+# FP64 operations of the FD_4th_central RHS + RK update per point and stage
+FLOPS_PER_POINT_STAGE = {2: 118, 3: 238}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="acm3d_sphere")
+    ap.add_argument("--variant", choices=["fast", "strict"], default="fast")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--jmax", type=int, default=None, help="override the workload's Jmax (smaller cases)")
+    return ap.parse_args()
+
+
+def dist_init(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons (200 ms)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile(prefix="clocks", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            with open(self.out.name) as f:
+                rows = [r.strip().split(",") for r in f if r.strip()]
+        except OSError:
+            rows = []
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip() == "Active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic(workload):
+    """dram bytes per stage launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", f"acm_stage_{workload}.md")
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+# --------------------------------------------------------------------- CPU
+def cpu_sample(workload, seconds=12.0, threads=None):
+    """Time the oracle on a bounded sample: the workload's physics on a
+    smaller grid (same block size, ghost width and mask), RK4 steps until
+    `seconds` of wall time have been spent."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from wabbit_gb300 import workloads
+    cfg = workloads.make_config(workload)
+    small = cfg.copy()
+    small.Jmax = max(cfg.Jmin + 1, cfg.Jmax - 2)
+    lv, co = workloads.make_grid(workload, small)
+    u = workloads.initial_condition(workload, small, lv, co)
+    full = pyoracle.pad_blocks(small, u if small.dim == 3 else u[:, :, 0])
+    threads = threads or os.cpu_count() or 1
+    o = pyoracle.Oracle(small, threads=threads)
+    o.set_grid(lv, co, full)
+    if small.dim == 3 and small.penalization:
+        ids, masks = workloads.sphere_mask(small, lv, co)
+        m = np.zeros((len(lv), 6) + full.shape[2:])
+        if len(ids):
+            m[ids] = masks
+        o.set_mask(m)
+    npts = len(lv) * int(np.prod([small.Bs[d] for d in range(small.dim)]))
+    t = 0.0
+    t, _ = o.step(t)  # warm-up
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        t, _ = o.step(t)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or steps >= 200:
+            break
+    value = npts * steps / el
+    sample = (f"{workload} physics on its Jmax={small.Jmax} grid ({len(lv)} blocks, {npts} points), "
+              f"{steps} RK4 steps in {el:.1f} s")
+    return value, threads, sample, el / steps
+
+
+# --------------------------------------------------------------------- GPU
+def run_ours(args, rank, world):
+    import torch
+    from wabbit_gb300 import build, workloads
+    from wabbit_gb300.solver import Context, probe_alu
+
+    build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    cfg, lv, co, u0, ids, masks = workloads.build(args.workload, jmax=args.jmax)
+    nblk = len(lv)
+    dim = cfg.dim
+    npts_blk = int(np.prod([cfg.Bs[d] for d in range(dim)]))
+    npts = nblk * npts_blk
+    ctx = Context(cfg, nblk + 16)
+    ctx.set_variant(args.variant == "fast")
+    f = ctx.forest()
+    f.set_grid(lv, co)
+    f.upload_interior(u0)
+    if masks is not None and len(ids):
+        f.set_mask_sparse(ids, masks)
+    _, nmasked = f.stats()
+    f.set_time(0.0)
+    f.sync_ghosts_RHS_tree()
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    # warm-up (also captures the graph)
+    f.run(max(args.warmup, 1), use_graph=True)
+    ctx.synchronize()
+    graph_kernels = capi_graph_kernels(ctx)
+
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    with Clocks(local) as clk:
+        e0.record(stream)
+        f.run(args.steps, use_graph=True)
+        e1.record(stream)
+        e1.synchronize()
+        ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(ms, world)
+    t_end, dt_last = f.time()  # raises if the run diverged
+    value = sum_over_ranks(npts * args.steps / (ms * 1e-3), world)
+
+    # roofline of the RK-stage kernel, timed alone
+    stage_ms = f.time_kernel(0, reps=20)
+    sync_ms = f.time_kernel(1, reps=20)
+    dt_ms = f.time_kernel(2, reps=20)
+    bytes_stage = 8.0 * npts * cfg.neq * WORDS_PER_POINT_STAGE + 8.0 * nmasked * npts_blk * MASK_WORDS
+    flops_stage = float(FLOPS_PER_POINT_STAGE[dim]) * npts
+    hbm_peak, hbm_src = measured_peaks()
+    fp64_peak, fp32_peak = probe_alu()
+    ach_gbs = bytes_stage / (stage_ms * 1e-3) / 1e9
+    ach_tf = flops_stage / (stage_ms * 1e-3) / 1e12
+    traffic = profile_traffic(args.workload)
+
+    # e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+        host_out = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+        host_in[...] = u0
+        k = max(3, min(args.steps, 10))
+        f.upload_interior(host_in)
+        f.timeStep_tree()
+        f.download_interior(host_out)
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            f.upload_interior(host_in)
+            f.timeStep_tree()
+            f.download_interior(host_out)
+        el = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": sum_over_ranks(npts * k / el, world), "unit": "point-updates/s",
+               "h2d_bytes_per_step": int(host_in.nbytes), "d2h_bytes_per_step": int(host_out.nbytes) + 16,
+               "steps": k, "path": "wg_upload_interior + wg_rk4_step + wg_download_interior (pinned host)"}
+
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        v, cores, sample, _ = cpu_sample(args.workload)
+        cpu = {"value": v, "unit": "point-updates/s", "cores": cores, "kind": "port", "sample": sample}
+
+    clocks = clk.summary()
+    line = {
+        "metric": "ACM point-updates/s/GPU",
+        "value": value,
+        "unit": "point-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded IC and grid, see wabbit_gb300/workloads.py)",
+        "config": {
+            "workload": args.workload, "dim": dim, "Bs": list(cfg.Bs)[:dim], "g": cfg.g, "g_rhs": cfg.g_rhs,
+            "wavelet": cfg.wavelet.decode(), "Jmax": cfg.Jmax, "blocks": nblk, "points": npts,
+            "masked_blocks": nmasked, "levels": np.bincount(lv).tolist(), "variant": args.variant,
+            "rk": "RK4", "graph": True, "l2": "state 2.9 GB > 129 MB L2 (no flush needed)" if dim == 3 else
+            "inputs smaller than L2",
+            "parallelism": "replicas" if world > 1 else "1 GPU",
+        },
+        "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": ach_gbs / hbm_peak, "traffic": traffic, "kernel": "acm_stage_kernel",
+                     "launch_ms": stage_ms, "peak_source": hbm_src,
+                     "algorithmic_bytes_per_launch": bytes_stage},
+        "roofline_alu": {"bound": "fp64", "achieved": ach_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": ach_tf / fp64_peak, "flops_per_launch": flops_stage,
+                         "peak_source": "FP64 FMA probe measured in this run (wg_probe_alu)",
+                         "fp32_peak_tflops": fp32_peak},
+        "kernels_ms": {"acm_stage": stage_ms, "sync_rhs": sync_ms, "dt": dt_ms},
+        "gpu_launches": graph_kernels * args.steps,
+        "clocks": clocks,
+        "t_end": t_end,
+        "dt_last": dt_last,
+    }
+    if e2e is not None:
+        line["e2e"] = e2e
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+
+
+def capi_graph_kernels(ctx):
+    from wabbit_gb300 import capi
+    n = ctx.L.wg_graph_kernels(ctx.h)
+    return int(capi.check(n))
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from wabbit_gb300 import workloads
+    cfg = workloads.make_config(args.workload)
+    # each bench step is one RK4 step of the oracle on the bounded sample
+    _, cores, sample, t_step = cpu_sample(args.workload, seconds=3.0)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    # time exactly K steps after W warm-up steps
+    import pyoracle
+    small = cfg.copy()
+    small.Jmax = max(cfg.Jmin + 1, cfg.Jmax - 2)
+    lv, co = workloads.make_grid(args.workload, small)
+    u = workloads.initial_condition(args.workload, small, lv, co)
+    full = pyoracle.pad_blocks(small, u if small.dim == 3 else u[:, :, 0])
+    o = pyoracle.Oracle(small, threads=cores)
+    o.set_grid(lv, co, full)
+    if small.dim == 3 and small.penalization:
+        ids, masks = workloads.sphere_mask(small, lv, co)
+        m = np.zeros((len(lv), 6) + full.shape[2:])
+        if len(ids):
+            m[ids] = masks
+        o.set_mask(m)
+    npts = len(lv) * int(np.prod([small.Bs[d] for d in range(small.dim)]))
+    t = 0.0
+    for _ in range(args.warmup):
+        t, _ = o.step(t)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t, _ = o.step(t)
+    el = time.perf_counter() - t0
+    value = npts * args.steps / el
+    sample = (f"{args.workload} physics on its Jmax={small.Jmax} grid ({len(lv)} blocks, {npts} points), "
+              f"one RK4 step per bench step")
+    line = {
+        "metric": "ACM point-updates/s/GPU", "value": value, "unit": "point-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded IC and grid, see wabbit_gb300/workloads.py)",
+        "config": {"workload": args.workload, "sample": sample},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "point-updates/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "point-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference is Fortran (no compiler in this image); the oracle is its bit-exact C++ restatement",
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world = dist_init(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -125,10 +125,17 @@ int wg_get_grid(wg_ctx *ctx, int tree, int cap, int *level, int *coords);
 /* Heavy data in the reference block layout (hvy_block, see top of file). */
 int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks);
 int wg_download_state(wg_ctx *ctx, int tree, double *host_blocks);
+/* Interior points only, compact (nblk, neq, Bz, By, Bx) x fastest: one
+ * contiguous copy each way; ghost nodes are refilled by the next sync. */
+int wg_upload_interior(wg_ctx *ctx, int tree, const double *host);
+int wg_download_interior(wg_ctx *ctx, int tree, double *host);
 /* Penalisation mask in the layout of hvy_mask (..., 1:6, Nb): chi, usx,
  * usy, usz, colour, sponge (createMask_tree, LIB/MESH/createMask_tree.f90);
  * NULL removes it. Only blocks with a non-zero mask keep a device copy. */
 int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask);
+/* Same for the n listed blocks only (mask holds n*6*npts doubles); every
+ * other block has chi = 0. */
+int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const double *mask);
 
 int wg_set_time(wg_ctx *ctx, int tree, double time);
 int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);
@@ -162,6 +169,16 @@ int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags,
  * (LIB/MESH/refinementExecute.f90:4-116). Block b becomes blocks
  * 2^d*b .. 2^d*b+2^d-1. Ghosts must hold g synced layers. */
 int wg_refine_everywhere(wg_ctx *ctx, int tree);
+
+/* ---- measurement -------------------------------------------------------- */
+/* FP64 / FP32 FMA throughput of the current device, TFLOP/s (FMA = 2). */
+int wg_probe_alu(double *fp64_tflops, double *fp32_tflops);
+/* Mean device time (ms) of one launch over reps launches, CUDA events on the
+ * context stream: which = 0 RK-stage kernel, 1 RHS ghost sync, 2 dt. */
+int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_launch);
+int wg_tree_stats(wg_ctx *ctx, int tree, int *nblocks, int *nmasked);
+/* kernel nodes in the captured RK4-step graph of the last wg_run(.., 1) */
+int wg_graph_kernels(wg_ctx *ctx);
 
 /* ---- inspection (tests, tooling) --------------------------------------- */
 /* ghost-patch table: returns the patch count; out receives 19 ints per

@@ -26,6 +26,7 @@ UNITS = {
     "k_wavelet.cu": [],
     "k_acm_strict.cu": ["-fmad=false"],
     "k_acm_fast.cu": [],
+    "k_probe.cu": [],
 }
 
 

@@ -24,6 +24,8 @@ EXPORTS = [
     "wg_get_nblocks", "wg_get_grid", "wg_upload_state", "wg_download_state", "wg_set_mask", "wg_set_time",
     "wg_get_time", "wg_sync_ghosts", "wg_rhs", "wg_compute_dt", "wg_rk4_step", "wg_run", "wg_threshold_flags",
     "wg_refine_everywhere", "wg_sync_table", "wg_block_slot", "wg_sync_table_host",
+    "wg_probe_alu", "wg_time_kernel", "wg_tree_stats", "wg_set_mask_sparse",
+    "wg_upload_interior", "wg_download_interior", "wg_graph_kernels",
 ]
 
 
@@ -67,6 +69,13 @@ _SIGS = {
     "wg_sync_table": (_i, [_vp, _i, _i, _i, _i, _i, _ip]),
     "wg_block_slot": (_i, [_vp, _i, _i]),
     "wg_sync_table_host": (_i, [ctypes.POINTER(WgConfig), _i, _ip, _ip, _i, _i, _i, _i, _ip]),
+    "wg_probe_alu": (_i, [_dp, _dp]),
+    "wg_time_kernel": (_i, [_vp, _i, _i, _i, _dp]),
+    "wg_tree_stats": (_i, [_vp, _i, _ip, _ip]),
+    "wg_set_mask_sparse": (_i, [_vp, _i, _i, _ip, _dp]),
+    "wg_upload_interior": (_i, [_vp, _i, _dp]),
+    "wg_download_interior": (_i, [_vp, _i, _dp]),
+    "wg_graph_kernels": (_i, [_vp]),
 }
 
 _lib = None

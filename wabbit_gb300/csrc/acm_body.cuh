@@ -141,6 +141,63 @@ __device__ __forceinline__ void rhs3d(const double *u, long long cs, int sx, int
 #undef PZ
 }
 
+
+#ifdef WG_FAST_ALGEBRA
+// Regrouped convective form for the fast path: per axis the pair differences
+// and sums of the +-1, +-2 neighbours give the first derivative
+// k1*(u1-u_1) - k2*(u2-u_2) and the viscous term m1*(u1+u_1) - m2*(u2+u_2),
+// with m0*u0 added once; about 111 FP64 instructions per point and stage
+// instead of ~167 for the reference's term order.
+template <int DIM, bool MASK>
+__device__ __forceinline__ void rhs_opt(const double *u, long long cs, int sx, int sy, const double *m, long long ms,
+                                        const TreeParams &tp, const BlockDesc &d, double r[4]) {
+    const int st[3] = {1, sx, sy};
+    double D1[4][3];
+    double L[3];
+#pragma unroll
+    for (int c = 0; c < DIM + 1; c++) {
+        const double *uc = u + c * cs;
+        const double u0 = uc[0];
+        double lap = c < DIM ? d.m0 * u0 : 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; k++) {
+            const double a = uc[st[k]], b = uc[-st[k]], e = uc[2 * st[k]], f = uc[-2 * st[k]];
+            D1[c][k] = fma(-d.k2[k], e - f, d.k1[k] * (a - b));
+            if (c < DIM) lap = fma(-d.m2[k], e + f, fma(d.m1[k], a + b, lap));
+        }
+        if (c < DIM) L[c] = lap;
+    }
+    const double p0 = u[DIM * cs];
+    double vel[3];
+#pragma unroll
+    for (int c = 0; c < DIM; c++) vel[c] = u[c * cs];
+    double chi = 0.0;
+    if (MASK) {
+        const int color = (int)m[4 * ms];
+        chi = color == 0 ? 0.0 : m[0] * tp.C_eta_inv;
+    }
+#pragma unroll
+    for (int c = 0; c < DIM; c++) {
+        double t = D1[DIM][c];                       // p_dx (pressure gradient along c)
+#pragma unroll
+        for (int k = 0; k < DIM; k++) t = fma(vel[k], D1[c][k], t);
+        double rc = L[c] - t;
+        if (MASK) rc = fma(-chi, vel[c] - m[(1 + c) * ms], rc);
+        r[c] = rc;
+    }
+    double div = D1[0][0];
+#pragma unroll
+    for (int k = 1; k < DIM; k++) div += D1[k][k];
+    r[DIM] = fma(-(tp.c0 * tp.c0), div, -tp.gamma_p * p0);
+    if (MASK && tp.use_sponge) {
+        const double spo = m[5 * ms] * tp.C_sponge_inv;
+#pragma unroll
+        for (int c = 0; c < DIM; c++) r[c] = fma(-(vel[c] - tp.u_mean_set[c]), spo, r[c]);
+        r[DIM] = fma(-p0, spo, r[DIM]);
+    }
+}
+#endif
+
 // RK4 Butcher coefficients (ini_file_to_params.f90:640-646)
 __device__ __forceinline__ double rk_b(int j) { return (j == 1 || j == 4) ? 1.0 / 6.0 : 1.0 / 3.0; }
 __device__ __forceinline__ double rk_a(int j) { return j == 3 ? 1.0 : 0.5; }   // a_{j+1,j}
@@ -166,6 +223,11 @@ __global__ void __launch_bounds__(256) acm_stage_kernel(StageArgs a) {
     long long ms = npts_int;
     if (MASK) m = a.mask + (long long)d.mask * 6 * npts_int + q;
     double r[4];
+#ifdef WG_FAST_ALGEBRA
+    if (!SKEW) {
+        rhs_opt<DIM, MASK>(u, cs, a.gin.nx, a.gin.nx * a.gin.ny, m, ms, tp, d, r);
+    } else
+#endif
     if (DIM == 2) {
         const double dxi = 1.0 / d.dx[0], dyi = 1.0 / d.dx[1];
         const double dx2 = 1.0 / (d.dx[0] * d.dx[0]), dy2 = 1.0 / (d.dx[1] * d.dx[1]);
@@ -200,11 +262,20 @@ __global__ void __launch_bounds__(256) acm_stage_kernel(StageArgs a) {
         for (int c = 0; c < nc; c++) {
             const double u0 = un[c * us];
             const double base = j == 1 ? u0 : acc[c * npts_int];
+#ifdef WG_FAST_ALGEBRA
+            acc[c * npts_int] = fma(db, r[c], base);
+            o[c * os] = fma(da, r[c], u0);
+#else
             acc[c * npts_int] = __dadd_rn(base, __dmul_rn(db, r[c]));
             o[c * os] = __dadd_rn(u0, __dmul_rn(da, r[c]));
+#endif
         }
     } else {
+#ifdef WG_FAST_ALGEBRA
+        for (int c = 0; c < nc; c++) un[c * us] = fma(db, r[c], acc[c * npts_int]);
+#else
         for (int c = 0; c < nc; c++) un[c * us] = __dadd_rn(acc[c * npts_int], __dmul_rn(db, r[c]));
+#endif
     }
 }
 

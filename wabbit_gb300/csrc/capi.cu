@@ -107,6 +107,8 @@ struct wg_ctx {
     cudaStream_t stream = nullptr;
     int variant_fast = 1;               // 1: FMA stencil, 0: strict reference arithmetic
     DevArray<int> d_tree_ids;
+    double *staging = nullptr;          // compact interior staging buffer
+    size_t staging_bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<int> graph_trees;
@@ -195,7 +197,11 @@ int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp) {
     const BufGeo geo = thin ? ctx->gT : ctx->gA;
     for (int s = 0; s < sp->table.nstages; s++) {
         const int b = sp->table.stage_begin[s], e = sp->table.stage_begin[s + 1];
-        WG_CUDA_OK(launch_sync(sp->d.p + b, e - b, buf, geo, ctx->geo.nc, ctx->wav.order_predictor, ctx->stream));
+        if (sp->table.stage_predict[s])
+            WG_CUDA_OK(launch_predict(sp->d.p + b, e - b, sp->table.max_coarse, buf, geo, ctx->geo.nc,
+                                      ctx->wav.order_predictor, ctx->stream));
+        else
+            WG_CUDA_OK(launch_sync(sp->d.p + b, e - b, buf, geo, ctx->geo.nc, ctx->wav.order_predictor, ctx->stream));
     }
     return WG_OK;
 }
@@ -229,6 +235,15 @@ int upload_desc(wg_ctx *ctx, Tree &t, int tree_id) {
         std::memset(&d, 0, sizeof(d));
         const int lv = t.forest.level[b];
         for (int k = 0; k < 3; k++) d.dx[k] = k < c.dim ? std::pow(2.0, -lv) * c.domain[k] / (double)c.Bs[k] : 0.0;
+        const double nu = t.cfg.nu;
+        d.m0 = 0.0;
+        for (int k = 0; k < c.dim; k++) {
+            d.k1[k] = (2.0 / 3.0) / d.dx[k];
+            d.k2[k] = (1.0 / 12.0) / d.dx[k];
+            d.m1[k] = nu * (4.0 / 3.0) / (d.dx[k] * d.dx[k]);
+            d.m2[k] = nu * (1.0 / 12.0) / (d.dx[k] * d.dx[k]);
+            d.m0 += nu * (-2.5) / (d.dx[k] * d.dx[k]);
+        }
         d.tree = tree_id;
         d.level = lv;
         d.mask = t.mask_slot[b];
@@ -369,7 +384,7 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
     cudaMemsetAsync(ctx->d_clk, 0, sizeof(TreeClock) * ctx->max_trees, ctx->stream);
     ctx->h_desc.resize(max_blocks);
     ctx->free_slots.reserve(max_blocks);
-    for (int i = max_blocks - 1; i >= 0; i--) ctx->free_slots.push_back(i);
+    for (int i = max_blocks - 1; i >= 0; i--) ctx->free_slots.push_back(i);   // back() = lowest slot
     ctx->trees.resize(ctx->max_trees);
     std::vector<int> ids(ctx->max_trees);
     for (int i = 0; i < ctx->max_trees; i++) ids[i] = i;
@@ -391,6 +406,7 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->C);
     cudaFree(ctx->acc);
     cudaFree(ctx->mask);
+    cudaFree(ctx->staging);
     cudaFree(ctx->d_desc);
     cudaFree(ctx->d_tp);
     cudaFree(ctx->d_clk);
@@ -451,6 +467,8 @@ int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *co
     release_tree_blocks(ctx, *t);
     if ((size_t)nblk > ctx->free_slots.size())
         return fail(WG_ENOMEM, "grid of %d blocks does not fit (%zu free slots)", nblk, ctx->free_slots.size());
+    // hand out the lowest free slots in ascending order (contiguous copies)
+    std::sort(ctx->free_slots.begin(), ctx->free_slots.end(), std::greater<int>());
     t->forest.set(nblk, level, coords);
     std::string err;
     if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "%s", err.c_str());
@@ -487,10 +505,22 @@ int wg_get_grid(wg_ctx *ctx, int tree, int cap, int *level, int *coords) {
 }
 
 // host_blocks: nblk * neq * npts doubles in the reference block layout
+static bool contiguous(const std::vector<int> &s) {
+    for (size_t i = 1; i < s.size(); i++)
+        if (s[i] != s[i - 1] + 1) return false;
+    return true;
+}
+
 int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !host_blocks) return fail(WG_EINVAL, "bad arguments");
     const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
+    if (!t->slots.empty() && contiguous(t->slots)) {
+        WG_CUDA_OK(cudaMemcpyAsync((char *)ctx->A + per * t->slots[0], host_blocks, per * t->slots.size(),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        return WG_OK;
+    }
     for (size_t b = 0; b < t->slots.size(); b++)
         WG_CUDA_OK(cudaMemcpyAsync((char *)ctx->A + per * t->slots[b], (const char *)host_blocks + per * b, per,
                                    cudaMemcpyHostToDevice, ctx->stream));
@@ -502,6 +532,12 @@ int wg_download_state(wg_ctx *ctx, int tree, double *host_blocks) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !host_blocks) return fail(WG_EINVAL, "bad arguments");
     const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
+    if (!t->slots.empty() && contiguous(t->slots)) {
+        WG_CUDA_OK(cudaMemcpyAsync(host_blocks, (const char *)ctx->A + per * t->slots[0], per * t->slots.size(),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        return WG_OK;
+    }
     for (size_t b = 0; b < t->slots.size(); b++)
         WG_CUDA_OK(cudaMemcpyAsync((char *)host_blocks + per * b, (const char *)ctx->A + per * t->slots[b], per,
                                    cudaMemcpyDeviceToHost, ctx->stream));
@@ -509,11 +545,13 @@ int wg_download_state(wg_ctx *ctx, int tree, double *host_blocks) {
     return WG_OK;
 }
 
-// host_mask: nblk * 6 * npts (reference layout hvy_mask) or NULL to drop
-// the mask. Blocks whose mask is zero everywhere get no device mask slot.
-int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
+// Masks of the listed blocks of a tree: mask holds n blocks of 6*npts doubles
+// (hvy_mask layout); all other blocks get no mask (chi = 0). Blocks whose
+// listed mask is zero (chi, u_s and sponge; the colour is ignored) keep no
+// device copy either.
+int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const double *mask) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t || n < 0 || (n && (!blocks || !mask))) return fail(WG_EINVAL, "bad arguments");
     cudaStreamSynchronize(ctx->stream);
     for (int &m : t->mask_slot) {
         if (m >= 0) ctx->mask_free.push_back(m);
@@ -526,40 +564,39 @@ int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
     const int *Bs = ctx->cfg.Bs;
     std::vector<double> packed;
     std::vector<int> need;
-    if (host_mask) {
-        for (int b = 0; b < nb; b++) {
-            const double *m = host_mask + (size_t)b * 6 * np;
-            bool any = false;
-            std::vector<double> blk(6 * ni);
-            for (int c = 0; c < 6; c++)
-                for (int iz = 0; iz < (dim == 3 ? Bs[2] : 1); iz++)
-                    for (int iy = 0; iy < Bs[1]; iy++)
-                        for (int ix = 0; ix < Bs[0]; ix++) {
-                            const long long src = ((long long)(iz + (dim == 3 ? g : 0)) * ctx->gA.ny + iy + g) * ctx->gA.nx + ix + g;
-                            const double v = m[c * np + src];
-                            blk[c * ni + ((long long)iz * Bs[1] + iy) * Bs[0] + ix] = v;
-                            if (v != 0.0 && c != 4) any = true;
-                        }
-            if (any) {
-                need.push_back(b);
-                packed.insert(packed.end(), blk.begin(), blk.end());
-            }
+    for (int k = 0; k < n; k++) {
+        const int b = blocks[k];
+        if (b < 0 || b >= nb) return fail(WG_EINVAL, "mask block id %d out of range", b);
+        const double *m = mask + (size_t)k * 6 * np;
+        bool any = false;
+        std::vector<double> blk(6 * ni);
+        for (int c = 0; c < 6; c++)
+            for (int iz = 0; iz < (dim == 3 ? Bs[2] : 1); iz++)
+                for (int iy = 0; iy < Bs[1]; iy++)
+                    for (int ix = 0; ix < Bs[0]; ix++) {
+                        const long long src = ((long long)(iz + (dim == 3 ? g : 0)) * ctx->gA.ny + iy + g) * ctx->gA.nx + ix + g;
+                        const double v = m[c * np + src];
+                        blk[c * ni + ((long long)iz * Bs[1] + iy) * Bs[0] + ix] = v;
+                        if (v != 0.0 && c != 4) any = true;
+                    }
+        if (any) {
+            need.push_back(b);
+            packed.insert(packed.end(), blk.begin(), blk.end());
         }
     }
-    // grow the pool if needed
-    int in_use = ctx->mask_cap - (int)ctx->mask_free.size();
-    int want = in_use + (int)need.size();
+    const int in_use = ctx->mask_cap - (int)ctx->mask_free.size();
+    const int want = in_use + (int)need.size();
     if (want > ctx->mask_cap) {
-        int ncap = std::max(want, ctx->mask_cap * 2);
+        const int ncap = std::max(want, ctx->mask_cap * 2);
         double *nm = nullptr;
         if (cudaMalloc(&nm, sizeof(double) * 6 * ni * (size_t)ncap) != cudaSuccess) {
             cudaGetLastError();
             return fail(WG_ENOMEM, "mask pool of %d blocks does not fit", ncap);
         }
         if (ctx->mask) {
-            cudaMemcpyAsync(nm, ctx->mask, sizeof(double) * 6 * ni * (size_t)ctx->mask_cap, cudaMemcpyDeviceToDevice,
-                            ctx->stream);
-            cudaStreamSynchronize(ctx->stream);
+            WG_CUDA_OK(cudaMemcpyAsync(nm, ctx->mask, sizeof(double) * 6 * ni * (size_t)ctx->mask_cap,
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+            WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
             cudaFree(ctx->mask);
         }
         for (int i = ncap - 1; i >= ctx->mask_cap; i--) ctx->mask_free.push_back(i);
@@ -567,7 +604,7 @@ int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
         ctx->mask_cap = ncap;
     }
     for (size_t k = 0; k < need.size(); k++) {
-        int slot = ctx->mask_free.back();
+        const int slot = ctx->mask_free.back();
         ctx->mask_free.pop_back();
         t->mask_slot[need[k]] = slot;
         WG_CUDA_OK(cudaMemcpyAsync(ctx->mask + (size_t)slot * 6 * ni, packed.data() + k * 6 * ni,
@@ -579,6 +616,16 @@ int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     ctx->grid_version++;
     return WG_OK;
+}
+
+// host_mask: nblk * 6 * npts (reference layout hvy_mask) or NULL to drop it
+int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    if (!host_mask) return wg_set_mask_sparse(ctx, tree, 0, nullptr, nullptr);
+    std::vector<int> ids(t->forest.size());
+    for (size_t i = 0; i < ids.size(); i++) ids[i] = (int)i;
+    return wg_set_mask_sparse(ctx, tree, (int)ids.size(), ids.data(), host_mask);
 }
 
 int wg_set_time(wg_ctx *ctx, int tree, double time) {
@@ -907,6 +954,136 @@ int wg_sync_table_host(const wg_config *cfg, int nblk, const int *level, const i
         }
     }
     return n;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// FP64 and FP32 FMA throughput of the current device in TFLOP/s (FMA = 2)
+int wg_probe_alu(double *fp64_tflops, double *fp32_tflops) {
+    if (!fp64_tflops || !fp32_tflops) return fail(WG_EINVAL, "null output");
+    WG_CUDA_OK(probe_alu(fp64_tflops, fp32_tflops));
+    return WG_OK;
+}
+
+// Average device time of one launch of a hot-path kernel over reps launches,
+// timed with CUDA events on the context stream. which: 0 = RK stage kernel
+// (stage 2, current variant, plain + masked lists), 1 = RHS ghost sync of a
+// stage buffer (all stages), 2 = dt reduction. The state is left unchanged
+// for which = 0 and 2 (stage 2 writes only the stage buffers).
+int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_launch) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || reps <= 0 || !ms_per_launch) return fail(WG_EINVAL, "bad arguments");
+    const int g_rhs = ctx->cfg.g_rhs;
+    const int *Bs = ctx->cfg.Bs;
+    SyncPlan *sp;
+    int st = get_sync(ctx, *t, g_rhs, g_rhs, true, &sp);
+    if (st) return st;
+    cudaEvent_t e0, e1;
+    WG_CUDA_OK(cudaEventCreate(&e0));
+    WG_CUDA_OK(cudaEventCreate(&e1));
+    auto once = [&]() -> int {
+        if (which == 0) return stage_launch(ctx, *t, 2, ctx->B, ctx->gT, ctx->C, ctx->gT);
+        if (which == 1) return run_sync(ctx, *t, ctx->B, true, g_rhs, g_rhs);
+        WG_CUDA_OK(launch_dt(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk,
+                             ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, ctx->stream));
+        return WG_OK;
+    };
+    if ((st = once())) return st;
+    WG_CUDA_OK(cudaEventRecord(e0, ctx->stream));
+    for (int r = 0; r < reps; r++)
+        if ((st = once())) return st;
+    WG_CUDA_OK(cudaEventRecord(e1, ctx->stream));
+    WG_CUDA_OK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    WG_CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_launch = ms / reps;
+    return WG_OK;
+}
+
+// Per-block interior points and masked-block count of a tree (for the bench)
+int wg_tree_stats(wg_ctx *ctx, int tree, int *nblocks, int *nmasked) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    if (nblocks) *nblocks = (int)t->slots.size();
+    if (nmasked) *nmasked = t->n_masked;
+    return WG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+int ensure_staging(wg_ctx *ctx, size_t bytes) {
+    if (ctx->staging_bytes >= bytes) return WG_OK;
+    if (ctx->staging) cudaFree(ctx->staging);
+    ctx->staging = nullptr;
+    ctx->staging_bytes = 0;
+    if (cudaMalloc(&ctx->staging, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(WG_ENOMEM, "staging buffer of %zu bytes does not fit", bytes);
+    }
+    ctx->staging_bytes = bytes;
+    return WG_OK;
+}
+}  // namespace
+
+extern "C" {
+
+// Interior-only state exchange: host array (nblk, neq, Bz, By, Bx), x
+// fastest. One contiguous host<->device copy plus a device scatter/gather;
+// ghost nodes are left to the next synchronisation.
+int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !host) return fail(WG_EINVAL, "bad arguments");
+    const int *Bs = ctx->cfg.Bs;
+    const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
+    const size_t bytes = sizeof(double) * t->slots.size() * ctx->geo.nc * ctx->nint;
+    int st = ensure_staging(ctx, bytes);
+    if (st) return st;
+    WG_CUDA_OK(cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, ctx->staging, ctx->geo.nc,
+                                    Bs[0], Bs[1], Bz, 1, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+int wg_download_interior(wg_ctx *ctx, int tree, double *host) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !host) return fail(WG_EINVAL, "bad arguments");
+    const int *Bs = ctx->cfg.Bs;
+    const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
+    const size_t bytes = sizeof(double) * t->slots.size() * ctx->geo.nc * ctx->nint;
+    int st = ensure_staging(ctx, bytes);
+    if (st) return st;
+    WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, ctx->staging, ctx->geo.nc,
+                                    Bs[0], Bs[1], Bz, 0, ctx->stream));
+    WG_CUDA_OK(cudaMemcpyAsync(host, ctx->staging, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// number of kernel nodes in the captured RK4-step graph of the last
+// wg_run(use_graph=1) call (the launches one replay performs)
+int wg_graph_kernels(wg_ctx *ctx) {
+    if (!ctx || !ctx->graph) return fail(WG_EINVAL, "no captured graph");
+    size_t n = 0;
+    WG_CUDA_OK(cudaGraphGetNodes(ctx->graph, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    WG_CUDA_OK(cudaGraphGetNodes(ctx->graph, nodes.data(), &n));
+    int k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        WG_CUDA_OK(cudaGraphNodeGetType(nd, &t));
+        if (t == cudaGraphNodeTypeKernel) k++;
+    }
+    return k;
 }
 
 }  // extern "C"

@@ -29,9 +29,12 @@ struct TreeClock {
     int    pad;
 };
 
-// Per-block descriptor.
+// Per-block descriptor. k1, k2: first-derivative weights (2/3)/dx, (1/12)/dx;
+// m1, m2, m0: viscous weights nu*(4/3)/dx^2, nu*(1/12)/dx^2 and
+// nu*(-5/2)*sum 1/dx^2 (regrouped FD_4th_central stencils of the fast path).
 struct BlockDesc {
     double dx[3];
+    double k1[3], k2[3], m1[3], m2[3], m0;
     int32_t tree;
     int32_t level;
     int32_t mask;                // slot in the mask pool, -1 = no mask
@@ -79,11 +82,16 @@ cudaError_t stage(int dim, const StageArgs &a, int nblk, bool skew, bool mask, c
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 
 // ---- kernel launchers (defined in the .cu files) -----------------------
+cudaError_t probe_alu(double *fp64_tflops, double *fp32_tflops);
 // constant-memory set-up; must run before any stream capture
 cudaError_t sync_init();
 cudaError_t wavelet_init();
 cudaError_t launch_sync(const Patch *patches, int npatch, double *buf, BufGeo geo, int nc, int order_predictor,
                         cudaStream_t s);
+// prediction patches only; max_smem_doubles = largest shared-memory need
+// (coarse box + x window + x-y window) of a patch, in doubles
+cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_doubles, double *buf, BufGeo geo, int nc,
+                           int order_predictor, cudaStream_t s);
 // RHS + RK stage (j = 1..4) over nblk blocks listed in blk
 cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, int nblk, const BlockDesc *desc,
                              const TreeParams *tp, const TreeClock *clk, const double *in, BufGeo gin,
@@ -96,6 +104,8 @@ cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, 
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
                       const int *trees, cudaStream_t s);
 cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
+cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
+                                 int Bx, int By, int Bz, int to_full, cudaStream_t s);
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,
                              int Bs2, int nc, int wavelet_x, int wavelet_y, const double *eps_use,
                              const int *tsvc, int *flags, double *details, cudaStream_t s);

@@ -359,6 +359,7 @@ bool make_sync_table(const Forest &f, const Geometry &geo, const WaveletInfo &w,
     for (int d = 0; d < 3; d++) nbuf[d] = d < geo.dim ? geo.Bs[d] + 2 * g_buf : 1;
     std::vector<std::vector<Patch>> per(nstages + 1);
     out.max_points = 0;
+    out.max_coarse = 0;
     for (int s = 0; s < f.size(); s++) {
         const int *nb = &f.nbr[size_t(s) * kNumRelations];
         for (int r = 1; r <= kNumRelations; r++) {
@@ -402,14 +403,38 @@ bool make_sync_table(const Forest &f, const Geometry &geo, const WaveletInfo &w,
                 }
             }
             out.max_points = std::max(out.max_points, npts);
+            if (p.op == 2) {
+                // shared memory of the separable prediction: coarse box, x
+                // window (even rows/planes) and x-y window (even planes)
+                const int h = w.order_predictor - 1;
+                const int cx = p.shi[0] - p.slo[0] + 1, cy = p.shi[1] - p.slo[1] + 1, cz = p.shi[2] - p.slo[2] + 1;
+                const int Fy = 2 * cy - 1, Fz = 2 * cz - 1;
+                const int ex = p.rhi[0] - p.rlo[0] + 1, ey = p.rhi[1] - p.rlo[1] + 1, ez = p.rhi[2] - p.rlo[2] + 1;
+                int yw0 = std::max(0, p.blo[1] - h), yw1 = std::min(Fy - 1, p.blo[1] + ey - 1 + h);
+                yw0 += yw0 & 1;
+                yw1 -= yw1 & 1;
+                int zw0 = std::max(0, p.blo[2] - h), zw1 = std::min(Fz - 1, p.blo[2] + ez - 1 + h);
+                zw0 += zw0 & 1;
+                zw1 -= zw1 & 1;
+                const int wy = (yw1 - yw0) / 2 + 1, wz = (zw1 - zw0) / 2 + 1;
+                const int need = cx * cy * cz + ex * wy * wz + ex * ey * wz;
+                out.max_coarse = std::max(out.max_coarse, need);
+            }
             per[stage].push_back(p);
         }
     }
     out.nstages = nstages;
     out.patches.clear();
     out.stage_begin.assign(nstages + 1, 0);
+    out.stage_predict.assign(nstages, 0);
     for (int s = 1; s <= nstages; s++) {
         out.stage_begin[s - 1] = (int)out.patches.size();
+        bool all_pred = !per[s].empty();
+        for (const Patch &p : per[s]) all_pred = all_pred && p.op == 2;
+        bool any_pred = false;
+        for (const Patch &p : per[s]) any_pred = any_pred || p.op == 2;
+        if (any_pred && !all_pred) { err = "prediction mixed with copies in one stage"; return false; }
+        out.stage_predict[s - 1] = all_pred ? 1 : 0;
         out.patches.insert(out.patches.end(), per[s].begin(), per[s].end());
     }
     out.stage_begin[nstages] = (int)out.patches.size();

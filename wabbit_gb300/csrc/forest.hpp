@@ -76,7 +76,9 @@ struct SyncTable {
     int nstages = 2;
     std::vector<Patch> patches;        // sorted by stage
     std::vector<int> stage_begin;      // nstages+1 offsets
+    std::vector<int> stage_predict;    // 1 if every patch of the stage is a prediction
     int max_points = 0;                // largest receiver box
+    int max_coarse = 0;                // largest shared-memory need of a prediction (doubles)
 };
 
 // Build the ghost-sync table of one forest for the reference's

@@ -20,10 +20,14 @@ __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc
     const int nint = Bs0 * Bs1 * (DIM == 3 ? Bs2 : 1);
     const double *ub = u + (long long)b * (DIM + 1) * np;
     double m = -1.0;
+    bool bad = false;
     for (int q = threadIdx.x; q < nint; q += blockDim.x) {
         const int ix = q % Bs0, iy = (q / Bs0) % Bs1, iz = DIM == 3 ? q / (Bs0 * Bs1) : 0;
         const long long o = ((long long)(iz + (DIM == 3 ? geo.gb : 0)) * geo.ny + (iy + geo.gb)) * geo.nx + (ix + geo.gb);
         const double a = ub[o], bb = ub[np + o];
+        // divergence guard of the ACM integral stage (rhs_ACM.f90:133-146)
+        for (int c = 0; c <= DIM; c++)
+            if (!(fabs(ub[c * np + o]) <= 1.0e12)) bad = true;
         double s = __dadd_rn(__dmul_rn(a, a), __dmul_rn(bb, bb));
         if (DIM == 3) {
             const double c = ub[2 * np + o];
@@ -38,6 +42,7 @@ __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc
         if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
         __syncthreads();
     }
+    if (bad) atomicOr(&clk[d.tree].diverged, 1);
     if (threadIdx.x == 0) {
         const TreeParams &p = tp[d.tree];
         const double u_mag = red[0];
@@ -104,6 +109,32 @@ cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, 
         else dt_kernel<3><<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2);
     }
     dt_finalize_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(tp, clk, trees, ntrees);
+    return cudaGetLastError();
+}
+
+// copy between a compact interior array (nblk, nc, Bz, By, Bx) and the
+// interiors of the listed block slots of a full-layout buffer
+__global__ void interior_copy_kernel(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
+                                     int Bx, int By, int Bz, int to_full) {
+    const long long nint = (long long)Bx * By * Bz;
+    const long long total = (long long)nblk * nc * nint;
+    const int gz = geo.nz > 1 ? geo.gb : 0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const long long r = q % nint;
+        const int c = (int)((q / nint) % nc);
+        const int b = (int)(q / (nint * nc));
+        const int ix = (int)(r % Bx), iy = (int)((r / Bx) % By), iz = (int)(r / ((long long)Bx * By));
+        double *f = full + ((long long)slots[b] * nc + c) * geo.npts() +
+                    ((long long)(iz + gz) * geo.ny + (iy + geo.gb)) * geo.nx + (ix + geo.gb);
+        if (to_full) *f = compact[q];
+        else compact[q] = *f;
+    }
+}
+
+cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
+                                 int Bx, int By, int Bz, int to_full, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    interior_copy_kernel<<<1024, 256, 0, s>>>(slots, nblk, full, geo, compact, nc, Bx, By, Bz, to_full);
     return cudaGetLastError();
 }
 

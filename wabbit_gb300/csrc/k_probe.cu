@@ -1,0 +1,54 @@
+// k_probe.cu -- measurement helpers: FP64/FP32 FMA throughput of this GPU
+// (the ALU denominators of the stencil roofline) and event timing of single
+// kernels of the hot path.
+#include "common.cuh"
+
+namespace wg {
+
+template <class T>
+__global__ void __launch_bounds__(256) fma_chain(T *out, int iters, T a, T b) {
+    T x0 = (T)threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+        x0 = x0 * a + b; x1 = x1 * a + b; x2 = x2 * a + b; x3 = x3 * a + b;
+        x4 = x4 * a + b; x5 = x5 * a + b; x6 = x6 * a + b; x7 = x7 * a + b;
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <class T>
+static cudaError_t probe_one(int iters, double *tflops) {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    const int blocks = sms * 16, threads = 256;
+    T *out = nullptr;
+    cudaError_t e = cudaMalloc(&out, sizeof(T) * blocks * threads);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fma_chain<T><<<blocks, threads>>>(out, iters, (T)0.999, (T)0.001);
+    float best = 1e30f;
+    for (int r = 0; r < 3; r++) {
+        cudaEventRecord(e0);
+        fma_chain<T><<<blocks, threads>>>(out, iters, (T)0.999, (T)0.001);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) best = ms;
+    }
+    e = cudaGetLastError();
+    *tflops = 2.0 * 8 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    return e;
+}
+
+cudaError_t probe_alu(double *fp64, double *fp32) {
+    cudaError_t e = probe_one<double>(2048, fp64);
+    if (e == cudaSuccess) e = probe_one<float>(16384, fp32);
+    return e;
+}
+
+}  // namespace wg

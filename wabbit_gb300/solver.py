@@ -16,6 +16,13 @@ from . import capi
 from .config import WgConfig
 
 
+def probe_alu():
+    """FP64 and FP32 FMA throughput of the current GPU in TFLOP/s."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    capi.check(capi.load().wg_probe_alu(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
+
+
 def _p(a, t=ctypes.c_double):
     return a.ctypes.data_as(ctypes.POINTER(t))
 
@@ -114,6 +121,23 @@ class Forest:
         capi.check(self.L.wg_download_state(self.ctx.h, self.tree, _p(out)))
         return out
 
+    @property
+    def interior_shape(self):
+        c = self.cfg
+        return (c.neq, c.Bs[2] if c.dim == 3 else 1, c.Bs[1], c.Bs[0])
+
+    def upload_interior(self, data):
+        data = np.ascontiguousarray(data, np.float64)
+        if data.size != self.nblocks * int(np.prod(self.interior_shape)):
+            raise ValueError("interior state has the wrong size for this grid")
+        capi.check(self.L.wg_upload_interior(self.ctx.h, self.tree, _p(data)))
+
+    def download_interior(self, out=None):
+        if out is None:
+            out = np.zeros((self.nblocks,) + self.interior_shape)
+        capi.check(self.L.wg_download_interior(self.ctx.h, self.tree, _p(out)))
+        return out
+
     def set_mask(self, mask):
         if mask is None:
             capi.check(self.L.wg_set_mask(self.ctx.h, self.tree, None))
@@ -123,6 +147,23 @@ class Forest:
         if mask.size != self.nblocks * 6 * c.npts:
             raise ValueError("mask has the wrong size")
         capi.check(self.L.wg_set_mask(self.ctx.h, self.tree, _p(mask)))
+
+    def set_mask_sparse(self, blocks, mask):
+        blocks = np.ascontiguousarray(blocks, np.int32)
+        mask = np.ascontiguousarray(mask, np.float64)
+        if mask.size != len(blocks) * 6 * self.cfg.npts:
+            raise ValueError("mask has the wrong size")
+        capi.check(self.L.wg_set_mask_sparse(self.ctx.h, self.tree, len(blocks), _p(blocks, ctypes.c_int), _p(mask)))
+
+    def stats(self):
+        n, m = ctypes.c_int(), ctypes.c_int()
+        capi.check(self.L.wg_tree_stats(self.ctx.h, self.tree, ctypes.byref(n), ctypes.byref(m)))
+        return n.value, m.value
+
+    def time_kernel(self, which: int, reps: int = 20) -> float:
+        ms = ctypes.c_double()
+        capi.check(self.L.wg_time_kernel(self.ctx.h, self.tree, which, reps, ctypes.byref(ms)))
+        return ms.value
 
     # ------------------------------------------------------------------ time
     def set_time(self, t: float):
