@@ -165,6 +165,23 @@ int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph)
  * detail thresholding; flags[b] = -1 (may coarsen) or 0. eps_use holds the
  * per-component threshold (eps * norm). Ghosts must hold g synced layers. */
 int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details);
+/* Allocation-free variant of wg_threshold_flags, for callers that may not
+ * allocate device memory while they run (e.g. a host code with its own
+ * memory pool or an externally enforced device-memory budget). It has no
+ * counterpart in the reference. It takes no context: d_blocks points to nblk
+ * blocks on the device in the hvy_block layout with g synced ghost layers,
+ * contiguous; eps_use (host, neq values) holds the per-component threshold;
+ * d_flags (device, nblk ints) and d_details (device, nblk*neq doubles, or
+ * NULL) receive the result on `stream` (a cudaStream_t, NULL = default).
+ * Its scratch is a file-scope static device array sized for at most 16384
+ * blocks and 8 components (~1.2 MB, held by every device that loads the
+ * library until exit); larger calls are rejected with WG_EINVAL. The first
+ * call on a device resolves the scratch address (cudaGetSymbolAddress) and
+ * fills a block list, synchronising that stream once, so make it before any
+ * stream capture. All calls share the scratch: calls whose work overlaps on
+ * the GPU race. */
+int wg_threshold_flags_noalloc(const wg_config *cfg, int nblk, const double *d_blocks, const double *eps_use,
+                               int *d_flags, double *d_details, void *stream);
 /* refine_tree(..., "everywhere") data part: refineBlock for every block
  * (LIB/MESH/refinementExecute.f90:4-116). Block b becomes blocks
  * 2^d*b .. 2^d*b+2^d-1. Ghosts must hold g synced layers. */

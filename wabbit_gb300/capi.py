@@ -26,6 +26,7 @@ EXPORTS = [
     "wg_refine_everywhere", "wg_sync_table", "wg_block_slot", "wg_sync_table_host",
     "wg_probe_alu", "wg_time_kernel", "wg_tree_stats", "wg_set_mask_sparse",
     "wg_upload_interior", "wg_download_interior", "wg_graph_kernels",
+    "wg_threshold_flags_noalloc",
 ]
 
 
@@ -76,6 +77,7 @@ _SIGS = {
     "wg_upload_interior": (_i, [_vp, _i, _dp]),
     "wg_download_interior": (_i, [_vp, _i, _dp]),
     "wg_graph_kernels": (_i, [_vp]),
+    "wg_threshold_flags_noalloc": (_i, [ctypes.POINTER(WgConfig), _i, _vp, _dp, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -1087,3 +1087,29 @@ int wg_graph_kernels(wg_ctx *ctx) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// Coarsening indicator without any device allocation (see the header).
+int wg_threshold_flags_noalloc(const wg_config *cfg, int nblk, const double *d_blocks, const double *eps_use,
+                               int *d_flags, double *d_details, void *stream) {
+    int st = check_cfg(cfg);
+    if (st) return st;
+    if (nblk < 0 || (nblk && (!d_blocks || !eps_use || !d_flags))) return fail(WG_EINVAL, "bad arguments");
+    if (nblk > noalloc_max_blocks())
+        return fail(WG_EINVAL, "wg_threshold_flags_noalloc handles at most %d blocks per call (got %d)",
+                    noalloc_max_blocks(), nblk);
+    if (cfg->neq > 8) return fail(WG_EINVAL, "at most 8 components");
+    WaveletInfo w;
+    make_wavelet(cfg->wavelet, w);
+    const int dim = cfg->dim;
+    BufGeo geo = {cfg->Bs[0] + 2 * cfg->g, cfg->Bs[1] + 2 * cfg->g, dim == 3 ? cfg->Bs[2] + 2 * cfg->g : 1, cfg->g};
+    cudaError_t e = launch_fwt_flags_noalloc(dim, nblk, d_blocks, geo, cfg->Bs[0], cfg->Bs[1],
+                                             dim == 3 ? cfg->Bs[2] : 1, cfg->neq, w.X, w.Y, eps_use,
+                                             cfg->threshold_state_vector_component, d_flags, d_details,
+                                             (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_fail(e, "wg_threshold_flags_noalloc", __FILE__, __LINE__);
+    return WG_OK;
+}
+
+}  // extern "C"

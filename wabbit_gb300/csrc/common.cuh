@@ -109,6 +109,11 @@ cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGe
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,
                              int Bs2, int nc, int wavelet_x, int wavelet_y, const double *eps_use,
                              const int *tsvc, int *flags, double *details, cudaStream_t s);
+// allocation-free variant (static device scratch, contiguous blocks 0..nblk-1)
+int noalloc_max_blocks();
+cudaError_t launch_fwt_flags_noalloc(int dim, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,
+                                     int nc, int wavelet_x, int wavelet_y, const double *eps_host,
+                                     const int *tsvc_host, int *flags, double *details, cudaStream_t s);
 cudaError_t launch_refine(int dim, const int *parent, int nparent, const int *child_base, const double *u,
                           BufGeo geo, int Bs0, int Bs1, int Bs2, int nc, int order_predictor, cudaStream_t s);
 

@@ -25,6 +25,8 @@ __constant__ double c_hd[32];
 __constant__ double c_gd[32];
 __constant__ int c_flt[4];   // hd_lo, hd_n, gd_lo, gd_n
 
+static int g_flt_key = -1;   // wavelet whose filters sit in constant memory
+
 struct FwtArgs {
     const int *blk;
     const double *u;
@@ -147,8 +149,6 @@ __global__ void flag_kernel(FwtArgs a, const double *detail_scratch, int nblk) {
     a.flags[bi] = all ? -1 : 0;
 }
 
-static int g_flt_key = -1;
-
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,
                              int Bs2, int nc, int wavelet_x, int wavelet_y, const double *eps_use, const int *tsvc,
                              int *flags, double *details, cudaStream_t s) {
@@ -203,6 +203,116 @@ cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u,
 }
 
 cudaError_t wavelet_init() { return init_predictor(); }
+
+// ---------------------------------------------------------------------------
+// Allocation-free coarsening indicator. Callers that must not allocate device
+// memory during a call (a host code that manages its own memory pool, runs
+// under a memory budget enforced outside CUDA, or links the library into a
+// runtime whose allocator it may not call) get a variant of
+// launch_fwt_flags whose per-block detail scratch, block list, thresholds
+// and component groups live in file-scope static device arrays. Every
+// device that loads the library holds these arrays (~1.2 MB) until exit.
+// All calls share them: two calls whose kernels overlap on the GPU race.
+// ---------------------------------------------------------------------------
+#define WG_NOALLOC_MAX_BLOCKS 16384
+#define WG_NOALLOC_MAX_COMP 8
+static __device__ __align__(256) double g_na_detail[WG_NOALLOC_MAX_BLOCKS * WG_NOALLOC_MAX_COMP];
+static __device__ __align__(256) int g_na_blocks[WG_NOALLOC_MAX_BLOCKS];
+static __device__ __align__(256) double g_na_eps[WG_NOALLOC_MAX_COMP];
+static __device__ __align__(256) int g_na_tsvc[WG_NOALLOC_MAX_COMP];
+
+struct NoAllocPtrs {
+    double *detail;
+    int *blocks;
+    double *eps;
+    int *tsvc;
+    bool ready;
+};
+static NoAllocPtrs g_na_ptrs[64];
+
+__global__ void noalloc_iota_kernel(int *b, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = i;
+}
+
+// once per device, with that device current: resolve the device addresses of
+// the static arrays (a host-side name of a __device__ array is not a device
+// address) and fill the identity block list
+static cudaError_t noalloc_setup(int dev, cudaStream_t s) {
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    NoAllocPtrs &p = g_na_ptrs[dev];
+    if (p.ready) return cudaSuccess;
+    cudaError_t e = cudaGetSymbolAddress((void **)&p.detail, g_na_detail);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&p.blocks, g_na_blocks);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&p.eps, g_na_eps);
+    if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&p.tsvc, g_na_tsvc);
+    if (e != cudaSuccess) return e;
+    e = init_predictor();
+    if (e != cudaSuccess) return e;
+    noalloc_iota_kernel<<<64, 256, 0, s>>>(p.blocks, WG_NOALLOC_MAX_BLOCKS);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) p.ready = true;
+    return e;
+}
+
+int noalloc_max_blocks() { return WG_NOALLOC_MAX_BLOCKS; }
+
+cudaError_t launch_fwt_flags_noalloc(int dim, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,
+                                     int nc, int wavelet_x, int wavelet_y, const double *eps_host,
+                                     const int *tsvc_host, int *flags, double *details, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    if (nblk > WG_NOALLOC_MAX_BLOCKS || nc > WG_NOALLOC_MAX_COMP) return cudaErrorInvalidValue;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = noalloc_setup(dev, s);
+    if (e != cudaSuccess) return e;
+    const NoAllocPtrs &P = g_na_ptrs[dev];
+    WaveletInfo w;
+    char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
+    if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
+    // filters, thresholds and groups for this call (no allocation: copies
+    // into constant memory and into the static arrays)
+    double hd[32] = {}, gd[32] = {};
+    for (size_t i = 0; i < w.HD.size(); i++) hd[i] = w.HD[i];
+    for (size_t i = 0; i < w.GD.size(); i++) gd[i] = w.GD[i];
+    int flt[4] = {w.hd_lo, (int)w.HD.size(), w.gd_lo, (int)w.GD.size()};
+    e = cudaMemcpyToSymbolAsync(c_hd, hd, sizeof(hd), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_gd, gd, sizeof(gd), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_flt, flt, sizeof(flt), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(P.eps, eps_host, sizeof(double) * nc, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(P.tsvc, tsvc_host, sizeof(int) * nc, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    g_flt_key = -1;   // the shared filter constants now hold this call's wavelet
+    FwtArgs a;
+    a.blk = P.blocks;
+    a.u = u;
+    a.geo = geo;
+    a.Bs[0] = Bs0;
+    a.Bs[1] = Bs1;
+    a.Bs[2] = Bs2;
+    a.nc = nc;
+    a.lazy = w.lifted ? 0 : 1;
+    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
+    a.fmax = std::max(std::max(w.hd_lo, hd_hi), std::max(w.gd_lo, gd_hi));
+    a.eps_use = P.eps;
+    a.tsvc = P.tsvc;
+    a.flags = flags;
+    a.details = details;
+    if (a.fmax > geo.gb) return cudaErrorInvalidValue;
+    const int ny = Bs1 + 2 * a.fmax, nz = dim == 3 ? Bs2 + 2 * a.fmax : 1;
+    const size_t smem = sizeof(double) * (size_t)Bs0 * ny * nz;
+    if (dim == 2) {
+        e = cudaFuncSetAttribute(fwt_detail_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) fwt_detail_kernel<2><<<nblk * nc, 256, smem, s>>>(a, P.detail);
+    } else {
+        e = cudaFuncSetAttribute(fwt_detail_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) fwt_detail_kernel<3><<<nblk * nc, 256, smem, s>>>(a, P.detail);
+    }
+    if (e != cudaSuccess) return e;
+    flag_kernel<<<(nblk + 127) / 128, 128, 0, s>>>(a, P.detail, nblk);
+    return cudaGetLastError();
+}
 
 // refineBlock: daughter k of parent p is written to slot child_base[p] + k
 __global__ void __launch_bounds__(256) refine_kernel(const int *parent, const int *child_base, const double *u,
