@@ -56,6 +56,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--jmax", type=int, default=None, help="override the workload's Jmax (smaller cases)")
+    ap.add_argument("--precision", choices=["fp64", "fp32"], default=None,
+                    help="RHS stencil precision (default: the workload's; fp32 = double-float on the FP32 units)")
+    ap.add_argument("--compare-plain", action="store_true",
+                    help="also time the plain per-solve FP64 path (one wg_rk4_step call per step, no graph) "
+                         "and report the speed-up and the L2 difference of the two after K steps")
     return ap.parse_args()
 
 
@@ -218,6 +223,8 @@ def run_ours(args, rank, world):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     cfg, lv, co, u0, ids, masks = workloads.build(args.workload, jmax=args.jmax)
+    if args.precision is not None:
+        cfg.rhs_precision = 1 if args.precision == "fp32" else 0
     nblk = len(lv)
     dim = cfg.dim
     npts_blk = int(np.prod([cfg.Bs[d] for d in range(dim)]))
@@ -290,6 +297,10 @@ def run_ours(args, rank, world):
                "h2d_bytes_per_step": int(host_in.nbytes), "d2h_bytes_per_step": int(host_out.nbytes) + 16,
                "steps": k, "path": "wg_upload_interior + wg_rk4_step + wg_download_interior (pinned host)"}
 
+    plain = None
+    if args.compare_plain:
+        plain = compare_plain(args, cfg, lv, co, u0, ids, masks, f, ctx, value / max(world, 1), npts)
+
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         v, cores, sample, _ = cpu_sample(args.workload)
@@ -307,12 +318,13 @@ def run_ours(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f64" if cfg.rhs_precision == 0 else "f64 state, double-float (2xf32) stencils",
         "data": "synthetic (seeded IC and grid, see wabbit_gb300/workloads.py)",
         "config": {
             "workload": args.workload, "dim": dim, "Bs": list(cfg.Bs)[:dim], "g": cfg.g, "g_rhs": cfg.g_rhs,
             "wavelet": cfg.wavelet.decode(), "Jmax": cfg.Jmax, "blocks": nblk, "points": npts,
             "masked_blocks": nmasked, "levels": np.bincount(lv).tolist(), "variant": args.variant,
+            "rhs_precision": "fp64" if cfg.rhs_precision == 0 else "fp32-pipe double-float",
             "rk": "RK4", "graph": True, "l2": "state 2.9 GB > 129 MB L2 (no flush needed)" if dim == 3 else
             "inputs smaller than L2",
             "parallelism": "replicas" if world > 1 else "1 GPU",
@@ -333,11 +345,56 @@ def run_ours(args, rank, world):
     }
     if e2e is not None:
         line["e2e"] = e2e
+    if plain is not None:
+        line["plain_fp64"] = plain
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
+
+
+def compare_plain(args, cfg, lv, co, u0, ids, masks, f, ctx, value, npts):
+    """Plain per-solve FP64 path on the same grid and IC: one wg_rk4_step call
+    per step, no graph. Also runs the measured configuration and the plain
+    one for K steps from the same state and reports their relative L2
+    difference (the FP64 path reproduces the oracle to 1e-12 per step)."""
+    import torch
+    from wabbit_gb300.solver import Context
+    c64 = cfg.copy()
+    c64.rhs_precision = 0
+    ctx64 = Context(c64, len(lv) + 16)
+    g = ctx64.forest()
+    g.set_grid(lv, co)
+    g.upload_interior(u0)
+    if masks is not None and len(ids):
+        g.set_mask_sparse(ids, masks)
+    g.set_time(0.0)
+    for _ in range(max(args.warmup, 1)):
+        g.timeStep_tree()
+    ctx64.synchronize()
+    k = args.steps
+    t0 = time.perf_counter()
+    for _ in range(k):
+        g.timeStep_tree()
+    ctx64.synchronize()
+    el = time.perf_counter() - t0
+    v_plain = npts * k / el
+    # accuracy: both from the IC for K steps
+    g.upload_interior(u0)
+    g.set_time(0.0)
+    f.upload_interior(u0)
+    f.set_time(0.0)
+    for _ in range(k):
+        g.timeStep_tree()
+    f.run(k, use_graph=True)
+    ctx.synchronize()
+    a = f.download_interior()
+    b = g.download_interior()
+    err = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    ctx64.close()
+    return {"value": v_plain, "unit": "point-updates/s", "speedup": value / v_plain, "steps": k,
+            "rel_l2_after_steps": err, "path": "FP64 strict-order-free fast stencils, wg_rk4_step per step, no graph"}
 
 
 def capi_graph_kernels(ctx):

@@ -27,6 +27,7 @@ UNITS = {
     "k_acm_strict.cu": ["-fmad=false"],
     "k_acm_fast.cu": [],
     "k_probe.cu": [],
+    "k_acm_df.cu": ["-fmad=false"],
 }
 
 

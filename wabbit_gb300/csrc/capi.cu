@@ -80,6 +80,7 @@ struct Tree {
     int n_plain = 0, n_masked = 0;
     std::map<long long, std::unique_ptr<SyncPlan>> sync;   // key: gm, gp, buffer
     double time = 0.0;
+    bool shadow_valid = false;         // double-float copy of u_n in B is current
 };
 
 }  // namespace wg
@@ -106,6 +107,7 @@ struct wg_ctx {
     std::vector<int> free_slots;
     cudaStream_t stream = nullptr;
     int variant_fast = 1;               // 1: FMA stencil, 0: strict reference arithmetic
+    int precision = WG_RHS_FP64;        // WG_RHS_FP32: double-float stencils on the FP32 units
     DevArray<int> d_tree_ids;
     double *staging = nullptr;          // compact interior staging buffer
     size_t staging_bytes = 0;
@@ -133,7 +135,18 @@ int check_cfg(const wg_config *c) {
     for (int d = 0; d < c->dim; d++)
         if (2 * c->g - 1 > c->Bs[d]) return fail(WG_EINVAL, "Bs=%d too small for g=%d (need Bs >= 2g-1)", c->Bs[d], c->g);
     if (c->Jmin < 0 || c->Jmax < c->Jmin || c->Jmax > 18) return fail(WG_EINVAL, "bad Jmin/Jmax");
+    if (c->rhs_precision != WG_RHS_FP64 && c->rhs_precision != WG_RHS_FP32)
+        return fail(WG_EINVAL, "rhs_precision must be WG_RHS_FP64 or WG_RHS_FP32");
+    if (c->rhs_precision == WG_RHS_FP32 && c->skew_symmetry)
+        return fail(WG_ENOTSUP, "the FP32 stencil path implements the convective form only (skew_symmetry=0)");
     return WG_OK;
+}
+
+// double -> (hi, lo) float pair
+void split_df(double v, float out[2]) {
+    const float h = (float)v;
+    out[0] = h;
+    out[1] = (float)(v - (double)h);
 }
 
 TreeParams make_params(const wg_config &c) {
@@ -158,6 +171,8 @@ TreeParams make_params(const wg_config &c) {
     p.penalization = c.penalization;
     p.use_sponge = c.use_sponge;
     p.skew = c.skew_symmetry;
+    split_df(c.c0 * c.c0, p.f_c0sq);
+    split_df(c.gamma_p, p.f_gamma);
     return p;
 }
 
@@ -190,14 +205,19 @@ int get_sync(wg_ctx *ctx, Tree &t, int gm, int gp, bool thin, SyncPlan **out) {
     return WG_OK;
 }
 
-int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp) {
+int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool df = false) {
     SyncPlan *sp;
     int st = get_sync(ctx, t, gm, gp, thin, &sp);
     if (st) return st;
     const BufGeo geo = thin ? ctx->gT : ctx->gA;
     for (int s = 0; s < sp->table.nstages; s++) {
         const int b = sp->table.stage_begin[s], e = sp->table.stage_begin[s + 1];
-        if (sp->table.stage_predict[s])
+        // copies and decimations move 8-byte elements: the same kernel serves
+        // FP64 and double-float buffers; predictions convert
+        if (sp->table.stage_predict[s] && df)
+            WG_CUDA_OK(launch_predict_df(sp->d.p + b, e - b, sp->table.max_coarse, buf, geo, ctx->geo.nc,
+                                         ctx->wav.order_predictor, ctx->stream));
+        else if (sp->table.stage_predict[s])
             WG_CUDA_OK(launch_predict(sp->d.p + b, e - b, sp->table.max_coarse, buf, geo, ctx->geo.nc,
                                       ctx->wav.order_predictor, ctx->stream));
         else
@@ -244,6 +264,13 @@ int upload_desc(wg_ctx *ctx, Tree &t, int tree_id) {
             d.m2[k] = nu * (1.0 / 12.0) / (d.dx[k] * d.dx[k]);
             d.m0 += nu * (-2.5) / (d.dx[k] * d.dx[k]);
         }
+        for (int k = 0; k < 3; k++) {
+            split_df(d.k1[k], d.fk1[k]);
+            split_df(d.k2[k], d.fk2[k]);
+            split_df(d.m1[k], d.fm1[k]);
+            split_df(d.m2[k], d.fm2[k]);
+        }
+        split_df(d.m0, d.fm0);
         d.tree = tree_id;
         d.level = lv;
         d.mask = t.mask_slot[b];
@@ -266,8 +293,54 @@ int stage_launch(wg_ctx *ctx, Tree &t, int stage, const double *in, BufGeo gin, 
     return WG_OK;
 }
 
+int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *out) {
+    const int dim = ctx->cfg.dim;
+    const int *Bs = ctx->cfg.Bs;
+    WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, t.d_plain.p, t.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
+                                   ctx->gT, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask, Bs[0], Bs[1], Bs[2],
+                                   ctx->geo.nc, ctx->stream));
+    WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, t.d_masked.p, t.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
+                                   ctx->gT, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask, Bs[0], Bs[1], Bs[2],
+                                   ctx->geo.nc, ctx->stream));
+    return WG_OK;
+}
+
+// double-float copy of u_n (interior of A) into B, needed once after the
+// state changed outside an RK step
+int ensure_shadow(wg_ctx *ctx, Tree &t) {
+    if (ctx->precision != WG_RHS_FP32 || t.shadow_valid) return WG_OK;
+    const int *Bs = ctx->cfg.Bs;
+    WG_CUDA_OK(launch_shadow(t.d_all.p, (int)t.slots.size(), ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0],
+                             Bs[1], ctx->cfg.dim == 3 ? Bs[2] : 1, ctx->stream));
+    t.shadow_valid = true;
+    return WG_OK;
+}
+
+// one RK4 step with double-float stencils: B holds the double-float copy of
+// u_n; stage inputs alternate C, B, C; stage 4 writes u_{n+1} to A and its
+// copy to B
+int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
+    Tree &t = ctx->trees[tree_id];
+    const int g_rhs = ctx->cfg.g_rhs;
+    const int *Bs = ctx->cfg.Bs;
+    int st;
+    if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true))) return st;
+    WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
+                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream));
+    if ((st = stage_launch_df(ctx, t, 1, ctx->B, ctx->C))) return st;
+    if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true))) return st;
+    if ((st = stage_launch_df(ctx, t, 2, ctx->C, ctx->B))) return st;
+    if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true))) return st;
+    if ((st = stage_launch_df(ctx, t, 3, ctx->B, ctx->C))) return st;
+    if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true))) return st;
+    if ((st = stage_launch_df(ctx, t, 4, ctx->C, ctx->B))) return st;
+    WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
+    return WG_OK;
+}
+
 // one RK4 step of one tree, fully asynchronous on ctx->stream
 int rk4_enqueue(wg_ctx *ctx, int tree_id) {
+    if (ctx->precision == WG_RHS_FP32) return rk4_enqueue_df(ctx, tree_id);
     Tree &t = ctx->trees[tree_id];
     const int g_rhs = ctx->cfg.g_rhs;
     const int *Bs = ctx->cfg.Bs;
@@ -344,6 +417,7 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
     if (max_blocks <= 0) return fail(WG_EINVAL, "max_blocks must be positive");
     std::unique_ptr<wg_ctx> ctx(new wg_ctx());
     ctx->cfg = *cfg;
+    ctx->precision = cfg->rhs_precision;
     ctx->geo.dim = cfg->dim;
     for (int d = 0; d < 3; d++) ctx->geo.Bs[d] = d < cfg->dim ? cfg->Bs[d] : 1;
     ctx->geo.g = cfg->g;
@@ -475,6 +549,7 @@ int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *co
     if (!t->forest.graded()) return fail(WG_EGRID, "grid is not graded (level jump > 1 between neighbours)");
     t->slots.resize(nblk);
     t->mask_slot.assign(nblk, -1);
+    t->shadow_valid = false;
     for (int b = 0; b < nblk; b++) {
         t->slots[b] = ctx->free_slots.back();
         ctx->free_slots.pop_back();
@@ -514,6 +589,7 @@ static bool contiguous(const std::vector<int> &s) {
 int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !host_blocks) return fail(WG_EINVAL, "bad arguments");
+    t->shadow_valid = false;
     const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
     if (!t->slots.empty() && contiguous(t->slots)) {
         WG_CUDA_OK(cudaMemcpyAsync((char *)ctx->A + per * t->slots[0], host_blocks, per * t->slots.size(),
@@ -706,7 +782,9 @@ int wg_compute_dt(wg_ctx *ctx, int tree, double *dt) {
 int wg_rk4_step(wg_ctx *ctx, int tree, double *time, double *dt) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return WG_EINVAL;
-    int st = rk4_enqueue(ctx, tree);
+    int st = ensure_shadow(ctx, *t);
+    if (st) return st;
+    st = rk4_enqueue(ctx, tree);
     if (st) return st;
     if (time || dt) return wg_get_time(ctx, tree, time, dt);
     return WG_OK;
@@ -716,8 +794,12 @@ int wg_rk4_step(wg_ctx *ctx, int tree, double *time, double *dt) {
 // use_graph the per-step launch sequence is captured once and replayed
 int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph) {
     if (!ctx || ntrees <= 0 || !trees || nsteps < 0) return fail(WG_EINVAL, "bad arguments");
-    for (int i = 0; i < ntrees; i++)
-        if (!get_tree(ctx, trees[i])) return WG_EINVAL;
+    for (int i = 0; i < ntrees; i++) {
+        Tree *t = get_tree(ctx, trees[i]);
+        if (!t) return WG_EINVAL;
+        int st = ensure_shadow(ctx, *t);
+        if (st) return st;
+    }
     if (!use_graph) {
         for (int s = 0; s < nsteps; s++)
             for (int i = 0; i < ntrees; i++) {
@@ -857,6 +939,7 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     ctx->free_slots = nf;
     t->slots = slots;
     t->mask_slot.assign(nb * nd, -1);
+    t->shadow_valid = false;
     t->sync.clear();
     t->forest.set(nb * nd, lv.data(), co.data());
     std::string err;
@@ -984,8 +1067,9 @@ int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_la
     WG_CUDA_OK(cudaEventCreate(&e0));
     WG_CUDA_OK(cudaEventCreate(&e1));
     auto once = [&]() -> int {
+        if (which == 0 && ctx->precision == WG_RHS_FP32) return stage_launch_df(ctx, *t, 2, ctx->C, ctx->B);
         if (which == 0) return stage_launch(ctx, *t, 2, ctx->B, ctx->gT, ctx->C, ctx->gT);
-        if (which == 1) return run_sync(ctx, *t, ctx->B, true, g_rhs, g_rhs);
+        if (which == 1) return run_sync(ctx, *t, ctx->B, true, g_rhs, g_rhs, ctx->precision == WG_RHS_FP32);
         WG_CUDA_OK(launch_dt(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk,
                              ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, ctx->stream));
         return WG_OK;
@@ -1001,6 +1085,7 @@ int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_la
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms_per_launch = ms / reps;
+    if (which == 0) t->shadow_valid = false;   // the timed stage wrote over B
     return WG_OK;
 }
 
@@ -1038,6 +1123,7 @@ extern "C" {
 int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !host) return fail(WG_EINVAL, "bad arguments");
+    t->shadow_valid = false;
     const int *Bs = ctx->cfg.Bs;
     const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
     const size_t bytes = sizeof(double) * t->slots.size() * ctx->geo.nc * ctx->nint;

@@ -18,6 +18,7 @@ struct TreeParams {
     double dt_fixed, dt_max, time_max, write_time, tsave_stats;
     int    penalization, use_sponge, skew;
     int    pad;
+    float  f_c0sq[2], f_gamma[2];   // c0^2 and gamma_p as double-float pairs
 };
 
 // Per-tree time state on the device.
@@ -35,6 +36,8 @@ struct TreeClock {
 struct BlockDesc {
     double dx[3];
     double k1[3], k2[3], m1[3], m2[3], m0;
+    // the same weights as double-float pairs (hi, lo) for the FP32-pipe path
+    float fk1[3][2], fk2[3][2], fm1[3][2], fm2[3][2], fm0[2];
     int32_t tree;
     int32_t level;
     int32_t mask;                // slot in the mask pool, -1 = no mask
@@ -97,6 +100,18 @@ cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, in
                              const TreeParams *tp, const TreeClock *clk, const double *in, BufGeo gin,
                              double *out, BufGeo gout, double *un, BufGeo gun, double *acc, const double *mask,
                              int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s);
+// double-float stage kernel (FP32-pipe stencils, FP64 RK state): in/out are
+// float2 (hi, lo) buffers; stage 4 writes u_{n+1} to un (FP64) and its
+// double-float copy to out
+cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
+                                const TreeParams *tp, const TreeClock *clk, const void *in, BufGeo gin, void *out,
+                                BufGeo gout, double *un, BufGeo gun, double *acc, const double *mask, int Bs0,
+                                int Bs1, int Bs2, int nc, cudaStream_t s);
+// double-float copy of the interiors of the listed blocks of an FP64 buffer
+cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
+                          int Bs0, int Bs1, int Bs2, cudaStream_t s);
+cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
+                              int order_predictor, cudaStream_t s);
 cudaError_t launch_rhs_only(int variant, int dim, const int *blk, int nblk, const BlockDesc *desc,
                             const TreeParams *tp, const double *in, BufGeo gin, double *rhs, const double *mask,
                             int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s);

@@ -18,6 +18,8 @@
 
 namespace wg {
 
+// Copy and restriction patches: one warp per patch, one lane per receiver
+// row (x fastest), so the index arithmetic is one division per row.
 __global__ void __launch_bounds__(128) sync_kernel(const Patch *__restrict__ patches, int npatch, double *buf,
                                                    BufGeo geo, int nc, int order_idx, int ncoef) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -25,39 +27,24 @@ __global__ void __launch_bounds__(128) sync_kernel(const Patch *__restrict__ pat
     if (warp >= npatch) return;
     const Patch p = patches[warp];
     const int ex = p.rhi[0] - p.rlo[0] + 1, ey = p.rhi[1] - p.rlo[1] + 1, ez = p.rhi[2] - p.rlo[2] + 1;
-    const int n = ex * ey * ez;
     const long long npts = geo.npts();
     double *dst = buf + (long long)p.dst * nc * npts;
     const double *src = buf + (long long)p.src * nc * npts;
-    for (int q = lane; q < n; q += 32) {
-        const int ix = q % ex, iy = (q / ex) % ey, iz = q / (ex * ey);
-        const long long di = ((long long)(p.rlo[2] + iz) * geo.ny + (p.rlo[1] + iy)) * geo.nx + (p.rlo[0] + ix);
-        if (p.op == 0) {
-            const long long si = ((long long)(p.slo[2] + iz) * geo.ny + (p.slo[1] + iy)) * geo.nx + (p.slo[0] + ix);
-            for (int c = 0; c < nc; c++) dst[c * npts + di] = src[c * npts + si];
-        } else if (p.op == 1) {
-            const int sx = p.slo[0] + 2 * (p.blo[0] + ix);
-            const int sy = p.slo[1] + 2 * (p.blo[1] + iy);
-            const int sz = p.slo[2] + 2 * (p.blo[2] + iz);
-            const long long si = ((long long)sz * geo.ny + sy) * geo.nx + sx;
-            for (int c = 0; c < nc; c++) dst[c * npts + di] = src[c * npts + si];
-        } else {
-            PredCtx pc;
-            pc.nx = geo.nx;
-            pc.ny = geo.ny;
-            pc.sx = p.slo[0];
-            pc.sy = p.slo[1];
-            pc.sz = p.slo[2];
-            pc.Fx = 2 * (p.shi[0] - p.slo[0] + 1) - 1;
-            pc.Fy = 2 * (p.shi[1] - p.slo[1] + 1) - 1;
-            pc.Fz = 2 * (p.shi[2] - p.slo[2] + 1) - 1;
-            pc.nc = ncoef;
-            pc.c = c_pred[order_idx];
-            const int fx = p.blo[0] + ix, fy = p.blo[1] + iy, fz = p.blo[2] + iz;
-            for (int c = 0; c < nc; c++) {
-                pc.src = src + c * npts;
-                dst[c * npts + di] = pred_xyz(pc, fx, fy, fz);
-            }
+    const int step = p.op == 1 ? 2 : 1;
+    const int rows = ey * ez;
+    for (int r = lane; r < rows; r += 32) {
+        const int iy = r % ey, iz = r / ey;
+        const long long di = ((long long)(p.rlo[2] + iz) * geo.ny + (p.rlo[1] + iy)) * geo.nx + p.rlo[0];
+        long long si;
+        if (p.op == 0)
+            si = ((long long)(p.slo[2] + iz) * geo.ny + (p.slo[1] + iy)) * geo.nx + p.slo[0];
+        else
+            si = ((long long)(p.slo[2] + 2 * (p.blo[2] + iz)) * geo.ny + (p.slo[1] + 2 * (p.blo[1] + iy))) * geo.nx +
+                 p.slo[0] + 2 * p.blo[0];
+        for (int c = 0; c < nc; c++) {
+            const double *sr = src + c * npts + si;
+            double *dr = dst + c * npts + di;
+            for (int ix = 0; ix < ex; ix++) dr[ix] = sr[step * ix];
         }
     }
 }
@@ -74,6 +61,27 @@ __device__ __forceinline__ double interp_line(const double *c, const double *v, 
     return s;
 }
 
+// storage of a sync buffer element: FP64, or a double-float pair (hi, lo)
+// held in the same 8 bytes (FP32-pipe path); predictions are always
+// evaluated in FP64
+template <bool DF>
+__device__ __forceinline__ double load_el(const double *p) {
+    if (!DF) return *p;
+    const float2 v = *reinterpret_cast<const float2 *>(p);
+    return (double)v.x + (double)v.y;
+}
+
+template <bool DF>
+__device__ __forceinline__ void store_el(double *p, double v) {
+    if (!DF) {
+        *p = v;
+        return;
+    }
+    const float h = __double2float_rn(v);
+    *reinterpret_cast<float2 *>(p) = make_float2(h, __double2float_rn(v - (double)h));
+}
+
+template <bool DF>
 __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ patches, double *buf, BufGeo geo,
                                                       int nc, int order_idx, int ncoef) {
     extern __shared__ double sm[];
@@ -103,7 +111,7 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
         double *dst = buf + ((long long)p.dst * nc + c) * npts;
         for (int i = threadIdx.x; i < ncp; i += blockDim.x) {
             const int x = i % cx, y = (i / cx) % cy, z = i / (cx * cy);
-            C[i] = src[((long long)(p.slo[2] + z) * geo.ny + (p.slo[1] + y)) * geo.nx + (p.slo[0] + x)];
+            C[i] = load_el<DF>(src + ((long long)(p.slo[2] + z) * geo.ny + (p.slo[1] + y)) * geo.nx + (p.slo[0] + x));
         }
         __syncthreads();
         // x pass on even rows / planes
@@ -139,7 +147,7 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
             if (!(fz & 1)) v = pl[(long long)((fz - zw0) >> 1) * ex * ey];
             else if (fz < h || fz > Fz - 1 - h) v = 0.0;
             else v = interp_line(cf, pl, ex * ey, (fz - h - zw0) >> 1, ncoef);
-            dst[((long long)(p.rlo[2] + k) * geo.ny + (p.rlo[1] + j)) * geo.nx + (p.rlo[0] + ix)] = v;
+            store_el<DF>(dst + ((long long)(p.rlo[2] + k) * geo.ny + (p.rlo[1] + j)) * geo.nx + (p.rlo[0] + ix), v);
         }
         __syncthreads();
     }
@@ -153,11 +161,26 @@ cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_double
     const size_t smem = sizeof(double) * (size_t)max_smem_doubles;
     static size_t attr = 0;
     if (smem > 48 * 1024 && smem > attr) {
-        cudaError_t e = cudaFuncSetAttribute(predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(predict_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr = smem;
     }
-    predict_kernel<<<npatch, 256, smem, s>>>(patches, buf, geo, nc, order_predictor / 2 - 1, order_predictor);
+    predict_kernel<false><<<npatch, 256, smem, s>>>(patches, buf, geo, nc, order_predictor / 2 - 1, order_predictor);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
+                              int order_predictor, cudaStream_t s) {
+    if (npatch <= 0) return cudaSuccess;
+    const size_t smem = sizeof(double) * (size_t)max_smem_doubles;
+    static size_t attr = 0;
+    if (smem > 48 * 1024 && smem > attr) {
+        cudaError_t e = cudaFuncSetAttribute(predict_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = smem;
+    }
+    predict_kernel<true><<<npatch, 256, smem, s>>>(patches, reinterpret_cast<double *>(buf), geo, nc,
+                                                   order_predictor / 2 - 1, order_predictor);
     return cudaGetLastError();
 }
 

@@ -14,7 +14,9 @@ the measurements are quoted on:
   cosine-smoothed mask (C_smooth = 1.5 dx_min); IC: u = (1,0,0) + 0.01 N(0,1)
   per point and component (seed 2), p = 0. Grid: refined around the sphere
   with level-dependent radii (about 4k blocks at Jmax=6).
-* ``acm3d_sphere_j7`` -- the same at Jmax=7 (about 30k blocks).
+* ``acm3d_sphere_j7`` -- the same at Jmax=7 with the stencils evaluated in
+  double-float arithmetic on the FP32 units (FP64 RK state, FP64
+  penalisation).
 
 All random draws use numpy's PCG64 generator with the stated seed, in block
 order, component order, then point order (x fastest).
@@ -50,6 +52,8 @@ def make_config(name: str):
         c.g, c.g_rhs = 6, 2
         c.Jmin = 2
         c.Jmax = 7 if name.endswith("j7") else 6
+        # config 3: FP32-pipe stencils (double-float) with FP64 RK state
+        c.rhs_precision = 1 if name.endswith("j7") else 0
         c.nu, c.c0, c.gamma_p = 1e-3, 15.0, 1.0
         c.penalization, c.C_eta = 1, 1e-3
         c.CFL = 0.5
