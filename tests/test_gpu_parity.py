@@ -224,12 +224,16 @@ def test_threshold_flags_bitexact(dim, wavelet, grids2d, grids3d):
     assert (fl == -1).any() and (fl == 0).any()
 
 
-@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("dim,wavelet", [(2, "CDF40"), (3, "CDF40"), (2, "CDF44"), (3, "CDF44")])
 @pytest.mark.parametrize("penal", [0, 1])
-def test_rk4_fp32_pipe_path_within_tolerance(dim, penal, grids2d, grids3d):
-    """Double-float stencils on the FP32 units with FP64 RK state and FP64
-    penalisation: relative L2 <= 1e-12 per step against the FP64 oracle."""
-    cfg = small_cfg(dim, skew=0, penal=penal, jmin=1 if dim == 3 else 2, jmax=3 if dim == 3 else 5)
+def test_rk4_fp32_pipe_path_within_tolerance(dim, wavelet, penal, grids2d, grids3d):
+    """Double-float stencils, stage arithmetic, ghost prediction and
+    penalisation on the FP32 units, FP64 state: relative L2 <= 1e-12 per step
+    against the FP64 oracle. The ghost nodes go through the pushed same-level
+    copies and the restriction / prediction stages (CDF40: two sync stages,
+    CDF44: three)."""
+    cfg = small_cfg(dim, wavelet, Bs=8 if wavelet == "CDF40" else 12, skew=0, penal=penal,
+                    jmin=1 if dim == 3 else 2, jmax=3 if dim == 3 else 5)
     cfg.C_eta = 1e-2
     cfg.rhs_precision = 1
     lv, co = grids2d if dim == 2 else grids3d

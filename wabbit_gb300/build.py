@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "forest.cpp": [],
     "capi.cu": [],
-    "k_sync.cu": [],
+    "k_sync.cu": ["-fmad=false"],
     "k_misc.cu": [],
     "k_wavelet.cu": [],
     "k_acm_strict.cu": ["-fmad=false"],

@@ -9,8 +9,12 @@
 // Device buffers per block slot:
 //   A    full layout (ghost width g): the state u (hvy_block)
 //   B, C thin layout (ghost width g_rhs): RK stage inputs
-//   acc  interior only: u_n + dt*sum b_j k_j (the RK accumulator)
-//   mask interior only, 6 components, only for blocks that carry a mask
+//   D    thin layout, FP32-pipe precision only: third stage-input buffer
+//        (B keeps the double-float copy of u_n through the step)
+//   acc  interior only: u_n + dt*sum b_j k_j (the RK accumulator; in the
+//        FP32-pipe precision the double-float increment dt*sum b_j k_j)
+//   mask interior only, 6 components, only for blocks that carry a mask;
+//        the FP32-pipe precision adds a double-float copy (5 components)
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -59,7 +63,7 @@ struct DevArray {
             cap = count;
         }
         n = count;
-        if (!count) return cudaSuccess;
+        if (!count || !h) return cudaSuccess;
         return cudaMemcpyAsync(p, h, sizeof(T) * count, cudaMemcpyHostToDevice, s);
     }
 };
@@ -67,6 +71,15 @@ struct DevArray {
 struct SyncPlan {
     SyncTable table;
     DevArray<Patch> d;
+    // gather form of the copy / restriction stages (empty: patch kernel)
+    DevArray<Patch> order;             // patches in expansion order (copies first per stage)
+    DevArray<unsigned> first;          // per patch of order: offset of its first point in its stage
+    DevArray<uint2> pairs;             // (receiver, sender) offsets, all stages
+    std::vector<unsigned> pair_begin;  // nstages+1 offsets into pairs
+    std::vector<unsigned> copy_end;    // per stage: end of its copy entries
+    // every copy patch is a same-level translation of a full ghost region:
+    // the stage kernels may write these ghost nodes themselves (ctx->d_push)
+    bool push_ok = false;
 };
 
 struct Tree {
@@ -94,8 +107,11 @@ struct wg_ctx {
     int max_blocks = 0;
     BufGeo gA, gT;                      // full and thin layouts
     long long nint = 0;                 // interior points per block
-    double *A = nullptr, *B = nullptr, *C = nullptr, *acc = nullptr;
+    double *A = nullptr, *B = nullptr, *C = nullptr, *D = nullptr, *acc = nullptr;
     double *mask = nullptr;
+    float2 *mask_df = nullptr;
+    int *d_push = nullptr;              // per slot 27 same-level receivers (FP32-pipe precision)
+    std::vector<int> h_push;
     int mask_cap = 0;
     std::vector<int> mask_free;
     BlockDesc *d_desc = nullptr;
@@ -173,6 +189,7 @@ TreeParams make_params(const wg_config &c) {
     p.skew = c.skew_symmetry;
     split_df(c.c0 * c.c0, p.f_c0sq);
     split_df(c.gamma_p, p.f_gamma);
+    for (int i = 0; i < 3; i++) split_df(c.u_mean_set[i], p.f_umean[i]);
     return p;
 }
 
@@ -185,6 +202,54 @@ Tree *get_tree(wg_ctx *ctx, int t) {
 }
 
 long long sync_key(int gm, int gp, int thin) { return ((long long)gm << 20) | ((long long)gp << 4) | thin; }
+
+// Check that every copy patch of a thin per-step plan is a same-level
+// translation of a full ghost region (the form push_ghosts writes) and, if
+// so, record per sender slot the receiver slot of each direction.
+int build_push(wg_ctx *ctx, Tree &t, SyncPlan &sp, const BufGeo &geo) {
+    const int gb = geo.gb, dim = ctx->cfg.dim;
+    const int *Bs = ctx->cfg.Bs;
+    std::vector<int> row_of(ctx->max_blocks, -1);
+    for (size_t i = 0; i < t.slots.size(); i++) row_of[t.slots[i]] = (int)i;
+    std::vector<int> rows(t.slots.size() * 27, -1);
+    bool ok = true;
+    for (const Patch &p : sp.table.patches) {
+        if (p.op != 0) continue;
+        int D[3] = {0, 0, 0};
+        for (int a = 0; a < 3 && ok; a++) {
+            const int r0 = p.rlo[a], r1 = p.rhi[a], s0 = p.slo[a], s1 = p.shi[a];
+            if (a >= dim) {
+                ok = r0 == 0 && r1 == 0 && s0 == 0 && s1 == 0;
+                continue;
+            }
+            const int B = Bs[a];
+            if (r0 == gb && r1 == gb + B - 1 && s0 == gb && s1 == gb + B - 1) D[a] = 0;
+            else if (r0 == gb + B && r1 == gb + B + gb - 1 && s0 == gb && s1 == 2 * gb - 1) D[a] = -1;
+            else if (r0 == 0 && r1 == gb - 1 && s0 == B && s1 == gb + B - 1) D[a] = 1;
+            else ok = false;
+        }
+        if (!ok) break;
+        const int r = p.src >= 0 && p.src < ctx->max_blocks ? row_of[p.src] : -1;
+        const int k = (D[2] + 1) * 9 + (D[1] + 1) * 3 + (D[0] + 1);
+        if (r < 0 || k == 13 || rows[(size_t)r * 27 + k] != -1) {
+            ok = false;
+            break;
+        }
+        rows[(size_t)r * 27 + k] = p.dst;
+    }
+    sp.push_ok = ok;
+    if (!ok || t.slots.empty()) return WG_OK;
+    int lo = ctx->max_blocks, hi = -1;
+    for (size_t i = 0; i < t.slots.size(); i++) {
+        std::memcpy(&ctx->h_push[(size_t)t.slots[i] * 27], &rows[i * 27], sizeof(int) * 27);
+        lo = std::min(lo, t.slots[i]);
+        hi = std::max(hi, t.slots[i]);
+    }
+    WG_CUDA_OK(cudaMemcpyAsync(ctx->d_push + (size_t)lo * 27, &ctx->h_push[(size_t)lo * 27],
+                               sizeof(int) * 27 * (size_t)(hi - lo + 1), cudaMemcpyHostToDevice, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
 
 int get_sync(wg_ctx *ctx, Tree &t, int gm, int gp, bool thin, SyncPlan **out) {
     const long long key = sync_key(gm, gp, thin ? 1 : 0);
@@ -199,13 +264,66 @@ int get_sync(wg_ctx *ctx, Tree &t, int gm, int gp, bool thin, SyncPlan **out) {
             p.dst = t.slots[p.dst];
         }
         WG_CUDA_OK(sp->d.upload(sp->table.patches.data(), sp->table.patches.size(), ctx->stream));
+        // the per-step syncs (g_rhs layers) get the gather form when every
+        // element offset of the buffer fits 32 bits
+        const BufGeo geo = thin ? ctx->gT : ctx->gA;
+        const unsigned long long elems = (unsigned long long)ctx->max_blocks * ctx->geo.nc * geo.npts();
+        if (gm == ctx->cfg.g_rhs && gp == ctx->cfg.g_rhs && elems < (1ull << 32)) {
+            const SyncTable &tb = sp->table;
+            const auto &pt = tb.patches;
+            std::vector<Patch> order;
+            std::vector<unsigned> first;
+            std::vector<int> order_begin(tb.nstages + 1, 0);
+            unsigned long long run = 0;
+            sp->pair_begin.assign(tb.nstages + 1, 0);
+            sp->copy_end.assign(tb.nstages, 0);
+            for (int st = 0; st < tb.nstages; st++) {
+                sp->pair_begin[st] = (unsigned)run;
+                order_begin[st] = (int)order.size();
+                sp->copy_end[st] = (unsigned)run;
+                if (tb.stage_predict[st]) continue;
+                for (int pass = 0; pass < 2; pass++) {
+                    for (int i = tb.stage_begin[st]; i < tb.stage_begin[st + 1]; i++) {
+                        if ((pt[i].op == 0) != (pass == 0)) continue;
+                        order.push_back(pt[i]);
+                        first.push_back((unsigned)(run - sp->pair_begin[st]));
+                        run += (unsigned long long)(pt[i].rhi[0] - pt[i].rlo[0] + 1) *
+                               (pt[i].rhi[1] - pt[i].rlo[1] + 1) * (pt[i].rhi[2] - pt[i].rlo[2] + 1);
+                    }
+                    if (pass == 0) sp->copy_end[st] = (unsigned)run;
+                }
+            }
+            order_begin[tb.nstages] = (int)order.size();
+            sp->pair_begin[tb.nstages] = (unsigned)run;
+            if (run < (1ull << 32)) {
+                WG_CUDA_OK(sp->order.upload(order.data(), order.size(), ctx->stream));
+                WG_CUDA_OK(sp->first.upload(first.data(), first.size(), ctx->stream));
+                WG_CUDA_OK(sp->pairs.upload(nullptr, run, ctx->stream));
+                for (int st = 0; st < tb.nstages; st++) {
+                    const int b = order_begin[st], e = order_begin[st + 1];
+                    if (e == b) continue;
+                    const unsigned n = sp->pair_begin[st + 1] - sp->pair_begin[st];
+                    WG_CUDA_OK(launch_expand(sp->order.p + b, sp->first.p + b, e - b, n, geo, ctx->geo.nc,
+                                             sp->pairs.p + sp->pair_begin[st], ctx->stream));
+                }
+                WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+                if (thin && ctx->d_push && gm == geo.gb) {
+                    int st2 = build_push(ctx, t, *sp, geo);
+                    if (st2) return st2;
+                }
+            } else {
+                sp->pair_begin.clear();
+            }
+        }
         it = t.sync.emplace(key, std::move(sp)).first;
     }
     *out = it->second.get();
     return WG_OK;
 }
 
-int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool df = false) {
+// skip_copies: the same-level copies were written by the kernel that wrote
+// buf's interiors (push); only restrictions and predictions remain
+int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool df = false, bool skip_copies = false) {
     SyncPlan *sp;
     int st = get_sync(ctx, t, gm, gp, thin, &sp);
     if (st) return st;
@@ -220,6 +338,11 @@ int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool 
         else if (sp->table.stage_predict[s])
             WG_CUDA_OK(launch_predict(sp->d.p + b, e - b, sp->table.max_coarse, buf, geo, ctx->geo.nc,
                                       ctx->wav.order_predictor, ctx->stream));
+        else if (!sp->pair_begin.empty()) {
+            const unsigned from = skip_copies && sp->push_ok ? sp->copy_end[s] : sp->pair_begin[s];
+            WG_CUDA_OK(launch_gather(sp->pairs.p + from, sp->pair_begin[s + 1] - from, buf, geo, ctx->geo.nc,
+                                     ctx->stream));
+        }
         else
             WG_CUDA_OK(launch_sync(sp->d.p + b, e - b, buf, geo, ctx->geo.nc, ctx->wav.order_predictor, ctx->stream));
     }
@@ -264,13 +387,14 @@ int upload_desc(wg_ctx *ctx, Tree &t, int tree_id) {
             d.m2[k] = nu * (1.0 / 12.0) / (d.dx[k] * d.dx[k]);
             d.m0 += nu * (-2.5) / (d.dx[k] * d.dx[k]);
         }
-        for (int k = 0; k < 3; k++) {
-            split_df(d.k1[k], d.fk1[k]);
-            split_df(d.k2[k], d.fk2[k]);
-            split_df(d.m1[k], d.fm1[k]);
-            split_df(d.m2[k], d.fm2[k]);
+        double sc = 0.0;
+        for (int k = 0; k < c.dim; k++) {
+            const double s2 = nu / (12.0 * d.dx[k] * d.dx[k]);
+            split_df(1.0 / (12.0 * d.dx[k]), d.fs1[k]);
+            split_df(s2, d.fs2[k]);
+            sc += -30.0 * s2;
         }
-        split_df(d.m0, d.fm0);
+        split_df(sc, d.fsc);
         d.tree = tree_id;
         d.level = lv;
         d.mask = t.mask_slot[b];
@@ -293,15 +417,27 @@ int stage_launch(wg_ctx *ctx, Tree &t, int stage, const double *in, BufGeo gin, 
     return WG_OK;
 }
 
-int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *out) {
+// u0 is always B (the double-float copy of u_n); with push the kernels also
+// write the same-level ghost copies of out
+int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *out, bool push) {
     const int dim = ctx->cfg.dim;
     const int *Bs = ctx->cfg.Bs;
+    const int *pp = push ? ctx->d_push : nullptr;
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, t.d_plain.p, t.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->gT, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask, Bs[0], Bs[1], Bs[2],
-                                   ctx->geo.nc, ctx->stream));
+                                   ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
+                                   Bs[2], ctx->stream));
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, t.d_masked.p, t.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->gT, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask, Bs[0], Bs[1], Bs[2],
-                                   ctx->geo.nc, ctx->stream));
+                                   ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
+                                   Bs[2], ctx->stream));
+    return WG_OK;
+}
+
+// the thin per-step plan of a tree, and whether its copies are pushed
+int thin_plan(wg_ctx *ctx, Tree &t, bool *push) {
+    SyncPlan *sp;
+    int st = get_sync(ctx, t, ctx->cfg.g_rhs, ctx->cfg.g_rhs, true, &sp);
+    if (st) return st;
+    *push = sp->push_ok && !sp->pair_begin.empty();
     return WG_OK;
 }
 
@@ -310,30 +446,38 @@ int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *o
 int ensure_shadow(wg_ctx *ctx, Tree &t) {
     if (ctx->precision != WG_RHS_FP32 || t.shadow_valid) return WG_OK;
     const int *Bs = ctx->cfg.Bs;
+    bool push;
+    int st = thin_plan(ctx, t, &push);
+    if (st) return st;
     WG_CUDA_OK(launch_shadow(t.d_all.p, (int)t.slots.size(), ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0],
-                             Bs[1], ctx->cfg.dim == 3 ? Bs[2] : 1, ctx->stream));
+                             Bs[1], ctx->cfg.dim == 3 ? Bs[2] : 1, push ? ctx->d_push : nullptr, ctx->stream));
     t.shadow_valid = true;
     return WG_OK;
 }
 
 // one RK4 step with double-float stencils: B holds the double-float copy of
-// u_n; stage inputs alternate C, B, C; stage 4 writes u_{n+1} to A and its
-// copy to B
+// u_n (stage 1 input) and keeps it through the step; the stage inputs 2-4
+// are C, D, C; stage 4 adds the increment to A and writes the copy of
+// u_{n+1} to B
 int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     Tree &t = ctx->trees[tree_id];
     const int g_rhs = ctx->cfg.g_rhs;
     const int *Bs = ctx->cfg.Bs;
     int st;
-    if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true))) return st;
+    bool push;
+    if ((st = thin_plan(ctx, t, &push))) return st;
+    // B's same-level ghosts were written with its interior (previous stage 4
+    // or the shadow copy) when push is on
+    if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true, push))) return st;
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
                          ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream));
-    if ((st = stage_launch_df(ctx, t, 1, ctx->B, ctx->C))) return st;
-    if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true))) return st;
-    if ((st = stage_launch_df(ctx, t, 2, ctx->C, ctx->B))) return st;
-    if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true))) return st;
-    if ((st = stage_launch_df(ctx, t, 3, ctx->B, ctx->C))) return st;
-    if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true))) return st;
-    if ((st = stage_launch_df(ctx, t, 4, ctx->C, ctx->B))) return st;
+    if ((st = stage_launch_df(ctx, t, 1, ctx->B, ctx->C, push))) return st;
+    if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true, push))) return st;
+    if ((st = stage_launch_df(ctx, t, 2, ctx->C, ctx->D, push))) return st;
+    if ((st = run_sync(ctx, t, ctx->D, true, g_rhs, g_rhs, true, push))) return st;
+    if ((st = stage_launch_df(ctx, t, 3, ctx->D, ctx->C, push))) return st;
+    if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true, push))) return st;
+    if ((st = stage_launch_df(ctx, t, 4, ctx->C, ctx->B, push))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
     return WG_OK;
 }
@@ -406,7 +550,8 @@ size_t wg_bytes_per_block(const wg_config *c) {
     const long long nT = (long long)(c->Bs[0] + 2 * c->g_rhs) * (c->Bs[1] + 2 * c->g_rhs) *
                          (c->dim == 3 ? c->Bs[2] + 2 * c->g_rhs : 1);
     const long long nI = (long long)c->Bs[0] * c->Bs[1] * (c->dim == 3 ? c->Bs[2] : 1);
-    return sizeof(double) * (size_t)c->neq * (size_t)(nA + 2 * nT + nI) + sizeof(BlockDesc);
+    const long long nbuf = c->rhs_precision == WG_RHS_FP32 ? 3 : 2;   // thin buffers B, C (, D)
+    return sizeof(double) * (size_t)c->neq * (size_t)(nA + nbuf * nT + nI) + sizeof(BlockDesc);
 }
 
 int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
@@ -440,7 +585,8 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
         return fail(WG_ECUDA, "constant-memory set-up failed");
     }
     auto alloc = [&](double **p, size_t n) { return cudaMalloc(p, n) == cudaSuccess; };
-    if (!alloc(&ctx->A, bytesA) || !alloc(&ctx->B, bytesT) || !alloc(&ctx->C, bytesT) || !alloc(&ctx->acc, bytesI)) {
+    if (!alloc(&ctx->A, bytesA) || !alloc(&ctx->B, bytesT) || !alloc(&ctx->C, bytesT) || !alloc(&ctx->acc, bytesI) ||
+        (ctx->precision == WG_RHS_FP32 && !alloc(&ctx->D, bytesT))) {
         cudaGetLastError();
         wg_ctx_destroy(ctx.release());
         return fail(WG_ENOMEM, "device allocation of %d blocks failed", max_blocks);
@@ -455,6 +601,16 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
     cudaMemsetAsync(ctx->A, 0, bytesA, ctx->stream);
     cudaMemsetAsync(ctx->B, 0, bytesT, ctx->stream);
     cudaMemsetAsync(ctx->C, 0, bytesT, ctx->stream);
+    if (ctx->D) cudaMemsetAsync(ctx->D, 0, bytesT, ctx->stream);
+    if (ctx->precision == WG_RHS_FP32) {
+        if (cudaMalloc(&ctx->d_push, sizeof(int) * 27 * (size_t)max_blocks) != cudaSuccess) {
+            cudaGetLastError();
+            wg_ctx_destroy(ctx.release());
+            return fail(WG_ENOMEM, "device allocation of the ghost push table failed");
+        }
+        ctx->h_push.assign((size_t)27 * max_blocks, -1);
+        cudaMemsetAsync(ctx->d_push, 0xff, sizeof(int) * 27 * (size_t)max_blocks, ctx->stream);
+    }
     cudaMemsetAsync(ctx->d_clk, 0, sizeof(TreeClock) * ctx->max_trees, ctx->stream);
     ctx->h_desc.resize(max_blocks);
     ctx->free_slots.reserve(max_blocks);
@@ -478,8 +634,11 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->A);
     cudaFree(ctx->B);
     cudaFree(ctx->C);
+    cudaFree(ctx->D);
     cudaFree(ctx->acc);
     cudaFree(ctx->mask);
+    cudaFree(ctx->mask_df);
+    cudaFree(ctx->d_push);
     cudaFree(ctx->staging);
     cudaFree(ctx->d_desc);
     cudaFree(ctx->d_tp);
@@ -665,19 +824,48 @@ int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const do
     if (want > ctx->mask_cap) {
         const int ncap = std::max(want, ctx->mask_cap * 2);
         double *nm = nullptr;
-        if (cudaMalloc(&nm, sizeof(double) * 6 * ni * (size_t)ncap) != cudaSuccess) {
+        float2 *nmd = nullptr;
+        const bool df = ctx->precision == WG_RHS_FP32;
+        if (cudaMalloc(&nm, sizeof(double) * 6 * ni * (size_t)ncap) != cudaSuccess ||
+            (df && cudaMalloc(&nmd, sizeof(float2) * 5 * ni * (size_t)ncap) != cudaSuccess)) {
             cudaGetLastError();
+            cudaFree(nm);
             return fail(WG_ENOMEM, "mask pool of %d blocks does not fit", ncap);
         }
         if (ctx->mask) {
             WG_CUDA_OK(cudaMemcpyAsync(nm, ctx->mask, sizeof(double) * 6 * ni * (size_t)ctx->mask_cap,
                                        cudaMemcpyDeviceToDevice, ctx->stream));
+            if (df)
+                WG_CUDA_OK(cudaMemcpyAsync(nmd, ctx->mask_df, sizeof(float2) * 5 * ni * (size_t)ctx->mask_cap,
+                                           cudaMemcpyDeviceToDevice, ctx->stream));
             WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
             cudaFree(ctx->mask);
+            cudaFree(ctx->mask_df);
         }
         for (int i = ncap - 1; i >= ctx->mask_cap; i--) ctx->mask_free.push_back(i);
         ctx->mask = nm;
+        ctx->mask_df = nmd;
         ctx->mask_cap = ncap;
+    }
+    // double-float copy for the FP32-pipe stage: chi/C_eta (colour 0 -> 0),
+    // u_s (three words, the third zero in 2D), sponge/C_sponge
+    std::vector<float2> packed_df;
+    if (ctx->precision == WG_RHS_FP32) {
+        packed_df.resize(need.size() * 5 * ni);
+        for (size_t k = 0; k < need.size(); k++) {
+            const double *m = packed.data() + k * 6 * ni;
+            float2 *o = packed_df.data() + k * 5 * ni;
+            for (long long i = 0; i < ni; i++) {
+                float f[2];
+                const double vals[5] = {(int)m[4 * ni + i] == 0 ? 0.0 : m[i] * t->tp.C_eta_inv, m[ni + i],
+                                        m[2 * ni + i], dim == 3 ? m[3 * ni + i] : 0.0,
+                                        m[5 * ni + i] * t->tp.C_sponge_inv};
+                for (int w = 0; w < 5; w++) {
+                    split_df(vals[w], f);
+                    o[w * ni + i] = make_float2(f[0], f[1]);
+                }
+            }
+        }
     }
     for (size_t k = 0; k < need.size(); k++) {
         const int slot = ctx->mask_free.back();
@@ -685,6 +873,9 @@ int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const do
         t->mask_slot[need[k]] = slot;
         WG_CUDA_OK(cudaMemcpyAsync(ctx->mask + (size_t)slot * 6 * ni, packed.data() + k * 6 * ni,
                                    sizeof(double) * 6 * ni, cudaMemcpyHostToDevice, ctx->stream));
+        if (!packed_df.empty())
+            WG_CUDA_OK(cudaMemcpyAsync(ctx->mask_df + (size_t)slot * 5 * ni, packed_df.data() + k * 5 * ni,
+                                       sizeof(float2) * 5 * ni, cudaMemcpyHostToDevice, ctx->stream));
     }
     int st;
     if ((st = upload_desc(ctx, *t, tree))) return st;
@@ -1067,9 +1258,11 @@ int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_la
     WG_CUDA_OK(cudaEventCreate(&e0));
     WG_CUDA_OK(cudaEventCreate(&e1));
     auto once = [&]() -> int {
-        if (which == 0 && ctx->precision == WG_RHS_FP32) return stage_launch_df(ctx, *t, 2, ctx->C, ctx->B);
+        const bool df = ctx->precision == WG_RHS_FP32;
+        const bool push = df && sp->push_ok && !sp->pair_begin.empty();
+        if (which == 0 && df) return stage_launch_df(ctx, *t, 2, ctx->C, ctx->D, push);
         if (which == 0) return stage_launch(ctx, *t, 2, ctx->B, ctx->gT, ctx->C, ctx->gT);
-        if (which == 1) return run_sync(ctx, *t, ctx->B, true, g_rhs, g_rhs, ctx->precision == WG_RHS_FP32);
+        if (which == 1) return run_sync(ctx, *t, ctx->D, true, g_rhs, g_rhs, df, push);
         WG_CUDA_OK(launch_dt(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk,
                              ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, ctx->stream));
         return WG_OK;
@@ -1085,7 +1278,6 @@ int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_la
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms_per_launch = ms / reps;
-    if (which == 0) t->shadow_valid = false;   // the timed stage wrote over B
     return WG_OK;
 }
 

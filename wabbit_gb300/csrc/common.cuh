@@ -19,6 +19,8 @@ struct TreeParams {
     int    penalization, use_sponge, skew;
     int    pad;
     float  f_c0sq[2], f_gamma[2];   // c0^2 and gamma_p as double-float pairs
+    float  f_umean[3][2];           // u_mean_set as double-float pairs
+    float  fpad[2];
 };
 
 // Per-tree time state on the device.
@@ -28,6 +30,9 @@ struct TreeClock {
     unsigned long long dt_min_bits;  // running min over blocks (positive double bits)
     int    diverged;
     int    pad;
+    // dt, dt/3 and dt/6 as double-float pairs (written with dt)
+    float  f_dt[2], f_dt3[2], f_dt6[2];
+    float  fpad[2];
 };
 
 // Per-block descriptor. k1, k2: first-derivative weights (2/3)/dx, (1/12)/dx;
@@ -36,8 +41,11 @@ struct TreeClock {
 struct BlockDesc {
     double dx[3];
     double k1[3], k2[3], m1[3], m2[3], m0;
-    // the same weights as double-float pairs (hi, lo) for the FP32-pipe path
-    float fk1[3][2], fk2[3][2], fm1[3][2], fm2[3][2], fm0[2];
+    // double-float weights of the FP32-pipe path, which evaluates the
+    // integer-coefficient stencils 8(u+1 - u-1) - (u+2 - u-2) and
+    // 16(u+1 + u-1) - (u+2 + u-2) and scales afterwards:
+    // fs1 = 1/(12 dx), fs2 = nu/(12 dx^2), fsc = -30 sum fs2
+    float fs1[3][2], fs2[3][2], fsc[2];
     int32_t tree;
     int32_t level;
     int32_t mask;                // slot in the mask pool, -1 = no mask
@@ -91,6 +99,13 @@ cudaError_t sync_init();
 cudaError_t wavelet_init();
 cudaError_t launch_sync(const Patch *patches, int npatch, double *buf, BufGeo geo, int nc, int order_predictor,
                         cudaStream_t s);
+// gather form of copy / restriction stages: expand npatch patches (first[p]
+// = offset of patch p's first point, total points < 2^32) into (receiver,
+// sender) element offsets of component 0 (uint2 each), then move nc 8-byte
+// components per point; every offset + (nc-1)*npts must be < 2^32
+cudaError_t launch_expand(const Patch *patches, const unsigned *first, int npatch, unsigned total, BufGeo geo,
+                          int nc, void *out, cudaStream_t s);
+cudaError_t launch_gather(const void *pairs, unsigned n, void *buf, BufGeo geo, int nc, cudaStream_t s);
 // prediction patches only; max_smem_doubles = largest shared-memory need
 // (coarse box + x window + x-y window) of a patch, in doubles
 cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_doubles, double *buf, BufGeo geo, int nc,
@@ -100,16 +115,21 @@ cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, in
                              const TreeParams *tp, const TreeClock *clk, const double *in, BufGeo gin,
                              double *out, BufGeo gout, double *un, BufGeo gun, double *acc, const double *mask,
                              int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s);
-// double-float stage kernel (FP32-pipe stencils, FP64 RK state): in/out are
-// float2 (hi, lo) buffers; stage 4 writes u_{n+1} to un (FP64) and its
-// double-float copy to out
+// double-float stage kernel (FP32-pipe stencils and RK stages, FP64 state;
+// push: per slot 27 same-level receiver slots whose ghost copies the kernel
+// writes along with its output, or null):
+// in, u0 and out are float2 (hi, lo) buffers of layout gt, u0 the copy of
+// u_n; acc (float2, interior) accumulates dt*sum b_j k_j; stage 4 adds it to
+// un (FP64) and writes the copy of u_{n+1} to out; maskdf holds 5 float2
+// words per point (chi/C_eta with colour applied, u_s, sponge/C_sponge)
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
-                                const TreeParams *tp, const TreeClock *clk, const void *in, BufGeo gin, void *out,
-                                BufGeo gout, double *un, BufGeo gun, double *acc, const double *mask, int Bs0,
-                                int Bs1, int Bs2, int nc, cudaStream_t s);
+                                const TreeParams *tp, const TreeClock *clk, const void *in, const void *u0,
+                                void *out, BufGeo gt, double *un, BufGeo gun, void *acc, const void *maskdf,
+                                const int *push, int Bs0, int Bs1, int Bs2, cudaStream_t s);
 // double-float copy of the interiors of the listed blocks of an FP64 buffer
+// (push: same-level ghost copies as in the stage kernel, or null)
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
-                          int Bs0, int Bs1, int Bs2, cudaStream_t s);
+                          int Bs0, int Bs1, int Bs2, const int *push, cudaStream_t s);
 cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
                               int order_predictor, cudaStream_t s);
 cudaError_t launch_rhs_only(int variant, int dim, const int *blk, int nblk, const BlockDesc *desc,

@@ -6,46 +6,108 @@
 // calculate_time_step.f90:50-118 -- all on the device, so that a whole RK4
 // step can be captured in a CUDA graph.
 #include "common.cuh"
+#include "df.cuh"
 
 namespace wg {
 
-// per-block max |u|^2 over the interior -> per-block dt -> atomic min per tree
+// |x| <= 1e12 on the bits (false for nan), the divergence guard of the ACM
+// integral stage (rhs_ACM.f90:133-146)
+__device__ __forceinline__ bool within_guard(double x) {
+    const unsigned long long a = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    return a <= 0x426d1a94a2000000ull;   // bits of 1.0e12
+}
+
+// float not above |x|, by truncation on the integer units (0 below 2^-126,
+// inf from 2^128): |x|(1 - 2^-23) < result <= |x| in the normal range
+__device__ __forceinline__ float trunc_abs_f(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if (e < -126) return 0.f;
+    if (e > 127) return __uint_as_float(0x7f800000u);
+    return __uint_as_float(((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+
+template <int DIM>
+__device__ __forceinline__ float usq_approx(const double *ub, long long np, long long o) {
+    const float a = trunc_abs_f(ub[o]), b = trunc_abs_f(ub[np + o]);
+    float s = a * a + b * b;
+    if (DIM == 3) {
+        const float c = trunc_abs_f(ub[2 * np + o]);
+        s += c * c;
+    }
+    return s;
+}
+
+// the reference's u*u + v*v (+ w*w) with every operation rounded in order
+template <int DIM>
+__device__ __forceinline__ double usq_exact(const double *ub, long long np, long long o) {
+    const double a = ub[o], bb = ub[np + o];
+    double s = __dadd_rn(__dmul_rn(a, a), __dmul_rn(bb, bb));
+    if (DIM == 3) {
+        const double c = ub[2 * np + o];
+        s = __dadd_rn(s, __dmul_rn(c, c));
+    }
+    return s;
+}
+
+// Per-block max |u|^2 over the interior -> per-block dt -> atomic min per
+// tree. The maximum is found in two passes so that the FP64 units only see
+// a few points: pass 1 takes the FP32 maximum m32 of truncated values
+// (relative error below 2^-20 against the exact sums); the point holding the
+// exact maximum then has its FP32 value above m32 (1 - 2^-17), and pass 2
+// evaluates the exact FP64 sum only for such points. The result is the
+// exact maximum of the reference's expression.
 template <int DIM>
 __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc *desc, const TreeParams *tp,
                                                  TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1,
                                                  int Bs2) {
+    constexpr int kCache = 4096;
+    __shared__ float s32[kCache];
+    __shared__ float red32[8];
+    __shared__ double red64[8];
     const int b = blk[blockIdx.x];
-    const BlockDesc d = desc[b];
+    const BlockDesc &d = desc[b];
     const long long np = geo.npts();
     const int nint = Bs0 * Bs1 * (DIM == 3 ? Bs2 : 1);
+    const bool cache = nint <= kCache;
     const double *ub = u + (long long)b * (DIM + 1) * np;
-    double m = -1.0;
-    bool bad = false;
-    for (int q = threadIdx.x; q < nint; q += blockDim.x) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    auto offset = [&](int q) {
         const int ix = q % Bs0, iy = (q / Bs0) % Bs1, iz = DIM == 3 ? q / (Bs0 * Bs1) : 0;
-        const long long o = ((long long)(iz + (DIM == 3 ? geo.gb : 0)) * geo.ny + (iy + geo.gb)) * geo.nx + (ix + geo.gb);
-        const double a = ub[o], bb = ub[np + o];
-        // divergence guard of the ACM integral stage (rhs_ACM.f90:133-146)
-        for (int c = 0; c <= DIM; c++)
-            if (!(fabs(ub[c * np + o]) <= 1.0e12)) bad = true;
-        double s = __dadd_rn(__dmul_rn(a, a), __dmul_rn(bb, bb));
-        if (DIM == 3) {
-            const double c = ub[2 * np + o];
-            s = __dadd_rn(s, __dmul_rn(c, c));
-        }
-        m = fmax(m, s);
+        return ((long long)(iz + (DIM == 3 ? geo.gb : 0)) * geo.ny + (iy + geo.gb)) * geo.nx + (ix + geo.gb);
+    };
+    float m32 = 0.f;
+    bool ok = true;
+    for (int q = threadIdx.x; q < nint; q += blockDim.x) {
+        const long long o = offset(q);
+#pragma unroll
+        for (int c = 0; c <= DIM; c++) ok &= within_guard(ub[c * np + o]);
+        const float v = usq_approx<DIM>(ub, np, o);
+        if (cache) s32[q] = v;
+        m32 = fmaxf(m32, v);
     }
-    __shared__ double red[256];
-    red[threadIdx.x] = m;
+    if (!ok) atomicOr(&clk[d.tree].diverged, 1);
+    for (int w = 16; w; w >>= 1) m32 = fmaxf(m32, __shfl_xor_sync(0xffffffffu, m32, w));
+    if (lane == 0) red32[warp] = m32;
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
-        __syncthreads();
+    m32 = red32[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) m32 = fmaxf(m32, red32[w]);
+    // below 2^-100 the squares may be FP32 subnormals without the error
+    // bound: then every point is a candidate
+    const float thr = m32 < 0x1p-100f ? 0.f : m32 * (1.0f - 0x1p-17f);
+    double m = -1.0;
+    for (int q = threadIdx.x; q < nint; q += blockDim.x) {
+        const long long o = offset(q);
+        const float v = cache ? s32[q] : usq_approx<DIM>(ub, np, o);
+        if (v >= thr) m = fmax(m, usq_exact<DIM>(ub, np, o));
     }
-    if (bad) atomicOr(&clk[d.tree].diverged, 1);
+    for (int w = 16; w; w >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, w));
+    if (lane == 0) red64[warp] = m;
+    __syncthreads();
     if (threadIdx.x == 0) {
+        double u_mag = red64[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) u_mag = fmax(u_mag, red64[w]);
         const TreeParams &p = tp[d.tree];
-        const double u_mag = red[0];
         const double u_eigen = __dadd_rn(sqrt(u_mag), sqrt(__dadd_rn(__dmul_rn(p.c0, p.c0), u_mag)));
         double dxmin = d.dx[0];
         for (int k = 1; k < DIM; k++) dxmin = fmin(dxmin, d.dx[k]);
@@ -90,6 +152,13 @@ __global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const i
     }
     if (__dadd_rn(time, dt) > p.time_max && time <= p.time_max) dt = __dsub_rn(p.time_max, time);
     c.dt = dt;
+    const df2 f1 = df_from(dt), f3 = df_from(__ddiv_rn(dt, 3.0)), f6 = df_from(__ddiv_rn(dt, 6.0));
+    c.f_dt[0] = f1.hi;
+    c.f_dt[1] = f1.lo;
+    c.f_dt3[0] = f3.hi;
+    c.f_dt3[1] = f3.lo;
+    c.f_dt6[0] = f6.hi;
+    c.f_dt6[1] = f6.lo;
 }
 
 __global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntrees) {

@@ -12,9 +12,14 @@
 // The interpolation is evaluated per fine point in the reference's separable
 // order (x on coarse rows, then y, then z, each sum left to right) with
 // explicit round-to-nearest multiplies and adds, so the ghost values are
-// bit-identical to the reference's.
+// bit-identical to the reference's. Double-float buffers (FP32-pipe
+// precision) get the same passes in double-float arithmetic
+// (predict_df_kernel), and the per-step copy / restriction stages run in
+// gather form (expand_kernel, gather_kernel).
 #include "common.cuh"
 #include "predict.cuh"
+#include "df.cuh"
+#include <algorithm>
 
 namespace wg {
 
@@ -41,12 +46,59 @@ __global__ void __launch_bounds__(128) sync_kernel(const Patch *__restrict__ pat
         else
             si = ((long long)(p.slo[2] + 2 * (p.blo[2] + iz)) * geo.ny + (p.slo[1] + 2 * (p.blo[1] + iy))) * geo.nx +
                  p.slo[0] + 2 * p.blo[0];
+        // sender and receiver boxes of one stage never overlap (checked when
+        // the table is built), so the loads of a row need not wait for its
+        // stores
         for (int c = 0; c < nc; c++) {
-            const double *sr = src + c * npts + si;
-            double *dr = dst + c * npts + di;
+            const double *__restrict__ sr = src + c * npts + si;
+            double *__restrict__ dr = dst + c * npts + di;
             for (int ix = 0; ix < ex; ix++) dr[ix] = sr[step * ix];
         }
     }
+}
+
+// Gather form of the copy and restriction stages: the patches of a stage are
+// expanded once per grid into (receiver, sender) element offsets of
+// component 0, in patch order with x fastest. Every ghost point is then one
+// thread that moves all nc components, so the loads of the nc components are
+// in flight together and consecutive threads touch consecutive addresses.
+__global__ void expand_kernel(const Patch *__restrict__ patches, const unsigned *__restrict__ first, int npatch,
+                              unsigned total, BufGeo geo, int nc, uint2 *__restrict__ out) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    int lo = 0, hi = npatch - 1;                     // last patch with first[p] <= i
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    const Patch p = patches[lo];
+    const int ex = p.rhi[0] - p.rlo[0] + 1, ey = p.rhi[1] - p.rlo[1] + 1;
+    const int k = (int)(i - first[lo]);
+    const int ix = k % ex, iy = (k / ex) % ey, iz = k / (ex * ey);
+    const unsigned long long bs = (unsigned long long)nc * geo.npts();
+    const unsigned long long d = p.dst * bs + ((unsigned long long)(p.rlo[2] + iz) * geo.ny + (p.rlo[1] + iy)) * geo.nx +
+                                 (p.rlo[0] + ix);
+    unsigned long long sidx;
+    if (p.op == 0)
+        sidx = ((unsigned long long)(p.slo[2] + iz) * geo.ny + (p.slo[1] + iy)) * geo.nx + (p.slo[0] + ix);
+    else
+        sidx = ((unsigned long long)(p.slo[2] + 2 * (p.blo[2] + iz)) * geo.ny + (p.slo[1] + 2 * (p.blo[1] + iy))) *
+                   geo.nx + (p.slo[0] + 2 * (p.blo[0] + ix));
+    out[i] = make_uint2((unsigned)d, (unsigned)(p.src * bs + sidx));
+}
+
+template <int NC>
+__global__ void __launch_bounds__(256) gather_kernel(const uint2 *__restrict__ pairs, unsigned n,
+                                                     unsigned long long *buf, unsigned cs) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint2 e = __ldg(pairs + i);
+    unsigned long long v[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) v[c] = buf[e.y + c * cs];
+#pragma unroll
+    for (int c = 0; c < NC; c++) buf[e.x + c * cs] = v[c];
 }
 
 // Prediction patches: one CTA per patch, one component at a time. The coarse
@@ -61,27 +113,6 @@ __device__ __forceinline__ double interp_line(const double *c, const double *v, 
     return s;
 }
 
-// storage of a sync buffer element: FP64, or a double-float pair (hi, lo)
-// held in the same 8 bytes (FP32-pipe path); predictions are always
-// evaluated in FP64
-template <bool DF>
-__device__ __forceinline__ double load_el(const double *p) {
-    if (!DF) return *p;
-    const float2 v = *reinterpret_cast<const float2 *>(p);
-    return (double)v.x + (double)v.y;
-}
-
-template <bool DF>
-__device__ __forceinline__ void store_el(double *p, double v) {
-    if (!DF) {
-        *p = v;
-        return;
-    }
-    const float h = __double2float_rn(v);
-    *reinterpret_cast<float2 *>(p) = make_float2(h, __double2float_rn(v - (double)h));
-}
-
-template <bool DF>
 __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ patches, double *buf, BufGeo geo,
                                                       int nc, int order_idx, int ncoef) {
     extern __shared__ double sm[];
@@ -111,7 +142,7 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
         double *dst = buf + ((long long)p.dst * nc + c) * npts;
         for (int i = threadIdx.x; i < ncp; i += blockDim.x) {
             const int x = i % cx, y = (i / cx) % cy, z = i / (cx * cy);
-            C[i] = load_el<DF>(src + ((long long)(p.slo[2] + z) * geo.ny + (p.slo[1] + y)) * geo.nx + (p.slo[0] + x));
+            C[i] = src[((long long)(p.slo[2] + z) * geo.ny + (p.slo[1] + y)) * geo.nx + (p.slo[0] + x)];
         }
         __syncthreads();
         // x pass on even rows / planes
@@ -147,7 +178,111 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
             if (!(fz & 1)) v = pl[(long long)((fz - zw0) >> 1) * ex * ey];
             else if (fz < h || fz > Fz - 1 - h) v = 0.0;
             else v = interp_line(cf, pl, ex * ey, (fz - h - zw0) >> 1, ncoef);
-            store_el<DF>(dst + ((long long)(p.rlo[2] + k) * geo.ny + (p.rlo[1] + j)) * geo.nx + (p.rlo[0] + ix), v);
+            dst[((long long)(p.rlo[2] + k) * geo.ny + (p.rlo[1] + j)) * geo.nx + (p.rlo[0] + ix)] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// Prediction into double-float buffers (FP32-pipe path): the same windows
+// and separable passes, evaluated in double-float arithmetic on the FP32
+// units with the predictors' integer weights (1)/2, (-1,9)/16,
+// (3,-25,150)/256, (-5,49,-245,1225)/2048 applied to symmetric pair sums
+// and the power-of-two scale applied exactly; all components of a patch in
+// one pass. Accuracy a few 2^-47 relative, like the stencils it feeds.
+template <int NCOEF>
+__device__ __forceinline__ df2 interp_df(const float2 *v, int stride, int first) {
+    constexpr float w2[1] = {1.f}, w4[2] = {-1.f, 9.f}, w6[3] = {3.f, -25.f, 150.f},
+                    w8[4] = {-5.f, 49.f, -245.f, 1225.f};
+    constexpr float scale = NCOEF == 2 ? 0.5f : NCOEF == 4 ? 0.0625f : NCOEF == 6 ? 0.00390625f : 0.00048828125f;
+    df2 acc = {0.f, 0.f};
+#pragma unroll
+    for (int m = 0; m < NCOEF / 2; m++) {
+        const float w = NCOEF == 2 ? w2[m] : NCOEF == 4 ? w4[m] : NCOEF == 6 ? w6[m] : w8[m];
+        const float2 a = v[(long long)(first + m) * stride], b = v[(long long)(first + NCOEF - 1 - m) * stride];
+        const df2 s = df_add_nr({a.x, a.y}, {b.x, b.y});
+        const float p = s.hi * w;
+        const df2 t = {p, fmaf(s.lo, w, fmaf(s.hi, w, -p))};
+        acc = m == 0 ? t : df_add_nr(acc, t);
+    }
+    return df_norm(df_pow2(acc, scale));
+}
+
+template <int NCOEF>
+__global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict__ patches, float2 *buf, BufGeo geo,
+                                                         int nc, int cg) {
+    extern __shared__ float2 sf[];
+    const Patch p = patches[blockIdx.x];
+    const int cx = p.shi[0] - p.slo[0] + 1, cy = p.shi[1] - p.slo[1] + 1, cz = p.shi[2] - p.slo[2] + 1;
+    const int Fx = 2 * cx - 1, Fy = 2 * cy - 1, Fz = 2 * cz - 1;
+    constexpr int h = NCOEF - 1;
+    const int ex = p.rhi[0] - p.rlo[0] + 1, ey = p.rhi[1] - p.rlo[1] + 1, ez = p.rhi[2] - p.rlo[2] + 1;
+    const int x0 = p.blo[0], y0 = p.blo[1], z0 = p.blo[2];
+    int yw0 = max(0, y0 - h), yw1 = min(Fy - 1, y0 + ey - 1 + h);
+    yw0 += yw0 & 1;
+    yw1 -= yw1 & 1;
+    int zw0 = max(0, z0 - h), zw1 = min(Fz - 1, z0 + ez - 1 + h);
+    zw0 += zw0 & 1;
+    zw1 -= zw1 & 1;
+    const int ny = (yw1 - yw0) / 2 + 1, nz = (zw1 - zw0) / 2 + 1;
+    const int ncp = cx * cy * cz, nX = ex * ny * nz, nXY = ex * ey * nz, nR = ex * ey * ez;
+    const long long npts = geo.npts();
+    for (int c0 = 0; c0 < nc; c0 += cg) {
+        const int ncg = min(cg, nc - c0);
+        float2 *C = sf;                      // ncg coarse boxes
+        float2 *X = C + ncg * ncp;           // ncg x-pass windows
+        float2 *XY = X + ncg * nX;           // ncg x-y windows
+        for (int i = threadIdx.x; i < ncg * ncp; i += blockDim.x) {
+            const int c = i / ncp, k = i - c * ncp;
+            const int x = k % cx, y = (k / cx) % cy, z = k / (cx * cy);
+            C[i] = buf[((long long)p.src * nc + c0 + c) * npts +
+                       ((long long)(p.slo[2] + z) * geo.ny + (p.slo[1] + y)) * geo.nx + (p.slo[0] + x)];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < ncg * nX; i += blockDim.x) {
+            const int c = i / nX, k = i - c * nX;
+            const int ix = k % ex, jy = (k / ex) % ny, kz = k / (ex * ny);
+            const int fx = x0 + ix;
+            const float2 *row = C + c * ncp + ((long long)((zw0 >> 1) + kz) * cy + (yw0 >> 1) + jy) * cx;
+            float2 v;
+            if (!(fx & 1)) v = row[fx >> 1];
+            else if (fx < h || fx > Fx - 1 - h) v = make_float2(0.f, 0.f);
+            else {
+                const df2 r = interp_df<NCOEF>(row, 1, (fx - h) >> 1);
+                v = make_float2(r.hi, r.lo);
+            }
+            X[i] = v;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < ncg * nXY; i += blockDim.x) {
+            const int c = i / nXY, k = i - c * nXY;
+            const int ix = k % ex, j = (k / ex) % ey, kz = k / (ex * ey);
+            const int fy = y0 + j;
+            const float2 *col = X + c * nX + (long long)kz * ny * ex + ix;
+            float2 v;
+            if (!(fy & 1)) v = col[(long long)((fy - yw0) >> 1) * ex];
+            else if (fy < h || fy > Fy - 1 - h) v = make_float2(0.f, 0.f);
+            else {
+                const df2 r = interp_df<NCOEF>(col, ex, (fy - h - yw0) >> 1);
+                v = make_float2(r.hi, r.lo);
+            }
+            XY[i] = v;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < ncg * nR; i += blockDim.x) {
+            const int c = i / nR, k = i - c * nR;
+            const int ix = k % ex, j = (k / ex) % ey, kk = k / (ex * ey);
+            const int fz = z0 + kk;
+            const float2 *pl = XY + c * nXY + (long long)j * ex + ix;
+            float2 v;
+            if (!(fz & 1)) v = pl[(long long)((fz - zw0) >> 1) * ex * ey];
+            else if (fz < h || fz > Fz - 1 - h) v = make_float2(0.f, 0.f);
+            else {
+                const df2 r = interp_df<NCOEF>(pl, ex * ey, (fz - h - zw0) >> 1);
+                v = make_float2(r.hi, r.lo);
+            }
+            buf[((long long)p.dst * nc + c0 + c) * npts +
+                ((long long)(p.rlo[2] + kk) * geo.ny + (p.rlo[1] + j)) * geo.nx + (p.rlo[0] + ix)] = v;
         }
         __syncthreads();
     }
@@ -161,26 +296,60 @@ cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_double
     const size_t smem = sizeof(double) * (size_t)max_smem_doubles;
     static size_t attr = 0;
     if (smem > 48 * 1024 && smem > attr) {
-        cudaError_t e = cudaFuncSetAttribute(predict_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr = smem;
     }
-    predict_kernel<false><<<npatch, 256, smem, s>>>(patches, buf, geo, nc, order_predictor / 2 - 1, order_predictor);
+    predict_kernel<<<npatch, 256, smem, s>>>(patches, buf, geo, nc, order_predictor / 2 - 1, order_predictor);
     return cudaGetLastError();
 }
 
 cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
                               int order_predictor, cudaStream_t s) {
     if (npatch <= 0) return cudaSuccess;
-    const size_t smem = sizeof(double) * (size_t)max_smem_doubles;
-    static size_t attr = 0;
-    if (smem > 48 * 1024 && smem > attr) {
-        cudaError_t e = cudaFuncSetAttribute(predict_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = smem;
+    // as many components per pass as fit the shared memory of one CTA
+    const size_t per = sizeof(float2) * (size_t)max_smem_doubles;
+    const size_t limit = 200 * 1024;
+    if (per > limit) return cudaErrorInvalidValue;
+    const int cg = (int)std::min<size_t>((size_t)nc, limit / per);
+    const size_t smem = per * cg;
+    float2 *b = reinterpret_cast<float2 *>(buf);
+    auto go = [&](auto kern) -> cudaError_t {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        kern<<<npatch, 256, smem, s>>>(patches, b, geo, nc, cg);
+        return cudaGetLastError();
+    };
+    switch (order_predictor) {
+        case 2: return go(predict_df_kernel<2>);
+        case 4: return go(predict_df_kernel<4>);
+        case 6: return go(predict_df_kernel<6>);
+        case 8: return go(predict_df_kernel<8>);
+        default: return cudaErrorInvalidValue;
     }
-    predict_kernel<true><<<npatch, 256, smem, s>>>(patches, reinterpret_cast<double *>(buf), geo, nc,
-                                                   order_predictor / 2 - 1, order_predictor);
+}
+
+cudaError_t launch_expand(const Patch *patches, const unsigned *first, int npatch, unsigned total, BufGeo geo,
+                          int nc, void *out, cudaStream_t s) {
+    if (total == 0) return cudaSuccess;
+    expand_kernel<<<(total + 255) / 256, 256, 0, s>>>(patches, first, npatch, total, geo, nc,
+                                                      reinterpret_cast<uint2 *>(out));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const void *pairs, unsigned n, void *buf, BufGeo geo, int nc, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint2 *pp = reinterpret_cast<const uint2 *>(pairs);
+    auto *b = reinterpret_cast<unsigned long long *>(buf);
+    const unsigned cs = (unsigned)geo.npts();
+    const unsigned blocks = (n + 255) / 256;
+    switch (nc) {
+        case 3: gather_kernel<3><<<blocks, 256, 0, s>>>(pp, n, b, cs); break;
+        case 4: gather_kernel<4><<<blocks, 256, 0, s>>>(pp, n, b, cs); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 
