@@ -325,6 +325,7 @@ def run_ours(args, rank, world):
             "wavelet": cfg.wavelet.decode(), "Jmax": cfg.Jmax, "blocks": nblk, "points": npts,
             "masked_blocks": nmasked, "levels": np.bincount(lv).tolist(), "variant": args.variant,
             "rhs_precision": "fp64" if cfg.rhs_precision == 0 else "fp32-pipe double-float",
+            "stage_form": ctx.stage_form() if cfg.rhs_precision else "direct",
             "rk": "RK4", "graph": True, "l2": "state 2.9 GB > 129 MB L2 (no flush needed)" if dim == 3 else
             "inputs smaller than L2",
             "parallelism": "replicas" if world > 1 else "1 GPU",

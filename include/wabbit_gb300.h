@@ -106,6 +106,17 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **ctx);
 int wg_ctx_destroy(wg_ctx *ctx);
 /* 1: FMA stencil (default); 0: strict reference arithmetic (no FMA). */
 int wg_set_variant(wg_ctx *ctx, int fast);
+/* Form of the FP32-pipe stage kernel (no counterpart in the reference, whose
+ * RHS is a per-block loop): WG_FORM_AUTO (default) times the forms that
+ * apply on the first wg_run of a grid and keeps the faster; WG_FORM_DIRECT
+ * reads the stencil from global memory; WG_FORM_TILE stages each block slab
+ * in shared memory by TMA (3-D, 16x16 planes, g_rhs = 2). wg_get_stage_form
+ * returns the form in use (the autotuner's choice once it has run). */
+#define WG_FORM_AUTO 0
+#define WG_FORM_DIRECT 1
+#define WG_FORM_TILE 2
+int wg_set_stage_form(wg_ctx *ctx, int form);
+int wg_get_stage_form(wg_ctx *ctx, int *form);
 int wg_synchronize(wg_ctx *ctx);
 /* the context's CUDA stream (cudaStream_t) */
 void *wg_stream(wg_ctx *ctx);

@@ -269,3 +269,37 @@ def test_fp32_pipe_rejects_skew_symmetric():
     cfg.rhs_precision = 1
     with pytest.raises(capi.WgError):
         Context(cfg, 8)
+
+
+@pytest.mark.parametrize("form", ["direct", "tile", "auto"])
+def test_fp32_pipe_stage_forms_16cubed(form):
+    """3-D 16^3 blocks (the benchmark geometry): the direct-load and the
+    TMA-staged stage kernels, and the autotuner's pick, all stay within
+    1e-12 per step of the FP64 oracle on a graded two-level grid with a
+    masked sphere."""
+    cfg = small_cfg(3, "CDF40", Bs=16, penal=1, jmin=1, jmax=2)
+    cfg.C_eta = 1e-2
+    cfg.rhs_precision = 1
+    lv, co = grids.random_graded(3, 1, 2, seed=3, frac=0.4)
+    data = smooth_state(cfg, lv, co, 29)
+    mask = sphere_mask(cfg, lv, co, [0.5, 0.6, 0.7], 0.3)
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    o.set_mask(mask)
+    with Context(cfg, len(lv) + 4) as ctx:
+        ctx.set_stage_form(form)
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(data)
+        f.set_mask(mask)
+        f.set_time(0.0)
+        t_ref = 0.0
+        for step in range(3):
+            t_ref, dt_ref = o.step(t_ref)
+            if step == 0:
+                f.timeStep_tree()
+            else:
+                f.run(1, use_graph=True)
+            err = rel_l2(interior(cfg, f.download()), interior(cfg, o.data()))
+            assert err < 1e-12, (form, step, err)
+        assert ctx.stage_form() in (("direct", "tile") if form == "auto" else (form,))

@@ -26,7 +26,7 @@ EXPORTS = [
     "wg_refine_everywhere", "wg_sync_table", "wg_block_slot", "wg_sync_table_host",
     "wg_probe_alu", "wg_time_kernel", "wg_tree_stats", "wg_set_mask_sparse",
     "wg_upload_interior", "wg_download_interior", "wg_graph_kernels",
-    "wg_threshold_flags_noalloc",
+    "wg_threshold_flags_noalloc", "wg_set_stage_form", "wg_get_stage_form",
 ]
 
 
@@ -48,6 +48,8 @@ _SIGS = {
     "wg_ctx_create": (_i, [ctypes.POINTER(WgConfig), _i, ctypes.POINTER(_vp)]),
     "wg_ctx_destroy": (_i, [_vp]),
     "wg_set_variant": (_i, [_vp, _i]),
+    "wg_set_stage_form": (_i, [_vp, _i]),
+    "wg_get_stage_form": (_i, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "wg_synchronize": (_i, [_vp]),
     "wg_stream": (_vp, [_vp]),
     "wg_tree_create": (_i, [_vp, ctypes.POINTER(WgConfig), _ip]),

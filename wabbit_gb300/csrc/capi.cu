@@ -25,6 +25,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
+
 #include "../../include/wabbit_gb300.h"
 #include "common.cuh"
 
@@ -112,6 +114,11 @@ struct wg_ctx {
     float2 *mask_df = nullptr;
     int *d_push = nullptr;              // per slot 27 same-level receivers (FP32-pipe precision)
     std::vector<int> h_push;
+    CUtensorMap tm[3];                  // TMA maps over B, C, D (3-D FP32-pipe precision)
+    bool have_tm = false;
+    int stage_form = WG_FORM_AUTO;      // requested form of the FP32-pipe stage kernel
+    int tuned_form = 0;                 // the autotuner's choice (0: not tuned yet)
+    int *d_err = nullptr;               // device error flag (a kernel's wait ran out)
     int mask_cap = 0;
     std::vector<int> mask_free;
     BlockDesc *d_desc = nullptr;
@@ -423,13 +430,61 @@ int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *o
     const int dim = ctx->cfg.dim;
     const int *Bs = ctx->cfg.Bs;
     const int *pp = push ? ctx->d_push : nullptr;
+    const void *tm = nullptr;
+    const int form = ctx->stage_form != WG_FORM_AUTO ? ctx->stage_form : ctx->tuned_form ? ctx->tuned_form : WG_FORM_DIRECT;
+    if (ctx->have_tm && form == WG_FORM_TILE)
+        tm = in == ctx->B ? &ctx->tm[0] : in == ctx->C ? &ctx->tm[1] : in == ctx->D ? &ctx->tm[2] : nullptr;
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, t.d_plain.p, t.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
                                    ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
-                                   Bs[2], ctx->stream));
+                                   Bs[2], tm, ctx->d_err, ctx->stream));
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, t.d_masked.p, t.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
                                    ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
-                                   Bs[2], ctx->stream));
+                                   Bs[2], tm, ctx->d_err, ctx->stream));
     return WG_OK;
+}
+
+// TMA maps over the three thin double-float buffers: a 3-D tensor of 8-byte
+// elements (x, y, plane-of-all-blocks-and-components), box nx * ny * (zt+4)
+int make_tensor_maps(wg_ctx *ctx) {
+    const int zt = tile_slab(ctx->cfg.dim, ctx->cfg.Bs[0], ctx->cfg.Bs[1], ctx->cfg.Bs[2], ctx->gT.gb);
+    if (!zt) return WG_OK;
+    using Encode = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+        cudaGetLastError();
+        return WG_OK;   // no TMA maps: the direct-load kernel runs
+    }
+    const BufGeo &g = ctx->gT;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny,
+                                (cuuint64_t)g.nz * ctx->geo.nc * (cuuint64_t)ctx->max_blocks};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.nx * 8, (cuuint64_t)g.nx * g.ny * 8};
+    const cuuint32_t box[3] = {(cuuint32_t)g.nx, (cuuint32_t)g.ny, (cuuint32_t)(zt + 4)};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    double *bufs[3] = {ctx->B, ctx->C, ctx->D};
+    for (int i = 0; i < 3; i++) {
+        const CUresult r = reinterpret_cast<Encode>(fn)(&ctx->tm[i], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, bufs[i], dims,
+                                                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(WG_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    }
+    ctx->have_tm = true;
+    return WG_OK;
+}
+
+// a kernel's bounded wait ran out (reported once, then cleared)
+int check_dev_err(wg_ctx *ctx) {
+    if (!ctx->d_err) return WG_OK;
+    int h = 0;
+    WG_CUDA_OK(cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    if (!h) return WG_OK;
+    WG_CUDA_OK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    return fail(WG_ETIMEOUT, "a stage kernel's shared-memory load did not complete within its time limit");
 }
 
 // the thin per-step plan of a tree, and whether its copies are pushed
@@ -453,6 +508,43 @@ int ensure_shadow(wg_ctx *ctx, Tree &t) {
                              Bs[1], ctx->cfg.dim == 3 ? Bs[2] : 1, push ? ctx->d_push : nullptr, ctx->stream));
     t.shadow_valid = true;
     return WG_OK;
+}
+
+// Autotuner of the FP32-pipe stage kernel: times a stage (C -> D, stage 2)
+// of this tree in each applicable form and keeps the faster for the context.
+int autotune_stage_form(wg_ctx *ctx, Tree &t) {
+    if (ctx->precision != WG_RHS_FP32 || ctx->stage_form != WG_FORM_AUTO || ctx->tuned_form) return WG_OK;
+    if (!ctx->have_tm || t.slots.empty()) {
+        ctx->tuned_form = WG_FORM_DIRECT;
+        return WG_OK;
+    }
+    bool push;
+    int st = thin_plan(ctx, t, &push);
+    if (st) return st;
+    cudaEvent_t e0, e1;
+    WG_CUDA_OK(cudaEventCreate(&e0));
+    WG_CUDA_OK(cudaEventCreate(&e1));
+    float best = 0.f;
+    int best_form = WG_FORM_DIRECT;
+    for (int form : {WG_FORM_DIRECT, WG_FORM_TILE}) {
+        ctx->tuned_form = form;
+        if ((st = stage_launch_df(ctx, t, 2, ctx->C, ctx->D, push))) break;   // warm-up
+        WG_CUDA_OK(cudaEventRecord(e0, ctx->stream));
+        for (int r = 0; r < 5 && !st; r++) st = stage_launch_df(ctx, t, 2, ctx->C, ctx->D, push);
+        WG_CUDA_OK(cudaEventRecord(e1, ctx->stream));
+        WG_CUDA_OK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        WG_CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+        if (form == WG_FORM_DIRECT || ms < best) {
+            best = ms;
+            best_form = form;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tuned_form = best_form;
+    if (st) return st;
+    return check_dev_err(ctx);
 }
 
 // one RK4 step with double-float stencils: B holds the double-float copy of
@@ -506,7 +598,7 @@ int rk4_enqueue(wg_ctx *ctx, int tree_id) {
 int read_clock(wg_ctx *ctx, int tree, TreeClock *out) {
     WG_CUDA_OK(cudaMemcpyAsync(out, ctx->d_clk + tree, sizeof(TreeClock), cudaMemcpyDeviceToHost, ctx->stream));
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-    return WG_OK;
+    return check_dev_err(ctx);
 }
 
 }  // namespace
@@ -610,7 +702,17 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
         }
         ctx->h_push.assign((size_t)27 * max_blocks, -1);
         cudaMemsetAsync(ctx->d_push, 0xff, sizeof(int) * 27 * (size_t)max_blocks, ctx->stream);
+        if ((st = make_tensor_maps(ctx.get()))) {
+            wg_ctx_destroy(ctx.release());
+            return st;
+        }
     }
+    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        wg_ctx_destroy(ctx.release());
+        return fail(WG_ENOMEM, "device allocation failed");
+    }
+    cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream);
     cudaMemsetAsync(ctx->d_clk, 0, sizeof(TreeClock) * ctx->max_trees, ctx->stream);
     ctx->h_desc.resize(max_blocks);
     ctx->free_slots.reserve(max_blocks);
@@ -639,6 +741,7 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->mask);
     cudaFree(ctx->mask_df);
     cudaFree(ctx->d_push);
+    cudaFree(ctx->d_err);
     cudaFree(ctx->staging);
     cudaFree(ctx->d_desc);
     cudaFree(ctx->d_tp);
@@ -1010,6 +1113,10 @@ int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph)
             if ((st = get_sync(ctx, t, ctx->cfg.g_rhs, ctx->cfg.g_rhs, false, &sp))) return st;
             if ((st = get_sync(ctx, t, ctx->cfg.g_rhs, ctx->cfg.g_rhs, true, &sp))) return st;
         }
+        for (int i = 0; i < ntrees; i++) {
+            int st = autotune_stage_form(ctx, ctx->trees[trees[i]]);
+            if (st) return st;
+        }
         WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
         if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
         if (ctx->graph) cudaGraphDestroy(ctx->graph);
@@ -1034,10 +1141,28 @@ int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph)
     return WG_OK;
 }
 
+int wg_set_stage_form(wg_ctx *ctx, int form) {
+    if (!ctx) return fail(WG_EINVAL, "null ctx");
+    if (form != WG_FORM_AUTO && form != WG_FORM_DIRECT && form != WG_FORM_TILE)
+        return fail(WG_EINVAL, "unknown stage form %d", form);
+    if (form == WG_FORM_TILE && !ctx->have_tm)
+        return fail(WG_ENOTSUP, "the tile form needs 3-D 16x16 planes, g_rhs = 2 and the FP32-pipe precision");
+    ctx->stage_form = form;
+    ctx->tuned_form = 0;
+    ctx->graph_version = -1;   // recapture with the new form
+    return WG_OK;
+}
+
+int wg_get_stage_form(wg_ctx *ctx, int *form) {
+    if (!ctx || !form) return fail(WG_EINVAL, "bad arguments");
+    *form = ctx->stage_form != WG_FORM_AUTO ? ctx->stage_form : ctx->tuned_form ? ctx->tuned_form : WG_FORM_DIRECT;
+    return WG_OK;
+}
+
 int wg_synchronize(wg_ctx *ctx) {
     if (!ctx) return fail(WG_EINVAL, "null ctx");
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-    return WG_OK;
+    return check_dev_err(ctx);
 }
 
 // the context's stream, for callers that time or order work around it

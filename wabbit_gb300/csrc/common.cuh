@@ -116,6 +116,7 @@ cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, in
                              double *out, BufGeo gout, double *un, BufGeo gun, double *acc, const double *mask,
                              int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s);
 // double-float stage kernel (FP32-pipe stencils and RK stages, FP64 state;
+// err: set to 1 by a CTA whose TMA load did not complete within a second;
 // push: per slot 27 same-level receiver slots whose ghost copies the kernel
 // writes along with its output, or null):
 // in, u0 and out are float2 (hi, lo) buffers of layout gt, u0 the copy of
@@ -125,7 +126,12 @@ cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, in
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
                                 const TreeParams *tp, const TreeClock *clk, const void *in, const void *u0,
                                 void *out, BufGeo gt, double *un, BufGeo gun, void *acc, const void *maskdf,
-                                const int *push, int Bs0, int Bs1, int Bs2, cudaStream_t s);
+                                const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int *err,
+                                cudaStream_t s);
+// slab height of the TMA tile form of the double-float stage kernel (3-D,
+// Bs0*Bs1 = 256), 0 where it does not apply; tmap (a CUtensorMap over the
+// stage-input buffer: dims nx, ny, nz*nc*slots; box nx, ny, zt+4) selects it
+int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g);
 // double-float copy of the interiors of the listed blocks of an FP64 buffer
 // (push: same-level ghost copies as in the stage kernel, or null)
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,

@@ -21,6 +21,7 @@
 // contracted; every FMA is explicit.
 #include "common.cuh"
 #include "df.cuh"
+#include "tma.cuh"
 
 namespace wg {
 
@@ -68,46 +69,30 @@ __device__ __forceinline__ void push_ghosts(const int *push, int b, int ix, int 
     const int sx = ix < g ? -1 : (ix >= Bs0 - g ? 1 : 0);
     const int sy = iy < g ? -1 : (iy >= Bs1 - g ? 1 : 0);
     const int sz = DIM == 3 ? (iz < g ? -1 : (iz >= Bs2 - g ? 1 : 0)) : 0;
-    if (!(sx | sy | sz)) return;
+    const int near = (sx ? 1 : 0) | (sy ? 2 : 0) | (sz ? 4 : 0);
+    if (!near) return;
     const int *row = push + b * 27;
-    for (int kz = 0; kz < (sz ? 2 : 1); kz++) {
-        const int dz = kz ? sz : 0;
-        for (int ky = 0; ky < (sy ? 2 : 1); ky++) {
-            const int dy = ky ? sy : 0;
-            for (int kx = 0; kx < (sx ? 2 : 1); kx++) {
-                const int dx = kx ? sx : 0;
-                if (!(dx | dy | dz)) continue;
-                const int nb = row[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
-                if (nb < 0) continue;
-                const long long o = (long long)nb * NV * cs +
-                                    ((long long)(DIM == 3 ? iz - dz * Bs2 + g : 0) * gt.ny + (iy - dy * Bs1 + g)) * gt.nx +
-                                    (ix - dx * Bs0 + g);
+    // the point's offset inside a block; a receiver across (dx, dy, dz) sees
+    // it shifted by -(dx Bs0 + dy Bs1 nx + dz Bs2 nx ny)
+    const long long own = ((long long)(DIM == 3 ? iz + g : 0) * gt.ny + (iy + g)) * gt.nx + (ix + g);
+    for (int sub = near; sub; sub = (sub - 1) & near) {          // non-empty subsets of the near axes
+        const int dx = sub & 1 ? sx : 0, dy = sub & 2 ? sy : 0, dz = sub & 4 ? sz : 0;
+        const int nb = row[(dz + 1) * 9 + (dy + 1) * 3 + (dx + 1)];
+        if (nb < 0) continue;
+        float2 *o = out + (long long)nb * NV * cs + own - (dx * Bs0 + (dy * Bs1 + dz * Bs2 * gt.ny) * gt.nx);
 #pragma unroll
-                for (int c = 0; c < NV; c++) out[o + c * cs] = v[c];
-            }
-        }
+        for (int c = 0; c < NV; c++) o[c * cs] = v[c];
     }
 }
 
-template <int DIM, bool MASK>
-__global__ void __launch_bounds__(256) acm_stage_df_kernel(StageArgsDF a) {
-    const int bi = blockIdx.x / a.chunks;
-    const int chunk = blockIdx.x % a.chunks;
-    const int npts_int = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
-    const int q = chunk * blockDim.x + threadIdx.x;
-    if (q >= npts_int) return;
-    const int b = a.blk[bi];
-    const BlockDesc &d = a.desc[b];
-    const TreeParams &tp = a.tp[d.tree];
-    const int ix = q % a.Bs0, iy = (q / a.Bs0) % a.Bs1, iz = DIM == 3 ? q / (a.Bs0 * a.Bs1) : 0;
-    const long long cs = a.gt.npts();
-    const long long off = (long long)b * (DIM + 1) * cs +
-                          ((long long)(iz + (DIM == 3 ? a.gt.gb : 0)) * a.gt.ny + (iy + a.gt.gb)) * a.gt.nx +
-                          (ix + a.gt.gb);
-    const float2 *u = a.in + off;
-    const int stv[3] = {1, a.gt.nx, a.gt.nx * a.gt.ny};
-
-    df2 vel[DIM], w[DIM], r[DIM + 1];
+// RHS of one interior point from a stencil input with strides stv (shared or
+// global memory). m: the point's double-float mask words (stride ms), or
+// null. Returns the RHS in r and the centre values vel, p0.
+template <int DIM, bool MASK, typename Idx>
+__device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3], const BlockDesc &d,
+                                       const TreeParams &tp, const float2 *m, int ms, df2 r[DIM + 1], df2 vel[DIM],
+                                       df2 &p0) {
+    df2 w[DIM];
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
         vel[k] = ld(u + k * cs);
@@ -131,7 +116,7 @@ __global__ void __launch_bounds__(256) acm_stage_df_kernel(StageArgsDF a) {
         r[c] = df_sub_nr(lap, adv);
     }
     const float2 *up = u + DIM * cs;
-    const df2 p0 = ld(up);
+    p0 = ld(up);
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
         const df2 A = ld(up + stv[k]), B = ld(up - stv[k]), E = ld(up + 2 * stv[k]), F = ld(up - 2 * stv[k]);
@@ -140,37 +125,82 @@ __global__ void __launch_bounds__(256) acm_stage_df_kernel(StageArgsDF a) {
     }
     r[DIM] = df_neg(df_add_nr(df_mul_nr(cf(tp.f_c0sq), div), df_mul_nr(cf(tp.f_gamma), p0)));
     if (MASK) {
-        const float2 *m = a.mask + (long long)d.mask * 5 * npts_int + q;
         const df2 chi = ld(m);
 #pragma unroll
-        for (int c = 0; c < DIM; c++)
-            r[c] = df_sub_nr(r[c], df_mul_nr(chi, df_sub_nr(vel[c], ld(m + (1 + c) * npts_int))));
+        for (int c = 0; c < DIM; c++) r[c] = df_sub_nr(r[c], df_mul_nr(chi, df_sub_nr(vel[c], ld(m + (1 + c) * ms))));
         if (tp.use_sponge) {
-            const df2 spo = ld(m + 4 * npts_int);
+            const df2 spo = ld(m + 4 * ms);
 #pragma unroll
             for (int c = 0; c < DIM; c++)
                 r[c] = df_sub_nr(r[c], df_mul_nr(spo, df_sub_nr(vel[c], cf(tp.f_umean[c]))));
             r[DIM] = df_sub_nr(r[DIM], df_mul_nr(spo, p0));
         }
     }
+}
 
-    // RK4 stage (runge_kutta_generic.f90:60-154): b = 1/6, 1/3, 1/3, 1/6;
-    // the stage inputs are u_n + dt/2 k1, u_n + dt/2 k2, u_n + dt k3
+// Per-point operands of the RK4 stage update that come from memory: the
+// copy of u_n (stages 1-3) or the bits of u_n itself (stage 4), and the
+// increment.
+template <int DIM>
+struct RkIn {
+    float2 u0[DIM + 1];
+    float2 acc[DIM + 1];
+};
+
+__device__ __forceinline__ float2 bits_f2(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return make_float2(__uint_as_float((unsigned)b), __uint_as_float((unsigned)(b >> 32)));
+}
+
+__device__ __forceinline__ double f2_bits(float2 v) {
+    return __longlong_as_double((long long)(((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x)));
+}
+
+template <int DIM>
+__device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int q, int ix, int iy, int iz, long long off,
+                                        RkIn<DIM> &in) {
+    const int npts_int = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
+    const long long cs = a.gt.npts();
+    const float2 *acc = a.acc + (long long)b * (DIM + 1) * npts_int + q;
+    if (a.stage > 1)
+#pragma unroll
+        for (int c = 0; c <= DIM; c++) in.acc[c] = acc[c * npts_int];
+    if (a.stage < 4) {
+#pragma unroll
+        for (int c = 0; c <= DIM; c++) in.u0[c] = a.u0[off + c * cs];
+    } else {
+        const long long us = a.gun.npts();
+        const double *un = a.un + (long long)b * (DIM + 1) * us +
+                           ((long long)(iz + (DIM == 3 ? a.gun.gb : 0)) * a.gun.ny + (iy + a.gun.gb)) * a.gun.nx +
+                           (ix + a.gun.gb);
+#pragma unroll
+        for (int c = 0; c <= DIM; c++) in.u0[c] = bits_f2(un[c * us]);
+    }
+}
+
+// RK4 stage update of one point (runge_kutta_generic.f90:60-154): b = 1/6,
+// 1/3, 1/3, 1/6; the stage inputs are u_n + dt/2 k1, u_n + dt/2 k2,
+// u_n + dt k3. q: interior index; (ix, iy, iz): interior coordinates; off:
+// the point's offset in the thin buffers (component 0).
+template <int DIM>
+__device__ __forceinline__ void rk_df(const StageArgsDF &a, const BlockDesc &d, int b, int q, int ix, int iy, int iz,
+                                      long long off, const df2 r[DIM + 1], const RkIn<DIM> &in) {
+    const int npts_int = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
+    const long long cs = a.gt.npts();
     const TreeClock &ck = a.clk[d.tree];
     const int j = a.stage;
     const df2 db = (j == 1 || j == 4) ? cf(ck.f_dt6) : cf(ck.f_dt3);
     float2 *acc = a.acc + (long long)b * (DIM + 1) * npts_int + q;
+    float2 *o = a.out + off;
     float2 ov[DIM + 1];
     if (j < 4) {
         const df2 da = j == 3 ? cf(ck.f_dt) : df_pow2(cf(ck.f_dt), 0.5f);
-        const float2 *u0 = a.u0 + off;
-        float2 *o = a.out + off;
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
             const df2 rc = df_norm(r[c]);
             const df2 inc = df_mul_nr(db, rc);
-            st(acc + c * npts_int, df_norm(j == 1 ? inc : df_add_nr(ld(acc + c * npts_int), inc)));
-            const df2 v = df_norm(df_add_nr(ld(u0 + c * cs), df_mul_nr(da, rc)));
+            st(acc + c * npts_int, df_norm(j == 1 ? inc : df_add_nr({in.acc[c].x, in.acc[c].y}, inc)));
+            const df2 v = df_norm(df_add_nr({in.u0[c].x, in.u0[c].y}, df_mul_nr(da, rc)));
             ov[c] = make_float2(v.hi, v.lo);
             o[c * cs] = ov[c];
         }
@@ -179,11 +209,10 @@ __global__ void __launch_bounds__(256) acm_stage_df_kernel(StageArgsDF a) {
         double *un = a.un + (long long)b * (DIM + 1) * us +
                      ((long long)(iz + (DIM == 3 ? a.gun.gb : 0)) * a.gun.ny + (iy + a.gun.gb)) * a.gun.nx +
                      (ix + a.gun.gb);
-        float2 *o = a.out + off;
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
-            const df2 inc = df_norm(df_add_nr(ld(acc + c * npts_int), df_mul_nr(db, df_norm(r[c]))));
-            const double v = __dadd_rn(__dadd_rn(un[c * us], f2d_bits(inc.hi)), f2d_bits(inc.lo));
+            const df2 inc = df_norm(df_add_nr({in.acc[c].x, in.acc[c].y}, df_mul_nr(db, df_norm(r[c]))));
+            const double v = __dadd_rn(__dadd_rn(f2_bits(in.u0[c]), f2d_bits(inc.hi)), f2d_bits(inc.lo));
             un[c * us] = v;
             const df2 w = df_split(v);
             ov[c] = make_float2(w.hi, w.lo);
@@ -193,10 +222,100 @@ __global__ void __launch_bounds__(256) acm_stage_df_kernel(StageArgsDF a) {
     if (a.push) push_ghosts<DIM, DIM + 1>(a.push, b, ix, iy, iz, a.Bs0, a.Bs1, a.Bs2, a.gt, a.out, cs, ov);
 }
 
+// One thread per interior point, stencil values read from global memory.
+// BS: the block edge when all Bs are equal to it (index arithmetic by
+// shifts), 0 for the general case.
+template <int DIM, bool MASK, int BS>
+__global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
+    const int Bs0 = BS ? BS : a.Bs0, Bs1 = BS ? BS : a.Bs1, Bs2 = BS ? BS : a.Bs2;
+    const int npts_int = Bs0 * Bs1 * (DIM == 3 ? Bs2 : 1);
+    const int chunks = BS ? (npts_int + 255) / 256 : a.chunks;
+    const int bi = blockIdx.x / chunks;
+    const int q = (blockIdx.x - bi * chunks) * blockDim.x + threadIdx.x;
+    if (q >= npts_int) return;
+    const int b = a.blk[bi];
+    const BlockDesc &d = a.desc[b];
+    const int ix = q % Bs0, iy = (q / Bs0) % Bs1, iz = DIM == 3 ? q / (Bs0 * Bs1) : 0;
+    const long long cs = a.gt.npts();
+    const long long off = (long long)b * (DIM + 1) * cs +
+                          ((long long)(iz + (DIM == 3 ? a.gt.gb : 0)) * a.gt.ny + (iy + a.gt.gb)) * a.gt.nx +
+                          (ix + a.gt.gb);
+    const int stv[3] = {1, a.gt.nx, a.gt.nx * a.gt.ny};
+    const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
+    df2 r[DIM + 1], vel[DIM], p0;
+    rhs_df<DIM, MASK>(a.in + off, cs, stv, d, a.tp[d.tree], m, npts_int, r, vel, p0);
+    RkIn<DIM> in;
+    rk_load<DIM>(a, b, q, ix, iy, iz, off, in);
+    rk_df<DIM>(a, d, b, q, ix, iy, iz, off, r, in);
+}
+
+// 3-D blocks of 16x16xBs2 points with 2 ghost layers (the stage-input
+// layout of FD_4th_central): each CTA of 256 threads takes a slab of ZT
+// interior planes of one block. One elected thread loads the slab's stencil
+// input (ZT+4 planes of 20x20 points per component, ghosts included) with
+// one TMA box per component into shared memory; every thread then walks its
+// (x, y) column through the slab, reading all stencil values from shared
+// memory at compile-time offsets. A TMA completion that does not arrive
+// within a second sets *err and ends the CTA.
+template <bool MASK, int ZT>
+__global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const __grid_constant__ CUtensorMap tin,
+                                                            int nslab, int *err) {
+    constexpr int NX = 20, NY = 20, GB = 2, BS = 16;
+    constexpr int PLANE = NX * NY, COMP = (ZT + 4) * PLANE;
+    extern __shared__ __align__(128) float2 sm[];
+    __shared__ unsigned long long bar;
+    const int bi = blockIdx.x / nslab, slab = blockIdx.x % nslab;
+    const int b = a.blk[bi];
+    const int zb = slab * ZT;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_arrive_expect_tx(&bar, (unsigned)(4 * COMP * sizeof(float2)));
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+            tma_load_3d(sm + c * COMP, &tin, 0, 0, (b * 4 + c) * a.gt.nz + zb + GB - 2, &bar);
+    }
+    __syncthreads();   // the barrier is initialised before anyone waits on it
+    const BlockDesc &d = a.desc[b];
+    const TreeParams &tp = a.tp[d.tree];
+    const int ix = threadIdx.x % BS, iy = threadIdx.x / BS;
+    const int npts_int = BS * BS * a.Bs2;
+    constexpr int stv[3] = {1, NX, PLANE};
+    const long long boff = (long long)b * 4 * a.gt.npts() + (long long)(iy + GB) * NX + (ix + GB);
+    // the memory operands of the RK update are fetched one plane ahead (the
+    // first plane's while the TMA load is in flight)
+    RkIn<3> nxt;
+    rk_load<3>(a, b, (zb * BS + iy) * BS + ix, ix, iy, zb, boff + (long long)(zb + GB) * PLANE, nxt);
+    if (!mbar_wait(&bar, 0, 1000000000ull)) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        return;
+    }
+#pragma unroll 1
+    for (int k = 0; k < ZT; k++) {
+        const int iz = zb + k;
+        const int q = (iz * BS + iy) * BS + ix;
+        const long long off = boff + (long long)(iz + GB) * PLANE;
+        const RkIn<3> cur = nxt;
+        if (k + 1 < ZT) rk_load<3>(a, b, q + BS * BS, ix, iy, iz + 1, off + PLANE, nxt);
+        const float2 *u = sm + ((k + 2) * NY + (iy + GB)) * NX + (ix + GB);
+        const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
+        df2 r[4], vel[3], p0;
+        rhs_df<3, MASK>(u, COMP, stv, d, tp, m, npts_int, r, vel, p0);
+        rk_df<3>(a, d, b, q, ix, iy, iz, off, r, cur);
+    }
+}
+
+// slab height of the tile kernel (0: not applicable): 16x16 planes, two
+// ghost layers, Bs2 a multiple of 4
+int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g) {
+    if (dim != 3 || Bs0 != 16 || Bs1 != 16 || g != 2 || Bs2 % 4) return 0;
+    return 4;
+}
+
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
                                 const TreeParams *tp, const TreeClock *clk, const void *in, const void *u0,
                                 void *out, BufGeo gt, double *un, BufGeo gun, void *acc, const void *maskdf,
-                                const int *push, int Bs0, int Bs1, int Bs2, cudaStream_t s) {
+                                const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int *err,
+                                cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
     StageArgsDF a;
     a.blk = blk;
@@ -216,16 +335,39 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.Bs1 = Bs1;
     a.Bs2 = Bs2;
     a.stage = stage;
+    const int zt = tmap ? tile_slab(dim, Bs0, Bs1, Bs2, gt.gb) : 0;
+    if (zt == 4 && gt.nx == 20 && gt.ny == 20) {
+        const int nslab = Bs2 / zt;
+        const size_t smem = sizeof(float2) * 4 * (size_t)(zt + 4) * gt.nx * gt.ny;
+        const CUtensorMap &map = *reinterpret_cast<const CUtensorMap *>(tmap);
+        auto kern = masked ? acm_stage_df_tile<true, 4> : acm_stage_df_tile<false, 4>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        a.chunks = 0;
+        kern<<<(unsigned)((long long)nblk * nslab), 256, smem, s>>>(a, map, nslab, err);
+        return cudaGetLastError();
+    }
     const int npts_int = Bs0 * Bs1 * (dim == 3 ? Bs2 : 1);
     const int threads = 256;
     a.chunks = (npts_int + threads - 1) / threads;
     const unsigned grid = (unsigned)((long long)nblk * a.chunks);
+    const bool b16 = Bs0 == 16 && Bs1 == 16 && (dim == 2 || Bs2 == 16);
     if (dim == 2) {
-        if (masked) acm_stage_df_kernel<2, true><<<grid, threads, 0, s>>>(a);
-        else acm_stage_df_kernel<2, false><<<grid, threads, 0, s>>>(a);
+        if (b16) {
+            if (masked) acm_stage_df_kernel<2, true, 16><<<grid, threads, 0, s>>>(a);
+            else acm_stage_df_kernel<2, false, 16><<<grid, threads, 0, s>>>(a);
+        } else {
+            if (masked) acm_stage_df_kernel<2, true, 0><<<grid, threads, 0, s>>>(a);
+            else acm_stage_df_kernel<2, false, 0><<<grid, threads, 0, s>>>(a);
+        }
     } else {
-        if (masked) acm_stage_df_kernel<3, true><<<grid, threads, 0, s>>>(a);
-        else acm_stage_df_kernel<3, false><<<grid, threads, 0, s>>>(a);
+        if (b16) {
+            if (masked) acm_stage_df_kernel<3, true, 16><<<grid, threads, 0, s>>>(a);
+            else acm_stage_df_kernel<3, false, 16><<<grid, threads, 0, s>>>(a);
+        } else {
+            if (masked) acm_stage_df_kernel<3, true, 0><<<grid, threads, 0, s>>>(a);
+            else acm_stage_df_kernel<3, false, 0><<<grid, threads, 0, s>>>(a);
+        }
     }
     return cudaGetLastError();
 }

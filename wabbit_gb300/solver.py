@@ -54,6 +54,18 @@ class Context:
     def set_variant(self, fast: bool):
         capi.check(self.L.wg_set_variant(self.h, 1 if fast else 0))
 
+    FORMS = {"auto": 0, "direct": 1, "tile": 2}
+
+    def set_stage_form(self, form: str):
+        """Form of the FP32-pipe stage kernel: auto (timed once per grid),
+        direct or tile (TMA-staged slabs)."""
+        capi.check(self.L.wg_set_stage_form(self.h, self.FORMS[form]))
+
+    def stage_form(self) -> str:
+        f = ctypes.c_int()
+        capi.check(self.L.wg_get_stage_form(self.h, ctypes.byref(f)))
+        return {v: k for k, v in self.FORMS.items()}[f.value]
+
     def synchronize(self):
         capi.check(self.L.wg_synchronize(self.h))
 
