@@ -3,18 +3,24 @@
 
 A step is one RK4 time step (timeStep_tree: ghost sync, dt, four RHS+RK
 stages) over every block of the workload grid. The default workload is the
-3-D ACM channel with a penalised sphere (Bs=16^3, g=6, CDF4,4, Jmax=6, FP64,
-~4.2k blocks; see wabbit_gb300/workloads.py).
+batched mixed-precision configuration: the 3-D ACM channel with a penalised
+sphere (Bs=16^3, g=6, CDF4,4) at Jmax=7, 36,688 blocks over five levels, the
+stencils and stage arithmetic in double-float on the FP32 units with the
+FP64 state, the RK4 step captured as one CUDA graph (see
+wabbit_gb300/workloads.py). `--workload acm3d_sphere` runs the FP64
+configuration at Jmax=6 (4,208 blocks).
 
 value: point-updates/s with the state resident in HBM, K steps replayed from
        a captured CUDA graph, timed with CUDA events on the solver's stream.
 e2e:   the same through the C ABI with host buffers: every step uploads the
        interior state from pinned host memory, runs wg_rk4_step (which reads
        back time and dt) and downloads the interior state.
+plain_fp64: the plain per-solve FP64 path on the same grid and IC (one
+       wg_rk4_step call per step, no graph), its speed and the relative L2
+       difference of the two states after K steps.
 roofline: the RK-stage kernel timed alone (CUDA events, mean over launches)
-       against the measured HBM copy bandwidth, plus its FP64 rate against
-       the FP64 FMA peak measured in the same run (the kernel is FP64-ALU
-       bound on GB300).
+       against the measured HBM copy bandwidth; for the FP64 precision also
+       its FP64 rate against the FP64 FMA peak measured in the same run.
 cpu_baseline: the CPU oracle (a scalar C++ restatement of the reference's
        Fortran, OpenMP over blocks) on a bounded sample of the same physics.
 
@@ -51,16 +57,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="acm3d_sphere")
+    ap.add_argument("--workload", default="acm3d_sphere_j7")
     ap.add_argument("--variant", choices=["fast", "strict"], default="fast")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--jmax", type=int, default=None, help="override the workload's Jmax (smaller cases)")
     ap.add_argument("--precision", choices=["fp64", "fp32"], default=None,
                     help="RHS stencil precision (default: the workload's; fp32 = double-float on the FP32 units)")
-    ap.add_argument("--compare-plain", action="store_true",
+    ap.add_argument("--rate", type=float, default=8.0, help="serving: Poisson arrival rate (requests/s)")
+    ap.add_argument("--requests", type=int, default=256, help="serving: number of requests")
+    ap.add_argument("--budget-gb", type=float, default=64.0, help="serving: HBM budget of the arenas")
+    ap.add_argument("--compare-plain", choices=["auto", "on", "off"], default="auto",
                     help="also time the plain per-solve FP64 path (one wg_rk4_step call per step, no graph) "
-                         "and report the speed-up and the L2 difference of the two after K steps")
+                         "and report the speed-up and the L2 difference of the two after K steps "
+                         "(auto: on for the FP32-pipe precision)")
     return ap.parse_args()
 
 
@@ -268,13 +278,17 @@ def run_ours(args, rank, world):
     stage_ms = f.time_kernel(0, reps=20)
     sync_ms = f.time_kernel(1, reps=20)
     dt_ms = f.time_kernel(2, reps=20)
-    bytes_stage = 8.0 * npts * cfg.neq * WORDS_PER_POINT_STAGE + 8.0 * nmasked * npts_blk * MASK_WORDS
+    mask_words = MASK_WORDS if cfg.rhs_precision == 0 else MASK_WORDS - 1   # the FP32-pipe mask folds the colour
+    bytes_stage = 8.0 * npts * cfg.neq * WORDS_PER_POINT_STAGE + 8.0 * nmasked * npts_blk * mask_words
     flops_stage = float(FLOPS_PER_POINT_STAGE[dim]) * npts
     hbm_peak, hbm_src = measured_peaks()
     fp64_peak, fp32_peak = probe_alu()
     ach_gbs = bytes_stage / (stage_ms * 1e-3) / 1e9
     ach_tf = flops_stage / (stage_ms * 1e-3) / 1e12
     traffic = profile_traffic(args.workload)
+    form = ctx.stage_form() if cfg.rhs_precision else "direct"
+    stage_kernel = ("acm_stage_kernel (FP64)" if cfg.rhs_precision == 0 else
+                    "acm_stage_df_tile (TMA slabs)" if form == "tile" else "acm_stage_df_kernel")
 
     # e2e through the C ABI with host buffers
     e2e = None
@@ -298,7 +312,7 @@ def run_ours(args, rank, world):
                "steps": k, "path": "wg_upload_interior + wg_rk4_step + wg_download_interior (pinned host)"}
 
     plain = None
-    if args.compare_plain:
+    if args.compare_plain == "on" or (args.compare_plain == "auto" and cfg.rhs_precision == 1):
         plain = compare_plain(args, cfg, lv, co, u0, ids, masks, f, ctx, value / max(world, 1), npts)
 
     cpu = None
@@ -307,6 +321,8 @@ def run_ours(args, rank, world):
         cpu = {"value": v, "unit": "point-updates/s", "cores": cores, "kind": "port", "sample": sample}
 
     clocks = clk.summary()
+    # bytes one RK stage touches (input, u_n copy, increment, next input)
+    state_gb = nblk * cfg.neq * 8.0 * ((cfg.Bs[0] + 2 * cfg.g_rhs) ** dim + 3 * npts_blk) / 1e9
     line = {
         "metric": "ACM point-updates/s/GPU",
         "value": value,
@@ -325,25 +341,29 @@ def run_ours(args, rank, world):
             "wavelet": cfg.wavelet.decode(), "Jmax": cfg.Jmax, "blocks": nblk, "points": npts,
             "masked_blocks": nmasked, "levels": np.bincount(lv).tolist(), "variant": args.variant,
             "rhs_precision": "fp64" if cfg.rhs_precision == 0 else "fp32-pipe double-float",
-            "stage_form": ctx.stage_form() if cfg.rhs_precision else "direct",
-            "rk": "RK4", "graph": True, "l2": "state 2.9 GB > 129 MB L2 (no flush needed)" if dim == 3 else
-            "inputs smaller than L2",
+            "stage_form": form,
+            "rk": "RK4", "graph": True,
+            "l2": (f"stage buffers {state_gb:.1f} GB > 129 MB L2 (no flush needed)" if state_gb > 0.5 else
+                   f"stage buffers {state_gb:.2f} GB: each stage streams more than L2 holds"),
             "parallelism": "replicas" if world > 1 else "1 GPU",
         },
         "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": ach_gbs / hbm_peak, "traffic": traffic, "kernel": "acm_stage_kernel",
+                     "frac": ach_gbs / hbm_peak, "traffic": traffic, "kernel": stage_kernel,
                      "launch_ms": stage_ms, "peak_source": hbm_src,
-                     "algorithmic_bytes_per_launch": bytes_stage},
-        "roofline_alu": {"bound": "fp64", "achieved": ach_tf, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": ach_tf / fp64_peak, "flops_per_launch": flops_stage,
-                         "peak_source": "FP64 FMA probe measured in this run (wg_probe_alu)",
-                         "fp32_peak_tflops": fp32_peak},
+                     "algorithmic_bytes_per_launch": bytes_stage,
+                     "bytes_per_point": "5 state words x neq x 8 B (stage input, u_n, increment read+write, "
+                                        "next input) + mask words of masked blocks"},
         "kernels_ms": {"acm_stage": stage_ms, "sync_rhs": sync_ms, "dt": dt_ms},
         "gpu_launches": graph_kernels * args.steps,
         "clocks": clocks,
         "t_end": t_end,
         "dt_last": dt_last,
     }
+    if cfg.rhs_precision == 0:
+        line["roofline_alu"] = {"bound": "fp64", "achieved": ach_tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                                "frac": ach_tf / fp64_peak, "flops_per_launch": flops_stage,
+                                "peak_source": "FP64 FMA probe measured in this run (wg_probe_alu)",
+                                "fp32_peak_tflops": fp32_peak}
     if e2e is not None:
         line["e2e"] = e2e
     if plain is not None:
@@ -396,6 +416,42 @@ def compare_plain(args, cfg, lv, co, u0, ids, masks, f, ctx, value, npts):
     ctx64.close()
     return {"value": v_plain, "unit": "point-updates/s", "speedup": value / v_plain, "steps": k,
             "rel_l2_after_steps": err, "path": "FP64 strict-order-free fast stencils, wg_rk4_step per step, no graph"}
+
+
+def run_serving(args, rank, world):
+    """Serving workload: a seeded Poisson stream of independent solves
+    (2-D and 3-D, 64-8192 blocks, 50 RK4 steps each), admitted by HBM
+    footprint and stepped in batched launches; aggregate point-updates/s
+    with p50/p99 time to solution (arrival to result on the host)."""
+    import torch
+    from wabbit_gb300 import build, serving
+    build.build()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    stream = serving.make_stream(args.requests, rate=args.rate, seed=4 + rank)
+    srv = serving.Server(budget_gb=args.budget_gb, chunk=5)
+    # warm-up: one small solve of each geometry (graph capture, autotuning)
+    srv.run([serving.Request(-1, 0.0, 2, 0, 1, 1e-3, nsteps=5), serving.Request(-2, 0.0, 3, 0, 2, 1e-3, nsteps=5)],
+            realtime=False)
+    barrier(world)
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        recs, summ = srv.run(stream, realtime=True)
+    srv.close()
+    wall = max_over_ranks(summ["wall_s"], world)
+    total = sum_over_ranks(summ["point_updates"], world)
+    line = {
+        "metric": "ACM point-updates/s/GPU", "value": total / wall, "unit": "point-updates/s", "n_gpus": world,
+        "steps": 50, "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 state, double-float (2xf32) stencils",
+        "data": "synthetic (seeded Poisson stream, vortex ICs; see wabbit_gb300/serving.py)",
+        "config": {"workload": "serving", "requests": args.requests, "arrival_rate_per_s": args.rate,
+                   "budget_gb": args.budget_gb, "chunk_steps": 5, "arena_blocks": srv.capacity,
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "serving": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "wall_s": summ["wall_s"],
+                    "requests": summ["requests"], "point_updates": summ["point_updates"]},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
 
 
 def capi_graph_kernels(ctx):
@@ -458,6 +514,8 @@ def main():
     rank, world = dist_init(args.gpus)
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "serving":
+        run_serving(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:

@@ -137,7 +137,9 @@ int wg_get_grid(wg_ctx *ctx, int tree, int cap, int *level, int *coords);
 int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks);
 int wg_download_state(wg_ctx *ctx, int tree, double *host_blocks);
 /* Interior points only, compact (nblk, neq, Bz, By, Bx) x fastest: one
- * contiguous copy each way; ghost nodes are refilled by the next sync. */
+ * contiguous copy each way; ghost nodes are refilled by the next sync. The
+ * array may be host memory (pageable or pinned) or device memory of the
+ * context's GPU (unified addressing picks the copy direction). */
 int wg_upload_interior(wg_ctx *ctx, int tree, const double *host);
 int wg_download_interior(wg_ctx *ctx, int tree, double *host);
 /* Penalisation mask in the layout of hvy_mask (..., 1:6, Nb): chi, usx,

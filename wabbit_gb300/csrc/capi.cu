@@ -84,6 +84,25 @@ struct SyncPlan {
     bool push_ok = false;
 };
 
+// The per-step work of several trees of the FP32-pipe precision fused into
+// one launch per kernel: their block lists, ghost gather entries and
+// prediction patches concatenated (the trees share the block geometry and
+// the wavelet, so their syncs have the same stages).
+struct BatchPlan {
+    std::vector<int> trees;
+    int version = -1;
+    DevArray<int> all, plain, masked, tree_ids;
+    int n_all = 0, n_plain = 0, n_masked = 0;
+    int nstages = 0;
+    std::vector<int> stage_predict;
+    DevArray<uint2> pairs;              // per stage: copies of all trees, then the other entries
+    std::vector<unsigned> pair_begin, copy_end;
+    DevArray<Patch> predict;            // per stage: prediction patches of all trees
+    std::vector<int> pred_begin;
+    int max_coarse = 0;
+    bool push = false;                  // every tree's copies are pushed by the stage kernels
+};
+
 struct Tree {
     bool live = false;
     wg_config cfg;
@@ -138,6 +157,7 @@ struct wg_ctx {
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<int> graph_trees;
     int graph_version = -1;
+    BatchPlan batch;
     int grid_version = 0;
 };
 
@@ -571,6 +591,137 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true, push))) return st;
     if ((st = stage_launch_df(ctx, t, 4, ctx->C, ctx->B, push))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
+    return WG_OK;
+}
+
+// (re)build ctx->batch for the listed trees (FP32-pipe precision)
+int build_batch(wg_ctx *ctx, const std::vector<int> &trees) {
+    BatchPlan &bp = ctx->batch;
+    if (bp.version == ctx->grid_version && bp.trees == trees) return WG_OK;
+    std::vector<SyncPlan *> plans;
+    bool push = true;
+    for (int id : trees) {
+        Tree &t = ctx->trees[id];
+        SyncPlan *sp;
+        int st = get_sync(ctx, t, ctx->cfg.g_rhs, ctx->cfg.g_rhs, true, &sp);
+        if (st) return st;
+        if (sp->pair_begin.empty()) return fail(WG_ENOTSUP, "batched step needs the gather form of the ghost sync");
+        push = push && sp->push_ok;
+        plans.push_back(sp);
+    }
+    const int ns = plans[0]->table.nstages;
+    std::vector<int> all, plain, masked;
+    for (int id : trees) {
+        Tree &t = ctx->trees[id];
+        for (size_t b = 0; b < t.slots.size(); b++) {
+            all.push_back(t.slots[b]);
+            (t.mask_slot[b] >= 0 ? masked : plain).push_back(t.slots[b]);
+        }
+    }
+    bp.n_all = (int)all.size();
+    bp.n_plain = (int)plain.size();
+    bp.n_masked = (int)masked.size();
+    WG_CUDA_OK(bp.all.upload(all.data(), all.size(), ctx->stream));
+    WG_CUDA_OK(bp.plain.upload(plain.data(), plain.size(), ctx->stream));
+    WG_CUDA_OK(bp.masked.upload(masked.data(), masked.size(), ctx->stream));
+    WG_CUDA_OK(bp.tree_ids.upload(trees.data(), trees.size(), ctx->stream));
+    // gather entries and prediction patches, stage by stage
+    bp.nstages = ns;
+    bp.stage_predict = plans[0]->table.stage_predict;
+    bp.pair_begin.assign(ns + 1, 0);
+    bp.copy_end.assign(ns, 0);
+    bp.pred_begin.assign(ns + 1, 0);
+    bp.max_coarse = 0;
+    unsigned long long total = 0;
+    std::vector<Patch> pred;
+    for (int st = 0; st < ns; st++) {
+        bp.pair_begin[st] = (unsigned)total;
+        bp.pred_begin[st] = (int)pred.size();
+        for (SyncPlan *sp : plans) total += sp->pair_begin[st + 1] - sp->pair_begin[st];
+        for (SyncPlan *sp : plans) {
+            if (!sp->table.stage_predict[st]) continue;
+            const auto &pt = sp->table.patches;
+            pred.insert(pred.end(), pt.begin() + sp->table.stage_begin[st], pt.begin() + sp->table.stage_begin[st + 1]);
+            bp.max_coarse = std::max(bp.max_coarse, sp->table.max_coarse);
+        }
+    }
+    bp.pair_begin[ns] = (unsigned)total;
+    bp.pred_begin[ns] = (int)pred.size();
+    if (total >= (1ull << 32)) return fail(WG_ENOTSUP, "batched ghost gather exceeds 2^32 entries");
+    WG_CUDA_OK(bp.pairs.upload(nullptr, total, ctx->stream));
+    WG_CUDA_OK(bp.predict.upload(pred.data(), pred.size(), ctx->stream));
+    for (int st = 0; st < ns; st++) {
+        unsigned at = bp.pair_begin[st];
+        for (int pass = 0; pass < 2; pass++) {          // copies of every tree first
+            for (SyncPlan *sp : plans) {
+                const unsigned b = pass == 0 ? sp->pair_begin[st] : sp->copy_end[st];
+                const unsigned e = pass == 0 ? sp->copy_end[st] : sp->pair_begin[st + 1];
+                if (e > b)
+                    WG_CUDA_OK(cudaMemcpyAsync(bp.pairs.p + at, sp->pairs.p + b, sizeof(uint2) * (e - b),
+                                               cudaMemcpyDeviceToDevice, ctx->stream));
+                at += e - b;
+            }
+            if (pass == 0) bp.copy_end[st] = at;
+        }
+    }
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    bp.push = push;
+    bp.trees = trees;
+    bp.version = ctx->grid_version;
+    return WG_OK;
+}
+
+int run_sync_batch(wg_ctx *ctx, double *buf) {
+    const BatchPlan &bp = ctx->batch;
+    for (int s = 0; s < bp.nstages; s++) {
+        if (bp.stage_predict[s]) {
+            WG_CUDA_OK(launch_predict_df(bp.predict.p + bp.pred_begin[s], bp.pred_begin[s + 1] - bp.pred_begin[s],
+                                         bp.max_coarse, buf, ctx->gT, ctx->geo.nc, ctx->wav.order_predictor,
+                                         ctx->stream));
+        } else {
+            const unsigned from = bp.push ? bp.copy_end[s] : bp.pair_begin[s];
+            WG_CUDA_OK(launch_gather(bp.pairs.p + from, bp.pair_begin[s + 1] - from, buf, ctx->gT, ctx->geo.nc,
+                                     ctx->stream));
+        }
+    }
+    return WG_OK;
+}
+
+int stage_launch_batch(wg_ctx *ctx, int stage, const double *in, double *out) {
+    const BatchPlan &bp = ctx->batch;
+    const int dim = ctx->cfg.dim;
+    const int *Bs = ctx->cfg.Bs;
+    const int *pp = bp.push ? ctx->d_push : nullptr;
+    const void *tm = nullptr;
+    const int form = ctx->stage_form != WG_FORM_AUTO ? ctx->stage_form : ctx->tuned_form ? ctx->tuned_form : WG_FORM_DIRECT;
+    if (ctx->have_tm && form == WG_FORM_TILE)
+        tm = in == ctx->B ? &ctx->tm[0] : in == ctx->C ? &ctx->tm[1] : in == ctx->D ? &ctx->tm[2] : nullptr;
+    WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, bp.plain.p, bp.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
+                                   ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
+                                   Bs[2], tm, ctx->d_err, ctx->stream));
+    WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, bp.masked.p, bp.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
+                                   ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
+                                   Bs[2], tm, ctx->d_err, ctx->stream));
+    return WG_OK;
+}
+
+// one RK4 step of every tree of ctx->batch (FP32-pipe precision): the same
+// sequence as rk4_enqueue_df, each kernel launched once for all trees
+int rk4_enqueue_batch(wg_ctx *ctx) {
+    const BatchPlan &bp = ctx->batch;
+    const int *Bs = ctx->cfg.Bs;
+    int st;
+    if ((st = run_sync_batch(ctx, ctx->B))) return st;
+    WG_CUDA_OK(launch_dt(ctx->cfg.dim, bp.all.p, bp.n_all, ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A, ctx->gA, Bs[0],
+                         Bs[1], Bs[2], (int)bp.trees.size(), bp.tree_ids.p, ctx->stream));
+    if ((st = stage_launch_batch(ctx, 1, ctx->B, ctx->C))) return st;
+    if ((st = run_sync_batch(ctx, ctx->C))) return st;
+    if ((st = stage_launch_batch(ctx, 2, ctx->C, ctx->D))) return st;
+    if ((st = run_sync_batch(ctx, ctx->D))) return st;
+    if ((st = stage_launch_batch(ctx, 3, ctx->D, ctx->C))) return st;
+    if ((st = run_sync_batch(ctx, ctx->C))) return st;
+    if ((st = stage_launch_batch(ctx, 4, ctx->C, ctx->B))) return st;
+    WG_CUDA_OK(launch_clock_advance(ctx->d_clk, bp.tree_ids.p, (int)bp.trees.size(), ctx->stream));
     return WG_OK;
 }
 
@@ -1091,15 +1242,30 @@ int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph)
     for (int i = 0; i < ntrees; i++) {
         Tree *t = get_tree(ctx, trees[i]);
         if (!t) return WG_EINVAL;
+        for (int k = 0; k < i; k++)
+            if (trees[k] == trees[i]) return fail(WG_EINVAL, "tree %d listed twice", trees[i]);
         int st = ensure_shadow(ctx, *t);
         if (st) return st;
     }
+    // the FP32-pipe precision steps all listed trees with one launch per
+    // kernel (batched); the FP64 precision tree by tree
+    const bool batched = ctx->precision == WG_RHS_FP32;
+    if (batched) {
+        int st = build_batch(ctx, std::vector<int>(trees, trees + ntrees));
+        if (st) return st;
+    }
     if (!use_graph) {
-        for (int s = 0; s < nsteps; s++)
+        for (int s = 0; s < nsteps; s++) {
+            if (batched) {
+                int st = rk4_enqueue_batch(ctx);
+                if (st) return st;
+                continue;
+            }
             for (int i = 0; i < ntrees; i++) {
                 int st = rk4_enqueue(ctx, trees[i]);
                 if (st) return st;
             }
+        }
         return WG_OK;
     }
     const bool same = ctx->graph_exec && ctx->graph_version == ctx->grid_version &&
@@ -1124,7 +1290,8 @@ int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph)
         ctx->graph = nullptr;
         WG_CUDA_OK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         int st = WG_OK;
-        for (int i = 0; i < ntrees && !st; i++) st = rk4_enqueue(ctx, trees[i]);
+        if (batched) st = rk4_enqueue_batch(ctx);
+        for (int i = 0; i < ntrees && !st && !batched; i++) st = rk4_enqueue(ctx, trees[i]);
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
         if (st) {
@@ -1446,7 +1613,7 @@ int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
     const size_t bytes = sizeof(double) * t->slots.size() * ctx->geo.nc * ctx->nint;
     int st = ensure_staging(ctx, bytes);
     if (st) return st;
-    WG_CUDA_OK(cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    WG_CUDA_OK(cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyDefault, ctx->stream));   // host or device memory
     WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, ctx->staging, ctx->geo.nc,
                                     Bs[0], Bs[1], Bz, 1, ctx->stream));
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
@@ -1463,7 +1630,7 @@ int wg_download_interior(wg_ctx *ctx, int tree, double *host) {
     if (st) return st;
     WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, ctx->staging, ctx->geo.nc,
                                     Bs[0], Bs[1], Bz, 0, ctx->stream));
-    WG_CUDA_OK(cudaMemcpyAsync(host, ctx->staging, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    WG_CUDA_OK(cudaMemcpyAsync(host, ctx->staging, bytes, cudaMemcpyDefault, ctx->stream));   // host or device memory
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     return WG_OK;
 }

@@ -1,0 +1,295 @@
+"""Serving loop: independent ACM solves admitted as they arrive, batched on
+the device.
+
+Requests are independent solves (the reference's tree_ID, LIB/MESH/forest.f90:
+one tree per solve) of one of two block geometries: 2-D (Bs=16, CDF4,0, g=4)
+or 3-D (Bs=16^3, CDF4,4, g=6). Each geometry has one context whose arena is
+sized from an HBM budget. The loop
+
+* admits queued requests first come first served per geometry as soon as
+  the arena has free slots for their blocks (admission by HBM footprint),
+* steps every active solve of a context with one wg_run per scheduling
+  round: one launch per kernel for all of them (batched FP32-pipe stages),
+  the two contexts on their own streams so that their work overlaps,
+* retires solves that reached their step count (downloads the interior
+  state, frees the slots) and records the time to solution.
+
+A solve's result does not depend on which other solves share its launches
+(every kernel works per block and per tree), so a solve served in the mix is
+bit-identical to the same solve run alone with the same step chunks.
+
+Synthetic stream (seeded): Poisson arrivals; half 2-D, half 3-D; grid sizes
+from a ladder spanning 64-2048 (2-D) and 512-8192 (3-D) blocks; Gaussian
+velocity-vortex initial conditions (2-D: point vortices; 3-D: vortex tubes
+with a uniformly random axis), nu ~ U[5e-4, 5e-3], p = 0, periodic unit
+domain, no mask.
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+
+import numpy as np
+
+from . import config, grids
+from .solver import Context
+
+# block-count ladders of the request grids (level jmin equidistant, refined
+# around a ball with the given radius at the next levels)
+LADDER = {
+    2: [(3, 3, 0.0), (3, 4, 0.22), (4, 4, 0.0), (4, 5, 0.18), (5, 5, 0.0), (5, 6, 0.3)],        # 64 .. 2020
+    3: [(3, 3, 0.0), (3, 4, 0.22), (3, 4, 0.32), (4, 4, 0.0), (4, 5, 0.17), (4, 5, 0.26)],     # 512 .. ~7700
+}
+
+
+def geometry(dim: int):
+    c = config.defaults(dim)
+    for d in range(dim):
+        c.Bs[d] = 16
+    c.domain[0] = c.domain[1] = c.domain[2] = 1.0
+    if dim == 2:
+        c.wavelet, c.g, c.g_rhs = b"CDF40", 4, 2
+    else:
+        c.wavelet, c.g, c.g_rhs = b"CDF44", 6, 2
+    c.Jmin, c.Jmax = 2, 7
+    c.c0, c.gamma_p = (20.0 if dim == 2 else 15.0), 1.0
+    c.penalization = 0
+    c.CFL = 0.5
+    c.time_max = 1e9
+    c.rhs_precision = 1
+    return c
+
+
+_grid_cache: dict = {}
+
+
+def request_grid(dim: int, size: int):
+    key = (dim, size)
+    if key not in _grid_cache:
+        jmin, jmax, r = LADDER[dim][size]
+        if jmax == jmin:
+            lv, co = grids.equidistant(dim, jmin)
+        else:
+            lv, co = grids.refined_around(dim, jmin, jmax, [1.0, 1.0, 1.0], [0.5, 0.5, 0.5],
+                                          lambda l, r=r: r)
+        _grid_cache[key] = (lv, co)
+    return _grid_cache[key]
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    arrival: float      # seconds after the start of the stream
+    dim: int
+    size: int           # index into LADDER[dim]
+    seed: int
+    nu: float
+    nsteps: int = 50
+
+
+def make_stream(n: int = 256, rate: float = 8.0, seed: int = 4, nsteps: int = 50, dims=(2, 3)):
+    """Seeded Poisson stream of n requests (rate per second)."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    out = []
+    for i in range(n):
+        dim = int(dims[rng.integers(len(dims))])
+        out.append(Request(i, float(t[i]), dim, int(rng.integers(len(LADDER[dim]))), int(rng.integers(1 << 31)),
+                           float(rng.uniform(5e-4, 5e-3)), nsteps))
+    return out
+
+
+def vortex_ic(cfg, lv, co, seed: int, nvort: int = 6):
+    """Interior IC (nblk, neq, Bz, By, Bx): Gaussian velocity vortices
+    u = G/(pi R^2) exp(-r^2/R^2) (axis x r) with minimum-image distances on
+    the unit torus; 2-D: axis = z; 3-D: tubes with a random unit axis."""
+    rng = np.random.default_rng(seed)
+    dim = cfg.dim
+    x0, dx = grids.block_geometry(lv, co, cfg.domain, cfg.Bs, dim)
+    Bx, By = cfg.Bs[0], cfg.Bs[1]
+    Bz = cfg.Bs[2] if dim == 3 else 1
+    nb = len(lv)
+    X = x0[:, 0, None, None, None] + np.arange(Bx)[None, None, None, :] * dx[:, 0, None, None, None]
+    Y = x0[:, 1, None, None, None] + np.arange(By)[None, None, :, None] * dx[:, 1, None, None, None]
+    Z = (x0[:, 2, None, None, None] + np.arange(Bz)[None, :, None, None] * dx[:, 2, None, None, None]
+         if dim == 3 else np.zeros((nb, 1, 1, 1)))
+    u = np.zeros((nb, dim + 1, Bz, By, Bx))
+    for _ in range(nvort):
+        c = rng.uniform(0.0, 1.0, size=3)
+        R = rng.uniform(0.05, 0.12)
+        G = rng.normal(0.0, 1.0)
+        a = np.array([0.0, 0.0, 1.0])
+        if dim == 3:
+            a = rng.normal(size=3)
+            a /= np.linalg.norm(a)
+        r = [X - c[0], Y - c[1], Z - c[2] if dim == 3 else np.zeros_like(X)]
+        r = [q - np.rint(q) for q in r]
+        ra = r[0] * a[0] + r[1] * a[1] + r[2] * a[2]
+        rp = [r[k] - ra * a[k] for k in range(3)]
+        amp = G / (np.pi * R * R) * np.exp(-(rp[0] ** 2 + rp[1] ** 2 + rp[2] ** 2) / (R * R))
+        # a x r_perp
+        cr = [a[1] * rp[2] - a[2] * rp[1], a[2] * rp[0] - a[0] * rp[2], a[0] * rp[1] - a[1] * rp[0]]
+        for k in range(dim):
+            u[:, k] += amp * cr[k]
+    return u
+
+
+def vortex_ic_device(cfg, lv, co, seed: int, nvort: int = 6):
+    """vortex_ic evaluated on the GPU (torch, float64): the same vortex
+    parameters (drawn on the host from the seed), the arithmetic on the
+    device so that large requests are set up in milliseconds."""
+    import torch
+    rng = np.random.default_rng(seed)
+    dim = cfg.dim
+    dev = torch.device("cuda")
+    x0, dx = grids.block_geometry(lv, co, cfg.domain, cfg.Bs, dim)
+    x0 = torch.as_tensor(x0, device=dev)
+    dx = torch.as_tensor(dx, device=dev)
+    Bx, By = cfg.Bs[0], cfg.Bs[1]
+    Bz = cfg.Bs[2] if dim == 3 else 1
+    nb = len(lv)
+    ar = lambda n: torch.arange(n, device=dev, dtype=torch.float64)
+    X = x0[:, 0, None, None, None] + ar(Bx)[None, None, None, :] * dx[:, 0, None, None, None]
+    Y = x0[:, 1, None, None, None] + ar(By)[None, None, :, None] * dx[:, 1, None, None, None]
+    Z = (x0[:, 2, None, None, None] + ar(Bz)[None, :, None, None] * dx[:, 2, None, None, None]
+         if dim == 3 else torch.zeros((nb, 1, 1, 1), device=dev, dtype=torch.float64))
+    u = torch.zeros((nb, dim + 1, Bz, By, Bx), device=dev, dtype=torch.float64)
+    for _ in range(nvort):
+        c = rng.uniform(0.0, 1.0, size=3)
+        R = rng.uniform(0.05, 0.12)
+        G = rng.normal(0.0, 1.0)
+        a = np.array([0.0, 0.0, 1.0])
+        if dim == 3:
+            a = rng.normal(size=3)
+            a /= np.linalg.norm(a)
+        r = [X - c[0], Y - c[1], Z - c[2] if dim == 3 else torch.zeros_like(X)]
+        r = [q - torch.round(q) for q in r]
+        ra = r[0] * a[0] + r[1] * a[1] + r[2] * a[2]
+        rp = [r[k] - ra * a[k] for k in range(3)]
+        amp = G / (np.pi * R * R) * torch.exp(-(rp[0] ** 2 + rp[1] ** 2 + rp[2] ** 2) / (R * R))
+        cr = [a[1] * rp[2] - a[2] * rp[1], a[2] * rp[0] - a[0] * rp[2], a[0] * rp[1] - a[1] * rp[0]]
+        for k in range(dim):
+            u[:, k] += amp * cr[k]
+    return u
+
+
+class Solve:
+    """One admitted request: its tree in the context of its geometry."""
+
+    def __init__(self, req: Request, ctx: Context, base):
+        self.req = req
+        cfg = base.copy()
+        cfg.nu = req.nu
+        self.cfg = cfg
+        lv, co = request_grid(req.dim, req.size)
+        self.nblk = len(lv)
+        self.f = ctx.forest(cfg)
+        self.f.set_grid(lv, co)
+        self.f.upload_interior(vortex_ic_device(cfg, lv, co, req.seed))
+        self.f.set_time(0.0)
+        self.done = 0
+        self.points = self.nblk * int(np.prod([cfg.Bs[d] for d in range(cfg.dim)]))
+
+
+class Server:
+    def __init__(self, budget_gb: float = 64.0, chunk: int = 5, share_3d: float = 0.85, keep_results=False):
+        from . import capi
+        self.chunk = chunk
+        self.keep = keep_results
+        self.base = {2: geometry(2), 3: geometry(3)}
+        L = capi.load()
+        self.ctx = {}
+        for dim, share in ((3, share_3d), (2, 1.0 - share_3d)):
+            per = L.wg_bytes_per_block(self.base[dim])
+            cap = max(64, int(budget_gb * 1e9 * share / per))
+            self.ctx[dim] = Context(self.base[dim], cap)
+        self.capacity = {d: self.ctx[d].max_blocks for d in self.ctx}
+
+    def close(self):
+        for c in self.ctx.values():
+            c.close()
+
+    def run(self, requests, realtime: bool = True):
+        """Serve the stream; returns per-request records and totals."""
+        queue = {2: [], 3: []}
+        pending = sorted(requests, key=lambda r: r.arrival)
+        active = {2: [], 3: []}
+        used = {2: 0, 3: 0}
+        records = {}
+        t0 = time.perf_counter()
+        total_points = 0
+        while pending or any(queue.values()) or any(active.values()):
+            now = time.perf_counter() - t0
+            if not realtime:   # every request has arrived
+                now = float("inf")
+            while pending and pending[0].arrival <= now:
+                r = pending.pop(0)
+                queue[r.dim].append(r)
+            for dim in (3, 2):
+                while queue[dim]:
+                    r = queue[dim][0]
+                    nb = len(request_grid(dim, r.size)[0])
+                    if nb > self.capacity[dim]:
+                        raise ValueError(f"request {r.rid} ({nb} blocks) exceeds the {dim}-D arena")
+                    if used[dim] + nb > self.capacity[dim]:
+                        break
+                    queue[dim].pop(0)
+                    s = Solve(r, self.ctx[dim], self.base[dim])
+                    s.admitted = time.perf_counter() - t0
+                    used[dim] += s.nblk
+                    active[dim].append(s)
+            if not any(active.values()):
+                if pending:
+                    time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
+                continue
+            # one scheduling round: every active solve advances one chunk
+            for dim in (3, 2):
+                if active[dim]:
+                    k = min(self.chunk, min(s.req.nsteps - s.done for s in active[dim]))
+                    self.ctx[dim].run([s.f for s in active[dim]], k, use_graph=True)
+                    for s in active[dim]:
+                        s.done += k
+                        total_points += s.points * k
+            for dim in (3, 2):
+                self.ctx[dim].synchronize()
+            for dim in (3, 2):
+                keep = []
+                for s in active[dim]:
+                    if s.done < s.req.nsteps:
+                        keep.append(s)
+                        continue
+                    u = s.f.download_interior()
+                    t_done = time.perf_counter() - t0
+                    rec = {"rid": s.req.rid, "dim": dim, "blocks": s.nblk, "arrival": s.req.arrival,
+                           "admitted": s.admitted, "done": t_done,
+                           "tts": t_done - (s.req.arrival if realtime else 0.0),
+                           "time": s.f.time()[0], "checksum": float(np.sum(u * u))}
+                    if self.keep:
+                        rec["u"] = u
+                    records[s.req.rid] = rec
+                    s.f.destroy()
+                    used[dim] -= s.nblk
+                active[dim] = keep
+        wall = time.perf_counter() - t0
+        tts = np.array([r["tts"] for r in records.values()])
+        summary = {"requests": len(records), "wall_s": wall, "point_updates": total_points,
+                   "throughput": total_points / wall,
+                   "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99))}
+        return records, summary
+
+
+def solve_alone(req: Request, chunk: int = 5):
+    """The same request on its own context, in the same step chunks."""
+    base = geometry(req.dim)
+    lv, _ = request_grid(req.dim, req.size)
+    ctx = Context(base, len(lv) + 4)
+    try:
+        s = Solve(req, ctx, base)
+        while s.done < req.nsteps:
+            k = min(chunk, req.nsteps - s.done)
+            ctx.run([s.f], k, use_graph=True)
+            s.done += k
+        ctx.synchronize()
+        return s.f.download_interior(), s.f.time()[0]
+    finally:
+        ctx.close()

@@ -139,8 +139,20 @@ class Forest:
         return (c.neq, c.Bs[2] if c.dim == 3 else 1, c.Bs[1], c.Bs[0])
 
     def upload_interior(self, data):
+        """Interior state (nblk, neq, Bz, By, Bx) from a numpy array or a
+        contiguous float64 CUDA tensor (device memory is copied on the
+        device after the tensor's stream has finished writing it)."""
+        n = self.nblocks * int(np.prod(self.interior_shape))
+        if hasattr(data, "data_ptr") and getattr(data, "is_cuda", False):
+            import torch
+            if data.dtype != torch.float64 or not data.is_contiguous() or data.numel() != n:
+                raise ValueError("device interior state must be a contiguous float64 tensor of the grid's size")
+            torch.cuda.current_stream(data.device).synchronize()
+            ptr = ctypes.cast(ctypes.c_void_p(data.data_ptr()), ctypes.POINTER(ctypes.c_double))
+            capi.check(self.L.wg_upload_interior(self.ctx.h, self.tree, ptr))
+            return
         data = np.ascontiguousarray(data, np.float64)
-        if data.size != self.nblocks * int(np.prod(self.interior_shape)):
+        if data.size != n:
             raise ValueError("interior state has the wrong size for this grid")
         capi.check(self.L.wg_upload_interior(self.ctx.h, self.tree, _p(data)))
 

@@ -14,9 +14,10 @@ the measurements are quoted on:
   cosine-smoothed mask (C_smooth = 1.5 dx_min); IC: u = (1,0,0) + 0.01 N(0,1)
   per point and component (seed 2), p = 0. Grid: refined around the sphere
   with level-dependent radii (about 4k blocks at Jmax=6).
-* ``acm3d_sphere_j7`` -- the same at Jmax=7 with the stencils evaluated in
-  double-float arithmetic on the FP32 units (FP64 RK state, FP64
-  penalisation).
+* ``acm3d_sphere_j7`` -- the same physics at Jmax=7 with the stencils and
+  the stage arithmetic evaluated in double-float arithmetic on the FP32 units
+  (FP64 state); grid refined around the sphere with wider level-dependent
+  radii (36,688 blocks over levels 3-7).
 
 All random draws use numpy's PCG64 generator with the stated seed, in block
 order, component order, then point order (x fastest).
@@ -96,8 +97,8 @@ def make_grid(name: str, cfg):
         return _to_arrays(leaves)
     centre = [0.5 * cfg.domain[d] for d in range(3)]
     jmin = cfg.Jmin
-    return grids.refined_around(3, jmin, cfg.Jmax, cfg.domain, centre,
-                                lambda l: 0.2 + 0.6 * 2.0 ** (-(l - jmin)))
+    a, b = (0.3, 0.8) if name.endswith("j7") else (0.2, 0.6)
+    return grids.refined_around(3, jmin, cfg.Jmax, cfg.domain, centre, lambda l: a + b * 2.0 ** (-(l - jmin)))
 
 
 def _points(cfg, lv, co):
