@@ -454,6 +454,92 @@ def run_serving(args, rank, world):
         print(json.dumps(line))
 
 
+def run_adapt(args, rank, world):
+    """The adapt path's heavy part at scale (configuration 5: 3-D CDF4,4,
+    99,184 blocks on five levels): one pass = ghost sync (g layers), the
+    in-place FWT of every block, the coarsening indicator on the decomposition
+    (detail threshold, flags), the ghost sync of the decomposed data and the
+    IWT.
+    value: interior points per second through one pass."""
+    import torch
+    from wabbit_gb300 import build, workloads
+    from wabbit_gb300.solver import Context
+    build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    name = "adapt3d_cdf44"
+    cfg = workloads.make_config(name)
+    if args.jmax is not None:
+        cfg.Jmax = args.jmax
+    lv, co = workloads.make_grid(name, cfg)
+    nblk = len(lv)
+    npts = nblk * 16 ** 3
+    ctx = Context(cfg, nblk + 4)
+    f = ctx.forest()
+    f.set_grid(lv, co)
+    u = workloads.adapt_field_device(cfg, lv, co)
+    norms = u.abs().amax(dim=(0, 2, 3, 4)).cpu().numpy()
+    f.upload_interior(u)
+    del u
+    torch.cuda.empty_cache()
+    eps_use = cfg.eps * norms
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def one_pass(times=None):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        ev[0].record(stream)
+        f.sync_ghosts_tree()
+        ev[1].record(stream)
+        f.wavelet_decompose()
+        ev[2].record(stream)
+        flags, _ = f.coarseningIndicator(eps_use, input_is_wd=True)
+        ev[3].record(stream)
+        f.sync_ghosts_tree()
+        ev[4].record(stream)
+        f.wavelet_reconstruct()
+        ev[5].record(stream)
+        ev[5].synchronize()
+        if times is not None:
+            for k, n in enumerate(("sync", "fwt", "indicator", "sync_wd", "iwt")):
+                times[n] = times.get(n, 0.0) + ev[k].elapsed_time(ev[k + 1])
+        return flags
+
+    for _ in range(max(args.warmup, 1)):
+        flags = one_pass()
+    barrier(world)
+    times = {}
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flags = one_pass(times)
+        el = time.perf_counter() - t0
+    el = max_over_ranks(el, world)
+    hbm_peak, hbm_src = measured_peaks()
+    fwt_ms = times["fwt"] / args.steps
+    iwt_ms = times["iwt"] / args.steps
+    bytes_t = 2.0 * 8 * cfg.neq * npts          # read + write every interior value once
+    line = {
+        "metric": "adapt-path points/s/GPU", "value": sum_over_ranks(npts * args.steps / el, world),
+        "unit": "points/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Fourier modes + tanh fronts; see wabbit_gb300/workloads.py)",
+        "config": {"workload": name, "blocks": nblk, "points": npts, "levels": np.bincount(lv).tolist(),
+                   "wavelet": "CDF44", "g": cfg.g, "eps": cfg.eps, "eps_normalized": "Linfty",
+                   "pass": "sync g, FWT, coarsening indicator on the decomposition, sync (decomposed), IWT",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "kernels_ms": {k: v / args.steps for k, v in times.items()},
+        "flags": {"coarsen": int((flags == -1).sum()), "stay": int((flags == 0).sum())},
+        "roofline": {"bound": "hbm", "kernel": "fwt (in place)", "achieved": bytes_t / (fwt_ms * 1e-3) / 1e9,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": bytes_t / (fwt_ms * 1e-3) / 1e9 / hbm_peak,
+                     "traffic": None, "peak_source": hbm_src,
+                     "algorithmic_bytes_per_launch": bytes_t, "iwt_achieved": bytes_t / (iwt_ms * 1e-3) / 1e9},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+
+
 def capi_graph_kernels(ctx):
     from wabbit_gb300 import capi
     n = ctx.L.wg_graph_kernels(ctx.h)
@@ -516,6 +602,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "serving":
         run_serving(args, rank, world)
+    elif args.workload == "adapt3d_cdf44":
+        run_adapt(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:

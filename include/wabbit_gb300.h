@@ -153,6 +153,19 @@ int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const do
 int wg_set_time(wg_ctx *ctx, int tree, double time);
 int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);
 
+/* One-level wavelet transforms of every block of the tree, in place on the
+ * state (interior points; the ghost nodes must be synchronised first, for the
+ * inverse with the decomposed data):
+ *   wg_wavelet_decompose   -- waveletDecomposition_optimized_block
+ *     (LIB/WAVELETS/wavelet_decomposition_reconstruction.f90:23-389), result
+ *     in spaghetti order (SC at even interior offsets)
+ *   wg_wavelet_reconstruct -- waveletReconstruction_optimized_block
+ *     (wavelet_decomposition_reconstruction.f90:426-840)
+ *   wg_wavelet_threshold   -- wc_threshold_tree (LIB/MESH/adapt_tree.f90:
+ *     1091-1180) on decomposed data: thresh holds neq values */
+int wg_wavelet_decompose(wg_ctx *ctx, int tree);
+int wg_wavelet_reconstruct(wg_ctx *ctx, int tree);
+int wg_wavelet_threshold(wg_ctx *ctx, int tree, const double *thresh);
 /* ---- the hot path ------------------------------------------------------ */
 /* sync_ghosts_RHS_tree / sync_ghosts_tree without the HD filter
  * (LIB/MPI/synchronize_ghosts_generic.f90:121-174): fill gminus/gplus ghost
@@ -178,6 +191,10 @@ int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph)
  * detail thresholding; flags[b] = -1 (may coarsen) or 0. eps_use holds the
  * per-component threshold (eps * norm). Ghosts must hold g synced layers. */
 int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details);
+/* The same flags from a state that already holds the one-level decomposition
+ * (wg_wavelet_decompose): coarseningIndicator_tree(..., input_is_WD=.true.)
+ * (LIB/MESH/coarseningIndicator_tree.f90:4), no second transform. */
+int wg_threshold_flags_wd(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details);
 /* Allocation-free variant of wg_threshold_flags, for callers that may not
  * allocate device memory while they run (e.g. a host code with its own
  * memory pool or an externally enforced device-memory budget). It has no

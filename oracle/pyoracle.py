@@ -54,6 +54,8 @@ def lib():
         L.or_timestep.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.or_threshold_flags.argtypes = [ctypes.c_void_p, _dp, _ip, _dp]
         L.or_fwt.argtypes = [ctypes.c_void_p, _dp]
+        L.or_iwt.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.or_wc_threshold.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.or_refine_everywhere.argtypes = [ctypes.c_void_p]
         L.or_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _dp]
         L.or_run.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
@@ -173,6 +175,21 @@ class Oracle:
     def fwt(self):
         out = np.zeros((self.nblocks,) + self.block_shape)
         self.L.or_fwt(self.h, _p(out))
+        return out
+
+    def iwt(self, wd):
+        """IWT of every block from spaghetti data with synchronised ghosts
+        (waveletReconstruction_optimized_block); ghosts copied through."""
+        wd = np.ascontiguousarray(wd, np.float64)
+        out = np.zeros_like(wd)
+        self.L.or_iwt(self.h, _p(wd), _p(out))
+        return out
+
+    def wc_threshold(self, wd, thresh):
+        """wc_threshold_tree on spaghetti data (returns a thresholded copy)."""
+        out = np.array(wd, np.float64, copy=True, order="C")
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(thresh, np.float64), (self.cfg.neq,)))
+        self.L.or_wc_threshold(self.h, _p(out), _p(t))
         return out
 
     def refine_everywhere(self):

@@ -875,6 +875,133 @@ static void fwt_block(const Oracle &o, const double *u_in, double *u_d) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// one-level IWT of a block, interior only, from spaghetti order
+// (waveletReconstruction_optimized_block,
+//  LIB/WAVELETS/wavelet_decomposition_reconstruction.f90:426-840).
+// Passes x, y, z; the x pass reads u and covers the ghost rows/planes the
+// later passes need, the y and z passes read the partial result. Term order
+// of the reference: unlifted wavelets keep the SC and add the odd HR taps to
+// each WC (value first); lifted wavelets write at an SC position
+// SC + odd GR taps, at a WC position the odd HR taps over the neighbouring
+// SCs, then GR(0)*WC, then the other even GR taps, each group in ascending
+// offset (non-zero taps).
+// ---------------------------------------------------------------------------
+static void iwt_block(const Oracle &o, const double *u_in, double *u_r) {
+    const wg_config &p = o.cfg;
+    const Wavelet &w = o.wav;
+    const int dim = p.dim;
+    int g[3] = {p.g, p.g, dim == 3 ? p.g : 0};
+    int Bs[3] = {p.Bs[0], p.Bs[1], dim == 3 ? p.Bs[2] : 1};
+    const int fmax = std::max({w.HR.lo, w.HR.hi, w.GR.lo, w.GR.hi});
+    int fm[3] = {fmax, fmax, dim == 3 ? fmax : 0};
+    const int nmax = std::max(o.nx, std::max(o.ny, o.nz)) + 2;
+    std::vector<double> buf(nmax + 8);
+    auto at = [&](int ix, int iy, int iz) { return ((size_t)(iz - 1) * o.ny + (iy - 1)) * o.nx + (ix - 1); };
+    const bool lazy = (w.Y == 0);
+    // reconstruct one line: get(i) reads the source at 1-based index i, the
+    // results for the interior go to buf
+    auto line = [&](auto get, int n0, int n1) {
+        for (int s = n0; s <= n1; s += 2) {
+            const int wpos = s + 1;
+            if (lazy) {
+                buf[s] = get(s);
+                double v = get(wpos);
+                for (int m = w.HR.lo; m <= w.HR.hi; m++)
+                    if ((m & 1) && w.HR(m) != 0.0) v = v + get(wpos + m) * w.HR(m);
+                buf[wpos] = v;
+            } else {
+                double sc = get(s);
+                for (int m = w.GR.lo; m <= w.GR.hi; m++)
+                    if ((m & 1) && w.GR(m) != 0.0) sc = sc + get(s + m) * w.GR(m);
+                double v = 0.0;
+                bool first = true;
+                for (int m = w.HR.lo; m <= w.HR.hi; m++) {
+                    if (!(m & 1) || w.HR(m) == 0.0) continue;
+                    const double t = get(wpos + m) * w.HR(m);
+                    v = first ? t : v + t;
+                    first = false;
+                }
+                v = v + get(wpos) * w.GR(0);
+                for (int m = w.GR.lo; m <= w.GR.hi; m++)
+                    if (!(m & 1) && m != 0 && w.GR(m) != 0.0) v = v + get(wpos + m) * w.GR(m);
+                buf[s] = sc;
+                buf[wpos] = v;
+            }
+        }
+    };
+    // X: reads u_in, writes u_r (x interior) on the extended rows/planes
+    for (int iz = g[2] + 1 - fm[2]; iz <= Bs[2] + g[2] + fm[2]; iz++)
+        for (int iy = g[1] + 1 - fm[1]; iy <= Bs[1] + g[1] + fm[1]; iy++) {
+            line([&](int ix) { return u_in[at(ix, iy, iz)]; }, g[0] + 1, Bs[0] + g[0] - 1);
+            for (int ix = g[0] + 1; ix <= Bs[0] + g[0]; ix++) u_r[at(ix, iy, iz)] = buf[ix];
+        }
+    // Y
+    for (int iz = g[2] + 1 - fm[2]; iz <= Bs[2] + g[2] + fm[2]; iz++)
+        for (int ix = g[0] + 1; ix <= Bs[0] + g[0]; ix++) {
+            line([&](int iy) { return u_r[at(ix, iy, iz)]; }, g[1] + 1, Bs[1] + g[1] - 1);
+            for (int iy = g[1] + 1; iy <= Bs[1] + g[1]; iy++) u_r[at(ix, iy, iz)] = buf[iy];
+        }
+    // Z
+    if (dim == 3)
+        for (int iy = g[1] + 1; iy <= Bs[1] + g[1]; iy++)
+            for (int ix = g[0] + 1; ix <= Bs[0] + g[0]; ix++) {
+                line([&](int iz) { return u_r[at(ix, iy, iz)]; }, g[2] + 1, Bs[2] + g[2] - 1);
+                for (int iz = g[2] + 1; iz <= Bs[2] + g[2]; iz++) u_r[at(ix, iy, iz)] = buf[iz];
+            }
+}
+
+// wc_threshold_tree (LIB/MESH/adapt_tree.f90:1091-1180) with Linfty renorm:
+// on spaghetti data, interior WC positions only. As in the reference,
+// components whose threshold_state_vector_component is 1 are skipped by the
+// per-component pass; 0 and >= 2 components are zeroed where |WC| < thresh;
+// each group l >= 2 is also zeroed where the group's Euclidean norm is below
+// the group's largest threshold.
+static void wc_threshold_block(const Oracle &o, double *u, const double *thresh) {
+    const wg_config &p = o.cfg;
+    const int g = p.g, dim = p.dim, nc = o.nc;
+    const int even_odd = (g + 1) % 2;
+    const int z1 = dim == 2 ? 1 : g + 1, z2 = dim == 2 ? 1 : p.Bs[2] + g;
+    auto is_sc = [&](int ix, int iy, int iz) {
+        return ix % 2 == even_odd && iy % 2 == even_odd && iz % 2 == (dim == 2 ? 1 : even_odd);
+    };
+    auto idx = [&](int ix, int iy, int iz) { return ((size_t)(iz - 1) * o.ny + (iy - 1)) * o.nx + (ix - 1); };
+    // the renormed copy (identity for Linfty) is read, the block is written
+    std::vector<double> wc(u, u + (size_t)nc * o.npts);
+    for (int c = 0; c < nc; c++) {
+        if (p.threshold_state_vector_component[c] == 1) continue;
+        for (int iz = z1; iz <= z2; iz++)
+            for (int iy = g + 1; iy <= p.Bs[1] + g; iy++)
+                for (int ix = g + 1; ix <= p.Bs[0] + g; ix++) {
+                    if (is_sc(ix, iy, iz)) continue;
+                    if (std::fabs(wc[c * o.npts + idx(ix, iy, iz)]) < thresh[c]) u[c * o.npts + idx(ix, iy, iz)] = 0.0;
+                }
+    }
+    int maxg = 0;
+    for (int c = 0; c < nc; c++) maxg = std::max(maxg, p.threshold_state_vector_component[c]);
+    for (int l = 2; l <= maxg; l++) {
+        double tmax = -1e300;
+        for (int c = 0; c < nc; c++)
+            if (p.threshold_state_vector_component[c] == l) tmax = std::max(tmax, thresh[c]);
+        for (int iz = z1; iz <= z2; iz++)
+            for (int iy = g + 1; iy <= p.Bs[1] + g; iy++)
+                for (int ix = g + 1; ix <= p.Bs[0] + g; ix++) {
+                    if (is_sc(ix, iy, iz)) continue;
+                    double s = 0.0;
+                    bool first = true;
+                    for (int c = 0; c < nc; c++) {
+                        if (p.threshold_state_vector_component[c] != l) continue;
+                        const double v = wc[c * o.npts + idx(ix, iy, iz)];
+                        s = first ? v * v : s + v * v;
+                        first = false;
+                    }
+                    if (std::sqrt(s) < tmax)
+                        for (int c = 0; c < nc; c++)
+                            if (p.threshold_state_vector_component[c] == l) u[c * o.npts + idx(ix, iy, iz)] = 0.0;
+                }
+    }
+}
+
 // threshold_block (LIB/INDICATORS/threshold_block.f90) with Linfty renorm
 // (wavelet_renorm_block, module_wavelets.f90:1848-1960): details are the max
 // |WC| over the interior with scaling coefficients zeroed. Returns -1 (coarsen)
@@ -1091,6 +1218,45 @@ int or_fwt(void *h, double *out) {
             const double *u = o.blk((int)b) + size_t(c) * o.npts;
             fwt_block(o, u, out + (b * o.nc + c) * o.npts);
         }
+    return WG_OK;
+}
+
+// IWT of every block: in holds spaghetti data with synchronised ghosts (full
+// layout); out receives the reconstructed interior (ghosts copied from in)
+int or_iwt(void *h, const double *in, double *out) {
+    Oracle &o = *(Oracle *)h;
+    const size_t n = (size_t)o.blocks.size() * o.nc * o.npts;
+    std::copy(in, in + n, out);
+    std::vector<double> tmp(o.npts);
+    for (size_t b = 0; b < o.blocks.size(); b++)
+        for (int c = 0; c < o.nc; c++) {
+            const double *u = in + (b * o.nc + c) * o.npts;
+            std::copy(u, u + o.npts, tmp.begin());
+            iwt_block(o, u, tmp.data());
+            double *dst = out + (b * o.nc + c) * o.npts;
+            std::copy(tmp.begin(), tmp.end(), dst);
+        }
+    // ghosts: keep in's values (the passes wrote interior x on ghost rows)
+    const wg_config &p = o.cfg;
+    const int g = p.g;
+    for (size_t b = 0; b < o.blocks.size(); b++)
+        for (int c = 0; c < o.nc; c++)
+            for (int iz = 1; iz <= o.nz; iz++)
+                for (int iy = 1; iy <= o.ny; iy++)
+                    for (int ix = 1; ix <= o.nx; ix++) {
+                        const bool interior = ix > g && ix <= p.Bs[0] + g && iy > g && iy <= p.Bs[1] + g &&
+                                              (p.dim == 2 || (iz > g && iz <= p.Bs[2] + g));
+                        if (interior) continue;
+                        const size_t q = (b * o.nc + c) * o.npts + ((size_t)(iz - 1) * o.ny + (iy - 1)) * o.nx + (ix - 1);
+                        out[q] = in[q];
+                    }
+    return WG_OK;
+}
+
+// wc_threshold_tree on spaghetti data of every block, in place
+int or_wc_threshold(void *h, double *data, const double *thresh) {
+    Oracle &o = *(Oracle *)h;
+    for (size_t b = 0; b < o.blocks.size(); b++) wc_threshold_block(o, data + b * o.nc * o.npts, thresh);
     return WG_OK;
 }
 

@@ -27,6 +27,7 @@ EXPORTS = [
     "wg_probe_alu", "wg_time_kernel", "wg_tree_stats", "wg_set_mask_sparse",
     "wg_upload_interior", "wg_download_interior", "wg_graph_kernels",
     "wg_threshold_flags_noalloc", "wg_set_stage_form", "wg_get_stage_form",
+    "wg_wavelet_decompose", "wg_wavelet_reconstruct", "wg_wavelet_threshold", "wg_threshold_flags_wd",
 ]
 
 
@@ -49,6 +50,9 @@ _SIGS = {
     "wg_ctx_destroy": (_i, [_vp]),
     "wg_set_variant": (_i, [_vp, _i]),
     "wg_set_stage_form": (_i, [_vp, _i]),
+    "wg_wavelet_decompose": (_i, [_vp, _i]),
+    "wg_wavelet_reconstruct": (_i, [_vp, _i]),
+    "wg_wavelet_threshold": (_i, [_vp, _i, _dp]),
     "wg_get_stage_form": (_i, [_vp, ctypes.POINTER(ctypes.c_int)]),
     "wg_synchronize": (_i, [_vp]),
     "wg_stream": (_vp, [_vp]),
@@ -68,6 +72,7 @@ _SIGS = {
     "wg_rk4_step": (_i, [_vp, _i, _dp, _dp]),
     "wg_run": (_i, [_vp, _i, _ip, _i, _i]),
     "wg_threshold_flags": (_i, [_vp, _i, _dp, _ip, _dp]),
+    "wg_threshold_flags_wd": (_i, [_vp, _i, _dp, _ip, _dp]),
     "wg_refine_everywhere": (_i, [_vp, _i]),
     "wg_sync_table": (_i, [_vp, _i, _i, _i, _i, _i, _ip]),
     "wg_block_slot": (_i, [_vp, _i, _i]),

@@ -1308,6 +1308,42 @@ int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph)
     return WG_OK;
 }
 
+// waveletDecomposition_optimized_block / waveletReconstruction_optimized_block
+// of every block of the tree, in place on the state; wc_threshold_tree
+int wg_wavelet_decompose(wg_ctx *ctx, int tree) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    const int *Bs = ctx->cfg.Bs;
+    WG_CUDA_OK(launch_wavelet_decompose(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0], Bs[1],
+                                        Bs[2], ctx->geo.nc, ctx->wav.X, ctx->wav.Y, ctx->stream));
+    t->shadow_valid = false;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+int wg_wavelet_reconstruct(wg_ctx *ctx, int tree) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    const int *Bs = ctx->cfg.Bs;
+    WG_CUDA_OK(launch_wavelet_reconstruct(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0],
+                                          Bs[1], Bs[2], ctx->geo.nc, ctx->wav.X, ctx->wav.Y, ctx->stream));
+    t->shadow_valid = false;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
+int wg_wavelet_threshold(wg_ctx *ctx, int tree, const double *thresh) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !thresh) return fail(WG_EINVAL, "bad arguments");
+    if (ctx->geo.nc > 8) return fail(WG_ENOTSUP, "at most 8 components");
+    const int *Bs = ctx->cfg.Bs;
+    WG_CUDA_OK(launch_wc_threshold(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0], Bs[1],
+                                   Bs[2], ctx->geo.nc, thresh, t->cfg.threshold_state_vector_component, ctx->stream));
+    t->shadow_valid = false;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
+}
+
 int wg_set_stage_form(wg_ctx *ctx, int form) {
     if (!ctx) return fail(WG_EINVAL, "null ctx");
     if (form != WG_FORM_AUTO && form != WG_FORM_DIRECT && form != WG_FORM_TILE)
@@ -1338,7 +1374,7 @@ void *wg_stream(wg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 // coarseningIndicator for every block of the tree on the current state
 // (ghosts synchronised with g points first): flags[b] = -1 (may coarsen) or
 // 0; details (nblk*neq, may be NULL) receives the per-component details
-int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details) {
+static int threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details, int input_is_wd) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !eps_use || !flags) return fail(WG_EINVAL, "bad arguments");
     const int nb = t->forest.size();
@@ -1356,7 +1392,7 @@ int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags,
     const int *Bs = ctx->cfg.Bs;
     if (e == cudaSuccess)
         e = launch_fwt_flags(ctx->cfg.dim, t->d_all.p, nb, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], nc, ctx->wav.X,
-                             ctx->wav.Y, d_eps, d_tsvc, d_flags, d_det, ctx->stream);
+                             ctx->wav.Y, d_eps, d_tsvc, d_flags, d_det, ctx->stream, input_is_wd);
     if (e == cudaSuccess) e = cudaMemcpyAsync(flags, d_flags, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess && details)
         e = cudaMemcpyAsync(details, d_det, sizeof(double) * nb * nc, cudaMemcpyDeviceToHost, ctx->stream);
@@ -1367,6 +1403,17 @@ int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags,
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(e, "wg_threshold_flags", __FILE__, __LINE__);
     return WG_OK;
+}
+
+int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details) {
+    return threshold_flags(ctx, tree, eps_use, flags, details, 0);
+}
+
+// coarseningIndicator_tree(..., input_is_WD=.true.): the state already holds
+// the one-level decomposition (wg_wavelet_decompose), the details are read
+// from it without a second FWT
+int wg_threshold_flags_wd(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details) {
+    return threshold_flags(ctx, tree, eps_use, flags, details, 1);
 }
 
 // refine_tree(..., "everywhere") data part: every block is replaced by its

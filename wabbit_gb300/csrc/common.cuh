@@ -149,7 +149,16 @@ cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGe
                                  int Bx, int By, int Bz, int to_full, cudaStream_t s);
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,
                              int Bs2, int nc, int wavelet_x, int wavelet_y, const double *eps_use,
-                             const int *tsvc, int *flags, double *details, cudaStream_t s);
+                             const int *tsvc, int *flags, double *details, cudaStream_t s, int input_is_wd = 0);
+// one-level FWT (spaghetti order) / IWT of the interiors of the listed blocks,
+// in place; the ghost nodes must be synchronised (IWT: with spaghetti data)
+cudaError_t launch_wavelet_decompose(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
+                                     int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s);
+cudaError_t launch_wavelet_reconstruct(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
+                                       int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s);
+// wc_threshold_tree on spaghetti data (thresh, tsvc: nc host values, nc <= 8)
+cudaError_t launch_wc_threshold(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,
+                                int nc, const double *thresh, const int *tsvc, cudaStream_t s);
 // allocation-free variant (static device scratch, contiguous blocks 0..nblk-1)
 int noalloc_max_blocks();
 cudaError_t launch_fwt_flags_noalloc(int dim, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,

@@ -13,6 +13,12 @@
 // explicit round-to-nearest operations in the reference's term order, so the
 // details -- and therefore the grid decisions -- are bit-identical.
 //
+// IWT: waveletReconstruction_optimized_block
+// (wavelet_decomposition_reconstruction.f90:426-840), the same separable
+// passes with the reconstruction filters HR, GR in the reference's term order
+// (see iwt_kernel). WC thresholding: wc_threshold_tree (LIB/MESH/
+// adapt_tree.f90:1091-1180).
+//
 // Refinement: refineBlock (LIB/MESH/refinementExecute.f90:4-116): the whole
 // parent block (ghosts included) is predicted to the fine grid and each of the
 // 2^d daughters takes its (Bs+2g)^d window.
@@ -24,8 +30,12 @@ namespace wg {
 __constant__ double c_hd[32];
 __constant__ double c_gd[32];
 __constant__ int c_flt[4];   // hd_lo, hd_n, gd_lo, gd_n
+__constant__ double c_hr[32];
+__constant__ double c_gr[32];
+__constant__ int c_rflt[4];  // hr_lo, hr_n, gr_lo, gr_n
 
-static int g_flt_key = -1;   // wavelet whose filters sit in constant memory
+static int g_flt_key = -1;   // wavelet whose analysis filters sit in constant memory
+static int g_rflt_key = -1;  // ... and whose reconstruction filters
 
 struct FwtArgs {
     const int *blk;
@@ -54,9 +64,11 @@ __device__ __forceinline__ double filt(const double *c, int lo, int n, const dou
 }
 
 // one CTA per (block, component); shared array holds the x-interior columns of
-// all rows/planes the later passes read
-template <int DIM>
-__global__ void __launch_bounds__(256) fwt_detail_kernel(FwtArgs a, double *detail_scratch) {
+// all rows/planes the later passes read. STORE: write the decomposed interior
+// (spaghetti order) to out instead of reducing the details; out may be the
+// input itself (every read of the CTA's block component precedes its writes).
+template <int DIM, bool STORE = false>
+__global__ void __launch_bounds__(256) fwt_detail_kernel(FwtArgs a, double *detail_scratch, double *out = nullptr) {
     extern __shared__ double sm[];
     const int bi = blockIdx.x / a.nc, c = blockIdx.x % a.nc;
     const int b = a.blk[bi];
@@ -108,9 +120,18 @@ __global__ void __launch_bounds__(256) fwt_detail_kernel(FwtArgs a, double *deta
         }
         __syncthreads();
     }
+    const int nint = Bx * By * Bz;
+    if (STORE) {
+        double *o = out + ((long long)b * a.nc + c) * np;
+        for (int q = threadIdx.x; q < nint; q += blockDim.x) {
+            const int ix = q % Bx, iy = (q / Bx) % By, iz = q / (Bx * By);
+            o[((long long)(DIM == 3 ? g + iz : 0) * a.geo.ny + (g + iy)) * a.geo.nx + (g + ix)] =
+                sm[((long long)(DIM == 3 ? f + iz : 0) * ny + (f + iy)) * Bx + ix];
+        }
+        return;
+    }
     // max |WC| over the interior, SC positions (all indices even) excluded
     double m = 0.0;
-    const int nint = Bx * By * Bz;
     for (int q = threadIdx.x; q < nint; q += blockDim.x) {
         const int ix = q % Bx, iy = (q / Bx) % By, iz = q / (Bx * By);
         if ((ix & 1) == 0 && (iy & 1) == 0 && (iz & 1) == 0) continue;
@@ -125,6 +146,33 @@ __global__ void __launch_bounds__(256) fwt_detail_kernel(FwtArgs a, double *deta
         __syncthreads();
     }
     if (threadIdx.x == 0) detail_scratch[(long long)bi * a.nc + c] = red[0];
+}
+
+// details from data that is already decomposed (spaghetti order): max |WC|
+// over the interior, SC positions excluded; one CTA per (block, component)
+template <int DIM>
+__global__ void __launch_bounds__(256) wd_detail_kernel(FwtArgs a, double *detail_scratch) {
+    const int bi = blockIdx.x / a.nc, c = blockIdx.x % a.nc;
+    const int b = a.blk[bi];
+    const int g = a.geo.gb;
+    const int Bx = a.Bs[0], By = a.Bs[1], Bz = DIM == 3 ? a.Bs[2] : 1;
+    const double *u = a.u + ((long long)b * a.nc + c) * a.geo.npts();
+    double m = 0.0;
+    const int nint = Bx * By * Bz;
+    for (int q = threadIdx.x; q < nint; q += blockDim.x) {
+        const int ix = q % Bx, iy = (q / Bx) % By, iz = q / (Bx * By);
+        if ((ix & 1) == 0 && (iy & 1) == 0 && (iz & 1) == 0) continue;
+        m = fmax(m, fabs(u[((long long)(DIM == 3 ? g + iz : 0) * a.geo.ny + (g + iy)) * a.geo.nx + (g + ix)]));
+    }
+    for (int w = 16; w; w >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, w));
+    __shared__ double red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmax(m, red[w]);
+        m = fmax(m, red[0]);
+        detail_scratch[(long long)bi * a.nc + c] = m;
+    }
 }
 
 __global__ void flag_kernel(FwtArgs a, const double *detail_scratch, int nblk) {
@@ -149,9 +197,12 @@ __global__ void flag_kernel(FwtArgs a, const double *detail_scratch, int nblk) {
     a.flags[bi] = all ? -1 : 0;
 }
 
+static cudaError_t launch_tpo(int mode, int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
+                              int Bs2, int nc, const WaveletInfo &w, int key, int f, double *scratch, cudaStream_t s);
+
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,
                              int Bs2, int nc, int wavelet_x, int wavelet_y, const double *eps_use, const int *tsvc,
-                             int *flags, double *details, cudaStream_t s) {
+                             int *flags, double *details, cudaStream_t s, int input_is_wd) {
     if (nblk <= 0) return cudaSuccess;
     WaveletInfo w;
     char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
@@ -189,7 +240,20 @@ cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u,
     double *scratch = nullptr;
     cudaError_t e = cudaMallocAsync(&scratch, sizeof(double) * (size_t)nblk * nc, s);
     if (e != cudaSuccess) return e;
-    if (dim == 2) {
+    cudaError_t et = cudaErrorNotSupported;
+    if (!input_is_wd)
+        et = launch_tpo(0, dim, blk, nblk, const_cast<double *>(u), geo, Bs0, Bs1, Bs2, nc, w, key, a.fmax, scratch, s);
+    if (et != cudaSuccess && et != cudaErrorNotSupported) {
+        cudaFreeAsync(scratch, s);
+        return et;
+    }
+    if (et == cudaErrorNotSupported) cudaGetLastError();
+    if (input_is_wd) {
+        if (dim == 2) wd_detail_kernel<2><<<nblk * nc, 256, 0, s>>>(a, scratch);
+        else wd_detail_kernel<3><<<nblk * nc, 256, 0, s>>>(a, scratch);
+    } else if (et == cudaSuccess) {
+        // details computed by the thread-per-output kernel
+    } else if (dim == 2) {
         cudaFuncSetAttribute(fwt_detail_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         fwt_detail_kernel<2><<<nblk * nc, 256, smem, s>>>(a, scratch);
     } else {
@@ -200,6 +264,454 @@ cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u,
     e = cudaGetLastError();
     cudaFreeAsync(scratch, s);
     return e;
+}
+
+// Reconstruct one line in place: src(i) for i in [at0 - F, at0 + n + F) holds
+// spaghetti data (SC at at0, at0+2, ...); the n interior results go to dst
+// with stride ds. Lazy (unlifted) wavelets keep the SCs and add the odd HR taps
+// to each WC (value first); lifted wavelets: SC + odd GR taps at an SC,
+// odd HR taps over the SCs, then GR(0) WC, then the other even GR taps at a WC.
+__device__ __forceinline__ void iwt_line(const double *src, long long ss, int at0, int n, bool lazy, double *dst,
+                                         long long ds) {
+    const int hr_lo = c_rflt[0], hr_n = c_rflt[1], gr_lo = c_rflt[2], gr_n = c_rflt[3];
+    for (int k = 0; k < n; k += 2) {
+        const int s0 = at0 + k, w0 = s0 + 1;
+        double sc, wc;
+        if (lazy) {
+            sc = src[s0 * ss];
+            wc = src[w0 * ss];
+            for (int t = 0; t < hr_n; t++) {
+                const int m = hr_lo + t;
+                if (!(m & 1) || c_hr[t] == 0.0) continue;
+                wc = __dadd_rn(wc, __dmul_rn(src[(w0 + m) * ss], c_hr[t]));
+            }
+        } else {
+            sc = src[s0 * ss];
+            for (int t = 0; t < gr_n; t++) {
+                const int m = gr_lo + t;
+                if (!(m & 1) || c_gr[t] == 0.0) continue;
+                sc = __dadd_rn(sc, __dmul_rn(src[(s0 + m) * ss], c_gr[t]));
+            }
+            bool first = true;
+            wc = 0.0;
+            for (int t = 0; t < hr_n; t++) {
+                const int m = hr_lo + t;
+                if (!(m & 1) || c_hr[t] == 0.0) continue;
+                const double v = __dmul_rn(src[(w0 + m) * ss], c_hr[t]);
+                wc = first ? v : __dadd_rn(wc, v);
+                first = false;
+            }
+            wc = __dadd_rn(wc, __dmul_rn(src[w0 * ss], c_gr[-gr_lo]));
+            for (int t = 0; t < gr_n; t++) {
+                const int m = gr_lo + t;
+                if ((m & 1) || m == 0 || c_gr[t] == 0.0) continue;
+                wc = __dadd_rn(wc, __dmul_rn(src[(w0 + m) * ss], c_gr[t]));
+            }
+        }
+        dst[k * ds] = sc;
+        dst[(k + 1) * ds] = wc;
+    }
+}
+
+// One-level IWT of every (block, component), in place on the interior; the
+// ghost nodes must hold the neighbours' spaghetti data (synchronised). Shared
+// memory holds the x-interior columns of the rows/planes the y and z passes
+// read (F = max HR/GR half-width around the interior).
+template <int DIM>
+__global__ void __launch_bounds__(256) iwt_kernel(const int *blk, double *u, BufGeo geo, int Bx, int By, int Bz,
+                                                  int nc, int lazy, int F) {
+    extern __shared__ double sm[];
+    const int bi = blockIdx.x / nc, c = blockIdx.x % nc;
+    const int b = blk[bi];
+    const int g = geo.gb;
+    if (DIM == 2) Bz = 1;
+    const int y0 = g - F, ny = By + 2 * F;
+    const int z0 = DIM == 3 ? g - F : 0, nz = DIM == 3 ? Bz + 2 * F : 1;
+    const long long np = geo.npts();
+    double *ub = u + ((long long)b * nc + c) * np;
+    // x pass from global memory on every row/plane of the extended window
+    for (int r = threadIdx.x; r < ny * nz; r += blockDim.x) {
+        const int yy = r % ny, zz = r / ny;
+        const double *line = ub + ((long long)(z0 + zz) * geo.ny + (y0 + yy)) * geo.nx;
+        iwt_line(line, 1, g, Bx, lazy, sm + (long long)r * Bx, 1);
+    }
+    __syncthreads();
+    double tmp[64];
+    for (int r = threadIdx.x; r < Bx * nz; r += blockDim.x) {
+        const int ix = r % Bx, zz = r / Bx;
+        double *col = sm + (long long)zz * ny * Bx + ix;     // stride Bx along y
+        iwt_line(col, Bx, F, By, lazy, tmp, 1);
+        for (int iy = 0; iy < By; iy++) col[(long long)(F + iy) * Bx] = tmp[iy];
+    }
+    __syncthreads();
+    if (DIM == 3) {
+        for (int r = threadIdx.x; r < Bx * By; r += blockDim.x) {
+            const int ix = r % Bx, iy = r / Bx;
+            double *col = sm + (long long)(F + iy) * Bx + ix;   // stride ny*Bx along z
+            iwt_line(col, (long long)ny * Bx, F, Bz, lazy, tmp, 1);
+            for (int iz = 0; iz < Bz; iz++) col[(long long)(F + iz) * ny * Bx] = tmp[iz];
+        }
+        __syncthreads();
+    }
+    const int nint = Bx * By * Bz;
+    for (int q = threadIdx.x; q < nint; q += blockDim.x) {
+        const int ix = q % Bx, iy = (q / Bx) % By, iz = q / (Bx * By);
+        ub[((long long)(DIM == 3 ? g + iz : 0) * geo.ny + (g + iy)) * geo.nx + (g + ix)] =
+            sm[((long long)(DIM == 3 ? F + iz : 0) * ny + (F + iy)) * Bx + ix];
+    }
+}
+
+struct WcThresh {
+    double t[8];
+    int tsvc[8];
+};
+
+// wc_threshold_tree on spaghetti data, one thread per interior point of a
+// block: components with threshold_state_vector_component 0 or >= 2 are
+// zeroed where |WC| < thresh (1 is skipped, as in the reference), then every
+// group l >= 2 where the group's Euclidean norm is below its largest threshold
+template <int DIM>
+__global__ void wc_threshold_kernel(const int *blk, int nblk, double *u, BufGeo geo, int Bx, int By, int Bz, int nc,
+                                    WcThresh th) {
+    const int nint = Bx * By * (DIM == 3 ? Bz : 1);
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)nblk * nint) return;
+    const int bi = (int)(q / nint), p = (int)(q % nint);
+    const int ix = p % Bx, iy = (p / Bx) % By, iz = DIM == 3 ? p / (Bx * By) : 0;
+    if ((ix & 1) == 0 && (iy & 1) == 0 && (iz & 1) == 0) return;   // scaling coefficient
+    const long long np = geo.npts();
+    double *ub = u + (long long)blk[bi] * nc * np +
+                 ((long long)(DIM == 3 ? geo.gb + iz : 0) * geo.ny + (geo.gb + iy)) * geo.nx + (geo.gb + ix);
+    double w[8];
+    for (int c = 0; c < nc; c++) w[c] = ub[c * np];
+    int maxg = 0;
+    for (int c = 0; c < nc; c++) {
+        maxg = max(maxg, th.tsvc[c]);
+        if (th.tsvc[c] != 1 && fabs(w[c]) < th.t[c]) ub[c * np] = 0.0;
+    }
+    for (int l = 2; l <= maxg; l++) {
+        double s = 0.0, tmax = -1e300;
+        bool first = true;
+        for (int c = 0; c < nc; c++) {
+            if (th.tsvc[c] != l) continue;
+            const double v = __dmul_rn(w[c], w[c]);
+            s = first ? v : __dadd_rn(s, v);
+            first = false;
+            tmax = fmax(tmax, th.t[c]);
+        }
+        if (__dsqrt_rn(s) < tmax)
+            for (int c = 0; c < nc; c++)
+                if (th.tsvc[c] == l) ub[c * np] = 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Thread-per-output form of the one-level FWT and IWT (blocks with
+// Bx*By*nz_ext <= 8192): 512 threads per (block, component); the x pass goes
+// from global memory into shared memory on the rows/planes the later passes
+// read, the y pass keeps its results in registers across a barrier and writes
+// them back in place, the z pass writes the state (FWT: every read of the
+// block component happened in the x pass) or reduces the details. Filter taps
+// are compacted on the host into (offset, value) lists in the reference's
+// term order.
+// ---------------------------------------------------------------------------
+struct Taps {
+    int n[5];              // 0 HD (non-zero or centre), 1 GD, 2 HR odd, 3 GR odd, 4 GR even without 0
+    int off[5][16];
+    double val[5][16];
+    double gr0;            // GR(0)
+    int lazy;
+};
+__constant__ Taps c_taps;
+static int g_taps_key = -1;
+
+constexpr int kTpoThreads = 512;
+constexpr int kTpoMaxPerThread = 16;
+
+// sum_t src[(at + off_t) * st] * val_t in order, the first term not added to 0
+__device__ __forceinline__ double tap_sum(int f, const double *src, long long st, int at) {
+    const int n = c_taps.n[f];
+    double s = __dmul_rn(src[(at + c_taps.off[f][0]) * st], c_taps.val[f][0]);
+    for (int t = 1; t < n; t++) s = __dadd_rn(s, __dmul_rn(src[(at + c_taps.off[f][t]) * st], c_taps.val[f][t]));
+    return s;
+}
+
+// FWT output at interior offset p (position at of the line)
+__device__ __forceinline__ double fwt_point(const double *src, long long st, int at, int p) {
+    if ((p & 1) == 0) return c_taps.lazy ? src[at * st] : tap_sum(0, src, st, at);
+    return tap_sum(1, src, st, at);
+}
+
+// IWT output at interior offset p (position at of the line)
+__device__ __forceinline__ double iwt_point(const double *src, long long st, int at, int p) {
+    if (c_taps.lazy) {
+        double v = src[at * st];
+        if (p & 1)
+            for (int t = 0; t < c_taps.n[2]; t++)
+                v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[2][t]) * st], c_taps.val[2][t]));
+        return v;
+    }
+    if ((p & 1) == 0) {
+        double v = src[at * st];
+        for (int t = 0; t < c_taps.n[3]; t++)
+            v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[3][t]) * st], c_taps.val[3][t]));
+        return v;
+    }
+    double v = tap_sum(2, src, st, at);
+    v = __dadd_rn(v, __dmul_rn(src[at * st], c_taps.gr0));
+    for (int t = 0; t < c_taps.n[4]; t++)
+        v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[4][t]) * st], c_taps.val[4][t]));
+    return v;
+}
+
+// MODE 0: details (max |WC|) into scratch; 1: FWT stored in place; 2: IWT
+// stored in place. f: half-width of the extended window.
+template <int DIM, int MODE>
+__global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, double *u, BufGeo geo, int Bx, int By,
+                                                             int Bz, int nc, int f, double *detail_scratch) {
+    extern __shared__ double sm[];
+    const int bi = blockIdx.x / nc, c = blockIdx.x % nc;
+    const int b = blk[bi];
+    const int g = geo.gb;
+    if (DIM == 2) Bz = 1;
+    const int ny = By + 2 * f, nz = DIM == 3 ? Bz + 2 * f : 1;
+    const int y0 = g - f, z0 = DIM == 3 ? g - f : 0;
+    const long long np = geo.npts();
+    double *ub = u + ((long long)b * nc + c) * np;
+    auto point = [&](const double *src, long long st, int at, int p) {
+        return MODE == 2 ? iwt_point(src, st, at, p) : fwt_point(src, st, at, p);
+    };
+    // x pass
+    const int nx_out = Bx * ny * nz;
+    for (int o = threadIdx.x; o < nx_out; o += kTpoThreads) {
+        const int ix = o % Bx, r = o / Bx;
+        const int yy = r % ny, zz = r / ny;
+        const double *line = ub + ((long long)(z0 + zz) * geo.ny + (y0 + yy)) * geo.nx;
+        sm[o] = point(line, 1, g + ix, ix);
+    }
+    __syncthreads();
+    // y pass on the interior rows of every plane of the window
+    double res[kTpoMaxPerThread];
+    const int ny_out = Bx * By * nz;
+#pragma unroll
+    for (int k = 0; k < kTpoMaxPerThread; k++) {
+        const int o = threadIdx.x + k * kTpoThreads;
+        if (o < ny_out) {
+            const int ix = o % Bx, iy = (o / Bx) % By, zz = o / (Bx * By);
+            res[k] = point(sm + (long long)zz * ny * Bx + ix, Bx, f + iy, iy);
+        }
+    }
+    double m = 0.0;
+    if (DIM == 2) {
+        // the y pass results are final
+#pragma unroll
+        for (int k = 0; k < kTpoMaxPerThread; k++) {
+            const int o = threadIdx.x + k * kTpoThreads;
+            if (o >= ny_out) continue;
+            const int ix = o % Bx, iy = o / Bx;
+            if (MODE == 0) {
+                if ((ix & 1) || (iy & 1)) m = fmax(m, fabs(res[k]));
+            } else {
+                ub[(long long)(g + iy) * geo.nx + (g + ix)] = res[k];
+            }
+        }
+    } else {
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kTpoMaxPerThread; k++) {
+            const int o = threadIdx.x + k * kTpoThreads;
+            if (o >= ny_out) continue;
+            const int ix = o % Bx, iy = (o / Bx) % By, zz = o / (Bx * By);
+            sm[((long long)zz * ny + (f + iy)) * Bx + ix] = res[k];
+        }
+        __syncthreads();
+        const int nint = Bx * By * Bz;
+        for (int o = threadIdx.x; o < nint; o += kTpoThreads) {
+            const int ix = o % Bx, iy = (o / Bx) % By, iz = o / (Bx * By);
+            const double v = point(sm + (long long)(f + iy) * Bx + ix, (long long)ny * Bx, f + iz, iz);
+            if (MODE == 0) {
+                if ((ix & 1) || (iy & 1) || (iz & 1)) m = fmax(m, fabs(v));
+            } else {
+                ub[((long long)(g + iz) * geo.ny + (g + iy)) * geo.nx + (g + ix)] = v;
+            }
+        }
+    }
+    if (MODE == 0) {
+        for (int w = 16; w; w >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, w));
+        __shared__ double red[kTpoThreads / 32];
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 0; w < kTpoThreads / 32; w++) m = fmax(m, red[w]);
+            detail_scratch[(long long)bi * nc + c] = m;
+        }
+    }
+}
+
+static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
+    if (g_taps_key == key) return cudaSuccess;
+    Taps t{};
+    auto add = [&](int f, int off, double v) {
+        if (t.n[f] >= 16) return false;
+        t.off[f][t.n[f]] = off;
+        t.val[f][t.n[f]] = v;
+        t.n[f]++;
+        return true;
+    };
+    bool ok = true;
+    for (size_t i = 0; i < w.HD.size(); i++) {
+        const int m = w.hd_lo + (int)i;
+        if (w.HD[i] != 0.0 || m == 0) ok &= add(0, m, w.HD[i]);
+    }
+    for (size_t i = 0; i < w.GD.size(); i++) {
+        const int m = w.gd_lo + (int)i;
+        if (w.GD[i] != 0.0 || m == 0) ok &= add(1, m, w.GD[i]);
+    }
+    for (size_t i = 0; i < w.HR.size(); i++) {
+        const int m = w.hr_lo + (int)i;
+        if ((m & 1) && w.HR[i] != 0.0) ok &= add(2, m, w.HR[i]);
+    }
+    for (size_t i = 0; i < w.GR.size(); i++) {
+        const int m = w.gr_lo + (int)i;
+        if (m == 0) t.gr0 = w.GR[i];
+        else if ((m & 1) && w.GR[i] != 0.0) ok &= add(3, m, w.GR[i]);
+        else if (!(m & 1) && w.GR[i] != 0.0) ok &= add(4, m, w.GR[i]);
+    }
+    t.lazy = w.lifted ? 0 : 1;
+    if (!ok || t.n[0] == 0 || t.n[1] == 0) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_taps, &t, sizeof(t), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) g_taps_key = key;
+    return e;
+}
+
+// launch the thread-per-output kernel if the block fits its limits; returns
+// cudaErrorNotSupported otherwise (the caller then uses the column kernels)
+static cudaError_t launch_tpo(int mode, int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
+                              int Bs2, int nc, const WaveletInfo &w, int key, int f, double *scratch, cudaStream_t s) {
+    const int ny = Bs1 + 2 * f, nz = dim == 3 ? Bs2 + 2 * f : 1;
+    if ((long long)Bs0 * Bs1 * nz > (long long)kTpoThreads * kTpoMaxPerThread) return cudaErrorNotSupported;
+    const size_t smem = sizeof(double) * (size_t)Bs0 * ny * nz;
+    if (smem > 110 * 1024) return cudaErrorNotSupported;
+    cudaError_t e = load_taps(w, key, s);
+    if (e != cudaSuccess) return e;
+    const int bz = dim == 3 ? Bs2 : 1;
+    auto go = [&](auto kern) -> cudaError_t {
+        cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e2 != cudaSuccess) return e2;
+        kern<<<nblk * nc, kTpoThreads, smem, s>>>(blk, u, geo, Bs0, Bs1, bz, nc, f, scratch);
+        return cudaGetLastError();
+    };
+    if (dim == 2) {
+        if (mode == 0) return go(tpo_kernel<2, 0>);
+        if (mode == 1) return go(tpo_kernel<2, 1>);
+        return go(tpo_kernel<2, 2>);
+    }
+    if (mode == 0) return go(tpo_kernel<3, 0>);
+    if (mode == 1) return go(tpo_kernel<3, 1>);
+    return go(tpo_kernel<3, 2>);
+}
+
+static cudaError_t load_analysis_filters(const WaveletInfo &w, int key, cudaStream_t s) {
+    if (g_flt_key == key) return cudaSuccess;
+    double hd[32] = {}, gd[32] = {};
+    for (size_t i = 0; i < w.HD.size(); i++) hd[i] = w.HD[i];
+    for (size_t i = 0; i < w.GD.size(); i++) gd[i] = w.GD[i];
+    int flt[4] = {w.hd_lo, (int)w.HD.size(), w.gd_lo, (int)w.GD.size()};
+    cudaError_t e = cudaMemcpyToSymbolAsync(c_hd, hd, sizeof(hd), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_gd, gd, sizeof(gd), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_flt, flt, sizeof(flt), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) g_flt_key = key;
+    return e;
+}
+
+cudaError_t launch_wavelet_decompose(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
+                                     int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    WaveletInfo w;
+    char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
+    if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
+    cudaError_t e = load_analysis_filters(w, wavelet_x * 10 + wavelet_y, s);
+    if (e != cudaSuccess) return e;
+    FwtArgs a{};
+    a.blk = blk;
+    a.u = u;
+    a.geo = geo;
+    a.Bs[0] = Bs0;
+    a.Bs[1] = Bs1;
+    a.Bs[2] = Bs2;
+    a.nc = nc;
+    a.lazy = w.lifted ? 0 : 1;
+    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
+    a.fmax = std::max(std::max(w.hd_lo, hd_hi), std::max(w.gd_lo, gd_hi));
+    if (a.fmax > geo.gb) return cudaErrorInvalidValue;
+    e = launch_tpo(1, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, wavelet_x * 10 + wavelet_y, a.fmax, nullptr, s);
+    if (e != cudaErrorNotSupported) return e;
+    cudaGetLastError();
+    const int ny = Bs1 + 2 * a.fmax, nz = dim == 3 ? Bs2 + 2 * a.fmax : 1;
+    const size_t smem = sizeof(double) * (size_t)Bs0 * ny * nz;
+    if (dim == 2) {
+        cudaFuncSetAttribute(fwt_detail_kernel<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        fwt_detail_kernel<2, true><<<nblk * nc, 256, smem, s>>>(a, nullptr, u);
+    } else {
+        cudaFuncSetAttribute(fwt_detail_kernel<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        fwt_detail_kernel<3, true><<<nblk * nc, 256, smem, s>>>(a, nullptr, u);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wavelet_reconstruct(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
+                                       int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    WaveletInfo w;
+    char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
+    if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
+    const int key = wavelet_x * 10 + wavelet_y;
+    if (g_rflt_key != key) {
+        double hr[32] = {}, gr[32] = {};
+        for (size_t i = 0; i < w.HR.size(); i++) hr[i] = w.HR[i];
+        for (size_t i = 0; i < w.GR.size(); i++) gr[i] = w.GR[i];
+        int flt[4] = {w.hr_lo, (int)w.HR.size(), w.gr_lo, (int)w.GR.size()};
+        cudaError_t e = cudaMemcpyToSymbolAsync(c_hr, hr, sizeof(hr), 0, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_gr, gr, sizeof(gr), 0, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_rflt, flt, sizeof(flt), 0, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+        g_rflt_key = key;
+    }
+    const int hr_hi = w.hr_lo + (int)w.HR.size() - 1, gr_hi = w.gr_lo + (int)w.GR.size() - 1;
+    const int F = std::max(std::max(w.hr_lo, hr_hi), std::max(w.gr_lo, gr_hi));
+    // the x pass reads up to F+1 points beyond an interior WC position
+    if (F + 1 > geo.gb + 1 || Bs0 > 64 || Bs1 > 64 || Bs2 > 64) return cudaErrorInvalidValue;
+    {
+        cudaError_t e = launch_tpo(2, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, key, F, nullptr, s);
+        if (e != cudaErrorNotSupported) return e;
+        cudaGetLastError();
+    }
+    const int ny = Bs1 + 2 * F, nz = dim == 3 ? Bs2 + 2 * F : 1;
+    const size_t smem = sizeof(double) * (size_t)Bs0 * ny * nz;
+    if (dim == 2) {
+        cudaFuncSetAttribute(iwt_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        iwt_kernel<2><<<nblk * nc, 256, smem, s>>>(blk, u, geo, Bs0, Bs1, 1, nc, w.lifted ? 0 : 1, F);
+    } else {
+        cudaFuncSetAttribute(iwt_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        iwt_kernel<3><<<nblk * nc, 256, smem, s>>>(blk, u, geo, Bs0, Bs1, Bs2, nc, w.lifted ? 0 : 1, F);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wc_threshold(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,
+                                int nc, const double *thresh, const int *tsvc, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    if (nc > 8) return cudaErrorInvalidValue;
+    WcThresh th{};
+    for (int c = 0; c < nc; c++) {
+        th.t[c] = thresh[c];
+        th.tsvc[c] = tsvc[c];
+    }
+    const long long n = (long long)nblk * Bs0 * Bs1 * (dim == 3 ? Bs2 : 1);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (dim == 2) wc_threshold_kernel<2><<<grid, 256, 0, s>>>(blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, th);
+    else wc_threshold_kernel<3><<<grid, 256, 0, s>>>(blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, th);
+    return cudaGetLastError();
 }
 
 cudaError_t wavelet_init() { return init_predictor(); }

@@ -227,13 +227,30 @@ class Forest:
     def run(self, nsteps: int, use_graph: bool = True):
         self.ctx.run([self], nsteps, use_graph)
 
-    def coarseningIndicator(self, eps_use):
+    def coarseningIndicator(self, eps_use, input_is_wd: bool = False):
+        """Flags (-1 may coarsen, 0 stay) and per-component details; with
+        input_is_wd the state already holds the decomposition."""
         eps_use = np.ascontiguousarray(np.broadcast_to(np.asarray(eps_use, np.float64), (self.cfg.neq,)))
         n = self.nblocks
         flags = np.zeros(n, np.int32)
         det = np.zeros((n, self.cfg.neq))
-        capi.check(self.L.wg_threshold_flags(self.ctx.h, self.tree, _p(eps_use), _p(flags, ctypes.c_int), _p(det)))
+        fn = self.L.wg_threshold_flags_wd if input_is_wd else self.L.wg_threshold_flags
+        capi.check(fn(self.ctx.h, self.tree, _p(eps_use), _p(flags, ctypes.c_int), _p(det)))
         return flags, det
+
+    def wavelet_decompose(self):
+        """One-level FWT of every block in place (spaghetti order); ghosts
+        must be synchronised first (sync_ghosts_tree)."""
+        capi.check(self.L.wg_wavelet_decompose(self.ctx.h, self.tree))
+
+    def wavelet_reconstruct(self):
+        """One-level IWT of every block in place; the ghosts must hold the
+        neighbours' decomposed data."""
+        capi.check(self.L.wg_wavelet_reconstruct(self.ctx.h, self.tree))
+
+    def wc_threshold(self, thresh):
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(thresh, np.float64), (self.cfg.neq,)))
+        capi.check(self.L.wg_wavelet_threshold(self.ctx.h, self.tree, _p(t)))
 
     def refine_everywhere(self):
         capi.check(self.L.wg_refine_everywhere(self.ctx.h, self.tree))

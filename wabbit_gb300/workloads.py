@@ -19,6 +19,14 @@ the measurements are quoted on:
   (FP64 state); grid refined around the sphere with wider level-dependent
   radii (36,688 blocks over levels 3-7).
 
+* ``adapt3d_cdf44`` -- the adapt path at scale: 3-D, Bs=16^3, g=6, CDF4,4,
+  periodic [0,1]^3, 99,184 blocks over levels 3-7 (four level jumps),
+  threshold eps=1e-4 (Linfty-normalised). Field (seed 5), per component: 16
+  Fourier modes with integer wave vectors |k| <= 8 drawn uniformly, random
+  phases and N(0,1)/|k|^2 amplitudes, plus 32 fronts tanh((n.x - d)/0.01)
+  with uniformly random unit normals n and offsets d (minimum image on the
+  torus); evaluated on the device (`adapt_field_device`).
+
 All random draws use numpy's PCG64 generator with the stated seed, in block
 order, component order, then point order (x fastest).
 """
@@ -28,7 +36,7 @@ import numpy as np
 
 from . import config, grids
 
-WORKLOADS = ("acm2d_vortex", "acm3d_sphere", "acm3d_sphere_j7")
+WORKLOADS = ("acm2d_vortex", "acm3d_sphere", "acm3d_sphere_j7", "adapt3d_cdf44")
 
 
 def make_config(name: str):
@@ -60,6 +68,17 @@ def make_config(name: str):
         c.CFL = 0.5
         c.eps, c.eps_normalized = 1e-3, 1
         c.u_mean_set[:] = (1.0, 0.0, 0.0)
+        c.time_max = 1e9
+        return c
+    if name == "adapt3d_cdf44":
+        c = config.defaults(3)
+        c.Bs[:] = (16, 16, 16)
+        c.domain[:] = (1.0, 1.0, 1.0)
+        c.wavelet = b"CDF44"
+        c.g, c.g_rhs = 6, 2
+        c.Jmin, c.Jmax = 3, 7
+        c.eps, c.eps_normalized = 1e-4, 1
+        c.penalization = 0
         c.time_max = 1e9
         return c
     raise ValueError(f"unknown workload {name}")
@@ -97,7 +116,7 @@ def make_grid(name: str, cfg):
         return _to_arrays(leaves)
     centre = [0.5 * cfg.domain[d] for d in range(3)]
     jmin = cfg.Jmin
-    a, b = (0.3, 0.8) if name.endswith("j7") else (0.2, 0.6)
+    a, b = (0.3, 0.8) if name.endswith("j7") else (0.16, 0.32) if name == "adapt3d_cdf44" else (0.2, 0.6)
     return grids.refined_around(3, jmin, cfg.Jmax, cfg.domain, centre, lambda l: a + b * 2.0 ** (-(l - jmin)))
 
 
@@ -137,6 +156,51 @@ def initial_condition(name: str, cfg, lv, co):
     u[:, 0] += 1.0
     u[:, 3] = 0.0
     return u
+
+
+def adapt_field_device(cfg, lv, co, seed: int = 5, nmodes: int = 16, nfronts: int = 32, chunk: int = 4096):
+    """Interior field of the adapt workload on the GPU (torch float64),
+    shape (nblk, 4, Bz, By, Bx)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    dev = torch.device("cuda")
+    nc = cfg.neq
+    params = []
+    for _ in range(nc):
+        ks = []
+        while len(ks) < nmodes:
+            k = rng.integers(-8, 9, size=3)
+            if 0 < np.linalg.norm(k) <= 8:
+                ks.append(k)
+        ks = np.array(ks, float)
+        phase = rng.uniform(0.0, 2.0 * np.pi, size=nmodes)
+        amp = rng.normal(0.0, 1.0, size=nmodes) / np.sum(ks * ks, axis=1)
+        n = rng.normal(size=(nfronts, 3))
+        n /= np.linalg.norm(n, axis=1, keepdims=True)
+        d = rng.uniform(0.0, 1.0, size=(nfronts, 3))
+        params.append((ks, phase, amp, n, d))
+    x0, dx = grids.block_geometry(lv, co, cfg.domain, cfg.Bs, 3)
+    B = cfg.Bs[0]
+    out = torch.empty((len(lv), nc, B, B, B), device=dev, dtype=torch.float64)
+    ar = torch.arange(B, device=dev, dtype=torch.float64)
+    for s0 in range(0, len(lv), chunk):
+        s1 = min(len(lv), s0 + chunk)
+        X0 = torch.as_tensor(x0[s0:s1], device=dev)
+        DX = torch.as_tensor(dx[s0:s1], device=dev)
+        X = X0[:, 0, None, None, None] + ar[None, None, None, :] * DX[:, 0, None, None, None]
+        Y = X0[:, 1, None, None, None] + ar[None, None, :, None] * DX[:, 1, None, None, None]
+        Z = X0[:, 2, None, None, None] + ar[None, :, None, None] * DX[:, 2, None, None, None]
+        for c, (ks, phase, amp, n, d) in enumerate(params):
+            f = torch.zeros((s1 - s0, B, B, B), device=dev, dtype=torch.float64)
+            for m in range(len(ks)):
+                arg = 2.0 * np.pi * (ks[m, 0] * X + ks[m, 1] * Y + ks[m, 2] * Z) + phase[m]
+                f += amp[m] * torch.cos(arg)
+            for m in range(len(n)):
+                r = [X - d[m, 0], Y - d[m, 1], Z - d[m, 2]]
+                r = [q - torch.round(q) for q in r]
+                f += torch.tanh((n[m, 0] * r[0] + n[m, 1] * r[1] + n[m, 2] * r[2]) / 0.01)
+            out[s0:s1, c] = f
+    return out
 
 
 def sphere_mask(cfg, lv, co, centre=None, radius=0.2, C_smooth=1.5):
