@@ -153,6 +153,19 @@ int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const do
 int wg_set_time(wg_ctx *ctx, int tree, double time);
 int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);
 
+/* adapt_tree (LIB/MESH/adapt_tree.f90:11-255) for unlifted wavelets (CDF X0,
+ * whose adaptation uses neither coarse extension nor security zone): full
+ * tree with every ancestor down to Jmin, mothers filled with their
+ * daughters' scaling coefficients (sync_D2M), coarsening indicator on every
+ * block (WG_ADAPT_THRESHOLD: threshold-state-vector with eps_use = eps *
+ * norm per component; WG_ADAPT_EVERYWHERE: every leaf), respectJmaxJmin,
+ * completeness, gradedness (ensureGradedness_tree with check_daughters),
+ * deletion and pruning; the grid and the state are replaced, *nblk_out
+ * receives the new block count (wg_get_grid returns the new grid). Masks are
+ * dropped. Needs free arena slots for the mothers (about nblk/(2^d-1)). */
+#define WG_ADAPT_THRESHOLD 0
+#define WG_ADAPT_EVERYWHERE 1
+int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *nblk_out);
 /* One-level wavelet transforms of every block of the tree, in place on the
  * state (interior points; the ghost nodes must be synchronised first, for the
  * inverse with the decomposed data):

@@ -55,6 +55,7 @@ def lib():
         L.or_threshold_flags.argtypes = [ctypes.c_void_p, _dp, _ip, _dp]
         L.or_fwt.argtypes = [ctypes.c_void_p, _dp]
         L.or_iwt.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.or_adapt.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.or_wc_threshold.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.or_refine_everywhere.argtypes = [ctypes.c_void_p]
         L.or_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _dp]
@@ -191,6 +192,18 @@ class Oracle:
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(thresh, np.float64), (self.cfg.neq,)))
         self.L.or_wc_threshold(self.h, _p(out), _p(t))
         return out
+
+    def adapt(self, eps_use=None, everywhere=False):
+        """adapt_tree for CDF X0 (threshold-state-vector or everywhere);
+        returns the new block count."""
+        if everywhere:
+            n = self.L.or_adapt(self.h, None, 1)
+        else:
+            e = np.ascontiguousarray(np.broadcast_to(np.asarray(eps_use, np.float64), (self.cfg.neq,)))
+            n = self.L.or_adapt(self.h, _p(e), 0)
+        if n < 0:
+            raise RuntimeError(f"or_adapt failed ({n})")
+        return n
 
     def refine_everywhere(self):
         self.L.or_refine_everywhere(self.h)

@@ -1096,6 +1096,220 @@ static void refine_everywhere(Oracle &o) {
     update_neighbors(o);
 }
 
+// ---------------------------------------------------------------------------
+// adapt_tree for unlifted wavelets (LIB/MESH/adapt_tree.f90:11-255; no coarse
+// extension, no security zone, no WC thresholding):
+//  * init_full_tree (adapt_tree.f90:995-1085): every block without a mother
+//    above Jmin whose last treecode digit is 2^dim-1 creates its mother,
+//    repeated until no block is added;
+//  * the leaves are synchronised with g layers and flagged; the mothers, from
+//    the finest level down, receive their daughters' scaling coefficients
+//    (sync_D2M, executeCoarsening_tree.f90:125-227: every second interior
+//    point for CDF X0) and, as ghost nodes, their same-level neighbours'
+//    values (the full-tree sync of sync_TMP_from_all: a non-leaf block of a
+//    graded tree has a same-level neighbour in every direction), then are
+//    flagged (coarseningIndicator_tree.f90: the "everywhere" indicator flags
+//    the leaves only);
+//  * respectJmaxJmin_tree, then ensureGradedness_tree(check_daughters) with
+//    ensure_completeness_block until nothing changes (ensureGradedness_tree.f90:
+//    13-219, ensure_completeness_block.f90:7-87);
+//  * blocks still at -1 are deleted, the remaining blocks without remaining
+//    daughters are the new grid (prune_fulltree2leafs), their data the
+//    leaves' own or the mothers' daughter coefficients; final ghost sync.
+// ---------------------------------------------------------------------------
+static int adapt_unlifted(Oracle &o, const double *eps_use, int everywhere) {
+    const wg_config &p = o.cfg;
+    const int dim = p.dim, g = p.g, nd = 1 << dim;
+    const int Jmin = p.Jmin;
+    sync_ghosts(o, g, g, true);
+    const int nleaf = (int)o.blocks.size();
+    // full tree
+    std::vector<int> mother(nleaf, -1);
+    auto digit_all_set = [&](const Block &b) { return tc_last_digit(b) == nd - 1; };
+    size_t nold = 0;
+    while (nold != o.blocks.size()) {
+        nold = o.blocks.size();
+        for (size_t i = 0; i < nold; i++) {
+            const Block b = o.blocks[i];
+            if (mother[i] >= 0 || b.level == Jmin) continue;
+            if (b.level < Jmin) return WG_EGRID;
+            if (!digit_all_set(b)) continue;
+            Block m;
+            m.level = b.level - 1;
+            for (int a = 0; a < 3; a++) m.c[a] = b.c[a] >> 1;
+            o.blocks.push_back(m);
+            mother.push_back(-1);
+            o.lookup[key_of(m.level, m.c[0], m.c[1], m.c[2])] = (int)o.blocks.size() - 1;
+            mother[i] = (int)o.blocks.size() - 1;
+        }
+        // link the other daughters of the new mothers
+        for (size_t i = 0; i < o.blocks.size(); i++) {
+            const Block &b = o.blocks[i];
+            if (mother[i] >= 0 || b.level == Jmin) continue;
+            int c[3] = {b.c[0] >> 1, b.c[1] >> 1, b.c[2] >> 1};
+            mother[i] = find_block(o, b.level - 1, c);
+        }
+    }
+    const int nt = (int)o.blocks.size();
+    std::vector<std::vector<int>> daughters(nt);
+    for (int i = 0; i < nt; i++)
+        if (mother[i] >= 0) daughters[mother[i]].push_back(i);
+    for (int i = 0; i < nt; i++)
+        if (!daughters[i].empty() && (int)daughters[i].size() != nd) return WG_EGRID;
+    o.data.resize(size_t(nt) * o.nc * o.npts, 0.0);
+    auto idx = [&](int ix, int iy, int iz) { return ((size_t)(iz - 1) * o.ny + (iy - 1)) * o.nx + (ix - 1); };
+    int lmax = 0;
+    for (const Block &b : o.blocks) lmax = std::max(lmax, b.level);
+    std::vector<int> flags(nt, 0);
+    // leaf flags (after the sync above)
+    for (int i = 0; i < nleaf; i++)
+        flags[i] = everywhere ? -1 : threshold_block(o, i, eps_use, nullptr);
+    const int zlo = dim == 3 ? g + 1 : 1, zhi = dim == 3 ? g + p.Bs[2] : 1;
+    const int half[3] = {p.Bs[0] / 2, p.Bs[1] / 2, dim == 3 ? p.Bs[2] / 2 : 1};
+    for (int l = lmax - 1; l >= Jmin; l--) {
+        // sync_D2M: the mother's interior point takes the daughter's SC
+        for (int m = nleaf; m < nt; m++) {
+            if (o.blocks[m].level != l) continue;
+            for (int dgt : daughters[m]) {
+                const Block &d = o.blocks[dgt];
+                const int kx = d.c[0] & 1, ky = d.c[1] & 1, kz = dim == 3 ? (d.c[2] & 1) : 0;
+                for (int c = 0; c < o.nc; c++) {
+                    const double *src = o.blk(dgt) + size_t(c) * o.npts;
+                    double *dst = o.blk(m) + size_t(c) * o.npts;
+                    for (int k = 0; k < (dim == 3 ? half[2] : 1); k++)
+                        for (int j = 0; j < half[1]; j++)
+                            for (int i = 0; i < half[0]; i++) {
+                                const int mi = g + 1 + kx * half[0] + i, mj = g + 1 + ky * half[1] + j;
+                                const int mk = dim == 3 ? g + 1 + kz * half[2] + k : 1;
+                                const int si = g + 1 + 2 * i, sj = g + 1 + 2 * j, sk = dim == 3 ? g + 1 + 2 * k : 1;
+                                dst[idx(mi, mj, mk)] = src[idx(si, sj, sk)];
+                            }
+                }
+            }
+        }
+        if (everywhere) continue;
+        // ghost nodes of the mothers from their same-level neighbours
+        for (int m = nleaf; m < nt; m++) {
+            if (o.blocks[m].level != l) continue;
+            const Block &mb = o.blocks[m];
+            for (int dz = (dim == 3 ? -1 : 0); dz <= (dim == 3 ? 1 : 0); dz++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dx = -1; dx <= 1; dx++) {
+                        if (!dx && !dy && !dz) continue;
+                        const int d[3] = {dx, dy, dz};
+                        const int n = 1 << l;
+                        int c[3] = {0, 0, 0};
+                        for (int a = 0; a < dim; a++) c[a] = ((mb.c[a] + d[a]) % n + n) % n;
+                        const int nb = find_block(o, l, c);
+                        if (nb < 0) continue;
+                        int lo[3], hi[3], so[3];
+                        for (int a = 0; a < 3; a++) {
+                            if (a >= dim) { lo[a] = hi[a] = so[a] = 1; continue; }
+                            const int B = p.Bs[a];
+                            lo[a] = d[a] < 0 ? 1 : d[a] == 0 ? g + 1 : g + B + 1;
+                            hi[a] = d[a] < 0 ? g : d[a] == 0 ? g + B : B + 2 * g;
+                            so[a] = d[a] < 0 ? B + 1 : g + 1;
+                        }
+                        for (int c2 = 0; c2 < o.nc; c2++) {
+                            const double *src = o.blk(nb) + size_t(c2) * o.npts;
+                            double *dst = o.blk(m) + size_t(c2) * o.npts;
+                            for (int k = lo[2]; k <= hi[2]; k++)
+                                for (int j = lo[1]; j <= hi[1]; j++)
+                                    for (int i = lo[0]; i <= hi[0]; i++)
+                                        dst[idx(i, j, k)] = src[idx(so[0] + i - lo[0], so[1] + j - lo[1], so[2] + k - lo[2])];
+                        }
+                    }
+        }
+        for (int m = nleaf; m < nt; m++)
+            if (o.blocks[m].level == l) flags[m] = threshold_block(o, m, eps_use, nullptr);
+    }
+    (void)zlo;
+    (void)zhi;
+    // respectJmaxJmin_tree
+    const int STAY = 9;
+    for (int i = 0; i < nt; i++)
+        if (flags[i] == -1 && o.blocks[i].level <= Jmin) flags[i] = STAY;
+    // ensureGradedness_tree(check_daughters, stay=REF_UNSIGNIFICANT_STAY)
+    bool changed = true;
+    int guard = 0;
+    while (changed) {
+        changed = false;
+        if (++guard > 10 * (p.Jmax + 1) + 100) return WG_EGRID;
+        for (int i = 0; i < nt; i++) {
+            if (flags[i] != -1) continue;
+            // ensure_completeness_block
+            const int m = mother[i];
+            const std::vector<int> &sis = daughters[m];
+            bool all_coarsen = true;
+            for (int s2 : sis)
+                if (flags[s2] >= 0) all_coarsen = false;
+            if (!all_coarsen) {
+                for (int s2 : sis)
+                    if (flags[s2] < 0) flags[s2] = STAY;
+                changed = true;
+                continue;
+            }
+            bool dstay = false;
+            for (int d2 : daughters[i])
+                if (flags[d2] == 0 || flags[d2] == STAY) dstay = true;
+            if (dstay) {
+                for (int s2 : sis)
+                    if (flags[s2] < 0) flags[s2] = STAY;
+                changed = true;
+                continue;
+            }
+            // gradedness: finer neighbours that stay
+            const Block b = o.blocks[i];
+            const int n = 1 << b.level;
+            bool keep = false;
+            for (int dz = (dim == 3 ? -1 : 0); dz <= (dim == 3 ? 1 : 0) && !keep; dz++)
+                for (int dy = -1; dy <= 1 && !keep; dy++)
+                    for (int dx = -1; dx <= 1 && !keep; dx++) {
+                        if (!dx && !dy && !dz) continue;
+                        const int d[3] = {dx, dy, dz};
+                        int c[3] = {0, 0, 0};
+                        for (int a = 0; a < dim; a++) c[a] = ((b.c[a] + d[a]) % n + n) % n;
+                        // finer blocks touching b across d
+                        for (int kz = 0; kz < (dim == 3 ? 2 : 1) && !keep; kz++)
+                            for (int ky = 0; ky < 2 && !keep; ky++)
+                                for (int kx = 0; kx < 2 && !keep; kx++) {
+                                    const int kk[3] = {kx, ky, kz};
+                                    bool adj = true;
+                                    for (int a = 0; a < dim; a++)
+                                        if ((d[a] == 1 && kk[a] != 0) || (d[a] == -1 && kk[a] != 1)) adj = false;
+                                    if (!adj) continue;
+                                    int fc[3] = {2 * c[0] + kx, 2 * c[1] + ky, dim == 3 ? 2 * c[2] + kz : 0};
+                                    const int f = find_block(o, b.level + 1, fc);
+                                    if (f >= 0 && (flags[f] == 0 || flags[f] == STAY)) keep = true;
+                                }
+                    }
+            if (keep) {
+                flags[i] = STAY;
+                changed = true;
+            }
+        }
+    }
+    // delete -1 blocks, prune to leaves
+    std::vector<Block> nbl;
+    std::vector<double> ndata;
+    for (int i = 0; i < nt; i++) {
+        if (flags[i] == -1) continue;
+        bool kept_daughter = false;
+        for (int d2 : daughters[i])
+            if (flags[d2] != -1) kept_daughter = true;
+        if (kept_daughter) continue;
+        nbl.push_back(o.blocks[i]);
+        ndata.insert(ndata.end(), o.blk(i), o.blk(i) + size_t(o.nc) * o.npts);
+    }
+    o.blocks = nbl;
+    o.data.swap(ndata);
+    o.mask.clear();   // masks depend on the grid
+    rebuild_lookup(o);
+    update_neighbors(o);
+    sync_ghosts(o, g, g, true);
+    return WG_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1258,6 +1472,15 @@ int or_wc_threshold(void *h, double *data, const double *thresh) {
     Oracle &o = *(Oracle *)h;
     for (size_t b = 0; b < o.blocks.size(); b++) wc_threshold_block(o, data + b * o.nc * o.npts, thresh);
     return WG_OK;
+}
+
+// adapt_tree (CDF X0): indicator 0 threshold-state-vector (eps_use per
+// component), 1 everywhere; returns the new block count or an error
+int or_adapt(void *h, const double *eps_use, int indicator) {
+    Oracle &o = *(Oracle *)h;
+    if (o.wav.Y != 0) return WG_ENOTSUP;
+    const int st = adapt_unlifted(o, eps_use, indicator == 1);
+    return st ? st : (int)o.blocks.size();
 }
 
 int or_refine_everywhere(void *h) {

@@ -1,0 +1,109 @@
+"""Grid adaptation (adapt_tree, unlifted wavelets) on the GPU: the new grid
+and the new state must equal the oracle's bit for bit, and the reference's
+coarsen-everywhere regression file (TESTING/wavelets/adaptive_CDF40) is
+reproduced."""
+import numpy as np
+import pytest
+
+from helpers import small_cfg, smooth_state
+from pyoracle import Oracle, interior, pad_blocks
+from wabbit_gb300 import config, grids
+from wabbit_gb300.solver import Context
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():
+    pytest.skip("no CUDA device", allow_module_level=True)
+
+
+def _sorted(lv, co, u):
+    order = np.lexsort((co[:, 0], co[:, 1], co[:, 2], lv))
+    return lv[order], co[order], u[order]
+
+
+def test_coarsen_everywhere_golden_cdf40(golden):
+    z = golden("wavelet_adaptive.npz")
+    cfg = config.defaults(2)
+    cfg.Bs[0] = cfg.Bs[1] = 32
+    cfg.domain[0] = cfg.domain[1] = 6.283185307179586
+    cfg.wavelet = b"CDF40"
+    cfg.g, cfg.g_rhs = 3, 2
+    cfg.Jmin, cfg.Jmax = 1, 7
+    u1 = z["refined_u"]                          # one component; the ACM state carries three copies
+    u3 = np.repeat(u1, 3, axis=1)
+    with Context(cfg, 2 * len(u1)) as ctx:
+        f = ctx.forest()
+        f.set_grid(z["refined_level"], z["refined_coords"])
+        f.upload(pad_blocks(cfg, u3))
+        n = f.adapt(everywhere=True)
+        assert n == 112
+        lv, co = f.grid()
+        lv, co, u = _sorted(lv, co, interior(cfg, f.download()))
+    assert np.array_equal(lv, z["coarsened_CDF40_level"])
+    assert np.array_equal(co, z["coarsened_CDF40_coords"])
+    for c in range(3):
+        assert np.array_equal(u[:, c:c + 1], z["coarsened_CDF40_u"])
+
+
+@pytest.mark.parametrize("dim,wavelet,quantile", [(2, "CDF40", 0.5), (2, "CDF20", 0.7), (2, "CDF60", 0.4),
+                                                  (3, "CDF40", 0.95)])
+def test_threshold_adapt_matches_oracle(dim, wavelet, quantile):
+    g, _ = config.wavelet_ghosts(wavelet)
+    Bs = 16 if dim == 2 else 8
+    cfg = small_cfg(dim, wavelet, Bs=Bs, jmin=2 if dim == 2 else 1, jmax=5 if dim == 2 else 3)
+    lv, co = grids.random_graded(dim, cfg.Jmin, cfg.Jmax, seed=21, frac=0.45)
+    data = smooth_state(cfg, lv, co, 7)
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    o.sync(cfg.g, cfg.g, ignore_filter=True)
+    _, det = o.flags(np.full(cfg.neq, 1.0))
+    eps = np.quantile(det, quantile, axis=0)
+    with Context(cfg, 2 * len(lv) + 8) as ctx:
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(data)
+        for rnd in range(2):
+            n_ref = o.adapt(eps)
+            n = f.adapt(eps)
+            assert n == n_ref
+            a = _sorted(*o.grid(), o.data())
+            b = _sorted(*f.grid(), f.download())
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+            assert np.array_equal(a[2], b[2])
+            eps = eps * 4.0
+        assert n < len(lv)
+
+
+def test_refine_step_adapt_loop_matches_oracle():
+    """Three cycles of the reference's main loop with adaptation (refine
+    everywhere, RK4 step, adapt; LIB/MAIN/main.f90:314-400) with the
+    bit-exact stencil variant."""
+    cfg = small_cfg(2, "CDF40", Bs=16, jmin=2, jmax=8)   # three refinements above level 4 stay below Jmax
+    cfg.eps, cfg.eps_normalized = 1e-2, 0
+    lv, co = grids.random_graded(2, 2, 4, seed=3, frac=0.4)
+    data = smooth_state(cfg, lv, co, 9)
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    eps = np.full(cfg.neq, cfg.eps)
+    with Context(cfg, 16 * len(lv)) as ctx:
+        ctx.set_variant(False)
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(data)
+        f.set_time(0.0)
+        t = 0.0
+        for cycle in range(3):
+            o.sync(cfg.g, cfg.g, ignore_filter=True)
+            o.refine_everywhere()
+            t, _ = o.step(t)
+            n_ref = o.adapt(eps)
+            f.sync_ghosts_tree()
+            f.refine_everywhere()
+            f.timeStep_tree()
+            n = f.adapt(eps)
+            assert n == n_ref, cycle
+            a = _sorted(*o.grid(), o.data())
+            b = _sorted(*f.grid(), f.download())
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+            assert np.array_equal(interior(cfg, a[2]), interior(cfg, b[2])), cycle

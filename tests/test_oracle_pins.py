@@ -147,3 +147,22 @@ def test_cdf40_filters_match_reference_log():
     assert np.array_equal(gd, [6.25e-2, 0.0, -5.625e-1, 1.0, -5.625e-1, 0.0, 6.25e-2])
     lo, hr = o.filter(2)
     assert np.array_equal(hr, [-6.25e-2, 0.0, 5.625e-1, 1.0, 5.625e-1, 0.0, -6.25e-2])
+
+
+def test_coarsen_everywhere_golden_cdf40(golden):
+    """adapt_tree with the 'everywhere' indicator on the refined grid (448
+    blocks, levels 3-6) reproduces the reference's coarsened file
+    (TESTING/wavelets/adaptive_CDF40/vor_00200.h5: 112 blocks, levels 2-5)
+    bit for bit: full tree, sync_D2M, completeness and gradedness."""
+    z = golden("wavelet_adaptive.npz")
+    cfg = wavelet_cfg("CDF40", 3)
+    o = Oracle(cfg)
+    o.set_grid(z["refined_level"], z["refined_coords"], pad_blocks(cfg, z["refined_u"]))
+    n = o.adapt(everywhere=True)
+    assert n == 112
+    lv, co = o.grid()
+    u = interior(cfg, o.data())
+    order = np.lexsort((co[:, 0], co[:, 1], co[:, 2], lv))
+    assert np.array_equal(lv[order], z["coarsened_CDF40_level"])
+    assert np.array_equal(co[order], z["coarsened_CDF40_coords"])
+    assert np.array_equal(u[order], z["coarsened_CDF40_u"])

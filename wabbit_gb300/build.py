@@ -20,6 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = {
     "forest.cpp": [],
+    "adapt.cpp": [],
     "capi.cu": [],
     "k_sync.cu": ["-fmad=false"],
     "k_misc.cu": [],

@@ -28,6 +28,7 @@
 #include <cuda.h>
 
 #include "../../include/wabbit_gb300.h"
+#include "adapt.hpp"
 #include "common.cuh"
 
 namespace wg {
@@ -1414,6 +1415,138 @@ int wg_threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags,
 // from it without a second FWT
 int wg_threshold_flags_wd(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details) {
     return threshold_flags(ctx, tree, eps_use, flags, details, 1);
+}
+
+// adapt_tree (LIB/MESH/adapt_tree.f90:11-255) for unlifted wavelets (CDF X0,
+// no coarse extension and no security zone): the full tree of the grid is
+// built on the host (adapt.cpp); the mothers, level by level from the
+// finest, receive their daughters' scaling coefficients (sync_D2M: every
+// second interior point for CDF X0) and the same-level neighbours' values as
+// ghost nodes; every block of the full tree is flagged by the coarsening
+// indicator on its own data (the leaves after a sync with g layers); the
+// host makes the flags consistent (Jmin, completeness, daughters,
+// gradedness) and keeps the blocks that remain without remaining daughters.
+// Their data is already in their slots: the old leaves' untouched, the
+// promoted mothers' from their daughters. Masks are dropped (they depend on
+// the grid and are set again by the caller). Ends with a ghost sync.
+int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *nblk_out) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    if (indicator != WG_ADAPT_THRESHOLD && indicator != WG_ADAPT_EVERYWHERE)
+        return fail(WG_EINVAL, "unknown indicator %d", indicator);
+    if (indicator == WG_ADAPT_THRESHOLD && !eps_use) return fail(WG_EINVAL, "eps_use is required");
+    if (ctx->wav.lifted)
+        return fail(WG_ENOTSUP, "adapt for lifted wavelets (coarse extension, security zone) is not built; CDF X0 only");
+    const int dim = ctx->cfg.dim, nc = ctx->geo.nc, g = ctx->cfg.g;
+    const int *Bs = ctx->cfg.Bs;
+    const int nb = t->forest.size();
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    int st = run_sync(ctx, *t, ctx->A, false, g, g);
+    if (st) return st;
+    FullTree ft;
+    std::string err;
+    if (!build_full_tree(dim, t->cfg.Jmin, nb, t->forest.level.data(), t->forest.coords.data(), ft, err))
+        return fail(WG_EGRID, "adapt: %s", err.c_str());
+    const int nt = ft.size(), nm = nt - nb;
+    if ((size_t)nm > ctx->free_slots.size())
+        return fail(WG_ENOMEM, "adapt needs %d free slots for the mothers (%zu free)", nm, ctx->free_slots.size());
+    std::vector<int> slot(nt);
+    for (int b = 0; b < nb; b++) slot[b] = t->slots[b];
+    std::sort(ctx->free_slots.begin(), ctx->free_slots.end(), std::greater<int>());
+    for (int b = nb; b < nt; b++) {
+        slot[b] = ctx->free_slots.back();
+        ctx->free_slots.pop_back();
+    }
+    auto give_back = [&](const std::vector<int> &keep) {
+        std::vector<char> kept(nt, 0);
+        for (int b : keep) kept[b] = 1;
+        for (int b = 0; b < nt; b++)
+            if (!kept[b]) ctx->free_slots.push_back(slot[b]);
+    };
+    std::vector<int> flags(nt, 0);
+    DevArray<int> d_flags, d_tsvc, d_list;
+    DevArray<double> d_eps;
+    const bool thr = indicator == WG_ADAPT_THRESHOLD;
+    cudaError_t e = cudaSuccess;
+    if (thr) {
+        e = d_flags.upload(nullptr, nt, ctx->stream);
+        if (e == cudaSuccess) e = d_eps.upload(eps_use, nc, ctx->stream);
+        if (e == cudaSuccess) e = d_tsvc.upload(t->cfg.threshold_state_vector_component, nc, ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_fwt_flags(dim, t->d_all.p, nb, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], nc, ctx->wav.X, ctx->wav.Y,
+                                 d_eps.p, d_tsvc.p, d_flags.p, nullptr, ctx->stream);
+    } else {
+        for (int b = 0; b < nb; b++) flags[b] = kFlagCoarsen;   // "everywhere": the leaves
+    }
+    // mothers level by level from the finest
+    const int lmax = ft.max_level();
+    std::vector<std::unique_ptr<DevArray<Patch>>> keep_alive;   // alive until the stream is synchronised
+    std::vector<std::unique_ptr<DevArray<int>>> keep_lists;
+    for (int l = lmax - 1; l >= t->cfg.Jmin && e == cudaSuccess; l--) {
+        std::vector<Patch> d2m, gh;
+        mother_patches(ft, ctx->geo, l, slot, d2m, gh);
+        if (d2m.empty()) continue;
+        keep_alive.emplace_back(new DevArray<Patch>());
+        e = keep_alive.back()->upload(d2m.data(), d2m.size(), ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_sync(keep_alive.back()->p, (int)d2m.size(), ctx->A, ctx->gA, nc, ctx->wav.order_predictor,
+                            ctx->stream);
+        if (!thr || e != cudaSuccess) continue;
+        keep_alive.emplace_back(new DevArray<Patch>());
+        e = keep_alive.back()->upload(gh.data(), gh.size(), ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_sync(keep_alive.back()->p, (int)gh.size(), ctx->A, ctx->gA, nc, ctx->wav.order_predictor,
+                            ctx->stream);
+        // indicator of this level's mothers (consecutive full-tree indices)
+        std::vector<int> ms;
+        int first = -1;
+        for (int b = nb; b < nt; b++)
+            if (ft.level[b] == l) {
+                if (first < 0) first = b;
+                ms.push_back(slot[b]);
+            }
+        keep_lists.emplace_back(new DevArray<int>());
+        if (e == cudaSuccess) e = keep_lists.back()->upload(ms.data(), ms.size(), ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_fwt_flags(dim, keep_lists.back()->p, (int)ms.size(), ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], nc,
+                                 ctx->wav.X, ctx->wav.Y, d_eps.p, d_tsvc.p, d_flags.p + first, nullptr, ctx->stream);
+    }
+    if (e == cudaSuccess && thr)
+        e = cudaMemcpyAsync(flags.data(), d_flags.p, sizeof(int) * nt, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(ctx->stream);
+        for (int b = nb; b < nt; b++) ctx->free_slots.push_back(slot[b]);   // the grid is unchanged
+        return cuda_fail(e, "wg_adapt", __FILE__, __LINE__);
+    }
+    std::vector<int> leaves;
+    adapt_decide(ft, flags, leaves);
+    // install the new grid
+    const int nn = (int)leaves.size();
+    std::vector<int> lv(nn), co(3 * nn), sl(nn);
+    for (int i = 0; i < nn; i++) {
+        const int b = leaves[i];
+        lv[i] = ft.level[b];
+        for (int a = 0; a < 3; a++) co[3 * i + a] = ft.coords[3 * b + a];
+        sl[i] = slot[b];
+    }
+    give_back(leaves);
+    for (int m : t->mask_slot)
+        if (m >= 0) ctx->mask_free.push_back(m);
+    t->forest.set(nn, lv.data(), co.data());
+    if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "adapt produced an invalid grid: %s", err.c_str());
+    if (!t->forest.graded()) return fail(WG_EGRID, "adapt produced a grid that is not graded");
+    t->slots = sl;
+    t->mask_slot.assign(nn, -1);
+    t->sync.clear();
+    t->shadow_valid = false;
+    if ((st = upload_desc(ctx, *t, tree))) return st;
+    if ((st = upload_lists(ctx, *t))) return st;
+    ctx->grid_version++;
+    if ((st = run_sync(ctx, *t, ctx->A, false, g, g))) return st;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    if (nblk_out) *nblk_out = nn;
+    return WG_OK;
 }
 
 // refine_tree(..., "everywhere") data part: every block is replaced by its

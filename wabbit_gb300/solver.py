@@ -252,6 +252,18 @@ class Forest:
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(thresh, np.float64), (self.cfg.neq,)))
         capi.check(self.L.wg_wavelet_threshold(self.ctx.h, self.tree, _p(t)))
 
+    def adapt(self, eps_use=None, everywhere: bool = False) -> int:
+        """adapt_tree (coarsening) with the threshold-state-vector indicator
+        (eps_use = eps * norm per component) or on every leaf; CDF X0 only.
+        Replaces grid and state, drops masks, returns the new block count."""
+        n = ctypes.c_int()
+        if everywhere:
+            capi.check(self.L.wg_adapt(self.ctx.h, self.tree, None, 1, ctypes.byref(n)))
+        else:
+            e = np.ascontiguousarray(np.broadcast_to(np.asarray(eps_use, np.float64), (self.cfg.neq,)))
+            capi.check(self.L.wg_adapt(self.ctx.h, self.tree, _p(e), 0, ctypes.byref(n)))
+        return n.value
+
     def refine_everywhere(self):
         capi.check(self.L.wg_refine_everywhere(self.ctx.h, self.tree))
 
