@@ -540,6 +540,116 @@ def run_adapt(args, rank, world):
     ctx.close()
 
 
+def run_adapt_loop(args, rank, world):
+    """Configuration 1: 2-D ACM (Bs=16, g=4, CDF4,0, Jmin=2, Jmax=5, eps=1e-3
+    absolute) with the grid adapted every step. The initial grid comes from
+    the vortex IC on the equidistant Jmax grid, adapted until it no longer
+    changes (adapt_inicond). One step = ghost sync, refine everywhere, one
+    RK4 step, adapt (LIB/MAIN/main.f90:314-400). value: point-updates/s of
+    the RK4 steps over the wall time of the whole loop (fused); the stepper
+    alone and the adapt part are reported beside it."""
+    import torch
+    from wabbit_gb300 import build, grids, workloads
+    from wabbit_gb300.solver import Context
+    build.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    cfg = workloads.make_config("acm2d_vortex")
+    lv, co = grids.equidistant(2, cfg.Jmax)
+    eps = np.full(cfg.neq, cfg.eps)
+    ctx = Context(cfg, 8 * len(lv))
+    f = ctx.forest()
+    f.set_grid(lv, co)
+    f.upload_interior(workloads.initial_condition("acm2d_vortex", cfg, lv, co))
+    n_prev = -1
+    while n_prev != f.nblocks:
+        n_prev = f.nblocks
+        f.adapt(eps)
+    f.set_time(0.0)
+    npts_blk = 16 * 16
+
+    def one(times=None):
+        t0 = time.perf_counter()
+        f.sync_ghosts_tree()
+        f.refine_everywhere()
+        t1 = time.perf_counter()
+        n = f.nblocks
+        f.timeStep_tree()
+        t2 = time.perf_counter()
+        f.adapt(eps)
+        t3 = time.perf_counter()
+        if times is not None:
+            times["refine"] += t1 - t0
+            times["step"] += t2 - t1
+            times["adapt"] += t3 - t2
+            times["points"] += n * npts_blk
+        return n
+
+    for _ in range(max(args.warmup, 1)):
+        one()
+    barrier(world)
+    times = {"refine": 0.0, "step": 0.0, "adapt": 0.0, "points": 0}
+    blocks = []
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            blocks.append(one(times))
+        el = max_over_ranks(time.perf_counter() - t0, world)
+    t_end, dt_last = f.time()
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        cpu = cpu_adapt_loop(cfg, lv, co, eps)
+    line = {
+        "metric": "ACM point-updates/s/GPU", "value": sum_over_ranks(times["points"] / el, world),
+        "unit": "point-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Gaussian vortices; see wabbit_gb300/workloads.py)",
+        "config": {"workload": "acm2d_vortex_adapt", "dim": 2, "Bs": [16, 16], "g": cfg.g, "wavelet": "CDF40",
+                   "Jmin": cfg.Jmin, "Jmax": cfg.Jmax, "eps": cfg.eps, "eps_normalized": False,
+                   "blocks_min": int(min(blocks)), "blocks_max": int(max(blocks)),
+                   "step": "sync g, refine everywhere, RK4 (FP64 fast), adapt",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "stepper_only": {"value": times["points"] / times["step"], "unit": "point-updates/s"},
+        "phase_ms_per_step": {k: 1e3 * times[k] / args.steps for k in ("refine", "step", "adapt")},
+        "clocks": clk.summary(), "t_end": t_end,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+
+
+def cpu_adapt_loop(cfg, lv, co, eps, seconds=12.0):
+    """The oracle running the same adapt loop (all host cores) for a bounded
+    time, from the same adapted initial grid."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from wabbit_gb300 import workloads
+    threads = os.cpu_count() or 1
+    o = pyoracle.Oracle(cfg, threads=threads)
+    u = workloads.initial_condition("acm2d_vortex", cfg, lv, co)
+    o.set_grid(lv, co, pyoracle.pad_blocks(cfg, u[:, :, 0]))
+    n_prev = -1
+    while n_prev != o.nblocks:
+        n_prev = o.nblocks
+        o.adapt(eps)
+    t = 0.0
+    points = 0
+    steps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds and steps < 50:
+        o.sync(cfg.g, cfg.g, ignore_filter=True)
+        o.refine_everywhere()
+        points += o.nblocks * 256
+        t, _ = o.step(t)
+        o.adapt(eps)
+        steps += 1
+    el = time.perf_counter() - t0
+    return {"value": points / el, "unit": "point-updates/s", "cores": threads, "kind": "port",
+            "sample": f"acm2d_vortex_adapt, {steps} steps of the same loop in {el:.1f} s"}
+
+
 def capi_graph_kernels(ctx):
     from wabbit_gb300 import capi
     n = ctx.L.wg_graph_kernels(ctx.h)
@@ -604,6 +714,8 @@ def main():
         run_serving(args, rank, world)
     elif args.workload == "adapt3d_cdf44":
         run_adapt(args, rank, world)
+    elif args.workload == "acm2d_vortex_adapt":
+        run_adapt_loop(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:

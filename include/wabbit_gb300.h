@@ -226,8 +226,10 @@ int wg_threshold_flags_wd(wg_ctx *ctx, int tree, const double *eps_use, int *fla
 int wg_threshold_flags_noalloc(const wg_config *cfg, int nblk, const double *d_blocks, const double *eps_use,
                                int *d_flags, double *d_details, void *stream);
 /* refine_tree(..., "everywhere") data part: refineBlock for every block
- * (LIB/MESH/refinementExecute.f90:4-116). Block b becomes blocks
- * 2^d*b .. 2^d*b+2^d-1. Ghosts must hold g synced layers. */
+ * below Jmax (LIB/MESH/refinementExecute.f90:4-116; blocks on Jmax stay,
+ * respectJmaxJmin_tree). In the new block order each refined block is
+ * replaced, at its position, by its 2^d daughters (digit order y, x, z).
+ * Ghosts must hold g synced layers. */
 int wg_refine_everywhere(wg_ctx *ctx, int tree);
 
 /* ---- measurement -------------------------------------------------------- */

@@ -1063,8 +1063,15 @@ static void refine_everywhere(Oracle &o) {
     const int fx = 2 * cx - 1, fy = 2 * cy - 1, fz = dim == 3 ? 2 * cz - 1 : 1;
     std::vector<double> fine(size_t(fx) * fy * fz);
     std::vector<double> coarse(size_t(o.npts));
-    // daughters are appended in (block, k_daughter) order
-    for (int b = 0; b < nblk; b++)
+    // daughters are appended in (block, k_daughter) order; blocks on Jmax stay
+    // (respectJmaxJmin_tree) and keep their place and data
+    std::vector<int> first(nblk);
+    for (int b = 0; b < nblk; b++) {
+        first[b] = (int)nbl.size();
+        if (o.blocks[b].level >= p.Jmax) {
+            nbl.push_back(o.blocks[b]);
+            continue;
+        }
         for (int k = 0; k < nd; k++) {
             Block d;
             d.level = o.blocks[b].level + 1;
@@ -1074,7 +1081,13 @@ static void refine_everywhere(Oracle &o) {
             d.c[2] = dim == 3 ? 2 * o.blocks[b].c[2] + bz : 0;
             nbl.push_back(d);
         }
+    }
+    ndata.assign(nbl.size() * o.nc * o.npts, 0.0);
     for (int b = 0; b < nblk; b++) {
+        if (o.blocks[b].level >= p.Jmax) {
+            std::copy(o.blk(b), o.blk(b) + size_t(o.nc) * o.npts, ndata.begin() + size_t(first[b]) * o.nc * o.npts);
+            continue;
+        }
         for (int c = 1; c <= o.nc; c++) {
             const double *u = o.blk(b) + size_t(c - 1) * o.npts;
             std::copy(u, u + o.npts, coarse.begin());
@@ -1083,7 +1096,7 @@ static void refine_everywhere(Oracle &o) {
                 int i0 = g + 1 + p.Bs[0] * ((k / 2) % 2);
                 int j0 = g + 1 + p.Bs[1] * (k % 2);
                 int k0 = dim == 3 ? g + 1 + p.Bs[2] * (k / 4) : 1;
-                double *dst = ndata.data() + (size_t(b) * nd + k) * o.nc * o.npts + size_t(c - 1) * o.npts;
+                double *dst = ndata.data() + (size_t(first[b]) + k) * o.nc * o.npts + size_t(c - 1) * o.npts;
                 for (int kk = 0; kk < o.nz; kk++)
                     for (int jj = 0; jj < o.ny; jj++)
                         for (int ii = 0; ii < o.nx; ii++)

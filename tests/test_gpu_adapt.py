@@ -79,8 +79,8 @@ def test_refine_step_adapt_loop_matches_oracle():
     """Three cycles of the reference's main loop with adaptation (refine
     everywhere, RK4 step, adapt; LIB/MAIN/main.f90:314-400) with the
     bit-exact stencil variant."""
-    cfg = small_cfg(2, "CDF40", Bs=16, jmin=2, jmax=8)   # three refinements above level 4 stay below Jmax
-    cfg.eps, cfg.eps_normalized = 1e-2, 0
+    cfg = small_cfg(2, "CDF40", Bs=16, jmin=2, jmax=5)   # blocks reaching Jmax stay when refining
+    cfg.eps, cfg.eps_normalized = 1e-6, 0
     lv, co = grids.random_graded(2, 2, 4, seed=3, frac=0.4)
     data = smooth_state(cfg, lv, co, 9)
     o = Oracle(cfg)
@@ -93,6 +93,7 @@ def test_refine_step_adapt_loop_matches_oracle():
         f.upload(data)
         f.set_time(0.0)
         t = 0.0
+        top = 0
         for cycle in range(3):
             o.sync(cfg.g, cfg.g, ignore_filter=True)
             o.refine_everywhere()
@@ -100,6 +101,7 @@ def test_refine_step_adapt_loop_matches_oracle():
             n_ref = o.adapt(eps)
             f.sync_ghosts_tree()
             f.refine_everywhere()
+            top = max(top, int(f.grid()[0].max()))
             f.timeStep_tree()
             n = f.adapt(eps)
             assert n == n_ref, cycle
@@ -107,3 +109,4 @@ def test_refine_step_adapt_loop_matches_oracle():
             b = _sorted(*f.grid(), f.download())
             assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
             assert np.array_equal(interior(cfg, a[2]), interior(cfg, b[2])), cycle
+        assert top == cfg.Jmax   # refinement reached Jmax and stayed there

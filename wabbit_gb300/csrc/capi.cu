@@ -1557,54 +1557,70 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     if (!t) return WG_EINVAL;
     const int dim = ctx->cfg.dim, nd = 1 << dim;
     const int nb = t->forest.size();
-    if ((size_t)nb * nd > ctx->free_slots.size()) return fail(WG_ENOMEM, "refinement needs %d free slots", nb * nd);
+    // blocks on Jmax stay (respectJmaxJmin_tree, LIB/MESH/respectJmaxJmin_tree.f90)
+    std::vector<int> ref;
     for (int b = 0; b < nb; b++)
-        if (t->forest.level[b] + 1 > t->cfg.Jmax) return fail(WG_EINVAL, "refinement beyond Jmax");
-    std::vector<int> lv(nb * nd), co(3 * nb * nd), slots(nb * nd), child_base(nb), parents(t->slots);
+        if (t->forest.level[b] < t->cfg.Jmax) ref.push_back(b);
+    const int nr = (int)ref.size();
+    if ((size_t)nr * nd > ctx->free_slots.size()) return fail(WG_ENOMEM, "refinement needs %d free slots", nr * nd);
+    const int nn = nb + nr * (nd - 1);
+    std::vector<int> lv, co, slots, child_base(nb, -1), parents, bases;
+    lv.reserve(nn);
+    co.reserve(3 * nn);
+    slots.reserve(nn);
     // daughters need consecutive slots: take them from the free list in runs
     std::vector<int> fs = ctx->free_slots;
     std::sort(fs.begin(), fs.end());
-    // consecutive run search
     std::vector<int> used;
     size_t i = 0;
-    for (int b = 0; b < nb; b++) {
+    for (int b : ref) {
         while (i + nd <= fs.size() && fs[i + nd - 1] - fs[i] != nd - 1) i++;
         if (i + nd > fs.size()) return fail(WG_ENOMEM, "no consecutive free slots for daughters");
         child_base[b] = fs[i];
         for (int k = 0; k < nd; k++) used.push_back(fs[i + k]);
         i += nd;
+        parents.push_back(t->slots[b]);
+        bases.push_back(fs[i - nd]);
     }
-    for (int b = 0; b < nb; b++)
-        for (int k = 0; k < nd; k++) {
-            const int c = b * nd + k;
-            lv[c] = t->forest.level[b] + 1;
-            co[3 * c + 0] = 2 * t->forest.coords[3 * b + 0] + (k / 2) % 2;
-            co[3 * c + 1] = 2 * t->forest.coords[3 * b + 1] + k % 2;
-            co[3 * c + 2] = dim == 3 ? 2 * t->forest.coords[3 * b + 2] + k / 4 : 0;
-            slots[c] = child_base[b] + k;
+    for (int b = 0; b < nb; b++) {
+        if (child_base[b] < 0) {   // stays on Jmax
+            lv.push_back(t->forest.level[b]);
+            for (int a = 0; a < 3; a++) co.push_back(t->forest.coords[3 * b + a]);
+            slots.push_back(t->slots[b]);
+            continue;
         }
-    DevArray<int> d_par, d_base;
-    WG_CUDA_OK(d_par.upload(parents.data(), nb, ctx->stream));
-    WG_CUDA_OK(d_base.upload(child_base.data(), nb, ctx->stream));
-    const int *Bs = ctx->cfg.Bs;
-    WG_CUDA_OK(launch_refine(dim, d_par.p, nb, d_base.p, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], ctx->geo.nc,
-                             ctx->wav.order_predictor, ctx->stream));
-    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-    // swap the tree onto the daughters
+        for (int k = 0; k < nd; k++) {
+            lv.push_back(t->forest.level[b] + 1);
+            co.push_back(2 * t->forest.coords[3 * b + 0] + (k / 2) % 2);
+            co.push_back(2 * t->forest.coords[3 * b + 1] + k % 2);
+            co.push_back(dim == 3 ? 2 * t->forest.coords[3 * b + 2] + k / 4 : 0);
+            slots.push_back(child_base[b] + k);
+        }
+    }
+    if (nr > 0) {
+        DevArray<int> d_par, d_base;
+        WG_CUDA_OK(d_par.upload(parents.data(), nr, ctx->stream));
+        WG_CUDA_OK(d_base.upload(bases.data(), nr, ctx->stream));
+        const int *Bs = ctx->cfg.Bs;
+        WG_CUDA_OK(launch_refine(dim, d_par.p, nr, d_base.p, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], ctx->geo.nc,
+                                 ctx->wav.order_predictor, ctx->stream));
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    }
+    // swap the tree onto the new blocks
     std::sort(used.begin(), used.end());
     std::vector<int> nf;
     nf.reserve(ctx->free_slots.size());
-    for (int s : ctx->free_slots)
-        if (!std::binary_search(used.begin(), used.end(), s)) nf.push_back(s);
-    for (int s : parents) nf.push_back(s);
+    for (int s2 : ctx->free_slots)
+        if (!std::binary_search(used.begin(), used.end(), s2)) nf.push_back(s2);
+    for (int s2 : parents) nf.push_back(s2);
     for (int m : t->mask_slot)
         if (m >= 0) ctx->mask_free.push_back(m);
     ctx->free_slots = nf;
     t->slots = slots;
-    t->mask_slot.assign(nb * nd, -1);
+    t->mask_slot.assign(nn, -1);
     t->shadow_valid = false;
     t->sync.clear();
-    t->forest.set(nb * nd, lv.data(), co.data());
+    t->forest.set(nn, lv.data(), co.data());
     std::string err;
     if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "%s", err.c_str());
     int st;
