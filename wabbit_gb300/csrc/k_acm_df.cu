@@ -85,33 +85,63 @@ __device__ __forceinline__ void push_ghosts(const int *push, int b, int ix, int 
     }
 }
 
+// The per-block and per-tree constants of a stage, loaded once per thread:
+// stencil weights (BlockDesc), physics (TreeParams) and the RK weights of the
+// stage from the tree's clock.
+struct DfConst {
+    df2 s1[3], s2[3], sc;      // 1/(12 dx), nu/(12 dx^2), -30 sum s2
+    df2 c0sq, gamma, umean[3];
+    df2 db, da;                // dt * b_j, dt * a_(j+1) of the stage
+    int sponge;
+};
+
+__device__ __forceinline__ DfConst load_const(const StageArgsDF &a, const BlockDesc &d) {
+    DfConst k;
+    const TreeParams &tp = a.tp[d.tree];
+    const TreeClock &ck = a.clk[d.tree];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        k.s1[i] = cf(d.fs1[i]);
+        k.s2[i] = cf(d.fs2[i]);
+        k.umean[i] = cf(tp.f_umean[i]);
+    }
+    k.sc = cf(d.fsc);
+    k.c0sq = cf(tp.f_c0sq);
+    k.gamma = cf(tp.f_gamma);
+    k.sponge = tp.use_sponge;
+    const int j = a.stage;
+    k.db = (j == 1 || j == 4) ? cf(ck.f_dt6) : cf(ck.f_dt3);
+    k.da = j == 3 ? cf(ck.f_dt) : df_pow2(cf(ck.f_dt), 0.5f);
+    return k;
+}
+
 // RHS of one interior point from a stencil input with strides stv (shared or
 // global memory). m: the point's double-float mask words (stride ms), or
 // null. Returns the RHS in r and the centre values vel, p0.
 template <int DIM, bool MASK, typename Idx>
-__device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3], const BlockDesc &d,
-                                       const TreeParams &tp, const float2 *m, int ms, df2 r[DIM + 1], df2 vel[DIM],
+__device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3], const DfConst &d,
+                                       const float2 *m, int ms, df2 r[DIM + 1], df2 vel[DIM],
                                        df2 &p0) {
     df2 w[DIM];
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
         vel[k] = ld(u + k * cs);
-        w[k] = df_mul_nr(vel[k], cf(d.fs1[k]));            // u_k / (12 dx_k)
+        w[k] = df_mul_nr(vel[k], d.s1[k]);                 // u_k / (12 dx_k)
     }
     df2 div = {0.f, 0.f};
 #pragma unroll
     for (int c = 0; c < DIM; c++) {
         const float2 *uc = u + c * cs;
         df2 adv = {0.f, 0.f};
-        df2 lap = df_mul_nr(cf(d.fsc), vel[c]);           // -30 u sum nu/(12 dx^2)
+        df2 lap = df_mul_nr(d.sc, vel[c]);                // -30 u sum nu/(12 dx^2)
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
             const df2 A = ld(uc + stv[k]), B = ld(uc - stv[k]), E = ld(uc + 2 * stv[k]), F = ld(uc - 2 * stv[k]);
             const df2 d1 = df_sub_nr(df_pow2(df_sub_nr(A, B), 8.f), df_sub_nr(E, F));
             adv = df_add_nr(adv, df_mul_nr(w[k], d1));
-            if (k == c) div = df_add_nr(div, df_mul_nr(cf(d.fs1[k]), d1));
+            if (k == c) div = df_add_nr(div, df_mul_nr(d.s1[k], d1));
             const df2 l = df_sub_nr(df_pow2(df_add_nr(A, B), 16.f), df_add_nr(E, F));
-            lap = df_add_nr(lap, df_mul_nr(cf(d.fs2[k]), l));
+            lap = df_add_nr(lap, df_mul_nr(d.s2[k], l));
         }
         r[c] = df_sub_nr(lap, adv);
     }
@@ -121,18 +151,18 @@ __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3]
     for (int k = 0; k < DIM; k++) {
         const df2 A = ld(up + stv[k]), B = ld(up - stv[k]), E = ld(up + 2 * stv[k]), F = ld(up - 2 * stv[k]);
         const df2 d1 = df_sub_nr(df_pow2(df_sub_nr(A, B), 8.f), df_sub_nr(E, F));
-        r[k] = df_sub_nr(r[k], df_mul_nr(cf(d.fs1[k]), d1));
+        r[k] = df_sub_nr(r[k], df_mul_nr(d.s1[k], d1));
     }
-    r[DIM] = df_neg(df_add_nr(df_mul_nr(cf(tp.f_c0sq), div), df_mul_nr(cf(tp.f_gamma), p0)));
+    r[DIM] = df_neg(df_add_nr(df_mul_nr(d.c0sq, div), df_mul_nr(d.gamma, p0)));
     if (MASK) {
         const df2 chi = ld(m);
 #pragma unroll
         for (int c = 0; c < DIM; c++) r[c] = df_sub_nr(r[c], df_mul_nr(chi, df_sub_nr(vel[c], ld(m + (1 + c) * ms))));
-        if (tp.use_sponge) {
+        if (d.sponge) {
             const df2 spo = ld(m + 4 * ms);
 #pragma unroll
             for (int c = 0; c < DIM; c++)
-                r[c] = df_sub_nr(r[c], df_mul_nr(spo, df_sub_nr(vel[c], cf(tp.f_umean[c]))));
+                r[c] = df_sub_nr(r[c], df_mul_nr(spo, df_sub_nr(vel[c], d.umean[c])));
             r[DIM] = df_sub_nr(r[DIM], df_mul_nr(spo, p0));
         }
     }
@@ -183,18 +213,17 @@ __device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int q, int 
 // u_n + dt k3. q: interior index; (ix, iy, iz): interior coordinates; off:
 // the point's offset in the thin buffers (component 0).
 template <int DIM>
-__device__ __forceinline__ void rk_df(const StageArgsDF &a, const BlockDesc &d, int b, int q, int ix, int iy, int iz,
+__device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, int b, int q, int ix, int iy, int iz,
                                       long long off, const df2 r[DIM + 1], const RkIn<DIM> &in) {
     const int npts_int = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
     const long long cs = a.gt.npts();
-    const TreeClock &ck = a.clk[d.tree];
     const int j = a.stage;
-    const df2 db = (j == 1 || j == 4) ? cf(ck.f_dt6) : cf(ck.f_dt3);
+    const df2 db = k.db;
     float2 *acc = a.acc + (long long)b * (DIM + 1) * npts_int + q;
     float2 *o = a.out + off;
     float2 ov[DIM + 1];
     if (j < 4) {
-        const df2 da = j == 3 ? cf(ck.f_dt) : df_pow2(cf(ck.f_dt), 0.5f);
+        const df2 da = k.da;
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
             const df2 rc = df_norm(r[c]);
@@ -243,10 +272,11 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
     const int stv[3] = {1, a.gt.nx, a.gt.nx * a.gt.ny};
     const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
     df2 r[DIM + 1], vel[DIM], p0;
-    rhs_df<DIM, MASK>(a.in + off, cs, stv, d, a.tp[d.tree], m, npts_int, r, vel, p0);
+    const DfConst k = load_const(a, d);
+    rhs_df<DIM, MASK>(a.in + off, cs, stv, k, m, npts_int, r, vel, p0);
     RkIn<DIM> in;
     rk_load<DIM>(a, b, q, ix, iy, iz, off, in);
-    rk_df<DIM>(a, d, b, q, ix, iy, iz, off, r, in);
+    rk_df<DIM>(a, k, b, q, ix, iy, iz, off, r, in);
 }
 
 // 3-D blocks of 16x16xBs2 points with 2 ghost layers (the stage-input
@@ -276,7 +306,7 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
     }
     __syncthreads();   // the barrier is initialised before anyone waits on it
     const BlockDesc &d = a.desc[b];
-    const TreeParams &tp = a.tp[d.tree];
+    const DfConst kc = load_const(a, d);
     const int ix = threadIdx.x % BS, iy = threadIdx.x / BS;
     const int npts_int = BS * BS * a.Bs2;
     constexpr int stv[3] = {1, NX, PLANE};
@@ -299,8 +329,8 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
         const float2 *u = sm + ((k + 2) * NY + (iy + GB)) * NX + (ix + GB);
         const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
         df2 r[4], vel[3], p0;
-        rhs_df<3, MASK>(u, COMP, stv, d, tp, m, npts_int, r, vel, p0);
-        rk_df<3>(a, d, b, q, ix, iy, iz, off, r, cur);
+        rhs_df<3, MASK>(u, COMP, stv, kc, m, npts_int, r, vel, p0);
+        rk_df<3>(a, kc, b, q, ix, iy, iz, off, r, cur);
     }
 }
 
