@@ -71,6 +71,15 @@ struct DevArray {
     }
 };
 
+// Prediction patches of the stages of a table, sorted within each stage by
+// the shared memory the CTA-per-patch kernel needs and cut into classes;
+// each class launches with its own largest need.
+struct PredClasses {
+    DevArray<Patch> patches;                 // sorted copy
+    std::vector<std::vector<int>> begin;     // per stage: class offsets into patches (n_class+1)
+    std::vector<std::vector<int>> need;      // per stage and class: largest need in doubles per component
+};
+
 struct SyncPlan {
     SyncTable table;
     DevArray<Patch> d;
@@ -80,6 +89,9 @@ struct SyncPlan {
     DevArray<uint2> pairs;             // (receiver, sender) offsets, all stages
     std::vector<unsigned> pair_begin;  // nstages+1 offsets into pairs
     std::vector<unsigned> copy_end;    // per stage: end of its copy entries
+    // prediction stages split into classes of similar shared-memory need
+    // (patches sorted by need), so that small patches launch small CTAs
+    PredClasses pcls;
     // every copy patch is a same-level translation of a full ghost region:
     // the stage kernels may write these ghost nodes themselves (ctx->d_push)
     bool push_ok = false;
@@ -100,6 +112,7 @@ struct BatchPlan {
     std::vector<unsigned> pair_begin, copy_end;
     DevArray<Patch> predict;            // per stage: prediction patches of all trees
     std::vector<int> pred_begin;
+    PredClasses pcls;                   // prediction patches by shared-memory class
     int max_coarse = 0;
     bool push = false;                  // every tree's copies are pushed by the stage kernels
 };
@@ -231,6 +244,65 @@ Tree *get_tree(wg_ctx *ctx, int t) {
 
 long long sync_key(int gm, int gp, int thin) { return ((long long)gm << 20) | ((long long)gp << 4) | thin; }
 
+// shared memory (doubles per component) of a prediction patch in the
+// CTA-per-patch kernel: coarse box, x window and x-y window
+static int pred_need(const Patch &p, int order_predictor) {
+    const int h = order_predictor - 1;
+    const int cx = p.shi[0] - p.slo[0] + 1, cy = p.shi[1] - p.slo[1] + 1, cz = p.shi[2] - p.slo[2] + 1;
+    const int Fy = 2 * cy - 1, Fz = 2 * cz - 1;
+    const int ex = p.rhi[0] - p.rlo[0] + 1, ey = p.rhi[1] - p.rlo[1] + 1, ez = p.rhi[2] - p.rlo[2] + 1;
+    int yw0 = std::max(0, p.blo[1] - h), yw1 = std::min(Fy - 1, p.blo[1] + ey - 1 + h);
+    yw0 += yw0 & 1;
+    yw1 -= yw1 & 1;
+    int zw0 = std::max(0, p.blo[2] - h), zw1 = std::min(Fz - 1, p.blo[2] + ez - 1 + h);
+    zw0 += zw0 & 1;
+    zw1 -= zw1 & 1;
+    const int ny = (yw1 - yw0) / 2 + 1, nz = (zw1 - zw0) / 2 + 1;
+    return cx * cy * cz + ex * ny * nz + ex * ey * nz;
+}
+
+int build_pred_classes(wg_ctx *ctx, const std::vector<Patch> &pt, const std::vector<int> &stage_begin,
+                       const std::vector<int> &stage_predict, PredClasses &pc) {
+    const int ns = (int)stage_predict.size();
+    std::vector<Patch> sorted;
+    pc.begin.assign(ns, {});
+    pc.need.assign(ns, {});
+    for (int st = 0; st < ns; st++) {
+        if (!stage_predict[st]) continue;
+        std::vector<std::pair<int, int>> byneed;
+        for (int i = stage_begin[st]; i < stage_begin[st + 1]; i++)
+            byneed.push_back({pred_need(pt[i], ctx->wav.order_predictor), i});
+        std::stable_sort(byneed.begin(), byneed.end());
+        // classes: a class grows while its largest need stays within twice
+        // its smallest
+        const int base = (int)sorted.size();
+        pc.begin[st].push_back(base);
+        int lo_need = byneed.empty() ? 0 : byneed[0].first;
+        for (size_t k = 0; k < byneed.size(); k++) {
+            if (byneed[k].first > 2 * lo_need && k > 0) {
+                pc.need[st].push_back(byneed[k - 1].first);
+                pc.begin[st].push_back(base + (int)k);
+                lo_need = byneed[k].first;
+            }
+            sorted.push_back(pt[byneed[k].second]);
+        }
+        if (!byneed.empty()) {
+            pc.need[st].push_back(byneed.back().first);
+            pc.begin[st].push_back(base + (int)byneed.size());
+        }
+    }
+    WG_CUDA_OK(pc.patches.upload(sorted.data(), sorted.size(), ctx->stream));
+    return WG_OK;
+}
+
+int run_pred_classes(wg_ctx *ctx, const PredClasses &pc, int st, double *buf, const BufGeo &geo) {
+    const std::vector<int> &b = pc.begin[st];
+    for (size_t k = 0; k + 1 < b.size(); k++)
+        WG_CUDA_OK(launch_predict_df(pc.patches.p + b[k], b[k + 1] - b[k], pc.need[st][k], buf, geo, ctx->geo.nc,
+                                     ctx->wav.order_predictor, ctx->stream));
+    return WG_OK;
+}
+
 // Check that every copy patch of a thin per-step plan is a same-level
 // translation of a full ghost region (the form push_ghosts writes) and, if
 // so, record per sender slot the receiver slot of each direction.
@@ -323,6 +395,10 @@ int get_sync(wg_ctx *ctx, Tree &t, int gm, int gp, bool thin, SyncPlan **out) {
             }
             order_begin[tb.nstages] = (int)order.size();
             sp->pair_begin[tb.nstages] = (unsigned)run;
+            {
+                int st2 = build_pred_classes(ctx, tb.patches, tb.stage_begin, tb.stage_predict, sp->pcls);
+                if (st2) return st2;
+            }
             if (run < (1ull << 32)) {
                 WG_CUDA_OK(sp->order.upload(order.data(), order.size(), ctx->stream));
                 WG_CUDA_OK(sp->first.upload(first.data(), first.size(), ctx->stream));
@@ -360,7 +436,10 @@ int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool 
         const int b = sp->table.stage_begin[s], e = sp->table.stage_begin[s + 1];
         // copies and decimations move 8-byte elements: the same kernel serves
         // FP64 and double-float buffers; predictions convert
-        if (sp->table.stage_predict[s] && df)
+        if (sp->table.stage_predict[s] && df && !sp->pcls.begin.empty()) {
+            int st3 = run_pred_classes(ctx, sp->pcls, s, buf, geo);
+            if (st3) return st3;
+        } else if (sp->table.stage_predict[s] && df)
             WG_CUDA_OK(launch_predict_df(sp->d.p + b, e - b, sp->table.max_coarse, buf, geo, ctx->geo.nc,
                                          ctx->wav.order_predictor, ctx->stream));
         else if (sp->table.stage_predict[s])
@@ -651,6 +730,12 @@ int build_batch(wg_ctx *ctx, const std::vector<int> &trees) {
     if (total >= (1ull << 32)) return fail(WG_ENOTSUP, "batched ghost gather exceeds 2^32 entries");
     WG_CUDA_OK(bp.pairs.upload(nullptr, total, ctx->stream));
     WG_CUDA_OK(bp.predict.upload(pred.data(), pred.size(), ctx->stream));
+    {
+        std::vector<int> sp_pred(ns, 0);
+        for (int st = 0; st < ns; st++) sp_pred[st] = bp.stage_predict[st];
+        int st2 = build_pred_classes(ctx, pred, bp.pred_begin, sp_pred, bp.pcls);
+        if (st2) return st2;
+    }
     for (int st = 0; st < ns; st++) {
         unsigned at = bp.pair_begin[st];
         for (int pass = 0; pass < 2; pass++) {          // copies of every tree first
@@ -676,9 +761,8 @@ int run_sync_batch(wg_ctx *ctx, double *buf) {
     const BatchPlan &bp = ctx->batch;
     for (int s = 0; s < bp.nstages; s++) {
         if (bp.stage_predict[s]) {
-            WG_CUDA_OK(launch_predict_df(bp.predict.p + bp.pred_begin[s], bp.pred_begin[s + 1] - bp.pred_begin[s],
-                                         bp.max_coarse, buf, ctx->gT, ctx->geo.nc, ctx->wav.order_predictor,
-                                         ctx->stream));
+            int st3 = run_pred_classes(ctx, bp.pcls, s, buf, ctx->gT);
+            if (st3) return st3;
         } else {
             const unsigned from = bp.push ? bp.copy_end[s] : bp.pair_begin[s];
             WG_CUDA_OK(launch_gather(bp.pairs.p + from, bp.pair_begin[s + 1] - from, buf, ctx->gT, ctx->geo.nc,

@@ -314,19 +314,22 @@ cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_dou
     const int cg = (int)std::min<size_t>((size_t)nc, limit / per);
     const size_t smem = per * cg;
     float2 *b = reinterpret_cast<float2 *>(buf);
-    auto go = [&](auto kern) -> cudaError_t {
-        if (smem > 48 * 1024) {
+    // the attribute only grows, so launches captured earlier stay valid
+    static size_t attr[4] = {0, 0, 0, 0};
+    auto go = [&](auto kern, int k) -> cudaError_t {
+        if (smem > 48 * 1024 && smem > attr[k]) {
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
+            attr[k] = smem;
         }
         kern<<<npatch, 256, smem, s>>>(patches, b, geo, nc, cg);
         return cudaGetLastError();
     };
     switch (order_predictor) {
-        case 2: return go(predict_df_kernel<2>);
-        case 4: return go(predict_df_kernel<4>);
-        case 6: return go(predict_df_kernel<6>);
-        case 8: return go(predict_df_kernel<8>);
+        case 2: return go(predict_df_kernel<2>, 0);
+        case 4: return go(predict_df_kernel<4>, 1);
+        case 6: return go(predict_df_kernel<6>, 2);
+        case 8: return go(predict_df_kernel<8>, 3);
         default: return cudaErrorInvalidValue;
     }
 }
