@@ -59,6 +59,7 @@ def lib():
         L.or_wc_threshold.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.or_refine_everywhere.argtypes = [ctypes.c_void_p]
         L.or_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _dp]
+        L.or_adapt_full_tree.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.or_run.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
         _lib = L
     return _lib
@@ -194,8 +195,9 @@ class Oracle:
         return out
 
     def adapt(self, eps_use=None, everywhere=False):
-        """adapt_tree for CDF X0 (threshold-state-vector or everywhere);
-        returns the new block count."""
+        """adapt_tree (threshold-state-vector or everywhere); CDF X0 by
+        decimation, CDF XY through the full tree with coarse extension and
+        security zone; returns the new block count."""
         if everywhere:
             n = self.L.or_adapt(self.h, None, 1)
         else:
@@ -203,6 +205,18 @@ class Oracle:
             n = self.L.or_adapt(self.h, _p(e), 0)
         if n < 0:
             raise RuntimeError(f"or_adapt failed ({n})")
+        return n
+
+    def adapt_full_tree(self, eps_use=None, everywhere=False):
+        """adapt_tree through the full-tree path with coarse extension (the
+        lifted-wavelet algorithm; for CDF X0 it reduces to the plain one)."""
+        if everywhere:
+            n = self.L.or_adapt_full_tree(self.h, None, 1)
+        else:
+            e = np.ascontiguousarray(np.broadcast_to(np.asarray(eps_use, np.float64), (self.cfg.neq,)))
+            n = self.L.or_adapt_full_tree(self.h, _p(e), 0)
+        if n < 0:
+            raise RuntimeError(f"or_adapt_full_tree failed ({n})")
         return n
 
     def refine_everywhere(self):

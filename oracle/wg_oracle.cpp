@@ -58,6 +58,7 @@ struct Wavelet {
     Filter HD, GD, HR, GR;
     int order_predictor = 4;
     int Nscl = 0, Nscr = 0, Nwcl = 0, Nwcr = 0;
+    int Nreconl = 0, Nreconr = 0, Ndep2l = 0, Ndep2r = 0;
     std::string name;
 };
 
@@ -99,11 +100,21 @@ static bool setup_wavelet(const char *name, int fd_max_size, Wavelet &w) {
     // coarse-extension widths (module_wavelets.f90:1341-1375)
     w.Nscl = std::max(std::abs(w.HD.lo) - 1, 0);
     w.Nwcl = w.Nscl + std::abs(w.GD.lo);
+    w.Nreconl = w.Nwcl + std::abs(w.GR.lo);
+    w.Ndep2l = w.Nreconl + std::max((std::abs(w.HR.lo) + 1) / 2 - 1, 0);
     w.Nscr = w.HD.hi;
     w.Nwcr = w.Nscr + w.GD.hi;
+    w.Nreconr = w.Nwcr + w.GR.hi;
+    w.Ndep2r = w.Nreconr + (w.HR.hi + 1) / 2;
+    // minimum WC width from the FD stencils (module_wavelets.f90:1405-1417)
     int i2 = 2 * fd_max_size;
-    w.Nwcl += std::max(i2 - w.Nwcl, 0);
-    w.Nwcr += std::max(i2 - w.Nwcr, 0);
+    const int dl = std::max(i2 - w.Nwcl, 0), dr = std::max(i2 - w.Nwcr, 0);
+    w.Nwcl += dl;
+    w.Nreconl += dl;
+    w.Ndep2l += dl;
+    w.Nwcr += dr;
+    w.Nreconr += dr;
+    w.Ndep2r += dr;
     return true;
 }
 
@@ -128,6 +139,9 @@ struct Oracle {
     std::vector<double> mask;       // nblk * 6 * npts (optional)
     std::vector<int> nb;            // nblk * 168
     std::unordered_map<uint64_t, int> lookup;
+    // full-tree adaptation: hvy_tmp, refinement status, family
+    std::vector<double> tmp;
+    std::vector<int> ref, mother, dau;   // dau: 8 per block, -1 where absent
     // RK registers: slot 0 = u_n, 1..4 = k1..k4 (full blocks, as hvy_work)
     std::vector<double> work;
     int nthreads = 1;
@@ -169,7 +183,7 @@ static void adjacent(const int c[3], const int d[3], int level, int dim, int out
 }
 
 // find_neighbor (LIB/MESH/find_neighbors.f90:18-215) for one direction
-static void find_neighbor(Oracle &o, int ib, const int dir_dim[3]) {
+static void find_neighbor(Oracle &o, int ib, const int dir_dim[3], bool overlapping) {
     const int dim = o.cfg.dim;
     const Block &B = o.blocks[ib];
     const int level = B.level;
@@ -213,14 +227,20 @@ static void find_neighbor(Oracle &o, int ib, const int dir_dim[3]) {
 
     int *nbr = o.nb.data() + size_t(ib) * 168;
     int d[3] = {dir_dim[0], dir_dim[1], dim == 3 ? dir_dim[2] : 0};
-    int cn[3];
+    int cn[3] = {0, 0, 0};
+    // with overlapping (full-tree) search every existing same, finer and
+    // coarser neighbour is recorded
     if (level == 0) {
         nbr[same - 1] = ib;
-        return;
+        if (!overlapping) return;
+    } else {
+        adjacent(B.c, d, level, dim, cn);
+        int idn = find_block(o, level, cn);
+        if (idn >= 0) {
+            nbr[same - 1] = idn;
+            if (!overlapping) return;
+        }
     }
-    adjacent(B.c, d, level, dim, cn);
-    int idn = find_block(o, level, cn);
-    if (idn >= 0) { nbr[same - 1] = idn; return; }
     if (level < o.cfg.Jmax) {
         for (int k = 0; k < dir_free; k++) {
             int dig = tcFiner[k];
@@ -231,7 +251,7 @@ static void find_neighbor(Oracle &o, int ib, const int dir_dim[3]) {
             int idf = find_block(o, level + 1, cf);
             if (idf >= 0) nbr[same + k - 1 + 2 * 56] = idf;
             else break;
-            if (k == dir_free - 1) return;
+            if (!overlapping && k == dir_free - 1) return;
         }
     }
     if (coarser != -1 && level > o.cfg.Jmin) {
@@ -242,7 +262,7 @@ static void find_neighbor(Oracle &o, int ib, const int dir_dim[3]) {
     }
 }
 
-static void update_neighbors(Oracle &o) {
+static void update_neighbors(Oracle &o, bool overlapping = false) {
     rebuild_lookup(o);
     const int nb = (int)o.blocks.size();
     o.nb.assign(size_t(nb) * 168, -1);
@@ -253,7 +273,7 @@ static void update_neighbors(Oracle &o) {
                 for (int dx = -1; dx <= 1; dx++) {
                     if (dx == 0 && dy == 0 && dz == 0) continue;
                     int dd[3] = {dx, dy, dz};
-                    find_neighbor(o, ib, dd);
+                    find_neighbor(o, ib, dd, overlapping);
                 }
     }
 }
@@ -1323,6 +1343,739 @@ static int adapt_unlifted(Oracle &o, const double *eps_use, int everywhere) {
     return WG_OK;
 }
 
+// ===========================================================================
+// Full-tree adaptation with coarse extension (lifted wavelets, CDF XY with
+// Y > 0): adapt_tree (LIB/MESH/adapt_tree.f90:11-255) with
+// wavelet_decompose_full_tree (:264-523), init_full_tree (:995-1085),
+// wavelet_reconstruct_full_tree_CEoptimized (:686-987) and
+// prune_fulltree2leafs. The sync is sync_ghosts_generic
+// (LIB/MPI/synchronize_ghosts_generic.f90:181-343) with the single-rank send
+// logic of prepare_ghost_synch_metadata (:352-694) and the data source rules
+// of unpack_ghostlayers_internal (LIB/MPI/xfer_block_data.f90:321-437).
+// Blocks are visited in index order (the reference's results do not depend
+// on the block order, which varies with the MPI partition).
+// ===========================================================================
+constexpr int kRefTmpEmpty = 10;          // REF_TMP_EMPTY (module_globals.f90:25)
+constexpr int kRefUnsignificantStay = 9;  // REF_UNSIGNIFICANT_STAY (:28)
+
+// updateFamily_tree (LIB/MESH/updateFamily_tree.f90:16-56): mother below
+// Jmin is not searched, daughters above Jmax neither
+static void update_family(Oracle &o, int Jmin) {
+    const int n = (int)o.blocks.size(), dim = o.cfg.dim, nd = 1 << dim;
+    o.mother.assign(n, -1);
+    o.dau.assign(size_t(n) * 8, -1);
+    for (int b = 0; b < n; b++) {
+        const Block &B = o.blocks[b];
+        if (B.level != Jmin) {
+            const int c[3] = {B.c[0] >> 1, B.c[1] >> 1, dim == 3 ? B.c[2] >> 1 : 0};
+            o.mother[b] = find_block(o, B.level - 1, c);
+        }
+        if (B.level != o.cfg.Jmax)
+            for (int k = 0; k < nd; k++) {
+                const int c[3] = {2 * B.c[0] + (k & 1), 2 * B.c[1] + ((k >> 1) & 1), dim == 3 ? 2 * B.c[2] + ((k >> 2) & 1) : 0};
+                o.dau[size_t(b) * 8 + k] = find_block(o, B.level + 1, c);
+            }
+    }
+}
+
+// block_is_leaf / block_is_root / block_has_valid_neighbor
+// (LIB/MPI/block_relations.f90:2-71)
+static bool blk_is_leaf(const Oracle &o, int b, bool check_empty) {
+    bool leaf = true;
+    for (int k = 0; k < 8; k++)
+        if (o.dau[size_t(b) * 8 + k] >= 0) leaf = false;
+    if (leaf || !check_empty) return leaf;
+    for (int k = 0; k < 8; k++) {
+        const int d = o.dau[size_t(b) * 8 + k];
+        if (d >= 0 && o.ref[d] != kRefTmpEmpty) return false;
+    }
+    return true;
+}
+
+static bool blk_is_root(const Oracle &o, int b, bool check_empty) {
+    if (o.mother[b] < 0) return true;
+    return check_empty && o.ref[o.mother[b]] == kRefTmpEmpty;
+}
+
+// np_l / np_u (LIB/TREE/neighborhood.f90:439-500): the relations of the
+// same patch at another level difference
+static void patch_range(int relation, int lvl_diff, int &lo, int &hi) {
+    const int t = (relation - 1) % 56 + 1;
+    int pid;
+    if (t <= 24) pid = (t - 1) / 4 + 1;
+    else if (t <= 48) pid = (t - 25) / 2 + 1 + 6;
+    else pid = (t - 49) + 1 + 6 + 12;
+    if (pid <= 6) { lo = (pid - 1) * 4 + 1; hi = pid * 4; }
+    else if (pid <= 18) { lo = (pid - 7) * 2 + 25; hi = (pid - 6) * 2 + 24; }
+    else { lo = (pid - 19) + 49; hi = (pid - 18) + 48; }
+    const int off = lvl_diff == +1 ? 56 : lvl_diff == -1 ? 112 : 0;
+    lo += off;
+    hi += off;
+}
+
+static bool blk_has_valid_neighbor(const Oracle &o, int b, int relation, int lvl_diff) {
+    int lo, hi;
+    patch_range(relation, lvl_diff, lo, hi);
+    for (int r = lo; r <= hi; r++) {
+        const int n = o.nb[size_t(b) * 168 + r - 1];
+        if (n >= 0 && o.ref[n] != kRefTmpEmpty) return true;
+    }
+    return false;
+}
+
+// coarseExtensionManipulateSC_block (module_wavelets.f90:966-1028): copy the
+// SC of the patch next to a coarser neighbour from u_copy
+static void ce_copy_sc(const Oracle &o, double *wc, const double *u_copy, int relation) {
+    const int g = o.cfg.g, dim = o.cfg.dim;
+    const int N[3] = {o.nx, o.ny, o.nz};
+    const int Ns[3] = {o.wav.Nscl, o.wav.Nscl, o.wav.Nscl}, Ne[3] = {o.wav.Nscr, o.wav.Nscr, o.wav.Nscr};
+    const int gg[3] = {g, g, g};
+    int idx[2][3];
+    modify_patch(dim, relation, idx, N, Ns, Ne, gg, gg, +1);
+    int io[3] = {0, 0, 0};
+    for (int d = 0; d < dim; d++) io[d] = ((g + idx[0][d] + 1) % 2 + 2) % 2;
+    for (int c = 1; c <= o.nc; c++)
+        for (int k = idx[0][2] + io[2]; k <= idx[1][2]; k += 2)
+            for (int j = idx[0][1] + io[1]; j <= idx[1][1]; j += 2)
+                for (int i = idx[0][0] + io[0]; i <= idx[1][0]; i += 2) wc[o.at(i, j, k, c)] = u_copy[o.at(i, j, k, c)];
+}
+
+// coarseExtensionManipulateWC_block (module_wavelets.f90:877-962): zero the
+// WC inside the patch next to a coarser neighbour and in its ghost patch
+static void ce_clear_wc(const Oracle &o, double *wc, int relation) {
+    const int g = o.cfg.g, dim = o.cfg.dim;
+    const int N[3] = {o.nx, o.ny, o.nz};
+    const int Ns[3] = {o.wav.Nwcl, o.wav.Nwcl, o.wav.Nwcl}, Ne[3] = {o.wav.Nwcr, o.wav.Nwcr, o.wav.Nwcr};
+    const int gg[3] = {g, g, g};
+    for (int set = 1; set <= 2; set++) {
+        int idx[2][3];
+        if (set == 1) modify_patch(dim, relation, idx, N, Ns, Ne, gg, gg, +1);
+        else ghost_patch(o.cfg.Bs, g, dim, relation, idx, g, g, +1);
+        if (dim == 2) idx[0][2] = idx[1][2] = 1;
+        int io[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) io[d] = ((g + idx[0][d] + 1) % 2 + 2) % 2;
+        for (int c = 1; c <= o.nc; c++) {
+            for (int k = idx[0][2] + io[2]; k <= idx[1][2]; k += 2)
+                for (int j = idx[0][1] + io[1]; j <= idx[1][1]; j += 2)
+                    for (int i = idx[0][0] + 1 - io[0]; i <= idx[1][0]; i += 2) wc[o.at(i, j, k, c)] = 0.0;
+            for (int k = idx[0][2] + io[2]; k <= idx[1][2]; k += 2)
+                for (int j = idx[0][1] + 1 - io[1]; j <= idx[1][1]; j += 2)
+                    for (int i = idx[0][0]; i <= idx[1][0]; i++) wc[o.at(i, j, k, c)] = 0.0;
+            if (dim == 3)
+                for (int k = idx[0][2] + 1 - io[2]; k <= idx[1][2]; k += 2)
+                    for (int j = idx[0][1]; j <= idx[1][1]; j++)
+                        for (int i = idx[0][0]; i <= idx[1][0]; i++) wc[o.at(i, j, k, c)] = 0.0;
+        }
+    }
+}
+
+// blockFilterXYZ_vct with do_restriction (module_wavelets.f90:307-401):
+// x pass on every second interior point over the rows the later passes
+// read, then y, then z; every sum starts from 0 and runs over all taps
+static void block_filter_restrict(const Oracle &o, const double *u, std::vector<double> &out) {
+    const Filter &F = o.wav.HD;
+    out.assign(u, u + size_t(o.nc) * o.npts);
+    if (F.lo == 0 && F.hi == 0 && std::fabs(F(0) - 1.0) <= 1.0e-10) return;
+    const int g = o.cfg.g, dim = o.cfg.dim;
+    int ifs[3], ife[3], ils[3], ile[3];
+    for (int d = 0; d < 3; d++) {
+        ifs[d] = g + 1 + F.lo;
+        ife[d] = o.cfg.Bs[d] + g + F.hi;
+        ils[d] = g + 1;
+        ile[d] = o.cfg.Bs[d] + g;
+    }
+    if (dim == 2) ifs[2] = ife[2] = ils[2] = ile[2] = 1;
+    std::vector<double> t(o.npts);
+    for (int c = 1; c <= o.nc; c++) {
+        double *uf = out.data() + size_t(c - 1) * o.npts;
+        auto T = [&](int i, int j, int k) { return t[((size_t)(k - 1) * o.ny + (j - 1)) * o.nx + (i - 1)]; };
+        auto UF = [&](int i, int j, int k) -> double & { return uf[((size_t)(k - 1) * o.ny + (j - 1)) * o.nx + (i - 1)]; };
+        std::copy(uf, uf + o.npts, t.begin());
+        for (int k = ifs[2]; k <= ife[2]; k++)
+            for (int j = ifs[1]; j <= ife[1]; j++)
+                for (int i = ils[0]; i <= ile[0]; i += 2) {
+                    double s = 0.0;
+                    for (int m = F.lo; m <= F.hi; m++) s = s + T(i + m, j, k) * F(m);
+                    UF(i, j, k) = s;
+                }
+        std::copy(uf, uf + o.npts, t.begin());
+        for (int k = ifs[2]; k <= ife[2]; k++)
+            for (int j = ils[1]; j <= ile[1]; j += 2)
+                for (int i = ils[0]; i <= ile[0]; i += 2) {
+                    double s = 0.0;
+                    for (int m = F.lo; m <= F.hi; m++) s = s + T(i, j + m, k) * F(m);
+                    UF(i, j, k) = s;
+                }
+        if (dim == 3) {
+            std::copy(uf, uf + o.npts, t.begin());
+            for (int k = ils[2]; k <= ile[2]; k += 2)
+                for (int j = ils[1]; j <= ile[1]; j += 2)
+                    for (int i = ils[0]; i <= ile[0]; i += 2) {
+                        double s = 0.0;
+                        for (int m = F.lo; m <= F.hi; m++) s = s + T(i, j, k + m) * F(m);
+                        UF(i, j, k) = s;
+                    }
+        }
+    }
+}
+
+// restrict_copy_at_CE (LIB/MPI/restrict_predict_data.f90:121-170): filtered
+// block, with the SC next to a coarser or finer neighbour copied back for a
+// leaf without a same-level neighbour on that patch
+static void restrict_copy_at_ce(const Oracle &o, const double *src, int b, std::vector<double> &out) {
+    block_filter_restrict(o, src, out);
+    const int lvl = o.blocks[b].level;
+    for (int r = 1; r <= 168; r++) {
+        const int n = o.nb[size_t(b) * 168 + r - 1];
+        if (n < 0) continue;
+        const int ld = lvl - o.blocks[n].level;
+        if ((ld == -1 || ld == 1) && blk_is_leaf(o, b, false) && !blk_has_valid_neighbor(o, b, r, 0))
+            ce_copy_sc(o, out.data(), src, r);
+    }
+}
+
+enum { kSyncFull = 1, kSyncFullLeaf = 2, kSyncMoC = 3, kSyncMoF = 4, kSyncMonly = 5 };
+enum { kTmpNone = 0, kTmpNotFlag = 1, kTmpDecomposed = 2 };
+
+struct SyncSpec {
+    int base = kSyncFull;
+    bool by_ref = false, by_level = false;
+    int s_ref = 0, s_level = 0;
+    int gminus = 0, gplus = 0;
+    int tmp_usage = kTmpNone;
+    bool ignore_filter = false;
+};
+
+static void sync_generic(Oracle &o, const SyncSpec &sp) {
+    const wg_config &cfg = o.cfg;
+    const int dim = cfg.dim;
+    const int nstages = o.wav.lifted ? 3 : 2, isUnl = o.wav.lifted ? 0 : 1;
+    const int nblk = (int)o.blocks.size();
+    std::vector<double> coarse, fine, filtered;
+    int filtered_id = -1;   // restricted_hvy_ID, reset once per sync
+    for (int istage = 1; istage <= nstages; istage++) {
+        for (int ib = 0; ib < nblk; ib++) {
+            if (sp.base == kSyncFullLeaf && !blk_is_leaf(o, ib, false)) continue;
+            if (o.ref[ib] == kRefTmpEmpty) continue;
+            const int level = o.blocks[ib].level;
+            for (int i_n = 1; i_n <= 168; i_n++) {
+                const int in = o.nb[size_t(ib) * 168 + i_n - 1];
+                if (in < 0) continue;
+                const int lvl_diff = level - o.blocks[in].level;
+                const int ref_n = o.ref[in];
+                if (ref_n == kRefTmpEmpty) continue;
+                const bool s1 = istage == 1 && lvl_diff == 0;
+                const bool s2 = istage == 2 - isUnl && lvl_diff == +1;
+                const bool s3 = istage == 3 - isUnl && lvl_diff == -1;
+                bool send = false;
+                switch (sp.base) {
+                case kSyncFull:
+                    if (s1 || s2 || s3) {
+                        send = true;
+                        if (lvl_diff == -1 && !blk_is_leaf(o, ib, true)) send = false;
+                        if (lvl_diff == +1 && !blk_is_root(o, ib, true)) send = false;
+                    }
+                    break;
+                case kSyncFullLeaf:
+                    if (s1 || s2 || s3) {
+                        send = true;
+                        if (lvl_diff >= 0 && blk_has_valid_neighbor(o, ib, i_n, -1)) send = false;
+                        else if (lvl_diff == +1 && blk_has_valid_neighbor(o, ib, i_n, 0)) send = false;
+                    }
+                    break;
+                case kSyncMoC:
+                    if (s1 || s3) {
+                        send = true;
+                        if (lvl_diff != 0 && !blk_is_leaf(o, ib, true)) send = false;
+                    }
+                    break;
+                case kSyncMoF:
+                    if (s1 || s2) {
+                        send = true;
+                        if (lvl_diff != 0 && !blk_is_root(o, ib, true)) send = false;
+                    }
+                    break;
+                default:
+                    send = s1;
+                }
+                if (send && sp.by_ref) send = sp.s_ref == ref_n;
+                if (send && sp.by_level) send = sp.s_level == o.blocks[in].level;
+                if (!send) continue;
+                // data source of the sender (hvy_tmp_usage)
+                bool tmp_rp = false, tmp_same = false;
+                if (sp.tmp_usage == kTmpNotFlag && o.ref[ib] != sp.s_ref) tmp_rp = tmp_same = true;
+                if (sp.tmp_usage == kTmpDecomposed) tmp_rp = true;
+                const int inv = inverse_relation(i_n);
+                int recv[2][3], sb[2][3], buf[2][3];
+                ghost_patch(cfg.Bs, cfg.g, dim, inv, recv, sp.gminus, sp.gplus, -lvl_diff);
+                send_bounds(cfg, o.wav.order_predictor, i_n, lvl_diff, sp.gminus, sp.gplus, sb, buf);
+                double *dst = o.blk(in);
+                if (lvl_diff == 0) {
+                    const double *src = (tmp_same ? o.tmp.data() : o.data.data()) + size_t(ib) * o.nc * o.npts;
+                    for (int c = 1; c <= o.nc; c++)
+                        for (int k = recv[0][2], ks = sb[0][2]; k <= recv[1][2]; k++, ks++)
+                            for (int j = recv[0][1], js = sb[0][1]; j <= recv[1][1]; j++, js++)
+                                for (int i = recv[0][0], is = sb[0][0]; i <= recv[1][0]; i++, is++)
+                                    dst[o.at(i, j, k, c)] = src[o.at(is, js, ks, c)];
+                    continue;
+                }
+                const double *src = (tmp_rp ? o.tmp.data() : o.data.data()) + size_t(ib) * o.nc * o.npts;
+                if (lvl_diff == +1) {
+                    const double *srcf = src;
+                    if (!sp.ignore_filter) {
+                        if (filtered_id != ib) {
+                            restrict_copy_at_ce(o, src, ib, filtered);
+                            filtered_id = ib;
+                        }
+                        srcf = filtered.data();
+                    }
+                    for (int c = 1; c <= o.nc; c++)
+                        for (int k = recv[0][2], kb = buf[0][2]; k <= recv[1][2]; k++, kb++)
+                            for (int j = recv[0][1], jb = buf[0][1]; j <= recv[1][1]; j++, jb++)
+                                for (int i = recv[0][0], ib2 = buf[0][0]; i <= recv[1][0]; i++, ib2++) {
+                                    const int is = sb[0][0] + 2 * (ib2 - 1), js = sb[0][1] + 2 * (jb - 1);
+                                    const int ks = dim == 3 ? sb[0][2] + 2 * (kb - 1) : 1;
+                                    dst[o.at(i, j, k, c)] = srcf[o.at(is, js, ks, c)];
+                                }
+                } else {
+                    const int cx = sb[1][0] - sb[0][0] + 1, cy = sb[1][1] - sb[0][1] + 1, cz = sb[1][2] - sb[0][2] + 1;
+                    const int fx = 2 * cx - 1, fy = 2 * cy - 1;
+                    coarse.resize(size_t(cx) * cy * cz);
+                    fine.resize(size_t(fx) * fy * (2 * cz - 1));
+                    for (int c = 1; c <= o.nc; c++) {
+                        size_t q = 0;
+                        for (int k = sb[0][2]; k <= sb[1][2]; k++)
+                            for (int j = sb[0][1]; j <= sb[1][1]; j++)
+                                for (int i = sb[0][0]; i <= sb[1][0]; i++) coarse[q++] = src[o.at(i, j, k, c)];
+                        prediction(coarse.data(), cx, cy, cz, fine.data(), o.wav.order_predictor);
+                        for (int k = recv[0][2], kb = buf[0][2]; k <= recv[1][2]; k++, kb++)
+                            for (int j = recv[0][1], jb = buf[0][1]; j <= recv[1][1]; j++, jb++)
+                                for (int i = recv[0][0], ib2 = buf[0][0]; i <= recv[1][0]; i++, ib2++)
+                                    dst[o.at(i, j, k, c)] = fine[(size_t(kb - 1) * fy + (jb - 1)) * fx + (ib2 - 1)];
+                    }
+                }
+            }
+        }
+    }
+}
+
+// coarse_extension_modify (LIB/MPI/reconstruction_step.f90:3-100); case 0
+// tree, 1 level, 2 ref, 3 level_ref
+static void ce_modify(Oracle &o, int ce_case, int s_level, int s_ref, bool clear_wc, bool copy_sc) {
+    const int n = (int)o.blocks.size();
+    for (int b = 0; b < n; b++) {
+        const int lv = o.blocks[b].level;
+        if ((ce_case == 1 || ce_case == 3) && lv != s_level) continue;
+        if ((ce_case == 2 || ce_case == 3) && o.ref[b] != s_ref) continue;
+        if (!blk_is_leaf(o, b, false)) continue;
+        for (int r = 1; r <= 168; r++) {
+            const int nb = o.nb[size_t(b) * 168 + r - 1];
+            if (nb < 0) continue;
+            if (o.blocks[nb].level < lv &&
+                !(blk_has_valid_neighbor(o, b, r, 0) || blk_has_valid_neighbor(o, b, r, -1))) {
+                if (clear_wc) ce_clear_wc(o, o.blk(b), r);
+                if (copy_sc) ce_copy_sc(o, o.blk(b), o.tmp.data() + size_t(b) * o.nc * o.npts, r);
+            }
+        }
+    }
+}
+
+// sync_D2M for one level (LIB/MESH/executeCoarsening_tree.f90:125-227):
+// the SC of every daughter go to its quadrant of the mother's interior
+static void sync_d2m(Oracle &o, int level) {
+    const int dim = o.cfg.dim, g = o.cfg.g;
+    const int half[3] = {o.cfg.Bs[0] / 2, o.cfg.Bs[1] / 2, dim == 3 ? o.cfg.Bs[2] / 2 : 1};
+    for (int b = 0; b < (int)o.blocks.size(); b++) {
+        if (o.blocks[b].level != level || o.mother[b] < 0) continue;
+        const int m = o.mother[b];
+        const Block &d = o.blocks[b];
+        const int kx = d.c[0] & 1, ky = d.c[1] & 1, kz = dim == 3 ? (d.c[2] & 1) : 0;
+        for (int c = 1; c <= o.nc; c++)
+            for (int k = 0; k < half[2]; k++)
+                for (int j = 0; j < half[1]; j++)
+                    for (int i = 0; i < half[0]; i++) {
+                        const int mk = dim == 3 ? g + 1 + kz * half[2] + k : 1, sk = dim == 3 ? g + 1 + 2 * k : 1;
+                        o.blk(m)[o.at(g + 1 + kx * half[0] + i, g + 1 + ky * half[1] + j, mk, c)] =
+                            o.blk(b)[o.at(g + 1 + 2 * i, g + 1 + 2 * j, sk, c)];
+                    }
+    }
+}
+
+// coarseningIndicator_block on decomposed data (input_is_WD): max |WC| over
+// the interior per component, vector groups as threshold_block
+static int threshold_wd(const Oracle &o, int b, const double *eps_use) {
+    const wg_config &p = o.cfg;
+    const int g = p.g;
+    const int z1 = p.dim == 2 ? 1 : g + 1, z2 = p.dim == 2 ? 1 : p.Bs[2] + g;
+    double compv[8] = {0, 0, 0, 0, 0, 0, 0, 0}, detail[8];
+    for (int c = 1; c <= o.nc; c++) {
+        const double *u = o.blk(b);
+        double m = 0.0;
+        bool any = false;
+        for (int k = z1; k <= z2; k++)
+            for (int j = g + 1; j <= p.Bs[1] + g; j++)
+                for (int i = g + 1; i <= p.Bs[0] + g; i++) {
+                    const bool sc = ((i - g - 1) % 2 == 0) && ((j - g - 1) % 2 == 0) && (p.dim == 2 || (k - g - 1) % 2 == 0);
+                    const double v = sc ? 0.0 : std::fabs(u[o.at(i, j, k, c)]);
+                    if (!any || v > m) { m = v; any = true; }
+                }
+        compv[c - 1] = m;
+    }
+    int maxgrp = 0;
+    for (int c = 0; c < o.nc; c++) maxgrp = std::max(maxgrp, p.threshold_state_vector_component[c]);
+    for (int c = 0; c < o.nc; c++) detail[c] = -1.0;
+    for (int l = 2; l <= maxgrp; l++) {
+        double m = 0.0;
+        for (int c = 0; c < o.nc; c++) if (p.threshold_state_vector_component[c] == l) m = std::max(m, compv[c]);
+        for (int c = 0; c < o.nc; c++) if (p.threshold_state_vector_component[c] == l) detail[c] = m;
+    }
+    for (int c = 0; c < o.nc; c++) {
+        if (p.threshold_state_vector_component[c] == 1) detail[c] = compv[c];
+        if (p.threshold_state_vector_component[c] == 0) detail[c] = 0.0;
+    }
+    for (int c = 0; c < o.nc; c++)
+        if (!(detail[c] <= eps_use[c])) return 0;
+    return -1;
+}
+
+// threshold_block on a patch of decomposed data (input_is_WD, Linfty): SC
+// of the patch zeroed by parity, max |WC| per component and vector group;
+// true if any component is significant
+static bool patch_significant(const Oracle &o, int b, const int idx[2][3], const double *eps_use) {
+    const wg_config &p = o.cfg;
+    const int g = p.g;
+    int io[3] = {0, 0, 0};
+    for (int d = 0; d < p.dim; d++) io[d] = ((g + idx[0][d] + 1) % 2 + 2) % 2;
+    double compv[8] = {0, 0, 0, 0, 0, 0, 0, 0}, detail[8];
+    for (int c = 1; c <= o.nc; c++) {
+        double m = 0.0;
+        bool any = false;
+        for (int k = idx[0][2]; k <= idx[1][2]; k++)
+            for (int j = idx[0][1]; j <= idx[1][1]; j++)
+                for (int i = idx[0][0]; i <= idx[1][0]; i++) {
+                    const bool sc = ((i - idx[0][0] - io[0]) % 2 == 0) && ((j - idx[0][1] - io[1]) % 2 == 0) &&
+                                    (p.dim == 2 || (k - idx[0][2] - io[2]) % 2 == 0);
+                    const double v = sc ? 0.0 : std::fabs(o.blk(b)[o.at(i, j, k, c)]);
+                    if (!any || v > m) { m = v; any = true; }
+                }
+        compv[c - 1] = m;
+    }
+    int maxgrp = 0;
+    for (int c = 0; c < o.nc; c++) maxgrp = std::max(maxgrp, p.threshold_state_vector_component[c]);
+    for (int c = 0; c < o.nc; c++) detail[c] = -1.0;
+    for (int l = 2; l <= maxgrp; l++) {
+        double m = 0.0;
+        for (int c = 0; c < o.nc; c++) if (p.threshold_state_vector_component[c] == l) m = std::max(m, compv[c]);
+        for (int c = 0; c < o.nc; c++) if (p.threshold_state_vector_component[c] == l) detail[c] = m;
+    }
+    for (int c = 0; c < o.nc; c++) {
+        if (p.threshold_state_vector_component[c] == 1) detail[c] = compv[c];
+        if (p.threshold_state_vector_component[c] == 0) detail[c] = 0.0;
+    }
+    for (int c = 0; c < o.nc; c++)
+        if (!(detail[c] <= eps_use[c])) return true;
+    return false;
+}
+
+// neighborhood2patchID (LIB/TREE/neighborhood.f90:413-434)
+static int patch_id(int relation) {
+    const int t = (relation - 1) % 56 + 1;
+    if (t <= 24) return (t - 1) / 4 + 1;
+    if (t <= 48) return (t - 25) / 2 + 1 + 6;
+    return (t - 49) + 1 + 6 + 12;
+}
+
+// addSecurityZone_CE_tree (LIB/MESH/securityZone_tree.f90:140-306): a block
+// that stays marks each same-level neighbour that wants to coarsen and whose
+// adjoining patch (Nwcl / Nwcr wide) holds significant details; the marked
+// neighbours stay. The marks are encoded in the status as bit patchID+3 plus
+// the flag bit 30, as lgt_encode_significant_patch (:308-340) does.
+static void security_zone(Oracle &o, const double *eps_use) {
+    constexpr int kTmpStatus = 17;
+    const int n = (int)o.blocks.size(), g = o.cfg.g, dim = o.cfg.dim;
+    const int N[3] = {o.nx, o.ny, o.nz};
+    const int Ns[3] = {o.wav.Nwcl, o.wav.Nwcl, o.wav.Nwcl}, Ne[3] = {o.wav.Nwcr, o.wav.Nwcr, o.wav.Nwcr};
+    const int gg[3] = {g, g, g};
+    auto flag_bit = [](int r) { return (r >> 30) & 1; };
+    for (int b = 0; b < n; b++) {
+        if (o.ref[b] != 0) continue;
+        for (int r = 1; r <= 168; r++) {
+            const int nb = o.nb[size_t(b) * 168 + r - 1];
+            if (nb < 0 || o.ref[nb] != -1 || o.blocks[nb].level != o.blocks[b].level) continue;
+            int idx[2][3];
+            modify_patch(dim, r, idx, N, Ns, Ne, gg, gg, 0);
+            if (patch_significant(o, b, idx, eps_use)) o.ref[b] |= (1 << (patch_id(r) + 3)) | (1 << 30);
+        }
+    }
+    for (int b = 0; b < n; b++) {
+        if (o.ref[b] != -1) continue;
+        for (int r = 1; r <= 168; r++) {
+            const int nb = o.nb[size_t(b) * 168 + r - 1];
+            if (nb < 0 || !(o.ref[nb] > 0) || o.blocks[nb].level != o.blocks[b].level) continue;
+            const int pid = patch_id(inverse_relation(r));
+            if (flag_bit(o.ref[nb]) && ((o.ref[nb] >> (pid + 3)) & 1)) o.ref[b] = kTmpStatus;
+        }
+    }
+    for (int b = 0; b < n; b++)
+        if (o.ref[b] > 0 && (o.ref[b] == kTmpStatus || flag_bit(o.ref[b]))) o.ref[b] = 0;
+}
+
+// keep the blocks whose flag is not del (and the new order of the kept ones)
+static void erase_blocks(Oracle &o, const std::vector<char> &del) {
+    std::vector<Block> nbl;
+    std::vector<double> nd, nt;
+    std::vector<int> nr;
+    const size_t bsz = size_t(o.nc) * o.npts;
+    for (int b = 0; b < (int)o.blocks.size(); b++) {
+        if (del[b]) continue;
+        nbl.push_back(o.blocks[b]);
+        nd.insert(nd.end(), o.data.begin() + b * bsz, o.data.begin() + (b + 1) * bsz);
+        nt.insert(nt.end(), o.tmp.begin() + b * bsz, o.tmp.begin() + (b + 1) * bsz);
+        nr.push_back(o.ref[b]);
+    }
+    o.blocks.swap(nbl);
+    o.data.swap(nd);
+    o.tmp.swap(nt);
+    o.ref.swap(nr);
+    rebuild_lookup(o);
+}
+
+static int adapt_lifted(Oracle &o, const double *eps_use, int everywhere) {
+    const wg_config &p = o.cfg;
+    const Wavelet &w = o.wav;
+    const int dim = p.dim, g = p.g, Jmin = p.Jmin;
+    const size_t bsz = size_t(o.nc) * o.npts;
+    const bool use_ce = w.lifted;
+    bool leaf_first = true;
+    for (int d = 0; d < dim; d++)
+        if (p.Bs[d] < 3 * std::max(std::abs(w.HD.lo), std::abs(w.HD.hi))) leaf_first = false;
+    // leaf grid metadata
+    const int nleaf = (int)o.blocks.size();
+    o.ref.assign(nleaf, 0);
+    update_neighbors(o, false);
+    update_family(o, Jmin);
+    int lmax = 0;
+    for (const Block &b : o.blocks) {
+        if (b.level < Jmin) return WG_EGRID;
+        lmax = std::max(lmax, b.level);
+    }
+    for (int b = 0; b < nleaf; b++)
+        if (o.blocks[b].level == lmax || leaf_first) o.ref[b] = -1;
+    o.tmp = o.data;
+    // init_full_tree: a mother per family whose last daughter exists
+    {
+        const int last = (1 << dim) - 1;
+        size_t nold = 0;
+        std::vector<char> has_mother(o.blocks.size(), 0);
+        while (nold != o.blocks.size()) {
+            nold = o.blocks.size();
+            has_mother.resize(nold, 0);
+            for (size_t i = 0; i < nold; i++) {
+                const Block b = o.blocks[i];
+                if (has_mother[i] || b.level == Jmin) continue;
+                const int c[3] = {b.c[0] >> 1, b.c[1] >> 1, dim == 3 ? b.c[2] >> 1 : 0};
+                if (find_block(o, b.level - 1, c) >= 0) { has_mother[i] = 1; continue; }
+                const int digit = (b.c[0] & 1) | ((b.c[1] & 1) << 1) | (dim == 3 ? (b.c[2] & 1) << 2 : 0);
+                if (digit != last) continue;
+                Block m;
+                m.level = b.level - 1;
+                m.c[0] = c[0];
+                m.c[1] = c[1];
+                m.c[2] = c[2];
+                o.blocks.push_back(m);
+                o.lookup[key_of(m.level, m.c[0], m.c[1], m.c[2])] = (int)o.blocks.size() - 1;
+                o.ref.push_back(kRefTmpEmpty);
+                has_mother[i] = 1;
+            }
+        }
+        o.data.resize(o.blocks.size() * bsz, 0.0);
+        o.tmp.resize(o.blocks.size() * bsz, 0.0);
+        rebuild_lookup(o);
+        update_neighbors(o, true);
+        update_family(o, Jmin);
+    }
+    const int nt = (int)o.blocks.size();
+    // wavelet_decompose_full_tree
+    {
+        int level = lmax, iteration = 0;
+        const int g_this = std::max(std::abs(w.HD.lo), w.GD.hi);
+        std::vector<double> ud(o.npts);
+        while (level >= Jmin) {
+            SyncSpec sp;
+            sp.base = (use_ce && (!leaf_first || iteration > 0)) ? kSyncMoF : kSyncFull;
+            sp.by_ref = true;
+            sp.s_ref = -1;
+            sp.gminus = sp.gplus = g_this;
+            sp.tmp_usage = kTmpNotFlag;
+            sync_generic(o, sp);
+            for (int b = 0; b < nt; b++) {
+                if (o.ref[b] != -1) continue;
+                std::copy(o.data.begin() + b * bsz, o.data.begin() + (b + 1) * bsz, o.tmp.begin() + b * bsz);
+                for (int c = 0; c < o.nc; c++)
+                    fwt_block(o, o.tmp.data() + b * bsz + size_t(c) * o.npts, o.blk(b) + size_t(c) * o.npts);
+            }
+            if (use_ce) ce_modify(o, 2, 0, -1, true, true);
+            for (int b = 0; b < nt; b++) {
+                if (o.ref[b] == -1) o.ref[b] = 0;
+                if ((o.ref[b] == kRefTmpEmpty || !leaf_first) && o.blocks[b].level == level - 1) o.ref[b] = -1;
+            }
+            sync_d2m(o, level);
+            iteration++;
+            level--;
+        }
+        std::fill(o.ref.begin(), o.ref.end(), 0);
+    }
+    // coarseningIndicator_tree (input_is_WD) / everywhere on leaves
+    for (int b = 0; b < nt; b++) {
+        if (everywhere) {
+            if (blk_is_leaf(o, b, false)) o.ref[b] = -1;
+        } else {
+            o.ref[b] = threshold_wd(o, b, eps_use);
+        }
+    }
+    if (!everywhere && use_ce) security_zone(o, eps_use);
+    // respectJmaxJmin_tree and ensureGradedness_tree (check_daughters)
+    for (int b = 0; b < nt; b++)
+        if (o.ref[b] == -1 && o.blocks[b].level <= Jmin) o.ref[b] = kRefUnsignificantStay;
+    auto stays = [](int f) { return f == 0 || f == kRefUnsignificantStay; };
+    const int nd = 1 << dim;
+    bool changed = true;
+    int guard = 0;
+    while (changed) {
+        changed = false;
+        if (++guard > 10 * (p.Jmax + 1) + 100) return WG_EGRID;
+        for (int i = 0; i < nt; i++) {
+            if (o.ref[i] != -1) continue;
+            const int m = o.mother[i];
+            auto family_stays = [&]() {
+                for (int k = 0; k < nd; k++) {
+                    const int s2 = o.dau[size_t(m) * 8 + k];
+                    if (s2 >= 0 && o.ref[s2] < 0) o.ref[s2] = kRefUnsignificantStay;
+                }
+                changed = true;
+            };
+            bool all_coarsen = true;
+            for (int k = 0; k < nd; k++) {
+                const int s2 = o.dau[size_t(m) * 8 + k];
+                if (s2 < 0 || o.ref[s2] >= 0) all_coarsen = false;
+            }
+            if (!all_coarsen) { family_stays(); continue; }
+            bool dstay = false;
+            for (int k = 0; k < nd; k++) {
+                const int d2 = o.dau[size_t(i) * 8 + k];
+                if (d2 >= 0 && stays(o.ref[d2])) dstay = true;
+            }
+            if (dstay) { family_stays(); continue; }
+            const Block b = o.blocks[i];
+            const int nn = 1 << b.level;
+            bool keep = false;
+            for (int dz = (dim == 3 ? -1 : 0); dz <= (dim == 3 ? 1 : 0) && !keep; dz++)
+                for (int dy = -1; dy <= 1 && !keep; dy++)
+                    for (int dx = -1; dx <= 1 && !keep; dx++) {
+                        if (!dx && !dy && !dz) continue;
+                        const int d[3] = {dx, dy, dz};
+                        int c[3] = {0, 0, 0};
+                        for (int a = 0; a < dim; a++) c[a] = ((b.c[a] + d[a]) % nn + nn) % nn;
+                        for (int kz = 0; kz < (dim == 3 ? 2 : 1) && !keep; kz++)
+                            for (int ky = 0; ky < 2 && !keep; ky++)
+                                for (int kx = 0; kx < 2 && !keep; kx++) {
+                                    const int kk[3] = {kx, ky, kz};
+                                    bool adj = true;
+                                    for (int a = 0; a < dim; a++)
+                                        if ((d[a] == 1 && kk[a] != 0) || (d[a] == -1 && kk[a] != 1)) adj = false;
+                                    if (!adj) continue;
+                                    const int fc[3] = {2 * c[0] + kx, 2 * c[1] + ky, dim == 3 ? 2 * c[2] + kz : 0};
+                                    const int f = find_block(o, b.level + 1, fc);
+                                    if (f >= 0 && stays(o.ref[f])) keep = true;
+                                }
+                    }
+            if (keep) {
+                o.ref[i] = kRefUnsignificantStay;
+                changed = true;
+            }
+        }
+    }
+    // delete the blocks still flagged -1; metadata of the remaining full tree
+    {
+        std::vector<char> del(nt, 0);
+        for (int b = 0; b < nt; b++) del[b] = o.ref[b] == -1;
+        erase_blocks(o, del);
+        update_neighbors(o, true);
+        update_family(o, Jmin);
+    }
+    const int n2 = (int)o.blocks.size();
+    if (use_ce) ce_modify(o, 0, 0, 0, true, false);
+    if (!use_ce) {
+        // nothing was modified: the original values are copied back
+        o.data = o.tmp;
+    } else {
+        // wavelet_reconstruct_full_tree_CEoptimized
+        bool leaf_only = true, recon_nb = false;
+        for (int d = 0; d < dim; d++) {
+            if (p.Bs[d] < w.Ndep2l || p.Bs[d] < w.Ndep2r) leaf_only = false;
+            if (p.Bs[d] < w.Nreconl || p.Bs[d] < w.Nreconr) recon_nb = true;
+        }
+        if (recon_nb) return WG_ENOTSUP;   // sync_M2D not restated (Bs below Nrecon)
+        std::fill(o.ref.begin(), o.ref.end(), 0);
+        for (int b = 0; b < n2; b++) {
+            if (!blk_is_leaf(o, b, false)) continue;
+            for (int r = 1; r <= 168; r++) {
+                const int nb = o.nb[size_t(b) * 168 + r - 1];
+                if (nb < 0) continue;
+                if (o.blocks[nb].level < o.blocks[b].level &&
+                    !(blk_has_valid_neighbor(o, b, r, 0) || blk_has_valid_neighbor(o, b, r, -1))) {
+                    o.ref[b] = -1;
+                    break;
+                }
+            }
+        }
+        auto reconstruct = [&](int b) {
+            if (o.ref[b] == -1)
+                for (int c = 0; c < o.nc; c++)
+                    iwt_block(o, o.blk(b) + size_t(c) * o.npts, o.tmp.data() + b * bsz + size_t(c) * o.npts);
+            std::copy(o.tmp.begin() + b * bsz, o.tmp.begin() + (b + 1) * bsz, o.data.begin() + b * bsz);
+        };
+        SyncSpec sp;
+        sp.base = kSyncMoC;
+        sp.by_ref = true;
+        sp.s_ref = -1;
+        sp.gminus = sp.gplus = g;
+        sp.tmp_usage = kTmpDecomposed;
+        if (leaf_only) {
+            sync_generic(o, sp);
+            if (use_ce) ce_modify(o, 0, 0, 0, true, false);
+            for (int b = 0; b < n2; b++) reconstruct(b);
+        } else {
+            int jmax = 0;
+            for (const Block &b : o.blocks) jmax = std::max(jmax, b.level);
+            for (int level = Jmin; level <= jmax; level++) {
+                sp.by_level = true;
+                sp.s_level = level;
+                sync_generic(o, sp);
+                if (use_ce) ce_modify(o, 1, level, 0, true, false);
+                for (int b = 0; b < n2; b++)
+                    if (o.blocks[b].level == level) reconstruct(b);
+            }
+        }
+        std::fill(o.ref.begin(), o.ref.end(), 0);
+    }
+    // prune_fulltree2leafs
+    {
+        std::vector<char> del(n2, 0);
+        for (int b = 0; b < n2; b++) del[b] = !blk_is_leaf(o, b, false);
+        erase_blocks(o, del);
+    }
+    o.mask.clear();
+    update_neighbors(o, false);
+    update_family(o, Jmin);
+    // final sync_ghosts_tree (filtered restriction)
+    SyncSpec sp;
+    sp.gminus = sp.gplus = g;
+    sync_generic(o, sp);
+    o.tmp.clear();
+    return WG_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1408,6 +2161,17 @@ int or_get_neighbors(void *h, int *out) {
 int or_sync_ghosts(void *h, int gminus, int gplus, int ignore_filter) {
     Oracle &o = *(Oracle *)h;
     if (gminus < 1 || gplus < 1 || gminus > o.cfg.g || gplus > o.cfg.g) return WG_EINVAL;
+    if (o.wav.lifted && !ignore_filter) {
+        // sync_ghosts_tree with the filtered restriction and the SC copies
+        // of restrict_copy_at_CE
+        o.ref.assign(o.blocks.size(), 0);
+        update_family(o, o.cfg.Jmin);
+        SyncSpec sp;
+        sp.gminus = gminus;
+        sp.gplus = gplus;
+        sync_generic(o, sp);
+        return WG_OK;
+    }
     sync_ghosts(o, gminus, gplus, ignore_filter != 0);
     return WG_OK;
 }
@@ -1491,8 +2255,15 @@ int or_wc_threshold(void *h, double *data, const double *thresh) {
 // component), 1 everywhere; returns the new block count or an error
 int or_adapt(void *h, const double *eps_use, int indicator) {
     Oracle &o = *(Oracle *)h;
-    if (o.wav.Y != 0) return WG_ENOTSUP;
-    const int st = adapt_unlifted(o, eps_use, indicator == 1);
+    const int st = o.wav.Y != 0 ? adapt_lifted(o, eps_use, indicator == 1) : adapt_unlifted(o, eps_use, indicator == 1);
+    return st ? st : (int)o.blocks.size();
+}
+
+// the same through the full-tree machinery of the lifted path, also for
+// unlifted wavelets (checks that machinery against the CDF X0 files)
+int or_adapt_full_tree(void *h, const double *eps_use, int indicator) {
+    Oracle &o = *(Oracle *)h;
+    const int st = adapt_lifted(o, eps_use, indicator == 1);
     return st ? st : (int)o.blocks.size();
 }
 

@@ -21,6 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "forest.cpp": [],
     "adapt.cpp": [],
+    "lifted.cpp": [],
+    "k_lifted.cu": ["-fmad=false"],
     "capi.cu": [],
     "k_sync.cu": ["-fmad=false"],
     "k_misc.cu": [],

@@ -29,6 +29,7 @@
 
 #include "../../include/wabbit_gb300.h"
 #include "adapt.hpp"
+#include "lifted.hpp"
 #include "common.cuh"
 
 namespace wg {
@@ -165,6 +166,7 @@ struct wg_ctx {
     int variant_fast = 1;               // 1: FMA stencil, 0: strict reference arithmetic
     int precision = WG_RHS_FP64;        // WG_RHS_FP32: double-float stencils on the FP32 units
     DevArray<int> d_tree_ids;
+    double *T = nullptr;                // hvy_tmp arena of the lifted adaptation (slot-indexed like A)
     double *staging = nullptr;          // compact interior staging buffer
     size_t staging_bytes = 0;
     cudaGraph_t graph = nullptr;
@@ -979,6 +981,7 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->d_push);
     cudaFree(ctx->d_err);
     cudaFree(ctx->staging);
+    cudaFree(ctx->T);
     cudaFree(ctx->d_desc);
     cudaFree(ctx->d_tp);
     cudaFree(ctx->d_clk);
@@ -1513,14 +1516,334 @@ int wg_threshold_flags_wd(wg_ctx *ctx, int tree, const double *eps_use, int *fla
 // Their data is already in their slots: the old leaves' untouched, the
 // promoted mothers' from their daughters. Masks are dropped (they depend on
 // the grid and are set again by the caller). Ends with a ghost sync.
+// adapt_tree for lifted wavelets (LIB/MESH/adapt_tree.f90:11-255): full-tree
+// decomposition with coarse extension, indicator on the decomposition,
+// security zone, flag consistency, deletion, reconstruction of the blocks at
+// coarse/fine interfaces, pruning and the final filtered sync. The host
+// plans every step (lifted.cpp); the data stays in A (hvy_block) and the
+// slot-indexed hvy_tmp arena T.
+static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, bool thr, int *nblk_out) {
+    const int dim = ctx->cfg.dim, nc = ctx->geo.nc, g = ctx->cfg.g;
+    const int *Bs = ctx->cfg.Bs;
+    const int nb = t->forest.size();
+    const WaveletInfo &w = ctx->wav;
+    const BufGeo gA = ctx->gA;
+    const long long per_block = (long long)nc * gA.npts();
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    LiftedTree L;
+    std::string err;
+    if (!L.init(ctx->geo, w, 2, t->cfg.Jmin, t->cfg.Jmax, nb, t->forest.level.data(), t->forest.coords.data(), err))
+        return fail(WG_EGRID, "adapt: %s", err.c_str());
+    bool leaf_only = true, recon_nb = false, leaf_first = true;
+    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1;
+    for (int d = 0; d < dim; d++) {
+        if (Bs[d] < L.Ndep2l || Bs[d] < L.Ndep2r) leaf_only = false;
+        if (Bs[d] < L.Nreconl || Bs[d] < L.Nreconr) recon_nb = true;
+        if (Bs[d] < 3 * std::max(std::abs(w.hd_lo), std::abs(hd_hi))) leaf_first = false;
+    }
+    if (recon_nb) return fail(WG_ENOTSUP, "lifted adapt with Bs below the coarse-extension reconstruction width");
+    const int nt = L.size();
+    if ((size_t)(nt - nb) > ctx->free_slots.size())
+        return fail(WG_ENOMEM, "adapt needs %d free slots for the mothers (%zu free)", nt - nb, ctx->free_slots.size());
+    if (!ctx->T) {
+        const size_t bytes = sizeof(double) * (size_t)per_block * ctx->max_blocks;
+        if (cudaMalloc(&ctx->T, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->T = nullptr;
+            return fail(WG_ENOMEM, "hvy_tmp arena of %zu bytes", bytes);
+        }
+    }
+    for (int b = 0; b < nb; b++) L.slot[b] = t->slots[b];
+    std::sort(ctx->free_slots.begin(), ctx->free_slots.end(), std::greater<int>());
+    for (int b = nb; b < nt; b++) {
+        L.slot[b] = ctx->free_slots.back();
+        ctx->free_slots.pop_back();
+    }
+    // device lists stay alive until the end (the stream is synchronised there)
+    std::vector<std::unique_ptr<DevArray<Patch>>> kp;
+    std::vector<std::unique_ptr<DevArray<FilterEntry>>> kf;
+    std::vector<std::unique_ptr<DevArray<ScBox>>> ks;
+    std::vector<std::unique_ptr<DevArray<BoxOp>>> kb;
+    std::vector<std::unique_ptr<DevArray<int>>> ki;
+    std::vector<std::unique_ptr<DevArray<double>>> kd;
+    auto up = [&](auto &keep, const auto &v) -> decltype(keep.back()->p) {
+        using E = typename std::remove_reference<decltype(*keep.back()->p)>::type;
+        keep.emplace_back(new DevArray<E>());
+        if (keep.back()->upload(v.data(), v.size(), ctx->stream) != cudaSuccess) return nullptr;
+        return keep.back()->p;
+    };
+    cudaError_t e = lifted_set_filter(w.HD.data(), w.hd_lo, (int)w.HD.size(), ctx->stream);
+    const int hx = Bs[0] / 2, hy = Bs[1] / 2, hz = dim == 3 ? Bs[2] / 2 : 1;
+    auto run_waves = [&](const std::vector<SyncWave> &waves) -> cudaError_t {
+        for (const SyncWave &wv : waves) {
+            cudaError_t r = cudaSuccess;
+            if (!wv.copy_blk.empty()) r = launch_xcopy(up(kp, wv.copy_blk), (int)wv.copy_blk.size(), ctx->A, ctx->A, gA, nc, ctx->stream);
+            if (r == cudaSuccess && !wv.copy_tmp.empty())
+                r = launch_xcopy(up(kp, wv.copy_tmp), (int)wv.copy_tmp.size(), ctx->T, ctx->A, gA, nc, ctx->stream);
+            if (r == cudaSuccess && !wv.restrict_.empty()) {
+                // every restricted point lies on the sender's interior SC lattice
+                for (const Patch &p : wv.restrict_)
+                    for (int d = 0; d < dim; d++) {
+                        const int a = p.slo[d] + 2 * p.blo[d], z = a + 2 * (p.rhi[d] - p.rlo[d]);
+                        if (((a - g) & 1) || a < g || z > g + Bs[d] - 2) return cudaErrorInvalidValue;
+                    }
+                std::vector<double> none;
+                kd.emplace_back(new DevArray<double>());
+                r = kd.back()->upload(nullptr, (size_t)wv.filters.size() * nc * hx * hy * hz, ctx->stream);
+                double *scratch = kd.back()->p;
+                const FilterEntry *fe = up(kf, wv.filters);
+                if (r == cudaSuccess)
+                    r = launch_hd_filter(dim, fe, (int)wv.filters.size(), ctx->A, ctx->T, gA, Bs[0], Bs[1], Bs[2], nc,
+                                         w.hd_lo, (int)w.HD.size(), scratch, ctx->stream);
+                if (r == cudaSuccess && !wv.ce_copies.empty())
+                    r = launch_scbox(up(ks, wv.ce_copies), (int)wv.ce_copies.size(), fe, ctx->A, ctx->T, gA, hx, hy,
+                                     hz, nc, scratch, ctx->stream);
+                if (r == cudaSuccess)
+                    r = launch_restrict_scratch(up(kp, wv.restrict_), (int)wv.restrict_.size(), scratch, ctx->A, gA,
+                                                hx, hy, hz, nc, ctx->stream);
+            }
+            if (r == cudaSuccess && !wv.pred_blk.empty())
+                r = launch_predict(up(kp, wv.pred_blk), (int)wv.pred_blk.size(), wv.max_coarse, ctx->A, gA, nc,
+                                   w.order_predictor, ctx->stream, ctx->A);
+            if (r == cudaSuccess && !wv.pred_tmp.empty())
+                r = launch_predict(up(kp, wv.pred_tmp), (int)wv.pred_tmp.size(), wv.max_coarse, ctx->A, gA, nc,
+                                   w.order_predictor, ctx->stream, ctx->T);
+            if (r != cudaSuccess) return r;
+        }
+        return cudaSuccess;
+    };
+    auto sync_spec = [&](SyncSpecL sp) -> cudaError_t {
+        std::vector<SyncWave> waves;
+        L.plan_sync(sp, waves);
+        return run_waves(waves);
+    };
+    auto ce = [&](int ce_case, int s_level, int s_ref, bool clear_wc, bool copy_sc) -> cudaError_t {
+        std::vector<BoxOp> ops;
+        L.plan_ce_modify(ce_case, s_level, s_ref, clear_wc, copy_sc, ops);
+        if (ops.empty()) return cudaSuccess;
+        return launch_boxop(up(kb, ops), (int)ops.size(), ctx->A, ctx->T, gA, nc, ctx->stream);
+    };
+    auto slots_where = [&](auto pred) {
+        std::vector<int> v;
+        for (int b = 0; b < nt; b++)
+            if (L.alive[b] && pred(b)) v.push_back(L.slot[b]);
+        return v;
+    };
+    auto fail_restore = [&](cudaError_t ce2, int st) {
+        cudaStreamSynchronize(ctx->stream);
+        for (int b = nb; b < nt; b++) ctx->free_slots.push_back(L.slot[b]);
+        if (ce2 != cudaSuccess) return cuda_fail(ce2, "wg_adapt (lifted)", __FILE__, __LINE__);
+        return st;
+    };
+    // the leaf grid's filtered sync (sync_ghosts_tree)
+    for (int b = 0; b < nt; b++) L.alive[b] = b < nb;
+    if (!L.update_metadata(err)) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
+    {
+        SyncSpecL sp;
+        sp.gminus = sp.gplus = g;
+        if (e == cudaSuccess) e = sync_spec(sp);
+    }
+    // wavelet_decompose_full_tree
+    std::fill(L.alive.begin(), L.alive.end(), 1);
+    if (!L.update_metadata(err)) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
+    const int lmax = L.ft.max_level();
+    for (int b = 0; b < nt; b++) L.ref[b] = b < nb ? ((L.ft.level[b] == lmax || leaf_first) ? -1 : 0) : kRefTmpEmpty;
+    {
+        std::vector<int> leaves(t->slots.begin(), t->slots.end());
+        if (e == cudaSuccess) e = launch_blockcopy(up(ki, leaves), nb, ctx->A, ctx->T, per_block, ctx->stream);
+    }
+    const int g_this = std::max(std::abs(w.hd_lo), w.gd_lo + (int)w.GD.size() - 1);
+    for (int level = lmax, it = 0; level >= t->cfg.Jmin && e == cudaSuccess; level--, it++) {
+        SyncSpecL sp;
+        sp.base = (leaf_first && it == 0) ? 1 : 4;
+        sp.by_ref = true;
+        sp.s_ref = -1;
+        sp.gminus = sp.gplus = g_this;
+        sp.tmp_usage = 1;
+        e = sync_spec(sp);
+        const std::vector<int> dec = slots_where([&](int b) { return L.ref[b] == -1; });
+        if (e == cudaSuccess && !dec.empty()) {
+            const int *d_dec = up(ki, dec);
+            e = launch_blockcopy(d_dec, (int)dec.size(), ctx->A, ctx->T, per_block, ctx->stream);
+            if (e == cudaSuccess)
+                e = launch_wavelet_decompose_window(dim, d_dec, (int)dec.size(), ctx->A, gA, Bs[0], Bs[1], Bs[2], nc,
+                                                    w.X, w.Y, ctx->stream);
+        }
+        if (e == cudaSuccess) e = ce(2, 0, -1, true, true);
+        for (int b = 0; b < nt; b++) {
+            if (L.ref[b] == -1) L.ref[b] = 0;
+            if ((L.ref[b] == kRefTmpEmpty || !leaf_first) && L.ft.level[b] == level - 1) L.ref[b] = -1;
+        }
+        std::vector<Patch> d2m, gh;
+        mother_patches(L.ft, ctx->geo, level - 1, L.slot, d2m, gh);
+        if (e == cudaSuccess && !d2m.empty())
+            e = launch_sync(up(kp, d2m), (int)d2m.size(), ctx->A, gA, nc, w.order_predictor, ctx->stream);
+    }
+    std::fill(L.ref.begin(), L.ref.end(), 0);
+    // coarseningIndicator_tree on the decomposition, security zone
+    std::vector<int> flags(nt, 0);
+    if (e == cudaSuccess && thr) {
+        std::vector<int> all(L.slot.begin(), L.slot.end());
+        std::vector<int> tsvc(t->cfg.threshold_state_vector_component, t->cfg.threshold_state_vector_component + nc);
+        std::vector<double> eps(eps_use, eps_use + nc);
+        const int *d_all = up(ki, all);
+        std::vector<int> zeros(nt, 0);
+        int *d_flags = up(ki, zeros);
+        e = launch_fwt_flags(dim, d_all, nt, ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X, w.Y, up(kd, eps), up(ki, tsvc),
+                             d_flags, nullptr, ctx->stream, 1);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(flags.data(), d_flags, sizeof(int) * nt, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e == cudaSuccess) {
+            L.ref = flags;
+            std::vector<LiftedTree::ZoneItem> items;
+            L.security_candidates(items);
+            if (!items.empty()) {
+                std::vector<int> zb;
+                for (const auto &z : items) {
+                    zb.push_back(L.slot[z.block]);
+                    for (int d = 0; d < 3; d++) zb.push_back(z.lo[d]);
+                    for (int d = 0; d < 3; d++) zb.push_back(z.hi[d]);
+                    for (int d = 0; d < 3; d++) zb.push_back(z.io[d]);
+                }
+                std::vector<double> det(items.size() * nc, 0.0);
+                kd.emplace_back(new DevArray<double>());
+                e = kd.back()->upload(nullptr, det.size(), ctx->stream);
+                if (e == cudaSuccess)
+                    e = launch_zone_detail(up(ki, zb), (int)items.size(), ctx->A, gA, nc, dim, kd.back()->p, ctx->stream);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(det.data(), kd.back()->p, sizeof(double) * det.size(), cudaMemcpyDeviceToHost,
+                                        ctx->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+                // threshold_block's component / vector-group rule
+                std::vector<char> sig(items.size(), 0);
+                int maxg = 0;
+                for (int c = 0; c < nc; c++) maxg = std::max(maxg, tsvc[c]);
+                for (size_t i = 0; i < items.size(); i++) {
+                    double detail[8];
+                    for (int c = 0; c < nc; c++) detail[c] = -1.0;
+                    for (int l = 2; l <= maxg; l++) {
+                        double m = 0.0;
+                        for (int c = 0; c < nc; c++) if (tsvc[c] == l) m = std::max(m, det[i * nc + c]);
+                        for (int c = 0; c < nc; c++) if (tsvc[c] == l) detail[c] = m;
+                    }
+                    for (int c = 0; c < nc; c++) {
+                        if (tsvc[c] == 1) detail[c] = det[i * nc + c];
+                        if (tsvc[c] == 0) detail[c] = 0.0;
+                    }
+                    for (int c = 0; c < nc; c++)
+                        if (!(detail[c] <= eps_use[c])) sig[i] = 1;
+                }
+                L.security_apply(items, sig);
+            }
+            flags = L.ref;
+        }
+    } else if (!thr) {
+        for (int b = 0; b < nb; b++) flags[b] = kFlagCoarsen;   // "everywhere": the leaves
+    }
+    if (e != cudaSuccess) return fail_restore(e, WG_ECUDA);
+    std::vector<int> leaves;
+    adapt_decide(L.ft, flags, leaves);
+    // delete, coarse extension on the remaining full tree, reconstruct
+    for (int b = 0; b < nt; b++) {
+        L.alive[b] = flags[b] != kFlagCoarsen;
+        L.ref[b] = 0;
+    }
+    if (!L.update_metadata(err)) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
+    e = ce(0, 0, 0, true, false);
+    for (int b = 0; b < nt; b++) {
+        if (!L.alive[b] || !L.is_leaf(b, false)) continue;
+        for (int r = 1; r <= kNumRelations; r++) {
+            const int n = L.nbr(b, r);
+            if (n < 0) continue;
+            if (L.ft.level[n] < L.ft.level[b] && !(L.has_valid_neighbor(b, r, 0) || L.has_valid_neighbor(b, r, -1))) {
+                L.ref[b] = -1;
+                break;
+            }
+        }
+    }
+    auto reconstruct = [&](auto on_level) -> cudaError_t {
+        const std::vector<int> rec = slots_where([&](int b) { return on_level(b) && L.ref[b] == -1; });
+        const std::vector<int> keep = slots_where([&](int b) { return on_level(b) && L.ref[b] != -1; });
+        cudaError_t r = cudaSuccess;
+        if (!rec.empty())
+            r = launch_wavelet_reconstruct(dim, up(ki, rec), (int)rec.size(), ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X,
+                                           w.Y, ctx->stream);
+        if (r == cudaSuccess && !keep.empty())
+            r = launch_blockcopy(up(ki, keep), (int)keep.size(), ctx->T, ctx->A, per_block, ctx->stream);
+        return r;
+    };
+    SyncSpecL rs;
+    rs.base = 3;
+    rs.by_ref = true;
+    rs.s_ref = -1;
+    rs.gminus = rs.gplus = g;
+    rs.tmp_usage = 2;
+    if (leaf_only) {
+        if (e == cudaSuccess) e = sync_spec(rs);
+        if (e == cudaSuccess) e = ce(0, 0, 0, true, false);
+        if (e == cudaSuccess) e = reconstruct([](int) { return true; });
+    } else {
+        int jmax = 0;
+        for (int b = 0; b < nt; b++)
+            if (L.alive[b]) jmax = std::max(jmax, L.ft.level[b]);
+        for (int level = t->cfg.Jmin; level <= jmax && e == cudaSuccess; level++) {
+            rs.by_level = true;
+            rs.s_level = level;
+            e = sync_spec(rs);
+            if (e == cudaSuccess) e = ce(1, level, 0, true, false);
+            if (e == cudaSuccess) e = reconstruct([&](int b) { return L.ft.level[b] == level; });
+        }
+    }
+    // prune: the new leaves; final filtered sync on the leaf grid
+    std::fill(L.alive.begin(), L.alive.end(), 0);
+    for (int b : leaves) L.alive[b] = 1;
+    std::fill(L.ref.begin(), L.ref.end(), 0);
+    if (!L.update_metadata(err)) return fail_restore(e, fail(WG_EGRID, "adapt: %s", err.c_str()));
+    {
+        SyncSpecL sp;
+        sp.gminus = sp.gplus = g;
+        if (e == cudaSuccess) e = sync_spec(sp);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail_restore(e, WG_ECUDA);
+    // install the new grid
+    const int nn = (int)leaves.size();
+    std::vector<int> lv(nn), co(3 * nn), sl(nn);
+    std::vector<char> kept(nt, 0);
+    for (int i = 0; i < nn; i++) {
+        const int b = leaves[i];
+        lv[i] = L.ft.level[b];
+        for (int a = 0; a < 3; a++) co[3 * i + a] = L.ft.coords[3 * b + a];
+        sl[i] = L.slot[b];
+        kept[b] = 1;
+    }
+    for (int b = 0; b < nt; b++)
+        if (!kept[b]) ctx->free_slots.push_back(L.slot[b]);
+    for (int m : t->mask_slot)
+        if (m >= 0) ctx->mask_free.push_back(m);
+    t->forest.set(nn, lv.data(), co.data());
+    if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "adapt produced an invalid grid: %s", err.c_str());
+    if (!t->forest.graded()) return fail(WG_EGRID, "adapt produced a grid that is not graded");
+    t->slots = sl;
+    t->mask_slot.assign(nn, -1);
+    t->sync.clear();
+    t->shadow_valid = false;
+    int st;
+    if ((st = upload_desc(ctx, *t, tree))) return st;
+    if ((st = upload_lists(ctx, *t))) return st;
+    ctx->grid_version++;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    if (nblk_out) *nblk_out = nn;
+    return WG_OK;
+}
+
 int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *nblk_out) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return WG_EINVAL;
     if (indicator != WG_ADAPT_THRESHOLD && indicator != WG_ADAPT_EVERYWHERE)
         return fail(WG_EINVAL, "unknown indicator %d", indicator);
     if (indicator == WG_ADAPT_THRESHOLD && !eps_use) return fail(WG_EINVAL, "eps_use is required");
-    if (ctx->wav.lifted)
-        return fail(WG_ENOTSUP, "adapt for lifted wavelets (coarse extension, security zone) is not built; CDF X0 only");
+    if (ctx->wav.lifted) return adapt_lifted(ctx, t, tree, eps_use, indicator == WG_ADAPT_THRESHOLD, nblk_out);
     const int dim = ctx->cfg.dim, nc = ctx->geo.nc, g = ctx->cfg.g;
     const int *Bs = ctx->cfg.Bs;
     const int nb = t->forest.size();

@@ -108,8 +108,9 @@ cudaError_t launch_expand(const Patch *patches, const unsigned *first, int npatc
 cudaError_t launch_gather(const void *pairs, unsigned n, void *buf, BufGeo geo, int nc, cudaStream_t s);
 // prediction patches only; max_smem_doubles = largest shared-memory need
 // (coarse box + x window + x-y window) of a patch, in doubles
+// src_buf: the sender blocks' buffer when it is not buf (same layout)
 cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_doubles, double *buf, BufGeo geo, int nc,
-                           int order_predictor, cudaStream_t s);
+                           int order_predictor, cudaStream_t s, const double *src_buf = nullptr);
 // RHS + RK stage (j = 1..4) over nblk blocks listed in blk
 cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, int nblk, const BlockDesc *desc,
                              const TreeParams *tp, const TreeClock *clk, const double *in, BufGeo gin,
@@ -156,6 +157,29 @@ cudaError_t launch_wavelet_decompose(int dim, const int *blk, int nblk, double *
                                      int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s);
 cudaError_t launch_wavelet_reconstruct(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
                                        int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s);
+// the FWT of waveletDecomposition_optimized_block with the pass results it
+// leaves on the ghost rows/planes of its window (adapt on the full tree)
+cudaError_t launch_wavelet_decompose_window(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
+                                            int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s);
+// full-tree adaptation with coarse extension (k_lifted.cu); the structs are
+// in lifted.hpp
+struct FilterEntry;
+struct ScBox;
+struct BoxOp;
+cudaError_t lifted_set_filter(const double *hd, int lo, int n, cudaStream_t s);
+cudaError_t launch_xcopy(const Patch *p, int n, const double *sbuf, double *dbuf, BufGeo geo, int nc, cudaStream_t s);
+cudaError_t launch_hd_filter(int dim, const FilterEntry *ent, int n, const double *A, const double *T, BufGeo geo,
+                             int Bx, int By, int Bz, int nc, int hd_lo, int hd_n, double *scratch, cudaStream_t s);
+cudaError_t launch_scbox(const ScBox *b, int n, const FilterEntry *ent, const double *A, const double *T, BufGeo geo,
+                         int hx, int hy, int hz, int nc, double *scratch, cudaStream_t s);
+cudaError_t launch_restrict_scratch(const Patch *p, int n, const double *scratch, double *A, BufGeo geo, int hx,
+                                    int hy, int hz, int nc, cudaStream_t s);
+cudaError_t launch_boxop(const BoxOp *o, int n, double *A, const double *T, BufGeo geo, int nc, cudaStream_t s);
+cudaError_t launch_blockcopy(const int *slots, int n, const double *src, double *dst, long long per_block,
+                             cudaStream_t s);
+// items: {slot, lo[3], hi[3], io[3]} ints; det: n x nc maxima
+cudaError_t launch_zone_detail(const void *items, int n, const double *A, BufGeo geo, int nc, int dim, double *det,
+                               cudaStream_t s);
 // wc_threshold_tree on spaghetti data (thresh, tsvc: nc host values, nc <= 8)
 cudaError_t launch_wc_threshold(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,
                                 int nc, const double *thresh, const int *tsvc, cudaStream_t s);

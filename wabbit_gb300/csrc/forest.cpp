@@ -188,7 +188,7 @@ uint64_t Forest::treecode(int b) const {
     return tc;
 }
 
-bool Forest::update_neighbors(std::string &err) {
+bool Forest::update_neighbors(std::string &err, bool overlapping) {
     const int n = size();
     lookup_.clear();
     lookup_.reserve(size_t(n) * 2);
@@ -217,11 +217,51 @@ bool Forest::update_neighbors(std::string &err) {
                     for (int i = 0; i < dim; i++) nfree += (d[i] == 0);
                     const int nparts = 1 << nfree;
                     const int rel0 = relation_of(d, 0, dim);
-                    if (lv == 0) { nb[rel0 - 1] = b; continue; }
+                    if (lv == 0) {
+                        nb[rel0 - 1] = b;
+                        if (!overlapping) continue;
+                    }
                     int a[3];
                     for (int i = 0; i < 3; i++) a[i] = i < dim ? ((c[i] + d[i]) % N + N) % N : 0;
-                    int s = find(lv, a[0], a[1], a[2]);
-                    if (s >= 0) { nb[rel0 - 1] = s; continue; }
+                    if (lv > 0) {
+                        const int s = find(lv, a[0], a[1], a[2]);
+                        if (s >= 0) {
+                            nb[rel0 - 1] = s;
+                            if (!overlapping) continue;
+                        }
+                    }
+                    if (overlapping) {
+                        // every finer part up to the first missing one, then
+                        // the coarser block
+                        if (lv < Jmax)
+                            for (int p = 0; p < nparts; p++) {
+                                int fc[3];
+                                int fr = 0;
+                                for (int i = 0; i < 3; i++) {
+                                    if (i >= dim) { fc[i] = 0; continue; }
+                                    int bit;
+                                    if (d[i] == 0) bit = (p >> fr++) & 1;
+                                    else bit = d[i] > 0 ? 1 : 0;
+                                    const int v = 2 * c[i] + bit + d[i];
+                                    fc[i] = ((v % (2 * N)) + 2 * N) % (2 * N);
+                                }
+                                const int fb = find(lv + 1, fc[0], fc[1], fc[2]);
+                                if (fb < 0) break;
+                                nb[relation_of(d, p, dim) - 1 + 112] = fb;
+                            }
+                        if (lv <= Jmin) continue;
+                        int part = 0, fr = 0;
+                        bool touches = true;
+                        for (int i = 0; i < dim; i++) {
+                            const int bit = c[i] & 1;
+                            if (d[i] == 0) part |= bit << fr++;
+                            else if ((d[i] > 0) != (bit == 1)) touches = false;
+                        }
+                        if (!touches) continue;
+                        const int cb = find(lv - 1, a[0] >> 1, a[1] >> 1, a[2] >> 1);
+                        if (cb >= 0) nb[relation_of(d, part, dim) - 1 + 56] = cb;
+                        continue;
+                    }
                     // finer neighbours: all parts must exist
                     bool all = lv < Jmax;
                     if (all) {
@@ -348,6 +388,63 @@ static void send_box(const Geometry &geo, int order_predictor, int relation, int
             if (b[1][d] - b[0][d] > g + a) buf[1][d] += geo.Bs[d];
         }
     }
+}
+
+Patch make_patch(const Geometry &geo, int order_predictor, int relation, int lvl_diff, int gminus, int gplus, int src,
+                 int dst) {
+    int rb[2][3], sb[2][3], bb[2][3];
+    recv_box(geo, inverse_relation(relation), gminus, gplus, -lvl_diff, rb);
+    send_box(geo, order_predictor, relation, lvl_diff, gminus, gplus, sb, bb);
+    Patch p;
+    std::memset(&p, 0, sizeof(p));
+    p.src = src;
+    p.dst = dst;
+    p.op = lvl_diff == 0 ? 0 : (lvl_diff == +1 ? 1 : 2);
+    for (int k = 0; k < 3; k++) {
+        p.rlo[k] = (int16_t)(rb[0][k] - 1);
+        p.rhi[k] = (int16_t)(rb[1][k] - 1);
+        p.slo[k] = (int16_t)(sb[0][k] - 1);
+        p.shi[k] = (int16_t)(sb[1][k] - 1);
+        p.blo[k] = (int16_t)(bb[0][k] - 1);
+    }
+    return p;
+}
+
+void modify_box0(const Geometry &geo, int relation, int Ns, int Ne, int gm, int gp, int lvl_diff, int lo[3], int hi[3]) {
+    int idx[2][3];
+    modify_box(geo, relation, Ns, Ne, gm, gp, lvl_diff, idx);
+    for (int d = 0; d < 3; d++) {
+        lo[d] = idx[0][d] - 1;
+        hi[d] = idx[1][d] - 1;
+    }
+}
+
+void ghost_box0(const Geometry &geo, int relation, int gminus, int gplus, int lvl_diff, int lo[3], int hi[3]) {
+    int idx[2][3];
+    recv_box(geo, relation, gminus, gplus, lvl_diff, idx);
+    for (int d = 0; d < 3; d++) {
+        lo[d] = idx[0][d] - 1;
+        hi[d] = idx[1][d] - 1;
+    }
+}
+
+int relation_inverse(int relation) { return inverse_relation(relation); }
+
+int relation_patch_id(int relation) {
+    const int t = (relation - 1) % 56 + 1;
+    if (t <= 24) return (t - 1) / 4 + 1;
+    if (t <= 48) return (t - 25) / 2 + 1 + 6;
+    return (t - 49) + 1 + 6 + 12;
+}
+
+void relation_range(int relation, int lvl_diff, int &lo, int &hi) {
+    const int pid = relation_patch_id(relation);
+    if (pid <= 6) { lo = (pid - 1) * 4 + 1; hi = pid * 4; }
+    else if (pid <= 18) { lo = (pid - 7) * 2 + 25; hi = (pid - 6) * 2 + 24; }
+    else { lo = (pid - 19) + 49; hi = (pid - 18) + 48; }
+    const int off = lvl_diff == +1 ? 56 : lvl_diff == -1 ? 112 : 0;
+    lo += off;
+    hi += off;
 }
 
 bool make_sync_table(const Forest &f, const Geometry &geo, const WaveletInfo &w, int gminus, int gplus, int g_buf,

@@ -47,8 +47,11 @@ public:
     void set(int nblk, const int *lv, const int *co);
     int find(int lv, int x, int y, int z) const;
     // neighbour search for all blocks; returns false and a message for an
-    // invalid grid (a face without any neighbour, overlapping blocks, ...)
-    bool update_neighbors(std::string &err);
+    // invalid grid (a face without any neighbour, overlapping blocks, ...).
+    // With overlapping (a full tree: leaves and their ancestors) every
+    // existing same-level, finer and coarser neighbour is recorded, as
+    // find_neighbor with search_overlapping (find_neighbors.f90:18-215).
+    bool update_neighbors(std::string &err, bool overlapping = false);
     // maximum level difference across any face/edge/corner is 1
     bool graded() const;
     uint64_t treecode(int b) const;  // reference bit layout (y bit0, x bit1, z bit2)
@@ -80,6 +83,23 @@ struct SyncTable {
     int max_points = 0;                // largest receiver box
     int max_coarse = 0;                // largest shared-memory need of a prediction (doubles)
 };
+
+// Patch of relation r (1..168) from src to dst with level difference
+// lvl_diff = level(src) - level(dst), boxes in the full layout (ghost width
+// geo.g): receiver box from get_indices_of_ghost_patch of the inverse
+// relation, sender / buffer boxes from set_send_bounds.
+Patch make_patch(const Geometry &geo, int order_predictor, int relation, int lvl_diff, int gminus, int gplus, int src,
+                 int dst);
+// get_indices_of_modify_patch (neighborhood.f90:23-126), 0-based inclusive
+void modify_box0(const Geometry &geo, int relation, int Ns, int Ne, int gm, int gp, int lvl_diff, int lo[3], int hi[3]);
+// get_indices_of_ghost_patch (neighborhood.f90:158-327), 0-based inclusive
+void ghost_box0(const Geometry &geo, int relation, int gminus, int gplus, int lvl_diff, int lo[3], int hi[3]);
+int relation_inverse(int relation);
+// np_l / np_u (neighborhood.f90:439-500): relations of the same patch at
+// another level difference
+void relation_range(int relation, int lvl_diff, int &lo, int &hi);
+// neighborhood2patchID (neighborhood.f90:413-434)
+int relation_patch_id(int relation);
 
 // Build the ghost-sync table of one forest for the reference's
 // sync_ghosts_RHS_tree / sync_ghosts_tree semantics on a leaf-only grid.

@@ -113,8 +113,8 @@ __device__ __forceinline__ double interp_line(const double *c, const double *v, 
     return s;
 }
 
-__global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ patches, double *buf, BufGeo geo,
-                                                      int nc, int order_idx, int ncoef) {
+__global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ patches, const double *sbuf,
+                                                      double *buf, BufGeo geo, int nc, int order_idx, int ncoef) {
     extern __shared__ double sm[];
     const Patch p = patches[blockIdx.x];
     const int cx = p.shi[0] - p.slo[0] + 1, cy = p.shi[1] - p.slo[1] + 1, cz = p.shi[2] - p.slo[2] + 1;
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
     double *XY = X + ex * ny * nz;        // ex * ey * nz
     const long long npts = geo.npts();
     for (int c = 0; c < nc; c++) {
-        const double *src = buf + ((long long)p.src * nc + c) * npts;
+        const double *src = sbuf + ((long long)p.src * nc + c) * npts;
         double *dst = buf + ((long long)p.dst * nc + c) * npts;
         for (int i = threadIdx.x; i < ncp; i += blockDim.x) {
             const int x = i % cx, y = (i / cx) % cy, z = i / (cx * cy);
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict
 cudaError_t sync_init() { return init_predictor(); }
 
 cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_doubles, double *buf, BufGeo geo, int nc,
-                           int order_predictor, cudaStream_t s) {
+                           int order_predictor, cudaStream_t s, const double *src_buf) {
     if (npatch <= 0) return cudaSuccess;
     const size_t smem = sizeof(double) * (size_t)max_smem_doubles;
     static size_t attr = 0;
@@ -300,7 +300,8 @@ cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_double
         if (e != cudaSuccess) return e;
         attr = smem;
     }
-    predict_kernel<<<npatch, 256, smem, s>>>(patches, buf, geo, nc, order_predictor / 2 - 1, order_predictor);
+    predict_kernel<<<npatch, 256, smem, s>>>(patches, src_buf ? src_buf : buf, buf, geo, nc, order_predictor / 2 - 1,
+                                             order_predictor);
     return cudaGetLastError();
 }
 

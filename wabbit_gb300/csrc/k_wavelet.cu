@@ -490,6 +490,16 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
         sm[o] = point(line, 1, g + ix, ix);
     }
     __syncthreads();
+    if (MODE == 3) {
+        // the x pass results outside the interior rows/planes stay in the
+        // block, as the reference's FWT leaves them in u_d
+        for (int o = threadIdx.x; o < nx_out; o += kTpoThreads) {
+            const int ix = o % Bx, r = o / Bx;
+            const int yy = r % ny, zz = r / ny;
+            const bool inner = yy >= f && yy < f + By && (DIM == 2 || (zz >= f && zz < f + Bz));
+            if (!inner) ub[((long long)(z0 + zz) * geo.ny + (y0 + yy)) * geo.nx + g + ix] = sm[o];
+        }
+    }
     // y pass on the interior rows of every plane of the window
     double res[kTpoMaxPerThread];
     const int ny_out = Bx * By * nz;
@@ -523,6 +533,8 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
             if (o >= ny_out) continue;
             const int ix = o % Bx, iy = (o / Bx) % By, zz = o / (Bx * By);
             sm[((long long)zz * ny + (f + iy)) * Bx + ix] = res[k];
+            if (MODE == 3 && (zz < f || zz >= f + Bz))
+                ub[((long long)(z0 + zz) * geo.ny + (g + iy)) * geo.nx + (g + ix)] = res[k];
         }
         __syncthreads();
         const int nint = Bx * By * Bz;
@@ -604,10 +616,12 @@ static cudaError_t launch_tpo(int mode, int dim, const int *blk, int nblk, doubl
     if (dim == 2) {
         if (mode == 0) return go(tpo_kernel<2, 0>);
         if (mode == 1) return go(tpo_kernel<2, 1>);
+        if (mode == 3) return go(tpo_kernel<2, 3>);
         return go(tpo_kernel<2, 2>);
     }
     if (mode == 0) return go(tpo_kernel<3, 0>);
     if (mode == 1) return go(tpo_kernel<3, 1>);
+    if (mode == 3) return go(tpo_kernel<3, 3>);
     return go(tpo_kernel<3, 2>);
 }
 
@@ -657,6 +671,22 @@ cudaError_t launch_wavelet_decompose(int dim, const int *blk, int nblk, double *
         fwt_detail_kernel<3, true><<<nblk * nc, 256, smem, s>>>(a, nullptr, u);
     }
     return cudaGetLastError();
+}
+
+// FWT of whole blocks in the layout the reference's
+// waveletDecomposition_optimized_block leaves in u_d: interior in spaghetti
+// order, x-pass results on the ghost rows/planes of the filter window,
+// y-pass results on the ghost planes (3-D)
+cudaError_t launch_wavelet_decompose_window(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
+                                            int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    WaveletInfo w;
+    char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
+    if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
+    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
+    const int fmax = std::max(std::max(w.hd_lo, hd_hi), std::max(w.gd_lo, gd_hi));
+    if (fmax > geo.gb) return cudaErrorInvalidValue;
+    return launch_tpo(3, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, wavelet_x * 10 + wavelet_y, fmax, nullptr, s);
 }
 
 cudaError_t launch_wavelet_reconstruct(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,

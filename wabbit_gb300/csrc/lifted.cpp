@@ -1,0 +1,412 @@
+// lifted.cpp -- host planning of the full-tree adaptation with coarse
+// extension (see lifted.hpp).
+#include "lifted.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <unordered_map>
+
+namespace wg {
+
+bool LiftedTree::init(const Geometry &g, const WaveletInfo &w, int fd_max_size, int jmin, int jmax, int nleaf,
+                      const int *level, const int *coords, std::string &err) {
+    geo = g;
+    wav = w;
+    Jmin = jmin;
+    Jmax = jmax;
+    nleaves = nleaf;
+    if (!build_full_tree(g.dim, jmin, nleaf, level, coords, ft, err)) return false;
+    alive.assign(ft.size(), 1);
+    ref.assign(ft.size(), 0);
+    slot.assign(ft.size(), -1);
+    // coarse-extension widths: setup_wavelet (module_wavelets.f90:1341-1417);
+    // CDF24/26/28/46 are not built, so no extra WC width applies
+    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
+    const int hr_hi = w.hr_lo + (int)w.HR.size() - 1, gr_hi = w.gr_lo + (int)w.GR.size() - 1;
+    Nscl = std::max(std::abs(w.hd_lo) - 1, 0);
+    Nwcl = Nscl + std::abs(w.gd_lo);
+    Nreconl = Nwcl + std::abs(w.gr_lo);
+    Ndep2l = Nreconl + std::max((std::abs(w.hr_lo) + 1) / 2 - 1, 0);
+    Nscr = hd_hi;
+    Nwcr = Nscr + gd_hi;
+    Nreconr = Nwcr + gr_hi;
+    Ndep2r = Nreconr + (hr_hi + 1) / 2;
+    const int i2 = 2 * fd_max_size, dl = std::max(i2 - Nwcl, 0), dr = std::max(i2 - Nwcr, 0);
+    Nwcl += dl;
+    Nreconl += dl;
+    Ndep2l += dl;
+    Nwcr += dr;
+    Nreconr += dr;
+    Ndep2r += dr;
+    return true;
+}
+
+bool LiftedTree::update_metadata(std::string &err) {
+    Forest f;
+    f.dim = geo.dim;
+    f.Jmin = Jmin;
+    f.Jmax = Jmax;
+    index_.clear();
+    std::vector<int> lv, co;
+    for (int b = 0; b < size(); b++) {
+        if (!alive[b]) continue;
+        index_.push_back(b);
+        lv.push_back(ft.level[b]);
+        for (int a = 0; a < 3; a++) co.push_back(ft.coords[3 * b + a]);
+    }
+    f.set((int)index_.size(), lv.data(), co.data());
+    if (!f.update_neighbors(err, true)) return false;
+    nb_.assign(size_t(size()) * kNumRelations, -1);
+    for (size_t i = 0; i < index_.size(); i++)
+        for (int r = 0; r < kNumRelations; r++) {
+            const int n = f.nbr[i * kNumRelations + r];
+            nb_[size_t(index_[i]) * kNumRelations + r] = n < 0 ? -1 : index_[n];
+        }
+    return true;
+}
+
+// updateFamily_tree (LIB/MESH/updateFamily_tree.f90:16-56): no mother on
+// Jmin, no daughters on Jmax
+int LiftedTree::mother(int b) const {
+    if (ft.level[b] == Jmin) return -1;
+    const int m = ft.mother[b];
+    return (m >= 0 && alive[m]) ? m : -1;
+}
+
+// block_is_leaf / block_is_root / block_has_valid_neighbor
+// (LIB/MPI/block_relations.f90:2-71)
+bool LiftedTree::is_leaf(int b, bool check_empty) const {
+    if (ft.level[b] == Jmax) return true;
+    bool any = false;
+    for (int k = 0; k < 8; k++) {
+        const int d = ft.daughters[8 * b + k];
+        if (d >= 0 && alive[d]) any = true;
+    }
+    if (!any) return true;
+    if (!check_empty) return false;
+    for (int k = 0; k < 8; k++) {
+        const int d = ft.daughters[8 * b + k];
+        if (d >= 0 && alive[d] && ref[d] != kRefTmpEmpty) return false;
+    }
+    return true;
+}
+
+bool LiftedTree::is_root(int b, bool check_empty) const {
+    const int m = mother(b);
+    if (m < 0) return true;
+    return check_empty && ref[m] == kRefTmpEmpty;
+}
+
+bool LiftedTree::has_valid_neighbor(int b, int relation, int lvl_diff) const {
+    int lo, hi;
+    relation_range(relation, lvl_diff, lo, hi);
+    for (int r = lo; r <= hi; r++) {
+        const int n = nbr(b, r);
+        if (n >= 0 && ref[n] != kRefTmpEmpty) return true;
+    }
+    return false;
+}
+
+namespace {
+struct Box {
+    int lo[3], hi[3];
+};
+inline bool overlap(const Box &a, const Box &b) {
+    for (int d = 0; d < 3; d++)
+        if (a.hi[d] < b.lo[d] || b.hi[d] < a.lo[d]) return false;
+    return true;
+}
+// boxes touched by a patch in the current wave, per arena slot
+struct WaveBoxes {
+    std::unordered_map<int, std::vector<Box>> rd, wr;
+    bool hits(const std::unordered_map<int, std::vector<Box>> &m, int s, const Box &b) const {
+        auto it = m.find(s);
+        if (it == m.end()) return false;
+        for (const Box &x : it->second)
+            if (overlap(x, b)) return true;
+        return false;
+    }
+    void clear() {
+        rd.clear();
+        wr.clear();
+    }
+};
+int pred_need_of(const Patch &p, int order_predictor) {
+    const int h = order_predictor - 1;
+    const int cx = p.shi[0] - p.slo[0] + 1, cy = p.shi[1] - p.slo[1] + 1, cz = p.shi[2] - p.slo[2] + 1;
+    const int Fy = 2 * cy - 1, Fz = 2 * cz - 1;
+    const int ex = p.rhi[0] - p.rlo[0] + 1, ey = p.rhi[1] - p.rlo[1] + 1, ez = p.rhi[2] - p.rlo[2] + 1;
+    int yw0 = std::max(0, p.blo[1] - h), yw1 = std::min(Fy - 1, p.blo[1] + ey - 1 + h);
+    yw0 += yw0 & 1;
+    yw1 -= yw1 & 1;
+    int zw0 = std::max(0, p.blo[2] - h), zw1 = std::min(Fz - 1, p.blo[2] + ez - 1 + h);
+    zw0 += zw0 & 1;
+    zw1 -= zw1 & 1;
+    const int ny = (yw1 - yw0) / 2 + 1, nz = (zw1 - zw0) / 2 + 1;
+    return cx * cy * cz + ex * ny * nz + ex * ey * nz;
+}
+}  // namespace
+
+// sync_ghosts_generic with the single-rank send logic of
+// prepare_ghost_synch_metadata (synchronize_ghosts_generic.f90:352-694)
+void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) const {
+    waves.clear();
+    const int nstages = wav.lifted ? 3 : 2, unl = wav.lifted ? 0 : 1;
+    for (int istage = 1; istage <= nstages; istage++) {
+        SyncWave cur;
+        cur.stage = istage;
+        WaveBoxes wb;
+        std::unordered_map<int, int> entry_of;   // (sender, source) -> filter entry of this wave
+        auto flush = [&]() {
+            const bool any = !cur.copy_blk.empty() || !cur.copy_tmp.empty() || !cur.restrict_.empty() ||
+                             !cur.pred_blk.empty() || !cur.pred_tmp.empty();
+            if (any) waves.push_back(std::move(cur));
+            cur = SyncWave();
+            cur.stage = istage;
+            wb.clear();
+            entry_of.clear();
+        };
+        for (int b = 0; b < size(); b++) {
+            if (!alive[b]) continue;
+            if (sp.base == 2 && !is_leaf(b, false)) continue;
+            if (ref[b] == kRefTmpEmpty) continue;
+            const int level = ft.level[b];
+            for (int r = 1; r <= kNumRelations; r++) {
+                const int n = nbr(b, r);
+                if (n < 0) continue;
+                const int lvl_diff = level - ft.level[n];
+                if (ref[n] == kRefTmpEmpty) continue;
+                const bool s1 = istage == 1 && lvl_diff == 0;
+                const bool s2 = istage == 2 - unl && lvl_diff == +1;
+                const bool s3 = istage == 3 - unl && lvl_diff == -1;
+                bool send = false;
+                switch (sp.base) {
+                case 1:
+                    if (s1 || s2 || s3) {
+                        send = true;
+                        if (lvl_diff == -1 && !is_leaf(b, true)) send = false;
+                        if (lvl_diff == +1 && !is_root(b, true)) send = false;
+                    }
+                    break;
+                case 2:
+                    if (s1 || s2 || s3) {
+                        send = true;
+                        if (lvl_diff >= 0 && has_valid_neighbor(b, r, -1)) send = false;
+                        else if (lvl_diff == +1 && has_valid_neighbor(b, r, 0)) send = false;
+                    }
+                    break;
+                case 3:
+                    if (s1 || s3) {
+                        send = true;
+                        if (lvl_diff != 0 && !is_leaf(b, true)) send = false;
+                    }
+                    break;
+                case 4:
+                    if (s1 || s2) {
+                        send = true;
+                        if (lvl_diff != 0 && !is_root(b, true)) send = false;
+                    }
+                    break;
+                default:
+                    send = s1;
+                }
+                if (send && sp.by_ref) send = sp.s_ref == ref[n];
+                if (send && sp.by_level) send = sp.s_level == ft.level[n];
+                if (!send) continue;
+                // hvy_tmp_usage (xfer_block_data.f90:376-395)
+                bool tmp_rp = false, tmp_same = false;
+                if (sp.tmp_usage == 1 && ref[b] != sp.s_ref) tmp_rp = tmp_same = true;
+                if (sp.tmp_usage == 2) tmp_rp = true;
+                Patch p = make_patch(geo, wav.order_predictor, r, lvl_diff, sp.gminus, sp.gplus, slot[b], slot[n]);
+                Box w{{p.rlo[0], p.rlo[1], p.rlo[2]}, {p.rhi[0], p.rhi[1], p.rhi[2]}};
+                Box rd{{0, 0, 0}, {-1, -1, -1}};
+                bool reads_blk = false;
+                if (lvl_diff == 0) {
+                    reads_blk = !tmp_same;
+                    for (int d = 0; d < 3; d++) {
+                        rd.lo[d] = p.slo[d];
+                        rd.hi[d] = p.slo[d] + p.rhi[d] - p.rlo[d];
+                    }
+                } else if (lvl_diff == -1) {
+                    reads_blk = !tmp_rp;
+                    for (int d = 0; d < 3; d++) {
+                        rd.lo[d] = p.slo[d];
+                        rd.hi[d] = p.shi[d];
+                    }
+                }
+                // a new wave where this patch would see, or clobber, a box an
+                // earlier patch of the wave touches
+                const bool conflict = (reads_blk && wb.hits(wb.wr, p.src, rd)) || wb.hits(wb.rd, p.dst, w) ||
+                                      wb.hits(wb.wr, p.dst, w);
+                if (conflict) flush();
+                if (reads_blk) wb.rd[p.src].push_back(rd);
+                wb.wr[p.dst].push_back(w);
+                if (lvl_diff == 0) {
+                    (tmp_same ? cur.copy_tmp : cur.copy_blk).push_back(p);
+                } else if (lvl_diff == -1) {
+                    (tmp_rp ? cur.pred_tmp : cur.pred_blk).push_back(p);
+                    cur.max_coarse = std::max(cur.max_coarse, pred_need_of(p, wav.order_predictor));
+                } else {
+                    const int key = 2 * b + (tmp_rp ? 1 : 0);
+                    auto it = entry_of.find(key);
+                    int e;
+                    if (it == entry_of.end()) {
+                        e = (int)cur.filters.size();
+                        entry_of[key] = e;
+                        cur.filters.push_back({slot[b], tmp_rp ? 1 : 0});
+                        // SC next to a coarser or finer neighbour without a
+                        // same-level one are copied, not filtered
+                        const int g = geo.g;
+                        for (int r2 = 1; r2 <= kNumRelations; r2++) {
+                            const int n2 = nbr(b, r2);
+                            if (n2 < 0 || !sp.filter) continue;
+                            const int ld = level - ft.level[n2];
+                            if ((ld == 1 || ld == -1) && is_leaf(b, false) && !has_valid_neighbor(b, r2, 0)) {
+                                int lo[3], hi[3];
+                                modify_box0(geo, r2, Nscl, Nscr, g, g, +1, lo, hi);
+                                ScBox sb;
+                                sb.entry = e;
+                                bool empty = false;
+                                for (int d = 0; d < 3; d++) {
+                                    if (d >= geo.dim) {
+                                        sb.lo[d] = sb.hi[d] = 0;
+                                        continue;
+                                    }
+                                    // SC lattice g + 2m (0-based); the box starts on it
+                                    const int first = lo[d] + ((lo[d] - g) & 1);
+                                    int last = hi[d] - ((hi[d] - g) & 1);
+                                    if (last > g + geo.Bs[d] - 2) last = g + geo.Bs[d] - 2;
+                                    sb.lo[d] = (int16_t)((first - g) / 2);
+                                    sb.hi[d] = (int16_t)((last - g) / 2);
+                                    if (first > last || first < g) empty = true;
+                                }
+                                if (!empty) cur.ce_copies.push_back(sb);
+                            }
+                        }
+                    } else {
+                        e = it->second;
+                    }
+                    p.src = e;
+                    cur.restrict_.push_back(p);
+                }
+            }
+        }
+        flush();
+    }
+}
+
+// coarseExtensionManipulateWC_block (module_wavelets.f90:877-962): zero the
+// WC in the Nwcl/Nwcr patch and in the ghost patch, SC skipped by parity
+void LiftedTree::ce_clear_wc(int b, int relation, std::vector<BoxOp> &ops) const {
+    const int g = geo.g, dim = geo.dim;
+    for (int set = 1; set <= 2; set++) {
+        int lo[3], hi[3];
+        if (set == 1) modify_box0(geo, relation, Nwcl, Nwcr, g, g, +1, lo, hi);
+        else ghost_box0(geo, relation, g, g, +1, lo, hi);
+        if (dim == 2) lo[2] = hi[2] = 0;
+        int io[3] = {0, 0, 0};
+        for (int d = 0; d < dim; d++) io[d] = ((g + lo[d]) % 2 + 2) % 2;
+        auto add = [&](const int first[3], const int step[3]) {
+            BoxOp o;
+            std::memset(&o, 0, sizeof(o));
+            o.slot = slot[b];
+            o.op = 0;
+            for (int d = 0; d < 3; d++) {
+                if (first[d] > hi[d]) return;
+                o.lo[d] = (int16_t)first[d];
+                o.hi[d] = (int16_t)hi[d];
+                o.step[d] = (int16_t)step[d];
+            }
+            ops.push_back(o);
+        };
+        {
+            const int f[3] = {lo[0] + 1 - io[0], lo[1] + io[1], lo[2] + io[2]}, s[3] = {2, 2, 2};
+            add(f, s);
+        }
+        {
+            const int f[3] = {lo[0], lo[1] + 1 - io[1], lo[2] + io[2]}, s[3] = {1, 2, 2};
+            add(f, s);
+        }
+        if (dim == 3) {
+            const int f[3] = {lo[0], lo[1], lo[2] + 1 - io[2]}, s[3] = {1, 1, 2};
+            add(f, s);
+        }
+    }
+}
+
+// coarseExtensionManipulateSC_block (module_wavelets.f90:966-1028) with the
+// copy taken from hvy_tmp
+void LiftedTree::ce_copy_sc(int b, int relation, std::vector<BoxOp> &ops) const {
+    const int g = geo.g, dim = geo.dim;
+    int lo[3], hi[3];
+    modify_box0(geo, relation, Nscl, Nscr, g, g, +1, lo, hi);
+    BoxOp o;
+    std::memset(&o, 0, sizeof(o));
+    o.slot = slot[b];
+    o.op = 1;
+    for (int d = 0; d < 3; d++) {
+        const int io = d < dim ? ((g + lo[d]) % 2 + 2) % 2 : 0;
+        if (lo[d] + io > hi[d]) return;
+        o.lo[d] = (int16_t)(lo[d] + io);
+        o.hi[d] = (int16_t)hi[d];
+        o.step[d] = 2;
+    }
+    ops.push_back(o);
+}
+
+void LiftedTree::plan_ce_modify(int ce_case, int s_level, int s_ref, bool clear_wc, bool copy_sc,
+                                std::vector<BoxOp> &ops) const {
+    for (int b = 0; b < size(); b++) {
+        if (!alive[b]) continue;
+        const int lv = ft.level[b];
+        if ((ce_case == 1 || ce_case == 3) && lv != s_level) continue;
+        if ((ce_case == 2 || ce_case == 3) && ref[b] != s_ref) continue;
+        if (!is_leaf(b, false)) continue;
+        for (int r = 1; r <= kNumRelations; r++) {
+            const int n = nbr(b, r);
+            if (n < 0) continue;
+            if (ft.level[n] < lv && !(has_valid_neighbor(b, r, 0) || has_valid_neighbor(b, r, -1))) {
+                if (clear_wc) ce_clear_wc(b, r, ops);
+                if (copy_sc) ce_copy_sc(b, r, ops);
+            }
+        }
+    }
+}
+
+void LiftedTree::security_candidates(std::vector<ZoneItem> &items) const {
+    items.clear();
+    const int g = geo.g;
+    for (int b = 0; b < size(); b++) {
+        if (!alive[b] || ref[b] != 0) continue;
+        for (int r = 1; r <= kNumRelations; r++) {
+            const int n = nbr(b, r);
+            if (n < 0 || ref[n] != -1 || ft.level[n] != ft.level[b]) continue;
+            ZoneItem it;
+            it.block = b;
+            it.relation = r;
+            modify_box0(geo, r, Nwcl, Nwcr, g, g, 0, it.lo, it.hi);
+            for (int d = 0; d < 3; d++) it.io[d] = d < geo.dim ? ((g + it.lo[d]) % 2 + 2) % 2 : 0;
+            items.push_back(it);
+        }
+    }
+}
+
+void LiftedTree::security_apply(const std::vector<ZoneItem> &items, const std::vector<char> &significant) {
+    constexpr int kTmpStatus = 17;
+    for (size_t i = 0; i < items.size(); i++)
+        if (significant[i]) ref[items[i].block] |= (1 << (relation_patch_id(items[i].relation) + 3)) | (1 << 30);
+    auto flag_bit = [](int v) { return (v >> 30) & 1; };
+    for (int b = 0; b < size(); b++) {
+        if (!alive[b] || ref[b] != -1) continue;
+        for (int r = 1; r <= kNumRelations; r++) {
+            const int n = nbr(b, r);
+            if (n < 0 || !(ref[n] > 0) || ft.level[n] != ft.level[b]) continue;
+            const int pid = relation_patch_id(relation_inverse(r));
+            if (flag_bit(ref[n]) && ((ref[n] >> (pid + 3)) & 1)) ref[b] = kTmpStatus;
+        }
+    }
+    for (int b = 0; b < size(); b++)
+        if (alive[b] && ref[b] > 0 && (ref[b] == kTmpStatus || flag_bit(ref[b]))) ref[b] = 0;
+}
+
+}  // namespace wg
