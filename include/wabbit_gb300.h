@@ -153,19 +153,33 @@ int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const do
 int wg_set_time(wg_ctx *ctx, int tree, double time);
 int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);
 
-/* adapt_tree (LIB/MESH/adapt_tree.f90:11-255) for unlifted wavelets (CDF X0,
- * whose adaptation uses neither coarse extension nor security zone): full
- * tree with every ancestor down to Jmin, mothers filled with their
- * daughters' scaling coefficients (sync_D2M), coarsening indicator on every
- * block (WG_ADAPT_THRESHOLD: threshold-state-vector with eps_use = eps *
- * norm per component; WG_ADAPT_EVERYWHERE: every leaf), respectJmaxJmin,
- * completeness, gradedness (ensureGradedness_tree with check_daughters),
- * deletion and pruning; the grid and the state are replaced, *nblk_out
- * receives the new block count (wg_get_grid returns the new grid). Masks are
- * dropped. Needs free arena slots for the mothers (about nblk/(2^d-1)). */
+/* adapt_tree (LIB/MESH/adapt_tree.f90:11-255): full tree with every
+ * ancestor down to Jmin, mothers filled with their daughters' scaling
+ * coefficients (sync_D2M), coarsening indicator on every block
+ * (WG_ADAPT_THRESHOLD: threshold-state-vector with eps_use = eps * norm per
+ * component; WG_ADAPT_EVERYWHERE: every leaf), respectJmaxJmin, completeness,
+ * gradedness (ensureGradedness_tree with check_daughters), deletion and
+ * pruning; the grid and the state are replaced, *nblk_out receives the new
+ * block count (wg_get_grid returns the new grid). Masks are dropped. Needs
+ * free arena slots for the mothers (about nblk/(2^d-1)).
+ * Unlifted wavelets (CDF X0): the original values are kept (decimation).
+ * Lifted wavelets (CDF XY): the reference's coarse-extension algorithm --
+ * filtered ghost sync, level-by-level FWT of the full tree
+ * (wavelet_decompose_full_tree), coarse extension, the indicator on the
+ * decomposition, the security zone (addSecurityZone_CE_tree), and the
+ * reconstruction of the blocks at coarse/fine interfaces
+ * (wavelet_reconstruct_full_tree_CEoptimized), then a filtered ghost sync of
+ * the new grid. It allocates, on first use, a second block arena of the size
+ * of the state (hvy_tmp). */
 #define WG_ADAPT_THRESHOLD 0
 #define WG_ADAPT_EVERYWHERE 1
 int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *nblk_out);
+/* Phase times of the last lifted adaptation in ms: [0] host planning, [1]
+ * ghost syncs, [2] FWT, [3] coarse extension and D2M copies, [4] indicator and
+ * security zone, [5] IWT, [6] hvy_tmp block copies, [7] total. enable 1 / 0
+ * switches timing on / off for later calls (it synchronises the stream at
+ * every phase boundary), -1 leaves it; ms_out may be NULL. */
+int wg_adapt_profile(wg_ctx *ctx, int enable, double *ms_out, int n);
 /* One-level wavelet transforms of every block of the tree, in place on the
  * state (interior points; the ghost nodes must be synchronised first, for the
  * inverse with the decomposed data):

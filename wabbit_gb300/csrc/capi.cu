@@ -16,6 +16,7 @@
 //   mask interior only, 6 components, only for blocks that carry a mask;
 //        the FP32-pipe precision adds a double-float copy (5 components)
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -167,6 +168,8 @@ struct wg_ctx {
     int precision = WG_RHS_FP64;        // WG_RHS_FP32: double-float stencils on the FP32 units
     DevArray<int> d_tree_ids;
     double *T = nullptr;                // hvy_tmp arena of the lifted adaptation (slot-indexed like A)
+    bool adapt_profile = false;         // time the phases of the lifted adaptation
+    double adapt_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     double *staging = nullptr;          // compact interior staging buffer
     size_t staging_bytes = 0;
     cudaGraph_t graph = nullptr;
@@ -1572,6 +1575,20 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         if (keep.back()->upload(v.data(), v.size(), ctx->stream) != cudaSuccess) return nullptr;
         return keep.back()->p;
     };
+    // phase timing (wg_adapt_profile): host planning, then device phases
+    // bracketed by stream synchronisations
+    enum { kPlan, kSync, kFwt, kCe, kFlags, kRecon, kCopy, kTotal };
+    std::fill(ctx->adapt_ms, ctx->adapt_ms + 8, 0.0);
+    using clk = std::chrono::steady_clock;
+    const auto t_start = clk::now();
+    auto tic = [&]() {
+        if (ctx->adapt_profile) cudaStreamSynchronize(ctx->stream);
+        return clk::now();
+    };
+    auto toc = [&](int phase, clk::time_point t0) {
+        if (ctx->adapt_profile) cudaStreamSynchronize(ctx->stream);
+        ctx->adapt_ms[phase] += std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    };
     cudaError_t e = lifted_set_filter(w.HD.data(), w.hd_lo, (int)w.HD.size(), ctx->stream);
     const int hx = Bs[0] / 2, hy = Bs[1] / 2, hz = dim == 3 ? Bs[2] / 2 : 1;
     auto run_waves = [&](const std::vector<SyncWave> &waves) -> cudaError_t {
@@ -1614,14 +1631,24 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     };
     auto sync_spec = [&](SyncSpecL sp) -> cudaError_t {
         std::vector<SyncWave> waves;
+        auto t0 = clk::now();
         L.plan_sync(sp, waves);
-        return run_waves(waves);
+        ctx->adapt_ms[kPlan] += std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+        t0 = tic();
+        const cudaError_t r = run_waves(waves);
+        toc(kSync, t0);
+        return r;
     };
     auto ce = [&](int ce_case, int s_level, int s_ref, bool clear_wc, bool copy_sc) -> cudaError_t {
         std::vector<BoxOp> ops;
+        auto t0 = clk::now();
         L.plan_ce_modify(ce_case, s_level, s_ref, clear_wc, copy_sc, ops);
+        ctx->adapt_ms[kPlan] += std::chrono::duration<double, std::milli>(clk::now() - t0).count();
         if (ops.empty()) return cudaSuccess;
-        return launch_boxop(up(kb, ops), (int)ops.size(), ctx->A, ctx->T, gA, nc, ctx->stream);
+        t0 = tic();
+        const cudaError_t r = launch_boxop(up(kb, ops), (int)ops.size(), ctx->A, ctx->T, gA, nc, ctx->stream);
+        toc(kCe, t0);
+        return r;
     };
     auto slots_where = [&](auto pred) {
         std::vector<int> v;
@@ -1664,10 +1691,14 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         const std::vector<int> dec = slots_where([&](int b) { return L.ref[b] == -1; });
         if (e == cudaSuccess && !dec.empty()) {
             const int *d_dec = up(ki, dec);
+            auto t0 = tic();
             e = launch_blockcopy(d_dec, (int)dec.size(), ctx->A, ctx->T, per_block, ctx->stream);
+            toc(kCopy, t0);
+            t0 = tic();
             if (e == cudaSuccess)
                 e = launch_wavelet_decompose_window(dim, d_dec, (int)dec.size(), ctx->A, gA, Bs[0], Bs[1], Bs[2], nc,
                                                     w.X, w.Y, ctx->stream);
+            toc(kFwt, t0);
         }
         if (e == cudaSuccess) e = ce(2, 0, -1, true, true);
         for (int b = 0; b < nt; b++) {
@@ -1676,12 +1707,15 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         }
         std::vector<Patch> d2m, gh;
         mother_patches(L.ft, ctx->geo, level - 1, L.slot, d2m, gh);
+        auto t0 = tic();
         if (e == cudaSuccess && !d2m.empty())
             e = launch_sync(up(kp, d2m), (int)d2m.size(), ctx->A, gA, nc, w.order_predictor, ctx->stream);
+        toc(kCe, t0);
     }
     std::fill(L.ref.begin(), L.ref.end(), 0);
     // coarseningIndicator_tree on the decomposition, security zone
     std::vector<int> flags(nt, 0);
+    const auto t_flags = tic();
     if (e == cudaSuccess && thr) {
         std::vector<int> all(L.slot.begin(), L.slot.end());
         std::vector<int> tsvc(t->cfg.threshold_state_vector_component, t->cfg.threshold_state_vector_component + nc);
@@ -1740,6 +1774,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     } else if (!thr) {
         for (int b = 0; b < nb; b++) flags[b] = kFlagCoarsen;   // "everywhere": the leaves
     }
+    toc(kFlags, t_flags);
     if (e != cudaSuccess) return fail_restore(e, WG_ECUDA);
     std::vector<int> leaves;
     adapt_decide(L.ft, flags, leaves);
@@ -1765,11 +1800,15 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         const std::vector<int> rec = slots_where([&](int b) { return on_level(b) && L.ref[b] == -1; });
         const std::vector<int> keep = slots_where([&](int b) { return on_level(b) && L.ref[b] != -1; });
         cudaError_t r = cudaSuccess;
+        auto t0 = tic();
         if (!rec.empty())
             r = launch_wavelet_reconstruct(dim, up(ki, rec), (int)rec.size(), ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X,
                                            w.Y, ctx->stream);
+        toc(kRecon, t0);
+        t0 = tic();
         if (r == cudaSuccess && !keep.empty())
             r = launch_blockcopy(up(ki, keep), (int)keep.size(), ctx->T, ctx->A, per_block, ctx->stream);
+        toc(kCopy, t0);
         return r;
     };
     SyncSpecL rs;
@@ -1833,7 +1872,16 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     if ((st = upload_lists(ctx, *t))) return st;
     ctx->grid_version++;
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    ctx->adapt_ms[kTotal] = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
     if (nblk_out) *nblk_out = nn;
+    return WG_OK;
+}
+
+int wg_adapt_profile(wg_ctx *ctx, int enable, double *ms_out, int n) {
+    if (!ctx) return WG_EINVAL;
+    if (enable >= 0) ctx->adapt_profile = enable != 0;
+    if (ms_out)
+        for (int i = 0; i < n && i < 8; i++) ms_out[i] = ctx->adapt_ms[i];
     return WG_OK;
 }
 

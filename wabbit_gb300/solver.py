@@ -254,7 +254,9 @@ class Forest:
 
     def adapt(self, eps_use=None, everywhere: bool = False) -> int:
         """adapt_tree (coarsening) with the threshold-state-vector indicator
-        (eps_use = eps * norm per component) or on every leaf; CDF X0 only.
+        (eps_use = eps * norm per component) or on every leaf. CDF X0: full
+        tree by decimation; CDF XY: full-tree FWT with coarse extension,
+        security zone and reconstruction at the coarse/fine interfaces.
         Replaces grid and state, drops masks, returns the new block count."""
         n = ctypes.c_int()
         if everywhere:
@@ -263,6 +265,14 @@ class Forest:
             e = np.ascontiguousarray(np.broadcast_to(np.asarray(eps_use, np.float64), (self.cfg.neq,)))
             capi.check(self.L.wg_adapt(self.ctx.h, self.tree, _p(e), 0, ctypes.byref(n)))
         return n.value
+
+    def adapt_profile(self, enable=None):
+        """Phase times (ms) of the last lifted adaptation: planning, syncs,
+        FWT, coarse extension + D2M, indicator + security zone, IWT, block
+        copies, total; enable switches the phase timing for later calls."""
+        out = np.zeros(8)
+        capi.check(self.L.wg_adapt_profile(self.ctx.h, -1 if enable is None else int(bool(enable)), _p(out), 8))
+        return dict(zip(("plan", "sync", "fwt", "ce_d2m", "flags", "iwt", "copy", "total"), out.tolist()))
 
     def refine_everywhere(self):
         capi.check(self.L.wg_refine_everywhere(self.ctx.h, self.tree))
