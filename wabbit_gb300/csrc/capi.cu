@@ -1787,14 +1787,11 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     e = ce(0, 0, 0, true, false);
     for (int b = 0; b < nt; b++) {
         if (!L.alive[b] || !L.is_leaf(b, false)) continue;
-        for (int r = 1; r <= kNumRelations; r++) {
-            const int n = L.nbr(b, r);
-            if (n < 0) continue;
-            if (L.ft.level[n] < L.ft.level[b] && !(L.has_valid_neighbor(b, r, 0) || L.has_valid_neighbor(b, r, -1))) {
+        L.for_neighbors(b, [&](int r, int n) {
+            if (L.ref[b] != -1 && L.ft.level[n] < L.ft.level[b] &&
+                !(L.has_valid_neighbor(b, r, 0) || L.has_valid_neighbor(b, r, -1)))
                 L.ref[b] = -1;
-                break;
-            }
-        }
+        });
     }
     auto reconstruct = [&](auto on_level) -> cudaError_t {
         const std::vector<int> rec = slots_where([&](int b) { return on_level(b) && L.ref[b] == -1; });

@@ -87,10 +87,18 @@ struct RelInfo {
     int half[3];
 };
 
+struct RelTable {
+    RelInfo t[57];
+    RelTable();
+};
+
+// built once (a function-local static: thread-safe initialisation)
 static const RelInfo *rel_table() {
-    static RelInfo t[57];
-    static bool init = false;
-    if (init) return t;
+    static const RelTable table;
+    return table.t;
+}
+
+RelTable::RelTable() {
     auto in = [](int r, std::initializer_list<int> l) {
         for (int v : l) if (v == r) return true;
         return false;
@@ -111,13 +119,32 @@ static const RelInfo *rel_table() {
         if (in(r, {3, 4, 7, 8, 11, 12, 15, 16, 26, 28, 30, 32})) x.half[2] = +1;
         if (in(r, {1, 2, 5, 6, 9, 10, 13, 14, 25, 27, 29, 31})) x.half[2] = -1;
     }
-    init = true;
-    return t;
 }
 
 // relation id (1..56) of a direction d[3] and, for finer/coarser neighbours,
 // the part index k (0..3) along the free directions (find_neighbors.f90:54-104)
+static int relation_of_scan(const int d[3], int part, int dim);
+
+// memoised per (dim, direction, part); the table is built once, thread-safe
+struct RelMemo {
+    int v[2][27][4];
+    RelMemo() {
+        for (int dm = 2; dm <= 3; dm++)
+            for (int k = 0; k < 27; k++)
+                for (int p = 0; p < 4; p++) {
+                    const int dd[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
+                    v[dm - 2][k][p] = relation_of_scan(dd, p, dm);
+                }
+    }
+};
+
 static int relation_of(const int d[3], int part, int dim) {
+    static const RelMemo memo;
+    const int k = (d[0] + 1) + 3 * (d[1] + 1) + 9 * ((dim == 3 ? d[2] : 0) + 1);
+    return memo.v[dim - 2][k][part & 3];
+}
+
+static int relation_of_scan(const int d[3], int part, int dim) {
     const RelInfo *t = rel_table();
     // part bit i belongs to the i-th free direction in x,y,z order
     int free_rank[3] = {-1, -1, -1}, nfree = 0;
@@ -143,7 +170,21 @@ static int relation_of(const int d[3], int part, int dim) {
     return -1;
 }
 
+static int inverse_relation_scan(int r);
+
+struct InvMemo {
+    int v[169];
+    InvMemo() {
+        for (int r = 1; r <= 168; r++) v[r] = inverse_relation_scan(r);
+    }
+};
+
 static int inverse_relation(int r) {
+    static const InvMemo memo;
+    return memo.v[r];
+}
+
+static int inverse_relation_scan(int r) {
     const RelInfo *t = rel_table();
     int base = (r - 1) % 56 + 1, range = (r - 1) / 56;
     int inv = -1;

@@ -62,6 +62,17 @@ bool LiftedTree::update_metadata(std::string &err) {
             const int n = f.nbr[i * kNumRelations + r];
             nb_[size_t(index_[i]) * kNumRelations + r] = n < 0 ? -1 : index_[n];
         }
+    adj_begin_.assign(size() + 1, 0);
+    adj_.clear();
+    for (int b = 0; b < size(); b++) {
+        adj_begin_[b] = (int)adj_.size();
+        if (!alive[b]) continue;
+        for (int r = 1; r <= kNumRelations; r++) {
+            const int n = nbr(b, r);
+            if (n >= 0) adj_.push_back({r, n});
+        }
+    }
+    adj_begin_[size()] = (int)adj_.size();
     return true;
 }
 
@@ -152,6 +163,26 @@ int pred_need_of(const Patch &p, int order_predictor) {
 void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) const {
     waves.clear();
     const int nstages = wav.lifted ? 3 : 2, unl = wav.lifted ? 0 : 1;
+    // one pass over the senders: the candidate patches of every stage in
+    // sender-major order, after the cheap receiver filters
+    struct Cand {
+        int b, r, n, lvl_diff;
+    };
+    std::vector<std::vector<Cand>> cand(nstages + 1);
+    for (int b = 0; b < size(); b++) {
+        if (!alive[b]) continue;
+        if (sp.base == 2 && !is_leaf(b, false)) continue;
+        if (ref[b] == kRefTmpEmpty) continue;
+        const int level = ft.level[b];
+        for_neighbors(b, [&](int r, int n) {
+            if (ref[n] == kRefTmpEmpty) return;
+            if (sp.by_ref && ref[n] != sp.s_ref) return;
+            if (sp.by_level && ft.level[n] != sp.s_level) return;
+            const int lvl_diff = level - ft.level[n];
+            const int stage = lvl_diff == 0 ? 1 : lvl_diff == +1 ? 2 - unl : 3 - unl;
+            cand[stage].push_back({b, r, n, lvl_diff});
+        });
+    }
     for (int istage = 1; istage <= nstages; istage++) {
         SyncWave cur;
         cur.stage = istage;
@@ -166,129 +197,107 @@ void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) co
             wb.clear();
             entry_of.clear();
         };
-        for (int b = 0; b < size(); b++) {
-            if (!alive[b]) continue;
-            if (sp.base == 2 && !is_leaf(b, false)) continue;
-            if (ref[b] == kRefTmpEmpty) continue;
+        for (const Cand &cd : cand[istage]) {
+            const int b = cd.b, r = cd.r, lvl_diff = cd.lvl_diff;
             const int level = ft.level[b];
-            for (int r = 1; r <= kNumRelations; r++) {
-                const int n = nbr(b, r);
-                if (n < 0) continue;
-                const int lvl_diff = level - ft.level[n];
-                if (ref[n] == kRefTmpEmpty) continue;
-                const bool s1 = istage == 1 && lvl_diff == 0;
-                const bool s2 = istage == 2 - unl && lvl_diff == +1;
-                const bool s3 = istage == 3 - unl && lvl_diff == -1;
-                bool send = false;
-                switch (sp.base) {
-                case 1:
-                    if (s1 || s2 || s3) {
-                        send = true;
-                        if (lvl_diff == -1 && !is_leaf(b, true)) send = false;
-                        if (lvl_diff == +1 && !is_root(b, true)) send = false;
-                    }
-                    break;
-                case 2:
-                    if (s1 || s2 || s3) {
-                        send = true;
-                        if (lvl_diff >= 0 && has_valid_neighbor(b, r, -1)) send = false;
-                        else if (lvl_diff == +1 && has_valid_neighbor(b, r, 0)) send = false;
-                    }
-                    break;
-                case 3:
-                    if (s1 || s3) {
-                        send = true;
-                        if (lvl_diff != 0 && !is_leaf(b, true)) send = false;
-                    }
-                    break;
-                case 4:
-                    if (s1 || s2) {
-                        send = true;
-                        if (lvl_diff != 0 && !is_root(b, true)) send = false;
-                    }
-                    break;
-                default:
-                    send = s1;
+            bool send = false;
+            switch (sp.base) {
+            case 1:
+                send = true;
+                if (lvl_diff == -1 && !is_leaf(b, true)) send = false;
+                if (lvl_diff == +1 && !is_root(b, true)) send = false;
+                break;
+            case 2:
+                send = true;
+                if (lvl_diff >= 0 && has_valid_neighbor(b, r, -1)) send = false;
+                else if (lvl_diff == +1 && has_valid_neighbor(b, r, 0)) send = false;
+                break;
+            case 3:
+                send = lvl_diff != +1;
+                if (send && lvl_diff != 0 && !is_leaf(b, true)) send = false;
+                break;
+            case 4:
+                send = lvl_diff != -1;
+                if (send && lvl_diff != 0 && !is_root(b, true)) send = false;
+                break;
+            default:
+                send = lvl_diff == 0;
+            }
+            if (!send) continue;
+            // hvy_tmp_usage (xfer_block_data.f90:376-395)
+            bool tmp_rp = false, tmp_same = false;
+            if (sp.tmp_usage == 1 && ref[b] != sp.s_ref) tmp_rp = tmp_same = true;
+            if (sp.tmp_usage == 2) tmp_rp = true;
+            Patch p = make_patch(geo, wav.order_predictor, r, lvl_diff, sp.gminus, sp.gplus, slot[b], slot[cd.n]);
+            Box w{{p.rlo[0], p.rlo[1], p.rlo[2]}, {p.rhi[0], p.rhi[1], p.rhi[2]}};
+            Box rd{{0, 0, 0}, {-1, -1, -1}};
+            bool reads_blk = false;
+            if (lvl_diff == 0) {
+                reads_blk = !tmp_same;
+                for (int d = 0; d < 3; d++) {
+                    rd.lo[d] = p.slo[d];
+                    rd.hi[d] = p.slo[d] + p.rhi[d] - p.rlo[d];
                 }
-                if (send && sp.by_ref) send = sp.s_ref == ref[n];
-                if (send && sp.by_level) send = sp.s_level == ft.level[n];
-                if (!send) continue;
-                // hvy_tmp_usage (xfer_block_data.f90:376-395)
-                bool tmp_rp = false, tmp_same = false;
-                if (sp.tmp_usage == 1 && ref[b] != sp.s_ref) tmp_rp = tmp_same = true;
-                if (sp.tmp_usage == 2) tmp_rp = true;
-                Patch p = make_patch(geo, wav.order_predictor, r, lvl_diff, sp.gminus, sp.gplus, slot[b], slot[n]);
-                Box w{{p.rlo[0], p.rlo[1], p.rlo[2]}, {p.rhi[0], p.rhi[1], p.rhi[2]}};
-                Box rd{{0, 0, 0}, {-1, -1, -1}};
-                bool reads_blk = false;
-                if (lvl_diff == 0) {
-                    reads_blk = !tmp_same;
-                    for (int d = 0; d < 3; d++) {
-                        rd.lo[d] = p.slo[d];
-                        rd.hi[d] = p.slo[d] + p.rhi[d] - p.rlo[d];
-                    }
-                } else if (lvl_diff == -1) {
-                    reads_blk = !tmp_rp;
-                    for (int d = 0; d < 3; d++) {
-                        rd.lo[d] = p.slo[d];
-                        rd.hi[d] = p.shi[d];
-                    }
+            } else if (lvl_diff == -1) {
+                reads_blk = !tmp_rp;
+                for (int d = 0; d < 3; d++) {
+                    rd.lo[d] = p.slo[d];
+                    rd.hi[d] = p.shi[d];
                 }
-                // a new wave where this patch would see, or clobber, a box an
-                // earlier patch of the wave touches
-                const bool conflict = (reads_blk && wb.hits(wb.wr, p.src, rd)) || wb.hits(wb.rd, p.dst, w) ||
-                                      wb.hits(wb.wr, p.dst, w);
-                if (conflict) flush();
-                if (reads_blk) wb.rd[p.src].push_back(rd);
-                wb.wr[p.dst].push_back(w);
-                if (lvl_diff == 0) {
-                    (tmp_same ? cur.copy_tmp : cur.copy_blk).push_back(p);
-                } else if (lvl_diff == -1) {
-                    (tmp_rp ? cur.pred_tmp : cur.pred_blk).push_back(p);
-                    cur.max_coarse = std::max(cur.max_coarse, pred_need_of(p, wav.order_predictor));
-                } else {
-                    const int key = 2 * b + (tmp_rp ? 1 : 0);
-                    auto it = entry_of.find(key);
-                    int e;
-                    if (it == entry_of.end()) {
-                        e = (int)cur.filters.size();
-                        entry_of[key] = e;
-                        cur.filters.push_back({slot[b], tmp_rp ? 1 : 0});
-                        // SC next to a coarser or finer neighbour without a
-                        // same-level one are copied, not filtered
-                        const int g = geo.g;
-                        for (int r2 = 1; r2 <= kNumRelations; r2++) {
-                            const int n2 = nbr(b, r2);
-                            if (n2 < 0 || !sp.filter) continue;
-                            const int ld = level - ft.level[n2];
-                            if ((ld == 1 || ld == -1) && is_leaf(b, false) && !has_valid_neighbor(b, r2, 0)) {
-                                int lo[3], hi[3];
-                                modify_box0(geo, r2, Nscl, Nscr, g, g, +1, lo, hi);
-                                ScBox sb;
-                                sb.entry = e;
-                                bool empty = false;
-                                for (int d = 0; d < 3; d++) {
-                                    if (d >= geo.dim) {
-                                        sb.lo[d] = sb.hi[d] = 0;
-                                        continue;
-                                    }
-                                    // SC lattice g + 2m (0-based); the box starts on it
-                                    const int first = lo[d] + ((lo[d] - g) & 1);
-                                    int last = hi[d] - ((hi[d] - g) & 1);
-                                    if (last > g + geo.Bs[d] - 2) last = g + geo.Bs[d] - 2;
-                                    sb.lo[d] = (int16_t)((first - g) / 2);
-                                    sb.hi[d] = (int16_t)((last - g) / 2);
-                                    if (first > last || first < g) empty = true;
-                                }
-                                if (!empty) cur.ce_copies.push_back(sb);
+            }
+            // a new wave where this patch would see, or clobber, a box an
+            // earlier patch of the wave touches
+            const bool conflict = (reads_blk && wb.hits(wb.wr, p.src, rd)) || wb.hits(wb.rd, p.dst, w) ||
+                                  wb.hits(wb.wr, p.dst, w);
+            if (conflict) flush();
+            if (reads_blk) wb.rd[p.src].push_back(rd);
+            wb.wr[p.dst].push_back(w);
+            if (lvl_diff == 0) {
+                (tmp_same ? cur.copy_tmp : cur.copy_blk).push_back(p);
+            } else if (lvl_diff == -1) {
+                (tmp_rp ? cur.pred_tmp : cur.pred_blk).push_back(p);
+                cur.max_coarse = std::max(cur.max_coarse, pred_need_of(p, wav.order_predictor));
+            } else {
+                const int key = 2 * b + (tmp_rp ? 1 : 0);
+                auto it = entry_of.find(key);
+                int e;
+                if (it == entry_of.end()) {
+                    e = (int)cur.filters.size();
+                    entry_of[key] = e;
+                    cur.filters.push_back({slot[b], tmp_rp ? 1 : 0});
+                    // SC next to a coarser or finer neighbour without a
+                    // same-level one are copied, not filtered
+                    const int g = geo.g;
+                    const bool leaf = is_leaf(b, false);
+                    for_neighbors(b, [&](int r2, int n2) {
+                        if (!sp.filter || !leaf) return;
+                        const int ld = level - ft.level[n2];
+                        if ((ld != 1 && ld != -1) || has_valid_neighbor(b, r2, 0)) return;
+                        int lo[3], hi[3];
+                        modify_box0(geo, r2, Nscl, Nscr, g, g, +1, lo, hi);
+                        ScBox sb;
+                        sb.entry = e;
+                        bool empty = false;
+                        for (int d = 0; d < 3; d++) {
+                            if (d >= geo.dim) {
+                                sb.lo[d] = sb.hi[d] = 0;
+                                continue;
                             }
+                            // SC lattice g + 2m (0-based); the box starts on it
+                            const int first = lo[d] + ((lo[d] - g) & 1);
+                            int last = hi[d] - ((hi[d] - g) & 1);
+                            if (last > g + geo.Bs[d] - 2) last = g + geo.Bs[d] - 2;
+                            sb.lo[d] = (int16_t)((first - g) / 2);
+                            sb.hi[d] = (int16_t)((last - g) / 2);
+                            if (first > last || first < g) empty = true;
                         }
-                    } else {
-                        e = it->second;
-                    }
-                    p.src = e;
-                    cur.restrict_.push_back(p);
+                        if (!empty) cur.ce_copies.push_back(sb);
+                    });
+                } else {
+                    e = it->second;
                 }
+                p.src = e;
+                cur.restrict_.push_back(p);
             }
         }
         flush();
@@ -362,14 +371,12 @@ void LiftedTree::plan_ce_modify(int ce_case, int s_level, int s_ref, bool clear_
         if ((ce_case == 1 || ce_case == 3) && lv != s_level) continue;
         if ((ce_case == 2 || ce_case == 3) && ref[b] != s_ref) continue;
         if (!is_leaf(b, false)) continue;
-        for (int r = 1; r <= kNumRelations; r++) {
-            const int n = nbr(b, r);
-            if (n < 0) continue;
+        for_neighbors(b, [&](int r, int n) {
             if (ft.level[n] < lv && !(has_valid_neighbor(b, r, 0) || has_valid_neighbor(b, r, -1))) {
                 if (clear_wc) ce_clear_wc(b, r, ops);
                 if (copy_sc) ce_copy_sc(b, r, ops);
             }
-        }
+        });
     }
 }
 
@@ -378,16 +385,15 @@ void LiftedTree::security_candidates(std::vector<ZoneItem> &items) const {
     const int g = geo.g;
     for (int b = 0; b < size(); b++) {
         if (!alive[b] || ref[b] != 0) continue;
-        for (int r = 1; r <= kNumRelations; r++) {
-            const int n = nbr(b, r);
-            if (n < 0 || ref[n] != -1 || ft.level[n] != ft.level[b]) continue;
+        for_neighbors(b, [&](int r, int n) {
+            if (ref[n] != -1 || ft.level[n] != ft.level[b]) return;
             ZoneItem it;
             it.block = b;
             it.relation = r;
             modify_box0(geo, r, Nwcl, Nwcr, g, g, 0, it.lo, it.hi);
             for (int d = 0; d < 3; d++) it.io[d] = d < geo.dim ? ((g + it.lo[d]) % 2 + 2) % 2 : 0;
             items.push_back(it);
-        }
+        });
     }
 }
 
@@ -398,12 +404,11 @@ void LiftedTree::security_apply(const std::vector<ZoneItem> &items, const std::v
     auto flag_bit = [](int v) { return (v >> 30) & 1; };
     for (int b = 0; b < size(); b++) {
         if (!alive[b] || ref[b] != -1) continue;
-        for (int r = 1; r <= kNumRelations; r++) {
-            const int n = nbr(b, r);
-            if (n < 0 || !(ref[n] > 0) || ft.level[n] != ft.level[b]) continue;
+        for_neighbors(b, [&](int r, int n) {
+            if (!(ref[n] > 0) || ft.level[n] != ft.level[b]) return;
             const int pid = relation_patch_id(relation_inverse(r));
             if (flag_bit(ref[n]) && ((ref[n] >> (pid + 3)) & 1)) ref[b] = kTmpStatus;
-        }
+        });
     }
     for (int b = 0; b < size(); b++)
         if (alive[b] && ref[b] > 0 && (ref[b] == kTmpStatus || flag_bit(ref[b]))) ref[b] = 0;

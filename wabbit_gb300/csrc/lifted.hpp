@@ -24,6 +24,7 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "adapt.hpp"
@@ -101,6 +102,11 @@ public:
     bool is_root(int b, bool check_empty) const;
     bool has_valid_neighbor(int b, int relation, int lvl_diff) const;
     int nbr(int b, int r) const { return nb_[size_t(b) * kNumRelations + r - 1]; }
+    // existing neighbours of b in ascending relation order: f(relation, n)
+    template <class F>
+    void for_neighbors(int b, F f) const {
+        for (int i = adj_begin_[b]; i < adj_begin_[b + 1]; i++) f(adj_[i].first, adj_[i].second);
+    }
 
     void plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) const;
     // coarse_extension_modify: case 0 tree, 1 level, 2 ref, 3 level_ref
@@ -118,6 +124,8 @@ public:
 private:
     std::vector<int> nb_;          // kNumRelations per full-tree block
     std::vector<int> index_;       // full-tree index of the Forest's blocks
+    std::vector<int> adj_begin_;   // compact neighbour lists
+    std::vector<std::pair<int, int>> adj_;
     void ce_clear_wc(int b, int relation, std::vector<BoxOp> &ops) const;
     void ce_copy_sc(int b, int relation, std::vector<BoxOp> &ops) const;
 };
