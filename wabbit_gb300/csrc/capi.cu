@@ -1664,7 +1664,13 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     };
     // the leaf grid's filtered sync (sync_ghosts_tree)
     for (int b = 0; b < nt; b++) L.alive[b] = b < nb;
-    if (!L.update_metadata(err)) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
+    auto meta = [&]() {
+        const auto t0 = clk::now();
+        const bool ok = L.update_metadata(err);
+        ctx->adapt_ms[kPlan] += std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+        return ok;
+    };
+    if (!meta()) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
     {
         SyncSpecL sp;
         sp.gminus = sp.gplus = g;
@@ -1672,7 +1678,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     }
     // wavelet_decompose_full_tree
     std::fill(L.alive.begin(), L.alive.end(), 1);
-    if (!L.update_metadata(err)) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
+    if (!meta()) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
     const int lmax = L.ft.max_level();
     for (int b = 0; b < nt; b++) L.ref[b] = b < nb ? ((L.ft.level[b] == lmax || leaf_first) ? -1 : 0) : kRefTmpEmpty;
     {
@@ -1783,7 +1789,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         L.alive[b] = flags[b] != kFlagCoarsen;
         L.ref[b] = 0;
     }
-    if (!L.update_metadata(err)) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
+    if (!meta()) return fail_restore(cudaSuccess, fail(WG_EGRID, "adapt: %s", err.c_str()));
     e = ce(0, 0, 0, true, false);
     for (int b = 0; b < nt; b++) {
         if (!L.alive[b] || !L.is_leaf(b, false)) continue;
@@ -1834,7 +1840,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     std::fill(L.alive.begin(), L.alive.end(), 0);
     for (int b : leaves) L.alive[b] = 1;
     std::fill(L.ref.begin(), L.ref.end(), 0);
-    if (!L.update_metadata(err)) return fail_restore(e, fail(WG_EGRID, "adapt: %s", err.c_str()));
+    if (!meta()) return fail_restore(e, fail(WG_EGRID, "adapt: %s", err.c_str()));
     {
         SyncSpecL sp;
         sp.gminus = sp.gplus = g;

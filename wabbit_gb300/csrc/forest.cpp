@@ -212,9 +212,24 @@ void Forest::set(int nblk, const int *lv, const int *co) {
         for (int b = 0; b < nblk; b++) coords[3 * b + 2] = 0;
 }
 
+bool Forest::insert_(uint64_t k, int b) {
+    for (uint64_t h = (k * 0x9E3779B97F4A7C15ull) >> 20 & mask_;; h = (h + 1) & mask_) {
+        if (vals_[h] < 0) {
+            keys_[h] = k;
+            vals_[h] = b;
+            return true;
+        }
+        if (keys_[h] == k) return false;
+    }
+}
+
 int Forest::find(int lv, int x, int y, int z) const {
-    auto it = lookup_.find(key_of(lv, x, y, z));
-    return it == lookup_.end() ? -1 : it->second;
+    if (keys_.empty()) return -1;
+    const uint64_t k = key_of(lv, x, y, z);
+    for (uint64_t h = (k * 0x9E3779B97F4A7C15ull) >> 20 & mask_;; h = (h + 1) & mask_) {
+        if (vals_[h] < 0) return -1;
+        if (keys_[h] == k) return vals_[h];
+    }
 }
 
 uint64_t Forest::treecode(int b) const {
@@ -231,14 +246,17 @@ uint64_t Forest::treecode(int b) const {
 
 bool Forest::update_neighbors(std::string &err, bool overlapping) {
     const int n = size();
-    lookup_.clear();
-    lookup_.reserve(size_t(n) * 2);
+    size_t cap = 16;
+    while (cap < size_t(n) * 2 + 16) cap <<= 1;
+    keys_.assign(cap, 0);
+    vals_.assign(cap, -1);
+    mask_ = cap - 1;
     for (int b = 0; b < n; b++) {
         int lv = level[b];
         if (lv < 0 || lv > 20) { err = "block level out of range"; return false; }
         for (int d = 0; d < dim; d++)
             if (coords[3 * b + d] < 0 || coords[3 * b + d] >= (1 << lv)) { err = "block coordinate out of range"; return false; }
-        if (!lookup_.emplace(key_of(lv, coords[3 * b], coords[3 * b + 1], coords[3 * b + 2]), b).second) {
+        if (!insert_(key_of(lv, coords[3 * b], coords[3 * b + 1], coords[3 * b + 2]), b)) {
             err = "duplicate block";
             return false;
         }

@@ -57,7 +57,11 @@ public:
     uint64_t treecode(int b) const;  // reference bit layout (y bit0, x bit1, z bit2)
 
 private:
-    std::unordered_map<uint64_t, int> lookup_;
+    // open-addressing table (linear probing) of block keys -> block index
+    std::vector<uint64_t> keys_;
+    std::vector<int> vals_;
+    uint64_t mask_ = 0;
+    bool insert_(uint64_t key, int b);
 };
 
 // One ghost patch: fill box [rlo,rhi] (0-based, inclusive) of block dst from

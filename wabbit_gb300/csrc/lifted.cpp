@@ -127,19 +127,31 @@ inline bool overlap(const Box &a, const Box &b) {
         if (a.hi[d] < b.lo[d] || b.hi[d] < a.lo[d]) return false;
     return true;
 }
-// boxes touched by a patch in the current wave, per arena slot
+// boxes read / written by the patches of the current wave, per arena slot
+// (dense, cleared through the list of touched slots)
 struct WaveBoxes {
-    std::unordered_map<int, std::vector<Box>> rd, wr;
-    bool hits(const std::unordered_map<int, std::vector<Box>> &m, int s, const Box &b) const {
-        auto it = m.find(s);
-        if (it == m.end()) return false;
-        for (const Box &x : it->second)
+    std::vector<std::vector<Box>> rd, wr;
+    std::vector<int> touched;
+    bool hits(const std::vector<std::vector<Box>> &m, int s, const Box &b) const {
+        if (s >= (int)m.size()) return false;
+        for (const Box &x : m[s])
             if (overlap(x, b)) return true;
         return false;
     }
+    void add(std::vector<std::vector<Box>> &m, int s, const Box &b) {
+        if (s >= (int)rd.size()) {
+            rd.resize(s + 1);
+            wr.resize(s + 1);
+        }
+        if (rd[s].empty() && wr[s].empty()) touched.push_back(s);
+        m[s].push_back(b);
+    }
     void clear() {
-        rd.clear();
-        wr.clear();
+        for (int s : touched) {
+            rd[s].clear();
+            wr[s].clear();
+        }
+        touched.clear();
     }
 };
 int pred_need_of(const Patch &p, int order_predictor) {
@@ -246,12 +258,17 @@ void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) co
                 }
             }
             // a new wave where this patch would see, or clobber, a box an
-            // earlier patch of the wave touches
-            const bool conflict = (reads_blk && wb.hits(wb.wr, p.src, rd)) || wb.hits(wb.rd, p.dst, w) ||
-                                  wb.hits(wb.wr, p.dst, w);
-            if (conflict) flush();
-            if (reads_blk) wb.rd[p.src].push_back(rd);
-            wb.wr[p.dst].push_back(w);
+            // earlier patch of the wave touches. Only predictions can: a
+            // same-level copy reads the sender's interior and writes ghost
+            // nodes, a restriction reads the filtered lattice, and the ghost
+            // boxes of different relations of one receiver are disjoint.
+            if (lvl_diff == -1) {
+                const bool conflict = (reads_blk && wb.hits(wb.wr, p.src, rd)) || wb.hits(wb.rd, p.dst, w) ||
+                                      wb.hits(wb.wr, p.dst, w);
+                if (conflict) flush();
+                if (reads_blk) wb.add(wb.rd, p.src, rd);
+                wb.add(wb.wr, p.dst, w);
+            }
             if (lvl_diff == 0) {
                 (tmp_same ? cur.copy_tmp : cur.copy_blk).push_back(p);
             } else if (lvl_diff == -1) {
