@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
         objs = list(ex.map(compile_one, UNITS.items()))
     tmp = LIB + ".tmp"
-    cmd = [cc, "-shared"] + ARCH + objs + ["-o", tmp, "-lcudart"]
+    cmd = [cc, "-shared"] + ARCH + objs + ["-o", tmp, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

@@ -489,6 +489,8 @@ void ghost_box0(const Geometry &geo, int relation, int gminus, int gplus, int lv
 
 int relation_inverse(int relation) { return inverse_relation(relation); }
 
+int relation_id(const int d[3], int part, int dim) { return relation_of(d, part, dim); }
+
 int relation_patch_id(int relation) {
     const int t = (relation - 1) % 56 + 1;
     if (t <= 24) return (t - 1) / 4 + 1;

@@ -99,6 +99,9 @@ void modify_box0(const Geometry &geo, int relation, int Ns, int Ne, int gm, int 
 // get_indices_of_ghost_patch (neighborhood.f90:158-327), 0-based inclusive
 void ghost_box0(const Geometry &geo, int relation, int gminus, int gplus, int lvl_diff, int lo[3], int hi[3]);
 int relation_inverse(int relation);
+// relation id 1..56 of direction d (components -1, 0, +1) and, for a finer or
+// coarser neighbour, the part index along the free directions
+int relation_id(const int d[3], int part, int dim);
 // np_l / np_u (neighborhood.f90:439-500): relations of the same patch at
 // another level difference
 void relation_range(int relation, int lvl_diff, int &lo, int &hi);

@@ -4,9 +4,42 @@
 
 #include <algorithm>
 #include <cstring>
+#include <thread>
 #include <unordered_map>
 
 namespace wg {
+
+namespace {
+// f(chunk, lo, hi) on contiguous chunks of [0, n), one host thread each
+template <class F>
+void par_chunks(int n, int nchunk, F f) {
+    if (nchunk <= 1 || n < 8192) {
+        f(0, 0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int c = 0; c < nchunk; c++) {
+        const int lo = (int)((long long)n * c / nchunk), hi = (int)((long long)n * (c + 1) / nchunk);
+        th.emplace_back([=, &f]() { f(c, lo, hi); });
+    }
+    for (auto &t : th) t.join();
+}
+// f(task) for task = 0..ntask-1, one host thread each
+template <class F>
+void par_tasks(int ntask, F f) {
+    if (ntask <= 1) {
+        if (ntask == 1) f(0);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < ntask; t++) th.emplace_back([=, &f]() { f(t); });
+    for (auto &t : th) t.join();
+}
+int host_threads() {
+    const unsigned h = std::thread::hardware_concurrency();
+    return h ? (int)std::min(h, 32u) : 4;
+}
+}  // namespace
 
 bool LiftedTree::init(const Geometry &g, const WaveletInfo &w, int fd_max_size, int jmin, int jmax, int nleaf,
                       const int *level, const int *coords, std::string &err) {
@@ -19,6 +52,19 @@ bool LiftedTree::init(const Geometry &g, const WaveletInfo &w, int fd_max_size, 
     alive.assign(ft.size(), 1);
     ref.assign(ft.size(), 0);
     slot.assign(ft.size(), -1);
+    size_t cap = 16;
+    while (cap < size_t(ft.size()) * 2 + 16) cap <<= 1;
+    keys_.assign(cap, 0);
+    vals_.assign(cap, -1);
+    mask_ = cap - 1;
+    for (int b = 0; b < ft.size(); b++) {
+        const uint64_t k = ((uint64_t)ft.level[b] << 60) | ((uint64_t)ft.coords[3 * b] << 40) |
+                           ((uint64_t)ft.coords[3 * b + 1] << 20) | (uint64_t)ft.coords[3 * b + 2];
+        uint64_t h = (k * 0x9E3779B97F4A7C15ull) >> 20 & mask_;
+        while (vals_[h] >= 0) h = (h + 1) & mask_;
+        keys_[h] = k;
+        vals_[h] = b;
+    }
     // coarse-extension widths: setup_wavelet (module_wavelets.f90:1341-1417);
     // CDF24/26/28/46 are not built, so no extra WC width applies
     const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
@@ -41,38 +87,92 @@ bool LiftedTree::init(const Geometry &g, const WaveletInfo &w, int fd_max_size, 
     return true;
 }
 
-bool LiftedTree::update_metadata(std::string &err) {
-    Forest f;
-    f.dim = geo.dim;
-    f.Jmin = Jmin;
-    f.Jmax = Jmax;
-    index_.clear();
-    std::vector<int> lv, co;
-    for (int b = 0; b < size(); b++) {
-        if (!alive[b]) continue;
-        index_.push_back(b);
-        lv.push_back(ft.level[b]);
-        for (int a = 0; a < 3; a++) co.push_back(ft.coords[3 * b + a]);
+int LiftedTree::find_(int lv, int x, int y, int z) const {
+    const uint64_t k = ((uint64_t)lv << 60) | ((uint64_t)x << 40) | ((uint64_t)y << 20) | (uint64_t)z;
+    for (uint64_t h = (k * 0x9E3779B97F4A7C15ull) >> 20 & mask_;; h = (h + 1) & mask_) {
+        if (vals_[h] < 0) return -1;
+        if (keys_[h] == k) return vals_[h];
     }
-    f.set((int)index_.size(), lv.data(), co.data());
-    if (!f.update_neighbors(err, true)) return false;
-    nb_.assign(size_t(size()) * kNumRelations, -1);
-    for (size_t i = 0; i < index_.size(); i++)
-        for (int r = 0; r < kNumRelations; r++) {
-            const int n = f.nbr[i * kNumRelations + r];
-            nb_[size_t(index_[i]) * kNumRelations + r] = n < 0 ? -1 : index_[n];
+}
+
+// find_neighbor with search_overlapping (find_neighbors.f90:18-215) on the
+// full tree: the same-level block, then the finer parts up to the first
+// missing one, then the coarser block; only alive blocks are recorded. The
+// finer blocks are daughters and the coarser block the mother of the
+// same-level position's block of the full tree, when it exists.
+bool LiftedTree::update_metadata(std::string &err) {
+    (void)err;
+    const int dim = geo.dim, nch = host_threads();
+    std::vector<std::vector<std::pair<int, int>>> part(nch);
+    std::vector<std::vector<int>> count(nch);
+    par_chunks(size(), nch, [&](int ch, int lo, int hi) {
+        std::vector<std::pair<int, int>> &out = part[ch];
+        std::vector<int> &cnt = count[ch];
+        cnt.assign(hi - lo, 0);
+        std::vector<std::pair<int, int>> tmp;
+        for (int b = lo; b < hi; b++) {
+            if (!alive[b]) continue;
+            const int lv = ft.level[b];
+            const int *c = &ft.coords[3 * b];
+            const int N = 1 << lv;
+            tmp.clear();
+            for (int dz = (dim == 3 ? -1 : 0); dz <= (dim == 3 ? 1 : 0); dz++)
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dx = -1; dx <= 1; dx++) {
+                        if (!dx && !dy && !dz) continue;
+                        const int d[3] = {dx, dy, dz};
+                        int nfree = 0;
+                        for (int i = 0; i < dim; i++) nfree += (d[i] == 0);
+                        const int nparts = 1 << nfree;
+                        int a[3] = {0, 0, 0};
+                        for (int i = 0; i < dim; i++) a[i] = ((c[i] + d[i]) % N + N) % N;
+                        const int same = lv == 0 ? b : find_(lv, a[0], a[1], a[2]);
+                        if (same >= 0 && alive[same]) tmp.push_back({relation_id(d, 0, dim), same});
+                        if (lv < Jmax && same >= 0)
+                            for (int p = 0; p < nparts; p++) {
+                                int k = 0, fr = 0;
+                                for (int i = 0; i < dim; i++) {
+                                    int bit;
+                                    if (d[i] == 0) bit = (p >> fr++) & 1;
+                                    else bit = d[i] > 0 ? 1 : 0;
+                                    // daughter bit of the fine neighbour: (2c + bit + d) mod 2
+                                    k |= (((bit + d[i]) % 2 + 2) % 2) << i;
+                                }
+                                const int f = ft.daughters[8 * same + k];
+                                if (f < 0 || !alive[f]) break;
+                                tmp.push_back({relation_id(d, p, dim) + 112, f});
+                            }
+                        if (lv <= Jmin) continue;
+                        int prt = 0, fr = 0;
+                        bool touches = true;
+                        for (int i = 0; i < dim; i++) {
+                            const int bit = c[i] & 1;
+                            if (d[i] == 0) prt |= bit << fr++;
+                            else if ((d[i] > 0) != (bit == 1)) touches = false;
+                        }
+                        if (!touches) continue;
+                        const int cb = same >= 0 ? ft.mother[same] : find_(lv - 1, a[0] >> 1, a[1] >> 1, a[2] >> 1);
+                        if (cb >= 0 && alive[cb]) tmp.push_back({relation_id(d, prt, dim) + 56, cb});
+                    }
+            std::sort(tmp.begin(), tmp.end());
+            cnt[b - lo] = (int)tmp.size();
+            out.insert(out.end(), tmp.begin(), tmp.end());
         }
+    });
     adj_begin_.assign(size() + 1, 0);
     adj_.clear();
-    for (int b = 0; b < size(); b++) {
-        adj_begin_[b] = (int)adj_.size();
-        if (!alive[b]) continue;
-        for (int r = 1; r <= kNumRelations; r++) {
-            const int n = nbr(b, r);
-            if (n >= 0) adj_.push_back({r, n});
+    size_t total = 0;
+    for (const auto &v : part) total += v.size();
+    adj_.reserve(total);
+    int b = 0;
+    for (int ch = 0; ch < nch; ch++) {
+        for (int k : count[ch]) {
+            adj_begin_[b + 1] = adj_begin_[b] + k;
+            b++;
         }
+        adj_.insert(adj_.end(), part[ch].begin(), part[ch].end());
     }
-    adj_begin_[size()] = (int)adj_.size();
+    for (; b < size(); b++) adj_begin_[b + 1] = adj_begin_[b];
     return true;
 }
 
@@ -111,9 +211,10 @@ bool LiftedTree::is_root(int b, bool check_empty) const {
 bool LiftedTree::has_valid_neighbor(int b, int relation, int lvl_diff) const {
     int lo, hi;
     relation_range(relation, lvl_diff, lo, hi);
-    for (int r = lo; r <= hi; r++) {
-        const int n = nbr(b, r);
-        if (n >= 0 && ref[n] != kRefTmpEmpty) return true;
+    for (int i = adj_begin_[b]; i < adj_begin_[b + 1]; i++) {
+        const int r = adj_[i].first;
+        if (r > hi) break;
+        if (r >= lo && ref[adj_[i].second] != kRefTmpEmpty) return true;
     }
     return false;
 }
@@ -175,148 +276,188 @@ int pred_need_of(const Patch &p, int order_predictor) {
 void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) const {
     waves.clear();
     const int nstages = wav.lifted ? 3 : 2, unl = wav.lifted ? 0 : 1;
-    // one pass over the senders: the candidate patches of every stage in
-    // sender-major order, after the cheap receiver filters
+    const int nch = host_threads();
+    // candidates of every stage in sender-major order, after the cheap
+    // receiver filters (one pass over the senders, in parallel chunks)
     struct Cand {
         int b, r, n, lvl_diff;
     };
-    std::vector<std::vector<Cand>> cand(nstages + 1);
-    for (int b = 0; b < size(); b++) {
-        if (!alive[b]) continue;
-        if (sp.base == 2 && !is_leaf(b, false)) continue;
-        if (ref[b] == kRefTmpEmpty) continue;
-        const int level = ft.level[b];
-        for_neighbors(b, [&](int r, int n) {
-            if (ref[n] == kRefTmpEmpty) return;
-            if (sp.by_ref && ref[n] != sp.s_ref) return;
-            if (sp.by_level && ft.level[n] != sp.s_level) return;
-            const int lvl_diff = level - ft.level[n];
-            const int stage = lvl_diff == 0 ? 1 : lvl_diff == +1 ? 2 - unl : 3 - unl;
-            cand[stage].push_back({b, r, n, lvl_diff});
-        });
-    }
+    std::vector<std::vector<std::vector<Cand>>> cpart(nch, std::vector<std::vector<Cand>>(nstages + 1));
+    par_chunks(size(), nch, [&](int ch, int lo, int hi) {
+        for (int b = lo; b < hi; b++) {
+            if (!alive[b]) continue;
+            if (sp.base == 2 && !is_leaf(b, false)) continue;
+            if (ref[b] == kRefTmpEmpty) continue;
+            const int level = ft.level[b];
+            for_neighbors(b, [&](int r, int n) {
+                if (ref[n] == kRefTmpEmpty) return;
+                if (sp.by_ref && ref[n] != sp.s_ref) return;
+                if (sp.by_level && ft.level[n] != sp.s_level) return;
+                const int lvl_diff = level - ft.level[n];
+                const int stage = lvl_diff == 0 ? 1 : lvl_diff == +1 ? 2 - unl : 3 - unl;
+                cpart[ch][stage].push_back({b, r, n, lvl_diff});
+            });
+        }
+    });
+    // the boxes of a patch depend on its relation and level difference only
+    std::vector<Patch> tmpl(3 * (kNumRelations + 1));
+    std::vector<int> tmpl_need(3 * (kNumRelations + 1), -1);
+    for (int ld = -1; ld <= 1; ld++)
+        for (int r = 1; r <= kNumRelations; r++) {
+            const int k = (ld + 1) * (kNumRelations + 1) + r;
+            tmpl[k] = make_patch(geo, wav.order_predictor, r, ld, sp.gminus, sp.gplus, 0, 0);
+            if (ld == -1) tmpl_need[k] = pred_need_of(tmpl[k], wav.order_predictor);
+        }
+    // send rule of the case, the data source and the patch of one candidate
+    auto prepare = [&](const Cand &cd, Patch &p, int &need, bool &tmp_rp, bool &tmp_same) {
+        const int b = cd.b, r = cd.r, lvl_diff = cd.lvl_diff;
+        bool send = false;
+        switch (sp.base) {
+        case 1:
+            send = true;
+            if (lvl_diff == -1 && !is_leaf(b, true)) send = false;
+            if (lvl_diff == +1 && !is_root(b, true)) send = false;
+            break;
+        case 2:
+            send = true;
+            if (lvl_diff >= 0 && has_valid_neighbor(b, r, -1)) send = false;
+            else if (lvl_diff == +1 && has_valid_neighbor(b, r, 0)) send = false;
+            break;
+        case 3:
+            send = lvl_diff != +1;
+            if (send && lvl_diff != 0 && !is_leaf(b, true)) send = false;
+            break;
+        case 4:
+            send = lvl_diff != -1;
+            if (send && lvl_diff != 0 && !is_root(b, true)) send = false;
+            break;
+        default:
+            send = lvl_diff == 0;
+        }
+        if (!send) return false;
+        // hvy_tmp_usage (xfer_block_data.f90:376-395)
+        tmp_rp = tmp_same = false;
+        if (sp.tmp_usage == 1 && ref[b] != sp.s_ref) tmp_rp = tmp_same = true;
+        if (sp.tmp_usage == 2) tmp_rp = true;
+        const int k = (lvl_diff + 1) * (kNumRelations + 1) + r;
+        p = tmpl[k];
+        p.src = slot[b];
+        p.dst = slot[cd.n];
+        need = tmpl_need[k];
+        return true;
+    };
+    // add a prepared patch to a wave (restrictions: one filter entry per
+    // sender and source in the wave, with its coarse-extension SC copies)
+    auto add = [&](const Cand &cd, Patch p, int need, bool tmp_rp, bool tmp_same, SyncWave &cur,
+                   std::unordered_map<int, int> &entry_of) {
+        const int b = cd.b, lvl_diff = cd.lvl_diff, level = ft.level[b];
+        if (lvl_diff == 0) {
+            (tmp_same ? cur.copy_tmp : cur.copy_blk).push_back(p);
+            return;
+        }
+        if (lvl_diff == -1) {
+            (tmp_rp ? cur.pred_tmp : cur.pred_blk).push_back(p);
+            cur.max_coarse = std::max(cur.max_coarse, need);
+            return;
+        }
+        const int key = 2 * b + (tmp_rp ? 1 : 0);
+        auto it = entry_of.find(key);
+        int e;
+        if (it == entry_of.end()) {
+            e = (int)cur.filters.size();
+            entry_of[key] = e;
+            cur.filters.push_back({slot[b], tmp_rp ? 1 : 0});
+            // SC next to a coarser or finer neighbour without a same-level
+            // one are copied, not filtered
+            const int g = geo.g;
+            const bool leaf = is_leaf(b, false);
+            for_neighbors(b, [&](int r2, int n2) {
+                if (!sp.filter || !leaf) return;
+                const int ld = level - ft.level[n2];
+                if ((ld != 1 && ld != -1) || has_valid_neighbor(b, r2, 0)) return;
+                int lo[3], hi[3];
+                modify_box0(geo, r2, Nscl, Nscr, g, g, +1, lo, hi);
+                ScBox sb;
+                sb.entry = e;
+                bool empty = false;
+                for (int d = 0; d < 3; d++) {
+                    if (d >= geo.dim) {
+                        sb.lo[d] = sb.hi[d] = 0;
+                        continue;
+                    }
+                    // SC lattice g + 2m (0-based); the box starts on it
+                    const int first = lo[d] + ((lo[d] - g) & 1);
+                    int last = hi[d] - ((hi[d] - g) & 1);
+                    if (last > g + geo.Bs[d] - 2) last = g + geo.Bs[d] - 2;
+                    sb.lo[d] = (int16_t)((first - g) / 2);
+                    sb.hi[d] = (int16_t)((last - g) / 2);
+                    if (first > last || first < g) empty = true;
+                }
+                if (!empty) cur.ce_copies.push_back(sb);
+            });
+        } else {
+            e = it->second;
+        }
+        p.src = e;
+        cur.restrict_.push_back(p);
+    };
     for (int istage = 1; istage <= nstages; istage++) {
+        size_t ncand = 0;
+        for (int ch = 0; ch < nch; ch++) ncand += cpart[ch][istage].size();
+        if (ncand == 0) continue;
+        if (istage != 3 - unl) {
+            // copies and restrictions never conflict within a stage (a copy
+            // reads the sender's interior and writes ghost nodes, a
+            // restriction reads the filtered lattice, and the ghost boxes of
+            // the relations of one receiver are disjoint): every chunk of
+            // senders becomes a wave of its own, built in parallel
+            std::vector<SyncWave> part(nch);
+            auto chunk = [&](int c) {
+                std::unordered_map<int, int> entry_of;
+                part[c].stage = istage;
+                for (const Cand &cd : cpart[c][istage]) {
+                    Patch p;
+                    int need;
+                    bool tmp_rp, tmp_same;
+                    if (prepare(cd, p, need, tmp_rp, tmp_same)) add(cd, p, need, tmp_rp, tmp_same, part[c], entry_of);
+                }
+            };
+            if (ncand >= 8192) par_tasks(nch, chunk);
+            else
+                for (int c = 0; c < nch; c++) chunk(c);
+            for (SyncWave &w : part)
+                if (!w.copy_blk.empty() || !w.copy_tmp.empty() || !w.restrict_.empty()) waves.push_back(std::move(w));
+            continue;
+        }
+        // predictions: in the reference's order, cut into waves where a
+        // patch would see or clobber a box an earlier patch of the wave
+        // touches
         SyncWave cur;
         cur.stage = istage;
         WaveBoxes wb;
-        std::unordered_map<int, int> entry_of;   // (sender, source) -> filter entry of this wave
+        std::unordered_map<int, int> entry_of;
         auto flush = [&]() {
-            const bool any = !cur.copy_blk.empty() || !cur.copy_tmp.empty() || !cur.restrict_.empty() ||
-                             !cur.pred_blk.empty() || !cur.pred_tmp.empty();
-            if (any) waves.push_back(std::move(cur));
+            if (!cur.pred_blk.empty() || !cur.pred_tmp.empty()) waves.push_back(std::move(cur));
             cur = SyncWave();
             cur.stage = istage;
             wb.clear();
-            entry_of.clear();
         };
-        for (const Cand &cd : cand[istage]) {
-            const int b = cd.b, r = cd.r, lvl_diff = cd.lvl_diff;
-            const int level = ft.level[b];
-            bool send = false;
-            switch (sp.base) {
-            case 1:
-                send = true;
-                if (lvl_diff == -1 && !is_leaf(b, true)) send = false;
-                if (lvl_diff == +1 && !is_root(b, true)) send = false;
-                break;
-            case 2:
-                send = true;
-                if (lvl_diff >= 0 && has_valid_neighbor(b, r, -1)) send = false;
-                else if (lvl_diff == +1 && has_valid_neighbor(b, r, 0)) send = false;
-                break;
-            case 3:
-                send = lvl_diff != +1;
-                if (send && lvl_diff != 0 && !is_leaf(b, true)) send = false;
-                break;
-            case 4:
-                send = lvl_diff != -1;
-                if (send && lvl_diff != 0 && !is_root(b, true)) send = false;
-                break;
-            default:
-                send = lvl_diff == 0;
-            }
-            if (!send) continue;
-            // hvy_tmp_usage (xfer_block_data.f90:376-395)
-            bool tmp_rp = false, tmp_same = false;
-            if (sp.tmp_usage == 1 && ref[b] != sp.s_ref) tmp_rp = tmp_same = true;
-            if (sp.tmp_usage == 2) tmp_rp = true;
-            Patch p = make_patch(geo, wav.order_predictor, r, lvl_diff, sp.gminus, sp.gplus, slot[b], slot[cd.n]);
-            Box w{{p.rlo[0], p.rlo[1], p.rlo[2]}, {p.rhi[0], p.rhi[1], p.rhi[2]}};
-            Box rd{{0, 0, 0}, {-1, -1, -1}};
-            bool reads_blk = false;
-            if (lvl_diff == 0) {
-                reads_blk = !tmp_same;
-                for (int d = 0; d < 3; d++) {
-                    rd.lo[d] = p.slo[d];
-                    rd.hi[d] = p.slo[d] + p.rhi[d] - p.rlo[d];
-                }
-            } else if (lvl_diff == -1) {
-                reads_blk = !tmp_rp;
-                for (int d = 0; d < 3; d++) {
-                    rd.lo[d] = p.slo[d];
-                    rd.hi[d] = p.shi[d];
-                }
-            }
-            // a new wave where this patch would see, or clobber, a box an
-            // earlier patch of the wave touches. Only predictions can: a
-            // same-level copy reads the sender's interior and writes ghost
-            // nodes, a restriction reads the filtered lattice, and the ghost
-            // boxes of different relations of one receiver are disjoint.
-            if (lvl_diff == -1) {
+        for (int ch = 0; ch < nch; ch++)
+            for (const Cand &cd : cpart[ch][istage]) {
+                Patch p;
+                int need;
+                bool tmp_rp, tmp_same;
+                if (!prepare(cd, p, need, tmp_rp, tmp_same)) continue;
+                const bool reads_blk = !tmp_rp;
+                const Box w{{p.rlo[0], p.rlo[1], p.rlo[2]}, {p.rhi[0], p.rhi[1], p.rhi[2]}};
+                const Box rd{{p.slo[0], p.slo[1], p.slo[2]}, {p.shi[0], p.shi[1], p.shi[2]}};
                 const bool conflict = (reads_blk && wb.hits(wb.wr, p.src, rd)) || wb.hits(wb.rd, p.dst, w) ||
                                       wb.hits(wb.wr, p.dst, w);
                 if (conflict) flush();
                 if (reads_blk) wb.add(wb.rd, p.src, rd);
                 wb.add(wb.wr, p.dst, w);
+                add(cd, p, need, tmp_rp, tmp_same, cur, entry_of);
             }
-            if (lvl_diff == 0) {
-                (tmp_same ? cur.copy_tmp : cur.copy_blk).push_back(p);
-            } else if (lvl_diff == -1) {
-                (tmp_rp ? cur.pred_tmp : cur.pred_blk).push_back(p);
-                cur.max_coarse = std::max(cur.max_coarse, pred_need_of(p, wav.order_predictor));
-            } else {
-                const int key = 2 * b + (tmp_rp ? 1 : 0);
-                auto it = entry_of.find(key);
-                int e;
-                if (it == entry_of.end()) {
-                    e = (int)cur.filters.size();
-                    entry_of[key] = e;
-                    cur.filters.push_back({slot[b], tmp_rp ? 1 : 0});
-                    // SC next to a coarser or finer neighbour without a
-                    // same-level one are copied, not filtered
-                    const int g = geo.g;
-                    const bool leaf = is_leaf(b, false);
-                    for_neighbors(b, [&](int r2, int n2) {
-                        if (!sp.filter || !leaf) return;
-                        const int ld = level - ft.level[n2];
-                        if ((ld != 1 && ld != -1) || has_valid_neighbor(b, r2, 0)) return;
-                        int lo[3], hi[3];
-                        modify_box0(geo, r2, Nscl, Nscr, g, g, +1, lo, hi);
-                        ScBox sb;
-                        sb.entry = e;
-                        bool empty = false;
-                        for (int d = 0; d < 3; d++) {
-                            if (d >= geo.dim) {
-                                sb.lo[d] = sb.hi[d] = 0;
-                                continue;
-                            }
-                            // SC lattice g + 2m (0-based); the box starts on it
-                            const int first = lo[d] + ((lo[d] - g) & 1);
-                            int last = hi[d] - ((hi[d] - g) & 1);
-                            if (last > g + geo.Bs[d] - 2) last = g + geo.Bs[d] - 2;
-                            sb.lo[d] = (int16_t)((first - g) / 2);
-                            sb.hi[d] = (int16_t)((last - g) / 2);
-                            if (first > last || first < g) empty = true;
-                        }
-                        if (!empty) cur.ce_copies.push_back(sb);
-                    });
-                } else {
-                    e = it->second;
-                }
-                p.src = e;
-                cur.restrict_.push_back(p);
-            }
-        }
         flush();
     }
 }

@@ -101,7 +101,12 @@ public:
     bool is_leaf(int b, bool check_empty) const;
     bool is_root(int b, bool check_empty) const;
     bool has_valid_neighbor(int b, int relation, int lvl_diff) const;
-    int nbr(int b, int r) const { return nb_[size_t(b) * kNumRelations + r - 1]; }
+    // neighbour of b in relation r (1..168) or -1
+    int nbr(int b, int r) const {
+        for (int i = adj_begin_[b]; i < adj_begin_[b + 1]; i++)
+            if (adj_[i].first == r) return adj_[i].second;
+        return -1;
+    }
     // existing neighbours of b in ascending relation order: f(relation, n)
     template <class F>
     void for_neighbors(int b, F f) const {
@@ -122,10 +127,12 @@ public:
     void security_apply(const std::vector<ZoneItem> &items, const std::vector<char> &significant);
 
 private:
-    std::vector<int> nb_;          // kNumRelations per full-tree block
-    std::vector<int> index_;       // full-tree index of the Forest's blocks
-    std::vector<int> adj_begin_;   // compact neighbour lists
+    std::vector<int> adj_begin_;   // neighbour lists, ascending relation
     std::vector<std::pair<int, int>> adj_;
+    std::vector<uint64_t> keys_;   // open-addressing table: block key -> full-tree index
+    std::vector<int> vals_;
+    uint64_t mask_ = 0;
+    int find_(int lv, int x, int y, int z) const;
     void ce_clear_wc(int b, int relation, std::vector<BoxOp> &ops) const;
     void ce_copy_sc(int b, int relation, std::vector<BoxOp> &ops) const;
 };
