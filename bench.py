@@ -66,7 +66,9 @@ def parse():
                     help="RHS stencil precision (default: the workload's; fp32 = double-float on the FP32 units)")
     ap.add_argument("--rate", type=float, default=8.0, help="serving: Poisson arrival rate (requests/s)")
     ap.add_argument("--requests", type=int, default=256, help="serving: number of requests")
-    ap.add_argument("--budget-gb", type=float, default=64.0, help="serving: HBM budget of the arenas")
+    ap.add_argument("--budget-gb", type=float, default=160.0, help="serving: HBM budget of the arenas")
+    ap.add_argument("--adapt-every", type=int, default=5,
+                    help="serving: adaptation cycle length in steps (0: no adaptation)")
     ap.add_argument("--compare-plain", choices=["auto", "on", "off"], default="auto",
                     help="also time the plain per-solve FP64 path (one wg_rk4_step call per step, no graph) "
                          "and report the speed-up and the L2 difference of the two after K steps "
@@ -420,7 +422,8 @@ def compare_plain(args, cfg, lv, co, u0, ids, masks, f, ctx, value, npts):
 
 def run_serving(args, rank, world):
     """Serving workload: a seeded Poisson stream of independent solves
-    (2-D and 3-D, 64-8192 blocks, 50 RK4 steps each), admitted by HBM
+    (2-D and 3-D, 64-8192 blocks, 50 RK4 steps each, adapted every 5 steps:
+    refine everywhere, 5 steps, adapt_tree with eps = 1e-3), admitted by HBM
     footprint and stepped in batched launches; aggregate point-updates/s
     with p50/p99 time to solution (arrival to result on the host)."""
     import torch
@@ -428,7 +431,7 @@ def run_serving(args, rank, world):
     build.build()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     stream = serving.make_stream(args.requests, rate=args.rate, seed=4 + rank)
-    srv = serving.Server(budget_gb=args.budget_gb, chunk=5)
+    srv = serving.Server(budget_gb=args.budget_gb, chunk=5, adapt_every=args.adapt_every)
     # warm-up: one small solve of each geometry (graph capture, autotuning)
     srv.run([serving.Request(-1, 0.0, 2, 0, 1, 1e-3, nsteps=5), serving.Request(-2, 0.0, 3, 0, 2, 1e-3, nsteps=5)],
             realtime=False)
@@ -445,6 +448,8 @@ def run_serving(args, rank, world):
         "data": "synthetic (seeded Poisson stream, vortex ICs; see wabbit_gb300/serving.py)",
         "config": {"workload": "serving", "requests": args.requests, "arrival_rate_per_s": args.rate,
                    "budget_gb": args.budget_gb, "chunk_steps": 5, "arena_blocks": srv.capacity,
+                   "adapt_every": args.adapt_every, "eps": srv.eps,
+                   "cycle": "sync, refine everywhere, chunk of RK4 steps, adapt_tree" if args.adapt_every else None,
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "serving": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "wall_s": summ["wall_s"],
                     "requests": summ["requests"], "point_updates": summ["point_updates"]},

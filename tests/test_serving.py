@@ -45,3 +45,27 @@ def test_stream_is_seeded():
     assert [(r.arrival, r.dim, r.size, r.seed, r.nu) for r in a] == [(r.arrival, r.dim, r.size, r.seed, r.nu) for r in b]
     assert all(5e-4 <= r.nu <= 5e-3 for r in a)
     assert np.all(np.diff([r.arrival for r in a]) > 0)
+
+
+def test_served_with_adaptation_equals_alone():
+    """With the reference's adaptation cycle every 5 steps (sync, refine
+    everywhere, 5 RK4 steps, adapt_tree; the 3-D solve with the lifted
+    CDF4,4 algorithm) a served solve still equals the same solve alone: grid
+    and state."""
+    reqs = [
+        Request(0, 0.00, 3, 1, 201, 1e-3, nsteps=10),
+        Request(1, 0.00, 2, 1, 202, 2e-3, nsteps=10),
+        Request(2, 0.01, 2, 3, 203, 3e-3, nsteps=15),
+    ]
+    srv = serving.Server(budget_gb=12.0, keep_results=True, adapt_every=5)
+    try:
+        recs, summ = srv.run(reqs, realtime=False)
+    finally:
+        srv.close()
+    assert summ["requests"] == len(reqs)
+    for r in reqs:
+        u, t = serving.solve_alone(r, adapt_every=5)
+        assert recs[r.rid]["u"].shape == u.shape, r.rid
+        assert np.array_equal(recs[r.rid]["u"], u), r.rid
+        assert recs[r.rid]["time"] == t
+        assert np.isfinite(u).all() and np.abs(u).max() > 0

@@ -11,6 +11,14 @@ sized from an HBM budget. The loop
 * steps every active solve of a context with one wg_run per scheduling
   round: one launch per kernel for all of them (batched FP32-pipe stages),
   the two contexts on their own streams so that their work overlaps,
+* adapts the grids every `adapt_every` steps as the reference's main loop
+  does (LIB/MAIN/main.f90:300-400: ghost sync, refine_tree "everywhere",
+  N_dt_per_grid time steps, adapt_tree with the threshold-state-vector
+  indicator, absolute eps): every chunk of a solve is one such cycle; the
+  3-D solves (CDF4,4) take the lifted full-tree adaptation. A request's Jmax
+  is the finest level of its initial grid. A solve takes part in a round
+  only if the arena can hold its refined grid plus the full tree's mothers;
+  otherwise it waits for the next round,
 * retires solves that reached their step count (downloads the interior
   state, frees the slots) and records the time to solution.
 
@@ -180,6 +188,7 @@ class Solve:
         self.req = req
         cfg = base.copy()
         cfg.nu = req.nu
+        cfg.Jmax = LADDER[req.dim][req.size][1]
         self.cfg = cfg
         lv, co = request_grid(req.dim, req.size)
         self.nblk = len(lv)
@@ -188,22 +197,54 @@ class Solve:
         self.f.upload_interior(vortex_ic_device(cfg, lv, co, req.seed))
         self.f.set_time(0.0)
         self.done = 0
-        self.points = self.nblk * int(np.prod([cfg.Bs[d] for d in range(cfg.dim)]))
+        self.pts_blk = int(np.prod([cfg.Bs[d] for d in range(cfg.dim)]))
+
+    @property
+    def points(self):
+        return self.nblk * self.pts_blk
+
+    def cycle_need(self):
+        """Blocks of the refined grid and of the full tree's mothers of the
+        next adaptation cycle (upper bound)."""
+        lv, _ = self.f.grid()
+        nd = 1 << self.cfg.dim
+        refined = int(np.sum(np.where(lv < self.cfg.Jmax, nd, 1)))
+        return refined, refined // (nd - 1) + 2 * (self.cfg.Jmax + 1)
+
+    def cycle(self):
+        """Before a chunk: sync and refine everywhere (main.f90:300-320)."""
+        self.f.sync_ghosts_tree()
+        self.f.refine_everywhere()
+        self.nblk = self.f.nblocks
 
 
 class Server:
-    def __init__(self, budget_gb: float = 64.0, chunk: int = 5, share_3d: float = 0.85, keep_results=False):
+    def __init__(self, budget_gb: float = 64.0, chunk: int = 5, share_3d: float = 0.85, keep_results=False,
+                 adapt_every: int = 0, eps: float = 1e-3):
         from . import capi
-        self.chunk = chunk
+        self.chunk = adapt_every if adapt_every else chunk
+        self.adapt = bool(adapt_every)
+        self.eps = eps
         self.keep = keep_results
         self.base = {2: geometry(2), 3: geometry(3)}
         L = capi.load()
         self.ctx = {}
         for dim, share in ((3, share_3d), (2, 1.0 - share_3d)):
             per = L.wg_bytes_per_block(self.base[dim])
+            if self.adapt and self.base[dim].wavelet.decode()[4] != "0":
+                # the lifted adaptation's hvy_tmp arena: one more full block
+                c = self.base[dim]
+                per += 8 * c.neq * int(np.prod([c.Bs[d] + 2 * c.g for d in range(dim)]))
             cap = max(64, int(budget_gb * 1e9 * share / per))
             self.ctx[dim] = Context(self.base[dim], cap)
         self.capacity = {d: self.ctx[d].max_blocks for d in self.ctx}
+
+    def _peak(self, dim, req):
+        """Blocks a request needs at the peak of its first cycle."""
+        lv, _ = request_grid(dim, req.size)
+        nd = 1 << dim
+        refined = int(np.sum(np.where(lv < LADDER[dim][req.size][1], nd, 1)))
+        return refined + refined // (nd - 1) + 2 * (LADDER[dim][req.size][1] + 1)
 
     def close(self):
         for c in self.ctx.values():
@@ -229,9 +270,10 @@ class Server:
                 while queue[dim]:
                     r = queue[dim][0]
                     nb = len(request_grid(dim, r.size)[0])
-                    if nb > self.capacity[dim]:
-                        raise ValueError(f"request {r.rid} ({nb} blocks) exceeds the {dim}-D arena")
-                    if used[dim] + nb > self.capacity[dim]:
+                    need = self._peak(dim, r) if self.adapt else nb
+                    if need > self.capacity[dim]:
+                        raise ValueError(f"request {r.rid} ({need} blocks at its peak) exceeds the {dim}-D arena")
+                    if used[dim] + need > self.capacity[dim]:
                         break
                     queue[dim].pop(0)
                     s = Solve(r, self.ctx[dim], self.base[dim])
@@ -243,13 +285,33 @@ class Server:
                     time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
                 continue
             # one scheduling round: every active solve advances one chunk
+            # (with adaptation: the solves whose cycle fits into the arena)
             for dim in (3, 2):
-                if active[dim]:
-                    k = min(self.chunk, min(s.req.nsteps - s.done for s in active[dim]))
-                    self.ctx[dim].run([s.f for s in active[dim]], k, use_graph=True)
+                if not active[dim]:
+                    continue
+                group = active[dim]
+                if self.adapt:
+                    group, grow, mothers = [], 0, 0
                     for s in active[dim]:
-                        s.done += k
-                        total_points += s.points * k
+                        refined, m = s.cycle_need()
+                        if used[dim] + grow + (refined - s.nblk) + max(mothers, m) <= self.capacity[dim]:
+                            grow += refined - s.nblk
+                            mothers = max(mothers, m)
+                            s.cycle()
+                            group.append(s)
+                    used[dim] += grow
+                    if not group:
+                        raise RuntimeError(f"no {dim}-D solve fits its adaptation cycle into the arena")
+                k = min(self.chunk, min(s.req.nsteps - s.done for s in group))
+                self.ctx[dim].run([s.f for s in group], k, use_graph=True)
+                for s in group:
+                    s.done += k
+                    total_points += s.points * k
+                if self.adapt:
+                    for s in group:
+                        before = s.nblk
+                        s.nblk = s.f.adapt(np.full(s.cfg.neq, self.eps))
+                        used[dim] += s.nblk - before
             for dim in (3, 2):
                 self.ctx[dim].synchronize()
             for dim in (3, 2):
@@ -278,17 +340,24 @@ class Server:
         return records, summary
 
 
-def solve_alone(req: Request, chunk: int = 5):
-    """The same request on its own context, in the same step chunks."""
+def solve_alone(req: Request, chunk: int = 5, adapt_every: int = 0, eps: float = 1e-3, max_blocks: int = 0):
+    """The same request on its own context, in the same step chunks (and,
+    with adapt_every, the same adaptation cycles)."""
     base = geometry(req.dim)
     lv, _ = request_grid(req.dim, req.size)
-    ctx = Context(base, len(lv) + 4)
+    ctx = Context(base, max_blocks or (len(lv) * (10 if adapt_every else 1) + 64))
+    if adapt_every:
+        chunk = adapt_every
     try:
         s = Solve(req, ctx, base)
         while s.done < req.nsteps:
+            if adapt_every:
+                s.cycle()
             k = min(chunk, req.nsteps - s.done)
             ctx.run([s.f], k, use_graph=True)
             s.done += k
+            if adapt_every:
+                s.nblk = s.f.adapt(np.full(s.cfg.neq, eps))
         ctx.synchronize()
         return s.f.download_interior(), s.f.time()[0]
     finally:
