@@ -57,7 +57,7 @@ def test_served_with_adaptation_equals_alone():
         Request(1, 0.00, 2, 1, 202, 2e-3, nsteps=10),
         Request(2, 0.01, 2, 3, 203, 3e-3, nsteps=15),
     ]
-    srv = serving.Server(budget_gb=12.0, keep_results=True, adapt_every=5)
+    srv = serving.Server(budget_gb=16.0, keep_results=True, adapt_every=5)
     try:
         recs, summ = srv.run(reqs, realtime=False)
     finally:
