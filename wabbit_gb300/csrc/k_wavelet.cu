@@ -23,6 +23,7 @@
 // parent block (ghosts included) is predicted to the fine grid and each of the
 // 2^d daughters takes its (Bs+2g)^d window.
 #include "common.cuh"
+#include "exact.cuh"
 #include "predict.cuh"
 
 namespace wg {
@@ -419,7 +420,9 @@ struct Taps {
     int n[5];              // 0 HD (non-zero or centre), 1 GD, 2 HR odd, 3 GR odd, 4 GR even without 0
     int off[5][16];
     double val[5][16];
+    int kind[5][16], sh[5][16];   // exact power-of-two taps (exact.cuh)
     double gr0;            // GR(0)
+    int gr0_kind, gr0_sh;
     int lazy;
 };
 __constant__ Taps c_taps;
@@ -428,11 +431,15 @@ static int g_taps_key = -1;
 constexpr int kTpoThreads = 512;
 constexpr int kTpoMaxPerThread = 16;
 
+__device__ __forceinline__ double tmul(int f, int t, double x) {
+    return tap_mul(x, c_taps.val[f][t], c_taps.kind[f][t], c_taps.sh[f][t]);
+}
+
 // sum_t src[(at + off_t) * st] * val_t in order, the first term not added to 0
 __device__ __forceinline__ double tap_sum(int f, const double *src, long long st, int at) {
     const int n = c_taps.n[f];
-    double s = __dmul_rn(src[(at + c_taps.off[f][0]) * st], c_taps.val[f][0]);
-    for (int t = 1; t < n; t++) s = __dadd_rn(s, __dmul_rn(src[(at + c_taps.off[f][t]) * st], c_taps.val[f][t]));
+    double s = tmul(f, 0, src[(at + c_taps.off[f][0]) * st]);
+    for (int t = 1; t < n; t++) s = __dadd_rn(s, tmul(f, t, src[(at + c_taps.off[f][t]) * st]));
     return s;
 }
 
@@ -447,20 +454,17 @@ __device__ __forceinline__ double iwt_point(const double *src, long long st, int
     if (c_taps.lazy) {
         double v = src[at * st];
         if (p & 1)
-            for (int t = 0; t < c_taps.n[2]; t++)
-                v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[2][t]) * st], c_taps.val[2][t]));
+            for (int t = 0; t < c_taps.n[2]; t++) v = __dadd_rn(v, tmul(2, t, src[(at + c_taps.off[2][t]) * st]));
         return v;
     }
     if ((p & 1) == 0) {
         double v = src[at * st];
-        for (int t = 0; t < c_taps.n[3]; t++)
-            v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[3][t]) * st], c_taps.val[3][t]));
+        for (int t = 0; t < c_taps.n[3]; t++) v = __dadd_rn(v, tmul(3, t, src[(at + c_taps.off[3][t]) * st]));
         return v;
     }
     double v = tap_sum(2, src, st, at);
-    v = __dadd_rn(v, __dmul_rn(src[at * st], c_taps.gr0));
-    for (int t = 0; t < c_taps.n[4]; t++)
-        v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[4][t]) * st], c_taps.val[4][t]));
+    v = __dadd_rn(v, tap_mul(src[at * st], c_taps.gr0, c_taps.gr0_kind, c_taps.gr0_sh));
+    for (int t = 0; t < c_taps.n[4]; t++) v = __dadd_rn(v, tmul(4, t, src[(at + c_taps.off[4][t]) * st]));
     return v;
 }
 
@@ -567,6 +571,7 @@ static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
         if (t.n[f] >= 16) return false;
         t.off[f][t.n[f]] = off;
         t.val[f][t.n[f]] = v;
+        classify_tap(v, t.kind[f][t.n[f]], t.sh[f][t.n[f]]);
         t.n[f]++;
         return true;
     };
@@ -589,6 +594,7 @@ static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
         else if ((m & 1) && w.GR[i] != 0.0) ok &= add(3, m, w.GR[i]);
         else if (!(m & 1) && w.GR[i] != 0.0) ok &= add(4, m, w.GR[i]);
     }
+    classify_tap(t.gr0, t.gr0_kind, t.gr0_sh);
     t.lazy = w.lifted ? 0 : 1;
     if (!ok || t.n[0] == 0 || t.n[1] == 0) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemcpyToSymbolAsync(c_taps, &t, sizeof(t), 0, cudaMemcpyHostToDevice, s);
