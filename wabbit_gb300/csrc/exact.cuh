@@ -29,17 +29,22 @@ inline void classify_tap(double c, int &kind, int &sh) {
     }
 }
 
-__device__ __forceinline__ double tap_mul(double x, double c, int kind, int sh) {
+// x * (+-2^sh) with integer operations only; sgn is the tap's sign bit
+// (0 or 1 << 63). Exact for zero and for normal x with a normal result;
+// otherwise bad is set and the caller recomputes with the FP64 multiply.
+__device__ __forceinline__ double pow2_mul(double x, int sh, long long sgn, bool &bad) {
+    const long long b = __double_as_longlong(x);
+    const long long a = b & 0x7fffffffffffffffLL;
+    const int e0 = (int)(a >> 52), e1 = e0 + sh;
+    bad |= a != 0 && (e0 == 0 || e0 == 0x7ff || e1 <= 0 || e1 >= 0x7ff);
+    const long long r = a == 0 ? b : b + (long long)sh * (1LL << 52);
+    return __longlong_as_double(r ^ sgn);
+}
+
+// the same decision per tap at run time (kind 0 general, 1 +-2^sh, 2 one)
+__device__ __forceinline__ double tap_mul(double x, double c, int kind, int sh, long long sgn, bool &bad) {
     if (kind == 2) return x;
-    if (kind == 1) {
-        const long long b = __double_as_longlong(x);
-        const int e0 = (int)((b >> 52) & 0x7ff), e1 = e0 + sh;
-        if (e0 != 0 && e0 != 0x7ff && e1 > 0 && e1 < 0x7ff) {
-            long long r = b + (long long)sh * (1LL << 52);
-            if (c < 0.0) r ^= (long long)0x8000000000000000ULL;
-            return __longlong_as_double(r);
-        }
-    }
+    if (kind == 1) return pow2_mul(x, sh, sgn, bad);
     return __dmul_rn(x, c);
 }
 

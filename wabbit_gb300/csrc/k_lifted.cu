@@ -28,6 +28,7 @@ namespace wg {
 
 __constant__ double c_lhd[32];
 __constant__ int c_lhd_k[32], c_lhd_s[32];   // exact power-of-two taps (exact.cuh)
+__constant__ long long c_lhd_g[32];          // sign bit of each tap
 __constant__ int c_lhd_n[2];   // lo, count
 
 __global__ void __launch_bounds__(128) xcopy_kernel(const Patch *__restrict__ patches, int npatch,
@@ -68,7 +69,12 @@ __global__ void __launch_bounds__(256) hd_filter_kernel(const FilterEntry *__res
         const int mx = i % hx, yy = (i / hx) % ny, zz = i / (hx * ny);
         const double *row = u + ((long long)(z0 + zz) * geo.ny + (y0 + yy)) * geo.nx + g + 2 * mx;
         double s = 0.0;
-        for (int t = 0; t < nt; t++) s = __dadd_rn(s, tap_mul(row[lo + t], c_lhd[t], c_lhd_k[t], c_lhd_s[t]));
+        bool bad = false;
+        for (int t = 0; t < nt; t++) s = __dadd_rn(s, tap_mul(row[lo + t], c_lhd[t], c_lhd_k[t], c_lhd_s[t], c_lhd_g[t], bad));
+        if (bad) {
+            s = 0.0;
+            for (int t = 0; t < nt; t++) s = __dadd_rn(s, __dmul_rn(row[lo + t], c_lhd[t]));
+        }
         X[i] = s;
     }
     __syncthreads();
@@ -76,8 +82,13 @@ __global__ void __launch_bounds__(256) hd_filter_kernel(const FilterEntry *__res
         const int mx = i % hx, my = (i / hx) % hy, zz = i / (hx * hy);
         const double *col = X + ((size_t)zz * ny + (g + 2 * my - y0)) * hx + mx;
         double s = 0.0;
+        bool bad = false;
         for (int t = 0; t < nt; t++)
-            s = __dadd_rn(s, tap_mul(col[(long long)(lo + t) * hx], c_lhd[t], c_lhd_k[t], c_lhd_s[t]));
+            s = __dadd_rn(s, tap_mul(col[(long long)(lo + t) * hx], c_lhd[t], c_lhd_k[t], c_lhd_s[t], c_lhd_g[t], bad));
+        if (bad) {
+            s = 0.0;
+            for (int t = 0; t < nt; t++) s = __dadd_rn(s, __dmul_rn(col[(long long)(lo + t) * hx], c_lhd[t]));
+        }
         Y[i] = s;
     }
     __syncthreads();
@@ -90,8 +101,14 @@ __global__ void __launch_bounds__(256) hd_filter_kernel(const FilterEntry *__res
         const int mx = i % hx, my = (i / hx) % hy, mz = i / (hx * hy);
         const double *pl = Y + ((size_t)(g + 2 * mz - z0) * hy + my) * hx + mx;
         double s = 0.0;
+        bool bad = false;
         for (int t = 0; t < nt; t++)
-            s = __dadd_rn(s, tap_mul(pl[(long long)(lo + t) * hx * hy], c_lhd[t], c_lhd_k[t], c_lhd_s[t]));
+            s = __dadd_rn(s, tap_mul(pl[(long long)(lo + t) * hx * hy], c_lhd[t], c_lhd_k[t], c_lhd_s[t],
+                                     c_lhd_g[t], bad));
+        if (bad) {
+            s = 0.0;
+            for (int t = 0; t < nt; t++) s = __dadd_rn(s, __dmul_rn(pl[(long long)(lo + t) * hx * hy], c_lhd[t]));
+        }
         out[i] = s;
     }
 }
@@ -213,14 +230,17 @@ cudaError_t lifted_set_filter(const double *hd, int lo, int n, cudaStream_t s) {
     if (n > 32) return cudaErrorInvalidValue;
     double h[32] = {};
     int kind[32] = {}, sh[32] = {};
+    long long sg[32] = {};
     for (int i = 0; i < n; i++) {
         h[i] = hd[i];
         classify_tap(h[i], kind[i], sh[i]);
+        sg[i] = h[i] < 0.0 ? (long long)0x8000000000000000ULL : 0LL;
     }
     const int ln[2] = {lo, n};
     cudaError_t e = cudaMemcpyToSymbolAsync(c_lhd, h, sizeof(h), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_k, kind, sizeof(kind), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_s, sh, sizeof(sh), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_g, sg, sizeof(sg), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_n, ln, sizeof(ln), 0, cudaMemcpyHostToDevice, s);
     return e;
 }

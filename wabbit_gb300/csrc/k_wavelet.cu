@@ -22,6 +22,8 @@
 // Refinement: refineBlock (LIB/MESH/refinementExecute.f90:4-116): the whole
 // parent block (ghosts included) is predicted to the fine grid and each of the
 // 2^d daughters takes its (Bs+2g)^d window.
+#include <type_traits>
+
 #include "common.cuh"
 #include "exact.cuh"
 #include "predict.cuh"
@@ -421,25 +423,53 @@ struct Taps {
     int off[5][16];
     double val[5][16];
     int kind[5][16], sh[5][16];   // exact power-of-two taps (exact.cuh)
+    long long sgn[5][16];         // sign bit of each tap
     double gr0;            // GR(0)
-    int gr0_kind, gr0_sh;
     int lazy;
 };
 __constant__ Taps c_taps;
 static int g_taps_key = -1;
+static bool g_taps_cdf44 = false;   // the loaded taps have the CDF4,4 kinds
 
 constexpr int kTpoThreads = 512;
 constexpr int kTpoMaxPerThread = 16;
 
-__device__ __forceinline__ double tmul(int f, int t, double x) {
-    return tap_mul(x, c_taps.val[f][t], c_taps.kind[f][t], c_taps.sh[f][t]);
-}
-
 // sum_t src[(at + off_t) * st] * val_t in order, the first term not added to 0
 __device__ __forceinline__ double tap_sum(int f, const double *src, long long st, int at) {
     const int n = c_taps.n[f];
-    double s = tmul(f, 0, src[(at + c_taps.off[f][0]) * st]);
-    for (int t = 1; t < n; t++) s = __dadd_rn(s, tmul(f, t, src[(at + c_taps.off[f][t]) * st]));
+    double s = __dmul_rn(src[(at + c_taps.off[f][0]) * st], c_taps.val[f][0]);
+    for (int t = 1; t < n; t++) s = __dadd_rn(s, __dmul_rn(src[(at + c_taps.off[f][t]) * st], c_taps.val[f][t]));
+    return s;
+}
+
+// Compile-time tap kinds of CDF4,4 (classify_tap of the lists load_taps
+// builds: HD -6..6 without +-5, GD -3..3 without +-2, HR odd, GR odd, GR even
+// without 0); the host checks them against the loaded taps before the
+// specialised kernel runs.
+struct Cdf44Taps {
+    __host__ __device__ static constexpr int nt(int f) { return f == 0 ? 11 : f == 1 ? 5 : f == 4 ? 6 : 4; }
+    __host__ __device__ static constexpr int kind(int f, int t) {
+        return f == 0 ? ((t == 0 || t == 2 || t == 8 || t == 10) ? 1 : 0)
+             : f == 1 ? ((t == 0 || t == 4) ? 1 : t == 2 ? 2 : 0)
+             : f == 4 ? ((t == 0 || t == 5) ? 1 : 0)
+             : ((t == 0 || t == 3) ? 1 : 0);
+    }
+};
+
+// the same sum with the kinds of K known at compile time: power-of-two taps
+// and the unit tap issue no FP64 instruction
+template <class K, int F>
+__device__ __forceinline__ double ktap_sum(const double *src, long long st, int at, bool &bad) {
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t < K::nt(F); t++) {
+        const double x = src[(at + c_taps.off[F][t]) * st];
+        double p;
+        if (K::kind(F, t) == 2) p = x;
+        else if (K::kind(F, t) == 1) p = pow2_mul(x, c_taps.sh[F][t], c_taps.sgn[F][t], bad);
+        else p = __dmul_rn(x, c_taps.val[F][t]);
+        s = t == 0 ? p : __dadd_rn(s, p);
+    }
     return s;
 }
 
@@ -454,23 +484,65 @@ __device__ __forceinline__ double iwt_point(const double *src, long long st, int
     if (c_taps.lazy) {
         double v = src[at * st];
         if (p & 1)
-            for (int t = 0; t < c_taps.n[2]; t++) v = __dadd_rn(v, tmul(2, t, src[(at + c_taps.off[2][t]) * st]));
+            for (int t = 0; t < c_taps.n[2]; t++)
+                v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[2][t]) * st], c_taps.val[2][t]));
         return v;
     }
     if ((p & 1) == 0) {
         double v = src[at * st];
-        for (int t = 0; t < c_taps.n[3]; t++) v = __dadd_rn(v, tmul(3, t, src[(at + c_taps.off[3][t]) * st]));
+        for (int t = 0; t < c_taps.n[3]; t++)
+            v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[3][t]) * st], c_taps.val[3][t]));
         return v;
     }
     double v = tap_sum(2, src, st, at);
-    v = __dadd_rn(v, tap_mul(src[at * st], c_taps.gr0, c_taps.gr0_kind, c_taps.gr0_sh));
-    for (int t = 0; t < c_taps.n[4]; t++) v = __dadd_rn(v, tmul(4, t, src[(at + c_taps.off[4][t]) * st]));
+    v = __dadd_rn(v, __dmul_rn(src[at * st], c_taps.gr0));
+    for (int t = 0; t < c_taps.n[4]; t++)
+        v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[4][t]) * st], c_taps.val[4][t]));
     return v;
+}
+
+// fwt_point / iwt_point with compile-time tap kinds (lifted wavelets); an
+// output whose power-of-two products left the exact range is recomputed
+template <class K>
+__device__ __forceinline__ double fwt_point_k(const double *src, long long st, int at, int p) {
+    bool bad = false;
+    const double v = (p & 1) == 0 ? ktap_sum<K, 0>(src, st, at, bad) : ktap_sum<K, 1>(src, st, at, bad);
+    return bad ? fwt_point(src, st, at, p) : v;
+}
+
+template <class K>
+__device__ __forceinline__ double iwt_point_k(const double *src, long long st, int at, int p) {
+    bool bad = false;
+    double v;
+    if ((p & 1) == 0) {
+        // the reference adds the odd GR taps one by one to the SC
+        v = src[at * st];
+#pragma unroll
+        for (int t = 0; t < K::nt(3); t++) {
+            const double x = src[(at + c_taps.off[3][t]) * st];
+            const double q = K::kind(3, t) == 1 ? pow2_mul(x, c_taps.sh[3][t], c_taps.sgn[3][t], bad)
+                                                : __dmul_rn(x, c_taps.val[3][t]);
+            v = __dadd_rn(v, q);
+        }
+    } else {
+        v = ktap_sum<K, 2>(src, st, at, bad);
+        v = __dadd_rn(v, __dmul_rn(src[at * st], c_taps.gr0));
+#pragma unroll
+        for (int t = 0; t < K::nt(4); t++) {
+            const double x = src[(at + c_taps.off[4][t]) * st];
+            const double q = K::kind(4, t) == 1 ? pow2_mul(x, c_taps.sh[4][t], c_taps.sgn[4][t], bad)
+                                                : __dmul_rn(x, c_taps.val[4][t]);
+            v = __dadd_rn(v, q);
+        }
+    }
+    return bad ? iwt_point(src, st, at, p) : v;
 }
 
 // MODE 0: details (max |WC|) into scratch; 1: FWT stored in place; 2: IWT
 // stored in place. f: half-width of the extended window.
-template <int DIM, int MODE>
+struct GenericTaps {};
+
+template <int DIM, int MODE, class K = GenericTaps>
 __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, double *u, BufGeo geo, int Bx, int By,
                                                              int Bz, int nc, int f, double *detail_scratch) {
     extern __shared__ double sm[];
@@ -483,7 +555,10 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
     const long long np = geo.npts();
     double *ub = u + ((long long)b * nc + c) * np;
     auto point = [&](const double *src, long long st, int at, int p) {
-        return MODE == 2 ? iwt_point(src, st, at, p) : fwt_point(src, st, at, p);
+        if constexpr (std::is_same<K, GenericTaps>::value)
+            return MODE == 2 ? iwt_point(src, st, at, p) : fwt_point(src, st, at, p);
+        else
+            return MODE == 2 ? iwt_point_k<K>(src, st, at, p) : fwt_point_k<K>(src, st, at, p);
     };
     // x pass
     const int nx_out = Bx * ny * nz;
@@ -572,6 +647,7 @@ static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
         t.off[f][t.n[f]] = off;
         t.val[f][t.n[f]] = v;
         classify_tap(v, t.kind[f][t.n[f]], t.sh[f][t.n[f]]);
+        t.sgn[f][t.n[f]] = v < 0.0 ? (long long)0x8000000000000000ULL : 0LL;
         t.n[f]++;
         return true;
     };
@@ -594,9 +670,15 @@ static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
         else if ((m & 1) && w.GR[i] != 0.0) ok &= add(3, m, w.GR[i]);
         else if (!(m & 1) && w.GR[i] != 0.0) ok &= add(4, m, w.GR[i]);
     }
-    classify_tap(t.gr0, t.gr0_kind, t.gr0_sh);
     t.lazy = w.lifted ? 0 : 1;
     if (!ok || t.n[0] == 0 || t.n[1] == 0) return cudaErrorInvalidValue;
+    // the compile-time kinds of the CDF4,4 kernels must describe these taps
+    g_taps_cdf44 = !t.lazy;
+    for (int f = 0; f < 5 && g_taps_cdf44; f++) {
+        if (t.n[f] != Cdf44Taps::nt(f)) g_taps_cdf44 = false;
+        for (int k = 0; k < t.n[f] && g_taps_cdf44; k++)
+            if (t.kind[f][k] != Cdf44Taps::kind(f, k)) g_taps_cdf44 = false;
+    }
     cudaError_t e = cudaMemcpyToSymbolAsync(c_taps, &t, sizeof(t), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) g_taps_key = key;
     return e;
@@ -621,11 +703,21 @@ static cudaError_t launch_tpo(int mode, int dim, const int *blk, int nblk, doubl
     };
     if (dim == 2) {
         if (mode == 0) return go(tpo_kernel<2, 0>);
+        if (g_taps_cdf44) {
+            if (mode == 1) return go(tpo_kernel<2, 1, Cdf44Taps>);
+            if (mode == 3) return go(tpo_kernel<2, 3, Cdf44Taps>);
+            return go(tpo_kernel<2, 2, Cdf44Taps>);
+        }
         if (mode == 1) return go(tpo_kernel<2, 1>);
         if (mode == 3) return go(tpo_kernel<2, 3>);
         return go(tpo_kernel<2, 2>);
     }
     if (mode == 0) return go(tpo_kernel<3, 0>);
+    if (g_taps_cdf44) {
+        if (mode == 1) return go(tpo_kernel<3, 1, Cdf44Taps>);
+        if (mode == 3) return go(tpo_kernel<3, 3, Cdf44Taps>);
+        return go(tpo_kernel<3, 2, Cdf44Taps>);
+    }
     if (mode == 1) return go(tpo_kernel<3, 1>);
     if (mode == 3) return go(tpo_kernel<3, 3>);
     return go(tpo_kernel<3, 2>);
