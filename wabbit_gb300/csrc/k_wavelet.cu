@@ -501,18 +501,17 @@ __device__ __forceinline__ double iwt_point(const double *src, long long st, int
     return v;
 }
 
-// fwt_point / iwt_point with compile-time tap kinds (lifted wavelets); an
-// output whose power-of-two products left the exact range is recomputed
+// fwt_point / iwt_point with compile-time tap kinds (lifted wavelets),
+// without the fallback: bad is set where a power-of-two product left the
+// exact range, and the caller recomputes those outputs with fwt_point /
+// iwt_point
 template <class K>
-__device__ __forceinline__ double fwt_point_k(const double *src, long long st, int at, int p) {
-    bool bad = false;
-    const double v = (p & 1) == 0 ? ktap_sum<K, 0>(src, st, at, bad) : ktap_sum<K, 1>(src, st, at, bad);
-    return bad ? fwt_point(src, st, at, p) : v;
+__device__ __forceinline__ double fwt_point_k(const double *src, long long st, int at, int p, bool &bad) {
+    return (p & 1) == 0 ? ktap_sum<K, 0>(src, st, at, bad) : ktap_sum<K, 1>(src, st, at, bad);
 }
 
 template <class K>
-__device__ __forceinline__ double iwt_point_k(const double *src, long long st, int at, int p) {
-    bool bad = false;
+__device__ __forceinline__ double iwt_point_k(const double *src, long long st, int at, int p, bool &bad) {
     double v;
     if ((p & 1) == 0) {
         // the reference adds the odd GR taps one by one to the SC
@@ -535,7 +534,7 @@ __device__ __forceinline__ double iwt_point_k(const double *src, long long st, i
             v = __dadd_rn(v, q);
         }
     }
-    return bad ? iwt_point(src, st, at, p) : v;
+    return v;
 }
 
 // MODE 0: details (max |WC|) into scratch; 1: FWT stored in place; 2: IWT
@@ -554,19 +553,33 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
     const int y0 = g - f, z0 = DIM == 3 ? g - f : 0;
     const long long np = geo.npts();
     double *ub = u + ((long long)b * nc + c) * np;
-    auto point = [&](const double *src, long long st, int at, int p) {
-        if constexpr (std::is_same<K, GenericTaps>::value)
-            return MODE == 2 ? iwt_point(src, st, at, p) : fwt_point(src, st, at, p);
-        else
-            return MODE == 2 ? iwt_point_k<K>(src, st, at, p) : fwt_point_k<K>(src, st, at, p);
+    // slow: the reference's FP64 multiplies; fast: compile-time tap kinds
+    // (power-of-two products on the integer pipe), bad marks outputs to redo
+    auto slow = [&](const double *src, long long st, int at, int p) {
+        return MODE == 2 ? iwt_point(src, st, at, p) : fwt_point(src, st, at, p);
     };
-    // x pass
+    auto fast = [&](const double *src, long long st, int at, int p, bool &bad) {
+        if constexpr (std::is_same<K, GenericTaps>::value)
+            return slow(src, st, at, p);
+        else
+            return MODE == 2 ? iwt_point_k<K>(src, st, at, p, bad) : fwt_point_k<K>(src, st, at, p, bad);
+    };
+    auto point = slow;
+    // x pass, two independent outputs per step
     const int nx_out = Bx * ny * nz;
-    for (int o = threadIdx.x; o < nx_out; o += kTpoThreads) {
-        const int ix = o % Bx, r = o / Bx;
-        const int yy = r % ny, zz = r / ny;
-        const double *line = ub + ((long long)(z0 + zz) * geo.ny + (y0 + yy)) * geo.nx;
-        sm[o] = point(line, 1, g + ix, ix);
+    auto xrow = [&](int o) { return ub + ((long long)(z0 + (o / Bx) / ny) * geo.ny + (y0 + (o / Bx) % ny)) * geo.nx; };
+    for (int o = threadIdx.x; o < nx_out; o += 2 * kTpoThreads) {
+        const int o2 = o + kTpoThreads;
+        const bool two = o2 < nx_out;
+        bool bad = false;
+        double v1 = fast(xrow(o), 1, g + o % Bx, o % Bx, bad);
+        double v2 = two ? fast(xrow(o2), 1, g + o2 % Bx, o2 % Bx, bad) : 0.0;
+        if (bad) {
+            v1 = slow(xrow(o), 1, g + o % Bx, o % Bx);
+            if (two) v2 = slow(xrow(o2), 1, g + o2 % Bx, o2 % Bx);
+        }
+        sm[o] = v1;
+        if (two) sm[o2] = v2;
     }
     __syncthreads();
     if (MODE == 3) {
@@ -582,12 +595,25 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
     // y pass on the interior rows of every plane of the window
     double res[kTpoMaxPerThread];
     const int ny_out = Bx * By * nz;
+    {
+        bool bad = false;
 #pragma unroll
-    for (int k = 0; k < kTpoMaxPerThread; k++) {
-        const int o = threadIdx.x + k * kTpoThreads;
-        if (o < ny_out) {
-            const int ix = o % Bx, iy = (o / Bx) % By, zz = o / (Bx * By);
-            res[k] = point(sm + (long long)zz * ny * Bx + ix, Bx, f + iy, iy);
+        for (int k = 0; k < kTpoMaxPerThread; k++) {
+            const int o = threadIdx.x + k * kTpoThreads;
+            if (o < ny_out) {
+                const int ix = o % Bx, iy = (o / Bx) % By, zz = o / (Bx * By);
+                res[k] = fast(sm + (long long)zz * ny * Bx + ix, Bx, f + iy, iy, bad);
+            }
+        }
+        if (bad) {
+#pragma unroll
+            for (int k = 0; k < kTpoMaxPerThread; k++) {
+                const int o = threadIdx.x + k * kTpoThreads;
+                if (o < ny_out) {
+                    const int ix = o % Bx, iy = (o / Bx) % By, zz = o / (Bx * By);
+                    res[k] = point(sm + (long long)zz * ny * Bx + ix, Bx, f + iy, iy);
+                }
+            }
         }
     }
     double m = 0.0;
@@ -617,14 +643,28 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
         }
         __syncthreads();
         const int nint = Bx * By * Bz;
-        for (int o = threadIdx.x; o < nint; o += kTpoThreads) {
+        auto zcol = [&](int o) { return sm + (long long)(f + (o / Bx) % By) * Bx + o % Bx; };
+        auto put = [&](int o, double v) {
             const int ix = o % Bx, iy = (o / Bx) % By, iz = o / (Bx * By);
-            const double v = point(sm + (long long)(f + iy) * Bx + ix, (long long)ny * Bx, f + iz, iz);
             if (MODE == 0) {
                 if ((ix & 1) || (iy & 1) || (iz & 1)) m = fmax(m, fabs(v));
             } else {
                 ub[((long long)(g + iz) * geo.ny + (g + iy)) * geo.nx + (g + ix)] = v;
             }
+        };
+        for (int o = threadIdx.x; o < nint; o += 2 * kTpoThreads) {
+            const int o2 = o + kTpoThreads;
+            const bool two = o2 < nint;
+            const long long st = (long long)ny * Bx;
+            bool bad = false;
+            double v1 = fast(zcol(o), st, f + o / (Bx * By), o / (Bx * By), bad);
+            double v2 = two ? fast(zcol(o2), st, f + o2 / (Bx * By), o2 / (Bx * By), bad) : 0.0;
+            if (bad) {
+                v1 = slow(zcol(o), st, f + o / (Bx * By), o / (Bx * By));
+                if (two) v2 = slow(zcol(o2), st, f + o2 / (Bx * By), o2 / (Bx * By));
+            }
+            put(o, v1);
+            if (two) put(o2, v2);
         }
     }
     if (MODE == 0) {
