@@ -2258,6 +2258,19 @@ extern "C" {
 // Interior-only state exchange: host array (nblk, neq, Bz, By, Bx), x
 // fastest. One contiguous host<->device copy plus a device scatter/gather;
 // ghost nodes are left to the next synchronisation.
+// device-side address of page-locked host memory (the interior copy kernels
+// then read / write it directly over the host link, without a staging copy),
+// or null for pageable memory
+static double *mapped_host(const void *p) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (pa.type != cudaMemoryTypeHost || !pa.devicePointer) return nullptr;
+    return (double *)pa.devicePointer;
+}
+
 int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !host) return fail(WG_EINVAL, "bad arguments");
@@ -2265,6 +2278,12 @@ int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
     const int *Bs = ctx->cfg.Bs;
     const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
     const size_t bytes = sizeof(double) * t->slots.size() * ctx->geo.nc * ctx->nint;
+    if (double *mh = mapped_host(host)) {
+        WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, mh, ctx->geo.nc, Bs[0],
+                                        Bs[1], Bz, 1, ctx->stream));
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        return WG_OK;
+    }
     int st = ensure_staging(ctx, bytes);
     if (st) return st;
     WG_CUDA_OK(cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyDefault, ctx->stream));   // host or device memory
@@ -2280,6 +2299,12 @@ int wg_download_interior(wg_ctx *ctx, int tree, double *host) {
     const int *Bs = ctx->cfg.Bs;
     const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
     const size_t bytes = sizeof(double) * t->slots.size() * ctx->geo.nc * ctx->nint;
+    if (double *mh = mapped_host(host)) {
+        WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, mh, ctx->geo.nc, Bs[0],
+                                        Bs[1], Bz, 0, ctx->stream));
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        return WG_OK;
+    }
     int st = ensure_staging(ctx, bytes);
     if (st) return st;
     WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, ctx->staging, ctx->geo.nc,
