@@ -171,6 +171,8 @@ struct wg_ctx {
     bool adapt_profile = false;         // time the phases of the lifted adaptation
     double adapt_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     double *staging = nullptr;          // compact interior staging buffer
+    cudaStream_t copy_stream = nullptr; // host<->device copies of the interior transfers
+    std::vector<cudaEvent_t> copy_ev;   // one per chunk
     size_t staging_bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -988,6 +990,8 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->d_desc);
     cudaFree(ctx->d_tp);
     cudaFree(ctx->d_clk);
+    for (cudaEvent_t ev : ctx->copy_ev) cudaEventDestroy(ev);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return WG_OK;
@@ -2256,62 +2260,82 @@ int ensure_staging(wg_ctx *ctx, size_t bytes) {
 extern "C" {
 
 // Interior-only state exchange: host array (nblk, neq, Bz, By, Bx), x
-// fastest. One contiguous host<->device copy plus a device scatter/gather;
-// ghost nodes are left to the next synchronisation.
-// device-side address of page-locked host memory (the interior copy kernels
-// then read / write it directly over the host link, without a staging copy),
-// or null for pageable memory
-static double *mapped_host(const void *p) {
-    cudaPointerAttributes pa;
-    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
+// fastest. The copy runs in chunks of whole blocks on a second stream so that
+// the host<->device transfer of one chunk overlaps the device scatter /
+// gather of the previous (next) one; ghost nodes are left to the next
+// synchronisation.
+static int ensure_copy_stream(wg_ctx *ctx, int nchunk) {
+    if (!ctx->copy_stream &&
+        cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        ctx->copy_stream = nullptr;
+        return fail(WG_ECUDA, "cudaStreamCreate failed");
     }
-    if (pa.type != cudaMemoryTypeHost || !pa.devicePointer) return nullptr;
-    return (double *)pa.devicePointer;
+    while ((int)ctx->copy_ev.size() < 2 * nchunk) {
+        cudaEvent_t ev;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return fail(WG_ECUDA, "cudaEventCreate failed");
+        ctx->copy_ev.push_back(ev);
+    }
+    return WG_OK;
+}
+
+// chunks of about 256 MB, at block granularity
+static int interior_chunks(const wg_ctx *ctx, int nblk, std::vector<int> &first) {
+    const size_t per = sizeof(double) * ctx->geo.nc * ctx->nint;
+    const int step = std::max(1, (int)((256u << 20) / per));
+    first.clear();
+    for (int b = 0; b < nblk; b += step) first.push_back(b);
+    first.push_back(nblk);
+    return (int)first.size() - 1;
+}
+
+static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) {
+    const int *Bs = ctx->cfg.Bs;
+    const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
+    const int nblk = (int)t->slots.size();
+    const size_t per = (size_t)ctx->geo.nc * ctx->nint;
+    int st = ensure_staging(ctx, sizeof(double) * per * nblk);
+    if (st) return st;
+    std::vector<int> first;
+    const int nch = interior_chunks(ctx, nblk, first);
+    if ((st = ensure_copy_stream(ctx, nch))) return st;
+    const cudaMemcpyKind kind = cudaMemcpyDefault;   // host or device memory
+    for (int k = 0; k < nch; k++) {
+        const int b0 = first[k], nb = first[k + 1] - first[k];
+        double *dev = ctx->staging + per * b0, *hst = host + per * b0;
+        const size_t bytes = sizeof(double) * per * nb;
+        cudaEvent_t done = ctx->copy_ev[2 * k], ready = ctx->copy_ev[2 * k + 1];
+        if (to_device) {
+            WG_CUDA_OK(cudaMemcpyAsync(dev, hst, bytes, kind, ctx->copy_stream));
+            WG_CUDA_OK(cudaEventRecord(done, ctx->copy_stream));
+            WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, done, 0));
+            WG_CUDA_OK(launch_interior_copy(t->d_all.p + b0, nb, ctx->A, ctx->gA, dev, ctx->geo.nc, Bs[0], Bs[1], Bz, 1,
+                                            ctx->stream));
+        } else {
+            WG_CUDA_OK(launch_interior_copy(t->d_all.p + b0, nb, ctx->A, ctx->gA, dev, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,
+                                            ctx->stream));
+            WG_CUDA_OK(cudaEventRecord(ready, ctx->stream));
+            WG_CUDA_OK(cudaStreamWaitEvent(ctx->copy_stream, ready, 0));
+            WG_CUDA_OK(cudaMemcpyAsync(hst, dev, bytes, kind, ctx->copy_stream));
+        }
+    }
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->copy_stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
 }
 
 int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !host) return fail(WG_EINVAL, "bad arguments");
     t->shadow_valid = false;
-    const int *Bs = ctx->cfg.Bs;
-    const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
-    const size_t bytes = sizeof(double) * t->slots.size() * ctx->geo.nc * ctx->nint;
-    if (double *mh = mapped_host(host)) {
-        WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, mh, ctx->geo.nc, Bs[0],
-                                        Bs[1], Bz, 1, ctx->stream));
-        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-        return WG_OK;
-    }
-    int st = ensure_staging(ctx, bytes);
-    if (st) return st;
-    WG_CUDA_OK(cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyDefault, ctx->stream));   // host or device memory
-    WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, ctx->staging, ctx->geo.nc,
-                                    Bs[0], Bs[1], Bz, 1, ctx->stream));
+    // the staging buffer is free once the stream's earlier work is done
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-    return WG_OK;
+    return interior_transfer(ctx, t, const_cast<double *>(host), 1);
 }
 
 int wg_download_interior(wg_ctx *ctx, int tree, double *host) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !host) return fail(WG_EINVAL, "bad arguments");
-    const int *Bs = ctx->cfg.Bs;
-    const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
-    const size_t bytes = sizeof(double) * t->slots.size() * ctx->geo.nc * ctx->nint;
-    if (double *mh = mapped_host(host)) {
-        WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, mh, ctx->geo.nc, Bs[0],
-                                        Bs[1], Bz, 0, ctx->stream));
-        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-        return WG_OK;
-    }
-    int st = ensure_staging(ctx, bytes);
-    if (st) return st;
-    WG_CUDA_OK(launch_interior_copy(t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, ctx->staging, ctx->geo.nc,
-                                    Bs[0], Bs[1], Bz, 0, ctx->stream));
-    WG_CUDA_OK(cudaMemcpyAsync(host, ctx->staging, bytes, cudaMemcpyDefault, ctx->stream));   // host or device memory
-    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-    return WG_OK;
+    return interior_transfer(ctx, t, host, 0);
 }
 
 }  // extern "C"
