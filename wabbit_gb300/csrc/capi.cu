@@ -2295,6 +2295,10 @@ static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) 
     const size_t per = (size_t)ctx->geo.nc * ctx->nint;
     int st = ensure_staging(ctx, sizeof(double) * per * nblk);
     if (st) return st;
+    // an upload also writes the double-float copy of the FP32-pipe precision
+    const bool shadow = to_device && ctx->precision == WG_RHS_FP32;
+    bool push = false;
+    if (shadow && (st = thin_plan(ctx, *t, &push))) return st;
     std::vector<int> first;
     const int nch = interior_chunks(ctx, nblk, first);
     if ((st = ensure_copy_stream(ctx, nch))) return st;
@@ -2308,11 +2312,12 @@ static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) 
             WG_CUDA_OK(cudaMemcpyAsync(dev, hst, bytes, kind, ctx->copy_stream));
             WG_CUDA_OK(cudaEventRecord(done, ctx->copy_stream));
             WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, done, 0));
-            WG_CUDA_OK(launch_interior_copy(t->d_all.p + b0, nb, ctx->A, ctx->gA, dev, ctx->geo.nc, Bs[0], Bs[1], Bz, 1,
+            WG_CUDA_OK(launch_interior_xfer(t->d_all.p + b0, nb, dev, ctx->A, ctx->gA, shadow ? ctx->B : nullptr,
+                                            ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz, push ? ctx->d_push : nullptr, 1,
                                             ctx->stream));
         } else {
-            WG_CUDA_OK(launch_interior_copy(t->d_all.p + b0, nb, ctx->A, ctx->gA, dev, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,
-                                            ctx->stream));
+            WG_CUDA_OK(launch_interior_xfer(t->d_all.p + b0, nb, dev, ctx->A, ctx->gA, nullptr, ctx->gT, ctx->geo.nc,
+                                            Bs[0], Bs[1], Bz, nullptr, 0, ctx->stream));
             WG_CUDA_OK(cudaEventRecord(ready, ctx->stream));
             WG_CUDA_OK(cudaStreamWaitEvent(ctx->copy_stream, ready, 0));
             WG_CUDA_OK(cudaMemcpyAsync(hst, dev, bytes, kind, ctx->copy_stream));
@@ -2320,6 +2325,7 @@ static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) 
     }
     WG_CUDA_OK(cudaStreamSynchronize(ctx->copy_stream));
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    if (shadow) t->shadow_valid = true;
     return WG_OK;
 }
 

@@ -146,6 +146,11 @@ cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, 
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
                       const int *trees, cudaStream_t s);
 cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
+// interior exchange state <-> compact array, one CTA row per (block,
+// component); towards the state optionally also the double-float copy B
+// (thin layout gt) with its same-level ghost pushes
+cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, void *B, BufGeo gt,
+                                 int nc, int Bx, int By, int Bz, const int *push, int to_state, cudaStream_t s);
 cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
                                  int Bx, int By, int Bz, int to_full, cudaStream_t s);
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,

@@ -427,6 +427,48 @@ __global__ void shadow_kernel(const int *blk, int nblk, const double *src, BufGe
     }
 }
 
+// Interior exchange with a compact array (nblk, nc, Bz, By, Bx): one CTA
+// row per (block, component), 32-bit index arithmetic. Towards the state it
+// also writes the double-float copy of the FP32-pipe precision (and its
+// same-level ghost pushes), so no separate shadow pass is needed.
+__global__ void __launch_bounds__(256) interior_xfer_kernel(const int *__restrict__ slots, double *compact, double *A,
+                                                            BufGeo ga, float2 *B, BufGeo gt, int nc, int Bx, int By,
+                                                            int Bz, const int *push, int to_state) {
+    const int b = slots[blockIdx.x], c = blockIdx.y;
+    const int nint = Bx * By * Bz;
+    double *cp = compact + ((long long)blockIdx.x * nc + c) * nint;
+    double *ab = A + ((long long)b * nc + c) * ga.npts();
+    const int za = ga.nz > 1 ? ga.gb : 0, zt = gt.nz > 1 ? gt.gb : 0;
+    for (int i = threadIdx.x; i < nint; i += blockDim.x) {
+        const int ix = i % Bx, iy = (i / Bx) % By, iz = i / (Bx * By);
+        double *pa = ab + ((long long)(iz + za) * ga.ny + (iy + ga.gb)) * ga.nx + (ix + ga.gb);
+        if (!to_state) {
+            cp[i] = *pa;
+            continue;
+        }
+        const double v = cp[i];
+        *pa = v;
+        if (B) {
+            const df2 w = df_split(v);
+            const float2 f = make_float2(w.hi, w.lo);
+            float2 *dc = B + (long long)c * gt.npts();
+            dc[(long long)b * nc * gt.npts() + ((long long)(iz + zt) * gt.ny + (iy + gt.gb)) * gt.nx + (ix + gt.gb)] = f;
+            if (push) {
+                if (gt.nz > 1) push_ghosts<3, 1>(push, b, ix, iy, iz, Bx, By, Bz, gt, dc, gt.npts() * nc, &f);
+                else push_ghosts<2, 1>(push, b, ix, iy, iz, Bx, By, Bz, gt, dc, gt.npts() * nc, &f);
+            }
+        }
+    }
+}
+
+cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, void *B, BufGeo gt,
+                                 int nc, int Bx, int By, int Bz, const int *push, int to_state, cudaStream_t s) {
+    if (nblk <= 0) return cudaSuccess;
+    interior_xfer_kernel<<<dim3(nblk, nc), 256, 0, s>>>(slots, compact, A, ga, reinterpret_cast<float2 *>(B), gt, nc,
+                                                        Bx, By, Bz, push, to_state);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
                           int Bs0, int Bs1, int Bs2, const int *push, cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
