@@ -296,22 +296,30 @@ def run_ours(args, rank, world):
     e2e = None
     if not args.no_e2e:
         host_in = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
-        host_out = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy()
+        host_out = [torch.empty(u0.shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(2)]
         host_in[...] = u0
         k = max(3, min(args.steps, 10))
-        f.upload_interior(host_in)
-        f.timeStep_tree()
-        f.download_interior(host_out)
+        f.rk4_stream([host_in] * 2, host_out)
         barrier(world)
+        t0 = time.perf_counter()
+        # every step: its input from pinned host memory, one RK4 step, its
+        # result back to pinned host memory (the copies of neighbouring steps
+        # overlap the step on the device)
+        f.rk4_stream([host_in] * k, [host_out[i % 2] for i in range(k)])
+        el = max_over_ranks(time.perf_counter() - t0, world)
+        e2e = {"value": sum_over_ranks(npts * k / el, world), "unit": "point-updates/s",
+               "h2d_bytes_per_step": int(host_in.nbytes), "d2h_bytes_per_step": int(host_out[0].nbytes),
+               "steps": k, "path": "wg_rk4_stream (pinned host buffers; input of step k+1 and result of step k "
+                                    "copied while the device steps)"}
+        # the same without overlap: upload, step, download one after another
         t0 = time.perf_counter()
         for _ in range(k):
             f.upload_interior(host_in)
             f.timeStep_tree()
-            f.download_interior(host_out)
-        el = max_over_ranks(time.perf_counter() - t0, world)
-        e2e = {"value": sum_over_ranks(npts * k / el, world), "unit": "point-updates/s",
-               "h2d_bytes_per_step": int(host_in.nbytes), "d2h_bytes_per_step": int(host_out.nbytes) + 16,
-               "steps": k, "path": "wg_upload_interior + wg_rk4_step + wg_download_interior (pinned host)"}
+            f.download_interior(host_out[0])
+        el2 = max_over_ranks(time.perf_counter() - t0, world)
+        e2e["sequential"] = {"value": sum_over_ranks(npts * k / el2, world),
+                             "path": "wg_upload_interior + wg_rk4_step + wg_download_interior"}
 
     plain = None
     if args.compare_plain == "on" or (args.compare_plain == "auto" and cfg.rhs_precision == 1):

@@ -28,7 +28,7 @@ EXPORTS = [
     "wg_upload_interior", "wg_download_interior", "wg_graph_kernels",
     "wg_threshold_flags_noalloc", "wg_set_stage_form", "wg_get_stage_form",
     "wg_wavelet_decompose", "wg_wavelet_reconstruct", "wg_wavelet_threshold", "wg_threshold_flags_wd",
-    "wg_adapt", "wg_adapt_profile",
+    "wg_adapt", "wg_adapt_profile", "wg_rk4_stream",
 ]
 
 
@@ -54,6 +54,7 @@ _SIGS = {
     "wg_wavelet_decompose": (_i, [_vp, _i]),
     "wg_adapt": (_i, [_vp, _i, _dp, _i, ctypes.POINTER(ctypes.c_int)]),
     "wg_adapt_profile": (_i, [_vp, _i, _dp, _i]),
+    "wg_rk4_stream": (_i, [_vp, _i, _i, ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "wg_wavelet_reconstruct": (_i, [_vp, _i]),
     "wg_wavelet_threshold": (_i, [_vp, _i, _dp]),
     "wg_get_stage_form": (_i, [_vp, ctypes.POINTER(ctypes.c_int)]),

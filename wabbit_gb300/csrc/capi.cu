@@ -173,6 +173,10 @@ struct wg_ctx {
     double *staging = nullptr;          // compact interior staging buffer
     cudaStream_t copy_stream = nullptr; // host<->device copies of the interior transfers
     std::vector<cudaEvent_t> copy_ev;   // one per chunk
+    cudaStream_t d2h_stream = nullptr;  // results of wg_rk4_stream
+    double *staging2 = nullptr;         // second staging buffer of wg_rk4_stream
+    size_t staging2_bytes = 0;
+    cudaEvent_t io_ev[8] = {};          // wg_rk4_stream: h2d done, d2h done, scattered, gathered (x2)
     size_t staging_bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -992,6 +996,10 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->d_clk);
     for (cudaEvent_t ev : ctx->copy_ev) cudaEventDestroy(ev);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    for (cudaEvent_t ev : ctx->io_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->d2h_stream) cudaStreamDestroy(ctx->d2h_stream);
+    cudaFree(ctx->staging2);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return WG_OK;
@@ -2342,6 +2350,74 @@ int wg_download_interior(wg_ctx *ctx, int tree, double *host) {
     Tree *t = get_tree(ctx, tree);
     if (!t || !host) return fail(WG_EINVAL, "bad arguments");
     return interior_transfer(ctx, t, host, 0);
+}
+
+// Streaming RK4 steps with host buffers: two staging buffers, the input of
+// step k+1 copied in (copy stream) while step k computes, the result of step
+// k copied out (d2h stream) while step k+1 computes. Every step scatters its
+// input into the state (and the FP32-pipe copy), steps, and gathers the
+// result.
+int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, double *const *outs) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || nsteps < 0 || (nsteps && (!ins || !outs))) return fail(WG_EINVAL, "bad arguments");
+    for (int k = 0; k < nsteps; k++)
+        if (!ins[k] || !outs[k]) return fail(WG_EINVAL, "null buffer for step %d", k);
+    if (nsteps == 0) return WG_OK;
+    const int *Bs = ctx->cfg.Bs;
+    const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
+    const int nblk = (int)t->slots.size();
+    const size_t per = (size_t)ctx->geo.nc * ctx->nint, bytes = sizeof(double) * per * nblk;
+    int st = ensure_staging(ctx, bytes);
+    if (st) return st;
+    if (ctx->staging2_bytes < bytes) {
+        cudaFree(ctx->staging2);
+        ctx->staging2 = nullptr;
+        ctx->staging2_bytes = 0;
+        if (cudaMalloc(&ctx->staging2, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(WG_ENOMEM, "second staging buffer of %zu bytes does not fit", bytes);
+        }
+        ctx->staging2_bytes = bytes;
+    }
+    if ((st = ensure_copy_stream(ctx, 1))) return st;
+    if (!ctx->d2h_stream && cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        ctx->d2h_stream = nullptr;
+        return fail(WG_ECUDA, "cudaStreamCreate failed");
+    }
+    for (cudaEvent_t &ev : ctx->io_ev)
+        if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return fail(WG_ECUDA, "cudaEventCreate failed");
+    cudaEvent_t *h2d_done = ctx->io_ev, *d2h_done = ctx->io_ev + 2, *gathered = ctx->io_ev + 4;
+    const bool shadow = ctx->precision == WG_RHS_FP32;
+    bool push = false;
+    if (shadow && (st = thin_plan(ctx, *t, &push))) return st;
+    double *S[2] = {ctx->staging, ctx->staging2};
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    WG_CUDA_OK(cudaMemcpyAsync(S[0], ins[0], bytes, cudaMemcpyDefault, ctx->copy_stream));
+    WG_CUDA_OK(cudaEventRecord(h2d_done[0], ctx->copy_stream));
+    for (int k = 0; k < nsteps; k++) {
+        const int cur = k & 1, nxt = cur ^ 1;
+        // the next input, into the other buffer once its last result is out
+        if (k + 1 < nsteps) {
+            if (k >= 1) WG_CUDA_OK(cudaStreamWaitEvent(ctx->copy_stream, d2h_done[nxt], 0));
+            WG_CUDA_OK(cudaMemcpyAsync(S[nxt], ins[k + 1], bytes, cudaMemcpyDefault, ctx->copy_stream));
+            WG_CUDA_OK(cudaEventRecord(h2d_done[nxt], ctx->copy_stream));
+        }
+        WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, h2d_done[cur], 0));
+        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, S[cur], ctx->A, ctx->gA, shadow ? ctx->B : nullptr, ctx->gT,
+                                        ctx->geo.nc, Bs[0], Bs[1], Bz, push ? ctx->d_push : nullptr, 1, ctx->stream));
+        t->shadow_valid = shadow;
+        if ((st = rk4_enqueue(ctx, tree))) return st;
+        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, S[cur], ctx->A, ctx->gA, nullptr, ctx->gT, ctx->geo.nc, Bs[0],
+                                        Bs[1], Bz, nullptr, 0, ctx->stream));
+        WG_CUDA_OK(cudaEventRecord(gathered[cur], ctx->stream));
+        WG_CUDA_OK(cudaStreamWaitEvent(ctx->d2h_stream, gathered[cur], 0));
+        WG_CUDA_OK(cudaMemcpyAsync(outs[k], S[cur], bytes, cudaMemcpyDefault, ctx->d2h_stream));
+        WG_CUDA_OK(cudaEventRecord(d2h_done[cur], ctx->d2h_stream));
+    }
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->d2h_stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->copy_stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return WG_OK;
 }
 
 }  // extern "C"

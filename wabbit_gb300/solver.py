@@ -162,6 +162,20 @@ class Forest:
         capi.check(self.L.wg_download_interior(self.ctx.h, self.tree, _p(out)))
         return out
 
+    def rk4_stream(self, ins, outs):
+        """len(ins) RK4 steps with host buffers (wg_rk4_stream): step k starts
+        from the interior state ins[k] and writes its result to outs[k];
+        page-locked buffers let the transfers overlap the steps."""
+        if len(ins) != len(outs):
+            raise ValueError("ins and outs differ in length")
+        n = self.nblocks * int(np.prod(self.interior_shape))
+        for a in list(ins) + list(outs):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != n:
+                raise ValueError("buffers must be contiguous float64 arrays of the interior size")
+        pin = (ctypes.POINTER(ctypes.c_double) * len(ins))(*[_p(a) for a in ins])
+        pout = (ctypes.POINTER(ctypes.c_double) * len(outs))(*[_p(a) for a in outs])
+        capi.check(self.L.wg_rk4_stream(self.ctx.h, self.tree, len(ins), pin, pout))
+
     def set_mask(self, mask):
         if mask is None:
             capi.check(self.L.wg_set_mask(self.ctx.h, self.tree, None))
