@@ -174,9 +174,9 @@ struct wg_ctx {
     cudaStream_t copy_stream = nullptr; // host<->device copies of the interior transfers
     std::vector<cudaEvent_t> copy_ev;   // one per chunk
     cudaStream_t d2h_stream = nullptr;  // results of wg_rk4_stream
-    double *staging2 = nullptr;         // second staging buffer of wg_rk4_stream
-    size_t staging2_bytes = 0;
-    cudaEvent_t io_ev[8] = {};          // wg_rk4_stream: h2d done, d2h done, scattered, gathered (x2)
+    double *stream_buf = nullptr;       // wg_rk4_stream: two input and two output staging buffers
+    size_t stream_buf_bytes = 0;
+    cudaEvent_t io_ev[8] = {};          // wg_rk4_stream: h2d done, d2h done, gathered, scattered (x2)
     size_t staging_bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -999,7 +999,7 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     for (cudaEvent_t ev : ctx->io_ev)
         if (ev) cudaEventDestroy(ev);
     if (ctx->d2h_stream) cudaStreamDestroy(ctx->d2h_stream);
-    cudaFree(ctx->staging2);
+    cudaFree(ctx->stream_buf);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return WG_OK;
@@ -2367,17 +2367,16 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     const int Bz = ctx->cfg.dim == 3 ? Bs[2] : 1;
     const int nblk = (int)t->slots.size();
     const size_t per = (size_t)ctx->geo.nc * ctx->nint, bytes = sizeof(double) * per * nblk;
-    int st = ensure_staging(ctx, bytes);
-    if (st) return st;
-    if (ctx->staging2_bytes < bytes) {
-        cudaFree(ctx->staging2);
-        ctx->staging2 = nullptr;
-        ctx->staging2_bytes = 0;
-        if (cudaMalloc(&ctx->staging2, bytes) != cudaSuccess) {
+    int st;
+    if (ctx->stream_buf_bytes < 4 * bytes) {
+        cudaFree(ctx->stream_buf);
+        ctx->stream_buf = nullptr;
+        ctx->stream_buf_bytes = 0;
+        if (cudaMalloc(&ctx->stream_buf, 4 * bytes) != cudaSuccess) {
             cudaGetLastError();
-            return fail(WG_ENOMEM, "second staging buffer of %zu bytes does not fit", bytes);
+            return fail(WG_ENOMEM, "staging buffers of 4 x %zu bytes do not fit", bytes);
         }
-        ctx->staging2_bytes = bytes;
+        ctx->stream_buf_bytes = 4 * bytes;
     }
     if ((st = ensure_copy_stream(ctx, 1))) return st;
     if (!ctx->d2h_stream && cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -2386,32 +2385,38 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     }
     for (cudaEvent_t &ev : ctx->io_ev)
         if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return fail(WG_ECUDA, "cudaEventCreate failed");
-    cudaEvent_t *h2d_done = ctx->io_ev, *d2h_done = ctx->io_ev + 2, *gathered = ctx->io_ev + 4;
+    // I[k & 1] receives step k's input, O[k & 1] its result: the copy in of
+    // step k+1 waits only for the scatter of step k-1, the copy out of step k
+    // only for its gather, so both directions use the link at once
+    cudaEvent_t *h2d_done = ctx->io_ev, *d2h_done = ctx->io_ev + 2, *gathered = ctx->io_ev + 4,
+                *scattered = ctx->io_ev + 6;
     const bool shadow = ctx->precision == WG_RHS_FP32;
     bool push = false;
     if (shadow && (st = thin_plan(ctx, *t, &push))) return st;
-    double *S[2] = {ctx->staging, ctx->staging2};
+    const size_t pb = per * nblk;
+    double *I[2] = {ctx->stream_buf, ctx->stream_buf + pb}, *O[2] = {ctx->stream_buf + 2 * pb, ctx->stream_buf + 3 * pb};
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-    WG_CUDA_OK(cudaMemcpyAsync(S[0], ins[0], bytes, cudaMemcpyDefault, ctx->copy_stream));
+    WG_CUDA_OK(cudaMemcpyAsync(I[0], ins[0], bytes, cudaMemcpyDefault, ctx->copy_stream));
     WG_CUDA_OK(cudaEventRecord(h2d_done[0], ctx->copy_stream));
     for (int k = 0; k < nsteps; k++) {
         const int cur = k & 1, nxt = cur ^ 1;
-        // the next input, into the other buffer once its last result is out
         if (k + 1 < nsteps) {
-            if (k >= 1) WG_CUDA_OK(cudaStreamWaitEvent(ctx->copy_stream, d2h_done[nxt], 0));
-            WG_CUDA_OK(cudaMemcpyAsync(S[nxt], ins[k + 1], bytes, cudaMemcpyDefault, ctx->copy_stream));
+            if (k >= 1) WG_CUDA_OK(cudaStreamWaitEvent(ctx->copy_stream, scattered[nxt], 0));
+            WG_CUDA_OK(cudaMemcpyAsync(I[nxt], ins[k + 1], bytes, cudaMemcpyDefault, ctx->copy_stream));
             WG_CUDA_OK(cudaEventRecord(h2d_done[nxt], ctx->copy_stream));
         }
         WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, h2d_done[cur], 0));
-        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, S[cur], ctx->A, ctx->gA, shadow ? ctx->B : nullptr, ctx->gT,
+        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, I[cur], ctx->A, ctx->gA, shadow ? ctx->B : nullptr, ctx->gT,
                                         ctx->geo.nc, Bs[0], Bs[1], Bz, push ? ctx->d_push : nullptr, 1, ctx->stream));
+        WG_CUDA_OK(cudaEventRecord(scattered[cur], ctx->stream));
         t->shadow_valid = shadow;
         if ((st = rk4_enqueue(ctx, tree))) return st;
-        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, S[cur], ctx->A, ctx->gA, nullptr, ctx->gT, ctx->geo.nc, Bs[0],
+        if (k >= 2) WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, d2h_done[cur], 0));
+        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[cur], ctx->A, ctx->gA, nullptr, ctx->gT, ctx->geo.nc, Bs[0],
                                         Bs[1], Bz, nullptr, 0, ctx->stream));
         WG_CUDA_OK(cudaEventRecord(gathered[cur], ctx->stream));
         WG_CUDA_OK(cudaStreamWaitEvent(ctx->d2h_stream, gathered[cur], 0));
-        WG_CUDA_OK(cudaMemcpyAsync(outs[k], S[cur], bytes, cudaMemcpyDefault, ctx->d2h_stream));
+        WG_CUDA_OK(cudaMemcpyAsync(outs[k], O[cur], bytes, cudaMemcpyDefault, ctx->d2h_stream));
         WG_CUDA_OK(cudaEventRecord(d2h_done[cur], ctx->d2h_stream));
     }
     WG_CUDA_OK(cudaStreamSynchronize(ctx->d2h_stream));
