@@ -1330,7 +1330,11 @@ int wg_compute_dt(wg_ctx *ctx, int tree, double *dt) {
 int wg_rk4_step(wg_ctx *ctx, int tree, double *time, double *dt) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return WG_EINVAL;
-    int st = ensure_shadow(ctx, *t);
+    // the stage-kernel form is chosen before the first step (stage buffers
+    // C and D are scratch at this point)
+    int st = autotune_stage_form(ctx, *t);
+    if (st) return st;
+    st = ensure_shadow(ctx, *t);
     if (st) return st;
     st = rk4_enqueue(ctx, tree);
     if (st) return st;
@@ -2393,6 +2397,7 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     const bool shadow = ctx->precision == WG_RHS_FP32;
     bool push = false;
     if (shadow && (st = thin_plan(ctx, *t, &push))) return st;
+    if ((st = autotune_stage_form(ctx, *t))) return st;
     const size_t pb = per * nblk;
     double *I[2] = {ctx->stream_buf, ctx->stream_buf + pb}, *O[2] = {ctx->stream_buf + 2 * pb, ctx->stream_buf + 3 * pb};
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
