@@ -461,7 +461,8 @@ def run_serving(args, rank, world):
                    "cycle": "sync, refine everywhere, chunk of RK4 steps, adapt_tree" if args.adapt_every else None,
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "serving": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "wall_s": summ["wall_s"],
-                    "requests": summ["requests"], "point_updates": summ["point_updates"]},
+                    "requests": summ["requests"], "point_updates": summ["point_updates"],
+                    "phase_s": summ["phase_s"]},
         "clocks": clk.summary(),
     }
     if rank == 0:

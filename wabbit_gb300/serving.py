@@ -259,6 +259,7 @@ class Server:
         records = {}
         t0 = time.perf_counter()
         total_points = 0
+        phase = {"refine": 0.0, "run": 0.0, "adapt": 0.0, "admit": 0.0, "retire": 0.0}
         while pending or any(queue.values()) or any(active.values()):
             now = time.perf_counter() - t0
             if not realtime:   # every request has arrived
@@ -266,6 +267,7 @@ class Server:
             while pending and pending[0].arrival <= now:
                 r = pending.pop(0)
                 queue[r.dim].append(r)
+            ta = time.perf_counter()
             for dim in (3, 2):
                 while queue[dim]:
                     r = queue[dim][0]
@@ -280,6 +282,7 @@ class Server:
                     s.admitted = time.perf_counter() - t0
                     used[dim] += s.nblk
                     active[dim].append(s)
+            phase["admit"] += time.perf_counter() - ta
             if not any(active.values()):
                 if pending:
                     time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
@@ -290,6 +293,7 @@ class Server:
                 if not active[dim]:
                     continue
                 group = active[dim]
+                tr = time.perf_counter()
                 if self.adapt:
                     group, grow, mothers = [], 0, 0
                     for s in active[dim]:
@@ -303,7 +307,12 @@ class Server:
                     if not group:
                         raise RuntimeError(f"no {dim}-D solve fits its adaptation cycle into the arena")
                 k = min(self.chunk, min(s.req.nsteps - s.done for s in group))
+                t1 = time.perf_counter()
+                phase["refine"] += t1 - tr
                 self.ctx[dim].run([s.f for s in group], k, use_graph=True)
+                self.ctx[dim].synchronize()
+                t2 = time.perf_counter()
+                phase["run"] += t2 - t1
                 for s in group:
                     s.done += k
                     total_points += s.points * k
@@ -312,8 +321,10 @@ class Server:
                         before = s.nblk
                         s.nblk = s.f.adapt(np.full(s.cfg.neq, self.eps))
                         used[dim] += s.nblk - before
+                phase["adapt"] += time.perf_counter() - t2
             for dim in (3, 2):
                 self.ctx[dim].synchronize()
+            tt = time.perf_counter()
             for dim in (3, 2):
                 keep = []
                 for s in active[dim]:
@@ -332,11 +343,13 @@ class Server:
                     s.f.destroy()
                     used[dim] -= s.nblk
                 active[dim] = keep
+            phase["retire"] += time.perf_counter() - tt
         wall = time.perf_counter() - t0
         tts = np.array([r["tts"] for r in records.values()])
         summary = {"requests": len(records), "wall_s": wall, "point_updates": total_points,
                    "throughput": total_points / wall,
-                   "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99))}
+                   "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
+                   "phase_s": phase}
         return records, summary
 
 
