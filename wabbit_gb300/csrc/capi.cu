@@ -2038,26 +2038,25 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     const int nr = (int)ref.size();
     if ((size_t)nr * nd > ctx->free_slots.size()) return fail(WG_ENOMEM, "refinement needs %d free slots", nr * nd);
     const int nn = nb + nr * (nd - 1);
-    std::vector<int> lv, co, slots, child_base(nb, -1), parents, bases;
+    std::vector<int> lv, co, slots, child_first(nb, -1), parents, bases;
     lv.reserve(nn);
     co.reserve(3 * nn);
     slots.reserve(nn);
-    // daughters need consecutive slots: take them from the free list in runs
+    // the daughters take any free slots (lowest first): bases[p * nd + k]
     std::vector<int> fs = ctx->free_slots;
     std::sort(fs.begin(), fs.end());
     std::vector<int> used;
     size_t i = 0;
     for (int b : ref) {
-        while (i + nd <= fs.size() && fs[i + nd - 1] - fs[i] != nd - 1) i++;
-        if (i + nd > fs.size()) return fail(WG_ENOMEM, "no consecutive free slots for daughters");
-        child_base[b] = fs[i];
-        for (int k = 0; k < nd; k++) used.push_back(fs[i + k]);
-        i += nd;
+        child_first[b] = (int)bases.size();
+        for (int k = 0; k < nd; k++) {
+            used.push_back(fs[i]);
+            bases.push_back(fs[i++]);
+        }
         parents.push_back(t->slots[b]);
-        bases.push_back(fs[i - nd]);
     }
     for (int b = 0; b < nb; b++) {
-        if (child_base[b] < 0) {   // stays on Jmax
+        if (child_first[b] < 0) {   // stays on Jmax
             lv.push_back(t->forest.level[b]);
             for (int a = 0; a < 3; a++) co.push_back(t->forest.coords[3 * b + a]);
             slots.push_back(t->slots[b]);
@@ -2068,13 +2067,13 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
             co.push_back(2 * t->forest.coords[3 * b + 0] + (k / 2) % 2);
             co.push_back(2 * t->forest.coords[3 * b + 1] + k % 2);
             co.push_back(dim == 3 ? 2 * t->forest.coords[3 * b + 2] + k / 4 : 0);
-            slots.push_back(child_base[b] + k);
+            slots.push_back(bases[child_first[b] + k]);
         }
     }
     if (nr > 0) {
         DevArray<int> d_par, d_base;
         WG_CUDA_OK(d_par.upload(parents.data(), nr, ctx->stream));
-        WG_CUDA_OK(d_base.upload(bases.data(), nr, ctx->stream));
+        WG_CUDA_OK(d_base.upload(bases.data(), bases.size(), ctx->stream));
         const int *Bs = ctx->cfg.Bs;
         WG_CUDA_OK(launch_refine(dim, d_par.p, nr, d_base.p, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], ctx->geo.nc,
                                  ctx->wav.order_predictor, ctx->stream));

@@ -193,7 +193,8 @@ int noalloc_max_blocks();
 cudaError_t launch_fwt_flags_noalloc(int dim, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,
                                      int nc, int wavelet_x, int wavelet_y, const double *eps_host,
                                      const int *tsvc_host, int *flags, double *details, cudaStream_t s);
-cudaError_t launch_refine(int dim, const int *parent, int nparent, const int *child_base, const double *u,
+// child_slot: 2^dim arena slots per parent, daughter k of parent p at [p * 2^dim + k]
+cudaError_t launch_refine(int dim, const int *parent, int nparent, const int *child_slot, const double *u,
                           BufGeo geo, int Bs0, int Bs1, int Bs2, int nc, int order_predictor, cudaStream_t s);
 
 }  // namespace wg

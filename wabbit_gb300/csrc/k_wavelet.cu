@@ -994,49 +994,50 @@ cudaError_t launch_fwt_flags_noalloc(int dim, int nblk, const double *u, BufGeo 
     return cudaGetLastError();
 }
 
-// refineBlock: daughter k of parent p is written to slot child_base[p] + k
-__global__ void __launch_bounds__(256) refine_kernel(const int *parent, const int *child_base, const double *u,
-                                                     BufGeo geo, int dim, int Bs0, int Bs1, int Bs2, int nc,
-                                                     int order_idx, int ncoef, long long npts_per) {
+// refineBlock: daughter k of parent p is written to slot child_slot[p * 2^d + k]
+__global__ void __launch_bounds__(256) refine_kernel(const int *parent, int nparent, const int *child_slot,
+                                                     const double *u, BufGeo geo, int dim, int Bs0, int Bs1, int Bs2,
+                                                     int nc, int order_idx, int ncoef) {
     const int nd = 1 << dim;
     const long long np = geo.npts();
     const long long total = (long long)nd * np;
-    const int pi = blockIdx.y;
-    const int pb = parent[pi];
-    const double *src = u + (long long)pb * nc * np;
-    PredCtx pc;
-    pc.nx = geo.nx;
-    pc.ny = geo.ny;
-    pc.sx = pc.sy = pc.sz = 0;
-    pc.Fx = 2 * geo.nx - 1;
-    pc.Fy = 2 * geo.ny - 1;
-    pc.Fz = dim == 3 ? 2 * geo.nz - 1 : 1;
-    pc.nc = ncoef;
-    pc.c = c_pred[order_idx];
-    const int g = geo.gb;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(q / np);
-        const long long r = q % np;
-        const int ix = (int)(r % geo.nx), iy = (int)((r / geo.nx) % geo.ny), iz = (int)(r / ((long long)geo.nx * geo.ny));
-        const int fx = g + Bs0 * ((k / 2) % 2) + ix;
-        const int fy = g + Bs1 * (k % 2) + iy;
-        const int fz = dim == 3 ? g + Bs2 * (k / 4) + iz : 0;
-        double *dst = const_cast<double *>(u) + ((long long)(child_base[pi] + k) * nc) * np + r;
-        for (int c = 0; c < nc; c++) {
-            pc.src = src + c * np;
-            dst[c * np] = pred_xyz(pc, fx, fy, fz);
+    for (int pi = blockIdx.y; pi < nparent; pi += gridDim.y) {
+        const int pb = parent[pi];
+        const double *src = u + (long long)pb * nc * np;
+        PredCtx pc;
+        pc.nx = geo.nx;
+        pc.ny = geo.ny;
+        pc.sx = pc.sy = pc.sz = 0;
+        pc.Fx = 2 * geo.nx - 1;
+        pc.Fy = 2 * geo.ny - 1;
+        pc.Fz = dim == 3 ? 2 * geo.nz - 1 : 1;
+        pc.nc = ncoef;
+        pc.c = c_pred[order_idx];
+        const int g = geo.gb;
+        for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+            const int k = (int)(q / np);
+            const long long r = q % np;
+            const int ix = (int)(r % geo.nx), iy = (int)((r / geo.nx) % geo.ny), iz = (int)(r / ((long long)geo.nx * geo.ny));
+            const int fx = g + Bs0 * ((k / 2) % 2) + ix;
+            const int fy = g + Bs1 * (k % 2) + iy;
+            const int fz = dim == 3 ? g + Bs2 * (k / 4) + iz : 0;
+            double *dst = const_cast<double *>(u) + ((long long)child_slot[(long long)pi * nd + k] * nc) * np + r;
+            for (int c = 0; c < nc; c++) {
+                pc.src = src + c * np;
+                dst[c * np] = pred_xyz(pc, fx, fy, fz);
+            }
         }
     }
 }
 
-cudaError_t launch_refine(int dim, const int *parent, int nparent, const int *child_base, const double *u,
+cudaError_t launch_refine(int dim, const int *parent, int nparent, const int *child_slot, const double *u,
                           BufGeo geo, int Bs0, int Bs1, int Bs2, int nc, int order_predictor, cudaStream_t s) {
     if (nparent <= 0) return cudaSuccess;
     cudaError_t e = init_predictor();
     if (e != cudaSuccess) return e;
-    dim3 grid(64, nparent);
-    refine_kernel<<<grid, 256, 0, s>>>(parent, child_base, u, geo, dim, Bs0, Bs1, Bs2, nc, order_predictor / 2 - 1,
-                                       order_predictor, 0);
+    dim3 grid(64, std::min(nparent, 65535));
+    refine_kernel<<<grid, 256, 0, s>>>(parent, nparent, child_slot, u, geo, dim, Bs0, Bs1, Bs2, nc,
+                                       order_predictor / 2 - 1, order_predictor);
     return cudaGetLastError();
 }
 
