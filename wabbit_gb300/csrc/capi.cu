@@ -73,6 +73,34 @@ struct DevArray {
     }
 };
 
+// Free arena slots as a bitmap (bit set = free): take() hands out the lowest
+// free slot, give() returns one; no sort of the free list per grid change.
+struct SlotPool {
+    std::vector<uint64_t> bits;
+    size_t nfree = 0;
+    size_t first = 0;   // every word below this one is empty
+    void init(int n) {
+        bits.assign(((size_t)n + 63) / 64, 0);
+        for (int i = 0; i < n; i++) bits[(size_t)i >> 6] |= 1ull << (i & 63);
+        nfree = (size_t)n;
+        first = 0;
+    }
+    size_t size() const { return nfree; }
+    void give(int s) {
+        bits[(size_t)s >> 6] |= 1ull << (s & 63);
+        nfree++;
+        first = std::min(first, (size_t)s >> 6);
+    }
+    int take() {
+        if (!nfree) return -1;
+        while (!bits[first]) first++;
+        const int b = __builtin_ctzll(bits[first]);
+        bits[first] &= bits[first] - 1;
+        nfree--;
+        return (int)(first * 64 + b);
+    }
+};
+
 // Prediction patches of the stages of a table, sorted within each stage by
 // the shared memory the CTA-per-patch kernel needs and cut into classes;
 // each class launches with its own largest need.
@@ -162,7 +190,7 @@ struct wg_ctx {
     TreeClock *d_clk = nullptr;
     int max_trees = 64;
     std::vector<Tree> trees;
-    std::vector<int> free_slots;
+    SlotPool free_slots;
     cudaStream_t stream = nullptr;
     int variant_fast = 1;               // 1: FMA stencil, 0: strict reference arithmetic
     int precision = WG_RHS_FP64;        // WG_RHS_FP32: double-float stencils on the FP32 units
@@ -468,7 +496,7 @@ int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool 
 }
 
 void release_tree_blocks(wg_ctx *ctx, Tree &t) {
-    for (int s : t.slots) ctx->free_slots.push_back(s);
+    for (int s : t.slots) ctx->free_slots.give(s);
     for (int m : t.mask_slot)
         if (m >= 0) ctx->mask_free.push_back(m);
     t.slots.clear();
@@ -517,7 +545,16 @@ int upload_desc(wg_ctx *ctx, Tree &t, int tree_id) {
         d.level = lv;
         d.mask = t.mask_slot[b];
         ctx->h_desc[t.slots[b]] = d;
-        WG_CUDA_OK(cudaMemcpyAsync(ctx->d_desc + t.slots[b], &d, sizeof(d), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    // one copy per run of consecutive slots from the host mirror
+    std::vector<int> sl(t.slots);
+    std::sort(sl.begin(), sl.end());
+    for (size_t i = 0; i < sl.size();) {
+        size_t j = i + 1;
+        while (j < sl.size() && sl[j] == sl[j - 1] + 1) j++;
+        WG_CUDA_OK(cudaMemcpyAsync(ctx->d_desc + sl[i], ctx->h_desc.data() + sl[i], sizeof(BlockDesc) * (j - i),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+        i = j;
     }
     return WG_OK;
 }
@@ -962,8 +999,7 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
     cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream);
     cudaMemsetAsync(ctx->d_clk, 0, sizeof(TreeClock) * ctx->max_trees, ctx->stream);
     ctx->h_desc.resize(max_blocks);
-    ctx->free_slots.reserve(max_blocks);
-    for (int i = max_blocks - 1; i >= 0; i--) ctx->free_slots.push_back(i);   // back() = lowest slot
+    ctx->free_slots.init(max_blocks);
     ctx->trees.resize(ctx->max_trees);
     std::vector<int> ids(ctx->max_trees);
     for (int i = 0; i < ctx->max_trees; i++) ids[i] = i;
@@ -1057,8 +1093,6 @@ int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *co
     release_tree_blocks(ctx, *t);
     if ((size_t)nblk > ctx->free_slots.size())
         return fail(WG_ENOMEM, "grid of %d blocks does not fit (%zu free slots)", nblk, ctx->free_slots.size());
-    // hand out the lowest free slots in ascending order (contiguous copies)
-    std::sort(ctx->free_slots.begin(), ctx->free_slots.end(), std::greater<int>());
     t->forest.set(nblk, level, coords);
     std::string err;
     if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "%s", err.c_str());
@@ -1066,10 +1100,8 @@ int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *co
     t->slots.resize(nblk);
     t->mask_slot.assign(nblk, -1);
     t->shadow_valid = false;
-    for (int b = 0; b < nblk; b++) {
-        t->slots[b] = ctx->free_slots.back();
-        ctx->free_slots.pop_back();
-    }
+    // the lowest free slots in ascending order (contiguous copies)
+    for (int b = 0; b < nblk; b++) t->slots[b] = ctx->free_slots.take();
     int st;
     if ((st = upload_desc(ctx, *t, tree))) return st;
     if ((st = upload_lists(ctx, *t))) return st;
@@ -1573,11 +1605,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         }
     }
     for (int b = 0; b < nb; b++) L.slot[b] = t->slots[b];
-    std::sort(ctx->free_slots.begin(), ctx->free_slots.end(), std::greater<int>());
-    for (int b = nb; b < nt; b++) {
-        L.slot[b] = ctx->free_slots.back();
-        ctx->free_slots.pop_back();
-    }
+    for (int b = nb; b < nt; b++) L.slot[b] = ctx->free_slots.take();
     // device lists stay alive until the end (the stream is synchronised there)
     std::vector<std::unique_ptr<DevArray<Patch>>> kp;
     std::vector<std::unique_ptr<DevArray<FilterEntry>>> kf;
@@ -1674,7 +1702,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     };
     auto fail_restore = [&](cudaError_t ce2, int st) {
         cudaStreamSynchronize(ctx->stream);
-        for (int b = nb; b < nt; b++) ctx->free_slots.push_back(L.slot[b]);
+        for (int b = nb; b < nt; b++) ctx->free_slots.give(L.slot[b]);
         if (ce2 != cudaSuccess) return cuda_fail(ce2, "wg_adapt (lifted)", __FILE__, __LINE__);
         return st;
     };
@@ -1876,7 +1904,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         kept[b] = 1;
     }
     for (int b = 0; b < nt; b++)
-        if (!kept[b]) ctx->free_slots.push_back(L.slot[b]);
+        if (!kept[b]) ctx->free_slots.give(L.slot[b]);
     for (int m : t->mask_slot)
         if (m >= 0) ctx->mask_free.push_back(m);
     t->forest.set(nn, lv.data(), co.data());
@@ -1926,16 +1954,12 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
         return fail(WG_ENOMEM, "adapt needs %d free slots for the mothers (%zu free)", nm, ctx->free_slots.size());
     std::vector<int> slot(nt);
     for (int b = 0; b < nb; b++) slot[b] = t->slots[b];
-    std::sort(ctx->free_slots.begin(), ctx->free_slots.end(), std::greater<int>());
-    for (int b = nb; b < nt; b++) {
-        slot[b] = ctx->free_slots.back();
-        ctx->free_slots.pop_back();
-    }
+    for (int b = nb; b < nt; b++) slot[b] = ctx->free_slots.take();
     auto give_back = [&](const std::vector<int> &keep) {
         std::vector<char> kept(nt, 0);
         for (int b : keep) kept[b] = 1;
         for (int b = 0; b < nt; b++)
-            if (!kept[b]) ctx->free_slots.push_back(slot[b]);
+            if (!kept[b]) ctx->free_slots.give(slot[b]);
     };
     std::vector<int> flags(nt, 0);
     DevArray<int> d_flags, d_tsvc, d_list;
@@ -1990,7 +2014,7 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         cudaStreamSynchronize(ctx->stream);
-        for (int b = nb; b < nt; b++) ctx->free_slots.push_back(slot[b]);   // the grid is unchanged
+        for (int b = nb; b < nt; b++) ctx->free_slots.give(slot[b]);   // the grid is unchanged
         return cuda_fail(e, "wg_adapt", __FILE__, __LINE__);
     }
     std::vector<int> leaves;
@@ -2043,16 +2067,9 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     co.reserve(3 * nn);
     slots.reserve(nn);
     // the daughters take any free slots (lowest first): bases[p * nd + k]
-    std::vector<int> fs = ctx->free_slots;
-    std::sort(fs.begin(), fs.end());
-    std::vector<int> used;
-    size_t i = 0;
     for (int b : ref) {
         child_first[b] = (int)bases.size();
-        for (int k = 0; k < nd; k++) {
-            used.push_back(fs[i]);
-            bases.push_back(fs[i++]);
-        }
+        for (int k = 0; k < nd; k++) bases.push_back(ctx->free_slots.take());
         parents.push_back(t->slots[b]);
     }
     for (int b = 0; b < nb; b++) {
@@ -2072,23 +2089,23 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     }
     if (nr > 0) {
         DevArray<int> d_par, d_base;
-        WG_CUDA_OK(d_par.upload(parents.data(), nr, ctx->stream));
-        WG_CUDA_OK(d_base.upload(bases.data(), bases.size(), ctx->stream));
         const int *Bs = ctx->cfg.Bs;
-        WG_CUDA_OK(launch_refine(dim, d_par.p, nr, d_base.p, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], ctx->geo.nc,
-                                 ctx->wav.order_predictor, ctx->stream));
-        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        cudaError_t e = d_par.upload(parents.data(), nr, ctx->stream);
+        if (e == cudaSuccess) e = d_base.upload(bases.data(), bases.size(), ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_refine(dim, d_par.p, nr, d_base.p, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], ctx->geo.nc,
+                              ctx->wav.order_predictor, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) {   // the grid is unchanged
+            cudaStreamSynchronize(ctx->stream);
+            for (int s2 : bases) ctx->free_slots.give(s2);
+            return cuda_fail(e, "wg_refine_everywhere", __FILE__, __LINE__);
+        }
     }
     // swap the tree onto the new blocks
-    std::sort(used.begin(), used.end());
-    std::vector<int> nf;
-    nf.reserve(ctx->free_slots.size());
-    for (int s2 : ctx->free_slots)
-        if (!std::binary_search(used.begin(), used.end(), s2)) nf.push_back(s2);
-    for (int s2 : parents) nf.push_back(s2);
+    for (int s2 : parents) ctx->free_slots.give(s2);
     for (int m : t->mask_slot)
         if (m >= 0) ctx->mask_free.push_back(m);
-    ctx->free_slots = nf;
     t->slots = slots;
     t->mask_slot.assign(nn, -1);
     t->shadow_valid = false;

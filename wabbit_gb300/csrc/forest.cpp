@@ -1,5 +1,6 @@
 // forest.cpp -- neighbour search and ghost-patch tables (host side).
 #include "forest.hpp"
+#include "par.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -262,7 +263,9 @@ bool Forest::update_neighbors(std::string &err, bool overlapping) {
         }
     }
     nbr.assign(size_t(n) * kNumRelations, -1);
-    for (int b = 0; b < n; b++) {
+    // the blocks are independent (each writes its own row); the first
+    // failing block in block order gives the error message
+    auto one = [&](int b, std::string &e) -> bool {
         const int lv = level[b];
         const int *c = &coords[3 * b];
         int *nb = &nbr[size_t(b) * kNumRelations];
@@ -365,9 +368,25 @@ bool Forest::update_neighbors(std::string &err, bool overlapping) {
                 int r = relation_of(d, p, dim);
                 if (nb[r - 1] >= 0 || nb[r - 1 + 56] >= 0 || nb[r - 1 + 112] >= 0) found = true;
             }
-            if (!found) { err = "block without a face neighbour (grid not complete or not graded)"; return false; }
+            if (!found) { e = "block without a face neighbour (grid not complete or not graded)"; return false; }
         }
-    }
+        return true;
+    };
+    const int nch = host_threads();
+    std::vector<int> bad(nch, n);
+    std::vector<std::string> msg(nch);
+    par_chunks(n, nch, [&](int ch, int lo, int hi) {
+        for (int b = lo; b < hi; b++)
+            if (!one(b, msg[ch])) {
+                bad[ch] = b;
+                return;
+            }
+    }, 4096);
+    for (int ch = 0; ch < nch; ch++)
+        if (bad[ch] < n) {
+            err = msg[ch];
+            return false;
+        }
     return true;
 }
 
@@ -515,31 +534,41 @@ bool make_sync_table(const Forest &f, const Geometry &geo, const WaveletInfo &w,
     const int shift = geo.g - g_buf;
     int nbuf[3];
     for (int d = 0; d < 3; d++) nbuf[d] = d < geo.dim ? geo.Bs[d] + 2 * g_buf : 1;
-    std::vector<std::vector<Patch>> per(nstages + 1);
     out.max_points = 0;
     out.max_coarse = 0;
-    for (int s = 0; s < f.size(); s++) {
+    const int n = f.size();
+    // the boxes of a patch depend only on (relation, level difference): one
+    // template per pair that occurs, checked once
+    struct Tmpl {
+        Patch p;
+        int npts = 0, need = 0;
+        const char *bad = nullptr;
+    };
+    std::vector<Tmpl> tm(3 * kNumRelations);
+    std::vector<char> used(3 * kNumRelations, 0);
+    for (int s = 0; s < n; s++) {
         const int *nb = &f.nbr[size_t(s) * kNumRelations];
         for (int r = 1; r <= kNumRelations; r++) {
             const int d = nb[r - 1];
             if (d < 0) continue;
             const int lvl_diff = f.level[s] - f.level[d];
-            int stage;
-            if (lvl_diff == 0) stage = 1;
-            else if (lvl_diff == +1) stage = 2 - unl;
-            else if (lvl_diff == -1) stage = 3 - unl;
-            else { err = "level jump larger than one between neighbours"; return false; }
+            if (lvl_diff < -1 || lvl_diff > 1) { err = "level jump larger than one between neighbours"; return false; }
+            used[(lvl_diff + 1) * kNumRelations + r - 1] = 1;
+        }
+    }
+    for (int lvl_diff = -1; lvl_diff <= 1; lvl_diff++)
+        for (int r = 1; r <= kNumRelations; r++) {
+            if (!used[(lvl_diff + 1) * kNumRelations + r - 1]) continue;
+            Tmpl &t = tm[(lvl_diff + 1) * kNumRelations + r - 1];
             int rb[2][3], sb[2][3], bb[2][3];
             recv_box(geo, inverse_relation(r), gminus, gplus, -lvl_diff, rb);
             send_box(geo, w.order_predictor, r, lvl_diff, gminus, gplus, sb, bb);
-            Patch p;
+            Patch &p = t.p;
             std::memset(&p, 0, sizeof(p));
-            p.src = s + block_offset;
-            p.dst = d + block_offset;
             p.op = lvl_diff == 0 ? 0 : (lvl_diff == +1 ? 1 : 2);
-            p.stage = (int16_t)stage;
+            p.stage = (int16_t)(lvl_diff == 0 ? 1 : lvl_diff == +1 ? 2 - unl : 3 - unl);
             int npts = 1;
-            for (int k = 0; k < 3; k++) {
+            for (int k = 0; k < 3 && !t.bad; k++) {
                 const bool active = k < geo.dim;
                 const int sh = active ? shift : 0;
                 p.rlo[k] = (int16_t)(rb[0][k] - 1 - sh);
@@ -549,19 +578,19 @@ bool make_sync_table(const Forest &f, const Geometry &geo, const WaveletInfo &w,
                 p.blo[k] = (int16_t)(bb[0][k] - 1);
                 npts *= (rb[1][k] - rb[0][k] + 1);
                 // bounds of every access in the ghost-width-g_buf buffer
-                if (p.rlo[k] < 0 || p.rhi[k] >= nbuf[k] || p.rlo[k] > p.rhi[k]) { err = "receiver box outside buffer"; return false; }
+                if (p.rlo[k] < 0 || p.rhi[k] >= nbuf[k] || p.rlo[k] > p.rhi[k]) { t.bad = "receiver box outside buffer"; break; }
                 if (p.op == 0) {
-                    if (p.slo[k] < 0 || p.slo[k] + (p.rhi[k] - p.rlo[k]) >= nbuf[k]) { err = "copy source outside buffer"; return false; }
+                    if (p.slo[k] < 0 || p.slo[k] + (p.rhi[k] - p.rlo[k]) >= nbuf[k]) t.bad = "copy source outside buffer";
                 } else if (p.op == 1) {
                     int hi = p.slo[k] + 2 * (p.blo[k] + p.rhi[k] - p.rlo[k]);
-                    if (p.slo[k] < 0 || hi >= nbuf[k] || (active && hi > p.shi[k])) { err = "restriction source outside buffer"; return false; }
+                    if (p.slo[k] < 0 || hi >= nbuf[k] || (active && hi > p.shi[k])) t.bad = "restriction source outside buffer";
                 } else {
                     int nf = 2 * (p.shi[k] - p.slo[k] + 1) - 1;
-                    if (p.slo[k] < 0 || p.shi[k] >= nbuf[k] || p.blo[k] + (p.rhi[k] - p.rlo[k]) >= nf) { err = "prediction box outside buffer"; return false; }
+                    if (p.slo[k] < 0 || p.shi[k] >= nbuf[k] || p.blo[k] + (p.rhi[k] - p.rlo[k]) >= nf) t.bad = "prediction box outside buffer";
                 }
             }
-            out.max_points = std::max(out.max_points, npts);
-            if (p.op == 2) {
+            t.npts = npts;
+            if (p.op == 2 && !t.bad) {
                 // shared memory of the separable prediction: coarse box, x
                 // window (even rows/planes) and x-y window (even planes)
                 const int h = w.order_predictor - 1;
@@ -575,26 +604,62 @@ bool make_sync_table(const Forest &f, const Geometry &geo, const WaveletInfo &w,
                 zw0 += zw0 & 1;
                 zw1 -= zw1 & 1;
                 const int wy = (yw1 - yw0) / 2 + 1, wz = (zw1 - zw0) / 2 + 1;
-                const int need = cx * cy * cz + ex * wy * wz + ex * ey * wz;
-                out.max_coarse = std::max(out.max_coarse, need);
+                t.need = cx * cy * cz + ex * wy * wz + ex * ey * wz;
             }
-            per[stage].push_back(p);
+            if (t.bad) { err = t.bad; return false; }
+            out.max_points = std::max(out.max_points, npts);
+            out.max_coarse = std::max(out.max_coarse, t.need);
         }
-    }
+    // a stage is a prediction stage iff all its relations predict
     out.nstages = nstages;
-    out.patches.clear();
     out.stage_begin.assign(nstages + 1, 0);
     out.stage_predict.assign(nstages, 0);
-    for (int s = 1; s <= nstages; s++) {
-        out.stage_begin[s - 1] = (int)out.patches.size();
-        bool all_pred = !per[s].empty();
-        for (const Patch &p : per[s]) all_pred = all_pred && p.op == 2;
-        bool any_pred = false;
-        for (const Patch &p : per[s]) any_pred = any_pred || p.op == 2;
-        if (any_pred && !all_pred) { err = "prediction mixed with copies in one stage"; return false; }
-        out.stage_predict[s - 1] = all_pred ? 1 : 0;
-        out.patches.insert(out.patches.end(), per[s].begin(), per[s].end());
+    for (int st = 1; st <= nstages; st++) {
+        bool any = false, all = true;
+        for (int i = 0; i < 3 * kNumRelations; i++)
+            if (used[i] && tm[i].p.stage == st) {
+                any = true;
+                all = all && tm[i].p.op == 2;
+                if (tm[i].p.op == 2) out.stage_predict[st - 1] = 1;
+            }
+        if (out.stage_predict[st - 1] && !all) { err = "prediction mixed with copies in one stage"; return false; }
+        if (!any) out.stage_predict[st - 1] = 0;
     }
+    // patches in (stage, sender, relation) order: count per chunk of senders,
+    // then every chunk writes its own ranges
+    const int nch = host_threads();
+    std::vector<int> cnt((size_t)nch * (nstages + 1), 0);
+    auto each = [&](int lo, int hi, auto g) {
+        for (int s = lo; s < hi; s++) {
+            const int *nb = &f.nbr[size_t(s) * kNumRelations];
+            for (int r = 1; r <= kNumRelations; r++) {
+                const int d = nb[r - 1];
+                if (d >= 0) g(s, d, tm[(f.level[s] - f.level[d] + 1) * kNumRelations + r - 1].p);
+            }
+        }
+    };
+    par_chunks(n, nch, [&](int ch, int lo, int hi) {
+        each(lo, hi, [&](int, int, const Patch &p) { cnt[(size_t)ch * (nstages + 1) + p.stage]++; });
+    }, 4096);
+    std::vector<size_t> off((size_t)nch * (nstages + 1), 0);
+    size_t at = 0;
+    for (int st = 1; st <= nstages; st++) {
+        out.stage_begin[st - 1] = (int)at;
+        for (int ch = 0; ch < nch; ch++) {
+            off[(size_t)ch * (nstages + 1) + st] = at;
+            at += cnt[(size_t)ch * (nstages + 1) + st];
+        }
+    }
+    out.patches.resize(at);
+    par_chunks(n, nch, [&](int ch, int lo, int hi) {
+        size_t *o = &off[(size_t)ch * (nstages + 1)];
+        each(lo, hi, [&](int s, int d, const Patch &t) {
+            Patch &p = out.patches[o[t.stage]++];
+            p = t;
+            p.src = s + block_offset;
+            p.dst = d + block_offset;
+        });
+    }, 4096);
     out.stage_begin[nstages] = (int)out.patches.size();
     return true;
 }

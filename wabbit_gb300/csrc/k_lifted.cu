@@ -27,7 +27,7 @@
 namespace wg {
 
 __constant__ double c_lhd[32];
-__constant__ int c_lhd_k[32], c_lhd_s[32];   // exact power-of-two taps (exact.cuh)
+__constant__ int c_lhd_k[32], c_lhd_s[32], c_lhd_m[32];   // tap kinds for the integer-pipe products (exact.cuh)
 __constant__ long long c_lhd_g[32];          // sign bit of each tap
 __constant__ int c_lhd_n[2];   // lo, count
 
@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(256) hd_filter_kernel(const FilterEntry *__res
         const double *row = u + ((long long)(z0 + zz) * geo.ny + (y0 + yy)) * geo.nx + g + 2 * mx;
         double s = 0.0;
         bool bad = false;
-        for (int t = 0; t < nt; t++) s = __dadd_rn(s, tap_mul(row[lo + t], c_lhd[t], c_lhd_k[t], c_lhd_s[t], c_lhd_g[t], bad));
+        for (int t = 0; t < nt; t++)
+            s = __dadd_rn(s, tap_mul(row[lo + t], c_lhd[t], c_lhd_k[t], c_lhd_s[t], c_lhd_m[t], c_lhd_g[t], bad));
         if (bad) {
             s = 0.0;
             for (int t = 0; t < nt; t++) s = __dadd_rn(s, __dmul_rn(row[lo + t], c_lhd[t]));
@@ -84,7 +85,8 @@ __global__ void __launch_bounds__(256) hd_filter_kernel(const FilterEntry *__res
         double s = 0.0;
         bool bad = false;
         for (int t = 0; t < nt; t++)
-            s = __dadd_rn(s, tap_mul(col[(long long)(lo + t) * hx], c_lhd[t], c_lhd_k[t], c_lhd_s[t], c_lhd_g[t], bad));
+            s = __dadd_rn(s, tap_mul(col[(long long)(lo + t) * hx], c_lhd[t], c_lhd_k[t], c_lhd_s[t], c_lhd_m[t],
+                                     c_lhd_g[t], bad));
         if (bad) {
             s = 0.0;
             for (int t = 0; t < nt; t++) s = __dadd_rn(s, __dmul_rn(col[(long long)(lo + t) * hx], c_lhd[t]));
@@ -104,7 +106,7 @@ __global__ void __launch_bounds__(256) hd_filter_kernel(const FilterEntry *__res
         bool bad = false;
         for (int t = 0; t < nt; t++)
             s = __dadd_rn(s, tap_mul(pl[(long long)(lo + t) * hx * hy], c_lhd[t], c_lhd_k[t], c_lhd_s[t],
-                                     c_lhd_g[t], bad));
+                                     c_lhd_m[t], c_lhd_g[t], bad));
         if (bad) {
             s = 0.0;
             for (int t = 0; t < nt; t++) s = __dadd_rn(s, __dmul_rn(pl[(long long)(lo + t) * hx * hy], c_lhd[t]));
@@ -229,17 +231,18 @@ __global__ void __launch_bounds__(128) zone_detail_kernel(const ZoneBox *__restr
 cudaError_t lifted_set_filter(const double *hd, int lo, int n, cudaStream_t s) {
     if (n > 32) return cudaErrorInvalidValue;
     double h[32] = {};
-    int kind[32] = {}, sh[32] = {};
+    int kind[32] = {}, sh[32] = {}, mul[32] = {};
     long long sg[32] = {};
     for (int i = 0; i < n; i++) {
         h[i] = hd[i];
-        classify_tap(h[i], kind[i], sh[i]);
+        classify_tap(h[i], kind[i], sh[i], mul[i]);
         sg[i] = h[i] < 0.0 ? (long long)0x8000000000000000ULL : 0LL;
     }
     const int ln[2] = {lo, n};
     cudaError_t e = cudaMemcpyToSymbolAsync(c_lhd, h, sizeof(h), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_k, kind, sizeof(kind), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_s, sh, sizeof(sh), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_m, mul, sizeof(mul), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_g, sg, sizeof(sg), 0, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_n, ln, sizeof(ln), 0, cudaMemcpyHostToDevice, s);
     return e;

@@ -422,9 +422,11 @@ struct Taps {
     int n[5];              // 0 HD (non-zero or centre), 1 GD, 2 HR odd, 3 GR odd, 4 GR even without 0
     int off[5][16];
     double val[5][16];
-    int kind[5][16], sh[5][16];   // exact power-of-two taps (exact.cuh)
+    int kind[5][16], sh[5][16], mul[5][16];   // tap kinds for the integer-pipe products (exact.cuh)
     long long sgn[5][16];         // sign bit of each tap
     double gr0;            // GR(0)
+    int gr0_kind, gr0_sh, gr0_mul;
+    long long gr0_sgn;
     int lazy;
 };
 __constant__ Taps c_taps;
@@ -449,25 +451,31 @@ __device__ __forceinline__ double tap_sum(int f, const double *src, long long st
 struct Cdf44Taps {
     __host__ __device__ static constexpr int nt(int f) { return f == 0 ? 11 : f == 1 ? 5 : f == 4 ? 6 : 4; }
     __host__ __device__ static constexpr int kind(int f, int t) {
-        return f == 0 ? ((t == 0 || t == 2 || t == 8 || t == 10) ? 1 : 0)
-             : f == 1 ? ((t == 0 || t == 4) ? 1 : t == 2 ? 2 : 0)
-             : f == 4 ? ((t == 0 || t == 5) ? 1 : 0)
-             : ((t == 0 || t == 3) ? 1 : 0);
+        return f == 0 ? ((t == 0 || t == 2 || t == 8 || t == 10) ? 1 : 3)
+             : f == 1 ? ((t == 0 || t == 4) ? 1 : t == 2 ? 2 : 3)
+             : f == 4 ? ((t == 0 || t == 5) ? 1 : 3)
+             : ((t == 0 || t == 3) ? 1 : 3);
     }
 };
 
-// the same sum with the kinds of K known at compile time: power-of-two taps
-// and the unit tap issue no FP64 instruction
+// product with tap t of list F, the kind known at compile time: every kind
+// but 0 is formed on the integer pipe
+template <class K, int F>
+__device__ __forceinline__ double ktap_mul(double x, int t, bool &bad) {
+    if (K::kind(F, t) == 2) return x;
+    if (K::kind(F, t) == 1) return pow2_mul(x, c_taps.sh[F][t], c_taps.sgn[F][t], bad);
+    if (K::kind(F, t) == 3) return short_mul(x, c_taps.mul[F][t], c_taps.sh[F][t], c_taps.sgn[F][t], bad);
+    return __dmul_rn(x, c_taps.val[F][t]);
+}
+
+// the same sum with the kinds of K known at compile time: the FP64 pipe
+// only adds
 template <class K, int F>
 __device__ __forceinline__ double ktap_sum(const double *src, long long st, int at, bool &bad) {
     double s = 0.0;
 #pragma unroll
     for (int t = 0; t < K::nt(F); t++) {
-        const double x = src[(at + c_taps.off[F][t]) * st];
-        double p;
-        if (K::kind(F, t) == 2) p = x;
-        else if (K::kind(F, t) == 1) p = pow2_mul(x, c_taps.sh[F][t], c_taps.sgn[F][t], bad);
-        else p = __dmul_rn(x, c_taps.val[F][t]);
+        const double p = ktap_mul<K, F>(src[(at + c_taps.off[F][t]) * st], t, bad);
         s = t == 0 ? p : __dadd_rn(s, p);
     }
     return s;
@@ -502,7 +510,7 @@ __device__ __forceinline__ double iwt_point(const double *src, long long st, int
 }
 
 // fwt_point / iwt_point with compile-time tap kinds (lifted wavelets),
-// without the fallback: bad is set where a power-of-two product left the
+// without the fallback: bad is set where an integer-pipe product left the
 // exact range, and the caller recomputes those outputs with fwt_point /
 // iwt_point
 template <class K>
@@ -518,21 +526,14 @@ __device__ __forceinline__ double iwt_point_k(const double *src, long long st, i
         v = src[at * st];
 #pragma unroll
         for (int t = 0; t < K::nt(3); t++) {
-            const double x = src[(at + c_taps.off[3][t]) * st];
-            const double q = K::kind(3, t) == 1 ? pow2_mul(x, c_taps.sh[3][t], c_taps.sgn[3][t], bad)
-                                                : __dmul_rn(x, c_taps.val[3][t]);
-            v = __dadd_rn(v, q);
+            v = __dadd_rn(v, ktap_mul<K, 3>(src[(at + c_taps.off[3][t]) * st], t, bad));
         }
     } else {
         v = ktap_sum<K, 2>(src, st, at, bad);
-        v = __dadd_rn(v, __dmul_rn(src[at * st], c_taps.gr0));
+        v = __dadd_rn(v, tap_mul(src[at * st], c_taps.gr0, c_taps.gr0_kind, c_taps.gr0_sh, c_taps.gr0_mul,
+                                 c_taps.gr0_sgn, bad));
 #pragma unroll
-        for (int t = 0; t < K::nt(4); t++) {
-            const double x = src[(at + c_taps.off[4][t]) * st];
-            const double q = K::kind(4, t) == 1 ? pow2_mul(x, c_taps.sh[4][t], c_taps.sgn[4][t], bad)
-                                                : __dmul_rn(x, c_taps.val[4][t]);
-            v = __dadd_rn(v, q);
-        }
+        for (int t = 0; t < K::nt(4); t++) v = __dadd_rn(v, ktap_mul<K, 4>(src[(at + c_taps.off[4][t]) * st], t, bad));
     }
     return v;
 }
@@ -554,7 +555,7 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
     const long long np = geo.npts();
     double *ub = u + ((long long)b * nc + c) * np;
     // slow: the reference's FP64 multiplies; fast: compile-time tap kinds
-    // (power-of-two products on the integer pipe), bad marks outputs to redo
+    // (products on the integer pipe), bad marks outputs to redo
     auto slow = [&](const double *src, long long st, int at, int p) {
         return MODE == 2 ? iwt_point(src, st, at, p) : fwt_point(src, st, at, p);
     };
@@ -686,7 +687,7 @@ static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
         if (t.n[f] >= 16) return false;
         t.off[f][t.n[f]] = off;
         t.val[f][t.n[f]] = v;
-        classify_tap(v, t.kind[f][t.n[f]], t.sh[f][t.n[f]]);
+        classify_tap(v, t.kind[f][t.n[f]], t.sh[f][t.n[f]], t.mul[f][t.n[f]]);
         t.sgn[f][t.n[f]] = v < 0.0 ? (long long)0x8000000000000000ULL : 0LL;
         t.n[f]++;
         return true;
@@ -706,7 +707,11 @@ static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
     }
     for (size_t i = 0; i < w.GR.size(); i++) {
         const int m = w.gr_lo + (int)i;
-        if (m == 0) t.gr0 = w.GR[i];
+        if (m == 0) {
+            t.gr0 = w.GR[i];
+            classify_tap(t.gr0, t.gr0_kind, t.gr0_sh, t.gr0_mul);
+            t.gr0_sgn = t.gr0 < 0.0 ? (long long)0x8000000000000000ULL : 0LL;
+        }
         else if ((m & 1) && w.GR[i] != 0.0) ok &= add(3, m, w.GR[i]);
         else if (!(m & 1) && w.GR[i] != 0.0) ok &= add(4, m, w.GR[i]);
     }

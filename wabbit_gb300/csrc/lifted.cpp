@@ -1,6 +1,7 @@
 // lifted.cpp -- host planning of the full-tree adaptation with coarse
 // extension (see lifted.hpp).
 #include "lifted.hpp"
+#include "par.hpp"
 
 #include <algorithm>
 #include <cstring>
@@ -8,38 +9,6 @@
 #include <unordered_map>
 
 namespace wg {
-
-namespace {
-// f(chunk, lo, hi) on contiguous chunks of [0, n), one host thread each
-template <class F>
-void par_chunks(int n, int nchunk, F f) {
-    if (nchunk <= 1 || n < 8192) {
-        f(0, 0, n);
-        return;
-    }
-    std::vector<std::thread> th;
-    for (int c = 0; c < nchunk; c++) {
-        const int lo = (int)((long long)n * c / nchunk), hi = (int)((long long)n * (c + 1) / nchunk);
-        th.emplace_back([=, &f]() { f(c, lo, hi); });
-    }
-    for (auto &t : th) t.join();
-}
-// f(task) for task = 0..ntask-1, one host thread each
-template <class F>
-void par_tasks(int ntask, F f) {
-    if (ntask <= 1) {
-        if (ntask == 1) f(0);
-        return;
-    }
-    std::vector<std::thread> th;
-    for (int t = 0; t < ntask; t++) th.emplace_back([=, &f]() { f(t); });
-    for (auto &t : th) t.join();
-}
-int host_threads() {
-    const unsigned h = std::thread::hardware_concurrency();
-    return h ? (int)std::min(h, 32u) : 4;
-}
-}  // namespace
 
 bool LiftedTree::init(const Geometry &g, const WaveletInfo &w, int fd_max_size, int jmin, int jmax, int nleaf,
                       const int *level, const int *coords, std::string &err) {
