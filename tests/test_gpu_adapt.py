@@ -110,3 +110,32 @@ def test_refine_step_adapt_loop_matches_oracle():
             assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
             assert np.array_equal(interior(cfg, a[2]), interior(cfg, b[2])), cycle
         assert top == cfg.Jmax   # refinement reached Jmax and stayed there
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim,wavelet,Bs", [(2, "CDF40", 16), (2, "CDF44", 16), (3, "CDF40", 8), (3, "CDF44", 16),
+                                            (3, "CDF40", 16)])
+def test_refine_everywhere_full_blocks_match_oracle(dim, wavelet, Bs):
+    """refine_everywhere (refinementExecute.f90:4-116) on every point of the
+    daughters, ghosts included, against the oracle: the separable prediction
+    per daughter slab reproduces the parent's full-block prediction. Tiny
+    (subnormal) and zero values in one component take the FP64 fallback of
+    the integer-pipe products."""
+    cfg = small_cfg(dim, wavelet, Bs=Bs, jmin=1 if dim == 3 else 2, jmax=4 if dim == 3 else 6)
+    lv, co = grids.random_graded(dim, cfg.Jmin + 1, cfg.Jmax - 1, seed=11, frac=0.4)
+    data = smooth_state(cfg, lv, co, 5)
+    data[: len(lv) // 3, 0] *= 1e-310          # subnormal products
+    data[len(lv) // 3: len(lv) // 2, 1] = 0.0   # signed zeros
+    data[len(lv) // 2: 2 * len(lv) // 3, 1] *= -1e300
+    o = Oracle(cfg)
+    o.set_grid(lv, co, data)
+    o.refine_everywhere()
+    with Context(cfg, 10 * len(lv)) as ctx:
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        f.upload(data)
+        f.refine_everywhere()
+        a = _sorted(*o.grid(), o.data())
+        b = _sorted(*f.grid(), f.download())
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(a[2].view(np.int64), b[2].view(np.int64))

@@ -2050,6 +2050,60 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
 // refine_tree(..., "everywhere") data part: every block is replaced by its
 // 2^d daughters (refineBlock); ghosts must be synchronised with g points.
 // Daughters of block b are blocks 2^d*b .. 2^d*b+2^d-1 of the new grid.
+// refineBlock (LIB/MESH/refinementExecute.f90:4-116) as prediction patches:
+// daughter k of a parent (x half (k/2)%2, y half k%2, z half k/4) holds the
+// parent's full-block prediction at fine indices g + Bs*half + i, i over the
+// daughter's full block. Each patch covers a slab of tz planes of one
+// daughter and reads a coarse sub-box of the parent that holds every stencil
+// of its points: within the sub-box no point reaches the zero fill at the
+// edges unless it does in the parent's full fine array, so the separable
+// prediction kernel returns the reference's values. Returns the shared
+// memory (doubles) of the largest patch.
+static int refine_patches(const wg_config &c, int g, int order, const std::vector<int> &parents,
+                          const std::vector<int> &daughters, int tz, std::vector<Patch> &out) {
+    const int dim = c.dim, nd = 1 << dim, h = order - 1;
+    int nb[3];
+    for (int d = 0; d < 3; d++) nb[d] = d < dim ? c.Bs[d] + 2 * g : 1;
+    const int nslab = dim == 3 ? (nb[2] + tz - 1) / tz : 1;
+    auto fdiv = [](int a) { return a >= 0 ? a / 2 : -((1 - a) / 2); };   // floor(a / 2)
+    int need = 0;
+    out.clear();
+    out.reserve(parents.size() * nd * nslab);
+    for (size_t p = 0; p < parents.size(); p++)
+        for (int k = 0; k < nd; k++)
+            for (int sl = 0; sl < nslab; sl++) {
+                Patch q;
+                std::memset(&q, 0, sizeof(q));
+                q.src = parents[p];
+                q.dst = daughters[p * nd + k];
+                q.op = 2;
+                const int half[3] = {(k / 2) % 2, k % 2, k / 4};
+                for (int d = 0; d < dim; d++) {
+                    const int ilo = d == 2 ? sl * tz : 0, ihi = d == 2 ? std::min(nb[2], (sl + 1) * tz) - 1 : nb[d] - 1;
+                    const int flo = g + c.Bs[d] * half[d] + ilo, fhi = g + c.Bs[d] * half[d] + ihi;
+                    const int clo = std::max(0, fdiv(flo - h)), chi = std::min(nb[d] - 1, fdiv(fhi + h + 1));
+                    q.rlo[d] = (int16_t)ilo;
+                    q.rhi[d] = (int16_t)ihi;
+                    q.slo[d] = (int16_t)clo;
+                    q.shi[d] = (int16_t)chi;
+                    q.blo[d] = (int16_t)(flo - 2 * clo);
+                }
+                // shared memory of predict_kernel: coarse box, x window, x-y window
+                const int cx = q.shi[0] - q.slo[0] + 1, cy = q.shi[1] - q.slo[1] + 1, cz = q.shi[2] - q.slo[2] + 1;
+                const int ex = q.rhi[0] - q.rlo[0] + 1, ey = q.rhi[1] - q.rlo[1] + 1, ez = q.rhi[2] - q.rlo[2] + 1;
+                int yw0 = std::max(0, q.blo[1] - h), yw1 = std::min(2 * cy - 2, q.blo[1] + ey - 1 + h);
+                yw0 += yw0 & 1;
+                yw1 -= yw1 & 1;
+                int zw0 = std::max(0, q.blo[2] - h), zw1 = std::min(2 * cz - 2, q.blo[2] + ez - 1 + h);
+                zw0 += zw0 & 1;
+                zw1 -= zw1 & 1;
+                const int wy = (yw1 - yw0) / 2 + 1, wz = (zw1 - zw0) / 2 + 1;
+                need = std::max(need, cx * cy * cz + ex * wy * wz + ex * ey * wz);
+                out.push_back(q);
+            }
+    return need;
+}
+
 int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return WG_EINVAL;
@@ -2090,11 +2144,25 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     if (nr > 0) {
         DevArray<int> d_par, d_base;
         const int *Bs = ctx->cfg.Bs;
-        cudaError_t e = d_par.upload(parents.data(), nr, ctx->stream);
-        if (e == cudaSuccess) e = d_base.upload(bases.data(), bases.size(), ctx->stream);
-        if (e == cudaSuccess)
-            e = launch_refine(dim, d_par.p, nr, d_base.p, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], ctx->geo.nc,
-                              ctx->wav.order_predictor, ctx->stream);
+        // separable prediction per daughter slab (7 planes: two CTAs per SM
+        // for 16^3 blocks); the point-wise kernel where a slab's windows do
+        // not fit the shared memory
+        std::vector<Patch> rp;
+        const int need = refine_patches(ctx->cfg, ctx->gA.gb, ctx->wav.order_predictor, parents, bases, 7, rp);
+        cudaError_t e = cudaSuccess;
+        DevArray<Patch> d_rp;
+        if ((size_t)need * sizeof(double) <= 200 * 1024) {
+            e = d_rp.upload(rp.data(), rp.size(), ctx->stream);
+            if (e == cudaSuccess)
+                e = launch_predict(d_rp.p, (int)rp.size(), need, ctx->A, ctx->gA, ctx->geo.nc, ctx->wav.order_predictor,
+                                   ctx->stream);
+        } else {
+            e = d_par.upload(parents.data(), nr, ctx->stream);
+            if (e == cudaSuccess) e = d_base.upload(bases.data(), bases.size(), ctx->stream);
+            if (e == cudaSuccess)
+                e = launch_refine(dim, d_par.p, nr, d_base.p, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], ctx->geo.nc,
+                                  ctx->wav.order_predictor, ctx->stream);
+        }
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) {   // the grid is unchanged
             cudaStreamSynchronize(ctx->stream);

@@ -19,6 +19,7 @@
 #include "common.cuh"
 #include "predict.cuh"
 #include "df.cuh"
+#include "exact.cuh"
 #include <algorithm>
 
 namespace wg {
@@ -113,6 +114,23 @@ __device__ __forceinline__ double interp_line(const double *c, const double *v, 
     return s;
 }
 
+// the order-4 predictor (-1, 9, 9, -1)/16 with its products on the integer
+// pipe (exact.cuh: -2^-4 and 9 2^-4 times v, bit-identical to the FP64
+// multiply); the FP64 multiplies redo it where a product left the exact range
+__device__ __forceinline__ double interp_pred(const double *c, const double *v, int stride, int first, int nc) {
+    if (nc == 4) {
+        constexpr long long kNeg = (long long)0x8000000000000000ULL;
+        const double *q = v + (long long)first * stride;
+        bool bad = false;
+        double s = pow2_mul(q[0], -4, kNeg, bad);
+        s = __dadd_rn(s, short_mul(q[stride], 9, -4, 0, bad));
+        s = __dadd_rn(s, short_mul(q[2 * (long long)stride], 9, -4, 0, bad));
+        s = __dadd_rn(s, pow2_mul(q[3 * (long long)stride], -4, kNeg, bad));
+        if (!bad) return s;
+    }
+    return interp_line(c, v, stride, first, nc);
+}
+
 __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ patches, const double *sbuf,
                                                       double *buf, BufGeo geo, int nc, int order_idx, int ncoef) {
     extern __shared__ double sm[];
@@ -153,7 +171,7 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
             double v;
             if (!(fx & 1)) v = row[fx >> 1];
             else if (fx < h || fx > Fx - 1 - h) v = 0.0;
-            else v = interp_line(cf, row, 1, (fx - h) >> 1, ncoef);
+            else v = interp_pred(cf, row, 1, (fx - h) >> 1, ncoef);
             X[i] = v;
         }
         __syncthreads();
@@ -165,7 +183,7 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
             double v;
             if (!(fy & 1)) v = col[(long long)((fy - yw0) >> 1) * ex];
             else if (fy < h || fy > Fy - 1 - h) v = 0.0;
-            else v = interp_line(cf, col, ex, (fy - h - yw0) >> 1, ncoef);
+            else v = interp_pred(cf, col, ex, (fy - h - yw0) >> 1, ncoef);
             XY[i] = v;
         }
         __syncthreads();
@@ -177,7 +195,7 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
             double v;
             if (!(fz & 1)) v = pl[(long long)((fz - zw0) >> 1) * ex * ey];
             else if (fz < h || fz > Fz - 1 - h) v = 0.0;
-            else v = interp_line(cf, pl, ex * ey, (fz - h - zw0) >> 1, ncoef);
+            else v = interp_pred(cf, pl, ex * ey, (fz - h - zw0) >> 1, ncoef);
             dst[((long long)(p.rlo[2] + k) * geo.ny + (p.rlo[1] + j)) * geo.nx + (p.rlo[0] + ix)] = v;
         }
         __syncthreads();
