@@ -73,6 +73,41 @@ struct DevArray {
     }
 };
 
+// Transient device lists of one adaptation: chunks of device memory kept
+// between calls (no allocation per list), handed out by a bump pointer and
+// reset when the stream is idle.
+struct DevScratch {
+    struct Chunk {
+        char *p;
+        size_t cap, used;
+    };
+    std::vector<Chunk> chunks;
+    size_t cur = 0;
+    void *alloc(size_t bytes) {
+        bytes = std::max<size_t>(256, (bytes + 255) & ~(size_t)255);
+        while (cur < chunks.size() && chunks[cur].used + bytes > chunks[cur].cap) cur++;
+        if (cur == chunks.size()) {
+            const size_t cap = std::max(bytes, (size_t)64 << 20);
+            char *p = nullptr;
+            if (cudaMalloc(&p, cap) != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;
+            }
+            chunks.push_back({p, cap, 0});
+        }
+        void *r = chunks[cur].p + chunks[cur].used;
+        chunks[cur].used += bytes;
+        return r;
+    }
+    void reset() {
+        for (Chunk &c : chunks) c.used = 0;
+        cur = 0;
+    }
+    ~DevScratch() {
+        for (Chunk &c : chunks) cudaFree(c.p);
+    }
+};
+
 // Free arena slots as a bitmap (bit set = free): take() hands out the lowest
 // free slot, give() returns one; no sort of the free list per grid change.
 struct SlotPool {
@@ -191,6 +226,7 @@ struct wg_ctx {
     int max_trees = 64;
     std::vector<Tree> trees;
     SlotPool free_slots;
+    DevScratch scratch;                 // transient lists of the lifted adaptation
     cudaStream_t stream = nullptr;
     int variant_fast = 1;               // 1: FMA stencil, 0: strict reference arithmetic
     int precision = WG_RHS_FP64;        // WG_RHS_FP32: double-float stencils on the FP32 units
@@ -1606,18 +1642,18 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     }
     for (int b = 0; b < nb; b++) L.slot[b] = t->slots[b];
     for (int b = nb; b < nt; b++) L.slot[b] = ctx->free_slots.take();
-    // device lists stay alive until the end (the stream is synchronised there)
-    std::vector<std::unique_ptr<DevArray<Patch>>> kp;
-    std::vector<std::unique_ptr<DevArray<FilterEntry>>> kf;
-    std::vector<std::unique_ptr<DevArray<ScBox>>> ks;
-    std::vector<std::unique_ptr<DevArray<BoxOp>>> kb;
-    std::vector<std::unique_ptr<DevArray<int>>> ki;
-    std::vector<std::unique_ptr<DevArray<double>>> kd;
-    auto up = [&](auto &keep, const auto &v) -> decltype(keep.back()->p) {
-        using E = typename std::remove_reference<decltype(*keep.back()->p)>::type;
-        keep.emplace_back(new DevArray<E>());
-        if (keep.back()->upload(v.data(), v.size(), ctx->stream) != cudaSuccess) return nullptr;
-        return keep.back()->p;
+    // device lists from the context's scratch arena, alive until the end
+    // (the stream is synchronised there and before the next reset); a null
+    // list makes its launcher fail
+    cudaStreamSynchronize(ctx->stream);
+    ctx->scratch.reset();
+    auto up = [&](const auto &v) {
+        using E = typename std::decay<decltype(*v.data())>::type;
+        E *p = static_cast<E *>(ctx->scratch.alloc(sizeof(E) * v.size()));
+        if (p && !v.empty() &&
+            cudaMemcpyAsync(p, v.data(), sizeof(E) * v.size(), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+            p = nullptr;
+        return p;
     };
     // phase timing (wg_adapt_profile): host planning, then device phases
     // bracketed by stream synchronisations
@@ -1635,39 +1671,61 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     };
     cudaError_t e = lifted_set_filter(w.HD.data(), w.hd_lo, (int)w.HD.size(), ctx->stream);
     const int hx = Bs[0] / 2, hy = Bs[1] / 2, hz = dim == 3 ? Bs[2] / 2 : 1;
+    // one device list from the same list of every part of a wave (or of
+    // the wave itself): one copy per part into consecutive scratch memory
+    auto gather = [&](const std::vector<const SyncWave *> &ps, auto mem, int &n) {
+        using E = typename std::decay<decltype(*(ps[0]->*mem).data())>::type;
+        size_t tot = 0;
+        for (const SyncWave *q : ps) tot += (q->*mem).size();
+        n = (int)tot;
+        E *d = tot ? static_cast<E *>(ctx->scratch.alloc(sizeof(E) * tot)) : nullptr;
+        size_t at = 0;
+        for (const SyncWave *q : ps) {
+            const auto &v = q->*mem;
+            if (d && !v.empty() &&
+                cudaMemcpyAsync(d + at, v.data(), sizeof(E) * v.size(), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+                d = nullptr;
+            at += v.size();
+        }
+        return d;
+    };
     auto run_waves = [&](const std::vector<SyncWave> &waves) -> cudaError_t {
         for (const SyncWave &wv : waves) {
+            std::vector<const SyncWave *> ps;
+            if (wv.parts.empty()) ps.push_back(&wv);
+            for (const SyncWave &q : wv.parts) ps.push_back(&q);
             cudaError_t r = cudaSuccess;
-            if (!wv.copy_blk.empty()) r = launch_xcopy(up(kp, wv.copy_blk), (int)wv.copy_blk.size(), ctx->A, ctx->A, gA, nc, ctx->stream);
-            if (r == cudaSuccess && !wv.copy_tmp.empty())
-                r = launch_xcopy(up(kp, wv.copy_tmp), (int)wv.copy_tmp.size(), ctx->T, ctx->A, gA, nc, ctx->stream);
-            if (r == cudaSuccess && !wv.restrict_.empty()) {
+            int n = 0;
+            const Patch *cb = gather(ps, &SyncWave::copy_blk, n);
+            if (n) r = launch_xcopy(cb, n, ctx->A, ctx->A, gA, nc, ctx->stream);
+            const Patch *ct = gather(ps, &SyncWave::copy_tmp, n);
+            if (r == cudaSuccess && n) r = launch_xcopy(ct, n, ctx->T, ctx->A, gA, nc, ctx->stream);
+            int nr = 0, nf = 0, ns = 0;
+            for (const SyncWave *q : ps) nr += (int)q->restrict_.size();
+            if (r == cudaSuccess && nr) {
                 // every restricted point lies on the sender's interior SC lattice
-                for (const Patch &p : wv.restrict_)
-                    for (int d = 0; d < dim; d++) {
-                        const int a = p.slo[d] + 2 * p.blo[d], z = a + 2 * (p.rhi[d] - p.rlo[d]);
-                        if (((a - g) & 1) || a < g || z > g + Bs[d] - 2) return cudaErrorInvalidValue;
-                    }
-                std::vector<double> none;
-                kd.emplace_back(new DevArray<double>());
-                r = kd.back()->upload(nullptr, (size_t)wv.filters.size() * nc * hx * hy * hz, ctx->stream);
-                double *scratch = kd.back()->p;
-                const FilterEntry *fe = up(kf, wv.filters);
+                for (const SyncWave *q : ps)
+                    for (const Patch &p : q->restrict_)
+                        for (int d = 0; d < dim; d++) {
+                            const int a = p.slo[d] + 2 * p.blo[d], z = a + 2 * (p.rhi[d] - p.rlo[d]);
+                            if (((a - g) & 1) || a < g || z > g + Bs[d] - 2) return cudaErrorInvalidValue;
+                        }
+                const FilterEntry *fe = gather(ps, &SyncWave::filters, nf);
+                const ScBox *sb = gather(ps, &SyncWave::ce_copies, ns);
+                const Patch *rp = gather(ps, &SyncWave::restrict_, nr);
+                double *scratch = static_cast<double *>(ctx->scratch.alloc(sizeof(double) * nf * nc * hx * hy * hz));
+                r = launch_hd_filter(dim, fe, nf, ctx->A, ctx->T, gA, Bs[0], Bs[1], Bs[2], nc, w.hd_lo,
+                                     (int)w.HD.size(), scratch, ctx->stream);
+                if (r == cudaSuccess && ns)
+                    r = launch_scbox(sb, ns, fe, ctx->A, ctx->T, gA, hx, hy, hz, nc, scratch, ctx->stream);
                 if (r == cudaSuccess)
-                    r = launch_hd_filter(dim, fe, (int)wv.filters.size(), ctx->A, ctx->T, gA, Bs[0], Bs[1], Bs[2], nc,
-                                         w.hd_lo, (int)w.HD.size(), scratch, ctx->stream);
-                if (r == cudaSuccess && !wv.ce_copies.empty())
-                    r = launch_scbox(up(ks, wv.ce_copies), (int)wv.ce_copies.size(), fe, ctx->A, ctx->T, gA, hx, hy,
-                                     hz, nc, scratch, ctx->stream);
-                if (r == cudaSuccess)
-                    r = launch_restrict_scratch(up(kp, wv.restrict_), (int)wv.restrict_.size(), scratch, ctx->A, gA,
-                                                hx, hy, hz, nc, ctx->stream);
+                    r = launch_restrict_scratch(rp, nr, scratch, ctx->A, gA, hx, hy, hz, nc, ctx->stream);
             }
             if (r == cudaSuccess && !wv.pred_blk.empty())
-                r = launch_predict(up(kp, wv.pred_blk), (int)wv.pred_blk.size(), wv.max_coarse, ctx->A, gA, nc,
+                r = launch_predict(up(wv.pred_blk), (int)wv.pred_blk.size(), wv.max_coarse, ctx->A, gA, nc,
                                    w.order_predictor, ctx->stream, ctx->A);
             if (r == cudaSuccess && !wv.pred_tmp.empty())
-                r = launch_predict(up(kp, wv.pred_tmp), (int)wv.pred_tmp.size(), wv.max_coarse, ctx->A, gA, nc,
+                r = launch_predict(up(wv.pred_tmp), (int)wv.pred_tmp.size(), wv.max_coarse, ctx->A, gA, nc,
                                    w.order_predictor, ctx->stream, ctx->T);
             if (r != cudaSuccess) return r;
         }
@@ -1690,7 +1748,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         ctx->adapt_ms[kPlan] += std::chrono::duration<double, std::milli>(clk::now() - t0).count();
         if (ops.empty()) return cudaSuccess;
         t0 = tic();
-        const cudaError_t r = launch_boxop(up(kb, ops), (int)ops.size(), ctx->A, ctx->T, gA, nc, ctx->stream);
+        const cudaError_t r = launch_boxop(up(ops), (int)ops.size(), ctx->A, ctx->T, gA, nc, ctx->stream);
         toc(kCe, t0);
         return r;
     };
@@ -1727,7 +1785,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     for (int b = 0; b < nt; b++) L.ref[b] = b < nb ? ((L.ft.level[b] == lmax || leaf_first) ? -1 : 0) : kRefTmpEmpty;
     {
         std::vector<int> leaves(t->slots.begin(), t->slots.end());
-        if (e == cudaSuccess) e = launch_blockcopy(up(ki, leaves), nb, ctx->A, ctx->T, per_block, ctx->stream);
+        if (e == cudaSuccess) e = launch_blockcopy(up(leaves), nb, ctx->A, ctx->T, per_block, ctx->stream);
     }
     const int g_this = std::max(std::abs(w.hd_lo), w.gd_lo + (int)w.GD.size() - 1);
     for (int level = lmax, it = 0; level >= t->cfg.Jmin && e == cudaSuccess; level--, it++) {
@@ -1740,7 +1798,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         e = sync_spec(sp);
         const std::vector<int> dec = slots_where([&](int b) { return L.ref[b] == -1; });
         if (e == cudaSuccess && !dec.empty()) {
-            const int *d_dec = up(ki, dec);
+            const int *d_dec = up(dec);
             auto t0 = tic();
             e = launch_blockcopy(d_dec, (int)dec.size(), ctx->A, ctx->T, per_block, ctx->stream);
             toc(kCopy, t0);
@@ -1759,7 +1817,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         mother_patches(L.ft, ctx->geo, level - 1, L.slot, d2m, gh);
         auto t0 = tic();
         if (e == cudaSuccess && !d2m.empty())
-            e = launch_sync(up(kp, d2m), (int)d2m.size(), ctx->A, gA, nc, w.order_predictor, ctx->stream);
+            e = launch_sync(up(d2m), (int)d2m.size(), ctx->A, gA, nc, w.order_predictor, ctx->stream);
         toc(kCe, t0);
     }
     std::fill(L.ref.begin(), L.ref.end(), 0);
@@ -1770,10 +1828,10 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         std::vector<int> all(L.slot.begin(), L.slot.end());
         std::vector<int> tsvc(t->cfg.threshold_state_vector_component, t->cfg.threshold_state_vector_component + nc);
         std::vector<double> eps(eps_use, eps_use + nc);
-        const int *d_all = up(ki, all);
+        const int *d_all = up(all);
         std::vector<int> zeros(nt, 0);
-        int *d_flags = up(ki, zeros);
-        e = launch_fwt_flags(dim, d_all, nt, ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X, w.Y, up(kd, eps), up(ki, tsvc),
+        int *d_flags = up(zeros);
+        e = launch_fwt_flags(dim, d_all, nt, ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X, w.Y, up(eps), up(tsvc),
                              d_flags, nullptr, ctx->stream, 1);
         if (e == cudaSuccess) e = cudaMemcpyAsync(flags.data(), d_flags, sizeof(int) * nt, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1790,12 +1848,10 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
                     for (int d = 0; d < 3; d++) zb.push_back(z.io[d]);
                 }
                 std::vector<double> det(items.size() * nc, 0.0);
-                kd.emplace_back(new DevArray<double>());
-                e = kd.back()->upload(nullptr, det.size(), ctx->stream);
+                double *d_det = static_cast<double *>(ctx->scratch.alloc(sizeof(double) * det.size()));
+                e = launch_zone_detail(up(zb), (int)items.size(), ctx->A, gA, nc, dim, d_det, ctx->stream);
                 if (e == cudaSuccess)
-                    e = launch_zone_detail(up(ki, zb), (int)items.size(), ctx->A, gA, nc, dim, kd.back()->p, ctx->stream);
-                if (e == cudaSuccess)
-                    e = cudaMemcpyAsync(det.data(), kd.back()->p, sizeof(double) * det.size(), cudaMemcpyDeviceToHost,
+                    e = cudaMemcpyAsync(det.data(), d_det, sizeof(double) * det.size(), cudaMemcpyDeviceToHost,
                                         ctx->stream);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
                 // threshold_block's component / vector-group rule
@@ -1849,12 +1905,12 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         cudaError_t r = cudaSuccess;
         auto t0 = tic();
         if (!rec.empty())
-            r = launch_wavelet_reconstruct(dim, up(ki, rec), (int)rec.size(), ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X,
+            r = launch_wavelet_reconstruct(dim, up(rec), (int)rec.size(), ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X,
                                            w.Y, ctx->stream);
         toc(kRecon, t0);
         t0 = tic();
         if (r == cudaSuccess && !keep.empty())
-            r = launch_blockcopy(up(ki, keep), (int)keep.size(), ctx->T, ctx->A, per_block, ctx->stream);
+            r = launch_blockcopy(up(keep), (int)keep.size(), ctx->T, ctx->A, per_block, ctx->stream);
         toc(kCopy, t0);
         return r;
     };

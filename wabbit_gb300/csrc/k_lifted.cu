@@ -252,6 +252,7 @@ static int warps_grid(int n) { return (n + 3) / 4; }
 
 cudaError_t launch_xcopy(const Patch *p, int n, const double *sbuf, double *dbuf, BufGeo geo, int nc, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (!p) return cudaErrorInvalidValue;
     xcopy_kernel<<<warps_grid(n), 128, 0, s>>>(p, n, sbuf, dbuf, geo, nc);
     return cudaGetLastError();
 }
@@ -259,6 +260,7 @@ cudaError_t launch_xcopy(const Patch *p, int n, const double *sbuf, double *dbuf
 cudaError_t launch_hd_filter(int dim, const FilterEntry *ent, int n, const double *A, const double *T, BufGeo geo,
                              int Bx, int By, int Bz, int nc, int hd_lo, int hd_n, double *scratch, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (!ent || !scratch) return cudaErrorInvalidValue;
     const int hi = hd_lo + hd_n - 1;
     if (-hd_lo > geo.gb || hi > geo.gb) return cudaErrorInvalidValue;
     const int hx = Bx / 2, hy = By / 2, ny = By + hi - hd_lo, nz = dim == 3 ? Bz + hi - hd_lo : 1;
@@ -278,6 +280,7 @@ cudaError_t launch_hd_filter(int dim, const FilterEntry *ent, int n, const doubl
 cudaError_t launch_scbox(const ScBox *b, int n, const FilterEntry *ent, const double *A, const double *T, BufGeo geo,
                          int hx, int hy, int hz, int nc, double *scratch, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (!b || !ent) return cudaErrorInvalidValue;
     scbox_kernel<<<warps_grid(n), 128, 0, s>>>(b, n, ent, A, T, geo, hx, hy, hz, nc, scratch);
     return cudaGetLastError();
 }
@@ -285,12 +288,14 @@ cudaError_t launch_scbox(const ScBox *b, int n, const FilterEntry *ent, const do
 cudaError_t launch_restrict_scratch(const Patch *p, int n, const double *scratch, double *A, BufGeo geo, int hx,
                                     int hy, int hz, int nc, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (!p || !scratch) return cudaErrorInvalidValue;
     restrict_scratch_kernel<<<warps_grid(n), 128, 0, s>>>(p, n, scratch, A, geo, hx, hy, hz, nc);
     return cudaGetLastError();
 }
 
 cudaError_t launch_boxop(const BoxOp *o, int n, double *A, const double *T, BufGeo geo, int nc, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (!o) return cudaErrorInvalidValue;
     boxop_kernel<<<warps_grid(n), 128, 0, s>>>(o, n, A, T, geo, nc);
     return cudaGetLastError();
 }
@@ -298,6 +303,7 @@ cudaError_t launch_boxop(const BoxOp *o, int n, double *A, const double *T, BufG
 cudaError_t launch_blockcopy(const int *slots, int n, const double *src, double *dst, long long per_block,
                              cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (!slots) return cudaErrorInvalidValue;
     const long long work = (long long)n * ((per_block + 1023) / 1024);
     const int grid = (int)std::min<long long>(work, 152LL * 16);
     blockcopy_kernel<<<grid, 256, 0, s>>>(slots, n, src, dst, per_block);
@@ -307,6 +313,7 @@ cudaError_t launch_blockcopy(const int *slots, int n, const double *src, double 
 cudaError_t launch_zone_detail(const void *items, int n, const double *A, BufGeo geo, int nc, int dim, double *det,
                                cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
+    if (!items || !det) return cudaErrorInvalidValue;
     zone_detail_kernel<<<n * nc, 128, 0, s>>>((const ZoneBox *)items, n, A, geo, nc, dim, det);
     return cudaGetLastError();
 }

@@ -311,6 +311,7 @@ cudaError_t sync_init() { return init_predictor(); }
 cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_doubles, double *buf, BufGeo geo, int nc,
                            int order_predictor, cudaStream_t s, const double *src_buf) {
     if (npatch <= 0) return cudaSuccess;
+    if (!patches) return cudaErrorInvalidValue;
     const size_t smem = sizeof(double) * (size_t)max_smem_doubles;
     static size_t attr = 0;
     if (smem > 48 * 1024 && smem > attr) {
@@ -378,6 +379,7 @@ cudaError_t launch_gather(const void *pairs, unsigned n, void *buf, BufGeo geo, 
 cudaError_t launch_sync(const Patch *patches, int npatch, double *buf, BufGeo geo, int nc, int order_predictor,
                         cudaStream_t s) {
     if (npatch <= 0) return cudaSuccess;
+    if (!patches) return cudaErrorInvalidValue;
     cudaError_t e = init_predictor();
     if (e != cudaSuccess) return e;
     const int oi = order_predictor / 2 - 1;

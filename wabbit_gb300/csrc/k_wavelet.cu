@@ -207,6 +207,7 @@ cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u,
                              int Bs2, int nc, int wavelet_x, int wavelet_y, const double *eps_use, const int *tsvc,
                              int *flags, double *details, cudaStream_t s, int input_is_wd) {
     if (nblk <= 0) return cudaSuccess;
+    if (!blk || !eps_use || !tsvc || !flags) return cudaErrorInvalidValue;
     WaveletInfo w;
     char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
     if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
@@ -823,6 +824,7 @@ cudaError_t launch_wavelet_decompose(int dim, const int *blk, int nblk, double *
 cudaError_t launch_wavelet_decompose_window(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
                                             int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
+    if (!blk) return cudaErrorInvalidValue;
     WaveletInfo w;
     char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
     if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
@@ -835,6 +837,7 @@ cudaError_t launch_wavelet_decompose_window(int dim, const int *blk, int nblk, d
 cudaError_t launch_wavelet_reconstruct(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
                                        int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
+    if (!blk) return cudaErrorInvalidValue;
     WaveletInfo w;
     char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
     if (!make_wavelet(name, w)) return cudaErrorInvalidValue;

@@ -127,7 +127,7 @@ bool LiftedTree::update_metadata(std::string &err) {
             cnt[b - lo] = (int)tmp.size();
             out.insert(out.end(), tmp.begin(), tmp.end());
         }
-    });
+    }, 2048);
     adj_begin_.assign(size() + 1, 0);
     adj_.clear();
     size_t total = 0;
@@ -267,7 +267,7 @@ void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) co
                 cpart[ch][stage].push_back({b, r, n, lvl_diff});
             });
         }
-    });
+    }, 2048);
     // the boxes of a patch depend on its relation and level difference only
     std::vector<Patch> tmpl(3 * (kNumRelations + 1));
     std::vector<int> tmpl_need(3 * (kNumRelations + 1), -1);
@@ -378,8 +378,9 @@ void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) co
             // copies and restrictions never conflict within a stage (a copy
             // reads the sender's interior and writes ghost nodes, a
             // restriction reads the filtered lattice, and the ghost boxes of
-            // the relations of one receiver are disjoint): every chunk of
-            // senders becomes a wave of its own, built in parallel
+            // the relations of one receiver are disjoint): the stage is one
+            // wave (all filters before all writes), built per chunk of
+            // senders in parallel
             std::vector<SyncWave> part(nch);
             auto chunk = [&](int c) {
                 std::unordered_map<int, int> entry_of;
@@ -391,11 +392,29 @@ void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) co
                     if (prepare(cd, p, need, tmp_rp, tmp_same)) add(cd, p, need, tmp_rp, tmp_same, part[c], entry_of);
                 }
             };
-            if (ncand >= 8192) par_tasks(nch, chunk);
+            if (ncand >= 2048) par_tasks(nch, chunk);
             else
                 for (int c = 0; c < nch; c++) chunk(c);
-            for (SyncWave &w : part)
-                if (!w.copy_blk.empty() || !w.copy_tmp.empty() || !w.restrict_.empty()) waves.push_back(std::move(w));
+            // one wave for the stage made of the chunks' lists in chunk
+            // order; filter entries renumbered in place
+            std::vector<int> off(nch + 1, 0);
+            for (int c = 0; c < nch; c++) off[c + 1] = off[c] + (int)part[c].filters.size();
+            auto renumber = [&](int c) {
+                for (ScBox &x : part[c].ce_copies) x.entry += off[c];
+                for (Patch &x : part[c].restrict_) x.src += off[c];
+            };
+            if (ncand >= 2048) par_tasks(nch, renumber);
+            else
+                for (int c = 0; c < nch; c++) renumber(c);
+            SyncWave all;
+            all.stage = istage;
+            bool any = false;
+            for (int c = 0; c < nch; c++) {
+                any = any || !part[c].copy_blk.empty() || !part[c].copy_tmp.empty() || !part[c].restrict_.empty();
+                if (!part[c].copy_blk.empty() || !part[c].copy_tmp.empty() || !part[c].filters.empty())
+                    all.parts.push_back(std::move(part[c]));
+            }
+            if (any) waves.push_back(std::move(all));
             continue;
         }
         // predictions: in the reference's order, cut into waves where a

@@ -23,6 +23,7 @@
 // reads, so each wave runs in parallel with the sequential result.
 #pragma once
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <utility>
 #include <vector>
@@ -60,14 +61,41 @@ struct ScBox {
     int16_t lo[3], hi[3];
 };
 
+// vectors of plain records whose resize leaves the new elements
+// uninitialised (they are written right after, in parallel)
+template <class T>
+struct NoInit : std::allocator<T> {
+    template <class U>
+    struct rebind {
+        using other = NoInit<U>;
+    };
+    NoInit() = default;
+    template <class U>
+    NoInit(const NoInit<U> &) {}
+    template <class U>
+    void construct(U *p) {
+        ::new (static_cast<void *>(p)) U;
+    }
+    template <class U, class... A>
+    void construct(U *p, A &&...a) {
+        ::new (static_cast<void *>(p)) U(std::forward<A>(a)...);
+    }
+};
+template <class T>
+using RecVec = std::vector<T, NoInit<T>>;
+
 struct SyncWave {
     int stage = 1;
-    std::vector<Patch> copy_blk, copy_tmp;      // op 0 from hvy_block / hvy_tmp
-    std::vector<FilterEntry> filters;           // restriction: filtered senders
-    std::vector<ScBox> ce_copies;               // SC copied back into the entries
-    std::vector<Patch> restrict_;               // op 1, src = filter entry index
-    std::vector<Patch> pred_blk, pred_tmp;      // op 2 from hvy_block / hvy_tmp
+    RecVec<Patch> copy_blk, copy_tmp;           // op 0 from hvy_block / hvy_tmp
+    RecVec<FilterEntry> filters;                // restriction: filtered senders
+    RecVec<ScBox> ce_copies;                    // SC copied back into the entries
+    RecVec<Patch> restrict_;                    // op 1, src = filter entry index
+    RecVec<Patch> pred_blk, pred_tmp;           // op 2 from hvy_block / hvy_tmp
     int max_coarse = 0;                         // shared memory of the largest prediction (doubles)
+    // a stage of copies and restrictions built per chunk of senders: the
+    // wave is the concatenation of these parts' lists (their filter entry
+    // numbers already count the entries of the parts before them)
+    std::vector<SyncWave> parts;
 };
 
 struct SyncSpecL {
