@@ -192,6 +192,7 @@ struct Tree {
     DevArray<int> d_all, d_plain, d_masked;   // slot lists
     int n_plain = 0, n_masked = 0;
     std::map<long long, std::unique_ptr<SyncPlan>> sync;   // key: gm, gp, buffer
+    std::map<long long, std::unique_ptr<SyncPlan>> spare;  // plans of an earlier grid: device buffers to reuse
     double time = 0.0;
     bool shadow_valid = false;         // double-float copy of u_n in B is current
 };
@@ -426,11 +427,32 @@ int build_push(wg_ctx *ctx, Tree &t, SyncPlan &sp, const BufGeo &geo) {
     return WG_OK;
 }
 
+// the tree's sync plans are stale (its grid changed): their device buffers
+// serve the plans of the new grid, so a grid change allocates and frees no
+// device memory for them (the stream is idle at every caller)
+void drop_sync(Tree &t) {
+    for (auto &kv : t.sync) {
+        SyncPlan &p = *kv.second;
+        p.pair_begin.clear();
+        p.copy_end.clear();
+        p.push_ok = false;
+        t.spare[kv.first] = std::move(kv.second);
+    }
+    t.sync.clear();
+}
+
 int get_sync(wg_ctx *ctx, Tree &t, int gm, int gp, bool thin, SyncPlan **out) {
     const long long key = sync_key(gm, gp, thin ? 1 : 0);
     auto it = t.sync.find(key);
     if (it == t.sync.end()) {
-        std::unique_ptr<SyncPlan> sp(new SyncPlan());
+        std::unique_ptr<SyncPlan> sp;
+        auto old = t.spare.find(key);
+        if (old != t.spare.end()) {
+            sp = std::move(old->second);
+            t.spare.erase(old);
+        } else {
+            sp.reset(new SyncPlan());
+        }
         std::string err;
         if (!make_sync_table(t.forest, ctx->geo, ctx->wav, gm, gp, thin ? ctx->gT.gb : ctx->gA.gb, 0, sp->table, err))
             return fail(WG_EGRID, "sync table: %s", err.c_str());
@@ -537,7 +559,7 @@ void release_tree_blocks(wg_ctx *ctx, Tree &t) {
         if (m >= 0) ctx->mask_free.push_back(m);
     t.slots.clear();
     t.mask_slot.clear();
-    t.sync.clear();
+    drop_sync(t);
     t.n_plain = t.n_masked = 0;
 }
 
@@ -1968,7 +1990,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     if (!t->forest.graded()) return fail(WG_EGRID, "adapt produced a grid that is not graded");
     t->slots = sl;
     t->mask_slot.assign(nn, -1);
-    t->sync.clear();
+    drop_sync(*t);
     t->shadow_valid = false;
     int st;
     if ((st = upload_desc(ctx, *t, tree))) return st;
@@ -2092,7 +2114,7 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
     if (!t->forest.graded()) return fail(WG_EGRID, "adapt produced a grid that is not graded");
     t->slots = sl;
     t->mask_slot.assign(nn, -1);
-    t->sync.clear();
+    drop_sync(*t);
     t->shadow_valid = false;
     if ((st = upload_desc(ctx, *t, tree))) return st;
     if ((st = upload_lists(ctx, *t))) return st;
@@ -2233,7 +2255,7 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     t->slots = slots;
     t->mask_slot.assign(nn, -1);
     t->shadow_valid = false;
-    t->sync.clear();
+    drop_sync(*t);
     t->forest.set(nn, lv.data(), co.data());
     std::string err;
     if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "%s", err.c_str());
