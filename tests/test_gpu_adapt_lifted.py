@@ -51,11 +51,14 @@ def test_coarsen_everywhere_cdf44_matches_oracle(golden):
     assert np.abs(interior(cfg, b[2])[:, :1] - z["coarsened_CDF44_u"]).max() <= 4e-15
 
 
-@pytest.mark.parametrize("dim,Bs,jmin,jmax,quantile", [(2, 32, 1, 4, 0.6), (2, 16, 2, 5, 0.5), (3, 16, 1, 3, 0.8)])
+@pytest.mark.parametrize("dim,Bs,jmin,jmax,quantile", [(2, 32, 1, 4, 0.6), (2, 16, 2, 5, 0.5), (3, 16, 1, 3, 0.8),
+                                                      (2, 16, 2, 7, 0.5)])
 def test_threshold_adapt_cdf44_matches_oracle(dim, Bs, jmin, jmax, quantile):
     """Bs=32 takes the leaf-first decomposition and the leaf-only
     reconstruction; Bs=16 (below 3 x the HD half-width and below Ndep2r)
-    the level-wise decomposition and reconstruction."""
+    the level-wise decomposition and reconstruction. The Jmax=7 grid (2,218
+    leaves, ~2,900 full-tree blocks) is planned on the host thread pool, and
+    its copy/restriction stages are waves made of per-chunk lists."""
     cfg = small_cfg(dim, "CDF44", Bs=Bs, jmin=jmin, jmax=jmax)
     lv, co = grids.random_graded(dim, cfg.Jmin, cfg.Jmax, seed=33, frac=0.45)
     data = smooth_state(cfg, lv, co, 9)

@@ -86,7 +86,10 @@ __device__ __forceinline__ df2 df_norm(df2 a) { return two_sum(a.hi, a.lo); }
 // [2^-74, 2^128) (where lo or hi would not be a normal float) and inf/nan go
 // through the FP64 units.
 __device__ __forceinline__ df2 df_split(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    // the bits through an opaque move: the compiler would otherwise turn the
+    // zero and exponent tests below into FP64 compares
+    unsigned long long b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(v));
     const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
     if ((b << 1) == 0ull) return {__uint_as_float(sign), 0.f};
     const int e = (int)((b >> 52) & 0x7ff) - 1023;

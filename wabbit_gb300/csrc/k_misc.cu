@@ -7,20 +7,22 @@
 // step can be captured in a CUDA graph.
 #include "common.cuh"
 #include "df.cuh"
+#include "exact.cuh"
 
 namespace wg {
 
 // |x| <= 1e12 on the bits (false for nan), the divergence guard of the ACM
-// integral stage (rhs_ACM.f90:133-146)
+// integral stage (rhs_ACM.f90:133-146); the bits through the opaque move of
+// exact.cuh, so that the test stays on the integer units
 __device__ __forceinline__ bool within_guard(double x) {
-    const unsigned long long a = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    const unsigned long long a = (unsigned long long)dbits(x) & 0x7fffffffffffffffull;
     return a <= 0x426d1a94a2000000ull;   // bits of 1.0e12
 }
 
 // float not above |x|, by truncation on the integer units (0 below 2^-126,
 // inf from 2^128): |x|(1 - 2^-23) < result <= |x| in the normal range
 __device__ __forceinline__ float trunc_abs_f(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long b = (unsigned long long)dbits(x);
     const int e = (int)((b >> 52) & 0x7ff) - 1023;
     if (e < -126) return 0.f;
     if (e > 127) return __uint_as_float(0x7f800000u);
