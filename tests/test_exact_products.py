@@ -3,7 +3,8 @@ IEEE multiply: the header compiles for the host, and a C++ driver checks
 millions of products (random bit patterns, normal ranges, significands with
 long runs of low zero or one bits for ties and carries) for bit identity, and
 that the fallback flag is raised only at subnormal, special or out-of-range
-inputs and results."""
+inputs and results. The same driver checks the assembly of double-float
+pairs into doubles (df_pair_to_double) against the FP64 sum."""
 import os
 import shutil
 import subprocess
@@ -28,5 +29,9 @@ def test_exact_tap_products_match_ieee_multiply(tmp_path):
     # every CDF4,4 / CDF4,0 tap and the 4th-order interpolation weights take
     # the integer pipe (kinds 1-3); only 0.1 and the 8th-order 245/2048 and
     # 1225/2048 fall back
-    kinds = [int(v) for v in fields[fields.index("kinds") + 1:]]
+    k = fields.index("kinds")
+    kinds = [int(v) for v in fields[k + 1:k + 5]]
     assert kinds[0] == 6 and sum(kinds) == 44
+    # double-float pairs assembled into doubles on the integer units: nearly
+    # all normalised pairs take that path, each exactly
+    assert int(fields[fields.index("accepted") + 1]) > 0.9 * int(fields[fields.index("pairs") + 1])

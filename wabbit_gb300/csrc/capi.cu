@@ -1926,9 +1926,15 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         const std::vector<int> keep = slots_where([&](int b) { return on_level(b) && L.ref[b] != -1; });
         cudaError_t r = cudaSuccess;
         auto t0 = tic();
+        // waveletReconstruction_optimized_block writes into hvy_tmp and
+        // hvy_block takes that copy (adapt_tree.f90:921-922): the later
+        // levels' syncs read these blocks from hvy_tmp
+        const int *d_rec = rec.empty() ? nullptr : up(rec);
         if (!rec.empty())
-            r = launch_wavelet_reconstruct(dim, up(rec), (int)rec.size(), ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X,
+            r = launch_wavelet_reconstruct(dim, d_rec, (int)rec.size(), ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X,
                                            w.Y, ctx->stream);
+        if (r == cudaSuccess && !rec.empty())
+            r = launch_blockcopy(d_rec, (int)rec.size(), ctx->A, ctx->T, per_block, ctx->stream);
         toc(kRecon, t0);
         t0 = tic();
         if (r == cudaSuccess && !keep.empty())

@@ -374,13 +374,52 @@ void LiftedTree::plan_sync(const SyncSpecL &sp, std::vector<SyncWave> &waves) co
         size_t ncand = 0;
         for (int ch = 0; ch < nch; ch++) ncand += cpart[ch][istage].size();
         if (ncand == 0) continue;
+        if (wav.lifted && sp.filter && istage == 2 - unl) {
+            // HD-filtered restrictions: the reference handles the senders in
+            // order and filters a sender's block when it first sends, from its
+            // current data, so restrictions written into its ghost nodes by
+            // earlier senders of the stage are part of its filter input. A
+            // wave runs all its filters before its writes: a new wave starts
+            // when a sender that reads hvy_block was written in this one.
+            SyncWave cur;
+            cur.stage = istage;
+            std::unordered_map<int, int> entry_of;
+            std::vector<char> written(size(), 0);
+            std::vector<int> touched;
+            int sender = -1;
+            auto flush = [&]() {
+                if (!cur.restrict_.empty()) waves.push_back(std::move(cur));
+                cur = SyncWave();
+                cur.stage = istage;
+                entry_of.clear();
+                for (int t : touched) written[t] = 0;
+                touched.clear();
+            };
+            for (int ch = 0; ch < nch; ch++)
+                for (const Cand &cd : cpart[ch][istage]) {
+                    Patch p;
+                    int need;
+                    bool tmp_rp, tmp_same;
+                    if (!prepare(cd, p, need, tmp_rp, tmp_same)) continue;
+                    if (cd.b != sender) {
+                        sender = cd.b;
+                        if (!tmp_rp && written[cd.b]) flush();
+                    }
+                    add(cd, p, need, tmp_rp, tmp_same, cur, entry_of);
+                    if (!written[cd.n]) {
+                        written[cd.n] = 1;
+                        touched.push_back(cd.n);
+                    }
+                }
+            flush();
+            continue;
+        }
         if (istage != 3 - unl) {
-            // copies and restrictions never conflict within a stage (a copy
-            // reads the sender's interior and writes ghost nodes, a
-            // restriction reads the filtered lattice, and the ghost boxes of
-            // the relations of one receiver are disjoint): the stage is one
-            // wave (all filters before all writes), built per chunk of
-            // senders in parallel
+            // copies (and unfiltered restrictions) never conflict within a
+            // stage (they read the sender's interior and write ghost nodes,
+            // and the ghost boxes of the relations of one receiver are
+            // disjoint): the stage is one wave, built per chunk of senders in
+            // parallel
             std::vector<SyncWave> part(nch);
             auto chunk = [&](int c) {
                 std::unordered_map<int, int> entry_of;
