@@ -3,8 +3,7 @@ IEEE multiply: the header compiles for the host, and a C++ driver checks
 millions of products (random bit patterns, normal ranges, significands with
 long runs of low zero or one bits for ties and carries) for bit identity, and
 that the fallback flag is raised only at subnormal, special or out-of-range
-inputs and results. The same driver checks the assembly of double-float
-pairs into doubles (df_pair_to_double) against the FP64 sum."""
+inputs and results."""
 import os
 import shutil
 import subprocess
@@ -32,6 +31,3 @@ def test_exact_tap_products_match_ieee_multiply(tmp_path):
     k = fields.index("kinds")
     kinds = [int(v) for v in fields[k + 1:k + 5]]
     assert kinds[0] == 6 and sum(kinds) == 44
-    # double-float pairs assembled into doubles on the integer units: nearly
-    # all normalised pairs take that path, each exactly
-    assert int(fields[fields.index("accepted") + 1]) > 0.9 * int(fields[fields.index("pairs") + 1])

@@ -52,13 +52,15 @@ def test_coarsen_everywhere_cdf44_matches_oracle(golden):
 
 
 @pytest.mark.parametrize("dim,Bs,jmin,jmax,quantile", [(2, 32, 1, 4, 0.6), (2, 16, 2, 5, 0.5), (3, 16, 1, 3, 0.8),
-                                                      (2, 16, 2, 7, 0.5)])
+                                                      (2, 16, 2, 7, 0.5), (3, 16, 1, 4, 0.7)])
 def test_threshold_adapt_cdf44_matches_oracle(dim, Bs, jmin, jmax, quantile):
     """Bs=32 takes the leaf-first decomposition and the leaf-only
     reconstruction; Bs=16 (below 3 x the HD half-width and below Ndep2r)
     the level-wise decomposition and reconstruction. The Jmax=7 grid (2,218
     leaves, ~2,900 full-tree blocks) is planned on the host thread pool, and
-    its copy/restriction stages are waves made of per-chunk lists."""
+    its copy/restriction stages are waves made of per-chunk lists; on it and
+    on the four-level 3-D grid the level-wise reconstruction reads blocks
+    reconstructed at the level below from hvy_tmp."""
     cfg = small_cfg(dim, "CDF44", Bs=Bs, jmin=jmin, jmax=jmax)
     lv, co = grids.random_graded(dim, cfg.Jmin, cfg.Jmax, seed=33, frac=0.45)
     data = smooth_state(cfg, lv, co, 9)

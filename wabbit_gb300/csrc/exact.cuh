@@ -133,30 +133,4 @@ WG_HD double tap_mul(double x, double c, int kind, int sh, int mul, long long sg
 #endif
 }
 
-// hi + lo of a normalised double-float pair (|lo| <= ulp(hi)/2) as a double,
-// assembled on the integer units: exact when both are normal floats (lo may
-// be zero) and lo's significand lies on the 53-bit grid of hi (exponent gap
-// at most 29) without a carry or borrow across hi's binade; ok is cleared
-// otherwise and the caller adds in FP64
-WG_HD double df_pair_to_double(float hi, float lo, bool &ok) {
-    unsigned hb, lb;
-#ifdef __CUDA_ARCH__
-    hb = __float_as_uint(hi);
-    lb = __float_as_uint(lo);
-#else
-    std::memcpy(&hb, &hi, 4);
-    std::memcpy(&lb, &lo, 4);
-#endif
-    const int eh = (int)((hb >> 23) & 0xffu), el = (int)((lb >> 23) & 0xffu);
-    const bool lz = (lb << 1) == 0u;
-    const int sh = 29 - (eh - el);   // lo's significand in units of hi's 53-bit ulp: << sh
-    ok = ok & ((unsigned)(eh - 1) < 254u) & (lz | (((unsigned)(el - 1) < 254u) & ((unsigned)sh <= 5u)));
-    const unsigned long long M = (unsigned long long)((hb & 0x7fffffu) | 0x800000u) << 29;
-    const unsigned long long L = lz ? 0ull : (unsigned long long)((lb & 0x7fffffu) | 0x800000u) << (sh & 7);
-    const unsigned long long R = ((hb ^ lb) & 0x80000000u) ? M - L : M + L;
-    ok = ok & ((R >> 52) == 1ull);
-    return dfrom((long long)(((unsigned long long)(hb & 0x80000000u) << 32) |
-                             ((unsigned long long)(eh + 896) << 52) | (R & 0xfffffffffffffULL)));
-}
-
 }  // namespace wg

@@ -21,7 +21,6 @@
 // contracted; every FMA is explicit.
 #include "common.cuh"
 #include "df.cuh"
-#include "exact.cuh"
 #include "tma.cuh"
 
 namespace wg {
@@ -242,13 +241,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
             const df2 inc = df_norm(df_add_nr({in.acc[c].x, in.acc[c].y}, df_mul_nr(db, df_norm(r[c]))));
-            // u_n+1 = u_n + inc in FP64: the pair assembled into one double
-            // on the integer units (exact for nearly every pair), else added
-            // in two FP64 steps
-            const double u0 = f2_bits(in.u0[c]);
-            bool whole = true;
-            const double iw = df_pair_to_double(inc.hi, inc.lo, whole);
-            const double v = whole ? __dadd_rn(u0, iw) : __dadd_rn(__dadd_rn(u0, f2d_bits(inc.hi)), f2d_bits(inc.lo));
+            const double v = __dadd_rn(__dadd_rn(f2_bits(in.u0[c]), f2d_bits(inc.hi)), f2d_bits(inc.lo));
             un[c * us] = v;
             const df2 w = df_split(v);
             ov[c] = make_float2(w.hi, w.lo);
