@@ -46,12 +46,15 @@ def test_coarsen_everywhere_golden_cdf40(golden):
         assert np.array_equal(u[:, c:c + 1], z["coarsened_CDF40_u"])
 
 
-@pytest.mark.parametrize("dim,wavelet,quantile", [(2, "CDF40", 0.5), (2, "CDF20", 0.7), (2, "CDF60", 0.4),
-                                                  (3, "CDF40", 0.95)])
-def test_threshold_adapt_matches_oracle(dim, wavelet, quantile):
+@pytest.mark.parametrize("dim,wavelet,quantile,jmax", [(2, "CDF40", 0.5, 5), (2, "CDF20", 0.7, 5), (2, "CDF60", 0.4, 5),
+                                                       (3, "CDF40", 0.95, 3), (2, "CDF40", 0.5, 7),
+                                                       (3, "CDF40", 0.8, 4)])
+def test_threshold_adapt_matches_oracle(dim, wavelet, quantile, jmax):
+    """Jmax=7 (2-D, six levels, ~2,200 leaves) and Jmax=4 (3-D, four levels)
+    take the host thread pool and full trees with long level chains."""
     g, _ = config.wavelet_ghosts(wavelet)
     Bs = 16 if dim == 2 else 8
-    cfg = small_cfg(dim, wavelet, Bs=Bs, jmin=2 if dim == 2 else 1, jmax=5 if dim == 2 else 3)
+    cfg = small_cfg(dim, wavelet, Bs=Bs, jmin=2 if dim == 2 else 1, jmax=jmax)
     lv, co = grids.random_graded(dim, cfg.Jmin, cfg.Jmax, seed=21, frac=0.45)
     data = smooth_state(cfg, lv, co, 7)
     o = Oracle(cfg)
