@@ -284,7 +284,7 @@ bool Forest::update_neighbors(std::string &err, bool overlapping) {
                         if (!overlapping) continue;
                     }
                     int a[3];
-                    for (int i = 0; i < 3; i++) a[i] = i < dim ? ((c[i] + d[i]) % N + N) % N : 0;
+                    for (int i = 0; i < 3; i++) a[i] = i < dim ? (c[i] + d[i]) & (N - 1) : 0;   // periodic, N a power of two
                     if (lv > 0) {
                         const int s = find(lv, a[0], a[1], a[2]);
                         if (s >= 0) {
@@ -305,7 +305,7 @@ bool Forest::update_neighbors(std::string &err, bool overlapping) {
                                     if (d[i] == 0) bit = (p >> fr++) & 1;
                                     else bit = d[i] > 0 ? 1 : 0;
                                     const int v = 2 * c[i] + bit + d[i];
-                                    fc[i] = ((v % (2 * N)) + 2 * N) % (2 * N);
+                                    fc[i] = v & (2 * N - 1);
                                 }
                                 const int fb = find(lv + 1, fc[0], fc[1], fc[2]);
                                 if (fb < 0) break;
@@ -336,7 +336,7 @@ bool Forest::update_neighbors(std::string &err, bool overlapping) {
                                 if (d[i] == 0) bit = (p >> fr++) & 1;
                                 else bit = d[i] > 0 ? 1 : 0;
                                 int v = 2 * c[i] + bit + d[i];
-                                fc[i] = ((v % (2 * N)) + 2 * N) % (2 * N);
+                                fc[i] = v & (2 * N - 1);
                             }
                             int fb = find(lv + 1, fc[0], fc[1], fc[2]);
                             if (fb < 0) { all = false; break; }

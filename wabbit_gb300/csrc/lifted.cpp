@@ -19,6 +19,7 @@ bool LiftedTree::init(const Geometry &g, const WaveletInfo &w, int fd_max_size, 
     nleaves = nleaf;
     if (!build_full_tree(g.dim, jmin, nleaf, level, coords, ft, err)) return false;
     alive.assign(ft.size(), 1);
+    full_ready_ = false;
     ref.assign(ft.size(), 0);
     slot.assign(ft.size(), -1);
     size_t cap = 16;
@@ -69,8 +70,7 @@ int LiftedTree::find_(int lv, int x, int y, int z) const {
 // missing one, then the coarser block; only alive blocks are recorded. The
 // finer blocks are daughters and the coarser block the mother of the
 // same-level position's block of the full tree, when it exists.
-bool LiftedTree::update_metadata(std::string &err) {
-    (void)err;
+void LiftedTree::search_all_() {
     const int dim = geo.dim, nch = host_threads();
     std::vector<std::vector<std::pair<int, int>>> part(nch);
     std::vector<std::vector<int>> count(nch);
@@ -78,13 +78,15 @@ bool LiftedTree::update_metadata(std::string &err) {
         std::vector<std::pair<int, int>> &out = part[ch];
         std::vector<int> &cnt = count[ch];
         cnt.assign(hi - lo, 0);
-        std::vector<std::pair<int, int>> tmp;
+        // neighbour per relation (each relation occurs at most once): read
+        // out in ascending order without a sort
+        int slot[kNumRelations];
+        int used[kNumRelations], nused = 0;
         for (int b = lo; b < hi; b++) {
-            if (!alive[b]) continue;
             const int lv = ft.level[b];
             const int *c = &ft.coords[3 * b];
             const int N = 1 << lv;
-            tmp.clear();
+            nused = 0;
             for (int dz = (dim == 3 ? -1 : 0); dz <= (dim == 3 ? 1 : 0); dz++)
                 for (int dy = -1; dy <= 1; dy++)
                     for (int dx = -1; dx <= 1; dx++) {
@@ -94,9 +96,13 @@ bool LiftedTree::update_metadata(std::string &err) {
                         for (int i = 0; i < dim; i++) nfree += (d[i] == 0);
                         const int nparts = 1 << nfree;
                         int a[3] = {0, 0, 0};
-                        for (int i = 0; i < dim; i++) a[i] = ((c[i] + d[i]) % N + N) % N;
+                        for (int i = 0; i < dim; i++) a[i] = (c[i] + d[i]) & (N - 1);   // periodic, N a power of two
                         const int same = lv == 0 ? b : find_(lv, a[0], a[1], a[2]);
-                        if (same >= 0 && alive[same]) tmp.push_back({relation_id(d, 0, dim), same});
+                        if (same >= 0) {
+                            const int r = relation_id(d, 0, dim) - 1;
+                            slot[r] = same;
+                            used[nused++] = r;
+                        }
                         if (lv < Jmax && same >= 0)
                             for (int p = 0; p < nparts; p++) {
                                 int k = 0, fr = 0;
@@ -105,11 +111,13 @@ bool LiftedTree::update_metadata(std::string &err) {
                                     if (d[i] == 0) bit = (p >> fr++) & 1;
                                     else bit = d[i] > 0 ? 1 : 0;
                                     // daughter bit of the fine neighbour: (2c + bit + d) mod 2
-                                    k |= (((bit + d[i]) % 2 + 2) % 2) << i;
+                                    k |= ((bit + d[i]) & 1) << i;
                                 }
                                 const int f = ft.daughters[8 * same + k];
-                                if (f < 0 || !alive[f]) break;
-                                tmp.push_back({relation_id(d, p, dim) + 112, f});
+                                if (f < 0) break;
+                                const int r = relation_id(d, p, dim) + 111;
+                                slot[r] = f;
+                                used[nused++] = r;
                             }
                         if (lv <= Jmin) continue;
                         int prt = 0, fr = 0;
@@ -121,27 +129,101 @@ bool LiftedTree::update_metadata(std::string &err) {
                         }
                         if (!touches) continue;
                         const int cb = same >= 0 ? ft.mother[same] : find_(lv - 1, a[0] >> 1, a[1] >> 1, a[2] >> 1);
-                        if (cb >= 0 && alive[cb]) tmp.push_back({relation_id(d, prt, dim) + 56, cb});
+                        if (cb >= 0) {
+                            const int r = relation_id(d, prt, dim) + 55;
+                            slot[r] = cb;
+                            used[nused++] = r;
+                        }
                     }
-            std::sort(tmp.begin(), tmp.end());
-            cnt[b - lo] = (int)tmp.size();
-            out.insert(out.end(), tmp.begin(), tmp.end());
+            // the used relations in ascending order: a 168-bit mask
+            uint64_t mk[3] = {0, 0, 0};
+            for (int i = 0; i < nused; i++) mk[used[i] >> 6] |= 1ull << (used[i] & 63);
+            for (int w = 0; w < 3; w++)
+                for (uint64_t m = mk[w]; m; m &= m - 1) {
+                    const int r = w * 64 + __builtin_ctzll(m);
+                    out.push_back({r + 1, slot[r]});
+                }
+            cnt[b - lo] = nused;
         }
     }, 2048);
-    adj_begin_.assign(size() + 1, 0);
-    adj_.clear();
+    full_begin_.assign(size() + 1, 0);
+    full_adj_.clear();
     size_t total = 0;
     for (const auto &v : part) total += v.size();
-    adj_.reserve(total);
+    full_adj_.reserve(total);
     int b = 0;
     for (int ch = 0; ch < nch; ch++) {
         for (int k : count[ch]) {
-            adj_begin_[b + 1] = adj_begin_[b] + k;
+            full_begin_[b + 1] = full_begin_[b] + k;
             b++;
         }
-        adj_.insert(adj_.end(), part[ch].begin(), part[ch].end());
+        full_adj_.insert(full_adj_.end(), part[ch].begin(), part[ch].end());
     }
-    for (; b < size(); b++) adj_begin_[b + 1] = adj_begin_[b];
+    for (; b < size(); b++) full_begin_[b + 1] = full_begin_[b];
+    // direction and part of every finer relation
+    rel_dir_.assign(kNumRelations, -1);
+    rel_part_.assign(kNumRelations, 0);
+    for (int dz = (dim == 3 ? -1 : 0); dz <= (dim == 3 ? 1 : 0); dz++)
+        for (int dy = -1; dy <= 1; dy++)
+            for (int dx = -1; dx <= 1; dx++) {
+                if (!dx && !dy && !dz) continue;
+                const int d[3] = {dx, dy, dz};
+                int nfree = 0;
+                for (int i = 0; i < dim; i++) nfree += (d[i] == 0);
+                for (int p = 0; p < (1 << nfree); p++) {
+                    const int r = relation_id(d, p, dim) + 111;
+                    rel_dir_[r] = (dx + 1) + 3 * (dy + 1) + 9 * (dz + 1);
+                    rel_part_[r] = p;
+                }
+            }
+    full_ready_ = true;
+}
+
+// find_neighbor with search_overlapping restricted to the alive blocks: a
+// filter of the all-alive search (computed once per tree). Same-level and
+// coarser neighbours stay when alive; the finer parts of a direction stay up
+// to the first part that is missing or not alive.
+bool LiftedTree::update_metadata(std::string &err) {
+    (void)err;
+    if (!full_ready_) search_all_();
+    const int n = size(), nch = host_threads();
+    std::vector<int> cnt(n, 0);
+    par_chunks(n, nch, [&](int, int lo, int hi) {
+        for (int b = lo; b < hi; b++) {
+            if (!alive[b]) continue;
+            int dead[27];
+            for (int k = 0; k < 27; k++) dead[k] = 1 << 20;
+            for (int i = full_begin_[b]; i < full_begin_[b + 1]; i++) {
+                const int r = full_adj_[i].first - 1;
+                if (r >= 112 && !alive[full_adj_[i].second]) dead[rel_dir_[r]] = std::min(dead[rel_dir_[r]], rel_part_[r]);
+            }
+            int c = 0;
+            for (int i = full_begin_[b]; i < full_begin_[b + 1]; i++) {
+                const int r = full_adj_[i].first - 1;
+                c += r < 112 ? alive[full_adj_[i].second] != 0 : rel_part_[r] < dead[rel_dir_[r]];
+            }
+            cnt[b] = c;
+        }
+    }, 2048);
+    adj_begin_.assign(n + 1, 0);
+    for (int b = 0; b < n; b++) adj_begin_[b + 1] = adj_begin_[b] + cnt[b];
+    adj_.resize(adj_begin_[n]);
+    par_chunks(n, nch, [&](int, int lo, int hi) {
+        for (int b = lo; b < hi; b++) {
+            if (!cnt[b]) continue;
+            int dead[27];
+            for (int k = 0; k < 27; k++) dead[k] = 1 << 20;
+            for (int i = full_begin_[b]; i < full_begin_[b + 1]; i++) {
+                const int r = full_adj_[i].first - 1;
+                if (r >= 112 && !alive[full_adj_[i].second]) dead[rel_dir_[r]] = std::min(dead[rel_dir_[r]], rel_part_[r]);
+            }
+            int at = adj_begin_[b];
+            for (int i = full_begin_[b]; i < full_begin_[b + 1]; i++) {
+                const int r = full_adj_[i].first - 1;
+                if (r < 112 ? alive[full_adj_[i].second] != 0 : rel_part_[r] < dead[rel_dir_[r]]) adj_[at++] = full_adj_[i];
+            }
+        }
+    }, 2048);
     return true;
 }
 
@@ -550,19 +632,27 @@ void LiftedTree::ce_copy_sc(int b, int relation, std::vector<BoxOp> &ops) const 
 
 void LiftedTree::plan_ce_modify(int ce_case, int s_level, int s_ref, bool clear_wc, bool copy_sc,
                                 std::vector<BoxOp> &ops) const {
-    for (int b = 0; b < size(); b++) {
-        if (!alive[b]) continue;
-        const int lv = ft.level[b];
-        if ((ce_case == 1 || ce_case == 3) && lv != s_level) continue;
-        if ((ce_case == 2 || ce_case == 3) && ref[b] != s_ref) continue;
-        if (!is_leaf(b, false)) continue;
-        for_neighbors(b, [&](int r, int n) {
-            if (ft.level[n] < lv && !(has_valid_neighbor(b, r, 0) || has_valid_neighbor(b, r, -1))) {
-                if (clear_wc) ce_clear_wc(b, r, ops);
-                if (copy_sc) ce_copy_sc(b, r, ops);
-            }
-        });
-    }
+    // per chunk of blocks on the host pool, joined in block order
+    const int nch = host_threads();
+    std::vector<std::vector<BoxOp>> part(nch);
+    par_chunks(size(), nch, [&](int ch, int lo, int hi) {
+        std::vector<BoxOp> &out = part[ch];
+        for (int b = lo; b < hi; b++) {
+            if (!alive[b]) continue;
+            const int lv = ft.level[b];
+            if ((ce_case == 1 || ce_case == 3) && lv != s_level) continue;
+            if ((ce_case == 2 || ce_case == 3) && ref[b] != s_ref) continue;
+            if (!is_leaf(b, false)) continue;
+            for_neighbors(b, [&](int r, int n) {
+                if (ft.level[n] < lv && !(has_valid_neighbor(b, r, 0) || has_valid_neighbor(b, r, -1))) {
+                    if (clear_wc) ce_clear_wc(b, r, out);
+                    if (copy_sc) ce_copy_sc(b, r, out);
+                }
+            });
+        }
+    }, 2048);
+    ops.clear();
+    for (const auto &v : part) ops.insert(ops.end(), v.begin(), v.end());
 }
 
 void LiftedTree::security_candidates(std::vector<ZoneItem> &items) const {

@@ -155,8 +155,14 @@ public:
     void security_apply(const std::vector<ZoneItem> &items, const std::vector<char> &significant);
 
 private:
-    std::vector<int> adj_begin_;   // neighbour lists, ascending relation
+    std::vector<int> adj_begin_;   // neighbour lists of the alive blocks, ascending relation
     std::vector<std::pair<int, int>> adj_;
+    // the same search with every block of the full tree alive (once per tree)
+    bool full_ready_ = false;
+    std::vector<int> full_begin_;
+    std::vector<std::pair<int, int>> full_adj_;
+    std::vector<int> rel_dir_, rel_part_;   // direction (0..26) and part of finer relation r-1
+    void search_all_();
     std::vector<uint64_t> keys_;   // open-addressing table: block key -> full-tree index
     std::vector<int> vals_;
     uint64_t mask_ = 0;
