@@ -539,6 +539,14 @@ __device__ __forceinline__ double iwt_point_k(const double *src, long long st, i
     return v;
 }
 
+// Zero, or a biased exponent in [16, 2030]: the product of such a value with
+// a CDF4,4 tap (2^-9 <= |c| <= 1) is zero or a normal number, so a pass
+// whose inputs all lie in this band needs no range check per product.
+__device__ __forceinline__ bool in_tap_band(double x) {
+    const unsigned long long a = (unsigned long long)dbits(x) & 0x7fffffffffffffffULL;
+    return (a == 0ULL) | ((unsigned)((int)(a >> 52) - 16) <= 2014u);
+}
+
 // MODE 0: details (max |WC|) into scratch; 1: FWT stored in place; 2: IWT
 // stored in place. f: half-width of the extended window.
 struct GenericTaps {};
@@ -567,23 +575,42 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
             return MODE == 2 ? iwt_point_k<K>(src, st, at, p, bad) : fwt_point_k<K>(src, st, at, p, bad);
     };
     auto point = slow;
+    constexpr bool kTyped = !std::is_same<K, GenericTaps>::value;
+    // inputs of every pass in the tap band (block-wide): the products skip
+    // their range checks (the compiler drops the unread flags)
+    bool band = false;
+    if constexpr (kTyped) {
+        bool ok = true;
+        for (long long i = threadIdx.x; i < np; i += kTpoThreads) ok &= in_tap_band(ub[i]);
+        band = __syncthreads_and(ok) != 0;
+    }
+    bool ok_next = true;   // this thread's outputs of the pass in the band
     // x pass, two independent outputs per step
     const int nx_out = Bx * ny * nz;
     auto xrow = [&](int o) { return ub + ((long long)(z0 + (o / Bx) / ny) * geo.ny + (y0 + (o / Bx) % ny)) * geo.nx; };
     for (int o = threadIdx.x; o < nx_out; o += 2 * kTpoThreads) {
         const int o2 = o + kTpoThreads;
         const bool two = o2 < nx_out;
-        bool bad = false;
-        double v1 = fast(xrow(o), 1, g + o % Bx, o % Bx, bad);
-        double v2 = two ? fast(xrow(o2), 1, g + o2 % Bx, o2 % Bx, bad) : 0.0;
-        if (bad) {
-            v1 = slow(xrow(o), 1, g + o % Bx, o % Bx);
-            if (two) v2 = slow(xrow(o2), 1, g + o2 % Bx, o2 % Bx);
+        double v1, v2;
+        if (band) {
+            bool unread = false;
+            v1 = fast(xrow(o), 1, g + o % Bx, o % Bx, unread);
+            v2 = two ? fast(xrow(o2), 1, g + o2 % Bx, o2 % Bx, unread) : 0.0;
+        } else {
+            bool bad = false;
+            v1 = fast(xrow(o), 1, g + o % Bx, o % Bx, bad);
+            v2 = two ? fast(xrow(o2), 1, g + o2 % Bx, o2 % Bx, bad) : 0.0;
+            if (bad) {
+                v1 = slow(xrow(o), 1, g + o % Bx, o % Bx);
+                if (two) v2 = slow(xrow(o2), 1, g + o2 % Bx, o2 % Bx);
+            }
         }
+        if constexpr (kTyped) ok_next &= in_tap_band(v1) & in_tap_band(v2);
         sm[o] = v1;
         if (two) sm[o2] = v2;
     }
-    __syncthreads();
+    if constexpr (kTyped) band = __syncthreads_and(ok_next) != 0;
+    else __syncthreads();
     if (MODE == 3) {
         // the x pass results outside the interior rows/planes stay in the
         // block, as the reference's FWT leaves them in u_d
@@ -597,7 +624,17 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
     // y pass on the interior rows of every plane of the window
     double res[kTpoMaxPerThread];
     const int ny_out = Bx * By * nz;
-    {
+    if (band) {
+        bool unread = false;
+#pragma unroll
+        for (int k = 0; k < kTpoMaxPerThread; k++) {
+            const int o = threadIdx.x + k * kTpoThreads;
+            if (o < ny_out) {
+                const int ix = o % Bx, iy = (o / Bx) % By, zz = o / (Bx * By);
+                res[k] = fast(sm + (long long)zz * ny * Bx + ix, Bx, f + iy, iy, unread);
+            }
+        }
+    } else {
         bool bad = false;
 #pragma unroll
         for (int k = 0; k < kTpoMaxPerThread; k++) {
@@ -634,6 +671,7 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
         }
     } else {
         __syncthreads();
+        ok_next = true;
 #pragma unroll
         for (int k = 0; k < kTpoMaxPerThread; k++) {
             const int o = threadIdx.x + k * kTpoThreads;
@@ -642,8 +680,11 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
             sm[((long long)zz * ny + (f + iy)) * Bx + ix] = res[k];
             if (MODE == 3 && (zz < f || zz >= f + Bz))
                 ub[((long long)(z0 + zz) * geo.ny + (g + iy)) * geo.nx + (g + ix)] = res[k];
+            if constexpr (kTyped) ok_next &= in_tap_band(res[k]);
         }
-        __syncthreads();
+        // the z pass reads only these y pass results
+        if constexpr (kTyped) band = __syncthreads_and(ok_next) != 0;
+        else __syncthreads();
         const int nint = Bx * By * Bz;
         auto zcol = [&](int o) { return sm + (long long)(f + (o / Bx) % By) * Bx + o % Bx; };
         auto put = [&](int o, double v) {
@@ -658,12 +699,19 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
             const int o2 = o + kTpoThreads;
             const bool two = o2 < nint;
             const long long st = (long long)ny * Bx;
-            bool bad = false;
-            double v1 = fast(zcol(o), st, f + o / (Bx * By), o / (Bx * By), bad);
-            double v2 = two ? fast(zcol(o2), st, f + o2 / (Bx * By), o2 / (Bx * By), bad) : 0.0;
-            if (bad) {
-                v1 = slow(zcol(o), st, f + o / (Bx * By), o / (Bx * By));
-                if (two) v2 = slow(zcol(o2), st, f + o2 / (Bx * By), o2 / (Bx * By));
+            double v1, v2;
+            if (band) {
+                bool unread = false;
+                v1 = fast(zcol(o), st, f + o / (Bx * By), o / (Bx * By), unread);
+                v2 = two ? fast(zcol(o2), st, f + o2 / (Bx * By), o2 / (Bx * By), unread) : 0.0;
+            } else {
+                bool bad = false;
+                v1 = fast(zcol(o), st, f + o / (Bx * By), o / (Bx * By), bad);
+                v2 = two ? fast(zcol(o2), st, f + o2 / (Bx * By), o2 / (Bx * By), bad) : 0.0;
+                if (bad) {
+                    v1 = slow(zcol(o), st, f + o / (Bx * By), o / (Bx * By));
+                    if (two) v2 = slow(zcol(o2), st, f + o2 / (Bx * By), o2 / (Bx * By));
+                }
             }
             put(o, v1);
             if (two) put(o2, v2);
