@@ -155,6 +155,16 @@ int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask);
 /* Same for the n listed blocks only (mask holds n*6*npts doubles); every
  * other block has chi = 0. */
 int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const double *mask);
+/* Mask of a fixed sphere (centre[3], radius) computed on the device for a
+ * 3-D tree (create_mask_3D_acm 'sphere-fixed' -> draw_sphere,
+ * LIB/EQUATION/ACMnew/create_mask.f90:58-61,
+ * LIB/EQUATION/insects/module_geometry.f90:49-117): chi is the cosine step
+ * of the signed distance over h = c_smooth * dx at Jmax, colour 1, u_s = 0;
+ * only blocks with chi > 0 at an interior point keep a mask. */
+int wg_set_mask_sphere(wg_ctx *ctx, int tree, const double *centre, double radius, double c_smooth);
+/* Interior mask of one block (6 * Bs^d doubles) for inspection: returns 1
+ * and fills out if the block has a mask, 0 if it has none. */
+int wg_get_mask_block(wg_ctx *ctx, int tree, int block, double *out);
 
 int wg_set_time(wg_ctx *ctx, int tree, double time);
 int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);

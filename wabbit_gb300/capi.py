@@ -24,7 +24,8 @@ EXPORTS = [
     "wg_get_nblocks", "wg_get_grid", "wg_upload_state", "wg_download_state", "wg_set_mask", "wg_set_time",
     "wg_get_time", "wg_sync_ghosts", "wg_rhs", "wg_compute_dt", "wg_rk4_step", "wg_run", "wg_threshold_flags",
     "wg_refine_everywhere", "wg_sync_table", "wg_block_slot", "wg_sync_table_host",
-    "wg_probe_alu", "wg_time_kernel", "wg_tree_stats", "wg_set_mask_sparse",
+    "wg_probe_alu", "wg_time_kernel", "wg_tree_stats", "wg_set_mask_sparse", "wg_set_mask_sphere",
+    "wg_get_mask_block",
     "wg_upload_interior", "wg_download_interior", "wg_graph_kernels",
     "wg_threshold_flags_noalloc", "wg_set_stage_form", "wg_get_stage_form",
     "wg_wavelet_decompose", "wg_wavelet_reconstruct", "wg_wavelet_threshold", "wg_threshold_flags_wd",
@@ -85,6 +86,8 @@ _SIGS = {
     "wg_time_kernel": (_i, [_vp, _i, _i, _i, _dp]),
     "wg_tree_stats": (_i, [_vp, _i, _ip, _ip]),
     "wg_set_mask_sparse": (_i, [_vp, _i, _i, _ip, _dp]),
+    "wg_set_mask_sphere": (_i, [_vp, _i, _dp, ctypes.c_double, ctypes.c_double]),
+    "wg_get_mask_block": (_i, [_vp, _i, _i, _dp]),
     "wg_upload_interior": (_i, [_vp, _i, _dp]),
     "wg_download_interior": (_i, [_vp, _i, _dp]),
     "wg_graph_kernels": (_i, [_vp]),

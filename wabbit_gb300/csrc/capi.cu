@@ -1231,6 +1231,40 @@ int wg_download_state(wg_ctx *ctx, int tree, double *host_blocks) {
 // (hvy_mask layout); all other blocks get no mask (chi = 0). Blocks whose
 // listed mask is zero (chi, u_s and sponge; the colour is ignored) keep no
 // device copy either.
+// room in the mask pool for `extra` more blocks (the pool and its
+// double-float copy grow by doubling; contents are kept)
+static int grow_mask_pool(wg_ctx *ctx, int extra) {
+    const long long ni = ctx->nint;
+    const int in_use = ctx->mask_cap - (int)ctx->mask_free.size();
+    const int want = in_use + extra;
+    if (want <= ctx->mask_cap) return WG_OK;
+    const int ncap = std::max(want, ctx->mask_cap * 2);
+    double *nm = nullptr;
+    float2 *nmd = nullptr;
+    const bool df = ctx->precision == WG_RHS_FP32;
+    if (cudaMalloc(&nm, sizeof(double) * 6 * ni * (size_t)ncap) != cudaSuccess ||
+        (df && cudaMalloc(&nmd, sizeof(float2) * 5 * ni * (size_t)ncap) != cudaSuccess)) {
+        cudaGetLastError();
+        cudaFree(nm);
+        return fail(WG_ENOMEM, "mask pool of %d blocks does not fit", ncap);
+    }
+    if (ctx->mask) {
+        WG_CUDA_OK(cudaMemcpyAsync(nm, ctx->mask, sizeof(double) * 6 * ni * (size_t)ctx->mask_cap,
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+        if (df)
+            WG_CUDA_OK(cudaMemcpyAsync(nmd, ctx->mask_df, sizeof(float2) * 5 * ni * (size_t)ctx->mask_cap,
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        cudaFree(ctx->mask);
+        cudaFree(ctx->mask_df);
+    }
+    for (int i = ncap - 1; i >= ctx->mask_cap; i--) ctx->mask_free.push_back(i);
+    ctx->mask = nm;
+    ctx->mask_df = nmd;
+    ctx->mask_cap = ncap;
+    return WG_OK;
+}
+
 int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const double *mask) {
     Tree *t = get_tree(ctx, tree);
     if (!t || n < 0 || (n && (!blocks || !mask))) return fail(WG_EINVAL, "bad arguments");
@@ -1266,33 +1300,9 @@ int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const do
             packed.insert(packed.end(), blk.begin(), blk.end());
         }
     }
-    const int in_use = ctx->mask_cap - (int)ctx->mask_free.size();
-    const int want = in_use + (int)need.size();
-    if (want > ctx->mask_cap) {
-        const int ncap = std::max(want, ctx->mask_cap * 2);
-        double *nm = nullptr;
-        float2 *nmd = nullptr;
-        const bool df = ctx->precision == WG_RHS_FP32;
-        if (cudaMalloc(&nm, sizeof(double) * 6 * ni * (size_t)ncap) != cudaSuccess ||
-            (df && cudaMalloc(&nmd, sizeof(float2) * 5 * ni * (size_t)ncap) != cudaSuccess)) {
-            cudaGetLastError();
-            cudaFree(nm);
-            return fail(WG_ENOMEM, "mask pool of %d blocks does not fit", ncap);
-        }
-        if (ctx->mask) {
-            WG_CUDA_OK(cudaMemcpyAsync(nm, ctx->mask, sizeof(double) * 6 * ni * (size_t)ctx->mask_cap,
-                                       cudaMemcpyDeviceToDevice, ctx->stream));
-            if (df)
-                WG_CUDA_OK(cudaMemcpyAsync(nmd, ctx->mask_df, sizeof(float2) * 5 * ni * (size_t)ctx->mask_cap,
-                                           cudaMemcpyDeviceToDevice, ctx->stream));
-            WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
-            cudaFree(ctx->mask);
-            cudaFree(ctx->mask_df);
-        }
-        for (int i = ncap - 1; i >= ctx->mask_cap; i--) ctx->mask_free.push_back(i);
-        ctx->mask = nm;
-        ctx->mask_df = nmd;
-        ctx->mask_cap = ncap;
+    {
+        const int st = grow_mask_pool(ctx, (int)need.size());
+        if (st) return st;
     }
     // double-float copy for the FP32-pipe stage: chi/C_eta (colour 0 -> 0),
     // u_s (three words, the third zero in 2D), sponge/C_sponge
@@ -1340,6 +1350,113 @@ int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
     std::vector<int> ids(t->forest.size());
     for (size_t i = 0; i < ids.size(); i++) ids[i] = (int)i;
     return wg_set_mask_sparse(ctx, tree, (int)ids.size(), ids.data(), host_mask);
+}
+
+// mask of a fixed sphere computed on the device: the blocks whose ghosted
+// box comes within radius + h + 3 max(dx) of the centre are candidates,
+// those with chi > 0 at an interior point get a mask slot (the selection of
+// the workloads' host mask, create_mask.f90:58-61 -> draw_sphere)
+int wg_set_mask_sphere(wg_ctx *ctx, int tree, const double *centre, double radius, double c_smooth) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !centre || !(radius > 0.0) || !(c_smooth > 0.0)) return fail(WG_EINVAL, "bad arguments");
+    if (ctx->cfg.dim != 3) return fail(WG_ENOTSUP, "sphere mask needs a 3-D context");
+    cudaStreamSynchronize(ctx->stream);
+    for (int &m : t->mask_slot) {
+        if (m >= 0) ctx->mask_free.push_back(m);
+        m = -1;
+    }
+    const wg_config &c = t->cfg;
+    const int g = ctx->cfg.g;
+    const int *Bs = ctx->cfg.Bs;
+    SphereArgs a;
+    double dx_min = 0.0;
+    for (int d = 0; d < 3; d++) {
+        a.centre[d] = centre[d];
+        a.domain[d] = c.domain[d];
+        a.Bs[d] = Bs[d];
+        const double v = std::ldexp(1.0, -c.Jmax) * c.domain[d] / Bs[d];
+        dx_min = d == 0 ? v : std::min(dx_min, v);
+    }
+    a.radius = radius;
+    a.h = c_smooth * dx_min;
+    // candidates by the distance of the ghosted block box to the centre
+    std::vector<int4> cand;
+    std::vector<int> cblk;
+    const int nb = t->forest.size();
+    for (int b = 0; b < nb; b++) {
+        const int lv = t->forest.level[b];
+        double d2 = 0.0, dxmax = 0.0;
+        for (int d = 0; d < 3; d++) {
+            const double dx = std::ldexp(1.0, -lv) * c.domain[d] / Bs[d];
+            const double x0 = (double)(t->forest.coords[3 * b + d] * Bs[d]) * dx;
+            const double lo = x0 - g * dx, hi = x0 + (Bs[d] + g) * dx;
+            const double e = std::max({lo - centre[d], 0.0, centre[d] - hi});
+            d2 += e * e;
+            dxmax = std::max(dxmax, dx);
+        }
+        if (std::sqrt(d2) > radius + a.h + 3.0 * dxmax) continue;
+        cand.push_back(make_int4(lv, t->forest.coords[3 * b], t->forest.coords[3 * b + 1], t->forest.coords[3 * b + 2]));
+        cblk.push_back(b);
+    }
+    std::vector<int> need;
+    std::vector<int4> ncand;
+    if (!cand.empty()) {
+        DevArray<int4> d_cand;
+        DevArray<int> d_flags;
+        std::vector<int> flags(cand.size(), 0);
+        cudaError_t e = d_cand.upload(cand.data(), cand.size(), ctx->stream);
+        if (e == cudaSuccess) e = d_flags.upload(nullptr, cand.size(), ctx->stream);
+        if (e == cudaSuccess) e = launch_sphere_flags(d_cand.p, (int)cand.size(), a, d_flags.p, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(flags.data(), d_flags.p, sizeof(int) * flags.size(), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "wg_set_mask_sphere", __FILE__, __LINE__);
+        for (size_t k = 0; k < cand.size(); k++)
+            if (flags[k]) {
+                need.push_back(cblk[k]);
+                ncand.push_back(cand[k]);
+            }
+    }
+    int st = grow_mask_pool(ctx, (int)need.size());
+    if (st) return st;
+    if (!need.empty()) {
+        std::vector<int> slots(need.size());
+        for (size_t k = 0; k < need.size(); k++) {
+            slots[k] = ctx->mask_free.back();
+            ctx->mask_free.pop_back();
+            t->mask_slot[need[k]] = slots[k];
+        }
+        DevArray<int4> d_cand;
+        DevArray<int> d_slot;
+        cudaError_t e = d_cand.upload(ncand.data(), ncand.size(), ctx->stream);
+        if (e == cudaSuccess) e = d_slot.upload(slots.data(), slots.size(), ctx->stream);
+        if (e == cudaSuccess)
+            e = launch_sphere_fill(d_cand.p, d_slot.p, (int)need.size(), a, ctx->mask,
+                                   ctx->precision == WG_RHS_FP32 ? ctx->mask_df : nullptr, t->tp.C_eta_inv,
+                                   ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "wg_set_mask_sphere", __FILE__, __LINE__);
+    }
+    if ((st = upload_desc(ctx, *t, tree))) return st;
+    if ((st = upload_lists(ctx, *t))) return st;
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    ctx->grid_version++;
+    return WG_OK;
+}
+
+// interior mask of one block (6 * Bs^d doubles, components chi, u_s x3,
+// colour, sponge) for inspection: returns 1 and fills out when the block has
+// a mask, 0 when it has none
+int wg_get_mask_block(wg_ctx *ctx, int tree, int block, double *out) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t || !out || block < 0 || block >= t->forest.size()) return fail(WG_EINVAL, "bad arguments");
+    const int slot = t->mask_slot[block];
+    if (slot < 0) return 0;
+    const long long ni = ctx->nint;
+    WG_CUDA_OK(cudaMemcpyAsync(out, ctx->mask + (size_t)slot * 6 * ni, sizeof(double) * 6 * ni,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+    WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    return 1;
 }
 
 int wg_set_time(wg_ctx *ctx, int tree, double time) {

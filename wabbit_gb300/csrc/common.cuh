@@ -142,6 +142,18 @@ cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_dou
 cudaError_t launch_rhs_only(int variant, int dim, const int *blk, int nblk, const BlockDesc *desc,
                             const TreeParams *tp, const double *in, BufGeo gin, double *rhs, const double *mask,
                             int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s);
+// fixed sphere of the penalisation (3-D): centre, radius, smoothing width,
+// domain and block size
+struct SphereArgs {
+    double centre[3];
+    double radius, h;
+    double domain[3];
+    int Bs[3];
+};
+// cand: (level, x, y, z) of candidate blocks
+cudaError_t launch_sphere_flags(const int4 *cand, int n, const SphereArgs &a, int *flags, cudaStream_t s);
+cudaError_t launch_sphere_fill(const int4 *cand, const int *slot, int n, const SphereArgs &a, double *mask,
+                               float2 *mask_df, double c_eta_inv, cudaStream_t s);
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
                       const int *trees, cudaStream_t s);

@@ -265,4 +265,92 @@ cudaError_t launch_rhs_only(int variant, int dim, const int *blk, int nblk, cons
     return strict::stage(dim, a, nblk, skew, masked, s);
 }
 
+// ---------------------------------------------------------------------------
+// Penalisation mask of a fixed sphere on the device (create_mask_3D_acm
+// 'sphere-fixed' -> draw_sphere, LIB/EQUATION/ACMnew/create_mask.f90:58-61,
+// LIB/EQUATION/insects/module_geometry.f90:49-117; step_cosine4,
+// LIB/HELPER/module_helpers.f90:467-487): chi is the cosine-smoothed step of
+// the signed distance over the width h, colour 1, u_s = 0, no sponge. Block
+// origin, spacing and point coordinates follow get_block_spacing_origin_b
+// (LIB/TREE/module_treelib.f90:96-101) with every product and sum rounded
+// separately, in the same order as the host mask of the workloads.
+
+__device__ __forceinline__ double sphere_chi(const SphereArgs &a, const int4 &blk, int ix, int iy, int iz) {
+    const int lv = blk.x;
+    const int co[3] = {blk.y, blk.z, blk.w};
+    const int ii[3] = {ix, iy, iz};
+    double r2 = 0.0;
+    for (int d = 0; d < 3; d++) {
+        const double dx = __ddiv_rn(__dmul_rn(ldexp(1.0, -lv), a.domain[d]), (double)a.Bs[d]);
+        const double x0 = __dmul_rn((double)(co[d] * a.Bs[d]), dx);
+        const double x = __dadd_rn(x0, __dmul_rn((double)ii[d], dx));
+        const double e = __dsub_rn(x, a.centre[d]);
+        r2 = d == 0 ? __dmul_rn(e, e) : __dadd_rn(r2, __dmul_rn(e, e));
+    }
+    const double dist = __dsub_rn(__dsqrt_rn(r2), a.radius);
+    if (dist <= -a.h) return 1.0;
+    if (dist >= a.h) return 0.0;
+    const double t = __ddiv_rn(__dmul_rn(__dadd_rn(dist, a.h), 3.141592653589793), __dmul_rn(2.0, a.h));
+    return __dmul_rn(0.5, __dadd_rn(1.0, cos(t)));
+}
+
+// flags[k] = 1 if chi > 0 at an interior point of candidate k
+__global__ void __launch_bounds__(256) sphere_flag_kernel(const int4 *cand, int n, SphereArgs a, int *flags) {
+    const int k = blockIdx.x;
+    if (k >= n) return;
+    const int4 blk = cand[k];
+    const int npts = a.Bs[0] * a.Bs[1] * a.Bs[2];
+    int any = 0;
+    for (int i = threadIdx.x; i < npts; i += blockDim.x) {
+        const int ix = i % a.Bs[0], iy = (i / a.Bs[0]) % a.Bs[1], iz = i / (a.Bs[0] * a.Bs[1]);
+        any |= sphere_chi(a, blk, ix, iy, iz) > 0.0;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) flags[k] = any;
+}
+
+// the interior mask of block k into pool slot slot[k]: chi, u_s (3), colour,
+// sponge in FP64, and the double-float words of the FP32-pipe stage
+// (chi / C_eta, u_s, sponge / C_sponge)
+__global__ void __launch_bounds__(256) sphere_fill_kernel(const int4 *cand, const int *slot, int n, SphereArgs a,
+                                                          double *mask, float2 *mask_df, double c_eta_inv) {
+    const int k = blockIdx.x;
+    if (k >= n) return;
+    const int4 blk = cand[k];
+    const long long ni = (long long)a.Bs[0] * a.Bs[1] * a.Bs[2];
+    double *m = mask + (long long)slot[k] * 6 * ni;
+    float2 *md = mask_df ? mask_df + (long long)slot[k] * 5 * ni : nullptr;
+    for (long long i = threadIdx.x; i < ni; i += blockDim.x) {
+        const int ix = (int)(i % a.Bs[0]), iy = (int)((i / a.Bs[0]) % a.Bs[1]), iz = (int)(i / (a.Bs[0] * a.Bs[1]));
+        const double chi = sphere_chi(a, blk, ix, iy, iz);
+        m[i] = chi;
+        m[ni + i] = 0.0;
+        m[2 * ni + i] = 0.0;
+        m[3 * ni + i] = 0.0;
+        m[4 * ni + i] = 1.0;
+        m[5 * ni + i] = 0.0;
+        if (md) {
+            const double v = __dmul_rn(chi, c_eta_inv);
+            const float hi = __double2float_rn(v);
+            md[i] = make_float2(hi, __double2float_rn(__dsub_rn(v, (double)hi)));
+            for (int w = 1; w < 5; w++) md[w * ni + i] = make_float2(0.f, 0.f);
+        }
+    }
+}
+
+cudaError_t launch_sphere_flags(const int4 *cand, int n, const SphereArgs &a, int *flags, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (!cand || !flags) return cudaErrorInvalidValue;
+    sphere_flag_kernel<<<n, 256, 0, s>>>(cand, n, a, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sphere_fill(const int4 *cand, const int *slot, int n, const SphereArgs &a, double *mask,
+                               float2 *mask_df, double c_eta_inv, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (!cand || !slot || !mask) return cudaErrorInvalidValue;
+    sphere_fill_kernel<<<n, 256, 0, s>>>(cand, slot, n, a, mask, mask_df, c_eta_inv);
+    return cudaGetLastError();
+}
+
 }  // namespace wg

@@ -193,6 +193,18 @@ class Forest:
             raise ValueError("mask has the wrong size")
         capi.check(self.L.wg_set_mask_sparse(self.ctx.h, self.tree, len(blocks), _p(blocks, ctypes.c_int), _p(mask)))
 
+    def set_mask_sphere(self, centre, radius, c_smooth=1.5):
+        """Fixed-sphere penalisation mask computed on the device (3-D)."""
+        c = np.ascontiguousarray(centre, np.float64)
+        capi.check(self.L.wg_set_mask_sphere(self.ctx.h, self.tree, _p(c), float(radius), float(c_smooth)))
+
+    def mask_block(self, block):
+        """Interior mask (6, Bz, By, Bx) of a block, or None without one."""
+        Bz = self.cfg.Bs[2] if self.cfg.dim == 3 else 1
+        out = np.zeros((6, Bz, self.cfg.Bs[1], self.cfg.Bs[0]))
+        r = capi.check(self.L.wg_get_mask_block(self.ctx.h, self.tree, int(block), _p(out)))
+        return out if r == 1 else None
+
     def stats(self):
         n, m = ctypes.c_int(), ctypes.c_int()
         capi.check(self.L.wg_tree_stats(self.ctx.h, self.tree, ctypes.byref(n), ctypes.byref(m)))
