@@ -1,5 +1,5 @@
 """Integer-pipe tap products (wabbit_gb300/csrc/exact.cuh) against the host's
-IEEE multiply: the header compiles for the host, and a C++ driver checks
+IEEE multiply: the header compiles for the host, and a C++ program checks
 millions of products (random bit patterns, normal ranges, significands with
 long runs of low zero or one bits for ties and carries) for bit identity, and
 that the fallback flag is raised only at subnormal, special or out-of-range

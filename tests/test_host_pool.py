@@ -1,5 +1,5 @@
 """The host thread pool of the planning code (wabbit_gb300/csrc/par.hpp):
-a C++ driver checks that every index of thousands of jobs runs exactly once,
+a C++ program checks that every index of thousands of jobs runs exactly once,
 that nested calls run inline, that callers on several threads take turns and
 that a forked child gets a working pool."""
 import os

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "..", "wabbit_gb300", "csrc")
 
 
 @pytest.fixture(scope="module")
-def driver(tmp_path_factory):
+def checker(tmp_path_factory):
     cxx = shutil.which("g++") or shutil.which("c++")
     if not cxx:
         pytest.skip("no host C++ compiler")
@@ -29,12 +29,12 @@ def driver(tmp_path_factory):
 
 
 @pytest.mark.parametrize("dim,jmin,jmax,seed", [(2, 2, 5, 1), (2, 2, 7, 33), (3, 1, 3, 2), (3, 2, 5, 4)])
-def test_lifted_neighbour_lists(driver, tmp_path, dim, jmin, jmax, seed):
+def test_lifted_neighbour_lists(checker, tmp_path, dim, jmin, jmax, seed):
     lv, co = grids.random_graded(dim, jmin, jmax, seed=seed, frac=0.45)
     path = tmp_path / "grid.txt"
     with open(path, "w") as f:
         f.write(f"{dim} {len(lv)}\n")
         for l, c in zip(lv, co):
             f.write(f"{l} {c[0]} {c[1]} {c[2] if len(c) > 2 else 0}\n")
-    r = subprocess.run([driver, str(path), str(jmin), str(jmax)], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([checker, str(path), str(jmin), str(jmax)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and "neighbour mismatches 0" in r.stdout, r.stdout + r.stderr
