@@ -81,8 +81,43 @@ typedef struct wg_config {
     int    threshold_state_vector_component[8];
     /* GB300 build options */
     int    rhs_precision;       /* WG_RHS_FP64 or WG_RHS_FP32                  */
-    int    reserved[14];
+    /* [Blocks] threshold_mask: blocks whose penalisation mask has an
+     * interface stay (coarseningIndicatorMask_tree,
+     * LIB/MESH/coarseningIndicator_tree.f90:333-420); needs a geometry
+     * (wg_set_geometry) */
+    int    threshold_mask;
+    /* [Blocks] force_maxlevel_dealiasing: blocks on Jmax are flagged for
+     * coarsening (coarseningIndicator_tree.f90:287-293) */
+    int    force_maxlevel_dealiasing;
+    int    reserved[12];
 } wg_config;
+
+/*
+ * Penalisation geometry of a tree: what the physics module draws in
+ * createMask_tree -> CREATE_MASK_meta -> create_mask_2D_acm /
+ * create_mask_3D_acm (LIB/MESH/createMask_tree.f90,
+ * LIB/EQUATION/module_physics_metamodule.f90:38-83,
+ * LIB/EQUATION/ACMnew/create_mask.f90:6-320) with the "all-parts" stage:
+ * mask = 0 and colour = 1 everywhere, then the obstacle's chi (cosine step of
+ * the signed distance over h = C_smooth * dx_min at Jmax,
+ * module_ACM.f90:468-471) with colour 1, then, with use_sponge, the sponge
+ * (LIB/EQUATION/ACMnew/sponge.f90). Keys in brackets are the .ini keys.
+ */
+#define WG_GEOM_NONE     0
+#define WG_GEOM_CYLINDER 1   /* 2-D 'cylinder'/'circle' (draw_circle)         */
+#define WG_GEOM_SPHERE   2   /* 3-D 'sphere-fixed' (draw_sphere)              */
+#define WG_SPONGE_RECT   0   /* [Sponge] sponge_type=rect                     */
+#define WG_SPONGE_PNORM  1   /* [Sponge] sponge_type=p-norm                   */
+typedef struct wg_geometry {
+    int    kind;                /* WG_GEOM_*  ([VPM] geometry)                 */
+    int    sponge_type;         /* WG_SPONGE_*                                  */
+    double x_cntr[3];           /* [VPM] x_cntr                                 */
+    double R_cyl;               /* [VPM] R_cyl                                  */
+    double C_smooth;            /* [VPM] C_smooth (default 1.5)                 */
+    double L_sponge;            /* [Sponge] L_sponge                            */
+    double p_sponge;            /* [Sponge] p_sponge (default 20)               */
+    int    reserved[8];
+} wg_geometry;
 
 typedef struct wg_ctx wg_ctx;
 
@@ -162,6 +197,17 @@ int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const do
  * of the signed distance over h = c_smooth * dx at Jmax, colour 1, u_s = 0;
  * only blocks with chi > 0 at an interior point keep a mask. */
 int wg_set_mask_sphere(wg_ctx *ctx, int tree, const double *centre, double radius, double c_smooth);
+/* Penalisation geometry of a tree (see wg_geometry); NULL removes it. The
+ * tree then draws its masks itself, as the reference's createMask_tree does
+ * in every RHS and adaptation: now, and after every grid change
+ * (wg_set_grid, wg_refine_everywhere, wg_adapt), on the host from the
+ * block geometry, keeping device copies only for blocks with a non-zero
+ * chi or sponge word. The same geometry supplies wg_adapt's threshold_mask
+ * test. wg_set_mask, wg_set_mask_sparse and wg_set_mask_sphere replace it
+ * by the caller's masks. Replaces createMask_tree
+ * (LIB/MESH/createMask_tree.f90:1-136) for 'cylinder' (2-D) and
+ * 'sphere-fixed' (3-D) with the 'rect' and 'p-norm' sponges. */
+int wg_set_geometry(wg_ctx *ctx, int tree, const wg_geometry *geo);
 /* Interior mask of one block (6 * Bs^d doubles) for inspection: returns 1
  * and fills out if the block has a mask, 0 if it has none. */
 int wg_get_mask_block(wg_ctx *ctx, int tree, int block, double *out);
@@ -173,10 +219,14 @@ int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);
  * ancestor down to Jmin, mothers filled with their daughters' scaling
  * coefficients (sync_D2M), coarsening indicator on every block
  * (WG_ADAPT_THRESHOLD: threshold-state-vector with eps_use = eps * norm per
- * component; WG_ADAPT_EVERYWHERE: every leaf), respectJmaxJmin, completeness,
+ * component; eps_use NULL takes cfg.eps, times the leaves' Linfty norm per
+ * component with eps_normalized as componentWiseNorm_tree gives it;
+ * WG_ADAPT_EVERYWHERE: every leaf), force_maxlevel_dealiasing and
+ * threshold_mask as configured, respectJmaxJmin, completeness,
  * gradedness (ensureGradedness_tree with check_daughters), deletion and
  * pruning; the grid and the state are replaced, *nblk_out receives the new
- * block count (wg_get_grid returns the new grid). Masks are dropped. Needs
+ * block count (wg_get_grid returns the new grid). Masks are redrawn from the
+ * tree's geometry (wg_set_geometry), else dropped. Needs
  * free arena slots for the mothers (about nblk/(2^d-1)).
  * Unlifted wavelets (CDF X0): the original values are kept (decimation).
  * Lifted wavelets (CDF XY): the reference's coarse-extension algorithm --

@@ -61,6 +61,11 @@ def lib():
         L.or_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _dp]
         L.or_adapt_full_tree.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.or_run.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+        L.or_set_geometry.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.or_make_mask.argtypes = [ctypes.c_void_p]
+        L.or_get_mask.argtypes = [ctypes.c_void_p, _dp]
+        L.or_mask_status.argtypes = [ctypes.c_void_p, _ip]
+        L.or_norm.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp]
         _lib = L
     return _lib
 
@@ -127,6 +132,42 @@ class Oracle:
         else:
             mask = np.ascontiguousarray(mask, np.float64)
             self.L.or_set_mask(self.h, _p(mask))
+
+    def set_geometry(self, geo):
+        """Penalisation geometry (a WgGeometry) the masks are drawn from."""
+        self.geo = geo
+        self.L.or_set_geometry(self.h, ctypes.byref(geo) if geo is not None else None)
+
+    def make_mask(self):
+        """createMask_tree on the current grid (needs a geometry)."""
+        self.L.or_make_mask(self.h)
+
+    def mask(self):
+        """The forest's masks (Nb, 6, nz, ny, nx), or None."""
+        c = self.cfg
+        out = np.zeros((self.nblocks, 6, c.nz, c.Bs[1] + 2 * c.g, c.nx))
+        return out if self.L.or_get_mask(self.h, _p(out)) == 1 else None
+
+    def mask_status(self):
+        out = np.zeros(self.nblocks, np.int32)
+        self.L.or_mask_status(self.h, _p(out, ctypes.c_int))
+        return out
+
+    def norm(self, which="Linfty"):
+        """componentWiseNorm_tree over the leaves (per component)."""
+        out = np.zeros(self.cfg.neq)
+        self.L.or_norm(self.h, 0 if which == "Linfty" else 1, _p(out))
+        return out
+
+    def eps_use(self):
+        """eps * norm per component as adapt_tree applies it with
+        eps_normalized (norm <= 1e-9 is replaced by 1,
+        coarseningIndicator_tree.f90:150-152), or eps without it."""
+        if not self.cfg.eps_normalized:
+            return np.full(self.cfg.neq, self.cfg.eps)
+        n = self.norm("Linfty")
+        n[n <= 1.0e-9] = 1.0
+        return self.cfg.eps * n
 
     def neighbors(self):
         out = np.zeros((self.nblocks, 168), np.int32)

@@ -145,6 +145,8 @@ struct Oracle {
     // RK registers: slot 0 = u_n, 1..4 = k1..k4 (full blocks, as hvy_work)
     std::vector<double> work;
     int nthreads = 1;
+    // penalisation geometry (createMask_tree); kind WG_GEOM_NONE = none
+    wg_geometry geom{};
 
     double *blk(int b) { return data.data() + size_t(b) * nc * npts; }
     const double *blk(int b) const { return data.data() + size_t(b) * nc * npts; }
@@ -690,6 +692,177 @@ static void block_spacing(const Oracle &o, int b, double x0[3], double dx[3]) {
     for (int d = 0; d < o.cfg.dim; d++) {
         dx[d] = std::pow(2.0, -B.level) * o.cfg.domain[d] / (double)o.cfg.Bs[d];
         x0[d] = (double)(B.c[d] * o.cfg.Bs[d]) * dx[d];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Penalisation mask of one block from the tree's geometry: CREATE_MASK_meta
+// (LIB/EQUATION/module_physics_metamodule.f90:38-83, mask = 0, colour = 1)
+// -> create_mask_2D_acm / create_mask_3D_acm "all-parts"
+// (LIB/EQUATION/ACMnew/create_mask.f90:6-320): draw_circle / draw_sphere
+// (LIB/EQUATION/insects/module_geometry.f90:49-117,315-381) with the cosine
+// step (step_cosine4, LIB/HELPER/module_helpers.f90:467-487) of width
+// h = C_smooth * dx_min(Jmax) and safety h (module_ACM.f90:468-471), then the
+// sponge (sponge_2D / sponge_3D, LIB/EQUATION/ACMnew/sponge.f90) on the
+// interior. m: 6 components of the full block (at(ix,iy,iz,ic)).
+// ---------------------------------------------------------------------------
+static const double kPi = 4.0 * std::atan(1.0);
+
+static double step_cosine(double x, double t, double h) {
+    const double x_rel = x - t;
+    if (x_rel <= -h) return 1.0;
+    if (x_rel >= +h) return 0.0;
+    return 0.5 * (1.0 + std::cos((x_rel + h) * kPi / (2.0 * h)));
+}
+
+static void mask_block(const Oracle &o, int b, double *m) {
+    const wg_config &p = o.cfg;
+    const wg_geometry &G = o.geom;
+    const int g = p.g, dim = p.dim;
+    std::fill(m, m + 6 * size_t(o.npts), 0.0);
+    for (size_t q = 0; q < size_t(o.npts); q++) m[4 * size_t(o.npts) + q] = 1.0;
+    if (!p.penalization) return;
+    double x0[3], dx[3];
+    block_spacing(o, b, x0, dx);
+    double dx_min = 9e9;
+    for (int d = 0; d < dim; d++) dx_min = std::min(dx_min, std::pow(2.0, -p.Jmax) * (p.domain[d] / (double)p.Bs[d]));
+    const double h = dx_min * G.C_smooth, safety = 1.0 * h;
+    if (G.kind == WG_GEOM_CYLINDER || G.kind == WG_GEOM_SPHERE) {
+        double dmin = dx[0];
+        for (int d = 1; d < dim; d++) dmin = std::min(dmin, dx[d]);
+        const int Nsafety = (int)std::ceil(safety / dmin);
+        const int n[3] = {o.nx, o.ny, o.nz};
+        int lo[3] = {1, 1, 1}, hi[3] = {1, 1, 1};
+        for (int d = 0; d < dim; d++) {
+            const int bmin = (int)((G.x_cntr[d] - G.R_cyl - x0[d]) / dx[d]) - Nsafety + (g + 1);
+            const int bmax = (int)std::ceil((G.x_cntr[d] + G.R_cyl - x0[d]) / dx[d]) + Nsafety + (g + 1);
+            lo[d] = std::max(bmin, g + 1);
+            hi[d] = std::min(bmax, n[d] - g + 1);
+        }
+        for (int iz = lo[2]; iz <= hi[2]; iz++)
+            for (int iy = lo[1]; iy <= hi[1]; iy++)
+                for (int ix = lo[0]; ix <= hi[0]; ix++) {
+                    const double xx = (double)(ix - (g + 1)) * dx[0] + x0[0];
+                    const double yy = (double)(iy - (g + 1)) * dx[1] + x0[1];
+                    double dist;
+                    if (dim == 2) {
+                        const double a = xx - G.x_cntr[0], c = yy - G.x_cntr[1];
+                        dist = std::sqrt(a * a + c * c) - G.R_cyl;
+                    } else {
+                        const double zz = (double)(iz - (g + 1)) * dx[2] + x0[2];
+                        const double a = xx - G.x_cntr[0], c = yy - G.x_cntr[1], e = zz - G.x_cntr[2];
+                        dist = std::sqrt(a * a + c * c + e * e) - G.R_cyl;
+                    }
+                    const double tmp = step_cosine(dist, 0.0, h);
+                    double &chi = m[o.at(ix, iy, iz, 1)];
+                    if (tmp >= chi) {
+                        chi = tmp;
+                        m[o.at(ix, iy, iz, 5)] = 1.0;
+                    }
+                }
+    }
+    if (!p.use_sponge) return;
+    const double Ls = G.L_sponge;
+    const int z1 = dim == 3 ? g + 1 : 1, z2 = dim == 3 ? p.Bs[2] + g : 1;
+    if (dim == 2) {
+        for (int iy = g + 1; iy <= p.Bs[1] + g; iy++)
+            for (int ix = g + 1; ix <= p.Bs[0] + g; ix++) {
+                double tmp;
+                if (G.sponge_type == WG_SPONGE_RECT) {
+                    const double x = (double)(ix - (g + 1)) * dx[0] + x0[0];
+                    const double y = (double)(iy - (g + 1)) * dx[1] + x0[1];
+                    tmp = std::min(std::min(x, y), std::min(-(x - p.domain[0]), -(y - p.domain[1])));
+                } else {
+                    const double off = 0.5 * p.domain[0];
+                    const double y = (double)(iy - (g + 1)) * dx[1] + x0[1] - off;
+                    const double x = (double)(ix - (g + 1)) * dx[0] + x0[0] - off;
+                    tmp = -(std::pow(std::pow(x, G.p_sponge) + std::pow(y, G.p_sponge), 1.0 / G.p_sponge) - off);
+                }
+                m[o.at(ix, iy, 1, 6)] = step_cosine(tmp, 0.5 * Ls, 0.5 * Ls);
+            }
+        return;
+    }
+    if (G.sponge_type == WG_SPONGE_RECT) {
+        double t = 9e99;
+        for (int d = 0; d < 3; d++) t = std::min(t, x0[d]);
+        for (int d = 0; d < 3; d++) t = std::min(t, p.domain[d] - (x0[d] + dx[d] * (double)p.Bs[d]));
+        if (t > Ls) return;
+    } else {
+        const double off = 0.5 * p.domain[0], pp = G.p_sponge, pinv = 1.0 / pp;
+        double e[3];
+        for (int d = 0; d < 3; d++)
+            e[d] = std::pow(std::max(std::fabs(x0[d] - off), std::fabs(x0[d] + dx[d] * (double)p.Bs[d] - off)), pp);
+        if (off - std::pow(e[0] + e[1] + e[2], pinv) > Ls) return;
+    }
+    for (int iz = z1; iz <= z2; iz++)
+        for (int iy = g + 1; iy <= p.Bs[1] + g; iy++)
+            for (int ix = g + 1; ix <= p.Bs[0] + g; ix++) {
+                double tmp;
+                if (G.sponge_type == WG_SPONGE_RECT) {
+                    const double z = (double)(iz - (g + 1)) * dx[2] + x0[2];
+                    const double y = (double)(iy - (g + 1)) * dx[1] + x0[1];
+                    const double x = (double)(ix - (g + 1)) * dx[0] + x0[0];
+                    const double v[6] = {x, y, z, -(x - p.domain[0]), -(y - p.domain[1]), -(z - p.domain[2])};
+                    tmp = v[0];
+                    for (int k = 1; k < 6; k++) tmp = std::min(tmp, v[k]);
+                } else {
+                    const double off = 0.5 * p.domain[0], pp = G.p_sponge, pinv = 1.0 / pp;
+                    const double z = std::pow((double)(iz - (g + 1)) * dx[2] + x0[2] - off, pp);
+                    const double y = std::pow((double)(iy - (g + 1)) * dx[1] + x0[1] - off, pp);
+                    const double x = std::pow((double)(ix - (g + 1)) * dx[0] + x0[0] - off, pp);
+                    tmp = -(std::pow(x + y + z, pinv) - off);
+                }
+                m[o.at(ix, iy, iz, 6)] = step_cosine(tmp, 0.5 * Ls, 0.5 * Ls);
+            }
+}
+
+// masks of every block of the current grid (createMask_tree with
+// dont_use_pruned_tree_mask / 2-D: createCompleteMaskDirect_tree,
+// LIB/MESH/createMask_tree.f90:118-136)
+static void make_masks(Oracle &o) {
+    if (o.geom.kind == WG_GEOM_NONE || !o.cfg.penalization) {
+        o.mask.clear();
+        return;
+    }
+    o.mask.assign(o.blocks.size() * 6 * size_t(o.npts), 0.0);
+    for (size_t b = 0; b < o.blocks.size(); b++) mask_block(o, (int)b, o.mask.data() + b * 6 * o.npts);
+}
+
+// coarseningIndicatorMask_tree (LIB/MESH/coarseningIndicator_tree.f90:
+// 333-420) for one block: 0 (stay) where chi has an interface point in the
+// interior or is not constant there, else -1
+static int mask_status(const Oracle &o, int b) {
+    std::vector<double> m(6 * size_t(o.npts));
+    mask_block(o, b, m.data());
+    const wg_config &p = o.cfg;
+    const int g = p.g;
+    const int z1 = p.dim == 3 ? g + 1 : 1, z2 = p.dim == 3 ? p.Bs[2] + g : 1;
+    bool iface = false;
+    double mx = -HUGE_VAL, mn = HUGE_VAL;
+    for (int iz = z1; iz <= z2; iz++)
+        for (int iy = g + 1; iy <= p.Bs[1] + g; iy++)
+            for (int ix = g + 1; ix <= p.Bs[0] + g; ix++) {
+                const double c = m[o.at(ix, iy, iz, 1)];
+                if (c > 1.0e-12 && c < 1.0 - 1.0e-12) iface = true;
+                mx = std::max(mx, c);
+                mn = std::min(mn, c);
+            }
+    if (iface || (mx - mn) > 1.0e-12) return 0;
+    return -1;
+}
+
+// the two indicator switches of coarseningIndicator_tree on a flag array
+// whose entries came from the block indicator: force_maxlevel_dealiasing
+// (Jmax blocks -1, :287-293) and threshold_mask (max with the mask status)
+static void indicator_switches(const Oracle &o, int nt, int *flags) {
+    const wg_config &p = o.cfg;
+    for (int b = 0; b < nt; b++) {
+        if (p.force_maxlevel_dealiasing && o.blocks[b].level == p.Jmax) {
+            flags[b] = -1;
+            continue;
+        }
+        if (p.threshold_mask && o.geom.kind != WG_GEOM_NONE && p.penalization)
+            flags[b] = std::max(flags[b], mask_status(o, b));
     }
 }
 
@@ -1258,6 +1431,7 @@ static int adapt_unlifted(Oracle &o, const double *eps_use, int everywhere) {
     }
     (void)zlo;
     (void)zhi;
+    if (!everywhere) indicator_switches(o, nt, flags.data());
     // respectJmaxJmin_tree
     const int STAY = 9;
     for (int i = 0; i < nt; i++)
@@ -1933,6 +2107,7 @@ static int adapt_lifted(Oracle &o, const double *eps_use, int everywhere) {
             o.ref[b] = threshold_wd(o, b, eps_use);
         }
     }
+    if (!everywhere) indicator_switches(o, nt, o.ref.data());
     if (!everywhere && use_ce) security_zone(o, eps_use);
     // respectJmaxJmin_tree and ensureGradedness_tree (check_daughters)
     for (int b = 0; b < nt; b++)
@@ -2279,6 +2454,75 @@ int or_filter(void *h, int which, int *lo, int *hi, double *coef) {
     *lo = f->lo;
     *hi = f->hi;
     if (coef) std::memcpy(coef, f->c.data(), f->c.size() * sizeof(double));
+    return WG_OK;
+}
+
+// penalisation geometry of the forest (NULL: none); masks are built by
+// or_make_mask on the current grid and used by the RHS
+int or_set_geometry(void *h, const wg_geometry *geo) {
+    Oracle &o = *(Oracle *)h;
+    if (geo) o.geom = *geo;
+    else o.geom = wg_geometry{};
+    o.mask.clear();
+    return WG_OK;
+}
+
+int or_make_mask(void *h) {
+    make_masks(*(Oracle *)h);
+    return WG_OK;
+}
+
+// the forest's masks (nblk * 6 * npts doubles); 0 if it has none
+int or_get_mask(void *h, double *out) {
+    Oracle &o = *(Oracle *)h;
+    if (o.mask.empty()) return 0;
+    std::memcpy(out, o.mask.data(), o.mask.size() * sizeof(double));
+    return 1;
+}
+
+// mask status of every block (coarseningIndicatorMask_tree's test)
+int or_mask_status(void *h, int *out) {
+    Oracle &o = *(Oracle *)h;
+    for (size_t b = 0; b < o.blocks.size(); b++) out[b] = mask_status(o, (int)b);
+    return WG_OK;
+}
+
+// componentWiseNorm_tree (LIB/OPERATORS/componentWiseNorm_tree.f90:1-140)
+// over the leaves' interiors: which 0 = Linfty (max |u|, -1 for components
+// the indicator skips), 1 = L2 (sqrt of sum u^2 dV)
+int or_norm(void *h, int which, double *norm) {
+    Oracle &o = *(Oracle *)h;
+    const wg_config &p = o.cfg;
+    const int g = p.g;
+    const int z1 = p.dim == 3 ? g + 1 : 1, z2 = p.dim == 3 ? p.Bs[2] + g : 1;
+    for (int c = 0; c < o.nc; c++) norm[c] = which == 0 ? -1.0 : 0.0;
+    for (size_t b = 0; b < o.blocks.size(); b++) {
+        double x0[3], dx[3];
+        block_spacing(o, (int)b, x0, dx);
+        double dV = 1.0;
+        for (int d = 0; d < p.dim; d++) dV *= dx[d];
+        for (int c = 1; c <= o.nc; c++) {
+            if (p.threshold_state_vector_component[c - 1] != 1) continue;
+            double acc = which == 0 ? 0.0 : 0.0;
+            bool first = true;
+            for (int iz = z1; iz <= z2; iz++)
+                for (int iy = g + 1; iy <= p.Bs[1] + g; iy++)
+                    for (int ix = g + 1; ix <= p.Bs[0] + g; ix++) {
+                        const double v = o.blk((int)b)[o.at(ix, iy, iz, c)];
+                        if (which == 0) {
+                            const double a = std::fabs(v);
+                            if (first || a > acc) acc = a;
+                            first = false;
+                        } else {
+                            acc += v * v;
+                        }
+                    }
+            if (which == 0) norm[c - 1] = std::max(norm[c - 1], acc);
+            else norm[c - 1] += dV * acc;
+        }
+    }
+    if (which == 1)
+        for (int c = 0; c < o.nc; c++) norm[c] = std::sqrt(norm[c]);
     return WG_OK;
 }
 

@@ -21,6 +21,13 @@ compare against them:
   (112 blocks, levels 2-5, Bs=32), the reference's refine-everywhere result
   with CDF40 (448 blocks) and its coarsen-everywhere results with CDF40 and
   CDF44.
+* acm_cyl.npz -- TESTING/acm/acm_CDF40 and acm_CDF44: 2-D ACM flow past a
+  cylinder (convective FD_4th_central, penalisation with cosine smoothing,
+  p-norm sponge, adaptation every step with mask thresholding and max-level
+  dealiasing, Bs=26, Jmax=6): the text of acm_cyl.ini, the state at t=0
+  (input), 0.05 and 0.1 (outputs) with their iteration counts, and the
+  saved mask (chi) on the t=0, 0.05 and 0.1 grids. Each case is stored under
+  the prefix "CDF40_" / "CDF44_".
 
 Block data are stored as interiors only, shape (Nb, ncomp, [Bs,] Bs, Bs),
 x fastest; block geometry as level (Nb,) and integer coords (Nb, 3).
@@ -120,11 +127,32 @@ def wavelets(ref):
     np.savez_compressed(os.path.join(HERE, "wavelet_adaptive.npz"), **out)
 
 
+def acm_cyl(ref):
+    out = {}
+    for w in ["CDF40", "CDF44"]:
+        folder = os.path.join(ref, "TESTING/acm", f"acm_{w}")
+        with open(os.path.join(folder, "acm_cyl.ini"), errors="ignore") as f:
+            out[f"{w}_ini"] = np.array(f.read())
+        for tag, key in [("000000000000", "t0"), ("000000050000", "t1"), ("000000100000", "t2")]:
+            d, u = _fields(folder, ["ux", "uy", "p"], tag)
+            lv, c, u = _sorted(d, u)
+            dm = read_wabbit(os.path.join(folder, f"mask_{tag}.h5"))
+            lvm, cm, m = _sorted(dm, _interior(dm)[:, None])
+            assert np.array_equal(lv, lvm) and np.array_equal(c, cm)
+            out.update({f"{w}_{key}_level": lv, f"{w}_{key}_coords": c, f"{w}_{key}_u": u,
+                        f"{w}_{key}_chi": m[:, 0], f"{w}_{key}_time": d["time"],
+                        f"{w}_{key}_iteration": d["iteration"]})
+    np.savez_compressed(os.path.join(HERE, "acm_cyl.npz"), **out)
+
+
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_fixtures.py <path of the reference checkout>")
+    ref = sys.argv[1]
     vortex2d(ref)
     tg3d(ref)
     wavelets(ref)
+    acm_cyl(ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -20,6 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 UNITS = {
     "forest.cpp": [],
+    "geometry.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "adapt.cpp": [],
     "lifted.cpp": [],
     "k_lifted.cu": ["-fmad=false"],

@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes
 import os
 
-from .config import WgConfig
+from .config import WgConfig, WgGeometry
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libwabbit_gb300.so")
@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libwabbit_gb300.so")
 WG_OK = 0
 ERRORS = {-1: "WG_EINVAL", -2: "WG_ENOMEM", -3: "WG_ECUDA", -4: "WG_EDIVERGED", -5: "WG_ETIMEOUT",
           -6: "WG_EGRID", -7: "WG_ENOTSUP"}
+ERRORS_BY_NAME = {v: k for k, v in ERRORS.items()}
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = [
@@ -29,7 +30,7 @@ EXPORTS = [
     "wg_upload_interior", "wg_download_interior", "wg_graph_kernels",
     "wg_threshold_flags_noalloc", "wg_set_stage_form", "wg_get_stage_form",
     "wg_wavelet_decompose", "wg_wavelet_reconstruct", "wg_wavelet_threshold", "wg_threshold_flags_wd",
-    "wg_adapt", "wg_adapt_profile", "wg_rk4_stream",
+    "wg_adapt", "wg_adapt_profile", "wg_rk4_stream", "wg_set_geometry",
 ]
 
 
@@ -92,6 +93,7 @@ _SIGS = {
     "wg_download_interior": (_i, [_vp, _i, _dp]),
     "wg_graph_kernels": (_i, [_vp]),
     "wg_threshold_flags_noalloc": (_i, [ctypes.POINTER(WgConfig), _i, _vp, _dp, _vp, _vp, _vp]),
+    "wg_set_geometry": (_i, [_vp, _i, ctypes.POINTER(WgGeometry)]),
 }
 
 _lib = None

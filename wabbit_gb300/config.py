@@ -45,7 +45,9 @@ class WgConfig(ctypes.Structure):
         ("eps_normalized", ctypes.c_int),
         ("threshold_state_vector_component", ctypes.c_int * 8),
         ("rhs_precision", ctypes.c_int),
-        ("reserved", ctypes.c_int * 14),
+        ("threshold_mask", ctypes.c_int),
+        ("force_maxlevel_dealiasing", ctypes.c_int),
+        ("reserved", ctypes.c_int * 12),
     ]
 
     def copy(self) -> "WgConfig":
@@ -64,6 +66,25 @@ class WgConfig(ctypes.Structure):
     @property
     def npts(self) -> int:
         return self.nx * (self.Bs[1] + 2 * self.g) * self.nz
+
+
+class WgGeometry(ctypes.Structure):
+    """ctypes mirror of ``wg_geometry`` (the penalisation geometry a tree's
+    masks are drawn from)."""
+    _fields_ = [
+        ("kind", ctypes.c_int),
+        ("sponge_type", ctypes.c_int),
+        ("x_cntr", ctypes.c_double * 3),
+        ("R_cyl", ctypes.c_double),
+        ("C_smooth", ctypes.c_double),
+        ("L_sponge", ctypes.c_double),
+        ("p_sponge", ctypes.c_double),
+        ("reserved", ctypes.c_int * 8),
+    ]
+
+
+GEOM_NONE, GEOM_CYLINDER, GEOM_SPHERE = 0, 1, 2
+SPONGE_RECT, SPONGE_PNORM = 0, 1
 
 
 # wavelet -> default number of ghost nodes g and the RHS ghost width g_rhs
@@ -132,7 +153,12 @@ def _num(v: str) -> list[float]:
 def from_ini(path: str) -> WgConfig:
     """Read the hot-path keys of a WABBIT .ini file into a WgConfig."""
     with open(path, errors="ignore") as f:
-        kv = _parse_ini(f.read())
+        return from_ini_text(f.read())
+
+
+def from_ini_text(text: str) -> WgConfig:
+    """The hot-path keys of a WABBIT .ini file's text as a WgConfig."""
+    kv = _parse_ini(text)
 
     def get(sec, key, default=None):
         v = kv.get((sec, key), "")
@@ -187,4 +213,44 @@ def from_ini(path: str) -> WgConfig:
         c.write_time = float(get("Time", "write_time", 1.0))
     ts = get("Statistics", "tsave_stats")
     c.tsave_stats = float(ts) if ts else 0.0
+    c.threshold_mask = int(float(get("Blocks", "threshold_mask", 0)))
+    c.force_maxlevel_dealiasing = int(float(get("Blocks", "force_maxlevel_dealiasing", 0)))
     return c
+
+
+def geometry_from_ini(path: str, cfg: WgConfig | None = None) -> WgGeometry:
+    """The penalisation geometry of a WABBIT .ini file ([VPM] geometry,
+    x_cntr, R_cyl, C_smooth; [Sponge] sponge_type, L_sponge, p_sponge) with
+    the reference's defaults (module_ACM.f90:290-362)."""
+    with open(path, errors="ignore") as f:
+        return geometry_from_ini_text(f.read(), cfg)
+
+
+def geometry_from_ini_text(text: str, cfg: WgConfig | None = None) -> WgGeometry:
+    """geometry_from_ini on the text of an .ini file."""
+    kv = _parse_ini(text)
+
+    def get(sec, key, default=None):
+        v = kv.get((sec, key), "")
+        return default if v == "" else v
+
+    cfg = cfg or from_ini_text(text)
+    geo = WgGeometry()
+    name = get("VPM", "geometry", "none").lower().replace("_", "")
+    kinds = {"cylinder": GEOM_CYLINDER, "circle": GEOM_CYLINDER, "sphere-fixed": GEOM_SPHERE, "none": GEOM_NONE}
+    if name not in kinds:
+        raise ValueError(f"geometry {name!r} is not supported")
+    geo.kind = kinds[name]
+    xc = get("VPM", "x_cntr")
+    xs = _num(xc) if xc else [0.5 * cfg.domain[i] for i in range(3)]
+    for i in range(3):
+        geo.x_cntr[i] = xs[i] if i < len(xs) else 0.5 * cfg.domain[i]
+    geo.R_cyl = float(get("VPM", "R_cyl", 0.5))
+    geo.C_smooth = float(get("VPM", "C_smooth", 1.5))
+    st = get("Sponge", "sponge_type", "rect")
+    if st not in ("rect", "p-norm"):
+        raise ValueError(f"sponge_type {st!r} is not supported")
+    geo.sponge_type = SPONGE_PNORM if st == "p-norm" else SPONGE_RECT
+    geo.L_sponge = float(get("Sponge", "L_sponge", 0.0))
+    geo.p_sponge = float(get("Sponge", "p_sponge", 20.0))
+    return geo

@@ -30,6 +30,8 @@
 
 #include "../../include/wabbit_gb300.h"
 #include "adapt.hpp"
+#include "geometry.hpp"
+#include "par.hpp"
 #include "lifted.hpp"
 #include "common.cuh"
 
@@ -195,6 +197,8 @@ struct Tree {
     std::map<long long, std::unique_ptr<SyncPlan>> spare;  // plans of an earlier grid: device buffers to reuse
     double time = 0.0;
     bool shadow_valid = false;         // double-float copy of u_n in B is current
+    wg_geometry geom{};                // penalisation geometry the masks are drawn from
+    bool has_geom = false;             // false: masks are set by the caller (wg_set_mask*)
 };
 
 }  // namespace wg
@@ -1143,6 +1147,8 @@ int wg_tree_destroy(wg_ctx *ctx, int tree) {
     return WG_OK;
 }
 
+static int regen_masks(wg_ctx *ctx, Tree *t, int tree);
+
 int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *coords) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return WG_EINVAL;
@@ -1163,6 +1169,7 @@ int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *co
     int st;
     if ((st = upload_desc(ctx, *t, tree))) return st;
     if ((st = upload_lists(ctx, *t))) return st;
+    if ((st = regen_masks(ctx, t, tree))) return st;
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     ctx->grid_version++;
     return WG_OK;
@@ -1265,14 +1272,14 @@ static int grow_mask_pool(wg_ctx *ctx, int extra) {
     return WG_OK;
 }
 
+static int install_masks(wg_ctx *ctx, Tree *t, int tree, const std::vector<int> &need,
+                         const std::vector<double> &packed);
+
 int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const double *mask) {
     Tree *t = get_tree(ctx, tree);
     if (!t || n < 0 || (n && (!blocks || !mask))) return fail(WG_EINVAL, "bad arguments");
     cudaStreamSynchronize(ctx->stream);
-    for (int &m : t->mask_slot) {
-        if (m >= 0) ctx->mask_free.push_back(m);
-        m = -1;
-    }
+    t->has_geom = false;
     const int nb = t->forest.size();
     const long long np = ctx->gA.npts();
     const long long ni = ctx->nint;
@@ -1300,6 +1307,20 @@ int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const do
             packed.insert(packed.end(), blk.begin(), blk.end());
         }
     }
+    return install_masks(ctx, t, tree, need, packed);
+}
+
+// Replace a tree's masks by the interior masks packed (6 * Bs^d doubles per
+// block, the pool's layout) of the blocks listed in need; every other block
+// runs without a mask.
+static int install_masks(wg_ctx *ctx, Tree *t, int tree, const std::vector<int> &need,
+                         const std::vector<double> &packed) {
+    for (int &m : t->mask_slot) {
+        if (m >= 0) ctx->mask_free.push_back(m);
+        m = -1;
+    }
+    const long long ni = ctx->nint;
+    const int dim = ctx->cfg.dim;
     {
         const int st = grow_mask_pool(ctx, (int)need.size());
         if (st) return st;
@@ -1352,6 +1373,43 @@ int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
     return wg_set_mask_sparse(ctx, tree, (int)ids.size(), ids.data(), host_mask);
 }
 
+// Masks of every block of a tree drawn from its geometry (createMask_tree
+// after each grid change, LIB/MESH/createMask_tree.f90:118-136), computed
+// on the host pool and installed for the blocks that carry a non-zero word.
+static int regen_masks(wg_ctx *ctx, Tree *t, int tree) {
+    if (!t->has_geom) return WG_OK;
+    const int nb = t->forest.size();
+    const long long ni = ctx->nint;
+    std::vector<char> any(nb, 0);
+    std::vector<double> all((size_t)nb * 6 * ni);
+    Pool::get().run(nb, [&](int b) {
+        any[b] = geometry_mask_block(t->cfg, t->geom, t->forest.level[b], &t->forest.coords[3 * b],
+                                     all.data() + (size_t)b * 6 * ni);
+    });
+    std::vector<int> need;
+    std::vector<double> packed;
+    for (int b = 0; b < nb; b++)
+        if (any[b]) {
+            need.push_back(b);
+            packed.insert(packed.end(), all.begin() + (size_t)b * 6 * ni, all.begin() + (size_t)(b + 1) * 6 * ni);
+        }
+    return install_masks(ctx, t, tree, need, packed);
+}
+
+int wg_set_geometry(wg_ctx *ctx, int tree, const wg_geometry *geo) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return WG_EINVAL;
+    wg_geometry G{};
+    if (geo) G = *geo;
+    const char *why = geometry_check(t->cfg, G);
+    if (*why) return fail(WG_EINVAL, "geometry: %s", why);
+    cudaStreamSynchronize(ctx->stream);
+    t->geom = G;
+    t->has_geom = geo != nullptr;
+    if (!t->has_geom) return install_masks(ctx, t, tree, {}, {});
+    return regen_masks(ctx, t, tree);
+}
+
 // mask of a fixed sphere computed on the device: the blocks whose ghosted
 // box comes within radius + h + 3 max(dx) of the centre are candidates,
 // those with chi > 0 at an interior point get a mask slot (the selection of
@@ -1361,6 +1419,7 @@ int wg_set_mask_sphere(wg_ctx *ctx, int tree, const double *centre, double radiu
     if (!t || !centre || !(radius > 0.0) || !(c_smooth > 0.0)) return fail(WG_EINVAL, "bad arguments");
     if (ctx->cfg.dim != 3) return fail(WG_ENOTSUP, "sphere mask needs a 3-D context");
     cudaStreamSynchronize(ctx->stream);
+    t->has_geom = false;
     for (int &m : t->mask_slot) {
         if (m >= 0) ctx->mask_free.push_back(m);
         m = -1;
@@ -1693,25 +1752,18 @@ static int threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *fl
     if (!t || !eps_use || !flags) return fail(WG_EINVAL, "bad arguments");
     const int nb = t->forest.size();
     const int nc = ctx->geo.nc;
-    double *d_eps = nullptr, *d_det = nullptr;
-    int *d_tsvc = nullptr, *d_flags = nullptr;
-    cudaError_t e = cudaMallocAsync(&d_eps, sizeof(double) * nc, ctx->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&d_tsvc, sizeof(int) * nc, ctx->stream);
-    if (e == cudaSuccess) e = cudaMallocAsync(&d_flags, sizeof(int) * (nb + 1), ctx->stream);
+    double *d_det = nullptr;
+    int *d_flags = nullptr;
+    cudaError_t e = cudaMallocAsync(&d_flags, sizeof(int) * (nb + 1), ctx->stream);
     if (e == cudaSuccess) e = cudaMallocAsync(&d_det, sizeof(double) * (nb + 1) * nc, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_eps, eps_use, sizeof(double) * nc, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_tsvc, t->cfg.threshold_state_vector_component, sizeof(int) * nc, cudaMemcpyHostToDevice,
-                            ctx->stream);
     const int *Bs = ctx->cfg.Bs;
     if (e == cudaSuccess)
         e = launch_fwt_flags(ctx->cfg.dim, t->d_all.p, nb, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], nc, ctx->wav.X,
-                             ctx->wav.Y, d_eps, d_tsvc, d_flags, d_det, ctx->stream, input_is_wd);
+                             ctx->wav.Y, eps_use, t->cfg.threshold_state_vector_component, d_flags, d_det,
+                             ctx->stream, input_is_wd);
     if (e == cudaSuccess) e = cudaMemcpyAsync(flags, d_flags, sizeof(int) * nb, cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess && details)
         e = cudaMemcpyAsync(details, d_det, sizeof(double) * nb * nc, cudaMemcpyDeviceToHost, ctx->stream);
-    cudaFreeAsync(d_eps, ctx->stream);
-    cudaFreeAsync(d_tsvc, ctx->stream);
     cudaFreeAsync(d_flags, ctx->stream);
     cudaFreeAsync(d_det, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -1748,6 +1800,50 @@ int wg_threshold_flags_wd(wg_ctx *ctx, int tree, const double *eps_use, int *fla
 // coarse/fine interfaces, pruning and the final filtered sync. The host
 // plans every step (lifted.cpp); the data stays in A (hvy_block) and the
 // slot-indexed hvy_tmp arena T.
+// The two switches of coarseningIndicator_tree applied to the block
+// indicator's flags of the full tree: force_maxlevel_dealiasing flags every
+// block on Jmax for coarsening (LIB/MESH/coarseningIndicator_tree.f90:
+// 287-293) and threshold_mask keeps the blocks whose mask has an interface
+// (coarseningIndicatorMask_tree, :333-420; the mask status comes from the
+// tree's geometry on the host pool).
+static void indicator_switches(const Tree &t, const FullTree &ft, std::vector<int> &flags) {
+    const wg_config &c = t.cfg;
+    const bool by_mask = c.threshold_mask && t.has_geom && c.penalization;
+    if (!c.force_maxlevel_dealiasing && !by_mask) return;
+    Pool::get().run(ft.size(), [&](int b) {
+        if (c.force_maxlevel_dealiasing && ft.level[b] == c.Jmax) {
+            flags[b] = kFlagCoarsen;
+            return;
+        }
+        if (by_mask) flags[b] = std::max(flags[b], geometry_mask_status(c, t.geom, ft.level[b], &ft.coords[3 * b]));
+    });
+}
+
+// eps * norm per component (adapt_tree / coarseningIndicator_tree with
+// eps_normalized: componentWiseNorm_tree's Linfty over the leaves, a norm
+// <= 1e-9 replaced by 1, coarseningIndicator_tree.f90:133-152), or eps.
+static int adapt_thresholds(wg_ctx *ctx, Tree *t, std::vector<double> &eps_use) {
+    const int nc = ctx->geo.nc;
+    const wg_config &c = t->cfg;
+    eps_use.assign(nc, c.eps);
+    if (!c.eps_normalized) return WG_OK;
+    DevArray<double> d_norm;
+    std::vector<double> norm(nc, 0.0);
+    cudaError_t e = d_norm.upload(nullptr, nc, ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_norm_linf(t->d_all.p, t->forest.size(), ctx->A, ctx->gA, ctx->cfg.Bs[0], ctx->cfg.Bs[1],
+                             ctx->cfg.dim == 3 ? ctx->cfg.Bs[2] : 1, nc, d_norm.p, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(norm.data(), d_norm.p, sizeof(double) * nc, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "adapt norm", __FILE__, __LINE__);
+    for (int p = 0; p < nc; p++) {
+        double n = c.threshold_state_vector_component[p] == 1 ? norm[p] : -1.0;
+        if (n <= 1.0e-9) n = 1.0;
+        eps_use[p] = c.eps * n;
+    }
+    return WG_OK;
+}
+
 static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, bool thr, int *nblk_out) {
     const int dim = ctx->cfg.dim, nc = ctx->geo.nc, g = ctx->cfg.g;
     const int *Bs = ctx->cfg.Bs;
@@ -1808,7 +1904,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         if (ctx->adapt_profile) cudaStreamSynchronize(ctx->stream);
         ctx->adapt_ms[phase] += std::chrono::duration<double, std::milli>(clk::now() - t0).count();
     };
-    cudaError_t e = lifted_set_filter(w.HD.data(), w.hd_lo, (int)w.HD.size(), ctx->stream);
+    cudaError_t e = cudaSuccess;
     const int hx = Bs[0] / 2, hy = Bs[1] / 2, hz = dim == 3 ? Bs[2] / 2 : 1;
     // one device list from the same list of every part of a wave (or of
     // the wave itself): one copy per part into consecutive scratch memory
@@ -1853,7 +1949,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
                 const ScBox *sb = gather(ps, &SyncWave::ce_copies, ns);
                 const Patch *rp = gather(ps, &SyncWave::restrict_, nr);
                 double *scratch = static_cast<double *>(ctx->scratch.alloc(sizeof(double) * nf * nc * hx * hy * hz));
-                r = launch_hd_filter(dim, fe, nf, ctx->A, ctx->T, gA, Bs[0], Bs[1], Bs[2], nc, w.hd_lo,
+                r = launch_hd_filter(dim, fe, nf, ctx->A, ctx->T, gA, Bs[0], Bs[1], Bs[2], nc, w.HD.data(), w.hd_lo,
                                      (int)w.HD.size(), scratch, ctx->stream);
                 if (r == cudaSuccess && ns)
                     r = launch_scbox(sb, ns, fe, ctx->A, ctx->T, gA, hx, hy, hz, nc, scratch, ctx->stream);
@@ -1970,11 +2066,12 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
         const int *d_all = up(all);
         std::vector<int> zeros(nt, 0);
         int *d_flags = up(zeros);
-        e = launch_fwt_flags(dim, d_all, nt, ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X, w.Y, up(eps), up(tsvc),
+        e = launch_fwt_flags(dim, d_all, nt, ctx->A, gA, Bs[0], Bs[1], Bs[2], nc, w.X, w.Y, eps.data(), tsvc.data(),
                              d_flags, nullptr, ctx->stream, 1);
         if (e == cudaSuccess) e = cudaMemcpyAsync(flags.data(), d_flags, sizeof(int) * nt, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e == cudaSuccess) {
+            indicator_switches(*t, L.ft, flags);
             L.ref = flags;
             std::vector<LiftedTree::ZoneItem> items;
             L.security_candidates(items);
@@ -2118,6 +2215,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     int st;
     if ((st = upload_desc(ctx, *t, tree))) return st;
     if ((st = upload_lists(ctx, *t))) return st;
+    if ((st = regen_masks(ctx, t, tree))) return st;
     ctx->grid_version++;
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     ctx->adapt_ms[kTotal] = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
@@ -2138,7 +2236,13 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
     if (!t) return WG_EINVAL;
     if (indicator != WG_ADAPT_THRESHOLD && indicator != WG_ADAPT_EVERYWHERE)
         return fail(WG_EINVAL, "unknown indicator %d", indicator);
-    if (indicator == WG_ADAPT_THRESHOLD && !eps_use) return fail(WG_EINVAL, "eps_use is required");
+    std::vector<double> eps_own;
+    if (indicator == WG_ADAPT_THRESHOLD && !eps_use) {
+        WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
+        const int st0 = adapt_thresholds(ctx, t, eps_own);
+        if (st0) return st0;
+        eps_use = eps_own.data();
+    }
     if (ctx->wav.lifted) return adapt_lifted(ctx, t, tree, eps_use, indicator == WG_ADAPT_THRESHOLD, nblk_out);
     const int dim = ctx->cfg.dim, nc = ctx->geo.nc, g = ctx->cfg.g;
     const int *Bs = ctx->cfg.Bs;
@@ -2163,17 +2267,14 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
             if (!kept[b]) ctx->free_slots.give(slot[b]);
     };
     std::vector<int> flags(nt, 0);
-    DevArray<int> d_flags, d_tsvc, d_list;
-    DevArray<double> d_eps;
+    DevArray<int> d_flags;
     const bool thr = indicator == WG_ADAPT_THRESHOLD;
     cudaError_t e = cudaSuccess;
     if (thr) {
         e = d_flags.upload(nullptr, nt, ctx->stream);
-        if (e == cudaSuccess) e = d_eps.upload(eps_use, nc, ctx->stream);
-        if (e == cudaSuccess) e = d_tsvc.upload(t->cfg.threshold_state_vector_component, nc, ctx->stream);
         if (e == cudaSuccess)
             e = launch_fwt_flags(dim, t->d_all.p, nb, ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], nc, ctx->wav.X, ctx->wav.Y,
-                                 d_eps.p, d_tsvc.p, d_flags.p, nullptr, ctx->stream);
+                                 eps_use, t->cfg.threshold_state_vector_component, d_flags.p, nullptr, ctx->stream);
     } else {
         for (int b = 0; b < nb; b++) flags[b] = kFlagCoarsen;   // "everywhere": the leaves
     }
@@ -2208,7 +2309,8 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
         if (e == cudaSuccess) e = keep_lists.back()->upload(ms.data(), ms.size(), ctx->stream);
         if (e == cudaSuccess)
             e = launch_fwt_flags(dim, keep_lists.back()->p, (int)ms.size(), ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], nc,
-                                 ctx->wav.X, ctx->wav.Y, d_eps.p, d_tsvc.p, d_flags.p + first, nullptr, ctx->stream);
+                                 ctx->wav.X, ctx->wav.Y, eps_use, t->cfg.threshold_state_vector_component,
+                                 d_flags.p + first, nullptr, ctx->stream);
     }
     if (e == cudaSuccess && thr)
         e = cudaMemcpyAsync(flags.data(), d_flags.p, sizeof(int) * nt, cudaMemcpyDeviceToHost, ctx->stream);
@@ -2218,6 +2320,7 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
         for (int b = nb; b < nt; b++) ctx->free_slots.give(slot[b]);   // the grid is unchanged
         return cuda_fail(e, "wg_adapt", __FILE__, __LINE__);
     }
+    if (thr) indicator_switches(*t, ft, flags);
     std::vector<int> leaves;
     adapt_decide(ft, flags, leaves);
     // install the new grid
@@ -2241,6 +2344,7 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
     t->shadow_valid = false;
     if ((st = upload_desc(ctx, *t, tree))) return st;
     if ((st = upload_lists(ctx, *t))) return st;
+    if ((st = regen_masks(ctx, t, tree))) return st;
     ctx->grid_version++;
     if ((st = run_sync(ctx, *t, ctx->A, false, g, g))) return st;
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
@@ -2385,6 +2489,7 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     int st;
     if ((st = upload_desc(ctx, *t, tree))) return st;
     if ((st = upload_lists(ctx, *t))) return st;
+    if ((st = regen_masks(ctx, t, tree))) return st;
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     ctx->grid_version++;
     return WG_OK;
@@ -2753,6 +2858,9 @@ int wg_threshold_flags_noalloc(const wg_config *cfg, int nblk, const double *d_b
     WaveletInfo w;
     make_wavelet(cfg->wavelet, w);
     const int dim = cfg->dim;
+    if (!noalloc_shape_supported(dim, cfg->Bs[0], cfg->Bs[1], dim == 3 ? cfg->Bs[2] : 1, w.X, w.Y))
+        return fail(WG_EINVAL, "wg_threshold_flags_noalloc: a %s transform of %dx%dx%d blocks does not fit the "
+                    "shared memory of one thread block", cfg->wavelet, cfg->Bs[0], cfg->Bs[1], dim == 3 ? cfg->Bs[2] : 1);
     BufGeo geo = {cfg->Bs[0] + 2 * cfg->g, cfg->Bs[1] + 2 * cfg->g, dim == 3 ? cfg->Bs[2] + 2 * cfg->g : 1, cfg->g};
     cudaError_t e = launch_fwt_flags_noalloc(dim, nblk, d_blocks, geo, cfg->Bs[0], cfg->Bs[1],
                                              dim == 3 ? cfg->Bs[2] : 1, cfg->neq, w.X, w.Y, eps_use,

@@ -158,6 +158,9 @@ cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, 
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
                       const int *trees, cudaStream_t s);
 cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
+// max |u| per component over the interiors of the listed blocks (Bs2 = 1 in 2-D)
+cudaError_t launch_norm_linf(const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int nc,
+                             double *out, cudaStream_t s);
 // interior exchange state <-> compact array, one CTA row per (block,
 // component); towards the state optionally also the double-float copy B
 // (thin layout gt) with its same-level ghost pushes
@@ -183,10 +186,10 @@ cudaError_t launch_wavelet_decompose_window(int dim, const int *blk, int nblk, d
 struct FilterEntry;
 struct ScBox;
 struct BoxOp;
-cudaError_t lifted_set_filter(const double *hd, int lo, int n, cudaStream_t s);
 cudaError_t launch_xcopy(const Patch *p, int n, const double *sbuf, double *dbuf, BufGeo geo, int nc, cudaStream_t s);
 cudaError_t launch_hd_filter(int dim, const FilterEntry *ent, int n, const double *A, const double *T, BufGeo geo,
-                             int Bx, int By, int Bz, int nc, int hd_lo, int hd_n, double *scratch, cudaStream_t s);
+                             int Bx, int By, int Bz, int nc, const double *hd, int hd_lo, int hd_n, double *scratch,
+                             cudaStream_t s);
 cudaError_t launch_scbox(const ScBox *b, int n, const FilterEntry *ent, const double *A, const double *T, BufGeo geo,
                          int hx, int hy, int hz, int nc, double *scratch, cudaStream_t s);
 cudaError_t launch_restrict_scratch(const Patch *p, int n, const double *scratch, double *A, BufGeo geo, int hx,
@@ -202,6 +205,7 @@ cudaError_t launch_wc_threshold(int dim, const int *blk, int nblk, double *u, Bu
                                 int nc, const double *thresh, const int *tsvc, cudaStream_t s);
 // allocation-free variant (static device scratch, contiguous blocks 0..nblk-1)
 int noalloc_max_blocks();
+bool noalloc_shape_supported(int dim, int Bs0, int Bs1, int Bs2, int wavelet_x, int wavelet_y);
 cudaError_t launch_fwt_flags_noalloc(int dim, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,
                                      int nc, int wavelet_x, int wavelet_y, const double *eps_host,
                                      const int *tsvc_host, int *flags, double *details, cudaStream_t s);

@@ -26,10 +26,14 @@
 
 namespace wg {
 
-__constant__ double c_lhd[32];
-__constant__ int c_lhd_k[32], c_lhd_s[32], c_lhd_m[32];   // tap kinds for the integer-pipe products (exact.cuh)
-__constant__ long long c_lhd_g[32];          // sign bit of each tap
-__constant__ int c_lhd_n[2];   // lo, count
+// HD filter taps of a launch, passed by value (no state shared between
+// launches, streams or devices)
+struct HdTaps {
+    double v[32];
+    int k[32], s[32], m[32];   // tap kinds for the integer-pipe products (exact.cuh)
+    long long g[32];           // sign bit of each tap
+    int lo, n;
+};
 
 __global__ void __launch_bounds__(128) xcopy_kernel(const Patch *__restrict__ patches, int npatch,
                                                     const double *__restrict__ sbuf, double *dbuf, BufGeo geo,
@@ -54,14 +58,18 @@ __global__ void __launch_bounds__(128) xcopy_kernel(const Patch *__restrict__ pa
 
 // one CTA per (entry, component); X: [nz][ny][hx], Y: [nz][hy][hx]
 template <int DIM>
-__global__ void __launch_bounds__(256) hd_filter_kernel(const FilterEntry *__restrict__ ent, const double *A,
+__global__ void __launch_bounds__(256) hd_filter_kernel(const __grid_constant__ HdTaps H,
+                                                        const FilterEntry *__restrict__ ent, const double *A,
                                                         const double *T, BufGeo geo, int Bx, int By, int Bz, int nc,
                                                         double *scratch) {
+    const double *c_lhd = H.v;
+    const int *c_lhd_k = H.k, *c_lhd_s = H.s, *c_lhd_m = H.m;
+    const long long *c_lhd_g = H.g;
     extern __shared__ double sm[];
     const int e = blockIdx.x / nc, c = blockIdx.x % nc;
     const FilterEntry fe = ent[e];
     const double *u = (fe.src_tmp ? T : A) + ((long long)fe.slot * nc + c) * geo.npts();
-    const int g = geo.gb, lo = c_lhd_n[0], nt = c_lhd_n[1], hi = lo + nt - 1;
+    const int g = geo.gb, lo = H.lo, nt = H.n, hi = lo + nt - 1;
     const int hx = Bx / 2, hy = By / 2, hz = DIM == 3 ? Bz / 2 : 1;
     const int y0 = g + lo, ny = By + hi - lo, z0 = DIM == 3 ? g + lo : 0, nz = DIM == 3 ? Bz + hi - lo : 1;
     double *X = sm, *Y = sm + (size_t)hx * ny * nz;
@@ -228,24 +236,17 @@ __global__ void __launch_bounds__(128) zone_detail_kernel(const ZoneBox *__restr
 }
 
 // ---------------------------------------------------------------------------
-cudaError_t lifted_set_filter(const double *hd, int lo, int n, cudaStream_t s) {
-    if (n > 32) return cudaErrorInvalidValue;
-    double h[32] = {};
-    int kind[32] = {}, sh[32] = {}, mul[32] = {};
-    long long sg[32] = {};
+static bool make_hd_taps(const double *hd, int lo, int n, HdTaps &H) {
+    if (n > 32 || n < 1 || !hd) return false;
+    H = HdTaps{};
     for (int i = 0; i < n; i++) {
-        h[i] = hd[i];
-        classify_tap(h[i], kind[i], sh[i], mul[i]);
-        sg[i] = h[i] < 0.0 ? (long long)0x8000000000000000ULL : 0LL;
+        H.v[i] = hd[i];
+        classify_tap(H.v[i], H.k[i], H.s[i], H.m[i]);
+        H.g[i] = H.v[i] < 0.0 ? (long long)0x8000000000000000ULL : 0LL;
     }
-    const int ln[2] = {lo, n};
-    cudaError_t e = cudaMemcpyToSymbolAsync(c_lhd, h, sizeof(h), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_k, kind, sizeof(kind), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_s, sh, sizeof(sh), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_m, mul, sizeof(mul), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_g, sg, sizeof(sg), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_lhd_n, ln, sizeof(ln), 0, cudaMemcpyHostToDevice, s);
-    return e;
+    H.lo = lo;
+    H.n = n;
+    return true;
 }
 
 static int warps_grid(int n) { return (n + 3) / 4; }
@@ -258,9 +259,11 @@ cudaError_t launch_xcopy(const Patch *p, int n, const double *sbuf, double *dbuf
 }
 
 cudaError_t launch_hd_filter(int dim, const FilterEntry *ent, int n, const double *A, const double *T, BufGeo geo,
-                             int Bx, int By, int Bz, int nc, int hd_lo, int hd_n, double *scratch, cudaStream_t s) {
+                             int Bx, int By, int Bz, int nc, const double *hd, int hd_lo, int hd_n, double *scratch,
+                             cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    if (!ent || !scratch) return cudaErrorInvalidValue;
+    HdTaps H;
+    if (!ent || !scratch || !make_hd_taps(hd, hd_lo, hd_n, H)) return cudaErrorInvalidValue;
     const int hi = hd_lo + hd_n - 1;
     if (-hd_lo > geo.gb || hi > geo.gb) return cudaErrorInvalidValue;
     const int hx = Bx / 2, hy = By / 2, ny = By + hi - hd_lo, nz = dim == 3 ? Bz + hi - hd_lo : 1;
@@ -271,7 +274,7 @@ cudaError_t launch_hd_filter(int dim, const FilterEntry *ent, int n, const doubl
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
         }
-        kern<<<n * nc, 256, smem, s>>>(ent, A, T, geo, Bx, By, Bz, nc, scratch);
+        kern<<<n * nc, 256, smem, s>>>(H, ent, A, T, geo, Bx, By, Bz, nc, scratch);
         return cudaGetLastError();
     };
     return dim == 2 ? go(hd_filter_kernel<2>) : go(hd_filter_kernel<3>);

@@ -353,4 +353,45 @@ cudaError_t launch_sphere_fill(const int4 *cand, const int *slot, int n, const S
     return cudaGetLastError();
 }
 
+// componentWiseNorm_tree (LIB/OPERATORS/componentWiseNorm_tree.f90:1-140),
+// Linfty over the interiors of the listed blocks: one CTA per (block,
+// component) reduces max |u| and merges it into out[c] with an integer
+// atomic max on the bits (non-negative doubles order like their bits).
+// out must hold zeros on entry.
+__global__ void __launch_bounds__(256) norm_linf_kernel(const int *blk, const double *u, BufGeo geo, int Bs0, int Bs1,
+                                                        int Bs2, int nc, unsigned long long *out) {
+    __shared__ unsigned long long red[8];
+    const int b = blk[blockIdx.x], c = blockIdx.y;
+    const long long np = geo.npts();
+    const double *ub = u + ((long long)b * nc + c) * np;
+    const int z3 = geo.nz > 1;
+    const int nint = Bs0 * Bs1 * Bs2;
+    unsigned long long m = 0ull;
+    for (int q = threadIdx.x; q < nint; q += blockDim.x) {
+        const int ix = q % Bs0, iy = (q / Bs0) % Bs1, iz = q / (Bs0 * Bs1);
+        const double v = ub[((long long)(iz + (z3 ? geo.gb : 0)) * geo.ny + (iy + geo.gb)) * geo.nx + (ix + geo.gb)];
+        const unsigned long long a = (unsigned long long)dbits(v) & 0x7fffffffffffffffull;
+        m = a > m ? a : m;
+    }
+    for (int o = 16; o; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, m, o);
+        m = t > m ? t : m;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = red[w] > m ? red[w] : m;
+        atomicMax(out + c, m);
+    }
+}
+
+cudaError_t launch_norm_linf(const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int nc,
+                             double *out, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * nc, s);
+    if (e != cudaSuccess || nblk <= 0) return e;
+    norm_linf_kernel<<<dim3(nblk, nc), 256, 0, s>>>(blk, u, geo, Bs0, Bs1, Bs2, nc,
+                                                    reinterpret_cast<unsigned long long *>(out));
+    return cudaGetLastError();
+}
+
 }  // namespace wg

@@ -21,6 +21,7 @@
 #include "df.cuh"
 #include "exact.cuh"
 #include <algorithm>
+#include <atomic>
 
 namespace wg {
 
@@ -306,18 +307,23 @@ __global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict
     }
 }
 
-cudaError_t sync_init() { return init_predictor(); }
+cudaError_t sync_init() { return cudaSuccess; }
 
 cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_doubles, double *buf, BufGeo geo, int nc,
                            int order_predictor, cudaStream_t s, const double *src_buf) {
     if (npatch <= 0) return cudaSuccess;
     if (!patches) return cudaErrorInvalidValue;
     const size_t smem = sizeof(double) * (size_t)max_smem_doubles;
-    static size_t attr = 0;
-    if (smem > 48 * 1024 && smem > attr) {
-        cudaError_t e = cudaFuncSetAttribute(predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the attribute belongs to the current device's context: set on every
+    // launch that needs it, to the largest size asked for so far (launches
+    // captured earlier in a graph keep a valid attribute)
+    static std::atomic<size_t> attr_max{0};
+    for (size_t cur = attr_max.load(); cur < smem && !attr_max.compare_exchange_weak(cur, smem);) {
+    }
+    const size_t want = std::max(smem, attr_max.load());
+    if (want > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
         if (e != cudaSuccess) return e;
-        attr = smem;
     }
     predict_kernel<<<npatch, 256, smem, s>>>(patches, src_buf ? src_buf : buf, buf, geo, nc, order_predictor / 2 - 1,
                                              order_predictor);
@@ -334,13 +340,18 @@ cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_dou
     const int cg = (int)std::min<size_t>((size_t)nc, limit / per);
     const size_t smem = per * cg;
     float2 *b = reinterpret_cast<float2 *>(buf);
-    // the attribute only grows, so launches captured earlier stay valid
-    static size_t attr[4] = {0, 0, 0, 0};
+    // the attribute belongs to the current device's context; it is raised to
+    // the largest size this launcher has asked for on any device (launches
+    // captured earlier in a graph keep a valid attribute)
+    static std::atomic<size_t> attr_max[4];
     auto go = [&](auto kern, int k) -> cudaError_t {
-        if (smem > 48 * 1024 && smem > attr[k]) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        size_t want = smem;
+        for (size_t cur = attr_max[k].load(); cur < want && !attr_max[k].compare_exchange_weak(cur, want);) {
+        }
+        want = std::max(want, attr_max[k].load());
+        if (want > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
             if (e != cudaSuccess) return e;
-            attr[k] = smem;
         }
         kern<<<npatch, 256, smem, s>>>(patches, b, geo, nc, cg);
         return cudaGetLastError();
@@ -380,8 +391,6 @@ cudaError_t launch_sync(const Patch *patches, int npatch, double *buf, BufGeo ge
                         cudaStream_t s) {
     if (npatch <= 0) return cudaSuccess;
     if (!patches) return cudaErrorInvalidValue;
-    cudaError_t e = init_predictor();
-    if (e != cudaSuccess) return e;
     const int oi = order_predictor / 2 - 1;
     const int threads = 128;
     const int blocks = (npatch * 32 + threads - 1) / threads;

@@ -22,6 +22,7 @@
 // Refinement: refineBlock (LIB/MESH/refinementExecute.f90:4-116): the whole
 // parent block (ghosts included) is predicted to the fine grid and each of the
 // 2^d daughters takes its (Bs+2g)^d window.
+#include <mutex>
 #include <type_traits>
 
 #include "common.cuh"
@@ -30,15 +31,40 @@
 
 namespace wg {
 
-__constant__ double c_hd[32];
-__constant__ double c_gd[32];
-__constant__ int c_flt[4];   // hd_lo, hd_n, gd_lo, gd_n
-__constant__ double c_hr[32];
-__constant__ double c_gr[32];
-__constant__ int c_rflt[4];  // hr_lo, hr_n, gr_lo, gr_n
+// The filters, thresholds and component groups of a launch travel in its
+// parameters (read through the constant bank like __constant__ data): no
+// state is shared between launches, so calls on different streams, host
+// threads or devices with different wavelets cannot see each other's taps.
+struct Filters {            // analysis filters HD, GD
+    double hd[32], gd[32];
+    int hd_lo, hd_n, gd_lo, gd_n;
+};
+struct RFilters {           // reconstruction filters HR, GR
+    double hr[32], gr[32];
+    int hr_lo, hr_n, gr_lo, gr_n;
+};
 
-static int g_flt_key = -1;   // wavelet whose analysis filters sit in constant memory
-static int g_rflt_key = -1;  // ... and whose reconstruction filters
+static Filters make_filters(const WaveletInfo &w) {
+    Filters f{};
+    for (size_t i = 0; i < w.HD.size() && i < 32; i++) f.hd[i] = w.HD[i];
+    for (size_t i = 0; i < w.GD.size() && i < 32; i++) f.gd[i] = w.GD[i];
+    f.hd_lo = w.hd_lo;
+    f.hd_n = (int)w.HD.size();
+    f.gd_lo = w.gd_lo;
+    f.gd_n = (int)w.GD.size();
+    return f;
+}
+
+static RFilters make_rfilters(const WaveletInfo &w) {
+    RFilters f{};
+    for (size_t i = 0; i < w.HR.size() && i < 32; i++) f.hr[i] = w.HR[i];
+    for (size_t i = 0; i < w.GR.size() && i < 32; i++) f.gr[i] = w.GR[i];
+    f.hr_lo = w.hr_lo;
+    f.hr_n = (int)w.HR.size();
+    f.gr_lo = w.gr_lo;
+    f.gr_n = (int)w.GR.size();
+    return f;
+}
 
 struct FwtArgs {
     const int *blk;
@@ -46,11 +72,28 @@ struct FwtArgs {
     BufGeo geo;
     int Bs[3];
     int nc, lazy, fmax;
-    const double *eps_use;   // nc entries
-    const int *tsvc;         // threshold_state_vector_component, nc entries
+    Filters F;
+    double eps[8];           // per-component threshold (eps * norm)
+    int tsvc[8];             // threshold_state_vector_component
     int *flags;
     double *details;
 };
+
+// FwtArgs of a wavelet, with its thresholds and groups (host arrays of nc)
+static bool make_fwt_args(const WaveletInfo &w, int nc, const double *eps_host, const int *tsvc_host, FwtArgs &a) {
+    if (nc > 8 || w.HD.size() > 32 || w.GD.size() > 32) return false;
+    a = FwtArgs{};
+    a.F = make_filters(w);
+    a.nc = nc;
+    a.lazy = w.lifted ? 0 : 1;
+    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
+    a.fmax = std::max(std::max(w.hd_lo, hd_hi), std::max(w.gd_lo, gd_hi));
+    for (int c = 0; c < nc; c++) {
+        a.eps[c] = eps_host ? eps_host[c] : 0.0;
+        a.tsvc[c] = tsvc_host ? tsvc_host[c] : 1;
+    }
+    return true;
+}
 
 __device__ __forceinline__ double filt(const double *c, int lo, int n, const double *line, int stride, int at) {
     double s = 0.0;
@@ -71,7 +114,8 @@ __device__ __forceinline__ double filt(const double *c, int lo, int n, const dou
 // (spaghetti order) to out instead of reducing the details; out may be the
 // input itself (every read of the CTA's block component precedes its writes).
 template <int DIM, bool STORE = false>
-__global__ void __launch_bounds__(256) fwt_detail_kernel(FwtArgs a, double *detail_scratch, double *out = nullptr) {
+__global__ void __launch_bounds__(256) fwt_detail_kernel(const __grid_constant__ FwtArgs a, double *detail_scratch,
+                                                         double *out = nullptr) {
     extern __shared__ double sm[];
     const int bi = blockIdx.x / a.nc, c = blockIdx.x % a.nc;
     const int b = a.blk[bi];
@@ -82,7 +126,8 @@ __global__ void __launch_bounds__(256) fwt_detail_kernel(FwtArgs a, double *deta
     const int z0 = DIM == 3 ? g - f : 0, nz = DIM == 3 ? Bz + 2 * f : 1;
     const long long np = a.geo.npts();
     const double *u = a.u + ((long long)b * a.nc + c) * np;
-    const int hd_lo = c_flt[0], hd_n = c_flt[1], gd_lo = c_flt[2], gd_n = c_flt[3];
+    const int hd_lo = a.F.hd_lo, hd_n = a.F.hd_n, gd_lo = a.F.gd_lo, gd_n = a.F.gd_n;
+    const double *c_hd = a.F.hd, *c_gd = a.F.gd;
     // sm[(z*ny + y)*Bx + x], x interior, y in [y0,y0+ny), z in [z0,z0+nz)
     // X pass straight from global memory
     for (int r = threadIdx.x; r < ny * nz; r += blockDim.x) {
@@ -154,7 +199,7 @@ __global__ void __launch_bounds__(256) fwt_detail_kernel(FwtArgs a, double *deta
 // details from data that is already decomposed (spaghetti order): max |WC|
 // over the interior, SC positions excluded; one CTA per (block, component)
 template <int DIM>
-__global__ void __launch_bounds__(256) wd_detail_kernel(FwtArgs a, double *detail_scratch) {
+__global__ void __launch_bounds__(256) wd_detail_kernel(const __grid_constant__ FwtArgs a, double *detail_scratch) {
     const int bi = blockIdx.x / a.nc, c = blockIdx.x % a.nc;
     const int b = a.blk[bi];
     const int g = a.geo.gb;
@@ -178,7 +223,7 @@ __global__ void __launch_bounds__(256) wd_detail_kernel(FwtArgs a, double *detai
     }
 }
 
-__global__ void flag_kernel(FwtArgs a, const double *detail_scratch, int nblk) {
+__global__ void flag_kernel(const __grid_constant__ FwtArgs a, const double *detail_scratch, int nblk) {
     const int bi = blockIdx.x * blockDim.x + threadIdx.x;
     if (bi >= nblk) return;
     double det[8];
@@ -194,14 +239,14 @@ __global__ void flag_kernel(FwtArgs a, const double *detail_scratch, int nblk) {
     for (int c = 0; c < a.nc; c++) {
         if (a.tsvc[c] == 1) det[c] = d[c];
         if (a.tsvc[c] == 0) det[c] = 0.0;
-        if (!(det[c] <= a.eps_use[c])) all = false;
+        if (!(det[c] <= a.eps[c])) all = false;
         if (a.details) a.details[(long long)bi * a.nc + c] = det[c];
     }
     a.flags[bi] = all ? -1 : 0;
 }
 
 static cudaError_t launch_tpo(int mode, int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
-                              int Bs2, int nc, const WaveletInfo &w, int key, int f, double *scratch, cudaStream_t s);
+                              int Bs2, int nc, const WaveletInfo &w, int f, double *scratch, cudaStream_t s);
 
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,
                              int Bs2, int nc, int wavelet_x, int wavelet_y, const double *eps_use, const int *tsvc,
@@ -211,31 +256,14 @@ cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u,
     WaveletInfo w;
     char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
     if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
-    const int key = wavelet_x * 10 + wavelet_y;
-    if (g_flt_key != key) {
-        double hd[32] = {}, gd[32] = {};
-        for (size_t i = 0; i < w.HD.size(); i++) hd[i] = w.HD[i];
-        for (size_t i = 0; i < w.GD.size(); i++) gd[i] = w.GD[i];
-        int flt[4] = {w.hd_lo, (int)w.HD.size(), w.gd_lo, (int)w.GD.size()};
-        cudaError_t e = cudaMemcpyToSymbolAsync(c_hd, hd, sizeof(hd), 0, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_gd, gd, sizeof(gd), 0, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_flt, flt, sizeof(flt), 0, cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return e;
-        g_flt_key = key;
-    }
     FwtArgs a;
+    if (!make_fwt_args(w, nc, eps_use, tsvc, a)) return cudaErrorInvalidValue;
     a.blk = blk;
     a.u = u;
     a.geo = geo;
     a.Bs[0] = Bs0;
     a.Bs[1] = Bs1;
     a.Bs[2] = Bs2;
-    a.nc = nc;
-    a.lazy = w.lifted ? 0 : 1;
-    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
-    a.fmax = std::max(std::max(w.hd_lo, hd_hi), std::max(w.gd_lo, gd_hi));
-    a.eps_use = eps_use;
-    a.tsvc = tsvc;
     a.flags = flags;
     a.details = details;
     if (a.fmax > geo.gb) return cudaErrorInvalidValue;   // filter needs more ghost nodes
@@ -246,7 +274,7 @@ cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u,
     if (e != cudaSuccess) return e;
     cudaError_t et = cudaErrorNotSupported;
     if (!input_is_wd)
-        et = launch_tpo(0, dim, blk, nblk, const_cast<double *>(u), geo, Bs0, Bs1, Bs2, nc, w, key, a.fmax, scratch, s);
+        et = launch_tpo(0, dim, blk, nblk, const_cast<double *>(u), geo, Bs0, Bs1, Bs2, nc, w, a.fmax, scratch, s);
     if (et != cudaSuccess && et != cudaErrorNotSupported) {
         cudaFreeAsync(scratch, s);
         return et;
@@ -275,9 +303,10 @@ cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u,
 // with stride ds. Lazy (unlifted) wavelets keep the SCs and add the odd HR taps
 // to each WC (value first); lifted wavelets: SC + odd GR taps at an SC,
 // odd HR taps over the SCs, then GR(0) WC, then the other even GR taps at a WC.
-__device__ __forceinline__ void iwt_line(const double *src, long long ss, int at0, int n, bool lazy, double *dst,
-                                         long long ds) {
-    const int hr_lo = c_rflt[0], hr_n = c_rflt[1], gr_lo = c_rflt[2], gr_n = c_rflt[3];
+__device__ __forceinline__ void iwt_line(const RFilters &R, const double *src, long long ss, int at0, int n, bool lazy,
+                                         double *dst, long long ds) {
+    const int hr_lo = R.hr_lo, hr_n = R.hr_n, gr_lo = R.gr_lo, gr_n = R.gr_n;
+    const double *c_hr = R.hr, *c_gr = R.gr;
     for (int k = 0; k < n; k += 2) {
         const int s0 = at0 + k, w0 = s0 + 1;
         double sc, wc;
@@ -322,7 +351,8 @@ __device__ __forceinline__ void iwt_line(const double *src, long long ss, int at
 // memory holds the x-interior columns of the rows/planes the y and z passes
 // read (F = max HR/GR half-width around the interior).
 template <int DIM>
-__global__ void __launch_bounds__(256) iwt_kernel(const int *blk, double *u, BufGeo geo, int Bx, int By, int Bz,
+__global__ void __launch_bounds__(256) iwt_kernel(const __grid_constant__ RFilters R, const int *blk, double *u,
+                                                  BufGeo geo, int Bx, int By, int Bz,
                                                   int nc, int lazy, int F) {
     extern __shared__ double sm[];
     const int bi = blockIdx.x / nc, c = blockIdx.x % nc;
@@ -337,14 +367,14 @@ __global__ void __launch_bounds__(256) iwt_kernel(const int *blk, double *u, Buf
     for (int r = threadIdx.x; r < ny * nz; r += blockDim.x) {
         const int yy = r % ny, zz = r / ny;
         const double *line = ub + ((long long)(z0 + zz) * geo.ny + (y0 + yy)) * geo.nx;
-        iwt_line(line, 1, g, Bx, lazy, sm + (long long)r * Bx, 1);
+        iwt_line(R, line, 1, g, Bx, lazy, sm + (long long)r * Bx, 1);
     }
     __syncthreads();
     double tmp[64];
     for (int r = threadIdx.x; r < Bx * nz; r += blockDim.x) {
         const int ix = r % Bx, zz = r / Bx;
         double *col = sm + (long long)zz * ny * Bx + ix;     // stride Bx along y
-        iwt_line(col, Bx, F, By, lazy, tmp, 1);
+        iwt_line(R, col, Bx, F, By, lazy, tmp, 1);
         for (int iy = 0; iy < By; iy++) col[(long long)(F + iy) * Bx] = tmp[iy];
     }
     __syncthreads();
@@ -352,7 +382,7 @@ __global__ void __launch_bounds__(256) iwt_kernel(const int *blk, double *u, Buf
         for (int r = threadIdx.x; r < Bx * By; r += blockDim.x) {
             const int ix = r % Bx, iy = r / Bx;
             double *col = sm + (long long)(F + iy) * Bx + ix;   // stride ny*Bx along z
-            iwt_line(col, (long long)ny * Bx, F, Bz, lazy, tmp, 1);
+            iwt_line(R, col, (long long)ny * Bx, F, Bz, lazy, tmp, 1);
             for (int iz = 0; iz < Bz; iz++) col[(long long)(F + iz) * ny * Bx] = tmp[iz];
         }
         __syncthreads();
@@ -430,22 +460,19 @@ struct Taps {
     long long gr0_sgn;
     int lazy;
 };
-__constant__ Taps c_taps;
-static int g_taps_key = -1;
-static bool g_taps_cdf44 = false;   // the loaded taps have the CDF4,4 kinds
 
 constexpr int kTpoThreads = 512;
 constexpr int kTpoMaxPerThread = 16;
 
 // sum_t src[(at + off_t) * st] * val_t in order, the first term not added to 0
-__device__ __forceinline__ double tap_sum(int f, const double *src, long long st, int at) {
+__device__ __forceinline__ double tap_sum(const Taps &c_taps, int f, const double *src, long long st, int at) {
     const int n = c_taps.n[f];
     double s = __dmul_rn(src[(at + c_taps.off[f][0]) * st], c_taps.val[f][0]);
     for (int t = 1; t < n; t++) s = __dadd_rn(s, __dmul_rn(src[(at + c_taps.off[f][t]) * st], c_taps.val[f][t]));
     return s;
 }
 
-// Compile-time tap kinds of CDF4,4 (classify_tap of the lists load_taps
+// Compile-time tap kinds of CDF4,4 (classify_tap of the lists make_taps
 // builds: HD -6..6 without +-5, GD -3..3 without +-2, HR odd, GR odd, GR even
 // without 0); the host checks them against the loaded taps before the
 // specialised kernel runs.
@@ -462,7 +489,7 @@ struct Cdf44Taps {
 // product with tap t of list F, the kind known at compile time: every kind
 // but 0 is formed on the integer pipe
 template <class K, int F>
-__device__ __forceinline__ double ktap_mul(double x, int t, bool &bad) {
+__device__ __forceinline__ double ktap_mul(const Taps &c_taps, double x, int t, bool &bad) {
     if (K::kind(F, t) == 2) return x;
     if (K::kind(F, t) == 1) return pow2_mul(x, c_taps.sh[F][t], c_taps.sgn[F][t], bad);
     if (K::kind(F, t) == 3) return short_mul(x, c_taps.mul[F][t], c_taps.sh[F][t], c_taps.sgn[F][t], bad);
@@ -472,24 +499,24 @@ __device__ __forceinline__ double ktap_mul(double x, int t, bool &bad) {
 // the same sum with the kinds of K known at compile time: the FP64 pipe
 // only adds
 template <class K, int F>
-__device__ __forceinline__ double ktap_sum(const double *src, long long st, int at, bool &bad) {
+__device__ __forceinline__ double ktap_sum(const Taps &c_taps, const double *src, long long st, int at, bool &bad) {
     double s = 0.0;
 #pragma unroll
     for (int t = 0; t < K::nt(F); t++) {
-        const double p = ktap_mul<K, F>(src[(at + c_taps.off[F][t]) * st], t, bad);
+        const double p = ktap_mul<K, F>(c_taps, src[(at + c_taps.off[F][t]) * st], t, bad);
         s = t == 0 ? p : __dadd_rn(s, p);
     }
     return s;
 }
 
 // FWT output at interior offset p (position at of the line)
-__device__ __forceinline__ double fwt_point(const double *src, long long st, int at, int p) {
-    if ((p & 1) == 0) return c_taps.lazy ? src[at * st] : tap_sum(0, src, st, at);
-    return tap_sum(1, src, st, at);
+__device__ __forceinline__ double fwt_point(const Taps &c_taps, const double *src, long long st, int at, int p) {
+    if ((p & 1) == 0) return c_taps.lazy ? src[at * st] : tap_sum(c_taps, 0, src, st, at);
+    return tap_sum(c_taps, 1, src, st, at);
 }
 
 // IWT output at interior offset p (position at of the line)
-__device__ __forceinline__ double iwt_point(const double *src, long long st, int at, int p) {
+__device__ __forceinline__ double iwt_point(const Taps &c_taps, const double *src, long long st, int at, int p) {
     if (c_taps.lazy) {
         double v = src[at * st];
         if (p & 1)
@@ -503,7 +530,7 @@ __device__ __forceinline__ double iwt_point(const double *src, long long st, int
             v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[3][t]) * st], c_taps.val[3][t]));
         return v;
     }
-    double v = tap_sum(2, src, st, at);
+    double v = tap_sum(c_taps, 2, src, st, at);
     v = __dadd_rn(v, __dmul_rn(src[at * st], c_taps.gr0));
     for (int t = 0; t < c_taps.n[4]; t++)
         v = __dadd_rn(v, __dmul_rn(src[(at + c_taps.off[4][t]) * st], c_taps.val[4][t]));
@@ -515,26 +542,29 @@ __device__ __forceinline__ double iwt_point(const double *src, long long st, int
 // exact range, and the caller recomputes those outputs with fwt_point /
 // iwt_point
 template <class K>
-__device__ __forceinline__ double fwt_point_k(const double *src, long long st, int at, int p, bool &bad) {
-    return (p & 1) == 0 ? ktap_sum<K, 0>(src, st, at, bad) : ktap_sum<K, 1>(src, st, at, bad);
+__device__ __forceinline__ double fwt_point_k(const Taps &c_taps, const double *src, long long st, int at, int p,
+                                              bool &bad) {
+    return (p & 1) == 0 ? ktap_sum<K, 0>(c_taps, src, st, at, bad) : ktap_sum<K, 1>(c_taps, src, st, at, bad);
 }
 
 template <class K>
-__device__ __forceinline__ double iwt_point_k(const double *src, long long st, int at, int p, bool &bad) {
+__device__ __forceinline__ double iwt_point_k(const Taps &c_taps, const double *src, long long st, int at, int p,
+                                              bool &bad) {
     double v;
     if ((p & 1) == 0) {
         // the reference adds the odd GR taps one by one to the SC
         v = src[at * st];
 #pragma unroll
         for (int t = 0; t < K::nt(3); t++) {
-            v = __dadd_rn(v, ktap_mul<K, 3>(src[(at + c_taps.off[3][t]) * st], t, bad));
+            v = __dadd_rn(v, ktap_mul<K, 3>(c_taps, src[(at + c_taps.off[3][t]) * st], t, bad));
         }
     } else {
-        v = ktap_sum<K, 2>(src, st, at, bad);
+        v = ktap_sum<K, 2>(c_taps, src, st, at, bad);
         v = __dadd_rn(v, tap_mul(src[at * st], c_taps.gr0, c_taps.gr0_kind, c_taps.gr0_sh, c_taps.gr0_mul,
                                  c_taps.gr0_sgn, bad));
 #pragma unroll
-        for (int t = 0; t < K::nt(4); t++) v = __dadd_rn(v, ktap_mul<K, 4>(src[(at + c_taps.off[4][t]) * st], t, bad));
+        for (int t = 0; t < K::nt(4); t++)
+            v = __dadd_rn(v, ktap_mul<K, 4>(c_taps, src[(at + c_taps.off[4][t]) * st], t, bad));
     }
     return v;
 }
@@ -552,8 +582,9 @@ __device__ __forceinline__ bool in_tap_band(double x) {
 struct GenericTaps {};
 
 template <int DIM, int MODE, class K = GenericTaps>
-__global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, double *u, BufGeo geo, int Bx, int By,
-                                                             int Bz, int nc, int f, double *detail_scratch) {
+__global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const __grid_constant__ Taps c_taps, const int *blk,
+                                                             double *u, BufGeo geo, int Bx, int By, int Bz, int nc,
+                                                             int f, double *detail_scratch) {
     extern __shared__ double sm[];
     const int bi = blockIdx.x / nc, c = blockIdx.x % nc;
     const int b = blk[bi];
@@ -566,13 +597,13 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
     // slow: the reference's FP64 multiplies; fast: compile-time tap kinds
     // (products on the integer pipe), bad marks outputs to redo
     auto slow = [&](const double *src, long long st, int at, int p) {
-        return MODE == 2 ? iwt_point(src, st, at, p) : fwt_point(src, st, at, p);
+        return MODE == 2 ? iwt_point(c_taps, src, st, at, p) : fwt_point(c_taps, src, st, at, p);
     };
     auto fast = [&](const double *src, long long st, int at, int p, bool &bad) {
         if constexpr (std::is_same<K, GenericTaps>::value)
             return slow(src, st, at, p);
         else
-            return MODE == 2 ? iwt_point_k<K>(src, st, at, p, bad) : fwt_point_k<K>(src, st, at, p, bad);
+            return MODE == 2 ? iwt_point_k<K>(c_taps, src, st, at, p, bad) : fwt_point_k<K>(c_taps, src, st, at, p, bad);
     };
     auto point = slow;
     constexpr bool kTyped = !std::is_same<K, GenericTaps>::value;
@@ -729,9 +760,10 @@ __global__ void __launch_bounds__(kTpoThreads, 2) tpo_kernel(const int *blk, dou
     }
 }
 
-static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
-    if (g_taps_key == key) return cudaSuccess;
-    Taps t{};
+// the compacted tap lists of a wavelet; cdf44: they have the kinds of the
+// CDF4,4-specialised kernels
+static bool make_taps(const WaveletInfo &w, Taps &t, bool &cdf44) {
+    t = Taps{};
     auto add = [&](int f, int off, double v) {
         if (t.n[f] >= 16) return false;
         t.off[f][t.n[f]] = off;
@@ -765,39 +797,38 @@ static cudaError_t load_taps(const WaveletInfo &w, int key, cudaStream_t s) {
         else if (!(m & 1) && w.GR[i] != 0.0) ok &= add(4, m, w.GR[i]);
     }
     t.lazy = w.lifted ? 0 : 1;
-    if (!ok || t.n[0] == 0 || t.n[1] == 0) return cudaErrorInvalidValue;
+    if (!ok || t.n[0] == 0 || t.n[1] == 0) return false;
     // the compile-time kinds of the CDF4,4 kernels must describe these taps
-    g_taps_cdf44 = !t.lazy;
-    for (int f = 0; f < 5 && g_taps_cdf44; f++) {
-        if (t.n[f] != Cdf44Taps::nt(f)) g_taps_cdf44 = false;
-        for (int k = 0; k < t.n[f] && g_taps_cdf44; k++)
-            if (t.kind[f][k] != Cdf44Taps::kind(f, k)) g_taps_cdf44 = false;
+    cdf44 = !t.lazy;
+    for (int f = 0; f < 5 && cdf44; f++) {
+        if (t.n[f] != Cdf44Taps::nt(f)) cdf44 = false;
+        for (int k = 0; k < t.n[f] && cdf44; k++)
+            if (t.kind[f][k] != Cdf44Taps::kind(f, k)) cdf44 = false;
     }
-    cudaError_t e = cudaMemcpyToSymbolAsync(c_taps, &t, sizeof(t), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) g_taps_key = key;
-    return e;
+    return true;
 }
 
 // launch the thread-per-output kernel if the block fits its limits; returns
 // cudaErrorNotSupported otherwise (the caller then uses the column kernels)
 static cudaError_t launch_tpo(int mode, int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
-                              int Bs2, int nc, const WaveletInfo &w, int key, int f, double *scratch, cudaStream_t s) {
+                              int Bs2, int nc, const WaveletInfo &w, int f, double *scratch, cudaStream_t s) {
     const int ny = Bs1 + 2 * f, nz = dim == 3 ? Bs2 + 2 * f : 1;
     if ((long long)Bs0 * Bs1 * nz > (long long)kTpoThreads * kTpoMaxPerThread) return cudaErrorNotSupported;
     const size_t smem = sizeof(double) * (size_t)Bs0 * ny * nz;
     if (smem > 110 * 1024) return cudaErrorNotSupported;
-    cudaError_t e = load_taps(w, key, s);
-    if (e != cudaSuccess) return e;
+    Taps taps;
+    bool cdf44 = false;
+    if (!make_taps(w, taps, cdf44)) return cudaErrorInvalidValue;
     const int bz = dim == 3 ? Bs2 : 1;
     auto go = [&](auto kern) -> cudaError_t {
         cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e2 != cudaSuccess) return e2;
-        kern<<<nblk * nc, kTpoThreads, smem, s>>>(blk, u, geo, Bs0, Bs1, bz, nc, f, scratch);
+        kern<<<nblk * nc, kTpoThreads, smem, s>>>(taps, blk, u, geo, Bs0, Bs1, bz, nc, f, scratch);
         return cudaGetLastError();
     };
     if (dim == 2) {
         if (mode == 0) return go(tpo_kernel<2, 0>);
-        if (g_taps_cdf44) {
+        if (cdf44) {
             if (mode == 1) return go(tpo_kernel<2, 1, Cdf44Taps>);
             if (mode == 3) return go(tpo_kernel<2, 3, Cdf44Taps>);
             return go(tpo_kernel<2, 2, Cdf44Taps>);
@@ -807,7 +838,7 @@ static cudaError_t launch_tpo(int mode, int dim, const int *blk, int nblk, doubl
         return go(tpo_kernel<2, 2>);
     }
     if (mode == 0) return go(tpo_kernel<3, 0>);
-    if (g_taps_cdf44) {
+    if (cdf44) {
         if (mode == 1) return go(tpo_kernel<3, 1, Cdf44Taps>);
         if (mode == 3) return go(tpo_kernel<3, 3, Cdf44Taps>);
         return go(tpo_kernel<3, 2, Cdf44Taps>);
@@ -817,40 +848,22 @@ static cudaError_t launch_tpo(int mode, int dim, const int *blk, int nblk, doubl
     return go(tpo_kernel<3, 2>);
 }
 
-static cudaError_t load_analysis_filters(const WaveletInfo &w, int key, cudaStream_t s) {
-    if (g_flt_key == key) return cudaSuccess;
-    double hd[32] = {}, gd[32] = {};
-    for (size_t i = 0; i < w.HD.size(); i++) hd[i] = w.HD[i];
-    for (size_t i = 0; i < w.GD.size(); i++) gd[i] = w.GD[i];
-    int flt[4] = {w.hd_lo, (int)w.HD.size(), w.gd_lo, (int)w.GD.size()};
-    cudaError_t e = cudaMemcpyToSymbolAsync(c_hd, hd, sizeof(hd), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_gd, gd, sizeof(gd), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_flt, flt, sizeof(flt), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) g_flt_key = key;
-    return e;
-}
-
 cudaError_t launch_wavelet_decompose(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
                                      int Bs2, int nc, int wavelet_x, int wavelet_y, cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
     WaveletInfo w;
     char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
     if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
-    cudaError_t e = load_analysis_filters(w, wavelet_x * 10 + wavelet_y, s);
-    if (e != cudaSuccess) return e;
-    FwtArgs a{};
+    FwtArgs a;
+    if (!make_fwt_args(w, nc, nullptr, nullptr, a)) return cudaErrorInvalidValue;
     a.blk = blk;
     a.u = u;
     a.geo = geo;
     a.Bs[0] = Bs0;
     a.Bs[1] = Bs1;
     a.Bs[2] = Bs2;
-    a.nc = nc;
-    a.lazy = w.lifted ? 0 : 1;
-    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
-    a.fmax = std::max(std::max(w.hd_lo, hd_hi), std::max(w.gd_lo, gd_hi));
     if (a.fmax > geo.gb) return cudaErrorInvalidValue;
-    e = launch_tpo(1, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, wavelet_x * 10 + wavelet_y, a.fmax, nullptr, s);
+    cudaError_t e = launch_tpo(1, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, a.fmax, nullptr, s);
     if (e != cudaErrorNotSupported) return e;
     cudaGetLastError();
     const int ny = Bs1 + 2 * a.fmax, nz = dim == 3 ? Bs2 + 2 * a.fmax : 1;
@@ -879,7 +892,7 @@ cudaError_t launch_wavelet_decompose_window(int dim, const int *blk, int nblk, d
     const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
     const int fmax = std::max(std::max(w.hd_lo, hd_hi), std::max(w.gd_lo, gd_hi));
     if (fmax > geo.gb) return cudaErrorInvalidValue;
-    return launch_tpo(3, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, wavelet_x * 10 + wavelet_y, fmax, nullptr, s);
+    return launch_tpo(3, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, fmax, nullptr, s);
 }
 
 cudaError_t launch_wavelet_reconstruct(int dim, const int *blk, int nblk, double *u, BufGeo geo, int Bs0, int Bs1,
@@ -889,24 +902,14 @@ cudaError_t launch_wavelet_reconstruct(int dim, const int *blk, int nblk, double
     WaveletInfo w;
     char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
     if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
-    const int key = wavelet_x * 10 + wavelet_y;
-    if (g_rflt_key != key) {
-        double hr[32] = {}, gr[32] = {};
-        for (size_t i = 0; i < w.HR.size(); i++) hr[i] = w.HR[i];
-        for (size_t i = 0; i < w.GR.size(); i++) gr[i] = w.GR[i];
-        int flt[4] = {w.hr_lo, (int)w.HR.size(), w.gr_lo, (int)w.GR.size()};
-        cudaError_t e = cudaMemcpyToSymbolAsync(c_hr, hr, sizeof(hr), 0, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_gr, gr, sizeof(gr), 0, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_rflt, flt, sizeof(flt), 0, cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) return e;
-        g_rflt_key = key;
-    }
+    if (w.HR.size() > 32 || w.GR.size() > 32) return cudaErrorInvalidValue;
+    const RFilters R = make_rfilters(w);
     const int hr_hi = w.hr_lo + (int)w.HR.size() - 1, gr_hi = w.gr_lo + (int)w.GR.size() - 1;
     const int F = std::max(std::max(w.hr_lo, hr_hi), std::max(w.gr_lo, gr_hi));
     // the x pass reads up to F+1 points beyond an interior WC position
     if (F + 1 > geo.gb + 1 || Bs0 > 64 || Bs1 > 64 || Bs2 > 64) return cudaErrorInvalidValue;
     {
-        cudaError_t e = launch_tpo(2, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, key, F, nullptr, s);
+        cudaError_t e = launch_tpo(2, dim, blk, nblk, u, geo, Bs0, Bs1, Bs2, nc, w, F, nullptr, s);
         if (e != cudaErrorNotSupported) return e;
         cudaGetLastError();
     }
@@ -914,10 +917,10 @@ cudaError_t launch_wavelet_reconstruct(int dim, const int *blk, int nblk, double
     const size_t smem = sizeof(double) * (size_t)Bs0 * ny * nz;
     if (dim == 2) {
         cudaFuncSetAttribute(iwt_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        iwt_kernel<2><<<nblk * nc, 256, smem, s>>>(blk, u, geo, Bs0, Bs1, 1, nc, w.lifted ? 0 : 1, F);
+        iwt_kernel<2><<<nblk * nc, 256, smem, s>>>(R, blk, u, geo, Bs0, Bs1, 1, nc, w.lifted ? 0 : 1, F);
     } else {
         cudaFuncSetAttribute(iwt_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        iwt_kernel<3><<<nblk * nc, 256, smem, s>>>(blk, u, geo, Bs0, Bs1, Bs2, nc, w.lifted ? 0 : 1, F);
+        iwt_kernel<3><<<nblk * nc, 256, smem, s>>>(R, blk, u, geo, Bs0, Bs1, Bs2, nc, w.lifted ? 0 : 1, F);
     }
     return cudaGetLastError();
 }
@@ -938,33 +941,31 @@ cudaError_t launch_wc_threshold(int dim, const int *blk, int nblk, double *u, Bu
     return cudaGetLastError();
 }
 
-cudaError_t wavelet_init() { return init_predictor(); }
+cudaError_t wavelet_init() { return cudaSuccess; }
 
 // ---------------------------------------------------------------------------
 // Allocation-free coarsening indicator. Callers that must not allocate device
 // memory during a call (a host code that manages its own memory pool, runs
 // under a memory budget enforced outside CUDA, or links the library into a
 // runtime whose allocator it may not call) get a variant of
-// launch_fwt_flags whose per-block detail scratch, block list, thresholds
-// and component groups live in file-scope static device arrays. Every
-// device that loads the library holds these arrays (~1.2 MB) until exit.
-// All calls share them: two calls whose kernels overlap on the GPU race.
+// launch_fwt_flags whose per-block detail scratch and block list live in
+// file-scope static device arrays; filters, thresholds and component groups
+// travel in the launch parameters. Every device that loads the library
+// holds these arrays (~0.6 MB) until exit. All calls share them: two calls
+// whose kernels overlap on the GPU race.
 // ---------------------------------------------------------------------------
 #define WG_NOALLOC_MAX_BLOCKS 16384
 #define WG_NOALLOC_MAX_COMP 8
 static __device__ __align__(256) double g_na_detail[WG_NOALLOC_MAX_BLOCKS * WG_NOALLOC_MAX_COMP];
 static __device__ __align__(256) int g_na_blocks[WG_NOALLOC_MAX_BLOCKS];
-static __device__ __align__(256) double g_na_eps[WG_NOALLOC_MAX_COMP];
-static __device__ __align__(256) int g_na_tsvc[WG_NOALLOC_MAX_COMP];
 
 struct NoAllocPtrs {
-    double *detail;
-    int *blocks;
-    double *eps;
-    int *tsvc;
-    bool ready;
+    double *detail = nullptr;
+    int *blocks = nullptr;
+    bool ready = false;
 };
 static NoAllocPtrs g_na_ptrs[64];
+static std::mutex g_na_mutex;
 
 __global__ void noalloc_iota_kernel(int *b, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = i;
@@ -973,25 +974,41 @@ __global__ void noalloc_iota_kernel(int *b, int n) {
 // once per device, with that device current: resolve the device addresses of
 // the static arrays (a host-side name of a __device__ array is not a device
 // address) and fill the identity block list
-static cudaError_t noalloc_setup(int dev, cudaStream_t s) {
+static cudaError_t noalloc_setup(int dev, cudaStream_t s, NoAllocPtrs &out) {
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_na_mutex);
     NoAllocPtrs &p = g_na_ptrs[dev];
-    if (p.ready) return cudaSuccess;
-    cudaError_t e = cudaGetSymbolAddress((void **)&p.detail, g_na_detail);
-    if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&p.blocks, g_na_blocks);
-    if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&p.eps, g_na_eps);
-    if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&p.tsvc, g_na_tsvc);
-    if (e != cudaSuccess) return e;
-    e = init_predictor();
-    if (e != cudaSuccess) return e;
-    noalloc_iota_kernel<<<64, 256, 0, s>>>(p.blocks, WG_NOALLOC_MAX_BLOCKS);
-    e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e == cudaSuccess) p.ready = true;
-    return e;
+    if (!p.ready) {
+        NoAllocPtrs q;
+        cudaError_t e = cudaGetSymbolAddress((void **)&q.detail, g_na_detail);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&q.blocks, g_na_blocks);
+        if (e != cudaSuccess) return e;
+        noalloc_iota_kernel<<<64, 256, 0, s>>>(q.blocks, WG_NOALLOC_MAX_BLOCKS);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        q.ready = true;
+        p = q;
+    }
+    out = p;
+    return cudaSuccess;
 }
 
 int noalloc_max_blocks() { return WG_NOALLOC_MAX_BLOCKS; }
+
+// whether one of the two transform forms takes blocks of this shape
+bool noalloc_shape_supported(int dim, int Bs0, int Bs1, int Bs2, int wavelet_x, int wavelet_y) {
+    WaveletInfo w;
+    char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
+    if (!make_wavelet(name, w)) return false;
+    FwtArgs a;
+    if (!make_fwt_args(w, 1, nullptr, nullptr, a)) return false;
+    const long long ny = Bs1 + 2 * a.fmax, nz = dim == 3 ? Bs2 + 2 * a.fmax : 1;
+    const long long smem = 8LL * Bs0 * ny * nz;
+    const bool tpo = (long long)Bs0 * Bs1 * nz <= (long long)kTpoThreads * kTpoMaxPerThread && smem <= 110 * 1024;
+    const bool column = smem <= 227 * 1024 && Bs1 <= 64 && Bs2 <= 64;
+    return tpo || column;
+}
 
 cudaError_t launch_fwt_flags_noalloc(int dim, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2,
                                      int nc, int wavelet_x, int wavelet_y, const double *eps_host,
@@ -1001,49 +1018,38 @@ cudaError_t launch_fwt_flags_noalloc(int dim, int nblk, const double *u, BufGeo 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    e = noalloc_setup(dev, s);
+    NoAllocPtrs P;
+    e = noalloc_setup(dev, s, P);
     if (e != cudaSuccess) return e;
-    const NoAllocPtrs &P = g_na_ptrs[dev];
     WaveletInfo w;
     char name[8] = {'C', 'D', 'F', (char)('0' + wavelet_x), (char)('0' + wavelet_y), 0};
     if (!make_wavelet(name, w)) return cudaErrorInvalidValue;
-    // filters, thresholds and groups for this call (no allocation: copies
-    // into constant memory and into the static arrays)
-    double hd[32] = {}, gd[32] = {};
-    for (size_t i = 0; i < w.HD.size(); i++) hd[i] = w.HD[i];
-    for (size_t i = 0; i < w.GD.size(); i++) gd[i] = w.GD[i];
-    int flt[4] = {w.hd_lo, (int)w.HD.size(), w.gd_lo, (int)w.GD.size()};
-    e = cudaMemcpyToSymbolAsync(c_hd, hd, sizeof(hd), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_gd, gd, sizeof(gd), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbolAsync(c_flt, flt, sizeof(flt), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(P.eps, eps_host, sizeof(double) * nc, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(P.tsvc, tsvc_host, sizeof(int) * nc, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return e;
-    g_flt_key = -1;   // the shared filter constants now hold this call's wavelet
     FwtArgs a;
+    if (!make_fwt_args(w, nc, eps_host, tsvc_host, a)) return cudaErrorInvalidValue;
     a.blk = P.blocks;
     a.u = u;
     a.geo = geo;
     a.Bs[0] = Bs0;
     a.Bs[1] = Bs1;
     a.Bs[2] = Bs2;
-    a.nc = nc;
-    a.lazy = w.lifted ? 0 : 1;
-    const int hd_hi = w.hd_lo + (int)w.HD.size() - 1, gd_hi = w.gd_lo + (int)w.GD.size() - 1;
-    a.fmax = std::max(std::max(w.hd_lo, hd_hi), std::max(w.gd_lo, gd_hi));
-    a.eps_use = P.eps;
-    a.tsvc = P.tsvc;
     a.flags = flags;
     a.details = details;
     if (a.fmax > geo.gb) return cudaErrorInvalidValue;
-    const int ny = Bs1 + 2 * a.fmax, nz = dim == 3 ? Bs2 + 2 * a.fmax : 1;
-    const size_t smem = sizeof(double) * (size_t)Bs0 * ny * nz;
-    if (dim == 2) {
-        e = cudaFuncSetAttribute(fwt_detail_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) fwt_detail_kernel<2><<<nblk * nc, 256, smem, s>>>(a, P.detail);
-    } else {
-        e = cudaFuncSetAttribute(fwt_detail_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) fwt_detail_kernel<3><<<nblk * nc, 256, smem, s>>>(a, P.detail);
+    // the thread-per-output transform where the block fits it, else the
+    // column form
+    e = launch_tpo(0, dim, P.blocks, nblk, const_cast<double *>(u), geo, Bs0, Bs1, Bs2, nc, w, a.fmax, P.detail, s);
+    if (e == cudaErrorNotSupported) {
+        cudaGetLastError();
+        const int ny = Bs1 + 2 * a.fmax, nz = dim == 3 ? Bs2 + 2 * a.fmax : 1;
+        const size_t smem = sizeof(double) * (size_t)Bs0 * ny * nz;
+        if (dim == 2) {
+            e = cudaFuncSetAttribute(fwt_detail_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) fwt_detail_kernel<2><<<nblk * nc, 256, smem, s>>>(a, P.detail);
+        } else {
+            e = cudaFuncSetAttribute(fwt_detail_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) fwt_detail_kernel<3><<<nblk * nc, 256, smem, s>>>(a, P.detail);
+        }
+        if (e == cudaSuccess) e = cudaGetLastError();
     }
     if (e != cudaSuccess) return e;
     flag_kernel<<<(nblk + 127) / 128, 128, 0, s>>>(a, P.detail, nblk);
@@ -1089,8 +1095,6 @@ __global__ void __launch_bounds__(256) refine_kernel(const int *parent, int npar
 cudaError_t launch_refine(int dim, const int *parent, int nparent, const int *child_slot, const double *u,
                           BufGeo geo, int Bs0, int Bs1, int Bs2, int nc, int order_predictor, cudaStream_t s) {
     if (nparent <= 0) return cudaSuccess;
-    cudaError_t e = init_predictor();
-    if (e != cudaSuccess) return e;
     dim3 grid(64, std::min(nparent, 65535));
     refine_kernel<<<grid, 256, 0, s>>>(parent, nparent, child_slot, u, geo, dim, Bs0, Bs1, Bs2, nc,
                                        order_predictor / 2 - 1, order_predictor);

@@ -13,26 +13,16 @@
 
 namespace wg {
 
-// predictor coefficients for order 2,4,6,8; one copy per translation unit
-static __constant__ double c_pred[4][8];
-
-static cudaError_t init_predictor() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    double h[4][8] = {};
-    h[0][0] = 0.5;
-    h[0][1] = 0.5;
-    const double c4[4] = {-1.0, 9.0, 9.0, -1.0};
-    for (int i = 0; i < 4; i++) h[1][i] = c4[i] / 16.0;
-    const double c6[6] = {3.0, -25.0, 150.0, 150.0, -25.0, 3.0};
-    for (int i = 0; i < 6; i++) h[2][i] = c6[i] / 256.0;
-    const double c8[8] = {-5.0, 49.0, -245.0, 1225.0, 1225.0, -245.0, 49.0, -5.0};
-    for (int i = 0; i < 8; i++) h[3][i] = c8[i] / 2048.0;
-    cudaError_t e = cudaMemcpyToSymbol(c_pred, h, sizeof(h));
-    if (e == cudaSuccess) done = true;
-    return e;
-}
-
+// predictor coefficients for order 2, 4, 6, 8 (module_wavelets.f90:126-128
+// and the order-2/6/8 rows): exact binary fractions, initialised with the
+// module on every device that loads it; one copy per translation unit
+static __constant__ double c_pred[4][8] = {
+    {0.5, 0.5},
+    {-1.0 / 16.0, 9.0 / 16.0, 9.0 / 16.0, -1.0 / 16.0},
+    {3.0 / 256.0, -25.0 / 256.0, 150.0 / 256.0, 150.0 / 256.0, -25.0 / 256.0, 3.0 / 256.0},
+    {-5.0 / 2048.0, 49.0 / 2048.0, -245.0 / 2048.0, 1225.0 / 2048.0, 1225.0 / 2048.0, -245.0 / 2048.0, 49.0 / 2048.0,
+     -5.0 / 2048.0},
+};
 
 struct PredCtx {
     const double *src;

@@ -193,6 +193,12 @@ class Forest:
             raise ValueError("mask has the wrong size")
         capi.check(self.L.wg_set_mask_sparse(self.ctx.h, self.tree, len(blocks), _p(blocks, ctypes.c_int), _p(mask)))
 
+    def set_geometry(self, geo):
+        """Penalisation geometry (config.WgGeometry) the tree draws its masks
+        from after every grid change, as createMask_tree does; None removes
+        it."""
+        capi.check(self.L.wg_set_geometry(self.ctx.h, self.tree, ctypes.byref(geo) if geo is not None else None))
+
     def set_mask_sphere(self, centre, radius, c_smooth=1.5):
         """Fixed-sphere penalisation mask computed on the device (3-D)."""
         c = np.ascontiguousarray(centre, np.float64)
@@ -280,13 +286,17 @@ class Forest:
 
     def adapt(self, eps_use=None, everywhere: bool = False) -> int:
         """adapt_tree (coarsening) with the threshold-state-vector indicator
-        (eps_use = eps * norm per component) or on every leaf. CDF X0: full
-        tree by decimation; CDF XY: full-tree FWT with coarse extension,
-        security zone and reconstruction at the coarse/fine interfaces.
-        Replaces grid and state, drops masks, returns the new block count."""
+        (eps_use = eps * norm per component; None: the configuration's eps,
+        normalised by the leaves' Linfty norm with eps_normalized) or on
+        every leaf. CDF X0: full tree by decimation; CDF XY: full-tree FWT
+        with coarse extension, security zone and reconstruction at the
+        coarse/fine interfaces. Replaces grid and state, redraws the masks
+        from the geometry (else drops them), returns the new block count."""
         n = ctypes.c_int()
         if everywhere:
             capi.check(self.L.wg_adapt(self.ctx.h, self.tree, None, 1, ctypes.byref(n)))
+        elif eps_use is None:
+            capi.check(self.L.wg_adapt(self.ctx.h, self.tree, None, 0, ctypes.byref(n)))
         else:
             e = np.ascontiguousarray(np.broadcast_to(np.asarray(eps_use, np.float64), (self.cfg.neq,)))
             capi.check(self.L.wg_adapt(self.ctx.h, self.tree, _p(e), 0, ctypes.byref(n)))
