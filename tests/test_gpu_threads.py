@@ -21,7 +21,7 @@ if not torch.cuda.is_available():
 
 def _sequence(w, rounds=3):
     """indicator, refinement and adaptation on one tree, several times"""
-    cfg = small_cfg(2, w, Bs=12, jmin=2, jmax=5)
+    cfg = small_cfg(2, w, Bs=16, jmin=2, jmax=5)
     lv, co = grids.random_graded(2, cfg.Jmin, 4, seed=51, frac=0.3)
     out = []
     with Context(cfg, 8 * len(lv) + 64) as ctx:
