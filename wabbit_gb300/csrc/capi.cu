@@ -16,6 +16,7 @@
 //   mask interior only, 6 components, only for blocks that carry a mask;
 //        the FP32-pipe precision adds a double-float copy (5 components)
 #include <algorithm>
+#include <cstddef>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -379,7 +380,7 @@ int run_pred_classes(wg_ctx *ctx, const PredClasses &pc, int st, double *buf, co
     const std::vector<int> &b = pc.begin[st];
     for (size_t k = 0; k + 1 < b.size(); k++)
         WG_CUDA_OK(launch_predict_df(pc.patches.p + b[k], b[k + 1] - b[k], pc.need[st][k], buf, geo, ctx->geo.nc,
-                                     ctx->wav.order_predictor, ctx->stream));
+                                     ctx->wav.order_predictor, ctx->d_desc, ctx->d_clk, ctx->stream));
     return WG_OK;
 }
 
@@ -542,7 +543,7 @@ int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool 
             if (st3) return st3;
         } else if (sp->table.stage_predict[s] && df)
             WG_CUDA_OK(launch_predict_df(sp->d.p + b, e - b, sp->table.max_coarse, buf, geo, ctx->geo.nc,
-                                         ctx->wav.order_predictor, ctx->stream));
+                                         ctx->wav.order_predictor, ctx->d_desc, ctx->d_clk, ctx->stream));
         else if (sp->table.stage_predict[s])
             WG_CUDA_OK(launch_predict(sp->d.p + b, e - b, sp->table.max_coarse, buf, geo, ctx->geo.nc,
                                       ctx->wav.order_predictor, ctx->stream));
@@ -714,8 +715,13 @@ int ensure_shadow(wg_ctx *ctx, Tree &t) {
     bool push;
     int st = thin_plan(ctx, t, &push);
     if (st) return st;
+    const int tid = (int)(&t - ctx->trees.data());
+    WG_CUDA_OK(launch_anchor_from_state(t.d_all.p, (int)t.slots.size(), ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1],
+                                        ctx->cfg.dim == 3 ? Bs[2] : 1, ctx->d_desc, ctx->d_clk,
+                                        ctx->d_tree_ids.p + tid, 1, 1, ctx->stream));
     WG_CUDA_OK(launch_shadow(t.d_all.p, (int)t.slots.size(), ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0],
-                             Bs[1], ctx->cfg.dim == 3 ? Bs[2] : 1, push ? ctx->d_push : nullptr, ctx->stream));
+                             Bs[1], ctx->cfg.dim == 3 ? Bs[2] : 1, push ? ctx->d_push : nullptr, ctx->d_desc,
+                             ctx->d_clk, ctx->stream));
     t.shadow_valid = true;
     return WG_OK;
 }
@@ -772,7 +778,7 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     // or the shadow copy) when push is on
     if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true, push))) return st;
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
-                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream));
+                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream, 1));
     if ((st = stage_launch_df(ctx, t, 1, ctx->B, ctx->C, push))) return st;
     if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true, push))) return st;
     if ((st = stage_launch_df(ctx, t, 2, ctx->C, ctx->D, push))) return st;
@@ -908,7 +914,7 @@ int rk4_enqueue_batch(wg_ctx *ctx) {
     int st;
     if ((st = run_sync_batch(ctx, ctx->B))) return st;
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, bp.all.p, bp.n_all, ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A, ctx->gA, Bs[0],
-                         Bs[1], Bs[2], (int)bp.trees.size(), bp.tree_ids.p, ctx->stream));
+                         Bs[1], Bs[2], (int)bp.trees.size(), bp.tree_ids.p, ctx->stream, 1));
     if ((st = stage_launch_batch(ctx, 1, ctx->B, ctx->C))) return st;
     if ((st = run_sync_batch(ctx, ctx->C))) return st;
     if ((st = stage_launch_batch(ctx, 2, ctx->C, ctx->D))) return st;
@@ -1524,7 +1530,10 @@ int wg_set_time(wg_ctx *ctx, int tree, double time) {
     TreeClock c;
     std::memset(&c, 0, sizeof(c));
     c.time = time;
-    WG_CUDA_OK(cudaMemcpyAsync(ctx->d_clk + tree, &c, sizeof(c), cudaMemcpyHostToDevice, ctx->stream));
+    // time, dt and the divergence flag; the anchoring constant and running
+    // max of the stage inputs stay (they describe the state, not the clock)
+    WG_CUDA_OK(cudaMemcpyAsync(ctx->d_clk + tree, &c, offsetof(TreeClock, anchor_M), cudaMemcpyHostToDevice,
+                               ctx->stream));
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     return WG_OK;
 }
@@ -2705,6 +2714,9 @@ static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) 
     const int nch = interior_chunks(ctx, nblk, first);
     if ((st = ensure_copy_stream(ctx, nch))) return st;
     const cudaMemcpyKind kind = cudaMemcpyDefault;   // host or device memory
+    const int tid = (int)(t - ctx->trees.data());
+    // the scatter records max |u|, from which the anchored copy takes its quantum
+    if (shadow) WG_CUDA_OK(launch_umax_reset(ctx->d_clk, ctx->d_tree_ids.p + tid, 1, ctx->stream));
     for (int k = 0; k < nch; k++) {
         const int b0 = first[k], nb = first[k + 1] - first[k];
         double *dev = ctx->staging + per * b0, *hst = host + per * b0;
@@ -2714,16 +2726,21 @@ static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) 
             WG_CUDA_OK(cudaMemcpyAsync(dev, hst, bytes, kind, ctx->copy_stream));
             WG_CUDA_OK(cudaEventRecord(done, ctx->copy_stream));
             WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, done, 0));
-            WG_CUDA_OK(launch_interior_xfer(t->d_all.p + b0, nb, dev, ctx->A, ctx->gA, shadow ? ctx->B : nullptr,
-                                            ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz, push ? ctx->d_push : nullptr, 1,
-                                            ctx->stream));
+            WG_CUDA_OK(launch_interior_xfer(t->d_all.p + b0, nb, dev, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz,
+                                            1, ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream));
         } else {
-            WG_CUDA_OK(launch_interior_xfer(t->d_all.p + b0, nb, dev, ctx->A, ctx->gA, nullptr, ctx->gT, ctx->geo.nc,
-                                            Bs[0], Bs[1], Bz, nullptr, 0, ctx->stream));
+            WG_CUDA_OK(launch_interior_xfer(t->d_all.p + b0, nb, dev, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz,
+                                            0, ctx->d_desc, nullptr, ctx->stream));
             WG_CUDA_OK(cudaEventRecord(ready, ctx->stream));
             WG_CUDA_OK(cudaStreamWaitEvent(ctx->copy_stream, ready, 0));
             WG_CUDA_OK(cudaMemcpyAsync(hst, dev, bytes, kind, ctx->copy_stream));
         }
+    }
+    if (shadow) {
+        WG_CUDA_OK(launch_anchor_from_state(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz,
+                                            ctx->d_desc, ctx->d_clk, ctx->d_tree_ids.p + tid, 1, 0, ctx->stream));
+        WG_CUDA_OK(launch_shadow(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz,
+                                 push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream));
     }
     WG_CUDA_OK(cudaStreamSynchronize(ctx->copy_stream));
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
@@ -2801,14 +2818,21 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
             WG_CUDA_OK(cudaEventRecord(h2d_done[nxt], ctx->copy_stream));
         }
         WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, h2d_done[cur], 0));
-        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, I[cur], ctx->A, ctx->gA, shadow ? ctx->B : nullptr, ctx->gT,
-                                        ctx->geo.nc, Bs[0], Bs[1], Bz, push ? ctx->d_push : nullptr, 1, ctx->stream));
+        if (shadow) WG_CUDA_OK(launch_umax_reset(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
+        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, I[cur], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 1,
+                                        ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream));
         WG_CUDA_OK(cudaEventRecord(scattered[cur], ctx->stream));
+        if (shadow) {
+            WG_CUDA_OK(launch_anchor_from_state(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz,
+                                                ctx->d_desc, ctx->d_clk, ctx->d_tree_ids.p + tree, 1, 0, ctx->stream));
+            WG_CUDA_OK(launch_shadow(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz,
+                                     push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream));
+        }
         t->shadow_valid = shadow;
         if ((st = rk4_enqueue(ctx, tree))) return st;
         if (k >= 2) WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, d2h_done[cur], 0));
-        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[cur], ctx->A, ctx->gA, nullptr, ctx->gT, ctx->geo.nc, Bs[0],
-                                        Bs[1], Bz, nullptr, 0, ctx->stream));
+        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[cur], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,
+                                        ctx->d_desc, nullptr, ctx->stream));
         WG_CUDA_OK(cudaEventRecord(gathered[cur], ctx->stream));
         WG_CUDA_OK(cudaStreamWaitEvent(ctx->d2h_stream, gathered[cur], 0));
         WG_CUDA_OK(cudaMemcpyAsync(outs[k], O[cur], bytes, cudaMemcpyDefault, ctx->d2h_stream));

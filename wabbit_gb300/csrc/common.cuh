@@ -32,7 +32,13 @@ struct TreeClock {
     int    pad;
     // dt, dt/3 and dt/6 as double-float pairs (written with dt)
     float  f_dt[2], f_dt3[2], f_dt6[2];
-    float  fpad[2];
+    // FP32-pipe stage inputs are anchored: the hi float of every value is a
+    // multiple of one quantum q per tree, rounded by (x + M) - M with
+    // M = 1.5 * 2^23 * q (0: no anchoring). umax_f: running max |u| (float
+    // bits) of the state written in this step, from which the next step's
+    // M is chosen.
+    float  anchor_M;
+    unsigned umax_f;
 };
 
 // Per-block descriptor. k1, k2: first-derivative weights (2/3)/dx, (1/12)/dx;
@@ -125,7 +131,7 @@ cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, in
 // un (FP64) and writes the copy of u_{n+1} to out; maskdf holds 5 float2
 // words per point (chi/C_eta with colour applied, u_s, sponge/C_sponge)
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
-                                const TreeParams *tp, const TreeClock *clk, const void *in, const void *u0,
+                                const TreeParams *tp, TreeClock *clk, const void *in, const void *u0,
                                 void *out, BufGeo gt, double *un, BufGeo gun, void *acc, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int *err,
                                 cudaStream_t s);
@@ -136,9 +142,17 @@ int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g);
 // double-float copy of the interiors of the listed blocks of an FP64 buffer
 // (push: same-level ghost copies as in the stage kernel, or null)
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
-                          int Bs0, int Bs1, int Bs2, const int *push, cudaStream_t s);
+                          int Bs0, int Bs1, int Bs2, const int *push, const BlockDesc *desc, const TreeClock *clk,
+                          cudaStream_t s);
+// anchoring constant of the FP32-pipe stage inputs (TreeClock::anchor_M):
+// reset of the running max, and the constant from the state (scan) or from
+// the running max an interior upload merged
+cudaError_t launch_umax_reset(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
+cudaError_t launch_anchor_from_state(const int *slots, int nblk, const double *A, BufGeo ga, int nc, int Bx, int By,
+                                     int Bz, const BlockDesc *desc, TreeClock *clk, const int *trees, int ntrees,
+                                     int scan, cudaStream_t s);
 cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
-                              int order_predictor, cudaStream_t s);
+                              int order_predictor, const BlockDesc *desc, const TreeClock *clk, cudaStream_t s);
 cudaError_t launch_rhs_only(int variant, int dim, const int *blk, int nblk, const BlockDesc *desc,
                             const TreeParams *tp, const double *in, BufGeo gin, double *rhs, const double *mask,
                             int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s);
@@ -156,7 +170,7 @@ cudaError_t launch_sphere_fill(const int4 *cand, const int *slot, int n, const S
                                float2 *mask_df, double c_eta_inv, cudaStream_t s);
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
-                      const int *trees, cudaStream_t s);
+                      const int *trees, cudaStream_t s, int step_start = 0);
 cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
 // max |u| per component over the interiors of the listed blocks (Bs2 = 1 in 2-D)
 cudaError_t launch_norm_linf(const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int nc,
@@ -164,8 +178,8 @@ cudaError_t launch_norm_linf(const int *blk, int nblk, const double *u, BufGeo g
 // interior exchange state <-> compact array, one CTA row per (block,
 // component); towards the state optionally also the double-float copy B
 // (thin layout gt) with its same-level ghost pushes
-cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, void *B, BufGeo gt,
-                                 int nc, int Bx, int By, int Bz, const int *push, int to_state, cudaStream_t s);
+cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, int nc, int Bx,
+                                 int By, int Bz, int to_state, const BlockDesc *desc, TreeClock *clk, cudaStream_t s);
 cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
                                  int Bx, int By, int Bz, int to_full, cudaStream_t s);
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,

@@ -103,6 +103,65 @@ __device__ __forceinline__ df2 df_split(double v) {
     return {hi, lo};
 }
 
+// ---------------------------------------------------------------------------
+// Anchored double-float values. Every hi part is a multiple of one quantum q
+// with |hi| <= 2^20 q at the start of a step (2^22 q leaves room for values
+// that double within the step and for interpolated ghost values above their
+// coarse data), so a sum of up to four hi parts with factors of one or two
+// is an exact FP32 operation, and
+// the lo parts (|lo| <= q/2, 24 bits below that) carry the rest. A stencil
+// difference A - B or second difference A + B - 2u then costs two FP32
+// instructions (hi exact, lo rounded about 2^-43 of the largest value)
+// instead of an error-free double-float addition; only the final weighted
+// combination of two such differences needs a two-sum.
+// ---------------------------------------------------------------------------
+
+// round v's hi part to the quantum of M = 1.5 * 2^23 * q (exact: v.hi - h is
+// the rounding residue); M = 0 leaves v as it is
+__device__ __forceinline__ df2 anchor(df2 v, float M) {
+    const float h = (v.hi + M) - M;
+    return {h, (v.hi - h) + v.lo};
+}
+
+// M for a state whose largest magnitude has the float bits umax_bits: the
+// quantum is 2^-20 of the power of two above the maximum; 0 (no anchoring)
+// for a zero state or a quantum outside the normal float range
+__host__ __device__ inline float anchor_constant(unsigned umax_bits) {
+    const int be = (int)((umax_bits >> 23) & 0xffu);
+    if (be == 0 || be == 0xff) return 0.f;
+    const int E = be - 127 + 1;               // max|u| < 2^E, q = 2^(E-20)
+    if (E - 20 < -126 || E + 3 > 127) return 0.f;
+    union { unsigned u; float f; } m;
+    m.u = ((unsigned)(E + 3 + 127) << 23) | 0x400000u;   // 1.5 * 2^(E+3) = 1.5 * 2^23 * q
+    return m.f;
+}
+
+// the double nearest hi + lo of a normalised pair (|lo| <= ulp(hi)/2), formed
+// on the integer units: the two significands are aligned in one 53-bit
+// integer (at most one bit of lo below the double's last place is cut);
+// zero, subnormal, inf or nan hi parts take the FP64 units
+__device__ __forceinline__ double df_to_double(df2 x) {
+    const unsigned hb = __float_as_uint(x.hi), lb = __float_as_uint(x.lo);
+    const int he = (int)((hb >> 23) & 0xffu);
+    if (he == 0 || he == 0xff) return __dadd_rn((double)x.hi, (double)x.lo);
+    long long S = (long long)((hb & 0x7fffffu) | 0x800000u) << 29;   // unit 2^(e(hi) - 52)
+    const int le = (int)((lb >> 23) & 0xffu);
+    if (le != 0) {
+        const int sh = le - he + 29;
+        const long long ml = (long long)((lb & 0x7fffffu) | 0x800000u);
+        const long long Y = sh >= 0 ? (ml << sh) : (sh > -24 ? (ml >> -sh) : 0LL);
+        S = ((hb ^ lb) >> 31) ? S - Y : S + Y;
+    }
+    int e = he - 127 + 1023;
+    if (S < (1LL << 52)) {   // lo of the other sign took the leading bit
+        S <<= 1;
+        e -= 1;
+    }
+    const unsigned long long bits = ((unsigned long long)(hb >> 31) << 63) | ((unsigned long long)e << 52) |
+                                    ((unsigned long long)S & 0xfffffffffffffULL);
+    return __longlong_as_double((long long)bits);
+}
+
 // float -> double (exact) by bit manipulation; zero, subnormal, inf and nan
 // inputs go through the conversion unit
 __device__ __forceinline__ double f2d_bits(float f) {

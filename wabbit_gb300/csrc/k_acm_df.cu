@@ -29,7 +29,7 @@ struct StageArgsDF {
     const int *blk;
     const BlockDesc *desc;
     const TreeParams *tp;
-    const TreeClock *clk;
+    TreeClock *clk;        // per tree: dt weights, anchoring constant, running max (stage 4)
     const float2 *in;      // stage input (thin layout, ghosts synchronised)
     const float2 *u0;      // double-float copy of u_n (thin layout)
     float2 *out;           // next stage input; at stage 4 the copy of u_{n+1}
@@ -86,12 +86,14 @@ __device__ __forceinline__ void push_ghosts(const int *push, int b, int ix, int 
 }
 
 // The per-block and per-tree constants of a stage, loaded once per thread:
-// stencil weights (BlockDesc), physics (TreeParams) and the RK weights of the
-// stage from the tree's clock.
+// stencil weights (BlockDesc), physics (TreeParams), the RK weights of the
+// stage from the tree's clock and the anchoring constant of the stage input
+// this stage writes.
 struct DfConst {
-    df2 s1[3], s2[3], sc;      // 1/(12 dx), nu/(12 dx^2), -30 sum s2
+    df2 s1[3], s2[3];          // 1/(12 dx), nu/(12 dx^2)
     df2 c0sq, gamma, umean[3];
     df2 db, da;                // dt * b_j, dt * a_(j+1) of the stage
+    float M;                   // anchoring constant of the tree (TreeClock::anchor_M)
     int sponge;
 };
 
@@ -105,23 +107,43 @@ __device__ __forceinline__ DfConst load_const(const StageArgsDF &a, const BlockD
         k.s2[i] = cf(d.fs2[i]);
         k.umean[i] = cf(tp.f_umean[i]);
     }
-    k.sc = cf(d.fsc);
     k.c0sq = cf(tp.f_c0sq);
     k.gamma = cf(tp.f_gamma);
     k.sponge = tp.use_sponge;
+    k.M = ck.anchor_M;
     const int j = a.stage;
     k.db = (j == 1 || j == 4) ? cf(ck.f_dt6) : cf(ck.f_dt3);
     k.da = j == 3 ? cf(ck.f_dt) : df_pow2(cf(ck.f_dt), 0.5f);
     return k;
 }
 
-// RHS of one interior point from a stencil input with strides stv (shared or
-// global memory). m: the point's double-float mask words (stride ms), or
-// null. Returns the RHS in r and the centre values vel, p0.
+// Stencil numerators of anchored inputs (df.cuh) as double-float pairs:
+// the neighbour differences / second differences are formed part by part
+// (hi parts exact), their weighted combination by one two-sum.
+//   first derivative  8 (A - B) - (E - F)               A, B at +-1, E, F at +-2
+//   second derivative 16 (A + B - 2u) - (E + F - 2u)     = 16 (A + B) - (E + F) - 30 u
+__device__ __forceinline__ df2 num1(float2 A, float2 B, float2 E, float2 F) {
+    const float dh = A.x - B.x, dl = A.y - B.y;
+    const float eh = E.x - F.x, el = E.y - F.y;
+    const df2 s = two_sum(8.f * dh, -eh);
+    return {s.hi, s.lo + fmaf(8.f, dl, -el)};
+}
+
+__device__ __forceinline__ df2 num2(float2 A, float2 B, float2 E, float2 F, float2 u2) {
+    const float ah = (A.x + B.x) - u2.x, al = (A.y + B.y) - u2.y;
+    const float bh = (E.x + F.x) - u2.x, bl = (E.y + F.y) - u2.y;
+    const df2 s = two_sum(16.f * ah, -bh);
+    return {s.hi, s.lo + fmaf(16.f, al, -bl)};
+}
+
+// RHS of one interior point (convective FD_4th_central, RHS_3D_acm /
+// RHS_2D_acm, rhs_ACM.f90:578-615,1206-1256, with the penalisation and the
+// sponge of :1734-1753) from an anchored stencil input with strides stv
+// (shared or global memory). m: the point's double-float mask words (stride
+// ms), or null. Returns the RHS in r and the centre values vel, p0.
 template <int DIM, bool MASK, typename Idx>
 __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3], const DfConst &d,
-                                       const float2 *m, int ms, df2 r[DIM + 1], df2 vel[DIM],
-                                       df2 &p0) {
+                                       const float2 *m, int ms, df2 r[DIM + 1], df2 vel[DIM], df2 &p0) {
     df2 w[DIM];
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
@@ -132,16 +154,19 @@ __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3]
 #pragma unroll
     for (int c = 0; c < DIM; c++) {
         const float2 *uc = u + c * cs;
-        df2 adv = {0.f, 0.f};
-        df2 lap = df_mul_nr(d.sc, vel[c]);                // -30 u sum nu/(12 dx^2)
+        const float2 u2 = make_float2(2.f * vel[c].hi, 2.f * vel[c].lo);
+        df2 adv = {0.f, 0.f}, lap = {0.f, 0.f};
 #pragma unroll
         for (int k = 0; k < DIM; k++) {
-            const df2 A = ld(uc + stv[k]), B = ld(uc - stv[k]), E = ld(uc + 2 * stv[k]), F = ld(uc - 2 * stv[k]);
-            const df2 d1 = df_sub_nr(df_pow2(df_sub_nr(A, B), 8.f), df_sub_nr(E, F));
-            adv = df_add_nr(adv, df_mul_nr(w[k], d1));
-            if (k == c) div = df_add_nr(div, df_mul_nr(d.s1[k], d1));
-            const df2 l = df_sub_nr(df_pow2(df_add_nr(A, B), 16.f), df_add_nr(E, F));
-            lap = df_add_nr(lap, df_mul_nr(d.s2[k], l));
+            const float2 A = uc[stv[k]], B = uc[-stv[k]], E = uc[2 * stv[k]], F = uc[-2 * stv[k]];
+            const df2 d1 = num1(A, B, E, F);
+            const df2 ta = df_mul_nr(w[k], d1), tl = df_mul_nr(d.s2[k], num2(A, B, E, F, u2));
+            adv = k == 0 ? ta : df_add_nr(adv, ta);
+            lap = k == 0 ? tl : df_add_nr(lap, tl);
+            if (k == c) {
+                const df2 td = df_mul_nr(d.s1[k], d1);
+                div = c == 0 ? td : df_add_nr(div, td);
+            }
         }
         r[c] = df_sub_nr(lap, adv);
     }
@@ -149,8 +174,7 @@ __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3]
     p0 = ld(up);
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
-        const df2 A = ld(up + stv[k]), B = ld(up - stv[k]), E = ld(up + 2 * stv[k]), F = ld(up - 2 * stv[k]);
-        const df2 d1 = df_sub_nr(df_pow2(df_sub_nr(A, B), 8.f), df_sub_nr(E, F));
+        const df2 d1 = num1(up[stv[k]], up[-stv[k]], up[2 * stv[k]], up[-2 * stv[k]]);
         r[k] = df_sub_nr(r[k], df_mul_nr(d.s1[k], d1));
     }
     r[DIM] = df_neg(df_add_nr(df_mul_nr(d.c0sq, div), df_mul_nr(d.gamma, p0)));
@@ -210,11 +234,14 @@ __device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int q, int 
 
 // RK4 stage update of one point (runge_kutta_generic.f90:60-154): b = 1/6,
 // 1/3, 1/3, 1/6; the stage inputs are u_n + dt/2 k1, u_n + dt/2 k2,
-// u_n + dt k3. q: interior index; (ix, iy, iz): interior coordinates; off:
-// the point's offset in the thin buffers (component 0).
+// u_n + dt k3, written anchored. The increment is kept unnormalised between
+// stages. Stage 4 forms u_n+1 = u_n + increment with one FP64 addition per
+// value and returns the largest |u_n+1| of the point in umax. q: interior
+// index; (ix, iy, iz): interior coordinates; off: the point's offset in the
+// thin buffers (component 0).
 template <int DIM>
 __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, int b, int q, int ix, int iy, int iz,
-                                      long long off, const df2 r[DIM + 1], const RkIn<DIM> &in) {
+                                      long long off, const df2 r[DIM + 1], const RkIn<DIM> &in, float &umax) {
     const int npts_int = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
     const long long cs = a.gt.npts();
     const int j = a.stage;
@@ -228,8 +255,8 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
         for (int c = 0; c <= DIM; c++) {
             const df2 rc = df_norm(r[c]);
             const df2 inc = df_mul_nr(db, rc);
-            st(acc + c * npts_int, df_norm(j == 1 ? inc : df_add_nr({in.acc[c].x, in.acc[c].y}, inc)));
-            const df2 v = df_norm(df_add_nr({in.u0[c].x, in.u0[c].y}, df_mul_nr(da, rc)));
+            st(acc + c * npts_int, j == 1 ? inc : df_add_nr({in.acc[c].x, in.acc[c].y}, inc));
+            const df2 v = anchor(df_add_nr({in.u0[c].x, in.u0[c].y}, df_mul_nr(da, rc)), k.M);
             ov[c] = make_float2(v.hi, v.lo);
             o[c * cs] = ov[c];
         }
@@ -241,14 +268,28 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
             const df2 inc = df_norm(df_add_nr({in.acc[c].x, in.acc[c].y}, df_mul_nr(db, df_norm(r[c]))));
-            const double v = __dadd_rn(__dadd_rn(f2_bits(in.u0[c]), f2d_bits(inc.hi)), f2d_bits(inc.lo));
+            const double v = __dadd_rn(f2_bits(in.u0[c]), df_to_double(inc));
             un[c * us] = v;
-            const df2 w = df_split(v);
+            const df2 w = anchor(df_split(v), k.M);
             ov[c] = make_float2(w.hi, w.lo);
             o[c * cs] = ov[c];
+            umax = fmaxf(umax, fabsf(w.hi));
         }
     }
     if (a.push) push_ghosts<DIM, DIM + 1>(a.push, b, ix, iy, iz, a.Bs0, a.Bs1, a.Bs2, a.gt, a.out, cs, ov);
+}
+
+// block-wide max of umax merged into the tree's running max (stage 4);
+// every thread of the CTA calls it
+__device__ __forceinline__ void merge_umax(float umax, TreeClock *clk, int tree) {
+    __shared__ float red[32];
+    for (int o = 16; o; o >>= 1) umax = fmaxf(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = umax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) umax = fmaxf(umax, red[w]);
+        atomicMax(&clk[tree].umax_f, __float_as_uint(umax));
+    }
 }
 
 // One thread per interior point, stencil values read from global memory.
@@ -261,22 +302,25 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
     const int chunks = BS ? (npts_int + 255) / 256 : a.chunks;
     const int bi = blockIdx.x / chunks;
     const int q = (blockIdx.x - bi * chunks) * blockDim.x + threadIdx.x;
-    if (q >= npts_int) return;
     const int b = a.blk[bi];
     const BlockDesc &d = a.desc[b];
-    const int ix = q % Bs0, iy = (q / Bs0) % Bs1, iz = DIM == 3 ? q / (Bs0 * Bs1) : 0;
-    const long long cs = a.gt.npts();
-    const long long off = (long long)b * (DIM + 1) * cs +
-                          ((long long)(iz + (DIM == 3 ? a.gt.gb : 0)) * a.gt.ny + (iy + a.gt.gb)) * a.gt.nx +
-                          (ix + a.gt.gb);
-    const int stv[3] = {1, a.gt.nx, a.gt.nx * a.gt.ny};
-    const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
-    df2 r[DIM + 1], vel[DIM], p0;
-    const DfConst k = load_const(a, d);
-    rhs_df<DIM, MASK>(a.in + off, cs, stv, k, m, npts_int, r, vel, p0);
-    RkIn<DIM> in;
-    rk_load<DIM>(a, b, q, ix, iy, iz, off, in);
-    rk_df<DIM>(a, k, b, q, ix, iy, iz, off, r, in);
+    float umax = 0.f;
+    if (q < npts_int) {
+        const int ix = q % Bs0, iy = (q / Bs0) % Bs1, iz = DIM == 3 ? q / (Bs0 * Bs1) : 0;
+        const long long cs = a.gt.npts();
+        const long long off = (long long)b * (DIM + 1) * cs +
+                              ((long long)(iz + (DIM == 3 ? a.gt.gb : 0)) * a.gt.ny + (iy + a.gt.gb)) * a.gt.nx +
+                              (ix + a.gt.gb);
+        const int stv[3] = {1, a.gt.nx, a.gt.nx * a.gt.ny};
+        const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
+        df2 r[DIM + 1], vel[DIM], p0;
+        const DfConst k = load_const(a, d);
+        rhs_df<DIM, MASK>(a.in + off, cs, stv, k, m, npts_int, r, vel, p0);
+        RkIn<DIM> in;
+        rk_load<DIM>(a, b, q, ix, iy, iz, off, in);
+        rk_df<DIM>(a, k, b, q, ix, iy, iz, off, r, in, umax);
+    }
+    if (a.stage == 4) merge_umax(umax, a.clk, d.tree);
 }
 
 // 3-D blocks of 16x16xBs2 points with 2 ghost layers (the stage-input
@@ -286,7 +330,9 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
 // one TMA box per component into shared memory; every thread then walks its
 // (x, y) column through the slab, reading all stencil values from shared
 // memory at compile-time offsets. A TMA completion that does not arrive
-// within a second sets *err and ends the CTA.
+// within a second on any thread sets *err and ends the CTA after giving the
+// copy in flight a second bounded wait; the context's state is then
+// undefined.
 template <bool MASK, int ZT>
 __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const __grid_constant__ CUtensorMap tin,
                                                             int nslab, int *err) {
@@ -315,10 +361,16 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
     // first plane's while the TMA load is in flight)
     RkIn<3> nxt;
     rk_load<3>(a, b, (zb * BS + iy) * BS + ix, ix, iy, zb, boff + (long long)(zb + GB) * PLANE, nxt);
-    if (!mbar_wait(&bar, 0, 1000000000ull)) {
-        if (threadIdx.x == 0) atomicExch(err, 1);
+    // the decision to go on is the CTA's, so every thread meets the barriers
+    // below or none does
+    if (!__syncthreads_and(mbar_wait(&bar, 0, 1000000000ull))) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, 1);
+            mbar_wait(&bar, 0, 1000000000ull);
+        }
         return;
     }
+    float umax = 0.f;
 #pragma unroll 1
     for (int k = 0; k < ZT; k++) {
         const int iz = zb + k;
@@ -330,8 +382,9 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
         const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
         df2 r[4], vel[3], p0;
         rhs_df<3, MASK>(u, COMP, stv, kc, m, npts_int, r, vel, p0);
-        rk_df<3>(a, kc, b, q, ix, iy, iz, off, r, cur);
+        rk_df<3>(a, kc, b, q, ix, iy, iz, off, r, cur, umax);
     }
+    if (a.stage == 4) merge_umax(umax, a.clk, d.tree);
 }
 
 // slab height of the tile kernel (0: not applicable): 16x16 planes, two
@@ -342,7 +395,7 @@ int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g) {
 }
 
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
-                                const TreeParams *tp, const TreeClock *clk, const void *in, const void *u0,
+                                const TreeParams *tp, TreeClock *clk, const void *in, const void *u0,
                                 void *out, BufGeo gt, double *un, BufGeo gun, void *acc, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int *err,
                                 cudaStream_t s) {
@@ -402,9 +455,10 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     return cudaGetLastError();
 }
 
-// double-float copy (df_split) of the interiors of the listed blocks
+// anchored double-float copy (df_split, then the tree's quantum) of the
+// interiors of the listed blocks
 __global__ void shadow_kernel(const int *blk, int nblk, const double *src, BufGeo gs, float2 *dst, BufGeo gd, int nc,
-                              int Bx, int By, int Bz, const int *push) {
+                              int Bx, int By, int Bz, const int *push, const BlockDesc *desc, const TreeClock *clk) {
     const long long nint = (long long)Bx * By * Bz;
     const long long total = (long long)nblk * nc * nint;
     const int zs = gs.nz > 1 ? gs.gb : 0, zd = gd.nz > 1 ? gd.gb : 0;
@@ -416,7 +470,7 @@ __global__ void shadow_kernel(const int *blk, int nblk, const double *src, BufGe
         const int ix = (int)(r % Bx), iy = (int)((r / Bx) % By), iz = (int)(r / ((long long)Bx * By));
         const double v = src[((long long)b * nc + c) * gs.npts() + ((long long)(iz + zs) * gs.ny + (iy + gs.gb)) * gs.nx +
                              (ix + gs.gb)];
-        const df2 w = df_split(v);
+        const df2 w = anchor(df_split(v), clk[desc[b].tree].anchor_M);
         const float2 f = make_float2(w.hi, w.lo);
         float2 *dc = dst + (long long)c * gd.npts();
         dc[(long long)b * nc * gd.npts() + ((long long)(iz + zd) * gd.ny + (iy + gd.gb)) * gd.nx + (ix + gd.gb)] = f;
@@ -429,16 +483,17 @@ __global__ void shadow_kernel(const int *blk, int nblk, const double *src, BufGe
 
 // Interior exchange with a compact array (nblk, nc, Bz, By, Bx): one CTA
 // row per (block, component), 32-bit index arithmetic. Towards the state it
-// also writes the double-float copy of the FP32-pipe precision (and its
-// same-level ghost pushes), so no separate shadow pass is needed.
+// also merges max |u| into the tree's running max (clk, when given), from
+// which the anchored copy of the FP32-pipe precision takes its quantum.
 __global__ void __launch_bounds__(256) interior_xfer_kernel(const int *__restrict__ slots, double *compact, double *A,
-                                                            BufGeo ga, float2 *B, BufGeo gt, int nc, int Bx, int By,
-                                                            int Bz, const int *push, int to_state) {
+                                                            BufGeo ga, int nc, int Bx, int By, int Bz, int to_state,
+                                                            const BlockDesc *desc, TreeClock *clk) {
     const int b = slots[blockIdx.x], c = blockIdx.y;
     const int nint = Bx * By * Bz;
     double *cp = compact + ((long long)blockIdx.x * nc + c) * nint;
     double *ab = A + ((long long)b * nc + c) * ga.npts();
-    const int za = ga.nz > 1 ? ga.gb : 0, zt = gt.nz > 1 ? gt.gb : 0;
+    const int za = ga.nz > 1 ? ga.gb : 0;
+    float umax = 0.f;
     for (int i = threadIdx.x; i < nint; i += blockDim.x) {
         const int ix = i % Bx, iy = (i / Bx) % By, iz = i / (Bx * By);
         double *pa = ab + ((long long)(iz + za) * ga.ny + (iy + ga.gb)) * ga.nx + (ix + ga.gb);
@@ -448,32 +503,72 @@ __global__ void __launch_bounds__(256) interior_xfer_kernel(const int *__restric
         }
         const double v = cp[i];
         *pa = v;
-        if (B) {
-            const df2 w = df_split(v);
-            const float2 f = make_float2(w.hi, w.lo);
-            float2 *dc = B + (long long)c * gt.npts();
-            dc[(long long)b * nc * gt.npts() + ((long long)(iz + zt) * gt.ny + (iy + gt.gb)) * gt.nx + (ix + gt.gb)] = f;
-            if (push) {
-                if (gt.nz > 1) push_ghosts<3, 1>(push, b, ix, iy, iz, Bx, By, Bz, gt, dc, gt.npts() * nc, &f);
-                else push_ghosts<2, 1>(push, b, ix, iy, iz, Bx, By, Bz, gt, dc, gt.npts() * nc, &f);
-            }
-        }
+        umax = fmaxf(umax, fabsf(df_split(v).hi));
     }
+    if (to_state && clk) merge_umax(umax, clk, desc[b].tree);
 }
 
-cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, void *B, BufGeo gt,
-                                 int nc, int Bx, int By, int Bz, const int *push, int to_state, cudaStream_t s) {
+// max |u| over the interiors of the listed blocks (all components) merged
+// into the trees' running max: the quantum of a state that changed outside
+// an RK step
+__global__ void __launch_bounds__(256) umax_state_kernel(const int *__restrict__ slots, const double *A, BufGeo ga,
+                                                         int nc, int Bx, int By, int Bz, const BlockDesc *desc,
+                                                         TreeClock *clk) {
+    const int b = slots[blockIdx.x], c = blockIdx.y;
+    const int nint = Bx * By * Bz;
+    const double *ab = A + ((long long)b * nc + c) * ga.npts();
+    const int za = ga.nz > 1 ? ga.gb : 0;
+    float umax = 0.f;
+    for (int i = threadIdx.x; i < nint; i += blockDim.x) {
+        const int ix = i % Bx, iy = (i / Bx) % By, iz = i / (Bx * By);
+        umax = fmaxf(umax, fabsf(df_split(ab[((long long)(iz + za) * ga.ny + (iy + ga.gb)) * ga.nx + (ix + ga.gb)]).hi));
+    }
+    merge_umax(umax, clk, desc[b].tree);
+}
+
+__global__ void umax_reset_kernel(TreeClock *clk, const int *trees, int ntrees) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ntrees) clk[trees[i]].umax_f = 0u;
+}
+
+__global__ void anchor_set_kernel(TreeClock *clk, const int *trees, int ntrees) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ntrees) clk[trees[i]].anchor_M = anchor_constant(clk[trees[i]].umax_f);
+}
+
+// the anchoring constant of the listed trees from their state: the running
+// max is reset, then (scan) rebuilt from A's interiors or (no scan) taken
+// from what an interior upload merged since the reset
+cudaError_t launch_umax_reset(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s) {
+    umax_reset_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_anchor_from_state(const int *slots, int nblk, const double *A, BufGeo ga, int nc, int Bx, int By,
+                                     int Bz, const BlockDesc *desc, TreeClock *clk, const int *trees, int ntrees,
+                                     int scan, cudaStream_t s) {
+    if (scan) {
+        cudaError_t e = launch_umax_reset(clk, trees, ntrees, s);
+        if (e != cudaSuccess) return e;
+        if (nblk > 0) umax_state_kernel<<<dim3(nblk, nc), 256, 0, s>>>(slots, A, ga, nc, Bx, By, Bz, desc, clk);
+    }
+    anchor_set_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, int nc, int Bx,
+                                 int By, int Bz, int to_state, const BlockDesc *desc, TreeClock *clk, cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
-    interior_xfer_kernel<<<dim3(nblk, nc), 256, 0, s>>>(slots, compact, A, ga, reinterpret_cast<float2 *>(B), gt, nc,
-                                                        Bx, By, Bz, push, to_state);
+    interior_xfer_kernel<<<dim3(nblk, nc), 256, 0, s>>>(slots, compact, A, ga, nc, Bx, By, Bz, to_state, desc, clk);
     return cudaGetLastError();
 }
 
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
-                          int Bs0, int Bs1, int Bs2, const int *push, cudaStream_t s) {
+                          int Bs0, int Bs1, int Bs2, const int *push, const BlockDesc *desc, const TreeClock *clk,
+                          cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
     shadow_kernel<<<1024, 256, 0, s>>>(blk, nblk, src, gs, reinterpret_cast<float2 *>(dst), gd, nc, Bs0, Bs1, Bs2,
-                                       push);
+                                       push, desc, clk);
     return cudaGetLastError();
 }
 

@@ -128,7 +128,7 @@ __global__ void dt_reset_kernel(TreeClock *clk, const int *trees, int ntrees) {
 }
 
 // calculate_time_step.f90:28-118 after the MIN reduction
-__global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const int *trees, int ntrees) {
+__global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const int *trees, int ntrees, int step_start) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ntrees) return;
     const int t = trees[i];
@@ -161,6 +161,13 @@ __global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const i
     c.f_dt3[1] = f3.lo;
     c.f_dt6[0] = f6.hi;
     c.f_dt6[1] = f6.lo;
+    // at the start of an RK step: the quantum of the stage inputs this step
+    // writes, from the largest |u| the previous step wrote (unchanged if none
+    // was recorded, e.g. in the FP64 precision)
+    if (step_start) {
+        if (c.umax_f) c.anchor_M = anchor_constant(c.umax_f);
+        c.umax_f = 0u;
+    }
 }
 
 __global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntrees) {
@@ -173,13 +180,13 @@ __global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntree
 
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
-                      const int *trees, cudaStream_t s) {
+                      const int *trees, cudaStream_t s, int step_start) {
     dt_reset_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
     if (nblk > 0) {
         if (dim == 2) dt_kernel<2><<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2);
         else dt_kernel<3><<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2);
     }
-    dt_finalize_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(tp, clk, trees, ntrees);
+    dt_finalize_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(tp, clk, trees, ntrees, step_start);
     return cudaGetLastError();
 }
 

@@ -229,9 +229,11 @@ __device__ __forceinline__ df2 interp_df(const float2 *v, int stride, int first)
 
 template <int NCOEF>
 __global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict__ patches, float2 *buf, BufGeo geo,
-                                                         int nc, int cg) {
+                                                         int nc, int cg, const BlockDesc *desc, const TreeClock *clk) {
     extern __shared__ float2 sf[];
     const Patch p = patches[blockIdx.x];
+    // the receiver's stage input is anchored to its tree's quantum
+    const float M = clk[desc[p.dst].tree].anchor_M;
     const int cx = p.shi[0] - p.slo[0] + 1, cy = p.shi[1] - p.slo[1] + 1, cz = p.shi[2] - p.slo[2] + 1;
     const int Fx = 2 * cx - 1, Fy = 2 * cy - 1, Fz = 2 * cz - 1;
     constexpr int h = NCOEF - 1;
@@ -300,8 +302,10 @@ __global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict
                 const df2 r = interp_df<NCOEF>(pl, ex * ey, (fz - h - zw0) >> 1);
                 v = make_float2(r.hi, r.lo);
             }
+            const df2 va = anchor({v.x, v.y}, M);
             buf[((long long)p.dst * nc + c0 + c) * npts +
-                ((long long)(p.rlo[2] + kk) * geo.ny + (p.rlo[1] + j)) * geo.nx + (p.rlo[0] + ix)] = v;
+                ((long long)(p.rlo[2] + kk) * geo.ny + (p.rlo[1] + j)) * geo.nx + (p.rlo[0] + ix)] =
+                make_float2(va.hi, va.lo);
         }
         __syncthreads();
     }
@@ -331,7 +335,7 @@ cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_double
 }
 
 cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
-                              int order_predictor, cudaStream_t s) {
+                              int order_predictor, const BlockDesc *desc, const TreeClock *clk, cudaStream_t s) {
     if (npatch <= 0) return cudaSuccess;
     // as many components per pass as fit the shared memory of one CTA
     const size_t per = sizeof(float2) * (size_t)max_smem_doubles;
@@ -353,7 +357,7 @@ cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_dou
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
             if (e != cudaSuccess) return e;
         }
-        kern<<<npatch, 256, smem, s>>>(patches, b, geo, nc, cg);
+        kern<<<npatch, 256, smem, s>>>(patches, b, geo, nc, cg, desc, clk);
         return cudaGetLastError();
     };
     switch (order_predictor) {
