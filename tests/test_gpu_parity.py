@@ -228,8 +228,9 @@ def test_threshold_flags_bitexact(dim, wavelet, grids2d, grids3d):
 @pytest.mark.parametrize("penal", [0, 1])
 def test_rk4_fp32_pipe_path_within_tolerance(dim, wavelet, penal, grids2d, grids3d):
     """Double-float stencils, stage arithmetic, ghost prediction and
-    penalisation on the FP32 units, FP64 state: relative L2 <= 1e-12 per step
-    against the FP64 oracle. The ghost nodes go through the pushed same-level
+    penalisation on the FP32 units, FP64 state: the relative L2 difference to
+    the FP64 oracle grows by at most 3e-13 per step (the anchored stage
+    inputs carry about 2^-44 of the state's largest magnitude). The ghost nodes go through the pushed same-level
     copies and the restriction / prediction stages (CDF40: two sync stages,
     CDF44: three)."""
     cfg = small_cfg(dim, wavelet, Bs=8 if wavelet == "CDF40" else 12, skew=0, penal=penal,
@@ -260,7 +261,7 @@ def test_rk4_fp32_pipe_path_within_tolerance(dim, wavelet, penal, grids2d, grids
             # that differ by rounding, so they may differ in the last bits
             assert dt == dt_ref if step == 0 else abs(dt - dt_ref) <= 1e-12 * dt_ref
             err = rel_l2(interior(cfg, f.download()), interior(cfg, o.data()))
-            assert err < 1e-12, (step, err)
+            assert err < 3e-13 * (step + 1), (step, err)
 
 
 def test_fp32_pipe_rejects_skew_symmetric():

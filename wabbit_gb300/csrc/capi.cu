@@ -213,12 +213,12 @@ struct wg_ctx {
     int max_blocks = 0;
     BufGeo gA, gT;                      // full and thin layouts
     long long nint = 0;                 // interior points per block
-    double *A = nullptr, *B = nullptr, *C = nullptr, *D = nullptr, *acc = nullptr;
+    double *A = nullptr, *B = nullptr, *C = nullptr, *D = nullptr, *E = nullptr, *acc = nullptr;
     double *mask = nullptr;
     float2 *mask_df = nullptr;
     int *d_push = nullptr;              // per slot 27 same-level receivers (FP32-pipe precision)
     std::vector<int> h_push;
-    CUtensorMap tm[3];                  // TMA maps over B, C, D (3-D FP32-pipe precision)
+    CUtensorMap tm[4];                  // TMA maps over B, C, D, E (3-D FP32-pipe precision)
     bool have_tm = false;
     int stage_form = WG_FORM_AUTO;      // requested form of the FP32-pipe stage kernel
     int tuned_form = 0;                 // the autotuner's choice (0: not tuned yet)
@@ -635,8 +635,15 @@ int stage_launch(wg_ctx *ctx, Tree &t, int stage, const double *in, BufGeo gin, 
     return WG_OK;
 }
 
-// u0 is always B (the double-float copy of u_n); with push the kernels also
-// write the same-level ghost copies of out
+// the TMA map over a thin stage buffer
+static const void *in_map(wg_ctx *ctx, const double *in) {
+    return in == ctx->B ? &ctx->tm[0] : in == ctx->C ? &ctx->tm[1] : in == ctx->D ? &ctx->tm[2]
+         : in == ctx->E ? &ctx->tm[3] : nullptr;
+}
+
+// u0 is always B (the anchored copy of u_n), the inputs of stages 2 and 3
+// are C and D; with push the kernels also write the same-level ghost copies
+// of out
 int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *out, bool push) {
     const int dim = ctx->cfg.dim;
     const int *Bs = ctx->cfg.Bs;
@@ -644,17 +651,17 @@ int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *o
     const void *tm = nullptr;
     const int form = ctx->stage_form != WG_FORM_AUTO ? ctx->stage_form : ctx->tuned_form ? ctx->tuned_form : WG_FORM_DIRECT;
     if (ctx->have_tm && form == WG_FORM_TILE)
-        tm = in == ctx->B ? &ctx->tm[0] : in == ctx->C ? &ctx->tm[1] : in == ctx->D ? &ctx->tm[2] : nullptr;
+        tm = in_map(ctx, in);
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, t.d_plain.p, t.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
-                                   Bs[2], tm, ctx->d_err, ctx->stream));
+                                   ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
+                                   Bs[1], Bs[2], tm, ctx->d_err, ctx->stream));
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, t.d_masked.p, t.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
-                                   Bs[2], tm, ctx->d_err, ctx->stream));
+                                   ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
+                                   Bs[1], Bs[2], tm, ctx->d_err, ctx->stream));
     return WG_OK;
 }
 
-// TMA maps over the three thin double-float buffers: a 3-D tensor of 8-byte
+// TMA maps over the four thin double-float buffers: a 3-D tensor of 8-byte
 // elements (x, y, plane-of-all-blocks-and-components), box nx * ny * (zt+4)
 int make_tensor_maps(wg_ctx *ctx) {
     const int zt = tile_slab(ctx->cfg.dim, ctx->cfg.Bs[0], ctx->cfg.Bs[1], ctx->cfg.Bs[2], ctx->gT.gb);
@@ -675,8 +682,8 @@ int make_tensor_maps(wg_ctx *ctx) {
     const cuuint64_t strides[2] = {(cuuint64_t)g.nx * 8, (cuuint64_t)g.nx * g.ny * 8};
     const cuuint32_t box[3] = {(cuuint32_t)g.nx, (cuuint32_t)g.ny, (cuuint32_t)(zt + 4)};
     const cuuint32_t estr[3] = {1, 1, 1};
-    double *bufs[3] = {ctx->B, ctx->C, ctx->D};
-    for (int i = 0; i < 3; i++) {
+    double *bufs[4] = {ctx->B, ctx->C, ctx->D, ctx->E};
+    for (int i = 0; i < 4; i++) {
         const CUresult r = reinterpret_cast<Encode>(fn)(&ctx->tm[i], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, bufs[i], dims,
                                                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -783,9 +790,9 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true, push))) return st;
     if ((st = stage_launch_df(ctx, t, 2, ctx->C, ctx->D, push))) return st;
     if ((st = run_sync(ctx, t, ctx->D, true, g_rhs, g_rhs, true, push))) return st;
-    if ((st = stage_launch_df(ctx, t, 3, ctx->D, ctx->C, push))) return st;
-    if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true, push))) return st;
-    if ((st = stage_launch_df(ctx, t, 4, ctx->C, ctx->B, push))) return st;
+    if ((st = stage_launch_df(ctx, t, 3, ctx->D, ctx->E, push))) return st;
+    if ((st = run_sync(ctx, t, ctx->E, true, g_rhs, g_rhs, true, push))) return st;
+    if ((st = stage_launch_df(ctx, t, 4, ctx->E, ctx->B, push))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
     return WG_OK;
 }
@@ -896,13 +903,13 @@ int stage_launch_batch(wg_ctx *ctx, int stage, const double *in, double *out) {
     const void *tm = nullptr;
     const int form = ctx->stage_form != WG_FORM_AUTO ? ctx->stage_form : ctx->tuned_form ? ctx->tuned_form : WG_FORM_DIRECT;
     if (ctx->have_tm && form == WG_FORM_TILE)
-        tm = in == ctx->B ? &ctx->tm[0] : in == ctx->C ? &ctx->tm[1] : in == ctx->D ? &ctx->tm[2] : nullptr;
+        tm = in_map(ctx, in);
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, bp.plain.p, bp.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
-                                   Bs[2], tm, ctx->d_err, ctx->stream));
+                                   ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
+                                   Bs[1], Bs[2], tm, ctx->d_err, ctx->stream));
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, bp.masked.p, bp.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->B, out, ctx->gT, ctx->A, ctx->gA, ctx->acc, ctx->mask_df, pp, Bs[0], Bs[1],
-                                   Bs[2], tm, ctx->d_err, ctx->stream));
+                                   ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
+                                   Bs[1], Bs[2], tm, ctx->d_err, ctx->stream));
     return WG_OK;
 }
 
@@ -919,9 +926,9 @@ int rk4_enqueue_batch(wg_ctx *ctx) {
     if ((st = run_sync_batch(ctx, ctx->C))) return st;
     if ((st = stage_launch_batch(ctx, 2, ctx->C, ctx->D))) return st;
     if ((st = run_sync_batch(ctx, ctx->D))) return st;
-    if ((st = stage_launch_batch(ctx, 3, ctx->D, ctx->C))) return st;
-    if ((st = run_sync_batch(ctx, ctx->C))) return st;
-    if ((st = stage_launch_batch(ctx, 4, ctx->C, ctx->B))) return st;
+    if ((st = stage_launch_batch(ctx, 3, ctx->D, ctx->E))) return st;
+    if ((st = run_sync_batch(ctx, ctx->E))) return st;
+    if ((st = stage_launch_batch(ctx, 4, ctx->E, ctx->B))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, bp.tree_ids.p, (int)bp.trees.size(), ctx->stream));
     return WG_OK;
 }
@@ -994,8 +1001,10 @@ size_t wg_bytes_per_block(const wg_config *c) {
     const long long nT = (long long)(c->Bs[0] + 2 * c->g_rhs) * (c->Bs[1] + 2 * c->g_rhs) *
                          (c->dim == 3 ? c->Bs[2] + 2 * c->g_rhs : 1);
     const long long nI = (long long)c->Bs[0] * c->Bs[1] * (c->dim == 3 ? c->Bs[2] : 1);
-    const long long nbuf = c->rhs_precision == WG_RHS_FP32 ? 3 : 2;   // thin buffers B, C (, D)
-    return sizeof(double) * (size_t)c->neq * (size_t)(nA + nbuf * nT + nI) + sizeof(BlockDesc);
+    // FP64: thin buffers B, C and the interior RK accumulator; FP32-pipe:
+    // thin buffers B, C, D, E (u_n copy and the stage inputs 2-4)
+    const bool df = c->rhs_precision == WG_RHS_FP32;
+    return sizeof(double) * (size_t)c->neq * (size_t)(nA + (df ? 4 : 2) * nT + (df ? 0 : nI)) + sizeof(BlockDesc);
 }
 
 int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
@@ -1029,8 +1038,9 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
         return fail(WG_ECUDA, "constant-memory set-up failed");
     }
     auto alloc = [&](double **p, size_t n) { return cudaMalloc(p, n) == cudaSuccess; };
-    if (!alloc(&ctx->A, bytesA) || !alloc(&ctx->B, bytesT) || !alloc(&ctx->C, bytesT) || !alloc(&ctx->acc, bytesI) ||
-        (ctx->precision == WG_RHS_FP32 && !alloc(&ctx->D, bytesT))) {
+    const bool df = ctx->precision == WG_RHS_FP32;
+    if (!alloc(&ctx->A, bytesA) || !alloc(&ctx->B, bytesT) || !alloc(&ctx->C, bytesT) ||
+        (!df && !alloc(&ctx->acc, bytesI)) || (df && (!alloc(&ctx->D, bytesT) || !alloc(&ctx->E, bytesT)))) {
         cudaGetLastError();
         wg_ctx_destroy(ctx.release());
         return fail(WG_ENOMEM, "device allocation of %d blocks failed", max_blocks);
@@ -1046,6 +1056,7 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
     cudaMemsetAsync(ctx->B, 0, bytesT, ctx->stream);
     cudaMemsetAsync(ctx->C, 0, bytesT, ctx->stream);
     if (ctx->D) cudaMemsetAsync(ctx->D, 0, bytesT, ctx->stream);
+    if (ctx->E) cudaMemsetAsync(ctx->E, 0, bytesT, ctx->stream);
     if (ctx->precision == WG_RHS_FP32) {
         if (cudaMalloc(&ctx->d_push, sizeof(int) * 27 * (size_t)max_blocks) != cudaSuccess) {
             cudaGetLastError();
@@ -1088,6 +1099,7 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->B);
     cudaFree(ctx->C);
     cudaFree(ctx->D);
+    cudaFree(ctx->E);
     cudaFree(ctx->acc);
     cudaFree(ctx->mask);
     cudaFree(ctx->mask_df);

@@ -126,13 +126,14 @@ cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, in
 // err: set to 1 by a CTA whose TMA load did not complete within a second;
 // push: per slot 27 same-level receiver slots whose ghost copies the kernel
 // writes along with its output, or null):
-// in, u0 and out are float2 (hi, lo) buffers of layout gt, u0 the copy of
-// u_n; acc (float2, interior) accumulates dt*sum b_j k_j; stage 4 adds it to
-// un (FP64) and writes the copy of u_{n+1} to out; maskdf holds 5 float2
-// words per point (chi/C_eta with colour applied, u_s, sponge/C_sponge)
+// in, u0, s2, s3 and out are float2 (hi, lo) buffers of layout gt: in the
+// stage's input, u0 the anchored copy of u_n, s2 / s3 the inputs of stages
+// 2 and 3 (read by stage 4); stage 4 adds the increment to un (FP64) and
+// writes the copy of u_{n+1} to out; maskdf holds 5 float2 words per point
+// (chi/C_eta with colour applied, u_s, sponge/C_sponge)
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
-                                const TreeParams *tp, TreeClock *clk, const void *in, const void *u0,
-                                void *out, BufGeo gt, double *un, BufGeo gun, void *acc, const void *maskdf,
+                                const TreeParams *tp, TreeClock *clk, const void *in, const void *u0, const void *s2,
+                                const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int *err,
                                 cudaStream_t s);
 // slab height of the TMA tile form of the double-float stage kernel (3-D,

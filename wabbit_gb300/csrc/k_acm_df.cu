@@ -9,13 +9,21 @@
 //   du/dx   = (8 (u+1 - u-1) - (u+2 - u-2)) / (12 dx)
 //   d2u/dx2 = (16 (u+1 + u-1) - (u+2 + u-2) - 30 u) / (12 dx^2)
 // with the integer weights applied exactly (powers of two) and the 1/(12 dx)
-// scalings applied once per term. The RK accumulator holds only the
-// increment dt * sum b_j k_j (runge_kutta_generic.f90:60-154), in
-// double-float; the state u_n stays FP64 and receives the increment in one
-// FP64 addition per value at stage 4, so the state carries full FP64
-// resolution while stages 1-3 issue no FP64 instruction. Penalisation and
-// sponge use the double-float mask (chi/C_eta with the colour applied, u_s,
-// sponge/C_sponge) built by the host from hvy_mask.
+// scalings applied once per term. The stage inputs are anchored (df.cuh), so
+// neighbour differences are exact FP32 operations.
+//
+// RK4 (runge_kutta_generic.f90:60-154 with the classic tableau) without an
+// increment register: the stage inputs s2 = u_n + dt/2 k1, s3 = u_n + dt/2 k2
+// and s4 = u_n + dt k3 stay in their own buffers, and stage 4 forms
+//   u_n+1 = u_n + [(s2 - u_n) + 2 (s3 - u_n) + (s4 - u_n)] / 3 + dt/6 k4,
+// the reference's dt (k1/6 + k2/3 + k3/3 + k4/6) regrouped, with one FP64
+// addition per value into the FP64 state. Stage 1 takes u_n from the centre
+// of its own stencil input, stages 2 and 3 read the copy of u_n, stage 4
+// reads s2, s3 and u_n: per point and step 2 + 3 reads and 3 + 2 writes of
+// interior values beside the stencil slabs, and no read-modify-write of an
+// accumulator. Penalisation and sponge use the double-float mask
+// (chi/C_eta with the colour applied, u_s, sponge/C_sponge) built by the
+// host from hvy_mask.
 //
 // Compiled with -fmad=false: the error-free transformations must not be
 // contracted; every FMA is explicit.
@@ -30,18 +38,19 @@ struct StageArgsDF {
     const BlockDesc *desc;
     const TreeParams *tp;
     TreeClock *clk;        // per tree: dt weights, anchoring constant, running max (stage 4)
-    const float2 *in;      // stage input (thin layout, ghosts synchronised)
-    const float2 *u0;      // double-float copy of u_n (thin layout)
+    const float2 *in;      // stage input s_j (thin layout, ghosts synchronised)
+    const float2 *u0;      // anchored copy of u_n = s1 (thin layout)
+    const float2 *s2, *s3; // stage inputs 2 and 3 (thin layout; read by stage 4)
     float2 *out;           // next stage input; at stage 4 the copy of u_{n+1}
     BufGeo gt;
     double *un;            // u_n, FP64 (full layout)
     BufGeo gun;
-    float2 *acc;           // increment, interior only
     const float2 *mask;    // 5 words per point, interior only
     const int *push;       // same-level ghost copies pushed by the writer, or null
     int Bs0, Bs1, Bs2;
     int stage;
     int chunks;
+    float third[2];        // 1/3 as a double-float pair
 };
 
 __device__ __forceinline__ df2 ld(const float2 *p) {
@@ -122,10 +131,12 @@ __device__ __forceinline__ DfConst load_const(const StageArgsDF &a, const BlockD
 // (hi parts exact), their weighted combination by one two-sum.
 //   first derivative  8 (A - B) - (E - F)               A, B at +-1, E, F at +-2
 //   second derivative 16 (A + B - 2u) - (E + F - 2u)     = 16 (A + B) - (E + F) - 30 u
+// In num1 8 dh - eh is exact unless it exceeds 2^24 q, which needs
+// |8 dh| > 2^23 q >= |eh|; the quick two-sum is therefore exact.
 __device__ __forceinline__ df2 num1(float2 A, float2 B, float2 E, float2 F) {
     const float dh = A.x - B.x, dl = A.y - B.y;
     const float eh = E.x - F.x, el = E.y - F.y;
-    const df2 s = two_sum(8.f * dh, -eh);
+    const df2 s = quick_two_sum(8.f * dh, -eh);
     return {s.hi, s.lo + fmaf(8.f, dl, -el)};
 }
 
@@ -193,12 +204,10 @@ __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3]
 }
 
 // Per-point operands of the RK4 stage update that come from memory: the
-// copy of u_n (stages 1-3) or the bits of u_n itself (stage 4), and the
-// increment.
+// copy of u_n (stages 2, 3), or s2, s3 and the bits of u_n (stage 4).
 template <int DIM>
 struct RkIn {
-    float2 u0[DIM + 1];
-    float2 acc[DIM + 1];
+    float2 a[DIM + 1], b[DIM + 1], c[DIM + 1];
 };
 
 __device__ __forceinline__ float2 bits_f2(double v) {
@@ -210,53 +219,45 @@ __device__ __forceinline__ double f2_bits(float2 v) {
     return __longlong_as_double((long long)(((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x)));
 }
 
-template <int DIM>
-__device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int q, int ix, int iy, int iz, long long off,
+template <int DIM, int STAGE>
+__device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int ix, int iy, int iz, long long off,
                                         RkIn<DIM> &in) {
-    const int npts_int = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
     const long long cs = a.gt.npts();
-    const float2 *acc = a.acc + (long long)b * (DIM + 1) * npts_int + q;
-    if (a.stage > 1)
+    if (STAGE == 2 || STAGE == 3) {
 #pragma unroll
-        for (int c = 0; c <= DIM; c++) in.acc[c] = acc[c * npts_int];
-    if (a.stage < 4) {
-#pragma unroll
-        for (int c = 0; c <= DIM; c++) in.u0[c] = a.u0[off + c * cs];
-    } else {
+        for (int c = 0; c <= DIM; c++) in.a[c] = a.u0[off + c * cs];
+    } else if (STAGE == 4) {
         const long long us = a.gun.npts();
         const double *un = a.un + (long long)b * (DIM + 1) * us +
                            ((long long)(iz + (DIM == 3 ? a.gun.gb : 0)) * a.gun.ny + (iy + a.gun.gb)) * a.gun.nx +
                            (ix + a.gun.gb);
 #pragma unroll
-        for (int c = 0; c <= DIM; c++) in.u0[c] = bits_f2(un[c * us]);
+        for (int c = 0; c <= DIM; c++) {
+            in.a[c] = a.s2[off + c * cs];
+            in.b[c] = a.s3[off + c * cs];
+            in.c[c] = bits_f2(un[c * us]);
+        }
     }
 }
 
-// RK4 stage update of one point (runge_kutta_generic.f90:60-154): b = 1/6,
-// 1/3, 1/3, 1/6; the stage inputs are u_n + dt/2 k1, u_n + dt/2 k2,
-// u_n + dt k3, written anchored. The increment is kept unnormalised between
-// stages. Stage 4 forms u_n+1 = u_n + increment with one FP64 addition per
-// value and returns the largest |u_n+1| of the point in umax. q: interior
-// index; (ix, iy, iz): interior coordinates; off: the point's offset in the
-// thin buffers (component 0).
-template <int DIM>
-__device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, int b, int q, int ix, int iy, int iz,
-                                      long long off, const df2 r[DIM + 1], const RkIn<DIM> &in, float &umax) {
-    const int npts_int = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
+// RK4 stage update of one point: stages 1-3 write the anchored next stage
+// input u_n + a dt k_j (a = 1/2, 1/2, 1), stage 4 writes u_n+1 to the FP64
+// state and its anchored copy, and returns the largest |u_n+1| of the point
+// in umax. ctr: the centre values of this stage's input (s1 = u_n at stage
+// 1, s4 at stage 4). (ix, iy, iz): interior coordinates; off: the point's
+// offset in the thin buffers (component 0).
+template <int DIM, int STAGE>
+__device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, int b, int ix, int iy, int iz,
+                                      long long off, const df2 r[DIM + 1], const df2 ctr[DIM + 1],
+                                      const RkIn<DIM> &in, float &umax) {
     const long long cs = a.gt.npts();
-    const int j = a.stage;
-    const df2 db = k.db;
-    float2 *acc = a.acc + (long long)b * (DIM + 1) * npts_int + q;
     float2 *o = a.out + off;
     float2 ov[DIM + 1];
-    if (j < 4) {
-        const df2 da = k.da;
+    if (STAGE < 4) {
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
-            const df2 rc = df_norm(r[c]);
-            const df2 inc = df_mul_nr(db, rc);
-            st(acc + c * npts_int, j == 1 ? inc : df_add_nr({in.acc[c].x, in.acc[c].y}, inc));
-            const df2 v = anchor(df_add_nr({in.u0[c].x, in.u0[c].y}, df_mul_nr(da, rc)), k.M);
+            const df2 u0 = STAGE == 1 ? ctr[c] : df2{in.a[c].x, in.a[c].y};
+            const df2 v = anchor(df_add_nr(u0, df_mul_nr(k.da, df_norm(r[c]))), k.M);
             ov[c] = make_float2(v.hi, v.lo);
             o[c * cs] = ov[c];
         }
@@ -265,12 +266,20 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
         double *un = a.un + (long long)b * (DIM + 1) * us +
                      ((long long)(iz + (DIM == 3 ? a.gun.gb : 0)) * a.gun.ny + (iy + a.gun.gb)) * a.gun.nx +
                      (ix + a.gun.gb);
+        const df2 third = {a.third[0], a.third[1]};
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
-            const df2 inc = df_norm(df_add_nr({in.acc[c].x, in.acc[c].y}, df_mul_nr(db, df_norm(r[c]))));
-            const double v = __dadd_rn(f2_bits(in.u0[c]), df_to_double(inc));
+            const double u = f2_bits(in.c[c]);
+            const df2 ud = df_split(u);
+            // s2 + 2 s3 + s4: the three inputs of this step share one quantum,
+            // so the hi sum is exact; then - 4 u_n as a double-float difference
+            const float sh = fmaf(2.f, in.b[c].x, in.a[c].x + ctr[c].hi);
+            const float sl = fmaf(2.f, in.b[c].y, in.a[c].y + ctr[c].lo);
+            const df2 sum = df_sub_nr({sh, sl}, df_pow2(ud, 4.f));
+            const df2 inc = df_norm(df_add_nr(df_mul_nr(third, sum), df_mul_nr(k.db, df_norm(r[c]))));
+            const double v = __dadd_rn(u, df_to_double(inc));
             un[c * us] = v;
-            const df2 w = anchor(df_split(v), k.M);
+            const df2 w = anchor(df_add_nr(ud, inc), k.M);
             ov[c] = make_float2(w.hi, w.lo);
             o[c * cs] = ov[c];
             umax = fmaxf(umax, fabsf(w.hi));
@@ -295,6 +304,17 @@ __device__ __forceinline__ void merge_umax(float umax, TreeClock *clk, int tree)
 // One thread per interior point, stencil values read from global memory.
 // BS: the block edge when all Bs are equal to it (index arithmetic by
 // shifts), 0 for the general case.
+template <int DIM, bool MASK, int STAGE>
+__device__ __forceinline__ void direct_point(const StageArgsDF &a, const DfConst &k, const float2 *u, long long cs,
+                                             const int stv[3], const float2 *m, int ms, int b, int ix, int iy, int iz,
+                                             long long off, float &umax) {
+    df2 r[DIM + 1], ctr[DIM + 1];
+    RkIn<DIM> in;
+    rk_load<DIM, STAGE>(a, b, ix, iy, iz, off, in);
+    rhs_df<DIM, MASK>(u, cs, stv, k, m, ms, r, ctr, ctr[DIM]);
+    rk_df<DIM, STAGE>(a, k, b, ix, iy, iz, off, r, ctr, in, umax);
+}
+
 template <int DIM, bool MASK, int BS>
 __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
     const int Bs0 = BS ? BS : a.Bs0, Bs1 = BS ? BS : a.Bs1, Bs2 = BS ? BS : a.Bs2;
@@ -313,12 +333,14 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
                               (ix + a.gt.gb);
         const int stv[3] = {1, a.gt.nx, a.gt.nx * a.gt.ny};
         const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
-        df2 r[DIM + 1], vel[DIM], p0;
         const DfConst k = load_const(a, d);
-        rhs_df<DIM, MASK>(a.in + off, cs, stv, k, m, npts_int, r, vel, p0);
-        RkIn<DIM> in;
-        rk_load<DIM>(a, b, q, ix, iy, iz, off, in);
-        rk_df<DIM>(a, k, b, q, ix, iy, iz, off, r, in, umax);
+        const float2 *u = a.in + off;
+        switch (a.stage) {
+            case 1: direct_point<DIM, MASK, 1>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
+            case 2: direct_point<DIM, MASK, 2>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
+            case 3: direct_point<DIM, MASK, 3>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
+            default: direct_point<DIM, MASK, 4>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
+        }
     }
     if (a.stage == 4) merge_umax(umax, a.clk, d.tree);
 }
@@ -333,7 +355,7 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
 // within a second on any thread sets *err and ends the CTA after giving the
 // copy in flight a second bounded wait; the context's state is then
 // undefined.
-template <bool MASK, int ZT>
+template <bool MASK, int ZT, int STAGE>
 __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const __grid_constant__ CUtensorMap tin,
                                                             int nslab, int *err) {
     constexpr int NX = 20, NY = 20, GB = 2, BS = 16;
@@ -360,7 +382,7 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
     // the memory operands of the RK update are fetched one plane ahead (the
     // first plane's while the TMA load is in flight)
     RkIn<3> nxt;
-    rk_load<3>(a, b, (zb * BS + iy) * BS + ix, ix, iy, zb, boff + (long long)(zb + GB) * PLANE, nxt);
+    rk_load<3, STAGE>(a, b, ix, iy, zb, boff + (long long)(zb + GB) * PLANE, nxt);
     // the decision to go on is the CTA's, so every thread meets the barriers
     // below or none does
     if (!__syncthreads_and(mbar_wait(&bar, 0, 1000000000ull))) {
@@ -377,14 +399,14 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
         const int q = (iz * BS + iy) * BS + ix;
         const long long off = boff + (long long)(iz + GB) * PLANE;
         const RkIn<3> cur = nxt;
-        if (k + 1 < ZT) rk_load<3>(a, b, q + BS * BS, ix, iy, iz + 1, off + PLANE, nxt);
+        if (k + 1 < ZT) rk_load<3, STAGE>(a, b, ix, iy, iz + 1, off + PLANE, nxt);
         const float2 *u = sm + ((k + 2) * NY + (iy + GB)) * NX + (ix + GB);
         const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
-        df2 r[4], vel[3], p0;
-        rhs_df<3, MASK>(u, COMP, stv, kc, m, npts_int, r, vel, p0);
-        rk_df<3>(a, kc, b, q, ix, iy, iz, off, r, cur, umax);
+        df2 r[4], ctr[4];
+        rhs_df<3, MASK>(u, COMP, stv, kc, m, npts_int, r, ctr, ctr[3]);
+        rk_df<3, STAGE>(a, kc, b, ix, iy, iz, off, r, ctr, cur, umax);
     }
-    if (a.stage == 4) merge_umax(umax, a.clk, d.tree);
+    if (STAGE == 4) merge_umax(umax, a.clk, d.tree);
 }
 
 // slab height of the tile kernel (0: not applicable): 16x16 planes, two
@@ -395,11 +417,12 @@ int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g) {
 }
 
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
-                                const TreeParams *tp, TreeClock *clk, const void *in, const void *u0,
-                                void *out, BufGeo gt, double *un, BufGeo gun, void *acc, const void *maskdf,
+                                const TreeParams *tp, TreeClock *clk, const void *in, const void *u0, const void *s2,
+                                const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int *err,
                                 cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
+    if (stage < 1 || stage > 4) return cudaErrorInvalidValue;
     StageArgsDF a;
     a.blk = blk;
     a.desc = desc;
@@ -407,23 +430,35 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.clk = clk;
     a.in = reinterpret_cast<const float2 *>(in);
     a.u0 = reinterpret_cast<const float2 *>(u0);
+    a.s2 = reinterpret_cast<const float2 *>(s2);
+    a.s3 = reinterpret_cast<const float2 *>(s3);
     a.out = reinterpret_cast<float2 *>(out);
     a.gt = gt;
     a.un = un;
     a.gun = gun;
-    a.acc = reinterpret_cast<float2 *>(acc);
     a.mask = reinterpret_cast<const float2 *>(maskdf);
     a.push = push;
     a.Bs0 = Bs0;
     a.Bs1 = Bs1;
     a.Bs2 = Bs2;
     a.stage = stage;
+    {
+        const double t = 1.0 / 3.0;
+        a.third[0] = (float)t;
+        a.third[1] = (float)(t - (double)a.third[0]);
+    }
     const int zt = tmap ? tile_slab(dim, Bs0, Bs1, Bs2, gt.gb) : 0;
     if (zt == 4 && gt.nx == 20 && gt.ny == 20) {
         const int nslab = Bs2 / zt;
         const size_t smem = sizeof(float2) * 4 * (size_t)(zt + 4) * gt.nx * gt.ny;
         const CUtensorMap &map = *reinterpret_cast<const CUtensorMap *>(tmap);
-        auto kern = masked ? acm_stage_df_tile<true, 4> : acm_stage_df_tile<false, 4>;
+        using K = void (*)(StageArgsDF, const CUtensorMap, int, int *);
+        static const K kerns[2][4] = {
+            {acm_stage_df_tile<false, 4, 1>, acm_stage_df_tile<false, 4, 2>, acm_stage_df_tile<false, 4, 3>,
+             acm_stage_df_tile<false, 4, 4>},
+            {acm_stage_df_tile<true, 4, 1>, acm_stage_df_tile<true, 4, 2>, acm_stage_df_tile<true, 4, 3>,
+             acm_stage_df_tile<true, 4, 4>}};
+        const K kern = kerns[masked ? 1 : 0][stage - 1];
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         a.chunks = 0;
