@@ -18,9 +18,14 @@ e2e:   the same through the C ABI with host buffers: every step uploads the
 plain_fp64: the plain per-solve FP64 path on the same grid and IC (one
        wg_rk4_step call per step, no graph), its speed and the relative L2
        difference of the two states after K steps.
-roofline: the RK-stage kernel timed alone (CUDA events, mean over launches)
-       against the measured HBM copy bandwidth; for the FP64 precision also
-       its FP64 rate against the FP64 FMA peak measured in the same run.
+roofline: the RK-stage kernels against the measured HBM copy bandwidth:
+       algorithmic bytes of one stage (5 state vectors, the ghost halo and the
+       mask of masked blocks per point) over the mean device time of the four
+       stages' kernels in profiled steps (CUDA events between the kernel
+       groups). traffic: DRAM bytes of the stage kernels measured in the run
+       by a one-pass ncu capture of the same workload at Jmax=5, scaled to the
+       full grid by points. For the FP64 precision also the FP64 rate against
+       the FP64 FMA peak measured in the same run.
 cpu_baseline: the CPU oracle (a scalar C++ restatement of the reference's
        Fortran, OpenMP over blocks) on a bounded sample of the same physics.
 
@@ -31,6 +36,7 @@ bit) on the same metric.
 import argparse
 import json
 import os
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -67,8 +73,17 @@ def parse():
     ap.add_argument("--rate", type=float, default=8.0, help="serving: Poisson arrival rate (requests/s)")
     ap.add_argument("--requests", type=int, default=256, help="serving: number of requests")
     ap.add_argument("--budget-gb", type=float, default=160.0, help="serving: HBM budget of the arenas")
+    ap.add_argument("--serving-requests", type=int, default=24,
+                    help="default workload: requests of the short serving stream run after it (0: none)")
     ap.add_argument("--adapt-every", type=int, default=5,
                     help="serving: adaptation cycle length in steps (0: no adaptation)")
+    ap.add_argument("--stage-form", default="auto",
+                    help="FP32-pipe stage kernel form: auto (timed per RK stage), direct, tile, march, or four "
+                         "comma-separated forms for RK stages 1-4")
+    ap.add_argument("--traffic", choices=["auto", "off"], default="auto",
+                    help="measure the stage kernels' DRAM bytes with a one-pass ncu capture (dram__bytes_read/"
+                         "write) of one RK4 step of the workload at Jmax=5, scaled to the full grid by points")
+    ap.add_argument("--traffic-case", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--compare-plain", choices=["auto", "on", "off"], default="auto",
                     help="also time the plain per-solve FP64 path (one wg_rk4_step call per step, no graph) "
                          "and report the speed-up and the L2 difference of the two after K steps "
@@ -172,57 +187,186 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(workload):
-    """dram bytes per stage launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", f"acm_stage_{workload}.md")
+def set_forms(ctx, spec):
+    """Apply a --stage-form value to a context."""
+    if "," in spec:
+        ctx.set_stage_forms(spec.split(","))
+    else:
+        ctx.set_stage_form(spec)
+
+
+TRAFFIC_JMAX = 5
+
+
+def run_traffic_case(args):
+    """The small case the traffic capture profiles: the workload at Jmax=5,
+    the given stage forms, one RK4 step of batched launches without a graph
+    (each stage kernel launched for the unmasked and the masked block list).
+    Prints the grid's sizes as JSON."""
+    import torch
+    from wabbit_gb300 import build, workloads
+    from wabbit_gb300.solver import Context
+    build.build()
+    torch.cuda.set_device(0)
+    cfg, lv, co, u0, ids, masks = workloads.build(args.workload, jmax=TRAFFIC_JMAX)
+    ctx = Context(cfg, len(lv) + 16)
+    set_forms(ctx, args.stage_form)
+    f = ctx.forest()
+    f.set_grid(lv, co)
+    f.upload_interior(u0)
+    if masks is not None and len(ids):
+        f.set_mask_sparse(ids, masks)
+    f.set_time(0.0)
+    f.run(1, use_graph=False)
+    ctx.synchronize()
+    npts = len(lv) * int(np.prod([cfg.Bs[d] for d in range(cfg.dim)]))
+    print(json.dumps({"blocks": len(lv), "points": npts, "masked_blocks": f.stats()[1]}))
+    ctx.close()
+
+
+def measure_traffic(args, forms):
+    """DRAM bytes of each RK stage's kernels (unmasked + masked launch) per
+    interior point, from ncu on the small case (one pass: two DRAM counters
+    of one unit, 8 launches, no replay of device memory). The small case is
+    first run without ncu and must exit 0. Returns (per-stage bytes per
+    point, description) or (None, reason)."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--traffic-case", "--workload", args.workload,
+           "--stage-form", ",".join(forms)]
     try:
-        with open(p) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return float(line.split(":")[1])
-    except OSError:
-        pass
-    return None
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+    except subprocess.TimeoutExpired:
+        return None, "the small case did not finish without ncu"
+    if r.returncode != 0:
+        return None, "the small case failed without ncu: " + r.stderr.strip()[-200:]
+    info = json.loads(r.stdout.strip().splitlines()[-1])
+    ncu = shutil.which("ncu") or "/usr/local/cuda/bin/ncu"
+    if not os.path.exists(ncu):
+        return None, "ncu not found"
+    log = tempfile.NamedTemporaryFile(prefix="traffic", suffix=".csv", delete=False).name
+    ncmd = [ncu, "--metrics", "dram__bytes_read.sum,dram__bytes_write.sum", "--clock-control", "none",
+            "-k", "regex:acm_stage_df", "-c", "8", "--csv", "--print-units", "base", "--log-file", log] + cmd
+    try:
+        r = subprocess.run(ncmd, capture_output=True, text=True, timeout=900)
+    except subprocess.TimeoutExpired:
+        return None, "ncu capture did not finish"
+    if r.returncode != 0:
+        return None, "ncu failed: " + (r.stderr.strip() or r.stdout.strip())[-200:]
+    import csv
+    launches = {}
+    with open(log) as fh:
+        rows = [row for row in csv.reader(fh)]
+    hdr = None
+    for row in rows:
+        if row and row[0] == "ID":
+            hdr = row
+            continue
+        if hdr is None or len(row) != len(hdr):
+            continue
+        d = dict(zip(hdr, row))
+        if d.get("Metric Name") in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            launches.setdefault(int(d["ID"]), 0.0)
+            launches[int(d["ID"])] += float(d["Metric Value"].replace(",", ""))
+    os.unlink(log)
+    ids = sorted(launches)
+    if len(ids) != 8:
+        return None, f"expected 8 stage launches in the capture, got {len(ids)}"
+    per_stage = [(launches[ids[2 * j]] + launches[ids[2 * j + 1]]) / info["points"] for j in range(4)]
+    desc = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the 8 stage launches (unmasked + masked, "
+            f"RK stages 1-4) of one step of {args.workload} at Jmax={TRAFFIC_JMAX} ({info['blocks']} blocks, "
+            f"{info['masked_blocks']} masked), per interior point, scaled to the full grid by its points")
+    return per_stage, desc
 
 
 # --------------------------------------------------------------------- CPU
-def cpu_sample(workload, seconds=12.0, threads=None):
-    """Time the oracle on a bounded sample: the workload's physics on a
-    smaller grid (same block size, ghost width and mask), RK4 steps until
-    `seconds` of wall time have been spent."""
+def oracle_for(workload, jmax=None, threads=None):
+    """The oracle (the reference's algorithm restated in C++, OpenMP over
+    blocks in the ghost sync, RHS, RK update and dt) loaded with the
+    workload's grid, initial condition and sparse mask. Returns (oracle,
+    interior points)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     from wabbit_gb300 import workloads
-    cfg = workloads.make_config(workload)
-    small = cfg.copy()
-    small.Jmax = max(cfg.Jmin + 1, cfg.Jmax - 2)
-    lv, co = workloads.make_grid(workload, small)
-    u = workloads.initial_condition(workload, small, lv, co)
-    full = pyoracle.pad_blocks(small, u if small.dim == 3 else u[:, :, 0])
+    cfg, lv, co, u, ids, masks = workloads.build(workload, jmax=jmax)
     threads = threads or os.cpu_count() or 1
-    o = pyoracle.Oracle(small, threads=threads)
-    o.set_grid(lv, co, full)
-    if small.dim == 3 and small.penalization:
-        ids, masks = workloads.sphere_mask(small, lv, co)
-        m = np.zeros((len(lv), 6) + full.shape[2:])
-        if len(ids):
-            m[ids] = masks
-        o.set_mask(m)
-    npts = len(lv) * int(np.prod([small.Bs[d] for d in range(small.dim)]))
+    o = pyoracle.Oracle(cfg, threads=threads)
+    o.set_grid(lv, co, None)
+    o.set_interior(u)
+    del u
+    if masks is not None and len(ids):
+        o.set_mask_sparse(ids, masks)
+    npts = len(lv) * int(np.prod([cfg.Bs[d] for d in range(cfg.dim)]))
+    return o, npts, cfg, len(lv)
+
+
+def oracle_bytes(workload, jmax):
+    """Host bytes the oracle needs for the workload at jmax (state with g
+    ghost layers, five interior RK registers, the initial condition)."""
+    from wabbit_gb300 import workloads
+    cfg = workloads.make_config(workload)
+    cfg.Jmax = jmax
+    lv, _ = workloads.make_grid(workload, cfg)
+    dim = cfg.dim
+    full = int(np.prod([cfg.Bs[d] + 2 * cfg.g for d in range(dim)]))
+    inner = int(np.prod([cfg.Bs[d] for d in range(dim)]))
+    return 8.0 * len(lv) * cfg.neq * (full + 5 * inner + 2 * inner) * 1.15
+
+
+def host_mem_available():
+    """Bytes this process may still allocate: MemAvailable, capped by a
+    cgroup memory limit if one is set."""
+    avail = None
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    avail = float(line.split()[1]) * 1024
+    except OSError:
+        pass
+    try:
+        with open("/sys/fs/cgroup/memory.max") as f:
+            lim = f.read().strip()
+        with open("/sys/fs/cgroup/memory.current") as f:
+            cur = float(f.read().strip())
+        if lim != "max":
+            room = float(lim) - cur
+            avail = room if avail is None else min(avail, room)
+    except OSError:
+        pass
+    return avail
+
+
+def time_oracle(o, steps, warmup=1, seconds=None):
+    """Warm-up steps, then `steps` RK4 steps (or as many as fit in
+    `seconds`, at least one); returns (steps, wall seconds)."""
     t = 0.0
-    t, _ = o.step(t)  # warm-up
-    steps = 0
+    for _ in range(warmup):
+        t, _ = o.step(t)
+    n = 0
     t0 = time.perf_counter()
     while True:
         t, _ = o.step(t)
-        steps += 1
+        n += 1
         el = time.perf_counter() - t0
-        if el >= seconds or steps >= 200:
-            break
+        if (seconds is None and n >= steps) or (seconds is not None and (el >= seconds or n >= steps)):
+            return n, el
+
+
+def cpu_sample(workload, seconds=12.0, threads=None):
+    """Time the oracle on a bounded sample: the workload's physics on its
+    Jmax=5 grid (same block size, ghost width, IC and mask), RK4 steps on
+    all host cores until `seconds` of wall time have been spent; and the
+    one-core rate on the Jmax=4 grid."""
+    threads = threads or os.cpu_count() or 1
+    o, npts, cfg, nblk = oracle_for(workload, jmax=5, threads=threads)
+    steps, el = time_oracle(o, 200, 1, seconds)
     value = npts * steps / el
-    sample = (f"{workload} physics on its Jmax={small.Jmax} grid ({len(lv)} blocks, {npts} points), "
-              f"{steps} RK4 steps in {el:.1f} s")
-    return value, threads, sample, el / steps
+    del o
+    o1, npts1, _, nblk1 = oracle_for(workload, jmax=4, threads=1)
+    steps1, el1 = time_oracle(o1, 50, 1, seconds / 2)
+    sample = (f"{workload} physics (IC, mask, block size, ghosts) on its Jmax=5 grid ({nblk} blocks, {npts} "
+              f"points), {steps} RK4 steps in {el:.1f} s on {threads} threads; one core: Jmax=4 grid "
+              f"({nblk1} blocks), {steps1} steps in {el1:.1f} s")
+    return value, threads, sample, el / steps, npts1 * steps1 / el1
 
 
 # --------------------------------------------------------------------- GPU
@@ -243,6 +387,8 @@ def run_ours(args, rank, world):
     npts = nblk * npts_blk
     ctx = Context(cfg, nblk + 16)
     ctx.set_variant(args.variant == "fast")
+    if cfg.rhs_precision:
+        set_forms(ctx, args.stage_form)
     f = ctx.forest()
     f.set_grid(lv, co)
     f.upload_interior(u0)
@@ -276,21 +422,35 @@ def run_ours(args, rank, world):
     t_end, dt_last = f.time()  # raises if the run diverged
     value = sum_over_ranks(npts * args.steps / (ms * 1e-3), world)
 
-    # roofline of the RK-stage kernel, timed alone
-    stage_ms = f.time_kernel(0, reps=20)
-    sync_ms = f.time_kernel(1, reps=20)
-    dt_ms = f.time_kernel(2, reps=20)
-    mask_words = MASK_WORDS if cfg.rhs_precision == 0 else MASK_WORDS - 1   # the FP32-pipe mask folds the colour
-    bytes_stage = 8.0 * npts * cfg.neq * WORDS_PER_POINT_STAGE + 8.0 * nmasked * npts_blk * mask_words
+    # per-kernel-group device times of real steps (events between the
+    # groups, same launches as the graph), after the timed region
+    nprof = max(3, min(args.steps, 5))
+    prof = ctx.step_profile([f], nprof)
+    stage_ms = [prof[f"stage{j}"] for j in range(1, 5)]
+    mean_stage_ms = float(np.mean(stage_ms))
+    # algorithmic bytes of one stage launch (FP64 basis, fused ideal): 5 state
+    # vectors of neq words per interior point (stage input, u_n, accumulator
+    # read + write, next input), the ghost halo of the stage input read and
+    # its sync written ((Bs+2 g_rhs)^d - Bs^d per Bs^d, x 2 x neq words), and
+    # 5 mask words per point of the masked blocks
+    halo_w = (float(np.prod([cfg.Bs[d] + 2 * cfg.g_rhs for d in range(dim)])) - npts_blk) / npts_blk * 2 * cfg.neq
+    mask_bytes = 8.0 * nmasked * npts_blk * 5
+    bytes_interior = 8.0 * npts * cfg.neq * WORDS_PER_POINT_STAGE + mask_bytes
+    bytes_stage = bytes_interior + 8.0 * npts * halo_w
     flops_stage = float(FLOPS_PER_POINT_STAGE[dim]) * npts
     hbm_peak, hbm_src = measured_peaks()
-    fp64_peak, fp32_peak = probe_alu()
-    ach_gbs = bytes_stage / (stage_ms * 1e-3) / 1e9
-    ach_tf = flops_stage / (stage_ms * 1e-3) / 1e12
-    traffic = profile_traffic(args.workload)
-    form = ctx.stage_form() if cfg.rhs_precision else "direct"
+    ach_gbs = bytes_stage / (mean_stage_ms * 1e-3) / 1e9
+    ach_tf = flops_stage / (mean_stage_ms * 1e-3) / 1e12
+    form = ctx.stage_forms() if cfg.rhs_precision else ["direct"] * 4
+    kname = {"direct": "acm_stage_df_kernel", "tile": "acm_stage_df_tile (TMA slabs)",
+             "march": "acm_stage_df_march (TMA plane ring)"}
     stage_kernel = ("acm_stage_kernel (FP64)" if cfg.rhs_precision == 0 else
-                    "acm_stage_df_tile (TMA slabs)" if form == "tile" else "acm_stage_df_kernel")
+                    ", ".join(kname[x] for x in dict.fromkeys(form)))
+    traffic, traffic_src = None, "not measured (--traffic off)"
+    if args.traffic == "auto" and cfg.rhs_precision and rank == 0 and world == 1:
+        per_pt, traffic_src = measure_traffic(args, form)
+        if per_pt is not None:
+            traffic = {"per_stage": [v * npts for v in per_pt], "mean": float(np.mean(per_pt)) * npts}
 
     # e2e through the C ABI with host buffers
     e2e = None
@@ -328,8 +488,9 @@ def run_ours(args, rank, world):
 
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
-        v, cores, sample, _ = cpu_sample(args.workload)
-        cpu = {"value": v, "unit": "point-updates/s", "cores": cores, "kind": "port", "sample": sample}
+        v, cores, sample, _, v1 = cpu_sample(args.workload)
+        cpu = {"value": v, "unit": "point-updates/s", "cores": cores, "kind": "port", "sample": sample,
+               "one_core_value": v1}
 
     clocks = clk.summary()
     # bytes one RK stage touches (input, u_n copy, increment, next input)
@@ -352,25 +513,35 @@ def run_ours(args, rank, world):
             "wavelet": cfg.wavelet.decode(), "Jmax": cfg.Jmax, "blocks": nblk, "points": npts,
             "masked_blocks": nmasked, "levels": np.bincount(lv).tolist(), "variant": args.variant,
             "rhs_precision": "fp64" if cfg.rhs_precision == 0 else "fp32-pipe double-float",
-            "stage_form": form,
+            "stage_forms": form,
             "rk": "RK4", "graph": True,
             "l2": (f"stage buffers {state_gb:.1f} GB > 129 MB L2 (no flush needed)" if state_gb > 0.5 else
                    f"stage buffers {state_gb:.2f} GB: each stage streams more than L2 holds"),
             "parallelism": "replicas" if world > 1 else "1 GPU",
         },
         "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": ach_gbs / hbm_peak, "traffic": traffic, "kernel": stage_kernel,
-                     "launch_ms": stage_ms, "peak_source": hbm_src,
+                     "frac": ach_gbs / hbm_peak, "traffic": traffic["mean"] if traffic else None,
+                     "kernel": stage_kernel, "stage_forms": form,
+                     "launch_ms": mean_stage_ms, "launch_ms_per_stage": stage_ms, "peak_source": hbm_src,
                      "algorithmic_bytes_per_launch": bytes_stage,
-                     "bytes_per_point": "5 state words x neq x 8 B (stage input, u_n, increment read+write, "
-                                        "next input) + mask words of masked blocks"},
-        "kernels_ms": {"acm_stage": stage_ms, "sync_rhs": sync_ms, "dt": dt_ms},
+                     "bytes_per_point": (f"{WORDS_PER_POINT_STAGE} state words x neq (stage input, u_n, accumulator "
+                                         f"read + write, next input) + {halo_w:.2f} halo words (ghost layers read "
+                                         f"and written) per interior point, + 5 mask words per point of masked "
+                                         f"blocks; x 8 B"),
+                     "frac_interior_only": bytes_interior / (mean_stage_ms * 1e-3) / 1e9 / hbm_peak,
+                     "frac_per_stage": [bytes_stage / (t * 1e-3) / 1e9 / hbm_peak for t in stage_ms],
+                     "timing": f"mean of the 4 stage kernels over {nprof} profiled steps (CUDA events between "
+                               f"the kernel groups on the solver stream, after the timed region)",
+                     "traffic_per_stage": traffic["per_stage"] if traffic else None,
+                     "traffic_source": traffic_src},
+        "kernels_ms": prof,
         "gpu_launches": graph_kernels * args.steps,
         "clocks": clocks,
         "t_end": t_end,
         "dt_last": dt_last,
     }
     if cfg.rhs_precision == 0:
+        fp64_peak, fp32_peak = probe_alu()
         line["roofline_alu"] = {"bound": "fp64", "achieved": ach_tf, "peak": fp64_peak, "unit": "TFLOP/s",
                                 "frac": ach_tf / fp64_peak, "flops_per_launch": flops_stage,
                                 "peak_source": "FP64 FMA probe measured in this run (wg_probe_alu)",
@@ -381,9 +552,34 @@ def run_ours(args, rank, world):
         line["plain_fp64"] = plain
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    ctx.close()
+    if args.serving_requests > 0:
+        line["serving"] = serving_block(args, rank, world)
     if rank == 0:
         print(json.dumps(line))
-    ctx.close()
+
+
+def serving_block(args, rank, world):
+    """A short seeded serving stream after the stepper measurement (its
+    context closed): the serving workload's Poisson arrivals, 2-D and 3-D
+    solves of 50 RK4 steps adapted every 5 steps, each geometry served by
+    its own host thread; p50/p99 time to solution and aggregate
+    point-updates/s."""
+    import torch
+    from wabbit_gb300 import serving
+    stream = serving.make_stream(args.serving_requests, rate=args.rate, seed=4 + rank)
+    srv = serving.Server(budget_gb=min(args.budget_gb, 48.0), chunk=5, adapt_every=5)
+    srv.run([serving.Request(-1, 0.0, 2, 0, 1, 1e-3, nsteps=5), serving.Request(-2, 0.0, 3, 0, 2, 1e-3, nsteps=5)],
+            realtime=False)
+    torch.cuda.synchronize()
+    recs, summ = srv.run(stream, realtime=True)
+    srv.close()
+    return {"requests": summ["requests"], "arrival_rate_per_s": args.rate, "steps_per_solve": 50,
+            "adapt_every": 5, "value": sum_over_ranks(summ["point_updates"], world) / max_over_ranks(
+                summ["wall_s"], world), "unit": "point-updates/s", "p50_s": summ["p50_s"], "p99_s": summ["p99_s"],
+            "wall_s": summ["wall_s"], "phase_s": summ["phase_s"],
+            "note": "time to solution = arrival to result on the host; IC generated on the device at admission "
+                    "(inside the window); full stream: --workload serving --requests 256"}
 
 
 def compare_plain(args, cfg, lv, co, u0, ids, masks, f, ctx, value, npts):
@@ -727,30 +923,61 @@ def capi_graph_kernels(ctx):
     return int(capi.check(n))
 
 
+# the reference's own logged rate: TESTING/acm/3vortices/3vorticesEquiFD4_CDF40/
+# log.original.txt, "TOPLEVEL: time stepper" 2.630 s for the 3073 RK4 steps
+# (t = 10 -> 20) of 64 blocks of 32^2 points on 12 MPI ranks
+REF_LOG = {"value": 3073 * 64 * 32 * 32 / 2.630, "unit": "point-updates/s", "ranks": 12,
+           "case": "3vorticesEquiFD4_CDF40: 2-D, 64 blocks of 32^2, CDF40, FD4 skew-symmetric, RK4",
+           "source": "TESTING/acm/3vortices/3vorticesEquiFD4_CDF40/log.original.txt, TOPLEVEL: time stepper "
+                     "2.630 s over 3073 steps"}
+
+
+def oracle_on_log_case(threads, steps=400):
+    """The oracle on the case of the reference's log (the committed t = 10
+    state of 3vorticesEquiFD4_CDF40), point-updates/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from wabbit_gb300 import config
+    z = np.load(os.path.join(ROOT, "tests", "golden", "vortex2d_equi.npz"))
+    c = config.defaults(2)
+    c.Bs[0] = c.Bs[1] = 32
+    c.domain[0] = c.domain[1] = 6.283185307179586
+    c.wavelet = b"CDF40"
+    c.g, c.g_rhs = 3, 2
+    c.Jmin = c.Jmax = 3
+    c.c0, c.nu, c.gamma_p = 7.0, 5.0e-5, 1.0
+    c.skew_symmetry, c.penalization = 1, 0
+    c.CFL = 1.0
+    c.time_max, c.write_time = 20.0, 10.0
+    o = pyoracle.Oracle(c, threads=threads)
+    o.set_grid(z["level"], z["coords"], None)
+    o.set_interior(z["u_in"])
+    t = float(z["t_in"])
+    t, _ = o.step(t)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        t, _ = o.step(t)
+    return 64 * 32 * 32 * steps / (time.perf_counter() - t0)
+
+
 def run_reference(args, rank, world):
+    """The reference's CPU implementation of the path: the oracle (the
+    reference is Fortran and no Fortran compiler exists in this image; the
+    oracle reproduces the reference's regression outputs bit for bit) on the
+    same workload as the GPU arm -- grid, IC, mask -- with every host core,
+    W warm-up and K timed RK4 steps of the whole grid. If the host cannot
+    hold the workload, the largest Jmax that fits is used and the line says
+    so."""
     if rank != 0:
         return
     from wabbit_gb300 import workloads
-    cfg = workloads.make_config(args.workload)
-    # each bench step is one RK4 step of the oracle on the bounded sample
-    _, cores, sample, t_step = cpu_sample(args.workload, seconds=3.0)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    # time exactly K steps after W warm-up steps
-    import pyoracle
-    small = cfg.copy()
-    small.Jmax = max(cfg.Jmin + 1, cfg.Jmax - 2)
-    lv, co = workloads.make_grid(args.workload, small)
-    u = workloads.initial_condition(args.workload, small, lv, co)
-    full = pyoracle.pad_blocks(small, u if small.dim == 3 else u[:, :, 0])
-    o = pyoracle.Oracle(small, threads=cores)
-    o.set_grid(lv, co, full)
-    if small.dim == 3 and small.penalization:
-        ids, masks = workloads.sphere_mask(small, lv, co)
-        m = np.zeros((len(lv), 6) + full.shape[2:])
-        if len(ids):
-            m[ids] = masks
-        o.set_mask(m)
-    npts = len(lv) * int(np.prod([small.Bs[d] for d in range(small.dim)]))
+    cores = os.cpu_count() or 1
+    jmax_full = args.jmax if args.jmax is not None else workloads.make_config(args.workload).Jmax
+    jmax = jmax_full
+    avail = host_mem_available()
+    while avail is not None and jmax > 4 and oracle_bytes(args.workload, jmax) > 0.8 * avail:
+        jmax -= 1
+    o, npts, cfg, nblk = oracle_for(args.workload, jmax=jmax, threads=cores)
     t = 0.0
     for _ in range(args.warmup):
         t, _ = o.step(t)
@@ -758,20 +985,35 @@ def run_reference(args, rank, world):
     for _ in range(args.steps):
         t, _ = o.step(t)
     el = time.perf_counter() - t0
+    del o
     value = npts * args.steps / el
-    sample = (f"{args.workload} physics on its Jmax={small.Jmax} grid ({len(lv)} blocks, {npts} points), "
-              f"one RK4 step per bench step")
+    same = jmax == jmax_full
+    sample = (f"{args.workload} at Jmax={jmax} ({nblk} blocks, {npts} points, same grid, IC and mask as the GPU "
+              f"arm{'' if same else '; the full grid does not fit into host memory'}), {args.steps} RK4 steps of "
+              f"the whole grid per run, {cores} threads")
+    # one core, and the oracle on the case of the reference's own log
+    o1, npts1, _, nblk1 = oracle_for(args.workload, jmax=4, threads=1)
+    steps1, el1 = time_oracle(o1, 50, 1, 6.0)
+    del o1
+    log_all = oracle_on_log_case(cores)
+    log_12 = oracle_on_log_case(min(12, cores))
     line = {
         "metric": "ACM point-updates/s/GPU", "value": value, "unit": "point-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded IC and grid, see wabbit_gb300/workloads.py)",
-        "config": {"workload": args.workload, "sample": sample},
+        "config": {"workload": args.workload, "Jmax": jmax, "blocks": nblk, "points": npts, "same_config": same,
+                   "sample": sample},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "point-updates/s", "cores": cores, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "one_core_value": npts1 * steps1 / el1,
+                         "one_core_sample": f"Jmax=4 grid ({nblk1} blocks), {steps1} RK4 steps in {el1:.1f} s",
+                         "build": "g++ -O3 -ffp-contract=off -fopenmp (oracle/Makefile)"},
         "e2e": {"value": value, "unit": "point-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "reference is Fortran (no compiler in this image); the oracle is its bit-exact C++ restatement",
+        "reference_log": dict(REF_LOG, oracle_same_case={f"{cores}_threads": log_all,
+                                                         f"{min(12, cores)}_threads": log_12}),
+        "note": "the reference is Fortran (no Fortran compiler in this image); the timed path is the oracle, "
+                "its bit-exact C++ restatement, labelled a CPU restatement, not the reference binary",
     }
     print(json.dumps(line))
 
@@ -779,7 +1021,9 @@ def run_reference(args, rank, world):
 def main():
     args = parse()
     rank, world = dist_init(args.gpus)
-    if args.impl == "reference":
+    if args.traffic_case:
+        run_traffic_case(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     elif args.workload == "serving":
         run_serving(args, rank, world)

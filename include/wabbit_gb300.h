@@ -36,7 +36,9 @@ extern "C" {
 #define WG_ENOMEM     -2   /* device allocation failed (HBM budget)          */
 #define WG_ECUDA      -3   /* a CUDA runtime call failed                      */
 #define WG_EDIVERGED  -4   /* |u| > 1e12 in the state (rhs_ACM.f90:133-146)  */
-#define WG_ETIMEOUT   -5   /* a bounded device wait gave up                   */
+#define WG_ETIMEOUT   -5   /* a bounded device wait gave up; the context is
+                              unusable from then on (every call but
+                              wg_ctx_destroy returns WG_ETIMEOUT)           */
 #define WG_EGRID      -6   /* grid is not a valid graded periodic forest      */
 #define WG_ENOTSUP    -7   /* configuration not supported by this build       */
 
@@ -142,16 +144,24 @@ int wg_ctx_destroy(wg_ctx *ctx);
 /* 1: FMA stencil (default); 0: strict reference arithmetic (no FMA). */
 int wg_set_variant(wg_ctx *ctx, int fast);
 /* Form of the FP32-pipe stage kernel (no counterpart in the reference, whose
- * RHS is a per-block loop): WG_FORM_AUTO (default) times the forms that
- * apply on the first wg_run of a grid and keeps the faster; WG_FORM_DIRECT
- * reads the stencil from global memory; WG_FORM_TILE stages each block slab
- * in shared memory by TMA (3-D, 16x16 planes, g_rhs = 2). wg_get_stage_form
- * returns the form in use (the autotuner's choice once it has run). */
+ * RHS is a per-block loop): WG_FORM_AUTO (default) times, for each of the
+ * four RK stages, the forms that apply before the first step of a context
+ * and keeps the fastest per stage; WG_FORM_DIRECT reads the stencil from
+ * global memory; WG_FORM_TILE stages 4-plane slabs of a block in shared
+ * memory by TMA (3-D, 16x16 planes, g_rhs = 2); WG_FORM_MARCH walks a whole
+ * 16^3 block through a ring of 5 planes loaded by TMA. wg_get_stage_form
+ * returns the form of stage 2, wg_get_stage_forms the forms of stages 1-4
+ * (the autotuner's choices once it has run). */
 #define WG_FORM_AUTO 0
 #define WG_FORM_DIRECT 1
 #define WG_FORM_TILE 2
+#define WG_FORM_MARCH 3
 int wg_set_stage_form(wg_ctx *ctx, int form);
 int wg_get_stage_form(wg_ctx *ctx, int *form);
+int wg_get_stage_forms(wg_ctx *ctx, int *forms);
+/* Fixes the forms of RK stages 1-4 (each WG_FORM_DIRECT, _TILE or _MARCH),
+ * e.g. to reuse the autotuner's choice of one context in another. */
+int wg_set_stage_forms(wg_ctx *ctx, const int *forms);
 int wg_synchronize(wg_ctx *ctx);
 /* the context's CUDA stream (cudaStream_t) */
 void *wg_stream(wg_ctx *ctx);
@@ -313,11 +323,17 @@ int wg_threshold_flags_noalloc(const wg_config *cfg, int nblk, const double *d_b
 int wg_refine_everywhere(wg_ctx *ctx, int tree);
 
 /* ---- measurement -------------------------------------------------------- */
-/* FP64 / FP32 FMA throughput of the current device, TFLOP/s (FMA = 2). */
-int wg_probe_alu(double *fp64_tflops, double *fp32_tflops);
 /* Mean device time (ms) of one launch over reps launches, CUDA events on the
  * context stream: which = 0 RK-stage kernel, 1 RHS ghost sync, 2 dt. */
 int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_launch);
+/* nsteps RK4 steps of the listed trees (the launches of wg_run without a
+ * graph), one step at a time with CUDA events between the kernel groups;
+ * ms[9] receives the mean device time (ms) per step of the ghost sync before
+ * stages 1-4 (ms[0..3]), the dt reduction (ms[4]) and the stage kernels of
+ * stages 1-4 (ms[5..8]). The state advances by nsteps steps. No counterpart
+ * in the reference (its toc timers, LIB/TIMING/module_timing.f90:76-127,
+ * time the same phases on the host). */
+int wg_step_profile(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, double *ms);
 int wg_tree_stats(wg_ctx *ctx, int tree, int *nblocks, int *nmasked);
 /* kernel nodes in the captured RK4-step graph of the last wg_run(.., 1) */
 int wg_graph_kernels(wg_ctx *ctx);

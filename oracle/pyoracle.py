@@ -46,6 +46,8 @@ def lib():
         L.or_get_data.argtypes = [ctypes.c_void_p, _dp]
         L.or_set_data.argtypes = [ctypes.c_void_p, _dp]
         L.or_set_mask.argtypes = [ctypes.c_void_p, _dp]
+        L.or_set_mask_sparse.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _dp]
+        L.or_set_interior.argtypes = [ctypes.c_void_p, _dp]
         L.or_get_neighbors.argtypes = [ctypes.c_void_p, _ip]
         L.or_sync_ghosts.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.or_sync_ghosts.restype = ctypes.c_int
@@ -132,6 +134,25 @@ class Oracle:
         else:
             mask = np.ascontiguousarray(mask, np.float64)
             self.L.or_set_mask(self.h, _p(mask))
+
+    def set_mask_sparse(self, ids, masks):
+        """Masks (n, 6, nz, ny, nx) of the listed blocks; every other block
+        has the all-zero mask."""
+        ids = np.ascontiguousarray(ids, np.int32)
+        masks = np.ascontiguousarray(masks, np.float64)
+        assert masks.size == len(ids) * 6 * int(np.prod(self.block_shape[1:]))
+        rc = self.L.or_set_mask_sparse(self.h, len(ids), _p(ids, ctypes.c_int), _p(masks))
+        if rc != 0:
+            raise RuntimeError(f"or_set_mask_sparse: {rc}")
+
+    def set_interior(self, u):
+        """Interior points of every block, (nblk, neq, Bz, By, Bx); the ghost
+        nodes keep their values."""
+        u = np.ascontiguousarray(u, np.float64)
+        c = self.cfg
+        bz = c.Bs[2] if c.dim == 3 else 1
+        assert u.size == self.nblocks * c.neq * bz * c.Bs[1] * c.Bs[0]
+        self.L.or_set_interior(self.h, _p(u))
 
     def set_geometry(self, geo):
         """Penalisation geometry (a WgGeometry) the masks are drawn from."""

@@ -136,13 +136,15 @@ struct Oracle {
     int nx, ny, nz, nc, npts;       // block extents incl. ghosts
     std::vector<Block> blocks;
     std::vector<double> data;       // nblk * nc * npts
-    std::vector<double> mask;       // nblk * 6 * npts (optional)
+    std::vector<double> mask;       // nblk * 6 * npts (optional), or per mask_slot
+    std::vector<int> mask_slot;     // empty: mask is dense; else block -> slot of mask (6 * npts each)
     std::vector<int> nb;            // nblk * 168
     std::unordered_map<uint64_t, int> lookup;
     // full-tree adaptation: hvy_tmp, refinement status, family
     std::vector<double> tmp;
     std::vector<int> ref, mother, dau;   // dau: 8 per block, -1 where absent
-    // RK registers: slot 0 = u_n, 1..4 = k1..k4 (full blocks, as hvy_work)
+    // RK registers: slot 0 = u_n, 1..4 = k1..k4 (hvy_work), interior points
+    // only (the only points the RK update reads or writes)
     std::vector<double> work;
     int nthreads = 1;
     // penalisation geometry (createMask_tree); kind WG_GEOM_NONE = none
@@ -155,6 +157,18 @@ struct Oracle {
         return ((size_t(ic - 1) * nz + (iz - 1)) * ny + (iy - 1)) * nx + (ix - 1);
     }
 };
+
+// the mask of block b (6 components of npts points), null without a mask
+static inline const double *mask_of(const Oracle &o, int b) {
+    if (o.mask.empty()) return nullptr;
+    const size_t slot = o.mask_slot.empty() ? size_t(b) : size_t(o.mask_slot[b]);
+    return o.mask.data() + slot * 6 * o.npts;
+}
+
+static inline void clear_mask(Oracle &o) {
+    o.mask.clear();
+    o.mask_slot.clear();
+}
 
 // treecode digit of a block at its own level: bit0 = y, bit1 = x, bit2 = z
 // (LIB/TREE/module_treelib.f90 encoding_b/decoding_b, find_neighbors.f90:46)
@@ -452,15 +466,94 @@ static void prediction(const double *coarse, int cx, int cy, int cz, double *fin
 // ---------------------------------------------------------------------------
 static void hd_filter_block(const Oracle &o, int b, std::vector<double> &out);
 
-static void sync_ghosts(Oracle &o, int gminus, int gplus, bool ignore_filter) {
+// one transfer of a sync stage: sender ib -> receiver in through relation i_n
+struct Xfer {
+    int ib, in, i_n, lvl_diff;
+};
+
+// per-thread scratch of the transfers (prediction patches, filtered sender)
+struct XferScratch {
+    std::vector<double> coarse, fine, filtered;
+    int filtered_id = -1;
+};
+
+static void do_xfer(Oracle &o, const Xfer &x, int gminus, int gplus, bool ignore_filter, XferScratch &sc) {
     const wg_config &cfg = o.cfg;
     const int dim = cfg.dim;
+    const int ib = x.ib, in = x.in, i_n = x.i_n, lvl_diff = x.lvl_diff;
+    const int inv = inverse_relation(i_n);
+    int recv[2][3], sb[2][3], buf[2][3];
+    ghost_patch(cfg.Bs, cfg.g, dim, inv, recv, gminus, gplus, -lvl_diff);
+    send_bounds(cfg, o.wav.order_predictor, i_n, lvl_diff, gminus, gplus, sb, buf);
+    double *dst = o.blk(in);
+    const double *src = o.blk(ib);
+    if (lvl_diff == 0) {
+        for (int c = 1; c <= o.nc; c++)
+            for (int k = recv[0][2], ks = sb[0][2]; k <= recv[1][2]; k++, ks++)
+                for (int j = recv[0][1], js = sb[0][1]; j <= recv[1][1]; j++, js++)
+                    for (int i = recv[0][0], is = sb[0][0]; i <= recv[1][0]; i++, is++)
+                        dst[o.at(i, j, k, c)] = src[o.at(is, js, ks, c)];
+    } else if (lvl_diff == +1) {
+        const double *srcf = src;
+        if (!ignore_filter && o.wav.lifted) {
+            if (sc.filtered_id != ib) { hd_filter_block(o, ib, sc.filtered); sc.filtered_id = ib; }
+            srcf = sc.filtered.data();
+        }
+        // res_data(1:...) = src(ijk(1):ijk(2):2), then receiver takes res_data(buffer box)
+        for (int c = 1; c <= o.nc; c++)
+            for (int k = recv[0][2], kb = buf[0][2]; k <= recv[1][2]; k++, kb++)
+                for (int j = recv[0][1], jb = buf[0][1]; j <= recv[1][1]; j++, jb++)
+                    for (int i = recv[0][0], ib2 = buf[0][0]; i <= recv[1][0]; i++, ib2++) {
+                        int is = sb[0][0] + 2 * (ib2 - 1);
+                        int js = sb[0][1] + 2 * (jb - 1);
+                        int ks = (dim == 3) ? sb[0][2] + 2 * (kb - 1) : 1;
+                        dst[o.at(i, j, k, c)] = srcf[o.at(is, js, ks, c)];
+                    }
+    } else {
+        const int cx = sb[1][0] - sb[0][0] + 1, cy = sb[1][1] - sb[0][1] + 1, cz = sb[1][2] - sb[0][2] + 1;
+        const int fx = 2 * cx - 1, fy = 2 * cy - 1;
+        sc.coarse.resize(size_t(cx) * cy * cz);
+        sc.fine.resize(size_t(fx) * fy * (2 * cz - 1));
+        for (int c = 1; c <= o.nc; c++) {
+            size_t p = 0;
+            for (int k = sb[0][2]; k <= sb[1][2]; k++)
+                for (int j = sb[0][1]; j <= sb[1][1]; j++)
+                    for (int i = sb[0][0]; i <= sb[1][0]; i++) sc.coarse[p++] = src[o.at(i, j, k, c)];
+            prediction(sc.coarse.data(), cx, cy, cz, sc.fine.data(), o.wav.order_predictor);
+            for (int k = recv[0][2], kb = buf[0][2]; k <= recv[1][2]; k++, kb++)
+                for (int j = recv[0][1], jb = buf[0][1]; j <= recv[1][1]; j++, jb++)
+                    for (int i = recv[0][0], ib2 = buf[0][0]; i <= recv[1][0]; i++, ib2++)
+                        dst[o.at(i, j, k, c)] = sc.fine[(size_t(kb - 1) * fy + (jb - 1)) * fx + (ib2 - 1)];
+        }
+    }
+}
+
+// whether a transfer reads ghost nodes of its sender (the filtered
+// restriction reads the whole block)
+static bool xfer_reads_ghosts(const Oracle &o, const Xfer &x, int gminus, int gplus, bool ignore_filter) {
+    const wg_config &cfg = o.cfg;
+    if (x.lvl_diff == +1 && !ignore_filter && o.wav.lifted) return true;
+    int sb[2][3], buf[2][3];
+    send_bounds(cfg, o.wav.order_predictor, x.i_n, x.lvl_diff, gminus, gplus, sb, buf);
+    for (int d = 0; d < cfg.dim; d++)
+        if (sb[0][d] < cfg.g + 1 || sb[1][d] > cfg.g + cfg.Bs[d]) return true;
+    return false;
+}
+
+// sync_ghosts_generic's stages on one process: in stage 1 the same-level
+// copies (and, unlifted, the restrictions), then the restrictions (lifted),
+// then the predictions; within a stage the transfers run in the order of the
+// sending blocks and their relations (unpack_ghostlayers_internal). With
+// several threads the receiving blocks of a stage are processed in parallel,
+// each receiver's transfers in that same order, which gives the sequential
+// result unless a sender reads ghost nodes that the same stage writes; such
+// stages run sequentially.
+static void sync_ghosts(Oracle &o, int gminus, int gplus, bool ignore_filter) {
     const int nstages = o.wav.lifted ? 3 : 2;
     const int isUnlifted = o.wav.lifted ? 0 : 1;
     const int nblk = (int)o.blocks.size();
-    std::vector<double> coarse, fine, filtered;
-    int filtered_id = -1;
     for (int istage = 1; istage <= nstages; istage++) {
+        std::vector<Xfer> xs;
         for (int ib = 0; ib < nblk; ib++) {
             const int level = o.blocks[ib].level;
             for (int i_n = 1; i_n <= 168; i_n++) {
@@ -469,53 +562,37 @@ static void sync_ghosts(Oracle &o, int gminus, int gplus, bool ignore_filter) {
                 const int lvl_diff = level - o.blocks[in].level;
                 bool send = (istage == 1 && lvl_diff == 0) || (istage == 2 - isUnlifted && lvl_diff == +1) ||
                             (istage == 3 - isUnlifted && lvl_diff == -1);
-                if (!send) continue;
-                const int inv = inverse_relation(i_n);
-                int recv[2][3], sb[2][3], buf[2][3];
-                ghost_patch(cfg.Bs, cfg.g, dim, inv, recv, gminus, gplus, -lvl_diff);
-                send_bounds(cfg, o.wav.order_predictor, i_n, lvl_diff, gminus, gplus, sb, buf);
-                double *dst = o.blk(in);
-                const double *src = o.blk(ib);
-                if (lvl_diff == 0) {
-                    for (int c = 1; c <= o.nc; c++)
-                        for (int k = recv[0][2], ks = sb[0][2]; k <= recv[1][2]; k++, ks++)
-                            for (int j = recv[0][1], js = sb[0][1]; j <= recv[1][1]; j++, js++)
-                                for (int i = recv[0][0], is = sb[0][0]; i <= recv[1][0]; i++, is++)
-                                    dst[o.at(i, j, k, c)] = src[o.at(is, js, ks, c)];
-                } else if (lvl_diff == +1) {
-                    const double *srcf = src;
-                    if (!ignore_filter && o.wav.lifted) {
-                        if (filtered_id != ib) { hd_filter_block(o, ib, filtered); filtered_id = ib; }
-                        srcf = filtered.data();
-                    }
-                    // res_data(1:...) = src(ijk(1):ijk(2):2), then receiver takes res_data(buffer box)
-                    for (int c = 1; c <= o.nc; c++)
-                        for (int k = recv[0][2], kb = buf[0][2]; k <= recv[1][2]; k++, kb++)
-                            for (int j = recv[0][1], jb = buf[0][1]; j <= recv[1][1]; j++, jb++)
-                                for (int i = recv[0][0], ib2 = buf[0][0]; i <= recv[1][0]; i++, ib2++) {
-                                    int is = sb[0][0] + 2 * (ib2 - 1);
-                                    int js = sb[0][1] + 2 * (jb - 1);
-                                    int ks = (dim == 3) ? sb[0][2] + 2 * (kb - 1) : 1;
-                                    dst[o.at(i, j, k, c)] = srcf[o.at(is, js, ks, c)];
-                                }
-                } else {
-                    const int cx = sb[1][0] - sb[0][0] + 1, cy = sb[1][1] - sb[0][1] + 1, cz = sb[1][2] - sb[0][2] + 1;
-                    const int fx = 2 * cx - 1, fy = 2 * cy - 1;
-                    coarse.resize(size_t(cx) * cy * cz);
-                    fine.resize(size_t(fx) * fy * (2 * cz - 1));
-                    for (int c = 1; c <= o.nc; c++) {
-                        size_t p = 0;
-                        for (int k = sb[0][2]; k <= sb[1][2]; k++)
-                            for (int j = sb[0][1]; j <= sb[1][1]; j++)
-                                for (int i = sb[0][0]; i <= sb[1][0]; i++) coarse[p++] = src[o.at(i, j, k, c)];
-                        prediction(coarse.data(), cx, cy, cz, fine.data(), o.wav.order_predictor);
-                        for (int k = recv[0][2], kb = buf[0][2]; k <= recv[1][2]; k++, kb++)
-                            for (int j = recv[0][1], jb = buf[0][1]; j <= recv[1][1]; j++, jb++)
-                                for (int i = recv[0][0], ib2 = buf[0][0]; i <= recv[1][0]; i++, ib2++)
-                                    dst[o.at(i, j, k, c)] = fine[(size_t(kb - 1) * fy + (jb - 1)) * fx + (ib2 - 1)];
-                    }
-                }
+                if (send) xs.push_back({ib, in, i_n, lvl_diff});
             }
+        }
+        bool parallel = o.nthreads > 1;
+        if (parallel) {
+            std::vector<char> recv(nblk, 0), reads(nblk, 0);
+            for (const Xfer &x : xs) {
+                recv[x.in] = 1;
+                if (!reads[x.ib] && xfer_reads_ghosts(o, x, gminus, gplus, ignore_filter)) reads[x.ib] = 1;
+            }
+            for (int b = 0; b < nblk && parallel; b++)
+                if (recv[b] && reads[b]) parallel = false;
+        }
+        if (!parallel) {
+            XferScratch sc;
+            for (const Xfer &x : xs) do_xfer(o, x, gminus, gplus, ignore_filter, sc);
+            continue;
+        }
+        std::vector<int> first(nblk + 1, 0), order(xs.size());
+        for (const Xfer &x : xs) first[x.in + 1]++;
+        for (int b = 0; b < nblk; b++) first[b + 1] += first[b];
+        {
+            std::vector<int> fill(first.begin(), first.end() - 1);
+            for (int k = 0; k < (int)xs.size(); k++) order[fill[xs[k].in]++] = k;
+        }
+#pragma omp parallel num_threads(o.nthreads)
+        {
+            XferScratch sc;
+#pragma omp for schedule(dynamic, 4)
+            for (int b = 0; b < nblk; b++)
+                for (int k = first[b]; k < first[b + 1]; k++) do_xfer(o, xs[order[k]], gminus, gplus, ignore_filter, sc);
         }
     }
 }
@@ -821,9 +898,10 @@ static void mask_block(const Oracle &o, int b, double *m) {
 // LIB/MESH/createMask_tree.f90:118-136)
 static void make_masks(Oracle &o) {
     if (o.geom.kind == WG_GEOM_NONE || !o.cfg.penalization) {
-        o.mask.clear();
+        clear_mask(o);
         return;
     }
+    o.mask_slot.clear();
     o.mask.assign(o.blocks.size() * 6 * size_t(o.npts), 0.0);
     for (size_t b = 0; b < o.blocks.size(); b++) mask_block(o, (int)b, o.mask.data() + b * 6 * o.npts);
 }
@@ -866,27 +944,41 @@ static void indicator_switches(const Oracle &o, int nt, int *flags) {
     }
 }
 
+// the divergence guard of the RHS's integral stage (rhs_ACM.f90:133-146):
+// |u| > 1e12 at an interior point of any block
+static bool diverged(const Oracle &o) {
+    const wg_config &p = o.cfg;
+    const int nblk = (int)o.blocks.size();
+    const int z1 = p.dim == 3 ? p.g + 1 : 1, z2 = p.dim == 3 ? p.Bs[2] + p.g : 1;
+    int bad = 0;
+#pragma omp parallel for reduction(| : bad) num_threads(o.nthreads) if (o.nthreads > 1)
+    for (int b = 0; b < nblk; b++) {
+        const double *u = o.blk(b);
+        for (int c = 1; c <= o.nc; c++)
+            for (int k = z1; k <= z2; k++)
+                for (int j = p.g + 1; j <= p.Bs[1] + p.g; j++)
+                    for (int i = p.g + 1; i <= p.Bs[0] + p.g; i++)
+                        if (std::fabs(u[o.at(i, j, k, c)]) > 1.0e12) bad = 1;
+    }
+    return bad != 0;
+}
+
+// RHS_wrapper local stage of one block into rhs (full-block layout; only the
+// interior points are written)
+static void rhs_block(const Oracle &o, int b, double *rhs) {
+    double x0[3], dx[3];
+    block_spacing(o, b, x0, dx);
+    if (o.cfg.dim == 2) rhs_2d(o, o.blk(b), mask_of(o, b), dx, rhs);
+    else rhs_3d(o, o.blk(b), mask_of(o, b), dx, rhs);
+}
+
 // RHS_wrapper local stage over all blocks, result into rhs (full-block layout)
 static int rhs_all(Oracle &o, double *rhs) {
     const int nblk = (int)o.blocks.size();
     const size_t bs = size_t(o.nc) * o.npts;
-    // integral stage: divergence guard (rhs_ACM.f90:133-146)
-    for (int b = 0; b < nblk; b++) {
-        const double *u = o.blk(b);
-        for (int c = 1; c <= o.nc; c++)
-            for (int k = (o.cfg.dim == 3 ? o.cfg.g + 1 : 1); k <= (o.cfg.dim == 3 ? o.cfg.Bs[2] + o.cfg.g : 1); k++)
-                for (int j = o.cfg.g + 1; j <= o.cfg.Bs[1] + o.cfg.g; j++)
-                    for (int i = o.cfg.g + 1; i <= o.cfg.Bs[0] + o.cfg.g; i++)
-                        if (std::fabs(u[o.at(i, j, k, c)]) > 1.0e12) return WG_EDIVERGED;
-    }
+    if (diverged(o)) return WG_EDIVERGED;
 #pragma omp parallel for schedule(dynamic) num_threads(o.nthreads) if (o.nthreads > 1)
-    for (int b = 0; b < nblk; b++) {
-        double x0[3], dx[3];
-        block_spacing(o, b, x0, dx);
-        const double *m = o.mask.empty() ? nullptr : o.mask.data() + size_t(b) * 6 * o.npts;
-        if (o.cfg.dim == 2) rhs_2d(o, o.blk(b), m, dx, rhs + b * bs);
-        else rhs_3d(o, o.blk(b), m, dx, rhs + b * bs);
-    }
+    for (int b = 0; b < nblk; b++) rhs_block(o, b, rhs + b * bs);
     return WG_OK;
 }
 
@@ -932,7 +1024,10 @@ static double calc_dt(const Oracle &o, double time) {
     double dt = 9.0e9;
     if (p.dt_fixed > 0.0) dt = p.dt_fixed;
     else {
-        for (int b = 0; b < (int)o.blocks.size(); b++) dt = std::min(dt, dt_block(o, b));
+        // the minimum does not depend on the order of the blocks
+        const int nblk = (int)o.blocks.size();
+#pragma omp parallel for reduction(min : dt) num_threads(o.nthreads) if (o.nthreads > 1)
+        for (int b = 0; b < nblk; b++) dt = std::min(dt, dt_block(o, b));
         if (p.dt_max > 0.0) dt = std::min(p.dt_max, dt);
     }
     if (p.write_time > 0.0) {
@@ -950,7 +1045,10 @@ static double calc_dt(const Oracle &o, double time) {
 }
 
 // RungeKuttaGeneric with the default RK4 Butcher tableau
-// (LIB/TIME/runge_kutta_generic.f90:1-156, ini_file_to_params.f90:640-646)
+// (LIB/TIME/runge_kutta_generic.f90:1-156, ini_file_to_params.f90:640-646).
+// The registers hold the interior points only; every update is a loop over
+// blocks with the same expression per point as the reference, so the
+// result does not depend on the number of threads.
 static int rk4_step(Oracle &o, double *time_inout, double *dt_out) {
     const wg_config &p = o.cfg;
     const int nblk = (int)o.blocks.size();
@@ -965,43 +1063,59 @@ static int rk4_step(Oracle &o, double *time_inout, double *dt_out) {
     const int grhs = p.g_rhs;
     sync_ghosts(o, grhs, grhs, true);
     double dt = calc_dt(o, time);
-    o.work.assign(bs * nblk * 5, 0.0);
-    auto W = [&](int slot, int b) { return o.work.data() + (size_t(slot) * nblk + b) * bs; };
     const int g = p.g;
-    const int z1 = p.dim == 2 ? 1 : g + 1, z2 = p.dim == 2 ? 1 : p.Bs[2] + g;
+    const int bz = p.dim == 3 ? p.Bs[2] : 1, z1 = p.dim == 2 ? 1 : g + 1;
+    const size_t ni = size_t(o.nc) * bz * p.Bs[1] * p.Bs[0];   // interior values of a block
+    if (o.work.size() != 5 * ni * nblk) o.work.resize(5 * ni * nblk);
+    auto W = [&](int slot, int b) { return o.work.data() + (size_t(slot) * nblk + b) * ni; };
+    // fn(b, index in the full block, index in the interior register)
     auto interior = [&](auto fn) {
-        for (int b = 0; b < nblk; b++)
+#pragma omp parallel for schedule(static) num_threads(o.nthreads) if (o.nthreads > 1)
+        for (int b = 0; b < nblk; b++) {
+            size_t n = 0;
             for (int c = 1; c <= o.nc; c++)
-                for (int k = z1; k <= z2; k++)
+                for (int k = z1; k < z1 + bz; k++)
                     for (int j = g + 1; j <= p.Bs[1] + g; j++)
-                        for (int i = g + 1; i <= p.Bs[0] + g; i++) fn(b, o.at(i, j, k, c));
+                        for (int i = g + 1; i <= p.Bs[0] + g; i++) fn(b, o.at(i, j, k, c), n++);
+        }
     };
-    interior([&](int b, size_t q) { W(0, b)[q] = o.blk(b)[q]; });
-    // stage 1
-    {
-        std::vector<double> r(bs * nblk, 0.0);
-        int st = rhs_all(o, r.data());
-        if (st) return st;
-        interior([&](int b, size_t q) { W(1, b)[q] = r[b * bs + q]; });
-    }
+    // RHS of every block into register `slot`
+    auto stage_rhs = [&](int slot) -> int {
+        if (diverged(o)) return WG_EDIVERGED;
+#pragma omp parallel num_threads(o.nthreads) if (o.nthreads > 1)
+        {
+            std::vector<double> r(bs);
+#pragma omp for schedule(dynamic)
+            for (int b = 0; b < nblk; b++) {
+                rhs_block(o, b, r.data());
+                double *w = W(slot, b);
+                size_t n = 0;
+                for (int c = 1; c <= o.nc; c++)
+                    for (int k = z1; k < z1 + bz; k++)
+                        for (int j = g + 1; j <= p.Bs[1] + g; j++)
+                            for (int i = g + 1; i <= p.Bs[0] + g; i++) w[n++] = r[o.at(i, j, k, c)];
+            }
+        }
+        return WG_OK;
+    };
+    interior([&](int b, size_t q, size_t n) { W(0, b)[n] = o.blk(b)[q]; });
+    int st = stage_rhs(1);
+    if (st) return st;
     for (int j = 2; j <= 4; j++) {
-        interior([&](int b, size_t q) { o.blk(b)[q] = W(0, b)[q]; });
+        interior([&](int b, size_t q, size_t n) { o.blk(b)[q] = W(0, b)[n]; });
         for (int l = 2; l <= j; l++) {
             double a = rk[j - 1][l - 1];
             if (std::fabs(a) < 1.0e-8) continue;
-            interior([&](int b, size_t q) { o.blk(b)[q] = o.blk(b)[q] + dt * a * W(l - 1, b)[q]; });
+            interior([&](int b, size_t q, size_t n) { o.blk(b)[q] = o.blk(b)[q] + dt * a * W(l - 1, b)[n]; });
         }
         sync_ghosts(o, grhs, grhs, true);
-        std::vector<double> r(bs * nblk, 0.0);
-        int st = rhs_all(o, r.data());
-        if (st) return st;
-        interior([&](int b, size_t q) { W(j, b)[q] = r[b * bs + q]; });
+        if ((st = stage_rhs(j))) return st;
     }
-    interior([&](int b, size_t q) { o.blk(b)[q] = W(0, b)[q]; });
+    interior([&](int b, size_t q, size_t n) { o.blk(b)[q] = W(0, b)[n]; });
     for (int j = 2; j <= 5; j++) {
         double bj = rk[4][j - 1];
         if (std::fabs(bj) < 1.0e-8) continue;
-        interior([&](int b, size_t q) { o.blk(b)[q] = o.blk(b)[q] + dt * bj * W(j - 1, b)[q]; });
+        interior([&](int b, size_t q, size_t n) { o.blk(b)[q] = o.blk(b)[q] + dt * bj * W(j - 1, b)[n]; });
     }
     *time_inout = time + dt;
     *dt_out = dt;
@@ -1510,7 +1624,7 @@ static int adapt_unlifted(Oracle &o, const double *eps_use, int everywhere) {
     }
     o.blocks = nbl;
     o.data.swap(ndata);
-    o.mask.clear();   // masks depend on the grid
+    clear_mask(o);   // masks depend on the grid
     rebuild_lookup(o);
     update_neighbors(o);
     sync_ghosts(o, g, g, true);
@@ -2240,7 +2354,7 @@ static int adapt_lifted(Oracle &o, const double *eps_use, int everywhere) {
         for (int b = 0; b < n2; b++) del[b] = !blk_is_leaf(o, b, false);
         erase_blocks(o, del);
     }
-    o.mask.clear();
+    clear_mask(o);
     update_neighbors(o, false);
     update_family(o, Jmin);
     // final sync_ghosts_tree (filtered restriction)
@@ -2291,7 +2405,7 @@ int or_set_grid(void *h, int nblk, const int *level, const int *coords, const do
     }
     o.data.assign(size_t(nblk) * o.nc * o.npts, 0.0);
     if (data) std::memcpy(o.data.data(), data, o.data.size() * sizeof(double));
-    o.mask.clear();
+    clear_mask(o);
     update_neighbors(o);
     return WG_OK;
 }
@@ -2321,8 +2435,44 @@ int or_set_data(void *h, const double *in) {
 
 int or_set_mask(void *h, const double *mask) {
     Oracle &o = *(Oracle *)h;
-    if (!mask) { o.mask.clear(); return WG_OK; }
+    if (!mask) { clear_mask(o); return WG_OK; }
+    o.mask_slot.clear();
     o.mask.assign(mask, mask + o.blocks.size() * 6 * size_t(o.npts));
+    return WG_OK;
+}
+
+// masks of the n listed blocks (n * 6 * npts doubles, full-block layout);
+// every other block has the all-zero mask (one shared copy)
+int or_set_mask_sparse(void *h, int n, const int *ids, const double *masks) {
+    Oracle &o = *(Oracle *)h;
+    const int nblk = (int)o.blocks.size();
+    const size_t per = 6 * size_t(o.npts);
+    o.mask.assign(size_t(n + 1) * per, 0.0);
+    o.mask_slot.assign(nblk, n);   // slot n: zeros
+    for (int i = 0; i < n; i++) {
+        if (ids[i] < 0 || ids[i] >= nblk) { clear_mask(o); return WG_EINVAL; }
+        o.mask_slot[ids[i]] = i;
+        std::memcpy(o.mask.data() + i * per, masks + i * per, per * sizeof(double));
+    }
+    return WG_OK;
+}
+
+// interior points of every block ((nblk, nc, Bz, By, Bx), x fastest) into
+// the state; ghost nodes are left as they are
+int or_set_interior(void *h, const double *u) {
+    Oracle &o = *(Oracle *)h;
+    const wg_config &p = o.cfg;
+    const int g = p.g, bz = p.dim == 3 ? p.Bs[2] : 1, z0 = p.dim == 3 ? g + 1 : 1;
+    const int nblk = (int)o.blocks.size();
+#pragma omp parallel for num_threads(o.nthreads) if (o.nthreads > 1)
+    for (int b = 0; b < nblk; b++) {
+        const double *src = u + size_t(b) * o.nc * bz * p.Bs[1] * p.Bs[0];
+        for (int c = 1; c <= o.nc; c++)
+            for (int k = 0; k < bz; k++)
+                for (int j = 0; j < p.Bs[1]; j++)
+                    for (int i = 0; i < p.Bs[0]; i++)
+                        o.blk(b)[o.at(g + 1 + i, g + 1 + j, z0 + k, c)] = *src++;
+    }
     return WG_OK;
 }
 
@@ -2463,7 +2613,7 @@ int or_set_geometry(void *h, const wg_geometry *geo) {
     Oracle &o = *(Oracle *)h;
     if (geo) o.geom = *geo;
     else o.geom = wg_geometry{};
-    o.mask.clear();
+    clear_mask(o);
     return WG_OK;
 }
 
@@ -2476,7 +2626,8 @@ int or_make_mask(void *h) {
 int or_get_mask(void *h, double *out) {
     Oracle &o = *(Oracle *)h;
     if (o.mask.empty()) return 0;
-    std::memcpy(out, o.mask.data(), o.mask.size() * sizeof(double));
+    for (size_t b = 0; b < o.blocks.size(); b++)
+        std::memcpy(out + b * 6 * o.npts, mask_of(o, (int)b), 6 * size_t(o.npts) * sizeof(double));
     return 1;
 }
 

@@ -29,6 +29,12 @@ compare against them:
   saved mask (chi) on the t=0, 0.05 and 0.1 grids. Each case is stored under
   the prefix "CDF40_" / "CDF44_".
 
+* h5_files.npz -- every dataset and every attribute of two field files as
+  the reference's saveHDF5_tree wrote them (2-D: acm_CDF40/mask_000000000000
+  .h5, 3-D: taylorGreen/taylorGreenEqui_FD4_CDF40/ux_000000000000.h5),
+  under the prefixes "f2_" / "f3_" ("ds_<name>", "at_<name>"), for the
+  writer's tests.
+
 Block data are stored as interiors only, shape (Nb, ncomp, [Bs,] Bs, Bs),
 x fastest; block geometry as level (Nb,) and integer coords (Nb, 3).
 """
@@ -145,6 +151,19 @@ def acm_cyl(ref):
     np.savez_compressed(os.path.join(HERE, "acm_cyl.npz"), **out)
 
 
+def h5_files(ref):
+    from wabbit_gb300.h5io import H5File
+    out = {}
+    for tag, rel in [("f2", "TESTING/acm/acm_CDF40/mask_000000000000.h5"),
+                     ("f3", "TESTING/acm/taylorGreen/taylorGreenEqui_FD4_CDF40/ux_000000000000.h5")]:
+        h = H5File(os.path.join(ref, rel))
+        for name in h.datasets:
+            out[f"{tag}_ds_{name}"] = h.read(name)
+            for a, v in h.attrs(name).items():
+                out[f"{tag}_at_{a}"] = np.atleast_1d(v)
+    np.savez_compressed(os.path.join(HERE, "h5_files.npz"), **out)
+
+
 if __name__ == "__main__":
     if len(sys.argv) != 2:
         sys.exit("usage: make_fixtures.py <path of the reference checkout>")
@@ -153,6 +172,7 @@ if __name__ == "__main__":
     tg3d(ref)
     wavelets(ref)
     acm_cyl(ref)
+    h5_files(ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -264,6 +264,34 @@ def test_rk4_fp32_pipe_path_within_tolerance(dim, wavelet, penal, grids2d, grids
             assert err < 3e-13 * (step + 1), (step, err)
 
 
+def test_fp32_pipe_stage_forms_bit_identical():
+    """The direct, tile and march forms of the FP32-pipe stage kernel do the
+    same arithmetic in the same order: three steps with any per-stage mix of
+    forms give the same bits, so the autotuner's choices never change a
+    result."""
+    cfg = small_cfg(3, "CDF40", Bs=16, penal=1, jmin=1, jmax=2)
+    cfg.C_eta = 1e-2
+    cfg.rhs_precision = 1
+    lv, co = grids.random_graded(3, 1, 2, seed=5, frac=0.4)
+    data = smooth_state(cfg, lv, co, 31)
+    mask = sphere_mask(cfg, lv, co, [0.5, 0.6, 0.7], 0.3)
+    out = []
+    for forms in (["direct"] * 4, ["tile"] * 4, ["march"] * 4, ["march", "tile", "direct", "march"]):
+        with Context(cfg, len(lv) + 4) as ctx:
+            ctx.set_stage_forms(forms)
+            f = ctx.forest()
+            f.set_grid(lv, co)
+            f.upload(data)
+            f.set_mask(mask)
+            f.set_time(0.0)
+            f.run(3, use_graph=True)
+            assert ctx.stage_forms() == forms
+            out.append((forms, f.download(), f.time()))
+    for forms, u, t in out[1:]:
+        assert t == out[0][2], forms
+        assert np.array_equal(u, out[0][1]), forms
+
+
 def test_fp32_pipe_rejects_skew_symmetric():
     from wabbit_gb300 import capi
     cfg = small_cfg(2, skew=1)
@@ -272,12 +300,12 @@ def test_fp32_pipe_rejects_skew_symmetric():
         Context(cfg, 8)
 
 
-@pytest.mark.parametrize("form", ["direct", "tile", "auto"])
+@pytest.mark.parametrize("form", ["direct", "tile", "march", "auto"])
 def test_fp32_pipe_stage_forms_16cubed(form):
-    """3-D 16^3 blocks (the benchmark geometry): the direct-load and the
-    TMA-staged stage kernels, and the autotuner's pick, all stay within
-    1e-12 per step of the FP64 oracle on a graded two-level grid with a
-    masked sphere."""
+    """3-D 16^3 blocks (the benchmark geometry): the direct-load stage
+    kernel, the TMA-staged slab and plane-ring kernels, and the autotuner's
+    per-stage picks, all stay within 1e-12 of the FP64 oracle over three
+    steps on a graded two-level grid with a masked sphere."""
     cfg = small_cfg(3, "CDF40", Bs=16, penal=1, jmin=1, jmax=2)
     cfg.C_eta = 1e-2
     cfg.rhs_precision = 1
@@ -303,4 +331,7 @@ def test_fp32_pipe_stage_forms_16cubed(form):
                 f.run(1, use_graph=True)
             err = rel_l2(interior(cfg, f.download()), interior(cfg, o.data()))
             assert err < 1e-12, (form, step, err)
-        assert ctx.stage_form() in (("direct", "tile") if form == "auto" else (form,))
+        forms = ctx.stage_forms()
+        assert len(forms) == 4
+        assert all(x in (("direct", "tile", "march") if form == "auto" else (form,)) for x in forms)
+        assert ctx.stage_form() == forms[1]

@@ -25,12 +25,13 @@ EXPORTS = [
     "wg_get_nblocks", "wg_get_grid", "wg_upload_state", "wg_download_state", "wg_set_mask", "wg_set_time",
     "wg_get_time", "wg_sync_ghosts", "wg_rhs", "wg_compute_dt", "wg_rk4_step", "wg_run", "wg_threshold_flags",
     "wg_refine_everywhere", "wg_sync_table", "wg_block_slot", "wg_sync_table_host",
-    "wg_probe_alu", "wg_time_kernel", "wg_tree_stats", "wg_set_mask_sparse", "wg_set_mask_sphere",
+    "wg_time_kernel", "wg_tree_stats", "wg_set_mask_sparse", "wg_set_mask_sphere",
     "wg_get_mask_block",
     "wg_upload_interior", "wg_download_interior", "wg_graph_kernels",
     "wg_threshold_flags_noalloc", "wg_set_stage_form", "wg_get_stage_form",
     "wg_wavelet_decompose", "wg_wavelet_reconstruct", "wg_wavelet_threshold", "wg_threshold_flags_wd",
-    "wg_adapt", "wg_adapt_profile", "wg_rk4_stream", "wg_set_geometry",
+    "wg_adapt", "wg_adapt_profile", "wg_rk4_stream", "wg_set_geometry", "wg_get_stage_forms",
+    "wg_step_profile", "wg_set_stage_forms",
 ]
 
 
@@ -60,6 +61,9 @@ _SIGS = {
     "wg_wavelet_reconstruct": (_i, [_vp, _i]),
     "wg_wavelet_threshold": (_i, [_vp, _i, _dp]),
     "wg_get_stage_form": (_i, [_vp, ctypes.POINTER(ctypes.c_int)]),
+    "wg_get_stage_forms": (_i, [_vp, _ip]),
+    "wg_step_profile": (_i, [_vp, _i, _ip, _i, _dp]),
+    "wg_set_stage_forms": (_i, [_vp, _ip]),
     "wg_synchronize": (_i, [_vp]),
     "wg_stream": (_vp, [_vp]),
     "wg_tree_create": (_i, [_vp, ctypes.POINTER(WgConfig), _ip]),
@@ -83,7 +87,6 @@ _SIGS = {
     "wg_sync_table": (_i, [_vp, _i, _i, _i, _i, _i, _ip]),
     "wg_block_slot": (_i, [_vp, _i, _i]),
     "wg_sync_table_host": (_i, [ctypes.POINTER(WgConfig), _i, _ip, _ip, _i, _i, _i, _i, _ip]),
-    "wg_probe_alu": (_i, [_dp, _dp]),
     "wg_time_kernel": (_i, [_vp, _i, _i, _i, _dp]),
     "wg_tree_stats": (_i, [_vp, _i, _ip, _ip]),
     "wg_set_mask_sparse": (_i, [_vp, _i, _i, _ip, _dp]),

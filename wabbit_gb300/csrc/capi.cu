@@ -39,6 +39,7 @@
 namespace wg {
 
 static thread_local std::string g_err;
+static thread_local int g_code = 0;   // status of the last fail() on this thread
 
 static int fail(int code, const char *fmt, ...) {
     char buf[512];
@@ -47,8 +48,13 @@ static int fail(int code, const char *fmt, ...) {
     vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
     g_err = buf;
+    g_code = code;
     return code;
 }
+
+// status of a failed get_tree (invalid id, or a context that a timed-out
+// device wait left unusable)
+static int tree_err() { return g_code ? g_code : WG_EINVAL; }
 
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line) {
     return fail(WG_ECUDA, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
@@ -218,10 +224,19 @@ struct wg_ctx {
     float2 *mask_df = nullptr;
     int *d_push = nullptr;              // per slot 27 same-level receivers (FP32-pipe precision)
     std::vector<int> h_push;
-    CUtensorMap tm[4];                  // TMA maps over B, C, D, E (3-D FP32-pipe precision)
-    bool have_tm = false;
+    CUtensorMap tm[4];                  // TMA maps over B, C, D, E (3-D FP32-pipe precision): slab boxes
+    CUtensorMap tp[4];                  // ... one-plane boxes (march form)
+    bool have_tm = false, have_march = false;
     int stage_form = WG_FORM_AUTO;      // requested form of the FP32-pipe stage kernel
-    int tuned_form = 0;                 // the autotuner's choice (0: not tuned yet)
+    int tuned[4] = {0, 0, 0, 0};        // the autotuner's choice per RK stage (0: not tuned yet)
+    // step profile (wg_step_profile): events recorded between the kernel
+    // groups of an RK4 step while prof_on is set
+    cudaEvent_t prof_ev[10] = {};
+    bool prof_on = false;
+    // set when a bounded device wait gave up (WG_ETIMEOUT): a bulk copy may
+    // still have been landing in shared memory, so nothing the context holds
+    // is trusted any more and every call but wg_ctx_destroy fails
+    bool dead = false;
     int *d_err = nullptr;               // device error flag (a kernel's wait ran out)
     int mask_cap = 0;
     std::vector<int> mask_free;
@@ -316,6 +331,10 @@ TreeParams make_params(const wg_config &c) {
 }
 
 Tree *get_tree(wg_ctx *ctx, int t) {
+    if (ctx && ctx->dead) {
+        fail(WG_ETIMEOUT, "the context is unusable after a timed-out device wait; destroy it");
+        return nullptr;
+    }
     if (!ctx || t < 0 || t >= (int)ctx->trees.size() || !ctx->trees[t].live) {
         fail(WG_EINVAL, "invalid tree id %d", t);
         return nullptr;
@@ -635,29 +654,46 @@ int stage_launch(wg_ctx *ctx, Tree &t, int stage, const double *in, BufGeo gin, 
     return WG_OK;
 }
 
-// the TMA map over a thin stage buffer
-static const void *in_map(wg_ctx *ctx, const double *in) {
-    return in == ctx->B ? &ctx->tm[0] : in == ctx->C ? &ctx->tm[1] : in == ctx->D ? &ctx->tm[2]
-         : in == ctx->E ? &ctx->tm[3] : nullptr;
+// the TMA map over a thin stage buffer (slab or one-plane boxes)
+static const void *in_map(wg_ctx *ctx, const double *in, bool plane) {
+    const CUtensorMap *m = plane ? ctx->tp : ctx->tm;
+    return in == ctx->B ? &m[0] : in == ctx->C ? &m[1] : in == ctx->D ? &m[2] : in == ctx->E ? &m[3] : nullptr;
+}
+
+// the stage-kernel form of RK stage `stage`
+static int form_of(const wg_ctx *ctx, int stage) {
+    if (ctx->stage_form != WG_FORM_AUTO) return ctx->stage_form;
+    return ctx->tuned[stage - 1] ? ctx->tuned[stage - 1] : WG_FORM_DIRECT;
+}
+
+// kernel arguments of a form: the tensor map (null: direct) and the march flag
+static void form_args(wg_ctx *ctx, int stage, const double *in, const void **tm, int *march) {
+    const int form = form_of(ctx, stage);
+    *tm = nullptr;
+    *march = 0;
+    if (form == WG_FORM_TILE && ctx->have_tm) *tm = in_map(ctx, in, false);
+    if (form == WG_FORM_MARCH && ctx->have_march) {
+        *tm = in_map(ctx, in, true);
+        *march = 1;
+    }
 }
 
 // u0 is always B (the anchored copy of u_n), the inputs of stages 2 and 3
 // are C and D; with push the kernels also write the same-level ghost copies
 // of out
-int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *out, bool push) {
+int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *out, bool push, int keep = 1) {
     const int dim = ctx->cfg.dim;
     const int *Bs = ctx->cfg.Bs;
     const int *pp = push ? ctx->d_push : nullptr;
     const void *tm = nullptr;
-    const int form = ctx->stage_form != WG_FORM_AUTO ? ctx->stage_form : ctx->tuned_form ? ctx->tuned_form : WG_FORM_DIRECT;
-    if (ctx->have_tm && form == WG_FORM_TILE)
-        tm = in_map(ctx, in);
+    int march = 0;
+    form_args(ctx, stage, in, &tm, &march);
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, t.d_plain.p, t.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
                                    ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
-                                   Bs[1], Bs[2], tm, ctx->d_err, ctx->stream));
+                                   Bs[1], Bs[2], tm, march, ctx->d_err, ctx->stream, keep));
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, t.d_masked.p, t.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
                                    ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
-                                   Bs[1], Bs[2], tm, ctx->d_err, ctx->stream));
+                                   Bs[1], Bs[2], tm, march, ctx->d_err, ctx->stream, keep));
     return WG_OK;
 }
 
@@ -681,16 +717,22 @@ int make_tensor_maps(wg_ctx *ctx) {
                                 (cuuint64_t)g.nz * ctx->geo.nc * (cuuint64_t)ctx->max_blocks};
     const cuuint64_t strides[2] = {(cuuint64_t)g.nx * 8, (cuuint64_t)g.nx * g.ny * 8};
     const cuuint32_t box[3] = {(cuuint32_t)g.nx, (cuuint32_t)g.ny, (cuuint32_t)(zt + 4)};
+    const cuuint32_t pbox[3] = {(cuuint32_t)g.nx, (cuuint32_t)g.ny, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     double *bufs[4] = {ctx->B, ctx->C, ctx->D, ctx->E};
+    const bool march = ctx->cfg.Bs[2] == 16;   // the march kernel walks 16 planes
     for (int i = 0; i < 4; i++) {
-        const CUresult r = reinterpret_cast<Encode>(fn)(&ctx->tm[i], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, bufs[i], dims,
-                                                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) return fail(WG_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        for (int k = 0; k < (march ? 2 : 1); k++) {
+            const CUresult r = reinterpret_cast<Encode>(fn)(k ? &ctx->tp[i] : &ctx->tm[i], CU_TENSOR_MAP_DATA_TYPE_UINT64,
+                                                            3, bufs[i], dims, strides, k ? pbox : box, estr,
+                                                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(WG_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        }
     }
     ctx->have_tm = true;
+    ctx->have_march = march;
     return WG_OK;
 }
 
@@ -701,8 +743,9 @@ int check_dev_err(wg_ctx *ctx) {
     WG_CUDA_OK(cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     if (!h) return WG_OK;
-    WG_CUDA_OK(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
-    return fail(WG_ETIMEOUT, "a stage kernel's shared-memory load did not complete within its time limit");
+    ctx->dead = true;
+    return fail(WG_ETIMEOUT, "a stage kernel's shared-memory load did not complete within its time limit; "
+                             "the context is unusable, destroy it");
 }
 
 // the thin per-step plan of a tree, and whether its copies are pushed
@@ -733,39 +776,54 @@ int ensure_shadow(wg_ctx *ctx, Tree &t) {
     return WG_OK;
 }
 
-// Autotuner of the FP32-pipe stage kernel: times a stage (C -> D, stage 2)
-// of this tree in each applicable form and keeps the faster for the context.
+// Autotuner of the FP32-pipe stage kernel: for each RK stage, times every
+// applicable form (direct, tile, march) on this tree's grid and keeps the
+// fastest for the context. The stages are timed in step order, each reading
+// the previous one's output (B -> C -> D -> E), so the timed kernels see
+// realistic values. Nothing the next step reads changes: stages 1-3 write
+// the scratch stage buffers, and stage 4 writes its copy of u_n+1 to C (not
+// B) and neither stores u_n+1 nor records its maximum (keep = 0). The
+// autotuner may therefore run between any two steps without changing a bit
+// of the results.
 int autotune_stage_form(wg_ctx *ctx, Tree &t) {
-    if (ctx->precision != WG_RHS_FP32 || ctx->stage_form != WG_FORM_AUTO || ctx->tuned_form) return WG_OK;
-    if (!ctx->have_tm || t.slots.empty()) {
-        ctx->tuned_form = WG_FORM_DIRECT;
+    if (ctx->precision != WG_RHS_FP32 || ctx->stage_form != WG_FORM_AUTO || ctx->tuned[0]) return WG_OK;
+    std::vector<int> forms = {WG_FORM_DIRECT};
+    if (ctx->have_tm && !t.slots.empty()) forms.push_back(WG_FORM_TILE);
+    if (ctx->have_march && !t.slots.empty()) forms.push_back(WG_FORM_MARCH);
+    if (forms.size() == 1) {
+        for (int &f : ctx->tuned) f = WG_FORM_DIRECT;
         return WG_OK;
     }
     bool push;
-    int st = thin_plan(ctx, t, &push);
+    int st = ensure_shadow(ctx, t);
     if (st) return st;
+    if ((st = thin_plan(ctx, t, &push))) return st;
     cudaEvent_t e0, e1;
     WG_CUDA_OK(cudaEventCreate(&e0));
     WG_CUDA_OK(cudaEventCreate(&e1));
-    float best = 0.f;
-    int best_form = WG_FORM_DIRECT;
-    for (int form : {WG_FORM_DIRECT, WG_FORM_TILE}) {
-        ctx->tuned_form = form;
-        if ((st = stage_launch_df(ctx, t, 2, ctx->C, ctx->D, push))) break;   // warm-up
-        WG_CUDA_OK(cudaEventRecord(e0, ctx->stream));
-        for (int r = 0; r < 5 && !st; r++) st = stage_launch_df(ctx, t, 2, ctx->C, ctx->D, push);
-        WG_CUDA_OK(cudaEventRecord(e1, ctx->stream));
-        WG_CUDA_OK(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        WG_CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
-        if (form == WG_FORM_DIRECT || ms < best) {
-            best = ms;
-            best_form = form;
+    double *in[4] = {ctx->B, ctx->C, ctx->D, ctx->E}, *out[4] = {ctx->C, ctx->D, ctx->E, ctx->C};
+    for (int stage = 1; stage <= 4 && !st; stage++) {
+        float best = 0.f;
+        int best_form = WG_FORM_DIRECT;
+        for (int form : forms) {
+            ctx->tuned[stage - 1] = form;
+            const int keep = stage == 4 ? 0 : 1;
+            if ((st = stage_launch_df(ctx, t, stage, in[stage - 1], out[stage - 1], push, keep))) break;   // warm-up
+            WG_CUDA_OK(cudaEventRecord(e0, ctx->stream));
+            for (int r = 0; r < 3 && !st; r++) st = stage_launch_df(ctx, t, stage, in[stage - 1], out[stage - 1], push, keep);
+            WG_CUDA_OK(cudaEventRecord(e1, ctx->stream));
+            WG_CUDA_OK(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            WG_CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+            if (form == forms[0] || ms < best) {
+                best = ms;
+                best_form = form;
+            }
         }
+        ctx->tuned[stage - 1] = best_form;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    ctx->tuned_form = best_form;
     if (st) return st;
     return check_dev_err(ctx);
 }
@@ -774,6 +832,12 @@ int autotune_stage_form(wg_ctx *ctx, Tree &t) {
 // u_n (stage 1 input) and keeps it through the step; the stage inputs 2-4
 // are C, D, C; stage 4 adds the increment to A and writes the copy of
 // u_{n+1} to B
+// event i of the step profile (0: step start, then after sync 1, dt,
+// stage 1, sync 2, stage 2, sync 3, stage 3, sync 4, stage 4)
+static inline void prof_mark(wg_ctx *ctx, int i) {
+    if (ctx->prof_on) cudaEventRecord(ctx->prof_ev[i], ctx->stream);
+}
+
 int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     Tree &t = ctx->trees[tree_id];
     const int g_rhs = ctx->cfg.g_rhs;
@@ -781,19 +845,29 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     int st;
     bool push;
     if ((st = thin_plan(ctx, t, &push))) return st;
+    prof_mark(ctx, 0);
     // B's same-level ghosts were written with its interior (previous stage 4
     // or the shadow copy) when push is on
     if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true, push))) return st;
+    prof_mark(ctx, 1);
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
                          ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream, 1));
+    prof_mark(ctx, 2);
     if ((st = stage_launch_df(ctx, t, 1, ctx->B, ctx->C, push))) return st;
+    prof_mark(ctx, 3);
     if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs, true, push))) return st;
+    prof_mark(ctx, 4);
     if ((st = stage_launch_df(ctx, t, 2, ctx->C, ctx->D, push))) return st;
+    prof_mark(ctx, 5);
     if ((st = run_sync(ctx, t, ctx->D, true, g_rhs, g_rhs, true, push))) return st;
+    prof_mark(ctx, 6);
     if ((st = stage_launch_df(ctx, t, 3, ctx->D, ctx->E, push))) return st;
+    prof_mark(ctx, 7);
     if ((st = run_sync(ctx, t, ctx->E, true, g_rhs, g_rhs, true, push))) return st;
+    prof_mark(ctx, 8);
     if ((st = stage_launch_df(ctx, t, 4, ctx->E, ctx->B, push))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
+    prof_mark(ctx, 9);
     return WG_OK;
 }
 
@@ -896,20 +970,20 @@ int run_sync_batch(wg_ctx *ctx, double *buf) {
 }
 
 int stage_launch_batch(wg_ctx *ctx, int stage, const double *in, double *out) {
+    const int keep = 1;
     const BatchPlan &bp = ctx->batch;
     const int dim = ctx->cfg.dim;
     const int *Bs = ctx->cfg.Bs;
     const int *pp = bp.push ? ctx->d_push : nullptr;
     const void *tm = nullptr;
-    const int form = ctx->stage_form != WG_FORM_AUTO ? ctx->stage_form : ctx->tuned_form ? ctx->tuned_form : WG_FORM_DIRECT;
-    if (ctx->have_tm && form == WG_FORM_TILE)
-        tm = in_map(ctx, in);
+    int march = 0;
+    form_args(ctx, stage, in, &tm, &march);
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, bp.plain.p, bp.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
                                    ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
-                                   Bs[1], Bs[2], tm, ctx->d_err, ctx->stream));
+                                   Bs[1], Bs[2], tm, march, ctx->d_err, ctx->stream, keep));
     WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, bp.masked.p, bp.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
                                    ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
-                                   Bs[1], Bs[2], tm, ctx->d_err, ctx->stream));
+                                   Bs[1], Bs[2], tm, march, ctx->d_err, ctx->stream, keep));
     return WG_OK;
 }
 
@@ -919,17 +993,27 @@ int rk4_enqueue_batch(wg_ctx *ctx) {
     const BatchPlan &bp = ctx->batch;
     const int *Bs = ctx->cfg.Bs;
     int st;
+    prof_mark(ctx, 0);
     if ((st = run_sync_batch(ctx, ctx->B))) return st;
+    prof_mark(ctx, 1);
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, bp.all.p, bp.n_all, ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A, ctx->gA, Bs[0],
                          Bs[1], Bs[2], (int)bp.trees.size(), bp.tree_ids.p, ctx->stream, 1));
+    prof_mark(ctx, 2);
     if ((st = stage_launch_batch(ctx, 1, ctx->B, ctx->C))) return st;
+    prof_mark(ctx, 3);
     if ((st = run_sync_batch(ctx, ctx->C))) return st;
+    prof_mark(ctx, 4);
     if ((st = stage_launch_batch(ctx, 2, ctx->C, ctx->D))) return st;
+    prof_mark(ctx, 5);
     if ((st = run_sync_batch(ctx, ctx->D))) return st;
+    prof_mark(ctx, 6);
     if ((st = stage_launch_batch(ctx, 3, ctx->D, ctx->E))) return st;
+    prof_mark(ctx, 7);
     if ((st = run_sync_batch(ctx, ctx->E))) return st;
+    prof_mark(ctx, 8);
     if ((st = stage_launch_batch(ctx, 4, ctx->E, ctx->B))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, bp.tree_ids.p, (int)bp.trees.size(), ctx->stream));
+    prof_mark(ctx, 9);
     return WG_OK;
 }
 
@@ -940,17 +1024,27 @@ int rk4_enqueue(wg_ctx *ctx, int tree_id) {
     const int g_rhs = ctx->cfg.g_rhs;
     const int *Bs = ctx->cfg.Bs;
     int st;
+    prof_mark(ctx, 0);
     if ((st = run_sync(ctx, t, ctx->A, false, g_rhs, g_rhs))) return st;
+    prof_mark(ctx, 1);
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
                          ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream));
+    prof_mark(ctx, 2);
     if ((st = stage_launch(ctx, t, 1, ctx->A, ctx->gA, ctx->B, ctx->gT))) return st;
+    prof_mark(ctx, 3);
     if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs))) return st;
+    prof_mark(ctx, 4);
     if ((st = stage_launch(ctx, t, 2, ctx->B, ctx->gT, ctx->C, ctx->gT))) return st;
+    prof_mark(ctx, 5);
     if ((st = run_sync(ctx, t, ctx->C, true, g_rhs, g_rhs))) return st;
+    prof_mark(ctx, 6);
     if ((st = stage_launch(ctx, t, 3, ctx->C, ctx->gT, ctx->B, ctx->gT))) return st;
+    prof_mark(ctx, 7);
     if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs))) return st;
+    prof_mark(ctx, 8);
     if ((st = stage_launch(ctx, t, 4, ctx->B, ctx->gT, nullptr, ctx->gT))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
+    prof_mark(ctx, 9);
     return WG_OK;
 }
 
@@ -1111,6 +1205,8 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->d_tp);
     cudaFree(ctx->d_clk);
     for (cudaEvent_t ev : ctx->copy_ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : ctx->prof_ev)
+        if (ev) cudaEventDestroy(ev);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     for (cudaEvent_t ev : ctx->io_ev)
         if (ev) cudaEventDestroy(ev);
@@ -1129,6 +1225,7 @@ int wg_set_variant(wg_ctx *ctx, int fast) {
 
 int wg_tree_create(wg_ctx *ctx, const wg_config *cfg, int *tree) {
     if (!ctx || !tree) return fail(WG_EINVAL, "null argument");
+    if (ctx->dead) return fail(WG_ETIMEOUT, "the context is unusable after a timed-out device wait; destroy it");
     const wg_config *c = cfg ? cfg : &ctx->cfg;
     if (c->dim != ctx->cfg.dim || c->g != ctx->cfg.g || c->g_rhs != ctx->cfg.g_rhs || c->neq != ctx->cfg.neq ||
         std::memcmp(c->Bs, ctx->cfg.Bs, sizeof(c->Bs)) || std::strcmp(c->wavelet, ctx->cfg.wavelet))
@@ -1157,7 +1254,7 @@ int wg_tree_create(wg_ctx *ctx, const wg_config *cfg, int *tree) {
 
 int wg_tree_destroy(wg_ctx *ctx, int tree) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     cudaStreamSynchronize(ctx->stream);
     release_tree_blocks(ctx, *t);
     *t = Tree();
@@ -1169,7 +1266,7 @@ static int regen_masks(wg_ctx *ctx, Tree *t, int tree);
 
 int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *coords) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     if (nblk < 0 || (nblk && (!level || !coords))) return fail(WG_EINVAL, "bad grid arguments");
     cudaStreamSynchronize(ctx->stream);
     release_tree_blocks(ctx, *t);
@@ -1195,14 +1292,15 @@ int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *co
 
 int wg_get_nblocks(wg_ctx *ctx, int tree, int *nblk) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !nblk) return WG_EINVAL;
+    if (!t) return tree_err();
+    if (!nblk) return fail(WG_EINVAL, "null output");
     *nblk = t->forest.size();
     return WG_OK;
 }
 
 int wg_get_grid(wg_ctx *ctx, int tree, int cap, int *level, int *coords) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     const int n = t->forest.size();
     if (cap < n) return fail(WG_EINVAL, "capacity %d < %d blocks", cap, n);
     std::memcpy(level, t->forest.level.data(), sizeof(int) * n);
@@ -1219,7 +1317,8 @@ static bool contiguous(const std::vector<int> &s) {
 
 int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !host_blocks) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!host_blocks) return fail(WG_EINVAL, "bad arguments");
     t->shadow_valid = false;
     const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
     if (!t->slots.empty() && contiguous(t->slots)) {
@@ -1237,7 +1336,8 @@ int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks) {
 
 int wg_download_state(wg_ctx *ctx, int tree, double *host_blocks) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !host_blocks) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!host_blocks) return fail(WG_EINVAL, "bad arguments");
     const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
     if (!t->slots.empty() && contiguous(t->slots)) {
         WG_CUDA_OK(cudaMemcpyAsync(host_blocks, (const char *)ctx->A + per * t->slots[0], per * t->slots.size(),
@@ -1295,7 +1395,8 @@ static int install_masks(wg_ctx *ctx, Tree *t, int tree, const std::vector<int> 
 
 int wg_set_mask_sparse(wg_ctx *ctx, int tree, int n, const int *blocks, const double *mask) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || n < 0 || (n && (!blocks || !mask))) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (n < 0 || (n && (!blocks || !mask))) return fail(WG_EINVAL, "bad arguments");
     cudaStreamSynchronize(ctx->stream);
     t->has_geom = false;
     const int nb = t->forest.size();
@@ -1384,7 +1485,7 @@ static int install_masks(wg_ctx *ctx, Tree *t, int tree, const std::vector<int> 
 // host_mask: nblk * 6 * npts (reference layout hvy_mask) or NULL to drop it
 int wg_set_mask(wg_ctx *ctx, int tree, const double *host_mask) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     if (!host_mask) return wg_set_mask_sparse(ctx, tree, 0, nullptr, nullptr);
     std::vector<int> ids(t->forest.size());
     for (size_t i = 0; i < ids.size(); i++) ids[i] = (int)i;
@@ -1416,7 +1517,7 @@ static int regen_masks(wg_ctx *ctx, Tree *t, int tree) {
 
 int wg_set_geometry(wg_ctx *ctx, int tree, const wg_geometry *geo) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     wg_geometry G{};
     if (geo) G = *geo;
     const char *why = geometry_check(t->cfg, G);
@@ -1434,7 +1535,8 @@ int wg_set_geometry(wg_ctx *ctx, int tree, const wg_geometry *geo) {
 // the workloads' host mask, create_mask.f90:58-61 -> draw_sphere)
 int wg_set_mask_sphere(wg_ctx *ctx, int tree, const double *centre, double radius, double c_smooth) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !centre || !(radius > 0.0) || !(c_smooth > 0.0)) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!centre || !(radius > 0.0) || !(c_smooth > 0.0)) return fail(WG_EINVAL, "bad arguments");
     if (ctx->cfg.dim != 3) return fail(WG_ENOTSUP, "sphere mask needs a 3-D context");
     cudaStreamSynchronize(ctx->stream);
     t->has_geom = false;
@@ -1526,7 +1628,8 @@ int wg_set_mask_sphere(wg_ctx *ctx, int tree, const double *centre, double radiu
 // a mask, 0 when it has none
 int wg_get_mask_block(wg_ctx *ctx, int tree, int block, double *out) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !out || block < 0 || block >= t->forest.size()) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!out || block < 0 || block >= t->forest.size()) return fail(WG_EINVAL, "bad arguments");
     const int slot = t->mask_slot[block];
     if (slot < 0) return 0;
     const long long ni = ctx->nint;
@@ -1538,7 +1641,7 @@ int wg_get_mask_block(wg_ctx *ctx, int tree, int block, double *out) {
 
 int wg_set_time(wg_ctx *ctx, int tree, double time) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     TreeClock c;
     std::memset(&c, 0, sizeof(c));
     c.time = time;
@@ -1552,10 +1655,11 @@ int wg_set_time(wg_ctx *ctx, int tree, double time) {
 
 int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     TreeClock c;
     int st = read_clock(ctx, tree, &c);
     if (st) return st;
+    if ((st = check_dev_err(ctx))) return st;
     if (time) *time = c.time;
     if (dt) *dt = c.dt;
     return c.diverged ? fail(WG_EDIVERGED, "ACM fail: very very large values in state vector") : WG_OK;
@@ -1564,7 +1668,7 @@ int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt) {
 // sync_ghosts_RHS_tree / sync_ghosts_tree on the state (no HD filter)
 int wg_sync_ghosts(wg_ctx *ctx, int tree, int gminus, int gplus) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     if (gminus < 1 || gplus < 1 || gminus > ctx->cfg.g || gplus > ctx->cfg.g)
         return fail(WG_EINVAL, "ghost widths must be in 1..g");
     int st = run_sync(ctx, *t, ctx->A, false, gminus, gplus);
@@ -1577,7 +1681,8 @@ int wg_sync_ghosts(wg_ctx *ctx, int tree, int gminus, int gplus) {
 // host_rhs receives nblk*neq*npts doubles (reference layout, interior set)
 int wg_rhs(wg_ctx *ctx, int tree, double *host_rhs) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !host_rhs) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!host_rhs) return fail(WG_EINVAL, "bad arguments");
     const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
     double *d = nullptr;
     WG_CUDA_OK(cudaMallocAsync(&d, per * ctx->max_blocks, ctx->stream));
@@ -1601,7 +1706,7 @@ int wg_rhs(wg_ctx *ctx, int tree, double *host_rhs) {
 // calculate_time_step at the tree's current time (state must be synced)
 int wg_compute_dt(wg_ctx *ctx, int tree, double *dt) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     const int *Bs = ctx->cfg.Bs;
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
                          ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, ctx->stream));
@@ -1616,7 +1721,7 @@ int wg_compute_dt(wg_ctx *ctx, int tree, double *dt) {
 // returned when the pointers are non-NULL (which synchronises)
 int wg_rk4_step(wg_ctx *ctx, int tree, double *time, double *dt) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     // the stage-kernel form is chosen before the first step (stage buffers
     // C and D are scratch at this point)
     int st = autotune_stage_form(ctx, *t);
@@ -1633,9 +1738,10 @@ int wg_rk4_step(wg_ctx *ctx, int tree, double *time, double *dt) {
 // use_graph the per-step launch sequence is captured once and replayed
 int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph) {
     if (!ctx || ntrees <= 0 || !trees || nsteps < 0) return fail(WG_EINVAL, "bad arguments");
+    if (ctx->dead) return fail(WG_ETIMEOUT, "the context is unusable after a timed-out device wait; destroy it");
     for (int i = 0; i < ntrees; i++) {
         Tree *t = get_tree(ctx, trees[i]);
-        if (!t) return WG_EINVAL;
+        if (!t) return tree_err();
         for (int k = 0; k < i; k++)
             if (trees[k] == trees[i]) return fail(WG_EINVAL, "tree %d listed twice", trees[i]);
         int st = ensure_shadow(ctx, *t);
@@ -1706,7 +1812,7 @@ int wg_run(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, int use_graph)
 // of every block of the tree, in place on the state; wc_threshold_tree
 int wg_wavelet_decompose(wg_ctx *ctx, int tree) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     const int *Bs = ctx->cfg.Bs;
     WG_CUDA_OK(launch_wavelet_decompose(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0], Bs[1],
                                         Bs[2], ctx->geo.nc, ctx->wav.X, ctx->wav.Y, ctx->stream));
@@ -1717,7 +1823,7 @@ int wg_wavelet_decompose(wg_ctx *ctx, int tree) {
 
 int wg_wavelet_reconstruct(wg_ctx *ctx, int tree) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     const int *Bs = ctx->cfg.Bs;
     WG_CUDA_OK(launch_wavelet_reconstruct(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0],
                                           Bs[1], Bs[2], ctx->geo.nc, ctx->wav.X, ctx->wav.Y, ctx->stream));
@@ -1728,7 +1834,8 @@ int wg_wavelet_reconstruct(wg_ctx *ctx, int tree) {
 
 int wg_wavelet_threshold(wg_ctx *ctx, int tree, const double *thresh) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !thresh) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!thresh) return fail(WG_EINVAL, "bad arguments");
     if (ctx->geo.nc > 8) return fail(WG_ENOTSUP, "at most 8 components");
     const int *Bs = ctx->cfg.Bs;
     WG_CUDA_OK(launch_wc_threshold(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0], Bs[1],
@@ -1740,24 +1847,47 @@ int wg_wavelet_threshold(wg_ctx *ctx, int tree, const double *thresh) {
 
 int wg_set_stage_form(wg_ctx *ctx, int form) {
     if (!ctx) return fail(WG_EINVAL, "null ctx");
-    if (form != WG_FORM_AUTO && form != WG_FORM_DIRECT && form != WG_FORM_TILE)
+    if (form != WG_FORM_AUTO && form != WG_FORM_DIRECT && form != WG_FORM_TILE && form != WG_FORM_MARCH)
         return fail(WG_EINVAL, "unknown stage form %d", form);
     if (form == WG_FORM_TILE && !ctx->have_tm)
         return fail(WG_ENOTSUP, "the tile form needs 3-D 16x16 planes, g_rhs = 2 and the FP32-pipe precision");
+    if (form == WG_FORM_MARCH && !ctx->have_march)
+        return fail(WG_ENOTSUP, "the march form needs 3-D 16^3 blocks, g_rhs = 2 and the FP32-pipe precision");
     ctx->stage_form = form;
-    ctx->tuned_form = 0;
+    for (int &f : ctx->tuned) f = 0;
     ctx->graph_version = -1;   // recapture with the new form
+    return WG_OK;
+}
+
+int wg_set_stage_forms(wg_ctx *ctx, const int *forms) {
+    if (!ctx || !forms) return fail(WG_EINVAL, "bad arguments");
+    for (int k = 0; k < 4; k++) {
+        if (forms[k] != WG_FORM_DIRECT && forms[k] != WG_FORM_TILE && forms[k] != WG_FORM_MARCH)
+            return fail(WG_EINVAL, "stage %d: form %d is not direct, tile or march", k + 1, forms[k]);
+        if ((forms[k] == WG_FORM_TILE && !ctx->have_tm) || (forms[k] == WG_FORM_MARCH && !ctx->have_march))
+            return fail(WG_ENOTSUP, "stage %d: form %d does not apply to this configuration", k + 1, forms[k]);
+    }
+    ctx->stage_form = WG_FORM_AUTO;
+    for (int k = 0; k < 4; k++) ctx->tuned[k] = forms[k];   // as if the autotuner had chosen them
+    ctx->graph_version = -1;
     return WG_OK;
 }
 
 int wg_get_stage_form(wg_ctx *ctx, int *form) {
     if (!ctx || !form) return fail(WG_EINVAL, "bad arguments");
-    *form = ctx->stage_form != WG_FORM_AUTO ? ctx->stage_form : ctx->tuned_form ? ctx->tuned_form : WG_FORM_DIRECT;
+    *form = form_of(ctx, 2);
+    return WG_OK;
+}
+
+int wg_get_stage_forms(wg_ctx *ctx, int *forms) {
+    if (!ctx || !forms) return fail(WG_EINVAL, "bad arguments");
+    for (int k = 0; k < 4; k++) forms[k] = form_of(ctx, k + 1);
     return WG_OK;
 }
 
 int wg_synchronize(wg_ctx *ctx) {
     if (!ctx) return fail(WG_EINVAL, "null ctx");
+    if (ctx->dead) return fail(WG_ETIMEOUT, "the context is unusable after a timed-out device wait; destroy it");
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     return check_dev_err(ctx);
 }
@@ -1770,7 +1900,8 @@ void *wg_stream(wg_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 // 0; details (nblk*neq, may be NULL) receives the per-component details
 static int threshold_flags(wg_ctx *ctx, int tree, const double *eps_use, int *flags, double *details, int input_is_wd) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !eps_use || !flags) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!eps_use || !flags) return fail(WG_EINVAL, "bad arguments");
     const int nb = t->forest.size();
     const int nc = ctx->geo.nc;
     double *d_det = nullptr;
@@ -2254,7 +2385,7 @@ int wg_adapt_profile(wg_ctx *ctx, int enable, double *ms_out, int n) {
 
 int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *nblk_out) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     if (indicator != WG_ADAPT_THRESHOLD && indicator != WG_ADAPT_EVERYWHERE)
         return fail(WG_EINVAL, "unknown indicator %d", indicator);
     std::vector<double> eps_own;
@@ -2432,7 +2563,7 @@ static int refine_patches(const wg_config &c, int g, int order, const std::vecto
 
 int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     const int dim = ctx->cfg.dim, nd = 1 << dim;
     const int nb = t->forest.size();
     // blocks on Jmax stay (respectJmaxJmin_tree, LIB/MESH/respectJmaxJmin_tree.f90)
@@ -2521,7 +2652,7 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
 // (src, dst, op, stage, rlo[3], rhi[3], slo[3], shi[3], blo[3])
 int wg_sync_table(wg_ctx *ctx, int tree, int gminus, int gplus, int thin, int cap, int *out) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     SyncPlan *sp;
     int st = get_sync(ctx, *t, gminus, gplus, thin != 0, &sp);
     if (st) return st;
@@ -2550,7 +2681,8 @@ int wg_sync_table(wg_ctx *ctx, int tree, int gminus, int gplus, int thin, int ca
 // block slot of block b of a tree (for tests that inspect the arena)
 int wg_block_slot(wg_ctx *ctx, int tree, int b) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || b < 0 || b >= (int)t->slots.size()) return fail(WG_EINVAL, "bad block");
+    if (!t) return tree_err();
+    if (b < 0 || b >= (int)t->slots.size()) return fail(WG_EINVAL, "bad block");
     return t->slots[b];
 }
 
@@ -2607,13 +2739,6 @@ int wg_sync_table_host(const wg_config *cfg, int nblk, const int *level, const i
 
 extern "C" {
 
-// FP64 and FP32 FMA throughput of the current device in TFLOP/s (FMA = 2)
-int wg_probe_alu(double *fp64_tflops, double *fp32_tflops) {
-    if (!fp64_tflops || !fp32_tflops) return fail(WG_EINVAL, "null output");
-    WG_CUDA_OK(probe_alu(fp64_tflops, fp32_tflops));
-    return WG_OK;
-}
-
 // Average device time of one launch of a hot-path kernel over reps launches,
 // timed with CUDA events on the context stream. which: 0 = RK stage kernel
 // (stage 2, current variant, plain + masked lists), 1 = RHS ghost sync of a
@@ -2621,7 +2746,8 @@ int wg_probe_alu(double *fp64_tflops, double *fp32_tflops) {
 // for which = 0 and 2 (stage 2 writes only the stage buffers).
 int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_launch) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || reps <= 0 || !ms_per_launch) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (reps <= 0 || !ms_per_launch) return fail(WG_EINVAL, "bad arguments");
     const int g_rhs = ctx->cfg.g_rhs;
     const int *Bs = ctx->cfg.Bs;
     SyncPlan *sp;
@@ -2654,10 +2780,51 @@ int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_la
     return WG_OK;
 }
 
+// nsteps RK4 steps of the listed trees (the same launches as wg_run without
+// a graph; batched for the FP32-pipe precision), one step at a time with CUDA
+// events on the context stream between the kernel groups; ms[9] receives the
+// mean device time per step of: sync before stages 1-4 (ms[0..3]), dt
+// (ms[4]), stages 1-4 (ms[5..8]). The state advances by nsteps steps.
+int wg_step_profile(wg_ctx *ctx, int ntrees, const int *trees, int nsteps, double *ms) {
+    if (!ctx || ntrees <= 0 || !trees || nsteps <= 0 || !ms) return fail(WG_EINVAL, "bad arguments");
+    if (ctx->dead) return fail(WG_ETIMEOUT, "the context is unusable after a timed-out device wait; destroy it");
+    for (int i = 0; i < 9; i++) ms[i] = 0.0;
+    for (cudaEvent_t &ev : ctx->prof_ev)
+        if (!ev) WG_CUDA_OK(cudaEventCreate(&ev));
+    static const int order[9][2] = {{0, 1}, {3, 4}, {5, 6}, {7, 8}, {1, 2}, {2, 3}, {4, 5}, {6, 7}, {8, 9}};
+    for (int s = 0; s < nsteps; s++) {
+        if (ctx->precision == WG_RHS_FP32) {
+            int st = wg_run(ctx, ntrees, trees, 0, 0);   // checks, shadows, batch plan
+            if (st) return st;
+            for (int i = 0; i < ntrees; i++)
+                if ((st = autotune_stage_form(ctx, ctx->trees[trees[i]]))) return st;
+            ctx->prof_on = true;
+            st = rk4_enqueue_batch(ctx);
+            ctx->prof_on = false;
+            if (st) return st;
+        } else {
+            if (ntrees != 1) return fail(WG_EINVAL, "the FP64 precision profiles one tree");
+            Tree *t = get_tree(ctx, trees[0]);
+            if (!t) return tree_err();
+            ctx->prof_on = true;
+            int st = rk4_enqueue(ctx, trees[0]);
+            ctx->prof_on = false;
+            if (st) return st;
+        }
+        WG_CUDA_OK(cudaEventSynchronize(ctx->prof_ev[9]));
+        for (int i = 0; i < 9; i++) {
+            float v = 0.f;
+            WG_CUDA_OK(cudaEventElapsedTime(&v, ctx->prof_ev[order[i][0]], ctx->prof_ev[order[i][1]]));
+            ms[i] += v / nsteps;
+        }
+    }
+    return check_dev_err(ctx);
+}
+
 // Per-block interior points and masked-block count of a tree (for the bench)
 int wg_tree_stats(wg_ctx *ctx, int tree, int *nblocks, int *nmasked) {
     Tree *t = get_tree(ctx, tree);
-    if (!t) return WG_EINVAL;
+    if (!t) return tree_err();
     if (nblocks) *nblocks = (int)t->slots.size();
     if (nmasked) *nmasked = t->n_masked;
     return WG_OK;
@@ -2762,7 +2929,8 @@ static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) 
 
 int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !host) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!host) return fail(WG_EINVAL, "bad arguments");
     t->shadow_valid = false;
     // the staging buffer is free once the stream's earlier work is done
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
@@ -2771,7 +2939,8 @@ int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
 
 int wg_download_interior(wg_ctx *ctx, int tree, double *host) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || !host) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (!host) return fail(WG_EINVAL, "bad arguments");
     return interior_transfer(ctx, t, host, 0);
 }
 
@@ -2782,7 +2951,8 @@ int wg_download_interior(wg_ctx *ctx, int tree, double *host) {
 // result.
 int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, double *const *outs) {
     Tree *t = get_tree(ctx, tree);
-    if (!t || nsteps < 0 || (nsteps && (!ins || !outs))) return fail(WG_EINVAL, "bad arguments");
+    if (!t) return tree_err();
+    if (nsteps < 0 || (nsteps && (!ins || !outs))) return fail(WG_EINVAL, "bad arguments");
     for (int k = 0; k < nsteps; k++)
         if (!ins[k] || !outs[k]) return fail(WG_EINVAL, "null buffer for step %d", k);
     if (nsteps == 0) return WG_OK;

@@ -99,7 +99,6 @@ cudaError_t stage(int dim, const StageArgs &a, int nblk, bool skew, bool mask, c
 int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
 
 // ---- kernel launchers (defined in the .cu files) -----------------------
-cudaError_t probe_alu(double *fp64_tflops, double *fp32_tflops);
 // constant-memory set-up; must run before any stream capture
 cudaError_t sync_init();
 cudaError_t wavelet_init();
@@ -134,8 +133,10 @@ cudaError_t launch_acm_stage(int variant, int dim, int stage, const int *blk, in
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
                                 const TreeParams *tp, TreeClock *clk, const void *in, const void *u0, const void *s2,
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
-                                const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int *err,
-                                cudaStream_t s);
+                                const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
+                                cudaStream_t s, int keep_state = 1);
+// (march: tmap is a map with one-plane boxes and the whole-block ring kernel
+// runs; keep_state 0 times stage 4 without storing u_n+1)
 // slab height of the TMA tile form of the double-float stage kernel (3-D,
 // Bs0*Bs1 = 256), 0 where it does not apply; tmap (a CUtensorMap over the
 // stage-input buffer: dims nx, ny, nz*nc*slots; box nx, ny, zt+4) selects it

@@ -80,6 +80,17 @@ __device__ __forceinline__ df2 df_pow2(df2 a, float s) { return {a.hi * s, a.lo 
 
 __device__ __forceinline__ df2 df_norm(df2 a) { return two_sum(a.hi, a.lo); }
 
+// The rare cases of the conversions below (zero, subnormal, inf or nan
+// operands) take the FP64 units; they are kept out of line so that the common
+// path is a real branch around them and never issues their FP64
+// instructions as predicated-off work (the FP64 units of this GPU run a warp
+// instruction in tens of cycles).
+static __device__ __noinline__ df2 df_from_slow(double v) { return df_from(v); }
+static __device__ __noinline__ double df_to_double_slow(float hi, float lo) {
+    return __dadd_rn((double)hi, (double)lo);
+}
+static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
+
 // double -> double-float by bit manipulation on the integer units: hi is v
 // truncated to 24 significant bits, lo the remainder truncated to 24 bits
 // (|v - hi - lo| < 2^-47 |v|). Zero is exact; magnitudes outside
@@ -93,7 +104,7 @@ __device__ __forceinline__ df2 df_split(double v) {
     const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
     if ((b << 1) == 0ull) return {__uint_as_float(sign), 0.f};
     const int e = (int)((b >> 52) & 0x7ff) - 1023;
-    if (e < -74 || e > 127) return df_from(v);
+    if (e < -74 || e > 127) return df_from_slow(v);
     const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
     const unsigned r = (unsigned)b & 0x1fffffffu;     // the 29 bits below hi
     if (r == 0u) return {hi, 0.f};
@@ -143,7 +154,7 @@ __host__ __device__ inline float anchor_constant(unsigned umax_bits) {
 __device__ __forceinline__ double df_to_double(df2 x) {
     const unsigned hb = __float_as_uint(x.hi), lb = __float_as_uint(x.lo);
     const int he = (int)((hb >> 23) & 0xffu);
-    if (he == 0 || he == 0xff) return __dadd_rn((double)x.hi, (double)x.lo);
+    if (he == 0 || he == 0xff) return df_to_double_slow(x.hi, x.lo);
     long long S = (long long)((hb & 0x7fffffu) | 0x800000u) << 29;   // unit 2^(e(hi) - 52)
     const int le = (int)((lb >> 23) & 0xffu);
     if (le != 0) {
@@ -167,7 +178,7 @@ __device__ __forceinline__ double df_to_double(df2 x) {
 __device__ __forceinline__ double f2d_bits(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned ex = (u >> 23) & 0xffu;
-    if (ex == 0u || ex == 0xffu) return (double)f;
+    if (ex == 0u || ex == 0xffu) return f2d_slow(f);
     const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
                                  ((unsigned long long)(ex - 127 + 1023) << 52) |
                                  ((unsigned long long)(u & 0x7fffffu) << 29);

@@ -44,6 +44,7 @@ struct StageArgsDF {
     float2 *out;           // next stage input; at stage 4 the copy of u_{n+1}
     BufGeo gt;
     double *un;            // u_n, FP64 (full layout)
+    double *un_out;        // where stage 4 stores u_n+1 (un, or null when timing the stage)
     BufGeo gun;
     const float2 *mask;    // 5 words per point, interior only
     const int *push;       // same-level ghost copies pushed by the writer, or null
@@ -203,6 +204,68 @@ __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3]
     }
 }
 
+// rhs_df for the march kernel: the x and y neighbours lie in the centre
+// plane's slot, the z neighbours in the slots of planes k-2 .. k+2 of the
+// ring (comp: stride of one component's ring, xy: offset in a plane).
+template <bool MASK>
+__device__ __forceinline__ void rhs_df_ring(const float2 *sm, int comp, int k, int xy, const float2 *ctrp,
+                                            const DfConst &d, const float2 *m, int ms, df2 r[4], df2 ctr[4]) {
+    constexpr int NS = 5, PLANE = 400;
+    const int zm2 = ((k + 0) % NS) * PLANE + xy, zm1 = ((k + 1) % NS) * PLANE + xy;
+    const int zp1 = ((k + 3) % NS) * PLANE + xy, zp2 = ((k + 4) % NS) * PLANE + xy;
+    auto at = [&](int c, int dir, int o) -> float2 {   // neighbour o (+-1, +-2) of component c along dir
+        if (dir < 2) return ctrp[c * comp + (dir == 0 ? o : o * 20)];
+        const int z = o == -2 ? zm2 : o == -1 ? zm1 : o == 1 ? zp1 : zp2;
+        return sm[c * comp + z];
+    };
+    df2 w[3], vel[3];
+#pragma unroll
+    for (int kk = 0; kk < 3; kk++) {
+        vel[kk] = ld(ctrp + kk * comp);
+        w[kk] = df_mul_nr(vel[kk], d.s1[kk]);
+    }
+    df2 div = {0.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float2 u2 = make_float2(2.f * vel[c].hi, 2.f * vel[c].lo);
+        df2 adv = {0.f, 0.f}, lap = {0.f, 0.f};
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            const float2 A = at(c, kk, 1), B = at(c, kk, -1), E = at(c, kk, 2), F = at(c, kk, -2);
+            const df2 d1 = num1(A, B, E, F);
+            const df2 ta = df_mul_nr(w[kk], d1), tl = df_mul_nr(d.s2[kk], num2(A, B, E, F, u2));
+            adv = kk == 0 ? ta : df_add_nr(adv, ta);
+            lap = kk == 0 ? tl : df_add_nr(lap, tl);
+            if (kk == c) {
+                const df2 td = df_mul_nr(d.s1[kk], d1);
+                div = c == 0 ? td : df_add_nr(div, td);
+            }
+        }
+        r[c] = df_sub_nr(lap, adv);
+    }
+    const df2 p0 = ld(ctrp + 3 * comp);
+#pragma unroll
+    for (int kk = 0; kk < 3; kk++) {
+        const df2 d1 = num1(at(3, kk, 1), at(3, kk, -1), at(3, kk, 2), at(3, kk, -2));
+        r[kk] = df_sub_nr(r[kk], df_mul_nr(d.s1[kk], d1));
+    }
+    r[3] = df_neg(df_add_nr(df_mul_nr(d.c0sq, div), df_mul_nr(d.gamma, p0)));
+    if (MASK) {
+        const df2 chi = ld(m);
+#pragma unroll
+        for (int c = 0; c < 3; c++) r[c] = df_sub_nr(r[c], df_mul_nr(chi, df_sub_nr(vel[c], ld(m + (1 + c) * ms))));
+        if (d.sponge) {
+            const df2 spo = ld(m + 4 * ms);
+#pragma unroll
+            for (int c = 0; c < 3; c++) r[c] = df_sub_nr(r[c], df_mul_nr(spo, df_sub_nr(vel[c], d.umean[c])));
+            r[3] = df_sub_nr(r[3], df_mul_nr(spo, p0));
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) ctr[c] = vel[c];
+    ctr[3] = p0;
+}
+
 // Per-point operands of the RK4 stage update that come from memory: the
 // copy of u_n (stages 2, 3), or s2, s3 and the bits of u_n (stage 4).
 template <int DIM>
@@ -242,8 +305,8 @@ __device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int ix, int
 
 // RK4 stage update of one point: stages 1-3 write the anchored next stage
 // input u_n + a dt k_j (a = 1/2, 1/2, 1), stage 4 writes u_n+1 to the FP64
-// state and its anchored copy, and returns the largest |u_n+1| of the point
-// in umax. ctr: the centre values of this stage's input (s1 = u_n at stage
+// state (unless un_out is null: a timing run) and its anchored copy, and
+// returns the largest |u_n+1| of the point in umax. ctr: the centre values of this stage's input (s1 = u_n at stage
 // 1, s4 at stage 4). (ix, iy, iz): interior coordinates; off: the point's
 // offset in the thin buffers (component 0).
 template <int DIM, int STAGE>
@@ -278,7 +341,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
             const df2 sum = df_sub_nr({sh, sl}, df_pow2(ud, 4.f));
             const df2 inc = df_norm(df_add_nr(df_mul_nr(third, sum), df_mul_nr(k.db, df_norm(r[c]))));
             const double v = __dadd_rn(u, df_to_double(inc));
-            un[c * us] = v;
+            if (a.un_out) un[c * us] = v;
             const df2 w = anchor(df_add_nr(ud, inc), k.M);
             ov[c] = make_float2(w.hi, w.lo);
             o[c * cs] = ov[c];
@@ -342,7 +405,7 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
             default: direct_point<DIM, MASK, 4>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
         }
     }
-    if (a.stage == 4) merge_umax(umax, a.clk, d.tree);
+    if (a.stage == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
 }
 
 // 3-D blocks of 16x16xBs2 points with 2 ghost layers (the stage-input
@@ -406,7 +469,83 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
         rhs_df<3, MASK>(u, COMP, stv, kc, m, npts_int, r, ctr, ctr[3]);
         rk_df<3, STAGE>(a, kc, b, ix, iy, iz, off, r, ctr, cur, umax);
     }
-    if (STAGE == 4) merge_umax(umax, a.clk, d.tree);
+    if (STAGE == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
+}
+
+// Whole-block form of the tile kernel ("march"): one CTA per 16x16x16
+// block walks its 16 planes in z. Shared memory holds a ring of 5 planes of
+// 20x20 points per component (the planes k-2 .. k+2 of the point being
+// computed, ghosts included, 64 KB), so three CTAs fit on an SM beside each
+// other; after plane k every thread has finished with plane k-2, whose slot
+// then receives plane k+3 by TMA (one box of 20x20x1 per component) while
+// the next plane is computed. The planes of a block are loaded once (20
+// planes for 16) instead of twice per 4-plane slab. A TMA completion that
+// does not arrive within a second on any thread sets *err and ends the CTA
+// after a bounded wait for the copies in flight; the context's state is then
+// undefined.
+template <bool MASK, int STAGE>
+__global__ void __launch_bounds__(256, 3) acm_stage_df_march(StageArgsDF a, const __grid_constant__ CUtensorMap tin,
+                                                             int *err) {
+    constexpr int NX = 20, NY = 20, GB = 2, BS = 16, NS = 5, NZ = 16;
+    constexpr int PLANE = NX * NY, COMP = NS * PLANE;
+    extern __shared__ __align__(128) float2 sm[];
+    __shared__ unsigned long long bar[NS];
+    const int b = a.blk[blockIdx.x];
+    // plane p (interior index -2 .. NZ+1) sits in slot (p + 2) % NS; its
+    // fill of that slot is the ((p + 2) / NS)-th
+    auto load_plane = [&](int p) {
+        const int slot = (p + 2) % NS;
+        mbar_arrive_expect_tx(&bar[slot], (unsigned)(4 * PLANE * sizeof(float2)));
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+            tma_load_3d(sm + c * COMP + slot * PLANE, &tin, 0, 0, (b * 4 + c) * a.gt.nz + p + GB, &bar[slot]);
+    };
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < NS; i++) mbar_init(&bar[i], 1);
+        for (int p = -2; p <= 2; p++) load_plane(p);
+    }
+    __syncthreads();   // the barriers are initialised before anyone waits on them
+    const BlockDesc &d = a.desc[b];
+    const DfConst kc = load_const(a, d);
+    const int ix = threadIdx.x % BS, iy = threadIdx.x / BS;
+    const int npts_int = BS * BS * a.Bs2;
+    constexpr int stv[3] = {1, NX, PLANE};
+    const long long boff = (long long)b * 4 * a.gt.npts() + (long long)(iy + GB) * NX + (ix + GB);
+    RkIn<3> nxt;
+    rk_load<3, STAGE>(a, b, ix, iy, 0, boff + (long long)GB * PLANE, nxt);
+    bool ok = true;
+    for (int p = -2; p <= 1; p++) ok &= mbar_wait(&bar[(p + 2) % NS], 0, 1000000000ull);
+    float umax = 0.f;
+#pragma unroll 1
+    for (int k = 0; k < NZ; k++) {
+        // plane k+2 completes the stencil of plane k
+        ok &= mbar_wait(&bar[(k + 4) % NS], ((k + 4) / NS) & 1, 1000000000ull);
+        const int q = (k * BS + iy) * BS + ix;
+        const long long off = boff + (long long)(k + GB) * PLANE;
+        const RkIn<3> cur = nxt;
+        if (k + 1 < NZ) rk_load<3, STAGE>(a, b, ix, iy, k + 1, off + PLANE, nxt);
+        // the ring's slots are not in z order: the stencil reads each plane
+        // through its own slot pointer
+        const float2 *ctrp = sm + ((k + 2) % NS) * PLANE + (iy + GB) * NX + (ix + GB);
+        const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
+        df2 r[4], ctr[4];
+        rhs_df_ring<MASK>(sm, COMP, k, (iy + GB) * NX + (ix + GB), ctrp, kc, m, npts_int, r, ctr);
+        rk_df<3, STAGE>(a, kc, b, ix, iy, k, off, r, ctr, cur, umax);
+        // every thread is done with plane k-2: its slot takes plane k+3; the
+        // decision to go on is the CTA's
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) {   // the copy of plane k+2 may still be landing
+                atomicExch(err, 1);
+                mbar_wait(&bar[(k + 4) % NS], ((k + 4) / NS) & 1, 1000000000ull);
+            }
+            return;
+        }
+        if (threadIdx.x == 0 && k + 3 <= NZ + 1) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            load_plane(k + 3);
+        }
+    }
+    if (STAGE == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
 }
 
 // slab height of the tile kernel (0: not applicable): 16x16 planes, two
@@ -419,8 +558,8 @@ int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g) {
 cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, int nblk, const BlockDesc *desc,
                                 const TreeParams *tp, TreeClock *clk, const void *in, const void *u0, const void *s2,
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
-                                const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int *err,
-                                cudaStream_t s) {
+                                const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
+                                cudaStream_t s, int keep_state) {
     if (nblk <= 0) return cudaSuccess;
     if (stage < 1 || stage > 4) return cudaErrorInvalidValue;
     StageArgsDF a;
@@ -435,6 +574,7 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.out = reinterpret_cast<float2 *>(out);
     a.gt = gt;
     a.un = un;
+    a.un_out = keep_state ? un : nullptr;
     a.gun = gun;
     a.mask = reinterpret_cast<const float2 *>(maskdf);
     a.push = push;
@@ -448,6 +588,22 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
         a.third[1] = (float)(t - (double)a.third[0]);
     }
     const int zt = tmap ? tile_slab(dim, Bs0, Bs1, Bs2, gt.gb) : 0;
+    if (march && zt == 4 && Bs2 == 16 && gt.nx == 20 && gt.ny == 20) {
+        const size_t smem = sizeof(float2) * 4 * 5 * (size_t)gt.nx * gt.ny;
+        const CUtensorMap &map = *reinterpret_cast<const CUtensorMap *>(tmap);
+        using K = void (*)(StageArgsDF, const CUtensorMap, int *);
+        static const K kerns[2][4] = {
+            {acm_stage_df_march<false, 1>, acm_stage_df_march<false, 2>, acm_stage_df_march<false, 3>,
+             acm_stage_df_march<false, 4>},
+            {acm_stage_df_march<true, 1>, acm_stage_df_march<true, 2>, acm_stage_df_march<true, 3>,
+             acm_stage_df_march<true, 4>}};
+        const K kern = kerns[masked ? 1 : 0][stage - 1];
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        a.chunks = 0;
+        kern<<<(unsigned)nblk, 256, smem, s>>>(a, map, err);
+        return cudaGetLastError();
+    }
     if (zt == 4 && gt.nx == 20 && gt.ny == 20) {
         const int nslab = Bs2 / zt;
         const size_t smem = sizeof(float2) * 4 * (size_t)(zt + 4) * gt.nx * gt.ny;

@@ -1,7 +1,8 @@
-// k_probe.cu -- measurement helpers: FP64/FP32 FMA throughput of this GPU
-// (the ALU denominators of the stencil roofline) and event timing of single
-// kernels of the hot path.
-#include "common.cuh"
+// k_probe.cu -- FP64/FP32 FMA throughput of this GPU (the ALU denominators
+// of the FP64 stencil and wavelet rooflines). A measurement helper, built as
+// its own library (libwg_probe.so) beside the product library and loaded only
+// by the benchmark.
+#include <cuda_runtime.h>
 
 namespace wg {
 
@@ -45,10 +46,13 @@ static cudaError_t probe_one(int iters, double *tflops) {
     return e;
 }
 
-cudaError_t probe_alu(double *fp64, double *fp32) {
-    cudaError_t e = probe_one<double>(2048, fp64);
-    if (e == cudaSuccess) e = probe_one<float>(16384, fp32);
-    return e;
-}
-
 }  // namespace wg
+
+// FP64 and FP32 FMA throughput of the current device in TFLOP/s (FMA = 2);
+// 0 on success, else the CUDA error code.
+extern "C" int wg_probe_alu(double *fp64_tflops, double *fp32_tflops) {
+    if (!fp64_tflops || !fp32_tflops) return (int)cudaErrorInvalidValue;
+    cudaError_t e = wg::probe_one<double>(2048, fp64_tflops);
+    if (e == cudaSuccess) e = wg::probe_one<float>(16384, fp32_tflops);
+    return (int)e;
+}

@@ -14,6 +14,11 @@ datasets (LIB/MODULE/module_hdf5_wrapper.f90:87,261-337).
 This module implements exactly that subset in pure numpy so that the
 reference's committed regression files can be read without libhdf5. It raises
 ``ValueError`` on anything outside the subset (filters, v2 B-trees, ...).
+
+``write_h5`` / ``save_wabbit`` write the same subset: a v0 superblock, a root
+symbol-table group, and datasets chunked as module_hdf5_wrapper.f90:261-293
+chunks them on one process (each dimension's chunk extent is the dataset's
+extent, at most 128), with the attributes saveHDF5_tree puts on ``blocks``.
 """
 from __future__ import annotations
 
@@ -295,3 +300,245 @@ def read_wabbit(path: str) -> dict:
     if "max_level" in a:
         out["max_level"] = int(np.ravel(a["max_level"])[0])
     return out
+
+
+# ============================================================================
+# writer
+# ============================================================================
+_GROUP_K = 16      # group internal node K (superblock v0 default)
+_LEAF_K = 4        # group leaf node K: a symbol-table node holds 2K entries
+_ISTORE_K = 32     # chunk B-tree K of v0 superblocks: 2K entries per node
+_MAX_CHUNK = 128   # module_hdf5_wrapper.f90:30 (max_chunk)
+
+
+def _pad8(n):
+    return (n + 7) & ~7
+
+
+def _dtype_msg(dt: np.dtype) -> bytes:
+    """Datatype message (version 1): little-endian IEEE float or integer."""
+    dt = np.dtype(dt)
+    if dt.kind == "f":
+        if dt.itemsize != 8:
+            raise ValueError("only float64 is written")
+        # class 1, bit field: little endian, implied mantissa MSB, sign at 63;
+        # offset 0, precision 64, exponent at 52 (11 bits), mantissa at 0 (52
+        # bits), bias 1023
+        return struct.pack("<BBBBIHHBBBBI", 0x11, 0x20, 0x3F, 0x00, 8, 0, 64, 52, 11, 0, 52, 1023)
+    if dt.kind in "iu":
+        bits0 = 0x08 if dt.kind == "i" else 0x00
+        return struct.pack("<BBBBIHH", 0x10, bits0, 0, 0, dt.itemsize, 0, 8 * dt.itemsize)
+    raise ValueError(f"dtype {dt} is not written")
+
+
+def _space_msg(shape) -> bytes:
+    """Dataspace message (version 1) with maximum dimensions equal to the
+    dimensions."""
+    rank = len(shape)
+    return struct.pack("<BBBB4x", 1, rank, 1, 0) + struct.pack(f"<{2 * rank}Q", *shape, *shape)
+
+
+def _attr_msg(name: str, value) -> bytes:
+    """Attribute message (version 1) of a 1-D array value."""
+    arr = np.ascontiguousarray(np.atleast_1d(value))
+    nb = name.encode() + b"\x00"
+    dtm = _dtype_msg(arr.dtype)
+    spm = _space_msg(arr.shape)
+    head = struct.pack("<BBHHH", 1, 0, len(nb), len(dtm), len(spm))
+    body = nb.ljust(_pad8(len(nb)), b"\x00") + dtm.ljust(_pad8(len(dtm)), b"\x00") + \
+        spm.ljust(_pad8(len(spm)), b"\x00") + arr.astype(arr.dtype.newbyteorder("<")).tobytes()
+    return head + body
+
+
+def _object_header(messages) -> bytes:
+    """Version-1 object header holding the (type, payload) messages in one
+    chunk, each payload padded to 8 bytes."""
+    chunk = b""
+    for mtype, payload in messages:
+        payload = payload.ljust(_pad8(len(payload)), b"\x00")
+        chunk += struct.pack("<HHB3x", mtype, len(payload), 0) + payload
+    return struct.pack("<BBHII4x", 1, 0, len(messages), 1, len(chunk)) + chunk
+
+
+class _Writer:
+    """Appends objects to a byte image; addresses are offsets in the file."""
+
+    def __init__(self):
+        self.buf = bytearray(96)   # superblock, written last
+
+    def alloc(self, n: int) -> int:
+        addr = len(self.buf)
+        self.buf += b"\x00" * _pad8(n)
+        return addr
+
+    def put(self, addr: int, data: bytes):
+        self.buf[addr:addr + len(data)] = data
+
+    def add(self, data: bytes) -> int:
+        addr = self.alloc(len(data))
+        self.put(addr, data)
+        return addr
+
+
+def _chunk_btree(w: _Writer, entries, rank: int) -> int:
+    """v1 B-tree (node type 1) over the chunks: entries are (offsets,
+    nbytes, address) in row-major chunk order, the final key one chunk past
+    the last. Nodes hold up to 2K entries; more chunks get internal levels."""
+    ksize = 8 + 8 * (rank + 1)
+    node_size = 24 + 2 * _ISTORE_K * (8 + ksize) + ksize
+
+    def key(offs, nbytes):
+        return struct.pack("<II", nbytes, 0) + struct.pack(f"<{rank + 1}Q", *offs, 0)
+
+    def write_node(level, children):
+        # children: (first key offsets, first nbytes, address, last key offsets, last nbytes)
+        addr = w.alloc(node_size)
+        out = b"TREE" + struct.pack("<BBHQQ", 1, level, len(children), _UNDEF, _UNDEF)
+        for c in children:
+            out += key(c[0], c[1]) + struct.pack("<Q", c[2])
+        out += key(children[-1][3], 0)
+        w.put(addr, out)
+        return addr
+
+    level = 0
+    nodes = [(e[0], e[1], e[2], e[3], e[1]) for e in entries]
+    cap = 2 * _ISTORE_K
+    while True:
+        groups = [nodes[i:i + cap] for i in range(0, len(nodes), cap)]
+        made = [(g[0][0], g[0][1], write_node(level, g), g[-1][3], g[-1][4]) for g in groups]
+        if len(made) == 1:
+            return made[0][2]
+        nodes = made
+        level += 1
+
+
+def _chunked_dataset(w: _Writer, name: str, data: np.ndarray, attrs: dict) -> int:
+    data = np.ascontiguousarray(data)
+    data = data.astype(data.dtype.newbyteorder("<"))
+    shape = data.shape
+    rank = len(shape)
+    chunk = tuple(min(n, _MAX_CHUNK) for n in shape)
+    nbytes = int(np.prod(chunk)) * data.itemsize
+    counts = [-(-n // c) for n, c in zip(shape, chunk)]
+    entries = []
+    for idx in np.ndindex(*counts):
+        offs = tuple(i * c for i, c in zip(idx, chunk))
+        block = np.zeros(chunk, data.dtype)
+        sl = tuple(slice(o, min(o + c, n)) for o, c, n in zip(offs, chunk, shape))
+        block[tuple(slice(0, s.stop - s.start) for s in sl)] = data[sl]
+        addr = w.add(block.tobytes())
+        past = tuple(o + c for o, c in zip(offs, chunk))
+        entries.append((offs, nbytes, addr, past))
+    btree = _chunk_btree(w, entries, rank)
+    layout = struct.pack("<BBBQ", 3, 2, rank + 1, btree) + struct.pack(f"<{rank + 1}I", *chunk, data.itemsize)
+    # fill value (version 2): allocated early, written if set, defined, none
+    msgs = [(0x01, _space_msg(shape)), (0x03, _dtype_msg(data.dtype)), (0x05, struct.pack("<BBBBI", 2, 1, 2, 1, 0)),
+            (0x08, layout)]
+    msgs += [(0x0C, _attr_msg(k, v)) for k, v in attrs.items()]
+    return w.add(_object_header(msgs))
+
+
+def write_h5(path: str, datasets: dict, attrs: dict | None = None):
+    """Write the named arrays as chunked datasets of the root group of a new
+    HDF5 file; attrs maps a dataset name to its {attribute: 1-D array}."""
+    attrs = attrs or {}
+    names = sorted(datasets, key=lambda n: n.encode())
+    if len(names) > 2 * _LEAF_K:
+        raise ValueError(f"at most {2 * _LEAF_K} datasets per file")
+    w = _Writer()
+    # local heap of the names: the empty name at 0, then each name, padded
+    # to 8 bytes, then one free block (next = 1: none, size 16)
+    heap_data = b"\x00" * 8
+    offsets = {}
+    for n in names:
+        offsets[n] = len(heap_data)
+        nb = n.encode() + b"\x00"
+        heap_data += nb.ljust(_pad8(len(nb)), b"\x00")
+    free = len(heap_data)
+    heap_data += struct.pack("<QQ", 1, 16)
+    heap_data_addr = w.add(heap_data)
+    heap_addr = w.add(b"HEAP" + struct.pack("<B3xQQQ", 0, len(heap_data), free, heap_data_addr))
+    ohdrs = {n: _chunked_dataset(w, n, datasets[n], attrs.get(n, {})) for n in names}
+    # one symbol-table node with every dataset, sorted by name
+    snod = w.alloc(8 + 2 * _LEAF_K * 40)
+    out = b"SNOD" + struct.pack("<BBH", 1, 0, len(names))
+    for n in names:
+        out += struct.pack("<QQII16x", offsets[n], ohdrs[n], 0, 0)
+    w.put(snod, out)
+    # group B-tree (node type 0): keys are heap offsets, the last the largest name
+    gnode = w.alloc(24 + 2 * _GROUP_K * 16 + 8)
+    w.put(gnode, b"TREE" + struct.pack("<BBHQQ", 0, 0, 1, _UNDEF, _UNDEF) +
+          struct.pack("<QQQ", 0, snod, offsets[names[-1]] if names else 0))
+    root = w.add(_object_header([(0x11, struct.pack("<QQ", gnode, heap_addr))]))
+    eof = len(w.buf)
+    sb = _SIG + struct.pack("<BBBBBBBBHHI", 0, 0, 0, 0, 0, 8, 8, 0, _LEAF_K, _GROUP_K, 0)
+    sb += struct.pack("<QQQQ", 0, _UNDEF, eof, _UNDEF)
+    sb += struct.pack("<QQII", 0, root, 1, 0) + struct.pack("<QQ", gnode, heap_addr)
+    assert len(sb) == 96
+    w.put(0, sb)
+    with open(path, "wb") as f:
+        f.write(bytes(w.buf))
+
+
+def treecode(level: int, coords, dim: int, max_level: int) -> int:
+    """The block's 64-bit treecode as lgt_block stores it (encoding_b,
+    LIB/TREE/module_treelib.f90:837-871 with max_level = Jmax): bit i of the
+    0-based block index along y, x, z goes to bit (i + Jmax - level) * dim +
+    (0, 1, 2)."""
+    ix = [int(coords[1]), int(coords[0])] + ([int(coords[2])] if dim == 3 else [])
+    tc = 0
+    for d in range(dim):
+        v, i = ix[d], 0
+        while v >> i:
+            tc |= ((v >> i) & 1) << ((i + max_level - level) * dim + d)
+            i += 1
+    return tc
+
+
+def timestr(time: float) -> str:
+    """The 12-digit time stamp of the reference's file names (timestr,
+    LIB/HELPER/module_helpers.f90:765-771): integer part, then micro units."""
+    ip = int(time + 1.0e-12)
+    frac = int(np.rint(max((time - np.floor(time + 1.0e-12)) * 1.0e6, 0.0)))
+    return f"{ip:06d}{frac:06d}"
+
+
+def save_wabbit(path: str, blocks, level, coords, time: float, iteration: int, domain, Bs, max_level: int,
+                refinement_status=None, lgt_ids=None, procs=None):
+    """One field file in saveHDF5_tree's layout (LIB/MESH/InputOutput.f90:
+    1-309) without ghost nodes: blocks (Nb, [Bs+1,] Bs+1, Bs+1) holding the
+    interior and the first ghost layer on the upper side, coords_origin /
+    coords_spacing in reversed axis order (z, y, x), the treecodes, levels,
+    refinement status, process ranks and light ids, and the attributes of
+    ``blocks`` (domain-size, periodic_BC, symmetry_BC, version, block-size,
+    time, iteration, total_number_blocks, max_level, dim)."""
+    blocks = np.ascontiguousarray(blocks, np.float64)
+    level = np.asarray(level, np.int64).ravel()
+    nb = len(level)
+    dim = blocks.ndim - 1
+    coords = np.asarray(coords, np.int64).reshape(nb, -1)[:, :dim]
+    domain = np.asarray(domain, np.float64).ravel()[:dim]
+    Bs = np.asarray(Bs, np.int64).ravel()[:dim]
+    if blocks.shape[0] != nb or tuple(blocks.shape[1:]) != tuple(int(b) + 1 for b in Bs[::-1]):
+        raise ValueError("blocks must be (Nb, [Bs+1,] Bs+1, Bs+1)")
+    # get_block_spacing_origin_b (module_treelib.f90:96-101)
+    dx = np.stack([2.0 ** (-level.astype(np.float64)) * domain[d] / float(Bs[d]) for d in range(dim)], axis=1)
+    x0 = np.stack([(coords[:, d] * Bs[d]).astype(np.float64) * dx[:, d] for d in range(dim)], axis=1)
+    bsz = np.ones(3, np.int32)
+    bsz[:dim] = Bs
+    ds = {
+        "blocks": blocks,
+        "coords_origin": np.ascontiguousarray(x0[:, ::-1]),
+        "coords_spacing": np.ascontiguousarray(dx[:, ::-1]),
+        "block_treecode_num": np.array([treecode(l, c, dim, max_level) for l, c in zip(level, coords)], np.int64),
+        "procs": np.zeros(nb, np.int32) if procs is None else np.asarray(procs, np.int32),
+        "refinement_status": np.zeros(nb, np.int32) if refinement_status is None
+        else np.asarray(refinement_status, np.int32),
+        "level": level.astype(np.int32),
+        "lgt_ids": np.arange(1, nb + 1, dtype=np.int32) if lgt_ids is None else np.asarray(lgt_ids, np.int32),
+    }
+    at = {"domain-size": domain, "periodic_BC": np.ones(3, np.int32), "symmetry_BC": np.zeros(3, np.int32),
+          "version": np.array([20240410], np.int32), "block-size": bsz, "time": np.array([time], np.float64),
+          "iteration": np.array([iteration], np.int32), "total_number_blocks": np.array([nb], np.int32),
+          "max_level": np.array([max_level], np.int32), "dim": np.array([dim], np.int32)}
+    write_h5(path, ds, {"blocks": at})

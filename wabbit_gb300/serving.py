@@ -8,9 +8,13 @@ sized from an HBM budget. The loop
 
 * admits queued requests first come first served per geometry as soon as
   the arena has free slots for their blocks (admission by HBM footprint),
+* serves each geometry from its own host thread (one context per thread,
+  the documented threading model): the 2-D and 3-D rounds, adaptations and
+  admissions run independently, and the two contexts' kernels overlap on
+  their own streams; a new arrival waits at most for the end of the current
+  round (one chunk) of its geometry,
 * steps every active solve of a context with one wg_run per scheduling
   round: one launch per kernel for all of them (batched FP32-pipe stages),
-  the two contexts on their own streams so that their work overlaps,
 * adapts the grids every `adapt_every` steps as the reference's main loop
   does (LIB/MAIN/main.f90:300-400: ghost sync, refine_tree "everywhere",
   N_dt_per_grid time steps, adapt_tree with the threshold-state-vector
@@ -35,6 +39,7 @@ domain, no mask.
 from __future__ import annotations
 
 import dataclasses
+import threading
 import time
 
 import numpy as np
@@ -264,108 +269,131 @@ class Server:
             c.close()
 
     def run(self, requests, realtime: bool = True):
-        """Serve the stream; returns per-request records and totals."""
-        queue = {2: [], 3: []}
-        pending = sorted(requests, key=lambda r: r.arrival)
-        active = {2: [], 3: []}
-        used = {2: 0, 3: 0}
-        records = {}
+        """Serve the stream; returns per-request records and totals. Each
+        geometry is served by its own host thread."""
         t0 = time.perf_counter()
-        total_points = 0
-        phase = {"refine": 0.0, "run": 0.0, "adapt": 0.0, "admit": 0.0, "retire": 0.0}
-        while pending or any(queue.values()) or any(active.values()):
-            now = time.perf_counter() - t0
-            if not realtime:   # every request has arrived
-                now = float("inf")
-            while pending and pending[0].arrival <= now:
-                r = pending.pop(0)
-                queue[r.dim].append(r)
-            ta = time.perf_counter()
-            for dim in (3, 2):
-                while queue[dim]:
-                    r = queue[dim][0]
-                    nb = len(request_grid(dim, r.size)[0])
-                    need = self._peak(dim, r) if self.adapt else nb
-                    if need > self.capacity[dim]:
-                        raise ValueError(f"request {r.rid} ({need} blocks at its peak) exceeds the {dim}-D arena")
-                    if used[dim] + need > self.capacity[dim]:
-                        break
-                    queue[dim].pop(0)
-                    s = Solve(r, self.ctx[dim], self.base[dim])
-                    s.admitted = time.perf_counter() - t0
-                    used[dim] += s.nblk
-                    active[dim].append(s)
-            phase["admit"] += time.perf_counter() - ta
-            if not any(active.values()):
-                if pending:
-                    time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
-                continue
-            # one scheduling round: every active solve advances one chunk
-            # (with adaptation: the solves whose cycle fits into the arena)
-            for dim in (3, 2):
-                if not active[dim]:
-                    continue
-                group = active[dim]
-                tr = time.perf_counter()
-                if self.adapt:
-                    group, grow, mothers = [], 0, 0
-                    for s in active[dim]:
-                        refined, m = s.cycle_need()
-                        if used[dim] + grow + (refined - s.nblk) + max(mothers, m) <= self.capacity[dim]:
-                            grow += refined - s.nblk
-                            mothers = max(mothers, m)
-                            s.cycle()
-                            group.append(s)
-                    used[dim] += grow
-                    if not group:
-                        raise RuntimeError(f"no {dim}-D solve fits its adaptation cycle into the arena")
-                k = min(self.chunk, min(s.req.nsteps - s.done for s in group))
-                t1 = time.perf_counter()
-                phase["refine"] += t1 - tr
-                self.ctx[dim].run([s.f for s in group], k, use_graph=True)
-                self.ctx[dim].synchronize()
-                t2 = time.perf_counter()
-                phase["run"] += t2 - t1
-                for s in group:
-                    s.done += k
-                    total_points += s.points * k
-                if self.adapt:
-                    for s in group:
-                        before = s.nblk
-                        s.nblk = s.f.adapt(np.full(s.cfg.neq, self.eps))
-                        used[dim] += s.nblk - before
-                phase["adapt"] += time.perf_counter() - t2
-            for dim in (3, 2):
-                self.ctx[dim].synchronize()
-            tt = time.perf_counter()
-            for dim in (3, 2):
-                keep = []
-                for s in active[dim]:
-                    if s.done < s.req.nsteps:
-                        keep.append(s)
-                        continue
-                    shape = (s.nblk,) + s.f.interior_shape
-                    flat = self._result_buffer(dim, int(np.prod(shape)))
-                    u = s.f.download_interior(out=flat.reshape(shape))
-                    t_done = time.perf_counter() - t0
-                    rec = {"rid": s.req.rid, "dim": dim, "blocks": s.nblk, "arrival": s.req.arrival,
-                           "admitted": s.admitted, "done": t_done,
-                           "tts": t_done - (s.req.arrival if realtime else 0.0),
-                           "time": s.f.time()[0], "checksum": float(np.dot(flat, flat))}
-                    if self.keep:
-                        rec["u"] = u.copy()
-                    records[s.req.rid] = rec
-                    s.f.destroy()
-                    used[dim] -= s.nblk
-                active[dim] = keep
-            phase["retire"] += time.perf_counter() - tt
+        out = {}
+        errors = []
+
+        def worker(dim):
+            try:
+                out[dim] = self._serve(dim, [r for r in requests if r.dim == dim], t0, realtime)
+            except BaseException as e:   # re-raised below
+                errors.append(e)
+
+        ths = [threading.Thread(target=worker, args=(dim,), name=f"serve-{dim}d") for dim in (3, 2)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        if errors:
+            raise errors[0]
         wall = time.perf_counter() - t0
-        tts = np.array([r["tts"] for r in records.values()])
+        records = {}
+        total_points = 0
+        phase = {}
+        for dim in (3, 2):
+            rec, pts, ph = out[dim]
+            records.update(rec)
+            total_points += pts
+            for k, v in ph.items():
+                phase[f"{k}_{dim}d"] = v
+        tts = np.array([r["tts"] for r in records.values()]) if records else np.zeros(1)
         summary = {"requests": len(records), "wall_s": wall, "point_updates": total_points,
                    "throughput": total_points / wall,
                    "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
                    "phase_s": phase}
         return records, summary
+
+    def _serve(self, dim, requests, t0, realtime):
+        """The scheduling loop of one geometry (its own thread and context)."""
+        ctx = self.ctx[dim]
+        pending = sorted(requests, key=lambda r: r.arrival)
+        queue, active = [], []
+        used = 0
+        records = {}
+        total_points = 0
+        phase = {"admit": 0.0, "refine": 0.0, "run": 0.0, "retire": 0.0}
+        while pending or queue or active:
+            now = time.perf_counter() - t0
+            if not realtime:   # every request has arrived
+                now = float("inf")
+            while pending and pending[0].arrival <= now:
+                queue.append(pending.pop(0))
+            ta = time.perf_counter()
+            while queue:
+                r = queue[0]
+                nb = len(request_grid(dim, r.size)[0])
+                need = self._peak(dim, r) if self.adapt else nb
+                if need > self.capacity[dim]:
+                    raise ValueError(f"request {r.rid} ({need} blocks at its peak) exceeds the {dim}-D arena")
+                if used + need > self.capacity[dim]:
+                    break
+                queue.pop(0)
+                s = Solve(r, ctx, self.base[dim])
+                s.admitted = time.perf_counter() - t0
+                used += s.nblk
+                active.append(s)
+            phase["admit"] += time.perf_counter() - ta
+            if not active:
+                if pending:
+                    time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
+                continue
+            # one scheduling round: every active solve advances one chunk
+            # (with adaptation: the solves whose cycle fits into the arena)
+            group = active
+            tr = time.perf_counter()
+            if self.adapt:
+                group, grow, mothers = [], 0, 0
+                for s in active:
+                    refined, m = s.cycle_need()
+                    if used + grow + (refined - s.nblk) + max(mothers, m) <= self.capacity[dim]:
+                        grow += refined - s.nblk
+                        mothers = max(mothers, m)
+                        s.cycle()
+                        group.append(s)
+                used += grow
+                if not group:
+                    raise RuntimeError(f"no {dim}-D solve fits its adaptation cycle into the arena")
+            k = min(self.chunk, min(s.req.nsteps - s.done for s in group))
+            t1 = time.perf_counter()
+            phase["refine"] += t1 - tr
+            ctx.run([s.f for s in group], k, use_graph=True)
+            for s in group:
+                s.done += k
+                total_points += s.points * k
+            if self.adapt:
+                # each adaptation waits for the batched steps on the stream
+                for s in group:
+                    before = s.nblk
+                    s.nblk = s.f.adapt(np.full(s.cfg.neq, self.eps))
+                    used += s.nblk - before
+            else:
+                ctx.synchronize()
+            t2 = time.perf_counter()
+            phase["run"] += t2 - t1   # the chunk's steps and the adaptations that follow them
+            tt = time.perf_counter()
+            keep = []
+            for s in active:
+                if s.done < s.req.nsteps:
+                    keep.append(s)
+                    continue
+                shape = (s.nblk,) + s.f.interior_shape
+                flat = self._result_buffer(dim, int(np.prod(shape)))
+                u = s.f.download_interior(out=flat.reshape(shape))
+                t_done = time.perf_counter() - t0
+                rec = {"rid": s.req.rid, "dim": dim, "blocks": s.nblk, "arrival": s.req.arrival,
+                       "admitted": s.admitted, "done": t_done,
+                       "tts": t_done - (s.req.arrival if realtime else 0.0),
+                       "time": s.f.time()[0], "checksum": float(np.dot(flat, flat))}
+                if self.keep:
+                    rec["u"] = u.copy()
+                records[s.req.rid] = rec
+                s.f.destroy()
+                used -= s.nblk
+            active = keep
+            phase["retire"] += time.perf_counter() - tt
+        return records, total_points, phase
 
 
 def solve_alone(req: Request, chunk: int = 5, adapt_every: int = 0, eps: float = 1e-3, max_blocks: int = 0):

@@ -17,9 +17,16 @@ from .config import WgConfig
 
 
 def probe_alu():
-    """FP64 and FP32 FMA throughput of the current GPU in TFLOP/s."""
+    """FP64 and FP32 FMA throughput of the current GPU in TFLOP/s, from the
+    measurement library libwg_probe.so (not part of the product library)."""
+    from . import build
+    lib = ctypes.CDLL(build.build_probe())
+    lib.wg_probe_alu.restype = ctypes.c_int
+    lib.wg_probe_alu.argtypes = [ctypes.POINTER(ctypes.c_double)] * 2
     a, b = ctypes.c_double(), ctypes.c_double()
-    capi.check(capi.load().wg_probe_alu(ctypes.byref(a), ctypes.byref(b)))
+    rc = lib.wg_probe_alu(ctypes.byref(a), ctypes.byref(b))
+    if rc != 0:
+        raise RuntimeError(f"wg_probe_alu: CUDA error {rc}")
     return a.value, b.value
 
 
@@ -54,17 +61,30 @@ class Context:
     def set_variant(self, fast: bool):
         capi.check(self.L.wg_set_variant(self.h, 1 if fast else 0))
 
-    FORMS = {"auto": 0, "direct": 1, "tile": 2}
+    FORMS = {"auto": 0, "direct": 1, "tile": 2, "march": 3}
 
     def set_stage_form(self, form: str):
-        """Form of the FP32-pipe stage kernel: auto (timed once per grid),
-        direct or tile (TMA-staged slabs)."""
+        """Form of the FP32-pipe stage kernel: auto (each RK stage timed in
+        every applicable form before the first step), direct, tile (TMA-staged
+        4-plane slabs) or march (whole blocks through a TMA plane ring)."""
         capi.check(self.L.wg_set_stage_form(self.h, self.FORMS[form]))
 
     def stage_form(self) -> str:
         f = ctypes.c_int()
         capi.check(self.L.wg_get_stage_form(self.h, ctypes.byref(f)))
         return {v: k for k, v in self.FORMS.items()}[f.value]
+
+    def set_stage_forms(self, forms):
+        """Fix the forms of RK stages 1-4 (names: direct, tile, march)."""
+        f = (ctypes.c_int * 4)(*[self.FORMS[x] for x in forms])
+        capi.check(self.L.wg_set_stage_forms(self.h, f))
+
+    def stage_forms(self) -> list:
+        """The forms of RK stages 1-4."""
+        f = (ctypes.c_int * 4)()
+        capi.check(self.L.wg_get_stage_forms(self.h, f))
+        names = {v: k for k, v in self.FORMS.items()}
+        return [names[x] for x in f]
 
     def synchronize(self):
         capi.check(self.L.wg_synchronize(self.h))
@@ -75,6 +95,16 @@ class Context:
     def run(self, forests, nsteps: int, use_graph: bool = True):
         ids = np.array([f.tree for f in forests], np.int32)
         capi.check(self.L.wg_run(self.h, len(ids), _p(ids, ctypes.c_int), int(nsteps), 1 if use_graph else 0))
+
+    PROFILE_KEYS = ("sync1", "sync2", "sync3", "sync4", "dt", "stage1", "stage2", "stage3", "stage4")
+
+    def step_profile(self, forests, nsteps: int) -> dict:
+        """Mean device time (ms) per RK4 step of each kernel group over
+        nsteps profiled steps (the state advances)."""
+        ids = np.array([f.tree for f in forests], np.int32)
+        ms = np.zeros(9)
+        capi.check(self.L.wg_step_profile(self.h, len(ids), _p(ids, ctypes.c_int), int(nsteps), _p(ms)))
+        return dict(zip(self.PROFILE_KEYS, ms.tolist()))
 
     @property
     def stream(self) -> int:
@@ -132,6 +162,63 @@ class Forest:
         out = np.zeros((self.nblocks,) + self.block_shape)
         capi.check(self.L.wg_download_state(self.ctx.h, self.tree, _p(out)))
         return out
+
+    # ------------------------------------------------------------ files
+    FIELD_NAMES = {2: ("ux", "uy", "p"), 3: ("ux", "uy", "uz", "p")}
+
+    def save_hdf5(self, directory: str, iteration: int = 0, names=None) -> list:
+        """save_data (LIB/IO/save_data.f90:1-90): one file per component,
+        <name>_<timestr>.h5 in saveHDF5_tree's layout (interior plus the
+        first ghost layer on the upper side, after a ghost sync of g
+        layers). Returns the paths written."""
+        import os
+
+        from . import h5io
+        c = self.cfg
+        dim = c.dim
+        names = names or self.FIELD_NAMES[dim]
+        self.sync_ghosts_tree()
+        full = self.download()                       # (Nb, neq, nz, ny, nx)
+        lv, co = self.grid()
+        t, _ = self.time()
+        g = c.g
+        sl = (slice(g, g + c.Bs[1] + 1), slice(g, g + c.Bs[0] + 1))
+        if dim == 3:
+            sl = (slice(g, g + c.Bs[2] + 1),) + sl
+        out = []
+        for k, name in enumerate(names):
+            comp = full[:, k] if dim == 3 else full[:, k, 0]
+            path = os.path.join(directory, f"{name}_{h5io.timestr(t)}.h5")
+            h5io.save_wabbit(path, comp[(slice(None),) + sl], lv, co[:, :dim], t, iteration,
+                             list(c.domain)[:dim], list(c.Bs)[:dim], c.Jmax)
+            out.append(path)
+        return out
+
+    def load_hdf5(self, paths):
+        """The grid, state and time from field files of one time stamp (one
+        file per component, in component order), as the reference's
+        readHDF5vct_tree does for a restart (LIB/MESH/InputOutput.f90:322)."""
+        from . import h5io
+        ds = [h5io.read_wabbit(p) for p in paths]
+        if len(ds) != self.cfg.neq:
+            raise ValueError(f"expected {self.cfg.neq} files, one per component")
+        c = self.cfg
+        lv, co = ds[0]["level"], ds[0]["coords"]
+        for d in ds[1:]:
+            if not (np.array_equal(d["level"], lv) and np.array_equal(d["coords"], co)):
+                raise ValueError("the files hold different grids")
+        if list(ds[0]["Bs"]) != list(c.Bs)[:c.dim]:
+            raise ValueError("block size of the files differs from the configuration")
+        co3 = np.zeros((len(lv), 3), np.int32)
+        co3[:, :c.dim] = co
+        self.set_grid(lv, co3)
+        inner = tuple(slice(0, b) for b in list(c.Bs)[:c.dim][::-1])
+        u = np.stack([d["blocks"][(slice(None),) + inner] for d in ds], axis=1)
+        if c.dim == 2:
+            u = u[:, :, None]
+        self.upload_interior(np.ascontiguousarray(u))
+        self.set_time(ds[0]["time"])
+        return ds[0]["iteration"]
 
     @property
     def interior_shape(self):
