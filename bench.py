@@ -201,8 +201,8 @@ TRAFFIC_JMAX = 5
 def run_traffic_case(args):
     """The small case the traffic capture profiles: the workload at Jmax=5,
     the given stage forms, one RK4 step of batched launches without a graph
-    (each stage kernel launched for the unmasked and the masked block list).
-    Prints the grid's sizes as JSON."""
+    (two launches per RK stage: unmasked and masked blocks). Prints the
+    grid's sizes as JSON."""
     import torch
     from wabbit_gb300 import build, workloads
     from wabbit_gb300.solver import Context
@@ -225,11 +225,11 @@ def run_traffic_case(args):
 
 
 def measure_traffic(args, forms):
-    """DRAM bytes of each RK stage's kernels (unmasked + masked launch) per
-    interior point, from ncu on the small case (one pass: two DRAM counters
-    of one unit, 8 launches, no replay of device memory). The small case is
-    first run without ncu and must exit 0. Returns (per-stage bytes per
-    point, description) or (None, reason)."""
+    """DRAM bytes of each RK stage's kernels per interior point, from ncu on
+    the small case (one pass: two DRAM counters of one unit, the 8 stage
+    launches of one step -- unmasked and masked blocks per stage -- no replay
+    of device memory). The small case is first run without ncu and must exit
+    0. Returns (per-stage bytes per point, description) or (None, reason)."""
     cmd = [sys.executable, os.path.abspath(__file__), "--traffic-case", "--workload", args.workload,
            "--stage-form", ",".join(forms)]
     try:
@@ -271,7 +271,7 @@ def measure_traffic(args, forms):
     if len(ids) != 8:
         return None, f"expected 8 stage launches in the capture, got {len(ids)}"
     per_stage = [(launches[ids[2 * j]] + launches[ids[2 * j + 1]]) / info["points"] for j in range(4)]
-    desc = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the 8 stage launches (unmasked + masked, "
+    desc = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the 8 stage launches (unmasked + masked blocks, "
             f"RK stages 1-4) of one step of {args.workload} at Jmax={TRAFFIC_JMAX} ({info['blocks']} blocks, "
             f"{info['masked_blocks']} masked), per interior point, scaled to the full grid by its points")
     return per_stage, desc
@@ -568,16 +568,15 @@ def serving_block(args, rank, world):
     import torch
     from wabbit_gb300 import serving
     stream = serving.make_stream(args.serving_requests, rate=args.rate, seed=4 + rank)
-    srv = serving.Server(budget_gb=min(args.budget_gb, 48.0), chunk=5, adapt_every=5)
-    srv.run([serving.Request(-1, 0.0, 2, 0, 1, 1e-3, nsteps=5), serving.Request(-2, 0.0, 3, 0, 2, 1e-3, nsteps=5)],
-            realtime=False)
+    srv = serving.Server(budget_gb=args.budget_gb, chunk=5, adapt_every=5)
+    srv.warm_up()
     torch.cuda.synchronize()
     recs, summ = srv.run(stream, realtime=True)
     srv.close()
     return {"requests": summ["requests"], "arrival_rate_per_s": args.rate, "steps_per_solve": 50,
             "adapt_every": 5, "value": sum_over_ranks(summ["point_updates"], world) / max_over_ranks(
                 summ["wall_s"], world), "unit": "point-updates/s", "p50_s": summ["p50_s"], "p99_s": summ["p99_s"],
-            "wall_s": summ["wall_s"], "phase_s": summ["phase_s"],
+            "wall_s": summ["wall_s"], "phase_s": summ["phase_s"], "contexts_blocks": summ["workers"],
             "note": "time to solution = arrival to result on the host; IC generated on the device at admission "
                     "(inside the window); full stream: --workload serving --requests 256"}
 
@@ -637,9 +636,8 @@ def run_serving(args, rank, world):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     stream = serving.make_stream(args.requests, rate=args.rate, seed=4 + rank)
     srv = serving.Server(budget_gb=args.budget_gb, chunk=5, adapt_every=args.adapt_every)
-    # warm-up: one small solve of each geometry (graph capture, autotuning)
-    srv.run([serving.Request(-1, 0.0, 2, 0, 1, 1e-3, nsteps=5), serving.Request(-2, 0.0, 3, 0, 2, 1e-3, nsteps=5)],
-            realtime=False)
+    # warm-up: one small solve on every context (graph capture, autotuning)
+    srv.warm_up()
     barrier(world)
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         recs, summ = srv.run(stream, realtime=True)
@@ -658,7 +656,7 @@ def run_serving(args, rank, world):
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "serving": {"p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "wall_s": summ["wall_s"],
                     "requests": summ["requests"], "point_updates": summ["point_updates"],
-                    "phase_s": summ["phase_s"]},
+                    "phase_s": summ["phase_s"], "contexts_blocks": summ["workers"]},
         "clocks": clk.summary(),
     }
     if rank == 0:

@@ -23,7 +23,7 @@ def test_served_equals_alone_and_admission_waits():
         Request(3, 0.02, 3, 1, 104, 7e-4, nsteps=10),   # 960 blocks: waits for a 512-block solve
         Request(4, 0.02, 2, 0, 105, 5e-3, nsteps=15),
     ]
-    srv = serving.Server(budget_gb=2.3, chunk=5, keep_results=True)
+    srv = serving.Server(budget_gb=2.3, chunk=5, keep_results=True, workers={3: 1, 2: 1})
     try:
         assert 1024 <= srv.capacity[3] < 1472
         recs, summ = srv.run(reqs, realtime=False)
@@ -69,3 +69,23 @@ def test_served_with_adaptation_equals_alone():
         assert np.array_equal(recs[r.rid]["u"], u), r.rid
         assert recs[r.rid]["time"] == t
         assert np.isfinite(u).all() and np.abs(u).max() > 0
+
+
+def test_several_contexts_per_geometry_equal_alone():
+    """Two 3-D contexts (the first sized for the largest request, each served
+    by its own host thread) with the adaptation cycle: every served solve
+    equals the same solve alone, and both contexts take requests."""
+    reqs = [Request(i, 0.005 * i, 3, i % 2, 300 + i, 1e-3 * (1 + i), nsteps=10) for i in range(6)]
+    reqs.append(Request(6, 0.0, 2, 1, 306, 2e-3, nsteps=10))
+    srv = serving.Server(budget_gb=24.0, keep_results=True, adapt_every=5, workers={3: 2, 2: 1})
+    try:
+        assert len(srv.workers[3]) == 2
+        recs, summ = srv.run(reqs, realtime=False)
+    finally:
+        srv.close()
+    assert summ["requests"] == len(reqs)
+    assert {recs[r.rid]["worker"] for r in reqs if r.dim == 3} == {0, 1}
+    for r in reqs:
+        u, t = serving.solve_alone(r, adapt_every=5)
+        assert np.array_equal(recs[r.rid]["u"], u), r.rid
+        assert recs[r.rid]["time"] == t

@@ -145,9 +145,11 @@ struct SlotPool {
     }
 };
 
-// Prediction patches of the stages of a table, sorted within each stage by
-// the shared memory the CTA-per-patch kernel needs and cut into classes;
-// each class launches with its own largest need.
+// Prediction patches of the stages of a table for one launch per stage,
+// sorted within each stage by the shared memory the CTA-per-patch kernel
+// needs, largest first (the long CTAs start first); the launch sizes its
+// shared memory for the largest and runs as many components per pass as
+// keep four CTAs on an SM.
 struct PredClasses {
     DevArray<Patch> patches;                 // sorted copy
     std::vector<std::vector<int>> begin;     // per stage: class offsets into patches (n_class+1)
@@ -179,6 +181,7 @@ struct BatchPlan {
     std::vector<int> trees;
     int version = -1;
     DevArray<int> all, plain, masked, tree_ids;
+    DevArray<int> stage;                // the FP32-pipe stage order: masked blocks first (the longer CTAs)
     int n_all = 0, n_plain = 0, n_masked = 0;
     int nstages = 0;
     std::vector<int> stage_predict;
@@ -199,6 +202,7 @@ struct Tree {
     std::vector<int> slots;            // block -> arena slot
     std::vector<int> mask_slot;        // block -> mask slot or -1
     DevArray<int> d_all, d_plain, d_masked;   // slot lists
+    DevArray<int> d_stage;                    // masked slots, then the others (FP32-pipe stage launches)
     int n_plain = 0, n_masked = 0;
     std::map<long long, std::unique_ptr<SyncPlan>> sync;   // key: gm, gp, buffer
     std::map<long long, std::unique_ptr<SyncPlan>> spare;  // plans of an earlier grid: device buffers to reuse
@@ -371,25 +375,12 @@ int build_pred_classes(wg_ctx *ctx, const std::vector<Patch> &pt, const std::vec
         if (!stage_predict[st]) continue;
         std::vector<std::pair<int, int>> byneed;
         for (int i = stage_begin[st]; i < stage_begin[st + 1]; i++)
-            byneed.push_back({pred_need(pt[i], ctx->wav.order_predictor), i});
+            byneed.push_back({-pred_need(pt[i], ctx->wav.order_predictor), i});
         std::stable_sort(byneed.begin(), byneed.end());
-        // classes: a class grows while its largest need stays within twice
-        // its smallest
         const int base = (int)sorted.size();
-        pc.begin[st].push_back(base);
-        int lo_need = byneed.empty() ? 0 : byneed[0].first;
-        for (size_t k = 0; k < byneed.size(); k++) {
-            if (byneed[k].first > 2 * lo_need && k > 0) {
-                pc.need[st].push_back(byneed[k - 1].first);
-                pc.begin[st].push_back(base + (int)k);
-                lo_need = byneed[k].first;
-            }
-            sorted.push_back(pt[byneed[k].second]);
-        }
-        if (!byneed.empty()) {
-            pc.need[st].push_back(byneed.back().first);
-            pc.begin[st].push_back(base + (int)byneed.size());
-        }
+        for (const auto &e : byneed) sorted.push_back(pt[e.second]);
+        pc.begin[st] = {base, base + (int)byneed.size()};
+        pc.need[st] = {byneed.empty() ? 0 : -byneed.front().first};
     }
     WG_CUDA_OK(pc.patches.upload(sorted.data(), sorted.size(), ctx->stream));
     return WG_OK;
@@ -399,7 +390,7 @@ int run_pred_classes(wg_ctx *ctx, const PredClasses &pc, int st, double *buf, co
     const std::vector<int> &b = pc.begin[st];
     for (size_t k = 0; k + 1 < b.size(); k++)
         WG_CUDA_OK(launch_predict_df(pc.patches.p + b[k], b[k + 1] - b[k], pc.need[st][k], buf, geo, ctx->geo.nc,
-                                     ctx->wav.order_predictor, ctx->d_desc, ctx->d_clk, ctx->stream));
+                                     ctx->wav.order_predictor, ctx->d_desc, ctx->d_clk, ctx->stream, 4));
     return WG_OK;
 }
 
@@ -595,6 +586,9 @@ int upload_lists(wg_ctx *ctx, Tree &t) {
     WG_CUDA_OK(t.d_all.upload(t.slots.data(), t.slots.size(), ctx->stream));
     WG_CUDA_OK(t.d_plain.upload(plain.data(), plain.size(), ctx->stream));
     WG_CUDA_OK(t.d_masked.upload(masked.data(), masked.size(), ctx->stream));
+    std::vector<int> order(masked);
+    order.insert(order.end(), plain.begin(), plain.end());
+    WG_CUDA_OK(t.d_stage.upload(order.data(), order.size(), ctx->stream));
     return WG_OK;
 }
 
@@ -678,23 +672,33 @@ static void form_args(wg_ctx *ctx, int stage, const double *in, const void **tm,
     }
 }
 
+// the two launches of an FP32-pipe stage, one after the other: the unmasked
+// blocks' kernel and the masked blocks' kernel (the mask words compiled out
+// of the first; one kernel testing the mask per block was 3 % slower, and
+// the two kernels side by side on two streams 25 % slower in the last stage)
+static int stage_pair(wg_ctx *ctx, int stage, const int *plain, int nplain, const int *masked, int nmasked,
+                      const double *in, double *out, const int *pp, int keep) {
+    const int dim = ctx->cfg.dim;
+    const int *Bs = ctx->cfg.Bs;
+    const void *tm = nullptr;
+    int march = 0;
+    form_args(ctx, stage, in, &tm, &march);
+    auto go = [&](int msk, const int *blk, int n) {
+        return launch_acm_stage_df(dim, stage, msk, blk, n, ctx->d_desc, ctx->d_tp, ctx->d_clk, in, ctx->B, ctx->C,
+                                   ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0], Bs[1], Bs[2], tm,
+                                   march, ctx->d_err, ctx->stream, keep);
+    };
+    WG_CUDA_OK(go(0, plain, nplain));
+    WG_CUDA_OK(go(1, masked, nmasked));
+    return WG_OK;
+}
+
 // u0 is always B (the anchored copy of u_n), the inputs of stages 2 and 3
 // are C and D; with push the kernels also write the same-level ghost copies
 // of out
 int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *out, bool push, int keep = 1) {
-    const int dim = ctx->cfg.dim;
-    const int *Bs = ctx->cfg.Bs;
-    const int *pp = push ? ctx->d_push : nullptr;
-    const void *tm = nullptr;
-    int march = 0;
-    form_args(ctx, stage, in, &tm, &march);
-    WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, t.d_plain.p, t.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
-                                   Bs[1], Bs[2], tm, march, ctx->d_err, ctx->stream, keep));
-    WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, t.d_masked.p, t.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
-                                   Bs[1], Bs[2], tm, march, ctx->d_err, ctx->stream, keep));
-    return WG_OK;
+    return stage_pair(ctx, stage, t.d_plain.p, t.n_plain, t.d_masked.p, t.n_masked, in, out,
+                      push ? ctx->d_push : nullptr, keep);
 }
 
 // TMA maps over the four thin double-float buffers: a 3-D tensor of 8-byte
@@ -901,6 +905,11 @@ int build_batch(wg_ctx *ctx, const std::vector<int> &trees) {
     WG_CUDA_OK(bp.all.upload(all.data(), all.size(), ctx->stream));
     WG_CUDA_OK(bp.plain.upload(plain.data(), plain.size(), ctx->stream));
     WG_CUDA_OK(bp.masked.upload(masked.data(), masked.size(), ctx->stream));
+    {
+        std::vector<int> order(masked);
+        order.insert(order.end(), plain.begin(), plain.end());
+        WG_CUDA_OK(bp.stage.upload(order.data(), order.size(), ctx->stream));
+    }
     WG_CUDA_OK(bp.tree_ids.upload(trees.data(), trees.size(), ctx->stream));
     // gather entries and prediction patches, stage by stage
     bp.nstages = ns;
@@ -970,21 +979,9 @@ int run_sync_batch(wg_ctx *ctx, double *buf) {
 }
 
 int stage_launch_batch(wg_ctx *ctx, int stage, const double *in, double *out) {
-    const int keep = 1;
     const BatchPlan &bp = ctx->batch;
-    const int dim = ctx->cfg.dim;
-    const int *Bs = ctx->cfg.Bs;
-    const int *pp = bp.push ? ctx->d_push : nullptr;
-    const void *tm = nullptr;
-    int march = 0;
-    form_args(ctx, stage, in, &tm, &march);
-    WG_CUDA_OK(launch_acm_stage_df(dim, stage, 0, bp.plain.p, bp.n_plain, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
-                                   Bs[1], Bs[2], tm, march, ctx->d_err, ctx->stream, keep));
-    WG_CUDA_OK(launch_acm_stage_df(dim, stage, 1, bp.masked.p, bp.n_masked, ctx->d_desc, ctx->d_tp, ctx->d_clk, in,
-                                   ctx->B, ctx->C, ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0],
-                                   Bs[1], Bs[2], tm, march, ctx->d_err, ctx->stream, keep));
-    return WG_OK;
+    return stage_pair(ctx, stage, bp.plain.p, bp.n_plain, bp.masked.p, bp.n_masked, in, out,
+                      bp.push ? ctx->d_push : nullptr, 1);
 }
 
 // one RK4 step of every tree of ctx->batch (FP32-pipe precision): the same

@@ -154,7 +154,8 @@ cudaError_t launch_anchor_from_state(const int *slots, int nblk, const double *A
                                      int Bz, const BlockDesc *desc, TreeClock *clk, const int *trees, int ntrees,
                                      int scan, cudaStream_t s);
 cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
-                              int order_predictor, const BlockDesc *desc, const TreeClock *clk, cudaStream_t s);
+                              int order_predictor, const BlockDesc *desc, const TreeClock *clk, cudaStream_t s,
+                              int min_ctas = 1);
 cudaError_t launch_rhs_only(int variant, int dim, const int *blk, int nblk, const BlockDesc *desc,
                             const TreeParams *tp, const double *in, BufGeo gin, double *rhs, const double *mask,
                             int Bs0, int Bs1, int Bs2, int nc, cudaStream_t s);
@@ -173,6 +174,7 @@ cudaError_t launch_sphere_fill(const int4 *cand, const int *slot, int n, const S
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
                       const int *trees, cudaStream_t s, int step_start = 0);
+
 cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
 // max |u| per component over the interiors of the listed blocks (Bs2 = 1 in 2-D)
 cudaError_t launch_norm_linf(const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int nc,

@@ -153,7 +153,7 @@ __device__ __forceinline__ df2 num2(float2 A, float2 B, float2 E, float2 F, floa
 // sponge of :1734-1753) from an anchored stencil input with strides stv
 // (shared or global memory). m: the point's double-float mask words (stride
 // ms), or null. Returns the RHS in r and the centre values vel, p0.
-template <int DIM, bool MASK, typename Idx>
+template <int DIM, typename Idx>
 __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3], const DfConst &d,
                                        const float2 *m, int ms, df2 r[DIM + 1], df2 vel[DIM], df2 &p0) {
     df2 w[DIM];
@@ -190,7 +190,7 @@ __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3]
         r[k] = df_sub_nr(r[k], df_mul_nr(d.s1[k], d1));
     }
     r[DIM] = df_neg(df_add_nr(df_mul_nr(d.c0sq, div), df_mul_nr(d.gamma, p0)));
-    if (MASK) {
+    if (m) {   // masked block (uniform over the CTA)
         const df2 chi = ld(m);
 #pragma unroll
         for (int c = 0; c < DIM; c++) r[c] = df_sub_nr(r[c], df_mul_nr(chi, df_sub_nr(vel[c], ld(m + (1 + c) * ms))));
@@ -207,7 +207,6 @@ __device__ __forceinline__ void rhs_df(const float2 *u, Idx cs, const int stv[3]
 // rhs_df for the march kernel: the x and y neighbours lie in the centre
 // plane's slot, the z neighbours in the slots of planes k-2 .. k+2 of the
 // ring (comp: stride of one component's ring, xy: offset in a plane).
-template <bool MASK>
 __device__ __forceinline__ void rhs_df_ring(const float2 *sm, int comp, int k, int xy, const float2 *ctrp,
                                             const DfConst &d, const float2 *m, int ms, df2 r[4], df2 ctr[4]) {
     constexpr int NS = 5, PLANE = 400;
@@ -250,7 +249,7 @@ __device__ __forceinline__ void rhs_df_ring(const float2 *sm, int comp, int k, i
         r[kk] = df_sub_nr(r[kk], df_mul_nr(d.s1[kk], d1));
     }
     r[3] = df_neg(df_add_nr(df_mul_nr(d.c0sq, div), df_mul_nr(d.gamma, p0)));
-    if (MASK) {
+    if (m) {   // masked block (uniform over the CTA)
         const df2 chi = ld(m);
 #pragma unroll
         for (int c = 0; c < 3; c++) r[c] = df_sub_nr(r[c], df_mul_nr(chi, df_sub_nr(vel[c], ld(m + (1 + c) * ms))));
@@ -367,18 +366,20 @@ __device__ __forceinline__ void merge_umax(float umax, TreeClock *clk, int tree)
 // One thread per interior point, stencil values read from global memory.
 // BS: the block edge when all Bs are equal to it (index arithmetic by
 // shifts), 0 for the general case.
-template <int DIM, bool MASK, int STAGE>
+template <int DIM, int STAGE>
 __device__ __forceinline__ void direct_point(const StageArgsDF &a, const DfConst &k, const float2 *u, long long cs,
                                              const int stv[3], const float2 *m, int ms, int b, int ix, int iy, int iz,
                                              long long off, float &umax) {
     df2 r[DIM + 1], ctr[DIM + 1];
     RkIn<DIM> in;
     rk_load<DIM, STAGE>(a, b, ix, iy, iz, off, in);
-    rhs_df<DIM, MASK>(u, cs, stv, k, m, ms, r, ctr, ctr[DIM]);
+    rhs_df<DIM>(u, cs, stv, k, m, ms, r, ctr, ctr[DIM]);
     rk_df<DIM, STAGE>(a, k, b, ix, iy, iz, off, r, ctr, in, umax);
 }
 
-template <int DIM, bool MASK, int BS>
+// Masked blocks (d.mask >= 0) and unmasked ones share the launch; the branch
+// between the two bodies is uniform per CTA.
+template <int DIM, int BS, bool MASKED>
 __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
     const int Bs0 = BS ? BS : a.Bs0, Bs1 = BS ? BS : a.Bs1, Bs2 = BS ? BS : a.Bs2;
     const int npts_int = Bs0 * Bs1 * (DIM == 3 ? Bs2 : 1);
@@ -395,14 +396,14 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
                               ((long long)(iz + (DIM == 3 ? a.gt.gb : 0)) * a.gt.ny + (iy + a.gt.gb)) * a.gt.nx +
                               (ix + a.gt.gb);
         const int stv[3] = {1, a.gt.nx, a.gt.nx * a.gt.ny};
-        const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
         const DfConst k = load_const(a, d);
         const float2 *u = a.in + off;
+        const float2 *m = MASKED ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
         switch (a.stage) {
-            case 1: direct_point<DIM, MASK, 1>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
-            case 2: direct_point<DIM, MASK, 2>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
-            case 3: direct_point<DIM, MASK, 3>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
-            default: direct_point<DIM, MASK, 4>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
+            case 1: direct_point<DIM, 1>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
+            case 2: direct_point<DIM, 2>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
+            case 3: direct_point<DIM, 3>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
+            default: direct_point<DIM, 4>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
         }
     }
     if (a.stage == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
 // within a second on any thread sets *err and ends the CTA after giving the
 // copy in flight a second bounded wait; the context's state is then
 // undefined.
-template <bool MASK, int ZT, int STAGE>
+template <int ZT, int STAGE, bool MASKED>
 __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const __grid_constant__ CUtensorMap tin,
                                                             int nslab, int *err) {
     constexpr int NX = 20, NY = 20, GB = 2, BS = 16;
@@ -464,9 +465,9 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
         const RkIn<3> cur = nxt;
         if (k + 1 < ZT) rk_load<3, STAGE>(a, b, ix, iy, iz + 1, off + PLANE, nxt);
         const float2 *u = sm + ((k + 2) * NY + (iy + GB)) * NX + (ix + GB);
-        const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
         df2 r[4], ctr[4];
-        rhs_df<3, MASK>(u, COMP, stv, kc, m, npts_int, r, ctr, ctr[3]);
+        rhs_df<3>(u, COMP, stv, kc, MASKED ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr, npts_int, r, ctr,
+                  ctr[3]);
         rk_df<3, STAGE>(a, kc, b, ix, iy, iz, off, r, ctr, cur, umax);
     }
     if (STAGE == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
@@ -483,7 +484,7 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
 // does not arrive within a second on any thread sets *err and ends the CTA
 // after a bounded wait for the copies in flight; the context's state is then
 // undefined.
-template <bool MASK, int STAGE>
+template <int STAGE, bool MASKED>
 __global__ void __launch_bounds__(256, 3) acm_stage_df_march(StageArgsDF a, const __grid_constant__ CUtensorMap tin,
                                                              int *err) {
     constexpr int NX = 20, NY = 20, GB = 2, BS = 16, NS = 5, NZ = 16;
@@ -527,9 +528,9 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_march(StageArgsDF a, cons
         // the ring's slots are not in z order: the stencil reads each plane
         // through its own slot pointer
         const float2 *ctrp = sm + ((k + 2) % NS) * PLANE + (iy + GB) * NX + (ix + GB);
-        const float2 *m = MASK ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr;
         df2 r[4], ctr[4];
-        rhs_df_ring<MASK>(sm, COMP, k, (iy + GB) * NX + (ix + GB), ctrp, kc, m, npts_int, r, ctr);
+        rhs_df_ring(sm, COMP, k, (iy + GB) * NX + (ix + GB), ctrp, kc,
+                    MASKED ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr, npts_int, r, ctr);
         rk_df<3, STAGE>(a, kc, b, ix, iy, k, off, r, ctr, cur, umax);
         // every thread is done with plane k-2: its slot takes plane k+3; the
         // decision to go on is the CTA's
@@ -593,10 +594,10 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
         const CUtensorMap &map = *reinterpret_cast<const CUtensorMap *>(tmap);
         using K = void (*)(StageArgsDF, const CUtensorMap, int *);
         static const K kerns[2][4] = {
-            {acm_stage_df_march<false, 1>, acm_stage_df_march<false, 2>, acm_stage_df_march<false, 3>,
-             acm_stage_df_march<false, 4>},
-            {acm_stage_df_march<true, 1>, acm_stage_df_march<true, 2>, acm_stage_df_march<true, 3>,
-             acm_stage_df_march<true, 4>}};
+            {acm_stage_df_march<1, false>, acm_stage_df_march<2, false>, acm_stage_df_march<3, false>,
+             acm_stage_df_march<4, false>},
+            {acm_stage_df_march<1, true>, acm_stage_df_march<2, true>, acm_stage_df_march<3, true>,
+             acm_stage_df_march<4, true>}};
         const K kern = kerns[masked ? 1 : 0][stage - 1];
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -610,10 +611,10 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
         const CUtensorMap &map = *reinterpret_cast<const CUtensorMap *>(tmap);
         using K = void (*)(StageArgsDF, const CUtensorMap, int, int *);
         static const K kerns[2][4] = {
-            {acm_stage_df_tile<false, 4, 1>, acm_stage_df_tile<false, 4, 2>, acm_stage_df_tile<false, 4, 3>,
-             acm_stage_df_tile<false, 4, 4>},
-            {acm_stage_df_tile<true, 4, 1>, acm_stage_df_tile<true, 4, 2>, acm_stage_df_tile<true, 4, 3>,
-             acm_stage_df_tile<true, 4, 4>}};
+            {acm_stage_df_tile<4, 1, false>, acm_stage_df_tile<4, 2, false>, acm_stage_df_tile<4, 3, false>,
+             acm_stage_df_tile<4, 4, false>},
+            {acm_stage_df_tile<4, 1, true>, acm_stage_df_tile<4, 2, true>, acm_stage_df_tile<4, 3, true>,
+             acm_stage_df_tile<4, 4, true>}};
         const K kern = kerns[masked ? 1 : 0][stage - 1];
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -626,45 +627,35 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.chunks = (npts_int + threads - 1) / threads;
     const unsigned grid = (unsigned)((long long)nblk * a.chunks);
     const bool b16 = Bs0 == 16 && Bs1 == 16 && (dim == 2 || Bs2 == 16);
-    if (dim == 2) {
-        if (b16) {
-            if (masked) acm_stage_df_kernel<2, true, 16><<<grid, threads, 0, s>>>(a);
-            else acm_stage_df_kernel<2, false, 16><<<grid, threads, 0, s>>>(a);
-        } else {
-            if (masked) acm_stage_df_kernel<2, true, 0><<<grid, threads, 0, s>>>(a);
-            else acm_stage_df_kernel<2, false, 0><<<grid, threads, 0, s>>>(a);
-        }
-    } else {
-        if (b16) {
-            if (masked) acm_stage_df_kernel<3, true, 16><<<grid, threads, 0, s>>>(a);
-            else acm_stage_df_kernel<3, false, 16><<<grid, threads, 0, s>>>(a);
-        } else {
-            if (masked) acm_stage_df_kernel<3, true, 0><<<grid, threads, 0, s>>>(a);
-            else acm_stage_df_kernel<3, false, 0><<<grid, threads, 0, s>>>(a);
-        }
-    }
+    using K = void (*)(StageArgsDF);
+    static const K kerns[2][2][2] = {
+        {{acm_stage_df_kernel<2, 0, false>, acm_stage_df_kernel<2, 0, true>},
+         {acm_stage_df_kernel<2, 16, false>, acm_stage_df_kernel<2, 16, true>}},
+        {{acm_stage_df_kernel<3, 0, false>, acm_stage_df_kernel<3, 0, true>},
+         {acm_stage_df_kernel<3, 16, false>, acm_stage_df_kernel<3, 16, true>}}};
+    kerns[dim == 3 ? 1 : 0][b16 ? 1 : 0][masked ? 1 : 0]<<<grid, threads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
 // anchored double-float copy (df_split, then the tree's quantum) of the
 // interiors of the listed blocks
-__global__ void shadow_kernel(const int *blk, int nblk, const double *src, BufGeo gs, float2 *dst, BufGeo gd, int nc,
-                              int Bx, int By, int Bz, const int *push, const BlockDesc *desc, const TreeClock *clk) {
-    const long long nint = (long long)Bx * By * Bz;
-    const long long total = (long long)nblk * nc * nint;
+__global__ void __launch_bounds__(256) shadow_kernel(const int *__restrict__ blk, const double *src, BufGeo gs,
+                                                     float2 *dst, BufGeo gd, int nc, int Bx, int By, int Bz,
+                                                     const int *push, const BlockDesc *desc, const TreeClock *clk) {
+    // one CTA per (block, component), 32-bit index arithmetic within the block
+    const int b = blk[blockIdx.x], c = blockIdx.y;
+    const int nint = Bx * By * Bz;
     const int zs = gs.nz > 1 ? gs.gb : 0, zd = gd.nz > 1 ? gd.gb : 0;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (long long)gridDim.x * blockDim.x) {
-        const long long r = q % nint;
-        const int c = (int)((q / nint) % nc);
-        const int b = blk[q / (nint * nc)];
-        const int ix = (int)(r % Bx), iy = (int)((r / Bx) % By), iz = (int)(r / ((long long)Bx * By));
-        const double v = src[((long long)b * nc + c) * gs.npts() + ((long long)(iz + zs) * gs.ny + (iy + gs.gb)) * gs.nx +
-                             (ix + gs.gb)];
-        const df2 w = anchor(df_split(v), clk[desc[b].tree].anchor_M);
+    const double *sb = src + ((long long)b * nc + c) * gs.npts();
+    float2 *dc = dst + (long long)c * gd.npts();
+    float2 *db = dc + (long long)b * nc * gd.npts();
+    const float M = clk[desc[b].tree].anchor_M;
+    for (int i = threadIdx.x; i < nint; i += blockDim.x) {
+        const int ix = i % Bx, iy = (i / Bx) % By, iz = i / (Bx * By);
+        const double v = sb[((iz + zs) * gs.ny + (iy + gs.gb)) * gs.nx + (ix + gs.gb)];
+        const df2 w = anchor(df_split(v), M);
         const float2 f = make_float2(w.hi, w.lo);
-        float2 *dc = dst + (long long)c * gd.npts();
-        dc[(long long)b * nc * gd.npts() + ((long long)(iz + zd) * gd.ny + (iy + gd.gb)) * gd.nx + (ix + gd.gb)] = f;
+        db[((iz + zd) * gd.ny + (iy + gd.gb)) * gd.nx + (ix + gd.gb)] = f;
         if (push) {
             if (gd.nz > 1) push_ghosts<3, 1>(push, b, ix, iy, iz, Bx, By, Bz, gd, dc, gd.npts() * nc, &f);
             else push_ghosts<2, 1>(push, b, ix, iy, iz, Bx, By, Bz, gd, dc, gd.npts() * nc, &f);
@@ -758,8 +749,8 @@ cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs
                           int Bs0, int Bs1, int Bs2, const int *push, const BlockDesc *desc, const TreeClock *clk,
                           cudaStream_t s) {
     if (nblk <= 0) return cudaSuccess;
-    shadow_kernel<<<1024, 256, 0, s>>>(blk, nblk, src, gs, reinterpret_cast<float2 *>(dst), gd, nc, Bs0, Bs1, Bs2,
-                                       push, desc, clk);
+    shadow_kernel<<<dim3((unsigned)nblk, (unsigned)nc), 256, 0, s>>>(blk, src, gs, reinterpret_cast<float2 *>(dst), gd,
+                                                                     nc, Bs0, Bs1, Bs2, push, desc, clk);
     return cudaGetLastError();
 }
 

@@ -8,26 +8,9 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "exact.cuh"
+#include "umag.cuh"
 
 namespace wg {
-
-// |x| <= 1e12 on the bits (false for nan), the divergence guard of the ACM
-// integral stage (rhs_ACM.f90:133-146); the bits through the opaque move of
-// exact.cuh, so that the test stays on the integer units
-__device__ __forceinline__ bool within_guard(double x) {
-    const unsigned long long a = (unsigned long long)dbits(x) & 0x7fffffffffffffffull;
-    return a <= 0x426d1a94a2000000ull;   // bits of 1.0e12
-}
-
-// float not above |x|, by truncation on the integer units (0 below 2^-126,
-// inf from 2^128): |x|(1 - 2^-23) < result <= |x| in the normal range
-__device__ __forceinline__ float trunc_abs_f(double x) {
-    const unsigned long long b = (unsigned long long)dbits(x);
-    const int e = (int)((b >> 52) & 0x7ff) - 1023;
-    if (e < -126) return 0.f;
-    if (e > 127) return __uint_as_float(0x7f800000u);
-    return __uint_as_float(((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
-}
 
 template <int DIM>
 __device__ __forceinline__ float usq_approx(const double *ub, long long np, long long o) {
@@ -52,13 +35,25 @@ __device__ __forceinline__ double usq_exact(const double *ub, long long np, long
     return s;
 }
 
-// Per-block max |u|^2 over the interior -> per-block dt -> atomic min per
-// tree. The maximum is found in two passes so that the FP64 units only see
-// a few points: pass 1 takes the FP32 maximum m32 of truncated values
-// (relative error below 2^-20 against the exact sums); the point holding the
-// exact maximum then has its FP32 value above m32 (1 - 2^-17), and pass 2
-// evaluates the exact FP64 sum only for such points. The result is the
-// exact maximum of the reference's expression.
+// GET_DT_BLOCK_ACM of one block from its max |u|^2, then the atomic min
+// over the blocks of its tree (calculate_time_step.f90:28-48)
+template <int DIM>
+__device__ __forceinline__ void dt_of_block(const TreeParams &p, const BlockDesc &d, double u_mag,
+                                            TreeClock &c) {
+    const double u_eigen = __dadd_rn(sqrt(u_mag), sqrt(__dadd_rn(__dmul_rn(p.c0, p.c0), u_mag)));
+    double dxmin = d.dx[0];
+    for (int k = 1; k < DIM; k++) dxmin = fmin(dxmin, d.dx[k]);
+    double dt = u_eigen >= 1.0e-6 ? __ddiv_rn(__dmul_rn(p.CFL, dxmin), u_eigen) : 1.0e-2;
+    if (p.nu > 1.0e-13) dt = fmin(dt, __ddiv_rn(__dmul_rn(p.CFL_nu, __dmul_rn(dxmin, dxmin)), p.nu));
+    if (p.gamma_p > 0) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.gamma_p));
+    if (p.penalization) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.C_eta));
+    if (p.use_sponge) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.C_sponge));
+    atomicMin(&c.dt_min_bits, (unsigned long long)__double_as_longlong(dt));
+}
+
+// Per-block max |u|^2 over the interior (two passes, umag.cuh) -> per-block
+// dt -> atomic min per tree; a value outside the divergence guard sets the
+// tree's flag.
 template <int DIM>
 __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc *desc, const TreeParams *tp,
                                                  TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1,
@@ -94,9 +89,7 @@ __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc
     __syncthreads();
     m32 = red32[0];
     for (int w = 1; w < (int)(blockDim.x >> 5); w++) m32 = fmaxf(m32, red32[w]);
-    // below 2^-100 the squares may be FP32 subnormals without the error
-    // bound: then every point is a candidate
-    const float thr = m32 < 0x1p-100f ? 0.f : m32 * (1.0f - 0x1p-17f);
+    const float thr = umag_threshold(m32);
     double m = -1.0;
     for (int q = threadIdx.x; q < nint; q += blockDim.x) {
         const long long o = offset(q);
@@ -109,16 +102,7 @@ __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc
     if (threadIdx.x == 0) {
         double u_mag = red64[0];
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) u_mag = fmax(u_mag, red64[w]);
-        const TreeParams &p = tp[d.tree];
-        const double u_eigen = __dadd_rn(sqrt(u_mag), sqrt(__dadd_rn(__dmul_rn(p.c0, p.c0), u_mag)));
-        double dxmin = d.dx[0];
-        for (int k = 1; k < DIM; k++) dxmin = fmin(dxmin, d.dx[k]);
-        double dt = u_eigen >= 1.0e-6 ? __ddiv_rn(__dmul_rn(p.CFL, dxmin), u_eigen) : 1.0e-2;
-        if (p.nu > 1.0e-13) dt = fmin(dt, __ddiv_rn(__dmul_rn(p.CFL_nu, __dmul_rn(dxmin, dxmin)), p.nu));
-        if (p.gamma_p > 0) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.gamma_p));
-        if (p.penalization) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.C_eta));
-        if (p.use_sponge) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.C_sponge));
-        atomicMin(&clk[d.tree].dt_min_bits, (unsigned long long)__double_as_longlong(dt));
+        dt_of_block<DIM>(tp[d.tree], d, u_mag, clk[d.tree]);
     }
 }
 

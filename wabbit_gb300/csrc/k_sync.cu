@@ -335,13 +335,16 @@ cudaError_t launch_predict(const Patch *patches, int npatch, int max_smem_double
 }
 
 cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
-                              int order_predictor, const BlockDesc *desc, const TreeClock *clk, cudaStream_t s) {
+                              int order_predictor, const BlockDesc *desc, const TreeClock *clk, cudaStream_t s,
+                              int min_ctas) {
     if (npatch <= 0) return cudaSuccess;
-    // as many components per pass as fit the shared memory of one CTA
+    // as many components per pass as fit the shared memory of one CTA, or of
+    // one of min_ctas CTAs on an SM (at least one component)
     const size_t per = sizeof(float2) * (size_t)max_smem_doubles;
     const size_t limit = 200 * 1024;
     if (per > limit) return cudaErrorInvalidValue;
-    const int cg = (int)std::min<size_t>((size_t)nc, limit / per);
+    const size_t room = std::min<size_t>(limit, (size_t)(224 * 1024) / (size_t)std::max(1, min_ctas));
+    const int cg = (int)std::max<size_t>(1, std::min<size_t>((size_t)nc, room / per));
     const size_t smem = per * cg;
     float2 *b = reinterpret_cast<float2 *>(buf);
     // the attribute belongs to the current device's context; it is raised to

@@ -223,39 +223,66 @@ class Solve:
         self.nblk = self.f.nblocks
 
 
+class _Worker:
+    """One context of a geometry with the solves it is stepping."""
+
+    def __init__(self, dim: int, ctx: Context):
+        self.dim = dim
+        self.ctx = ctx
+        self.capacity = ctx.max_blocks
+        self.pinned = None
+
+    def result_buffer(self, n):
+        """Pinned host buffer of n doubles for a finished solve's state
+        (grown on demand and reused: the download runs at copy-engine speed
+        and touches no fresh pages)."""
+        t = self.pinned
+        if t is None or t.numel() < n:
+            import torch
+            t = torch.empty(max(n, int(1.25 * (t.numel() if t is not None else 0))), dtype=torch.float64,
+                            pin_memory=True)
+            self.pinned = t
+        return t.numpy()[:n]
+
+
 class Server:
+    """workers: contexts (each served by its own host thread) per geometry.
+    With several contexts of one geometry the first is sized for the largest
+    request's peak and the others share the rest of the geometry's budget;
+    each takes the earliest waiting request that fits its free slots (the
+    large context takes small requests only while no large one waits), so
+    the adaptations and admissions of different contexts overlap."""
+
     def __init__(self, budget_gb: float = 64.0, chunk: int = 5, share_3d: float = 0.85, keep_results=False,
-                 adapt_every: int = 0, eps: float = 1e-3):
+                 adapt_every: int = 0, eps: float = 1e-3, workers=None):
         from . import capi
         self.chunk = adapt_every if adapt_every else chunk
         self.adapt = bool(adapt_every)
         self.eps = eps
         self.keep = keep_results
         self.base = {2: geometry(2), 3: geometry(3)}
+        workers = dict(workers or {3: 2, 2: 1})
         L = capi.load()
-        self.ctx = {}
+        self.workers = {}
         for dim, share in ((3, share_3d), (2, 1.0 - share_3d)):
             per = L.wg_bytes_per_block(self.base[dim])
             if self.adapt and self.base[dim].wavelet.decode()[4] != "0":
                 # the lifted adaptation's hvy_tmp arena: one more full block
                 c = self.base[dim]
                 per += 8 * c.neq * int(np.prod([c.Bs[d] + 2 * c.g for d in range(dim)]))
-            cap = max(64, int(budget_gb * 1e9 * share / per))
-            self.ctx[dim] = Context(self.base[dim], cap)
-        self.capacity = {d: self.ctx[d].max_blocks for d in self.ctx}
-        self._pinned = {}
-
-    def _result_buffer(self, dim, n):
-        """Pinned host buffer of n doubles for a finished solve's state
-        (grown on demand and reused: the download runs at copy-engine speed
-        and touches no fresh pages)."""
-        t = self._pinned.get(dim)
-        if t is None or t.numel() < n:
-            import torch
-            t = torch.empty(max(n, int(1.25 * (t.numel() if t is not None else 0))), dtype=torch.float64,
-                            pin_memory=True)
-            self._pinned[dim] = t
-        return t.numpy()[:n]
+            total = budget_gb * 1e9 * share / per
+            n = max(1, int(workers.get(dim, 1)))
+            if n == 1:
+                caps = [total]
+            else:
+                # the largest request peak that the whole budget can hold
+                needs = [self._need(dim, Request(0, 0.0, dim, k, 0, 1e-3)) for k in range(len(LADDER[dim]))]
+                big = max([x for x in needs if 1.02 * x <= total] or [0])
+                first = min(total, max(total / n, 1.02 * big))
+                caps = [first] + [max(0.0, (total - first) / (n - 1))] * (n - 1)
+            self.workers[dim] = [_Worker(dim, Context(self.base[dim], max(64, int(c)))) for c in caps]
+        self.capacity = {d: max(w.capacity for w in ws) for d, ws in self.workers.items()}
+        self.ctx = {d: ws[0].ctx for d, ws in self.workers.items()}
 
     def _peak(self, dim, req):
         """Blocks a request needs at the peak of its first cycle."""
@@ -264,24 +291,55 @@ class Server:
         refined = int(np.sum(np.where(lv < LADDER[dim][req.size][1], nd, 1)))
         return refined + refined // (nd - 1) + 2 * (LADDER[dim][req.size][1] + 1)
 
+    def _need(self, dim, req):
+        return self._peak(dim, req) if self.adapt else len(request_grid(dim, req.size)[0])
+
+    def warm_up(self):
+        """One small solve of 5 steps (one adaptation cycle) on every context:
+        graph capture and the stage-kernel autotuner happen here, not in the
+        first served requests."""
+        for dim, ws in self.workers.items():
+            for w in ws:
+                s = Solve(Request(-1, 0.0, dim, 0, 1, 1e-3, nsteps=self.chunk), w.ctx, self.base[dim])
+                if self.adapt:
+                    s.cycle()
+                w.ctx.run([s.f], self.chunk, use_graph=True)
+                if self.adapt:
+                    s.f.adapt(np.full(s.cfg.neq, self.eps))
+                w.ctx.synchronize()
+                s.f.destroy()
+
     def close(self):
-        for c in self.ctx.values():
-            c.close()
+        for ws in self.workers.values():
+            for w in ws:
+                w.ctx.close()
 
     def run(self, requests, realtime: bool = True):
-        """Serve the stream; returns per-request records and totals. Each
-        geometry is served by its own host thread."""
+        """Serve the stream; returns per-request records and totals. Every
+        context is served by its own host thread."""
         t0 = time.perf_counter()
         out = {}
         errors = []
+        shared = {}
+        for dim in self.workers:
+            shared[dim] = {"pending": sorted([r for r in requests if r.dim == dim], key=lambda r: r.arrival),
+                           "queue": [], "lock": threading.Lock()}
+            for r in shared[dim]["pending"]:
+                if self._need(dim, r) > self.capacity[dim]:
+                    raise ValueError(f"request {r.rid} ({self._need(dim, r)} blocks at its peak) exceeds the "
+                                     f"{dim}-D arena")
 
-        def worker(dim):
+        def worker(dim, k):
             try:
-                out[dim] = self._serve(dim, [r for r in requests if r.dim == dim], t0, realtime)
+                out[(dim, k)] = self._serve(dim, k, shared[dim], t0, realtime)
             except BaseException as e:   # re-raised below
                 errors.append(e)
+                with shared[dim]["lock"]:
+                    shared[dim]["pending"].clear()
+                    shared[dim]["queue"].clear()
 
-        ths = [threading.Thread(target=worker, args=(dim,), name=f"serve-{dim}d") for dim in (3, 2)]
+        ths = [threading.Thread(target=worker, args=(dim, k), name=f"serve-{dim}d-{k}")
+               for dim in (3, 2) for k in range(len(self.workers[dim]))]
         for th in ths:
             th.start()
         for th in ths:
@@ -292,52 +350,64 @@ class Server:
         records = {}
         total_points = 0
         phase = {}
-        for dim in (3, 2):
-            rec, pts, ph = out[dim]
+        for (dim, k), (rec, pts, ph) in sorted(out.items()):
             records.update(rec)
             total_points += pts
-            for k, v in ph.items():
-                phase[f"{k}_{dim}d"] = v
+            for key, v in ph.items():
+                phase[f"{key}_{dim}d"] = phase.get(f"{key}_{dim}d", 0.0) + v
         tts = np.array([r["tts"] for r in records.values()]) if records else np.zeros(1)
         summary = {"requests": len(records), "wall_s": wall, "point_updates": total_points,
                    "throughput": total_points / wall,
                    "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
-                   "phase_s": phase}
+                   "phase_s": phase, "workers": {d: [w.capacity for w in ws] for d, ws in self.workers.items()}}
         return records, summary
 
-    def _serve(self, dim, requests, t0, realtime):
-        """The scheduling loop of one geometry (its own thread and context)."""
-        ctx = self.ctx[dim]
-        pending = sorted(requests, key=lambda r: r.arrival)
-        queue, active = [], []
+    def _take(self, dim, w, sh, used, t0, realtime):
+        """The waiting requests this worker admits now (earliest first)."""
+        with sh["lock"]:
+            now = float("inf") if not realtime else time.perf_counter() - t0
+            while sh["pending"] and sh["pending"][0].arrival <= now:
+                sh["queue"].append(sh["pending"].pop(0))
+            others = [x for x in self.workers[dim] if x is not w]
+            small = max((x.capacity for x in others), default=0)
+            big_waiting = w.capacity > small and any(self._need(dim, r) > small for r in sh["queue"])
+            taken = []
+            for r in list(sh["queue"]):
+                need = self._need(dim, r)
+                if used + need > w.capacity:
+                    continue
+                if big_waiting and need <= small:
+                    continue
+                sh["queue"].remove(r)
+                taken.append(r)
+                used += need
+            idle_until = sh["pending"][0].arrival if sh["pending"] else None
+            done = not sh["pending"] and not sh["queue"]
+        return taken, idle_until, done
+
+    def _serve(self, dim, k, sh, t0, realtime):
+        """The scheduling loop of one context (its own thread)."""
+        w = self.workers[dim][k]
+        ctx = w.ctx
+        active = []
         used = 0
         records = {}
         total_points = 0
         phase = {"admit": 0.0, "refine": 0.0, "run": 0.0, "retire": 0.0}
-        while pending or queue or active:
-            now = time.perf_counter() - t0
-            if not realtime:   # every request has arrived
-                now = float("inf")
-            while pending and pending[0].arrival <= now:
-                queue.append(pending.pop(0))
+        while True:
             ta = time.perf_counter()
-            while queue:
-                r = queue[0]
-                nb = len(request_grid(dim, r.size)[0])
-                need = self._peak(dim, r) if self.adapt else nb
-                if need > self.capacity[dim]:
-                    raise ValueError(f"request {r.rid} ({need} blocks at its peak) exceeds the {dim}-D arena")
-                if used + need > self.capacity[dim]:
-                    break
-                queue.pop(0)
+            taken, idle_until, done = self._take(dim, w, sh, used, t0, realtime)
+            for r in taken:
                 s = Solve(r, ctx, self.base[dim])
                 s.admitted = time.perf_counter() - t0
                 used += s.nblk
                 active.append(s)
             phase["admit"] += time.perf_counter() - ta
             if not active:
-                if pending:
-                    time.sleep(max(0.0, min(0.05, pending[0].arrival - (time.perf_counter() - t0))))
+                if done:
+                    break
+                wait = 0.01 if idle_until is None else idle_until - (time.perf_counter() - t0)
+                time.sleep(max(0.0, min(0.05, wait)))
                 continue
             # one scheduling round: every active solve advances one chunk
             # (with adaptation: the solves whose cycle fits into the arena)
@@ -347,7 +417,7 @@ class Server:
                 group, grow, mothers = [], 0, 0
                 for s in active:
                     refined, m = s.cycle_need()
-                    if used + grow + (refined - s.nblk) + max(mothers, m) <= self.capacity[dim]:
+                    if used + grow + (refined - s.nblk) + max(mothers, m) <= w.capacity:
                         grow += refined - s.nblk
                         mothers = max(mothers, m)
                         s.cycle()
@@ -355,13 +425,13 @@ class Server:
                 used += grow
                 if not group:
                     raise RuntimeError(f"no {dim}-D solve fits its adaptation cycle into the arena")
-            k = min(self.chunk, min(s.req.nsteps - s.done for s in group))
+            kk = min(self.chunk, min(s.req.nsteps - s.done for s in group))
             t1 = time.perf_counter()
             phase["refine"] += t1 - tr
-            ctx.run([s.f for s in group], k, use_graph=True)
+            ctx.run([s.f for s in group], kk, use_graph=True)
             for s in group:
-                s.done += k
-                total_points += s.points * k
+                s.done += kk
+                total_points += s.points * kk
             if self.adapt:
                 # each adaptation waits for the batched steps on the stream
                 for s in group:
@@ -379,11 +449,11 @@ class Server:
                     keep.append(s)
                     continue
                 shape = (s.nblk,) + s.f.interior_shape
-                flat = self._result_buffer(dim, int(np.prod(shape)))
+                flat = w.result_buffer(int(np.prod(shape)))
                 u = s.f.download_interior(out=flat.reshape(shape))
                 t_done = time.perf_counter() - t0
                 rec = {"rid": s.req.rid, "dim": dim, "blocks": s.nblk, "arrival": s.req.arrival,
-                       "admitted": s.admitted, "done": t_done,
+                       "admitted": s.admitted, "done": t_done, "worker": k,
                        "tts": t_done - (s.req.arrival if realtime else 0.0),
                        "time": s.f.time()[0], "checksum": float(np.dot(flat, flat))}
                 if self.keep:

@@ -158,12 +158,13 @@ def initial_condition(name: str, cfg, lv, co):
     return u
 
 
-def adapt_field_device(cfg, lv, co, seed: int = 5, nmodes: int = 16, nfronts: int = 32, chunk: int = 4096):
-    """Interior field of the adapt workload on the GPU (torch float64),
-    shape (nblk, 4, Bz, By, Bx)."""
+def adapt_field_device(cfg, lv, co, seed: int = 5, nmodes: int = 16, nfronts: int = 32, chunk: int = 4096,
+                       device: str = "cuda"):
+    """Interior field of the adapt workload on the GPU (or `device`; torch
+    float64), shape (nblk, 4, Bz, By, Bx)."""
     import torch
     rng = np.random.default_rng(seed)
-    dev = torch.device("cuda")
+    dev = torch.device(device)
     nc = cfg.neq
     params = []
     for _ in range(nc):
