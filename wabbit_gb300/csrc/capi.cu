@@ -237,6 +237,10 @@ struct wg_ctx {
     // groups of an RK4 step while prof_on is set
     cudaEvent_t prof_ev[10] = {};
     bool prof_on = false;
+    // wg_rk4_stream: stage 4 of the tree's step also writes u_n+1 into this
+    // compact array (positions by block slot in d_pos), instead of a gather
+    double *s4_out = nullptr;
+    DevArray<int> d_pos;
     // set when a bounded device wait gave up (WG_ETIMEOUT): a bulk copy may
     // still have been landing in shared memory, so nothing the context holds
     // is trusted any more and every call but wg_ctx_destroy fails
@@ -686,7 +690,7 @@ static int stage_pair(wg_ctx *ctx, int stage, const int *plain, int nplain, cons
     auto go = [&](int msk, const int *blk, int n) {
         return launch_acm_stage_df(dim, stage, msk, blk, n, ctx->d_desc, ctx->d_tp, ctx->d_clk, in, ctx->B, ctx->C,
                                    ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0], Bs[1], Bs[2], tm,
-                                   march, ctx->d_err, ctx->stream, keep);
+                                   march, ctx->d_err, ctx->stream, keep, ctx->s4_out, ctx->d_pos.p);
     };
     WG_CUDA_OK(go(0, plain, nplain));
     WG_CUDA_OK(go(1, masked, nmasked));
@@ -2903,7 +2907,8 @@ static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) 
             WG_CUDA_OK(cudaEventRecord(done, ctx->copy_stream));
             WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, done, 0));
             WG_CUDA_OK(launch_interior_xfer(t->d_all.p + b0, nb, dev, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz,
-                                            1, ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream));
+                                            1, ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream,
+                                            shadow ? ctx->B : nullptr, ctx->gT, push ? ctx->d_push : nullptr));
         } else {
             WG_CUDA_OK(launch_interior_xfer(t->d_all.p + b0, nb, dev, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz,
                                             0, ctx->d_desc, nullptr, ctx->stream));
@@ -2913,10 +2918,11 @@ static int interior_transfer(wg_ctx *ctx, Tree *t, double *host, int to_device) 
         }
     }
     if (shadow) {
-        WG_CUDA_OK(launch_anchor_from_state(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz,
-                                            ctx->d_desc, ctx->d_clk, ctx->d_tree_ids.p + tid, 1, 0, ctx->stream));
+        // the scatter wrote the anchored copy with the tree's current
+        // constant; redone only if the new state's constant differs
+        WG_CUDA_OK(launch_anchor_check(ctx->d_clk, ctx->d_tree_ids.p + tid, 1, ctx->stream));
         WG_CUDA_OK(launch_shadow(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz,
-                                 push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream));
+                                 push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream, 1));
     }
     WG_CUDA_OK(cudaStreamSynchronize(ctx->copy_stream));
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
@@ -2986,6 +2992,12 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     if ((st = autotune_stage_form(ctx, *t))) return st;
     const size_t pb = per * nblk;
     double *I[2] = {ctx->stream_buf, ctx->stream_buf + pb}, *O[2] = {ctx->stream_buf + 2 * pb, ctx->stream_buf + 3 * pb};
+    // FP32-pipe: the last stage writes the result into O directly
+    if (shadow) {
+        std::vector<int> pos(ctx->max_blocks, 0);
+        for (int i = 0; i < nblk; i++) pos[t->slots[i]] = i;
+        WG_CUDA_OK(ctx->d_pos.upload(pos.data(), pos.size(), ctx->stream));
+    }
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     WG_CUDA_OK(cudaMemcpyAsync(I[0], ins[0], bytes, cudaMemcpyDefault, ctx->copy_stream));
     WG_CUDA_OK(cudaEventRecord(h2d_done[0], ctx->copy_stream));
@@ -2999,19 +3011,24 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
         WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, h2d_done[cur], 0));
         if (shadow) WG_CUDA_OK(launch_umax_reset(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
         WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, I[cur], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 1,
-                                        ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream));
+                                        ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream,
+                                        shadow ? ctx->B : nullptr, ctx->gT, push ? ctx->d_push : nullptr));
         WG_CUDA_OK(cudaEventRecord(scattered[cur], ctx->stream));
         if (shadow) {
-            WG_CUDA_OK(launch_anchor_from_state(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz,
-                                                ctx->d_desc, ctx->d_clk, ctx->d_tree_ids.p + tree, 1, 0, ctx->stream));
+            WG_CUDA_OK(launch_anchor_check(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
             WG_CUDA_OK(launch_shadow(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz,
-                                     push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream));
+                                     push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream, 1));
         }
         t->shadow_valid = shadow;
-        if ((st = rk4_enqueue(ctx, tree))) return st;
+        // the result buffer O[cur] is free once the result of step k-2 is out
         if (k >= 2) WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, d2h_done[cur], 0));
-        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[cur], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,
-                                        ctx->d_desc, nullptr, ctx->stream));
+        if (shadow) ctx->s4_out = O[cur];
+        st = rk4_enqueue(ctx, tree);
+        ctx->s4_out = nullptr;
+        if (st) return st;
+        if (!shadow)
+            WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[cur], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,
+                                            ctx->d_desc, nullptr, ctx->stream));
         WG_CUDA_OK(cudaEventRecord(gathered[cur], ctx->stream));
         WG_CUDA_OK(cudaStreamWaitEvent(ctx->d2h_stream, gathered[cur], 0));
         WG_CUDA_OK(cudaMemcpyAsync(outs[k], O[cur], bytes, cudaMemcpyDefault, ctx->d2h_stream));

@@ -29,7 +29,7 @@ struct TreeClock {
     double dt;
     unsigned long long dt_min_bits;  // running min over blocks (positive double bits)
     int    diverged;
-    int    pad;
+    int    reshadow;   // the anchored copy an upload wrote with a guessed constant must be redone
     // dt, dt/3 and dt/6 as double-float pairs (written with dt)
     float  f_dt[2], f_dt3[2], f_dt6[2];
     // FP32-pipe stage inputs are anchored: the hi float of every value is a
@@ -134,7 +134,8 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const TreeParams *tp, TreeClock *clk, const void *in, const void *u0, const void *s2,
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
-                                cudaStream_t s, int keep_state = 1);
+                                cudaStream_t s, int keep_state = 1, double *cout = nullptr,
+                                const int *cpos = nullptr);
 // (march: tmap is a map with one-plane boxes and the whole-block ring kernel
 // runs; keep_state 0 times stage 4 without storing u_n+1)
 // slab height of the TMA tile form of the double-float stage kernel (3-D,
@@ -143,9 +144,14 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
 int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g);
 // double-float copy of the interiors of the listed blocks of an FP64 buffer
 // (push: same-level ghost copies as in the stage kernel, or null)
+// (only_if_flagged: only blocks of trees whose TreeClock::reshadow is set)
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
                           int Bs0, int Bs1, int Bs2, const int *push, const BlockDesc *desc, const TreeClock *clk,
-                          cudaStream_t s);
+                          cudaStream_t s, int only_if_flagged = 0);
+// after an upload that wrote the anchored copy with the trees' current
+// constant: the constant from the merged running max, and reshadow set
+// where it differs from the one used
+cudaError_t launch_anchor_check(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
 // anchoring constant of the FP32-pipe stage inputs (TreeClock::anchor_M):
 // reset of the running max, and the constant from the state (scan) or from
 // the running max an interior upload merged
@@ -180,10 +186,13 @@ cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, c
 cudaError_t launch_norm_linf(const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int nc,
                              double *out, cudaStream_t s);
 // interior exchange state <-> compact array, one CTA row per (block,
-// component); towards the state optionally also the double-float copy B
-// (thin layout gt) with its same-level ghost pushes
+// component); towards the state it merges max |u| into clk (when given) and
+// optionally also writes the anchored double-float copy shadow (thin layout
+// gs, same-level ghost pushes), anchored with the trees' current constant
+// (launch_anchor_check decides whether that was the right one)
 cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, int nc, int Bx,
-                                 int By, int Bz, int to_state, const BlockDesc *desc, TreeClock *clk, cudaStream_t s);
+                                 int By, int Bz, int to_state, const BlockDesc *desc, TreeClock *clk, cudaStream_t s,
+                                 void *shadow = nullptr, BufGeo gs = BufGeo{0, 0, 0, 0}, const int *push = nullptr);
 cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
                                  int Bx, int By, int Bz, int to_full, cudaStream_t s);
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,

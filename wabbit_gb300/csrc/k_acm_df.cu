@@ -45,6 +45,8 @@ struct StageArgsDF {
     BufGeo gt;
     double *un;            // u_n, FP64 (full layout)
     double *un_out;        // where stage 4 stores u_n+1 (un, or null when timing the stage)
+    double *cout;          // stage 4: u_n+1 also into a compact interior array (nblk, nc, Bz, By, Bx), or null
+    const int *cpos;       // block slot -> its position in cout
     BufGeo gun;
     const float2 *mask;    // 5 words per point, interior only
     const int *push;       // same-level ghost copies pushed by the writer, or null
@@ -341,6 +343,9 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
             const df2 inc = df_norm(df_add_nr(df_mul_nr(third, sum), df_mul_nr(k.db, df_norm(r[c]))));
             const double v = __dadd_rn(u, df_to_double(inc));
             if (a.un_out) un[c * us] = v;
+            if (a.cout)
+                a.cout[((long long)a.cpos[b] * (DIM + 1) + c) * a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1) +
+                       ((DIM == 3 ? iz * a.Bs1 : 0) + iy) * a.Bs0 + ix] = v;
             const df2 w = anchor(df_add_nr(ud, inc), k.M);
             ov[c] = make_float2(w.hi, w.lo);
             o[c * cs] = ov[c];
@@ -560,7 +565,7 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const TreeParams *tp, TreeClock *clk, const void *in, const void *u0, const void *s2,
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
-                                cudaStream_t s, int keep_state) {
+                                cudaStream_t s, int keep_state, double *cout, const int *cpos) {
     if (nblk <= 0) return cudaSuccess;
     if (stage < 1 || stage > 4) return cudaErrorInvalidValue;
     StageArgsDF a;
@@ -576,6 +581,8 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.gt = gt;
     a.un = un;
     a.un_out = keep_state ? un : nullptr;
+    a.cout = keep_state && stage == 4 ? cout : nullptr;
+    a.cpos = cpos;
     a.gun = gun;
     a.mask = reinterpret_cast<const float2 *>(maskdf);
     a.push = push;
@@ -641,9 +648,11 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
 // interiors of the listed blocks
 __global__ void __launch_bounds__(256) shadow_kernel(const int *__restrict__ blk, const double *src, BufGeo gs,
                                                      float2 *dst, BufGeo gd, int nc, int Bx, int By, int Bz,
-                                                     const int *push, const BlockDesc *desc, const TreeClock *clk) {
+                                                     const int *push, const BlockDesc *desc, const TreeClock *clk,
+                                                     int only_if_flagged) {
     // one CTA per (block, component), 32-bit index arithmetic within the block
     const int b = blk[blockIdx.x], c = blockIdx.y;
+    if (only_if_flagged && !clk[desc[b].tree].reshadow) return;
     const int nint = Bx * By * Bz;
     const int zs = gs.nz > 1 ? gs.gb : 0, zd = gd.nz > 1 ? gd.gb : 0;
     const double *sb = src + ((long long)b * nc + c) * gs.npts();
@@ -669,12 +678,16 @@ __global__ void __launch_bounds__(256) shadow_kernel(const int *__restrict__ blk
 // which the anchored copy of the FP32-pipe precision takes its quantum.
 __global__ void __launch_bounds__(256) interior_xfer_kernel(const int *__restrict__ slots, double *compact, double *A,
                                                             BufGeo ga, int nc, int Bx, int By, int Bz, int to_state,
-                                                            const BlockDesc *desc, TreeClock *clk) {
+                                                            const BlockDesc *desc, TreeClock *clk, float2 *shadow,
+                                                            BufGeo gs, const int *push) {
     const int b = slots[blockIdx.x], c = blockIdx.y;
     const int nint = Bx * By * Bz;
     double *cp = compact + ((long long)blockIdx.x * nc + c) * nint;
     double *ab = A + ((long long)b * nc + c) * ga.npts();
-    const int za = ga.nz > 1 ? ga.gb : 0;
+    const int za = ga.nz > 1 ? ga.gb : 0, zs = gs.nz > 1 ? gs.gb : 0;
+    float2 *dc = shadow ? shadow + (long long)c * gs.npts() : nullptr;
+    float2 *db = shadow ? dc + (long long)b * nc * gs.npts() : nullptr;
+    const float M = shadow ? clk[desc[b].tree].anchor_M : 0.f;
     float umax = 0.f;
     for (int i = threadIdx.x; i < nint; i += blockDim.x) {
         const int ix = i % Bx, iy = (i / Bx) % By, iz = i / (Bx * By);
@@ -685,9 +698,28 @@ __global__ void __launch_bounds__(256) interior_xfer_kernel(const int *__restric
         }
         const double v = cp[i];
         *pa = v;
-        umax = fmaxf(umax, fabsf(df_split(v).hi));
+        const df2 sv = df_split(v);
+        umax = fmaxf(umax, fabsf(sv.hi));
+        if (shadow) {
+            const df2 w = anchor(sv, M);
+            const float2 f = make_float2(w.hi, w.lo);
+            db[((iz + zs) * gs.ny + (iy + gs.gb)) * gs.nx + (ix + gs.gb)] = f;
+            if (push) {
+                if (gs.nz > 1) push_ghosts<3, 1>(push, b, ix, iy, iz, Bx, By, Bz, gs, dc, gs.npts() * nc, &f);
+                else push_ghosts<2, 1>(push, b, ix, iy, iz, Bx, By, Bz, gs, dc, gs.npts() * nc, &f);
+            }
+        }
     }
     if (to_state && clk) merge_umax(umax, clk, desc[b].tree);
+}
+
+__global__ void anchor_check_kernel(TreeClock *clk, const int *trees, int ntrees) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntrees) return;
+    TreeClock &c = clk[trees[i]];
+    const float M = anchor_constant(c.umax_f);
+    c.reshadow = M != c.anchor_M;
+    c.anchor_M = M;
 }
 
 // max |u| over the interiors of the listed blocks (all components) merged
@@ -739,18 +771,27 @@ cudaError_t launch_anchor_from_state(const int *slots, int nblk, const double *A
 }
 
 cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, int nc, int Bx,
-                                 int By, int Bz, int to_state, const BlockDesc *desc, TreeClock *clk, cudaStream_t s) {
+                                 int By, int Bz, int to_state, const BlockDesc *desc, TreeClock *clk, cudaStream_t s,
+                                 void *shadow, BufGeo gs, const int *push) {
     if (nblk <= 0) return cudaSuccess;
-    interior_xfer_kernel<<<dim3(nblk, nc), 256, 0, s>>>(slots, compact, A, ga, nc, Bx, By, Bz, to_state, desc, clk);
+    if (shadow && (!to_state || !clk)) return cudaErrorInvalidValue;
+    interior_xfer_kernel<<<dim3(nblk, nc), 256, 0, s>>>(slots, compact, A, ga, nc, Bx, By, Bz, to_state, desc, clk,
+                                                         reinterpret_cast<float2 *>(shadow), gs, push);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_anchor_check(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s) {
+    anchor_check_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
     return cudaGetLastError();
 }
 
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
                           int Bs0, int Bs1, int Bs2, const int *push, const BlockDesc *desc, const TreeClock *clk,
-                          cudaStream_t s) {
+                          cudaStream_t s, int only_if_flagged) {
     if (nblk <= 0) return cudaSuccess;
     shadow_kernel<<<dim3((unsigned)nblk, (unsigned)nc), 256, 0, s>>>(blk, src, gs, reinterpret_cast<float2 *>(dst), gd,
-                                                                     nc, Bs0, Bs1, Bs2, push, desc, clk);
+                                                                     nc, Bs0, Bs1, Bs2, push, desc, clk,
+                                                                     only_if_flagged);
     return cudaGetLastError();
 }
 
