@@ -78,7 +78,7 @@ def parse():
     ap.add_argument("--adapt-every", type=int, default=5,
                     help="serving: adaptation cycle length in steps (0: no adaptation)")
     ap.add_argument("--stage-form", default="auto",
-                    help="FP32-pipe stage kernel form: auto (timed per RK stage), direct, tile, march, or four "
+                    help="FP32-pipe stage kernel form: auto (timed per RK stage), direct, tile, march, pipe, or four "
                          "comma-separated forms for RK stages 1-4")
     ap.add_argument("--traffic", choices=["auto", "off"], default="auto",
                     help="measure the stage kernels' DRAM bytes with a one-pass ncu capture (dram__bytes_read/"
@@ -201,7 +201,8 @@ TRAFFIC_JMAX = 5
 def run_traffic_case(args):
     """The small case the traffic capture profiles: the workload at Jmax=5,
     the given stage forms, one RK4 step of batched launches without a graph
-    (two launches per RK stage: unmasked and masked blocks). Prints the
+    (two launches per RK stage, unmasked and masked blocks; one in the pipe
+    form). Prints the
     grid's sizes as JSON."""
     import torch
     from wabbit_gb300 import build, workloads
@@ -243,8 +244,10 @@ def measure_traffic(args, forms):
     if not os.path.exists(ncu):
         return None, "ncu not found"
     log = tempfile.NamedTemporaryFile(prefix="traffic", suffix=".csv", delete=False).name
+    # launches per RK stage: unmasked and masked blocks, or one (pipe form)
+    per = [1 if fm == "pipe" else 2 for fm in forms]
     ncmd = [ncu, "--metrics", "dram__bytes_read.sum,dram__bytes_write.sum", "--clock-control", "none",
-            "-k", "regex:acm_stage_df", "-c", "8", "--csv", "--print-units", "base", "--log-file", log] + cmd
+            "-k", "regex:acm_stage_df", "-c", str(sum(per)), "--csv", "--print-units", "base", "--log-file", log] + cmd
     try:
         r = subprocess.run(ncmd, capture_output=True, text=True, timeout=900)
     except subprocess.TimeoutExpired:
@@ -268,12 +271,16 @@ def measure_traffic(args, forms):
             launches[int(d["ID"])] += float(d["Metric Value"].replace(",", ""))
     os.unlink(log)
     ids = sorted(launches)
-    if len(ids) != 8:
-        return None, f"expected 8 stage launches in the capture, got {len(ids)}"
-    per_stage = [(launches[ids[2 * j]] + launches[ids[2 * j + 1]]) / info["points"] for j in range(4)]
-    desc = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the 8 stage launches (unmasked + masked blocks, "
-            f"RK stages 1-4) of one step of {args.workload} at Jmax={TRAFFIC_JMAX} ({info['blocks']} blocks, "
-            f"{info['masked_blocks']} masked), per interior point, scaled to the full grid by its points")
+    if len(ids) != sum(per):
+        return None, f"expected {sum(per)} stage launches in the capture, got {len(ids)}"
+    per_stage, at = [], 0
+    for j in range(4):
+        per_stage.append(sum(launches[ids[at + k]] for k in range(per[j])) / info["points"])
+        at += per[j]
+    desc = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of the {sum(per)} stage launches (RK stages 1-4; "
+            f"unmasked and masked blocks apart except in the pipe form) of one step of {args.workload} at "
+            f"Jmax={TRAFFIC_JMAX} ({info['blocks']} blocks, {info['masked_blocks']} masked), per interior point, "
+            f"scaled to the full grid by its points")
     return per_stage, desc
 
 
@@ -443,7 +450,8 @@ def run_ours(args, rank, world):
     ach_tf = flops_stage / (mean_stage_ms * 1e-3) / 1e12
     form = ctx.stage_forms() if cfg.rhs_precision else ["direct"] * 4
     kname = {"direct": "acm_stage_df_kernel", "tile": "acm_stage_df_tile (TMA slabs)",
-             "march": "acm_stage_df_march (TMA plane ring)"}
+             "march": "acm_stage_df_march (TMA plane ring)",
+             "pipe": "acm_stage_df_pipe (persistent TMA slab pipeline)"}
     stage_kernel = ("acm_stage_kernel (FP64)" if cfg.rhs_precision == 0 else
                     ", ".join(kname[x] for x in dict.fromkeys(form)))
     traffic, traffic_src = None, "not measured (--traffic off)"

@@ -94,3 +94,33 @@ def test_tree_listed_twice_rejected():
         f = _load(ctx, cfg, lv, co, data, mask)
         with pytest.raises(capi.WgError):
             ctx.run([f, f], 1)
+
+
+def test_batched_stage_forms_bit_identical_on_many_slabs():
+    """Three 3-D solves of a few hundred 16^3 blocks each, stepped together:
+    the persistent slab form (each CTA walks many slabs, crossing the trees'
+    boundaries, where stage 4 hands its running maximum to the right tree)
+    gives the same bits and times as the tile and direct forms."""
+    solves = []
+    for k, (seed, nu, masked) in enumerate([(13, 1e-2, True), (17, 5e-3, False), (19, 2e-2, True)]):
+        cfg = small_cfg(3, "CDF44", Bs=16, penal=1 if masked else 0, jmin=2, jmax=3)
+        cfg.C_eta = 1e-2
+        cfg.nu = nu
+        cfg.rhs_precision = 1
+        lv, co = grids.random_graded(3, cfg.Jmin, cfg.Jmax, seed=seed, frac=0.3)
+        data = smooth_state(cfg, lv, co, 60 + k)
+        mask = sphere_mask(cfg, lv, co, [0.5, 0.6, 0.7], 0.25) if masked else None
+        solves.append((cfg, lv, co, data, mask))
+    cap = sum(len(s[1]) for s in solves) + 8
+    assert 4 * (cap - 8) > 4 * 152      # several slabs per SM
+    out = []
+    for forms in (["tile"] * 4, ["pipe"] * 4, ["direct", "pipe", "tile", "pipe"]):
+        with Context(solves[0][0], cap) as ctx:
+            ctx.set_stage_forms(forms)
+            fs = [_load(ctx, *s) for s in solves]
+            ctx.run(fs, 3, use_graph=True)
+            out.append([(f.download(), f.time()) for f in fs])
+    for res in out[1:]:
+        for (u, t), (u0, t0) in zip(res, out[0]):
+            assert t == t0
+            assert np.array_equal(u, u0)

@@ -265,10 +265,10 @@ def test_rk4_fp32_pipe_path_within_tolerance(dim, wavelet, penal, grids2d, grids
 
 
 def test_fp32_pipe_stage_forms_bit_identical():
-    """The direct, tile and march forms of the FP32-pipe stage kernel do the
-    same arithmetic in the same order: three steps with any per-stage mix of
-    forms give the same bits, so the autotuner's choices never change a
-    result."""
+    """The direct, tile, march and pipe forms of the FP32-pipe stage kernel
+    do the same arithmetic in the same order: three steps with any per-stage
+    mix of forms give the same bits, so the autotuner's choices never change
+    a result."""
     cfg = small_cfg(3, "CDF40", Bs=16, penal=1, jmin=1, jmax=2)
     cfg.C_eta = 1e-2
     cfg.rhs_precision = 1
@@ -276,7 +276,8 @@ def test_fp32_pipe_stage_forms_bit_identical():
     data = smooth_state(cfg, lv, co, 31)
     mask = sphere_mask(cfg, lv, co, [0.5, 0.6, 0.7], 0.3)
     out = []
-    for forms in (["direct"] * 4, ["tile"] * 4, ["march"] * 4, ["march", "tile", "direct", "march"]):
+    for forms in (["direct"] * 4, ["tile"] * 4, ["march"] * 4, ["pipe"] * 4, ["march", "tile", "direct", "march"],
+                  ["pipe", "direct", "tile", "pipe"]):
         with Context(cfg, len(lv) + 4) as ctx:
             ctx.set_stage_forms(forms)
             f = ctx.forest()
@@ -300,10 +301,10 @@ def test_fp32_pipe_rejects_skew_symmetric():
         Context(cfg, 8)
 
 
-@pytest.mark.parametrize("form", ["direct", "tile", "march", "auto"])
+@pytest.mark.parametrize("form", ["direct", "tile", "march", "pipe", "auto"])
 def test_fp32_pipe_stage_forms_16cubed(form):
     """3-D 16^3 blocks (the benchmark geometry): the direct-load stage
-    kernel, the TMA-staged slab and plane-ring kernels, and the autotuner's
+    kernel, the TMA-staged slab, plane-ring and persistent slab kernels, and the autotuner's
     per-stage picks, all stay within 1e-12 of the FP64 oracle over three
     steps on a graded two-level grid with a masked sphere."""
     cfg = small_cfg(3, "CDF40", Bs=16, penal=1, jmin=1, jmax=2)
@@ -333,5 +334,5 @@ def test_fp32_pipe_stage_forms_16cubed(form):
             assert err < 1e-12, (form, step, err)
         forms = ctx.stage_forms()
         assert len(forms) == 4
-        assert all(x in (("direct", "tile", "march") if form == "auto" else (form,)) for x in forms)
+        assert all(x in (("direct", "tile", "march", "pipe") if form == "auto" else (form,)) for x in forms)
         assert ctx.stage_form() == forms[1]

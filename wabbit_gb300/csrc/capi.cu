@@ -245,7 +245,9 @@ struct wg_ctx {
     // still have been landing in shared memory, so nothing the context holds
     // is trusted any more and every call but wg_ctx_destroy fails
     bool dead = false;
-    int *d_err = nullptr;               // device error flag (a kernel's wait ran out)
+    int *d_err = nullptr;               // device error flag (a kernel's wait ran out), then the three
+                                        // work counters of the fused ghost sync and the finished-CTA
+                                        // counter of the dt reduction (all zero between launches)
     int mask_cap = 0;
     std::vector<int> mask_free;
     BlockDesc *d_desc = nullptr;
@@ -280,6 +282,16 @@ struct wg_ctx {
 };
 
 namespace {
+
+// a tree's clock at time t: no dt yet, the running dt minimum at its start
+// value, no anchoring constant
+TreeClock fresh_clock(double t) {
+    TreeClock c;
+    std::memset(&c, 0, sizeof(c));
+    c.time = t;
+    c.dt_min_bits = kDtStartBits;
+    return c;
+}
 
 int check_cfg(const wg_config *c) {
     if (!c) return fail(WG_EINVAL, "null config");
@@ -541,6 +553,31 @@ int get_sync(wg_ctx *ctx, Tree &t, int gm, int gp, bool thin, SyncPlan **out) {
     return WG_OK;
 }
 
+// The shape the fused sync launch covers: gather stages of which at most one
+// has entries left once the pushed copies are skipped (*gst, or -1), then a
+// single prediction stage, the last (*pst). False: run the stages one by one.
+static bool fused_shape(const std::vector<int> &stage_predict, const std::vector<unsigned> &pair_begin,
+                        const std::vector<unsigned> &copy_end, bool skip_copies, int *gst, int *pst) {
+    const int ns = (int)stage_predict.size();
+    if (ns == 0 || (int)pair_begin.size() != ns + 1 || !stage_predict[ns - 1]) return false;
+    *gst = -1;
+    *pst = ns - 1;
+    for (int s = 0; s + 1 < ns; s++) {
+        if (stage_predict[s]) return false;
+        const unsigned from = skip_copies ? copy_end[s] : pair_begin[s];
+        if (pair_begin[s + 1] == from) continue;
+        if (*gst >= 0) return false;
+        *gst = s;
+    }
+    return true;
+}
+
+// counters of the fused sync (after the error flag)
+static unsigned *fused_ctr(wg_ctx *ctx) { return reinterpret_cast<unsigned *>(ctx->d_err + 1); }
+
+// finished-CTA counter of the one-launch dt reduction
+static unsigned *dt_done(wg_ctx *ctx) { return reinterpret_cast<unsigned *>(ctx->d_err + 4); }
+
 // skip_copies: the same-level copies were written by the kernel that wrote
 // buf's interiors (push); only restrictions and predictions remain
 int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool df = false, bool skip_copies = false) {
@@ -548,6 +585,18 @@ int run_sync(wg_ctx *ctx, Tree &t, double *buf, bool thin, int gm, int gp, bool 
     int st = get_sync(ctx, t, gm, gp, thin, &sp);
     if (st) return st;
     const BufGeo geo = thin ? ctx->gT : ctx->gA;
+    int gst, pst;
+    if (df && !sp->pair_begin.empty() && !sp->pcls.begin.empty() &&
+        fused_shape(sp->table.stage_predict, sp->pair_begin, sp->copy_end, skip_copies && sp->push_ok, &gst, &pst) &&
+        sp->pcls.begin[pst].size() == 2) {
+        const unsigned from = gst < 0 ? 0 : (skip_copies && sp->push_ok ? sp->copy_end[gst] : sp->pair_begin[gst]);
+        const unsigned n = gst < 0 ? 0 : sp->pair_begin[gst + 1] - from;
+        const std::vector<int> &pb = sp->pcls.begin[pst];
+        WG_CUDA_OK(launch_sync_df_fused(sp->pairs.p + from, n, sp->pcls.patches.p + pb[0], pb[1] - pb[0],
+                                        sp->pcls.need[pst][0], buf, geo, ctx->geo.nc, ctx->wav.order_predictor,
+                                        ctx->d_desc, ctx->d_clk, fused_ctr(ctx), ctx->d_err, ctx->stream, 4));
+        return WG_OK;
+    }
     for (int s = 0; s < sp->table.nstages; s++) {
         const int b = sp->table.stage_begin[s], e = sp->table.stage_begin[s + 1];
         // copies and decimations move 8-byte elements: the same kernel serves
@@ -674,14 +723,20 @@ static void form_args(wg_ctx *ctx, int stage, const double *in, const void **tm,
         *tm = in_map(ctx, in, true);
         *march = 1;
     }
+    if (form == WG_FORM_PIPE && ctx->have_tm) {
+        *tm = in_map(ctx, in, false);
+        *march = 2;
+    }
 }
 
 // the two launches of an FP32-pipe stage, one after the other: the unmasked
 // blocks' kernel and the masked blocks' kernel (the mask words compiled out
 // of the first; one kernel testing the mask per block was 3 % slower, and
 // the two kernels side by side on two streams 25 % slower in the last stage)
+// (the pipe form: one launch over `both`, the masked blocks followed by the
+// others)
 static int stage_pair(wg_ctx *ctx, int stage, const int *plain, int nplain, const int *masked, int nmasked,
-                      const double *in, double *out, const int *pp, int keep) {
+                      const int *both, const double *in, double *out, const int *pp, int keep) {
     const int dim = ctx->cfg.dim;
     const int *Bs = ctx->cfg.Bs;
     const void *tm = nullptr;
@@ -692,6 +747,10 @@ static int stage_pair(wg_ctx *ctx, int stage, const int *plain, int nplain, cons
                                    ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0], Bs[1], Bs[2], tm,
                                    march, ctx->d_err, ctx->stream, keep, ctx->s4_out, ctx->d_pos.p);
     };
+    if (march == 2) {
+        WG_CUDA_OK(go(nmasked, both, nplain + nmasked));
+        return WG_OK;
+    }
     WG_CUDA_OK(go(0, plain, nplain));
     WG_CUDA_OK(go(1, masked, nmasked));
     return WG_OK;
@@ -701,7 +760,7 @@ static int stage_pair(wg_ctx *ctx, int stage, const int *plain, int nplain, cons
 // are C and D; with push the kernels also write the same-level ghost copies
 // of out
 int stage_launch_df(wg_ctx *ctx, Tree &t, int stage, const double *in, double *out, bool push, int keep = 1) {
-    return stage_pair(ctx, stage, t.d_plain.p, t.n_plain, t.d_masked.p, t.n_masked, in, out,
+    return stage_pair(ctx, stage, t.d_plain.p, t.n_plain, t.d_masked.p, t.n_masked, t.d_stage.p, in, out,
                       push ? ctx->d_push : nullptr, keep);
 }
 
@@ -752,8 +811,8 @@ int check_dev_err(wg_ctx *ctx) {
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     if (!h) return WG_OK;
     ctx->dead = true;
-    return fail(WG_ETIMEOUT, "a stage kernel's shared-memory load did not complete within its time limit; "
-                             "the context is unusable, destroy it");
+    return fail(WG_ETIMEOUT, "a bounded device wait (a stage kernel's shared-memory load or the ghost sync's "
+                             "wait for its restrictions) ran out; the context is unusable, destroy it");
 }
 
 // the thin per-step plan of a tree, and whether its copies are pushed
@@ -798,6 +857,7 @@ int autotune_stage_form(wg_ctx *ctx, Tree &t) {
     std::vector<int> forms = {WG_FORM_DIRECT};
     if (ctx->have_tm && !t.slots.empty()) forms.push_back(WG_FORM_TILE);
     if (ctx->have_march && !t.slots.empty()) forms.push_back(WG_FORM_MARCH);
+    if (ctx->have_tm && !t.slots.empty()) forms.push_back(WG_FORM_PIPE);
     if (forms.size() == 1) {
         for (int &f : ctx->tuned) f = WG_FORM_DIRECT;
         return WG_OK;
@@ -859,7 +919,7 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true, push))) return st;
     prof_mark(ctx, 1);
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
-                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream, 1));
+                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx), ctx->stream, 1));
     prof_mark(ctx, 2);
     if ((st = stage_launch_df(ctx, t, 1, ctx->B, ctx->C, push))) return st;
     prof_mark(ctx, 3);
@@ -969,6 +1029,17 @@ int build_batch(wg_ctx *ctx, const std::vector<int> &trees) {
 
 int run_sync_batch(wg_ctx *ctx, double *buf) {
     const BatchPlan &bp = ctx->batch;
+    int gst, pst;
+    if (!bp.pcls.begin.empty() && fused_shape(bp.stage_predict, bp.pair_begin, bp.copy_end, bp.push, &gst, &pst) &&
+        bp.pcls.begin[pst].size() == 2) {
+        const unsigned from = gst < 0 ? 0 : (bp.push ? bp.copy_end[gst] : bp.pair_begin[gst]);
+        const unsigned n = gst < 0 ? 0 : bp.pair_begin[gst + 1] - from;
+        const std::vector<int> &pb = bp.pcls.begin[pst];
+        WG_CUDA_OK(launch_sync_df_fused(bp.pairs.p + from, n, bp.pcls.patches.p + pb[0], pb[1] - pb[0],
+                                        bp.pcls.need[pst][0], buf, ctx->gT, ctx->geo.nc, ctx->wav.order_predictor,
+                                        ctx->d_desc, ctx->d_clk, fused_ctr(ctx), ctx->d_err, ctx->stream, 4));
+        return WG_OK;
+    }
     for (int s = 0; s < bp.nstages; s++) {
         if (bp.stage_predict[s]) {
             int st3 = run_pred_classes(ctx, bp.pcls, s, buf, ctx->gT);
@@ -984,7 +1055,7 @@ int run_sync_batch(wg_ctx *ctx, double *buf) {
 
 int stage_launch_batch(wg_ctx *ctx, int stage, const double *in, double *out) {
     const BatchPlan &bp = ctx->batch;
-    return stage_pair(ctx, stage, bp.plain.p, bp.n_plain, bp.masked.p, bp.n_masked, in, out,
+    return stage_pair(ctx, stage, bp.plain.p, bp.n_plain, bp.masked.p, bp.n_masked, bp.stage.p, in, out,
                       bp.push ? ctx->d_push : nullptr, 1);
 }
 
@@ -998,7 +1069,7 @@ int rk4_enqueue_batch(wg_ctx *ctx) {
     if ((st = run_sync_batch(ctx, ctx->B))) return st;
     prof_mark(ctx, 1);
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, bp.all.p, bp.n_all, ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A, ctx->gA, Bs[0],
-                         Bs[1], Bs[2], (int)bp.trees.size(), bp.tree_ids.p, ctx->stream, 1));
+                         Bs[1], Bs[2], (int)bp.trees.size(), bp.tree_ids.p, dt_done(ctx), ctx->stream, 1));
     prof_mark(ctx, 2);
     if ((st = stage_launch_batch(ctx, 1, ctx->B, ctx->C))) return st;
     prof_mark(ctx, 3);
@@ -1029,7 +1100,7 @@ int rk4_enqueue(wg_ctx *ctx, int tree_id) {
     if ((st = run_sync(ctx, t, ctx->A, false, g_rhs, g_rhs))) return st;
     prof_mark(ctx, 1);
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
-                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, ctx->stream));
+                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx), ctx->stream));
     prof_mark(ctx, 2);
     if ((st = stage_launch(ctx, t, 1, ctx->A, ctx->gA, ctx->B, ctx->gT))) return st;
     prof_mark(ctx, 3);
@@ -1165,13 +1236,18 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
             return st;
         }
     }
-    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess) {
+    if (cudaMalloc(&ctx->d_err, 8 * sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         wg_ctx_destroy(ctx.release());
         return fail(WG_ENOMEM, "device allocation failed");
     }
-    cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream);
-    cudaMemsetAsync(ctx->d_clk, 0, sizeof(TreeClock) * ctx->max_trees, ctx->stream);
+    cudaMemsetAsync(ctx->d_err, 0, 8 * sizeof(int), ctx->stream);
+    {
+        std::vector<TreeClock> clk0(ctx->max_trees, fresh_clock(0.0));
+        cudaMemcpyAsync(ctx->d_clk, clk0.data(), sizeof(TreeClock) * ctx->max_trees, cudaMemcpyHostToDevice,
+                        ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+    }
     ctx->h_desc.resize(max_blocks);
     ctx->free_slots.init(max_blocks);
     ctx->trees.resize(ctx->max_trees);
@@ -1242,8 +1318,7 @@ int wg_tree_create(wg_ctx *ctx, const wg_config *cfg, int *tree) {
         t.forest.Jmin = c->Jmin;
         t.forest.Jmax = c->Jmax;
         WG_CUDA_OK(cudaMemcpyAsync(ctx->d_tp + i, &t.tp, sizeof(TreeParams), cudaMemcpyHostToDevice, ctx->stream));
-        TreeClock clk;
-        std::memset(&clk, 0, sizeof(clk));
+        const TreeClock clk = fresh_clock(0.0);
         WG_CUDA_OK(cudaMemcpyAsync(ctx->d_clk + i, &clk, sizeof(clk), cudaMemcpyHostToDevice, ctx->stream));
         WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
         *tree = i;
@@ -1643,9 +1718,7 @@ int wg_get_mask_block(wg_ctx *ctx, int tree, int block, double *out) {
 int wg_set_time(wg_ctx *ctx, int tree, double time) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return tree_err();
-    TreeClock c;
-    std::memset(&c, 0, sizeof(c));
-    c.time = time;
+    const TreeClock c = fresh_clock(time);
     // time, dt and the divergence flag; the anchoring constant and running
     // max of the stage inputs stay (they describe the state, not the clock)
     WG_CUDA_OK(cudaMemcpyAsync(ctx->d_clk + tree, &c, offsetof(TreeClock, anchor_M), cudaMemcpyHostToDevice,
@@ -1710,7 +1783,7 @@ int wg_compute_dt(wg_ctx *ctx, int tree, double *dt) {
     if (!t) return tree_err();
     const int *Bs = ctx->cfg.Bs;
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
-                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, ctx->stream));
+                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, dt_done(ctx), ctx->stream));
     TreeClock c;
     int st = read_clock(ctx, tree, &c);
     if (st) return st;
@@ -1848,10 +1921,11 @@ int wg_wavelet_threshold(wg_ctx *ctx, int tree, const double *thresh) {
 
 int wg_set_stage_form(wg_ctx *ctx, int form) {
     if (!ctx) return fail(WG_EINVAL, "null ctx");
-    if (form != WG_FORM_AUTO && form != WG_FORM_DIRECT && form != WG_FORM_TILE && form != WG_FORM_MARCH)
+    if (form != WG_FORM_AUTO && form != WG_FORM_DIRECT && form != WG_FORM_TILE && form != WG_FORM_MARCH &&
+        form != WG_FORM_PIPE)
         return fail(WG_EINVAL, "unknown stage form %d", form);
-    if (form == WG_FORM_TILE && !ctx->have_tm)
-        return fail(WG_ENOTSUP, "the tile form needs 3-D 16x16 planes, g_rhs = 2 and the FP32-pipe precision");
+    if ((form == WG_FORM_TILE || form == WG_FORM_PIPE) && !ctx->have_tm)
+        return fail(WG_ENOTSUP, "the tile and pipe forms need 3-D 16x16 planes, g_rhs = 2 and the FP32-pipe precision");
     if (form == WG_FORM_MARCH && !ctx->have_march)
         return fail(WG_ENOTSUP, "the march form needs 3-D 16^3 blocks, g_rhs = 2 and the FP32-pipe precision");
     ctx->stage_form = form;
@@ -1863,9 +1937,11 @@ int wg_set_stage_form(wg_ctx *ctx, int form) {
 int wg_set_stage_forms(wg_ctx *ctx, const int *forms) {
     if (!ctx || !forms) return fail(WG_EINVAL, "bad arguments");
     for (int k = 0; k < 4; k++) {
-        if (forms[k] != WG_FORM_DIRECT && forms[k] != WG_FORM_TILE && forms[k] != WG_FORM_MARCH)
-            return fail(WG_EINVAL, "stage %d: form %d is not direct, tile or march", k + 1, forms[k]);
-        if ((forms[k] == WG_FORM_TILE && !ctx->have_tm) || (forms[k] == WG_FORM_MARCH && !ctx->have_march))
+        if (forms[k] != WG_FORM_DIRECT && forms[k] != WG_FORM_TILE && forms[k] != WG_FORM_MARCH &&
+            forms[k] != WG_FORM_PIPE)
+            return fail(WG_EINVAL, "stage %d: form %d is not direct, tile, march or pipe", k + 1, forms[k]);
+        if (((forms[k] == WG_FORM_TILE || forms[k] == WG_FORM_PIPE) && !ctx->have_tm) ||
+            (forms[k] == WG_FORM_MARCH && !ctx->have_march))
             return fail(WG_ENOTSUP, "stage %d: form %d does not apply to this configuration", k + 1, forms[k]);
     }
     ctx->stage_form = WG_FORM_AUTO;
@@ -2764,7 +2840,7 @@ int wg_time_kernel(wg_ctx *ctx, int tree, int which, int reps, double *ms_per_la
         if (which == 0) return stage_launch(ctx, *t, 2, ctx->B, ctx->gT, ctx->C, ctx->gT);
         if (which == 1) return run_sync(ctx, *t, ctx->D, true, g_rhs, g_rhs, df, push);
         WG_CUDA_OK(launch_dt(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk,
-                             ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, ctx->stream));
+                             ctx->A, ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree, dt_done(ctx), ctx->stream));
         return WG_OK;
     };
     if ((st = once())) return st;

@@ -24,10 +24,13 @@ struct TreeParams {
 };
 
 // Per-tree time state on the device.
+// start value of a tree's running dt minimum: the bits of 9e9
+constexpr unsigned long long kDtStartBits = 0x4200C388D0000000ull;
+
 struct TreeClock {
     double time;
     double dt;
-    unsigned long long dt_min_bits;  // running min over blocks (positive double bits)
+    unsigned long long dt_min_bits;  // running min over blocks (positive double bits); kDtStartBits between reductions
     int    diverged;
     int    reshadow;   // the anchored copy an upload wrote with a guessed constant must be redone
     // dt, dt/3 and dt/6 as double-float pairs (written with dt)
@@ -136,8 +139,11 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
                                 cudaStream_t s, int keep_state = 1, double *cout = nullptr,
                                 const int *cpos = nullptr);
-// (march: tmap is a map with one-plane boxes and the whole-block ring kernel
-// runs; keep_state 0 times stage 4 without storing u_n+1)
+// (march 0: tmap is a slab map and the tile kernel runs; 1: tmap is a map
+// with one-plane boxes and the whole-block ring kernel runs; 2: tmap is a
+// slab map and the persistent double-buffered slab kernel runs over masked
+// and unmasked blocks at once, masked then being the number of masked blocks
+// at the head of blk; keep_state 0 times stage 4 without storing u_n+1)
 // slab height of the TMA tile form of the double-float stage kernel (3-D,
 // Bs0*Bs1 = 256), 0 where it does not apply; tmap (a CUtensorMap over the
 // stage-input buffer: dims nx, ny, nz*nc*slots; box nx, ny, zt+4) selects it
@@ -159,6 +165,15 @@ cudaError_t launch_umax_reset(TreeClock *clk, const int *trees, int ntrees, cuda
 cudaError_t launch_anchor_from_state(const int *slots, int nblk, const double *A, BufGeo ga, int nc, int Bx, int By,
                                      int Bz, const BlockDesc *desc, TreeClock *clk, const int *trees, int ntrees,
                                      int scan, cudaStream_t s);
+// the per-step ghost sync of a double-float buffer as one persistent launch:
+// npairs restriction entries (gather form) and then npatch prediction
+// patches (largest first; max_smem_doubles: the largest need per component);
+// ctr: three zeroed counters of this stream (left zeroed), err: set when a
+// wait for the restrictions ran out
+cudaError_t launch_sync_df_fused(const void *pairs, unsigned npairs, const Patch *patches, int npatch,
+                                 int max_smem_doubles, void *buf, BufGeo geo, int nc, int order_predictor,
+                                 const BlockDesc *desc, const TreeClock *clk, unsigned *ctr, int *err, cudaStream_t s,
+                                 int min_ctas);
 cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_doubles, void *buf, BufGeo geo, int nc,
                               int order_predictor, const BlockDesc *desc, const TreeClock *clk, cudaStream_t s,
                               int min_ctas = 1);
@@ -177,9 +192,12 @@ struct SphereArgs {
 cudaError_t launch_sphere_flags(const int4 *cand, int n, const SphereArgs &a, int *flags, cudaStream_t s);
 cudaError_t launch_sphere_fill(const int4 *cand, const int *slot, int n, const SphereArgs &a, double *mask,
                                float2 *mask_df, double c_eta_inv, cudaStream_t s);
+// dt of the listed trees in one launch (the last CTA finalises; done: a
+// zeroed counter of this stream, left zeroed); every TreeClock's dt_min_bits
+// holds kDtStartBits between reductions
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
-                      const int *trees, cudaStream_t s, int step_start = 0);
+                      const int *trees, unsigned *done, cudaStream_t s, int step_start = 0);
 
 cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
 // max |u| per component over the interiors of the listed blocks (Bs2 = 1 in 2-D)

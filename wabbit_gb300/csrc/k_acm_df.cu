@@ -554,6 +554,112 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_march(StageArgsDF a, cons
     if (STAGE == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
 }
 
+// Persistent form of the tile kernel ("pipe"): one launch per RK stage for
+// all blocks of all listed trees, masked and unmasked. One CTA of 512
+// threads per SM walks the slabs s = blockIdx.x, blockIdx.x + gridDim.x, ...
+// of the block list (4 slabs of 4 planes per 16^3 block; the masked blocks
+// come first, and a slab runs the masked or the unmasked body, uniform over
+// the CTA). Shared memory holds two slab buffers (2 x 102.4 KB): while the
+// CTA computes the slab in one, TMA fills the other with the CTA's next
+// slab, so the 16 warps keep issuing while the loads run (the tile form's
+// CTAs wait for their own slab, and an SM then computes with half of its
+// warps). Threads 0-255 compute planes 0-1 of their (x, y) column, threads
+// 256-511 planes 2-3. Neighbouring CTAs take neighbouring slabs at the same
+// time, so the halo planes two slabs share come from L2. The arithmetic is
+// the tile form's, in the same order. A TMA completion that does not arrive
+// within a second on any thread sets *err and ends the CTA after bounded
+// waits for both buffers' copies in flight; the context's state is then
+// undefined.
+template <int STAGE, bool MASKED>
+__device__ __forceinline__ void pipe_planes(const StageArgsDF &a, const DfConst &kc, const BlockDesc &d, int b,
+                                            const float2 *sb, int zs, int z0, int ix, int iy, long long boff,
+                                            RkIn<3> &nxt, float &umax) {
+    constexpr int NX = 20, NY = 20, GB = 2, BS = 16, ZT = 4;
+    constexpr int PLANE = NX * NY, COMP = (ZT + 4) * PLANE;
+    constexpr int stv[3] = {1, NX, PLANE};
+    const int npts_int = BS * BS * a.Bs2;
+#pragma unroll 1
+    for (int k = 0; k < 2; k++) {
+        const int iz = z0 + k;
+        const int q = (iz * BS + iy) * BS + ix;
+        const long long off = boff + (long long)(iz + GB) * PLANE;
+        const RkIn<3> cur = nxt;
+        if (k == 0) rk_load<3, STAGE>(a, b, ix, iy, iz + 1, off + PLANE, nxt);
+        const float2 *u = sb + ((iz - zs + 2) * NY + (iy + GB)) * NX + (ix + GB);
+        df2 r[4], ctr[4];
+        rhs_df<3>(u, COMP, stv, kc, MASKED ? a.mask + (long long)d.mask * 5 * npts_int + q : nullptr, npts_int, r,
+                  ctr, ctr[3]);
+        rk_df<3, STAGE>(a, kc, b, ix, iy, iz, off, r, ctr, cur, umax);
+    }
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(512, 1) acm_stage_df_pipe(StageArgsDF a, const __grid_constant__ CUtensorMap tin,
+                                                            int nslab_total, int nslab_masked, int *err) {
+    constexpr int NX = 20, NY = 20, GB = 2, BS = 16, ZT = 4;
+    constexpr int PLANE = NX * NY, COMP = (ZT + 4) * PLANE, BUF = 4 * COMP;
+    extern __shared__ __align__(128) float2 sm[];
+    __shared__ unsigned long long bar[2];
+    const int nsb = a.Bs2 / ZT;   // slabs per block
+    const int total = nslab_total;
+    const int step = (int)gridDim.x;
+    auto issue = [&](int s, int buf) {
+        const int b = a.blk[s / nsb], zb = (s % nsb) * ZT;
+        mbar_arrive_expect_tx(&bar[buf], (unsigned)(4 * COMP * sizeof(float2)));
+#pragma unroll
+        for (int c = 0; c < 4; c++)
+            tma_load_3d(sm + buf * BUF + c * COMP, &tin, 0, 0, (b * 4 + c) * a.gt.nz + zb + GB - 2, &bar[buf]);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        if ((int)blockIdx.x < total) issue((int)blockIdx.x, 0);
+        if ((int)blockIdx.x + step < total) issue((int)blockIdx.x + step, 1);
+    }
+    __syncthreads();   // the barriers are initialised before anyone waits on them
+    const int col = threadIdx.x & 255, half = threadIdx.x >> 8;
+    const int ix = col % BS, iy = col / BS;
+    float umax = 0.f;
+    int utree = -1;   // tree whose maximum umax holds (stage 4)
+    int j = 0;
+#pragma unroll 1
+    for (int s = (int)blockIdx.x; s < total; s += step, j++) {
+        const int buf = j & 1;
+        const int b = a.blk[s / nsb];
+        const int zs = (s % nsb) * ZT;      // first plane of the slab
+        const int z0 = zs + 2 * half;       // first plane of this thread
+        const BlockDesc &d = a.desc[b];
+        if (STAGE == 4 && a.un_out && d.tree != utree) {   // uniform over the CTA
+            if (utree >= 0) merge_umax(umax, a.clk, utree);
+            umax = 0.f;
+            utree = d.tree;
+        }
+        const DfConst kc = load_const(a, d);
+        const long long boff = (long long)b * 4 * a.gt.npts() + (long long)(iy + GB) * NX + (ix + GB);
+        RkIn<3> nxt;
+        rk_load<3, STAGE>(a, b, ix, iy, z0, boff + (long long)(z0 + GB) * PLANE, nxt);
+        // the n-th fill of a buffer completes its phase n; the decision to go
+        // on is the CTA's, so every thread meets the barriers below or none does
+        if (!__syncthreads_and(mbar_wait(&bar[buf], (unsigned)(j >> 1) & 1u, 1000000000ull))) {
+            if (threadIdx.x == 0) {   // this slab's copy and the next one's may still be landing
+                atomicExch(err, 1);
+                mbar_wait(&bar[buf], (unsigned)(j >> 1) & 1u, 1000000000ull);
+                if (s + step < total) mbar_wait(&bar[buf ^ 1], (unsigned)((j + 1) >> 1) & 1u, 1000000000ull);
+            }
+            return;
+        }
+        const float2 *sb = sm + buf * BUF;
+        if (s < nslab_masked) pipe_planes<STAGE, true>(a, kc, d, b, sb, zs, z0, ix, iy, boff, nxt, umax);
+        else pipe_planes<STAGE, false>(a, kc, d, b, sb, zs, z0, ix, iy, boff, nxt, umax);
+        __syncthreads();   // every thread is done with this buffer: it takes the slab after next
+        if (threadIdx.x == 0 && s + 2 * step < total) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(s + 2 * step, buf);
+        }
+    }
+    if (STAGE == 4 && a.un_out && utree >= 0) merge_umax(umax, a.clk, utree);
+}
+
 // slab height of the tile kernel (0: not applicable): 16x16 planes, two
 // ghost layers, Bs2 a multiple of 4
 int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g) {
@@ -596,7 +702,28 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
         a.third[1] = (float)(t - (double)a.third[0]);
     }
     const int zt = tmap ? tile_slab(dim, Bs0, Bs1, Bs2, gt.gb) : 0;
-    if (march && zt == 4 && Bs2 == 16 && gt.nx == 20 && gt.ny == 20) {
+    if (march == 2 && zt == 4 && gt.nx == 20 && gt.ny == 20) {
+        // masked: the number of masked blocks at the head of blk
+        if (masked < 0 || masked > nblk) return cudaErrorInvalidValue;
+        const long long total = (long long)nblk * (Bs2 / zt);
+        if (total >= (1ll << 31)) return cudaErrorInvalidValue;
+        const size_t smem = sizeof(float2) * 2 * 4 * (size_t)(zt + 4) * gt.nx * gt.ny;
+        const CUtensorMap &map = *reinterpret_cast<const CUtensorMap *>(tmap);
+        using K = void (*)(StageArgsDF, const CUtensorMap, int, int, int *);
+        static const K kerns[4] = {acm_stage_df_pipe<1>, acm_stage_df_pipe<2>, acm_stage_df_pipe<3>,
+                                   acm_stage_df_pipe<4>};
+        const K kern = kerns[stage - 1];
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int dev = 0, nsm = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        a.chunks = 0;
+        const unsigned grid = (unsigned)std::min<long long>(total, (long long)std::max(1, nsm));
+        kern<<<grid, 512, smem, s>>>(a, map, (int)total, masked * (Bs2 / zt), err);
+        return cudaGetLastError();
+    }
+    if (march == 1 && zt == 4 && Bs2 == 16 && gt.nx == 20 && gt.ny == 20) {
         const size_t smem = sizeof(float2) * 4 * 5 * (size_t)gt.nx * gt.ny;
         const CUtensorMap &map = *reinterpret_cast<const CUtensorMap *>(tmap);
         using K = void (*)(StageArgsDF, const CUtensorMap, int *);

@@ -54,10 +54,19 @@ __device__ __forceinline__ void dt_of_block(const TreeParams &p, const BlockDesc
 // Per-block max |u|^2 over the interior (two passes, umag.cuh) -> per-block
 // dt -> atomic min per tree; a value outside the divergence guard sets the
 // tree's flag.
-template <int DIM>
+// The last CTA to finish (counter *done, set back to zero by it) finalises
+// the listed trees, so the whole reduction is one launch.
+__device__ void dt_finalize_tree(const TreeParams *tp, TreeClock *clk, int t, int step_start);
+
+// BS: the block edge when all edges equal it (index arithmetic by shifts),
+// 0 for the general case
+template <int DIM, int BS>
 __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc *desc, const TreeParams *tp,
-                                                 TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1,
-                                                 int Bs2) {
+                                                 TreeClock *clk, const double *u, BufGeo geo, int Bs0_, int Bs1_,
+                                                 int Bs2_, const int *trees, int ntrees, int step_start,
+                                                 unsigned *done) {
+    const int Bs0 = BS ? BS : Bs0_, Bs1 = BS ? BS : Bs1_, Bs2 = BS ? BS : Bs2_;
+    __shared__ int s_last;
     constexpr int kCache = 4096;
     __shared__ float s32[kCache];
     __shared__ float red32[8];
@@ -103,26 +112,32 @@ __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc
         double u_mag = red64[0];
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) u_mag = fmax(u_mag, red64[w]);
         dt_of_block<DIM>(tp[d.tree], d, u_mag, clk[d.tree]);
+        // acquire-release count of the finished CTAs: the last one sees every
+        // other CTA's minimum (and flag) before it finalises
+        unsigned n;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(n) : "l"(done) : "memory");
+        s_last = n == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        for (int i = threadIdx.x; i < ntrees; i += blockDim.x) dt_finalize_tree(tp, clk, trees[i], step_start);
+        if (threadIdx.x == 0) *done = 0u;
     }
 }
 
-__global__ void dt_reset_kernel(TreeClock *clk, const int *trees, int ntrees) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ntrees) clk[trees[i]].dt_min_bits = (unsigned long long)__double_as_longlong(9.0e9);
-}
-
-// calculate_time_step.f90:28-118 after the MIN reduction
-__global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const int *trees, int ntrees, int step_start) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ntrees) return;
-    const int t = trees[i];
+// calculate_time_step.f90:28-118 after the MIN reduction, for tree t; the
+// running minimum is read through L2 (the other CTAs' atomics) and set back
+// to its start value for the next reduction
+__device__ void dt_finalize_tree(const TreeParams *tp, TreeClock *clk, int t, int step_start) {
     const TreeParams &p = tp[t];
     TreeClock &c = clk[t];
     const double time = c.time;
+    const unsigned long long mbits = __ldcg(&c.dt_min_bits);
+    c.dt_min_bits = kDtStartBits;
     double dt;
     if (p.dt_fixed > 0.0) dt = p.dt_fixed;
     else {
-        dt = __longlong_as_double((long long)c.dt_min_bits);
+        dt = __longlong_as_double((long long)mbits);
         if (p.dt_max > 0.0) dt = fmin(p.dt_max, dt);
     }
     if (p.write_time > 0.0) {
@@ -154,6 +169,11 @@ __global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const i
     }
 }
 
+__global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const int *trees, int ntrees, int step_start) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ntrees) dt_finalize_tree(tp, clk, trees[i], step_start);
+}
+
 __global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntrees) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < ntrees) {
@@ -164,13 +184,15 @@ __global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntree
 
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
-                      const int *trees, cudaStream_t s, int step_start) {
-    dt_reset_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
+                      const int *trees, unsigned *done, cudaStream_t s, int step_start) {
+    if (!done) return cudaErrorInvalidValue;
     if (nblk > 0) {
-        if (dim == 2) dt_kernel<2><<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2);
-        else dt_kernel<3><<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2);
+        const bool b16 = Bs0 == 16 && Bs1 == 16 && (dim == 2 || Bs2 == 16);
+        auto k = dim == 2 ? (b16 ? dt_kernel<2, 16> : dt_kernel<2, 0>) : (b16 ? dt_kernel<3, 16> : dt_kernel<3, 0>);
+        k<<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2, trees, ntrees, step_start, done);
+    } else {
+        dt_finalize_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(tp, clk, trees, ntrees, step_start);
     }
-    dt_finalize_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(tp, clk, trees, ntrees, step_start);
     return cudaGetLastError();
 }
 

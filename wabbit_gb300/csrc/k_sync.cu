@@ -25,6 +25,21 @@
 
 namespace wg {
 
+// Division by a divisor fixed for a patch: q = floor(n / d) as the high
+// word of n * ceil(2^64 / d), exact for every 32-bit n and d >= 2 (the error
+// term n * (ceil(2^64/d) d - 2^64) / 2^64 stays below n d / 2^64 < 1). The
+// element loops of a prediction patch divide every index by up to four such
+// extents, and the generic 32-bit division was most of the kernel's
+// instructions.
+struct FastDiv {
+    unsigned d;
+    unsigned long long m;
+    __device__ __forceinline__ explicit FastDiv(unsigned dd) : d(dd), m(dd > 1u ? ~0ull / dd + 1ull : 0ull) {}
+    __device__ __forceinline__ unsigned div(unsigned n) const {
+        return d > 1u ? (unsigned)__umul64hi((unsigned long long)n, m) : n;
+    }
+};
+
 // Copy and restriction patches: one warp per patch, one lane per receiver
 // row (x fastest), so the index arithmetic is one division per row.
 __global__ void __launch_bounds__(128) sync_kernel(const Patch *__restrict__ patches, int npatch, double *buf,
@@ -152,6 +167,7 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
     zw1 -= zw1 & 1;
     const int ny = (yw1 - yw0) / 2 + 1, nz = (zw1 - zw0) / 2 + 1;
     const int ncp = cx * cy * cz;
+    const FastDiv f_cx(cx), f_cy(cy), f_ex(ex), f_ey(ey), f_ny(ny);
     double *C = sm;                       // coarse box
     double *X = C + ncp;                  // ex * ny * nz
     double *XY = X + ex * ny * nz;        // ex * ey * nz
@@ -160,13 +176,15 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
         const double *src = sbuf + ((long long)p.src * nc + c) * npts;
         double *dst = buf + ((long long)p.dst * nc + c) * npts;
         for (int i = threadIdx.x; i < ncp; i += blockDim.x) {
-            const int x = i % cx, y = (i / cx) % cy, z = i / (cx * cy);
+            const int kx = (int)f_cx.div(i), x = i - kx * cx;
+            const int z = (int)f_cy.div(kx), y = kx - z * cy;
             C[i] = src[((long long)(p.slo[2] + z) * geo.ny + (p.slo[1] + y)) * geo.nx + (p.slo[0] + x)];
         }
         __syncthreads();
         // x pass on even rows / planes
         for (int i = threadIdx.x; i < ex * ny * nz; i += blockDim.x) {
-            const int ix = i % ex, jy = (i / ex) % ny, kz = i / (ex * ny);
+            const int kx = (int)f_ex.div(i), ix = i - kx * ex;
+            const int kz = (int)f_ny.div(kx), jy = kx - kz * ny;
             const int fx = x0 + ix, cyy = (yw0 >> 1) + jy, czz = (zw0 >> 1) + kz;
             const double *row = C + ((long long)czz * cy + cyy) * cx;
             double v;
@@ -178,7 +196,8 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
         __syncthreads();
         // y pass on the receiver rows, even planes
         for (int i = threadIdx.x; i < ex * ey * nz; i += blockDim.x) {
-            const int ix = i % ex, j = (i / ex) % ey, kz = i / (ex * ey);
+            const int kx = (int)f_ex.div(i), ix = i - kx * ex;
+            const int kz = (int)f_ey.div(kx), j = kx - kz * ey;
             const int fy = y0 + j;
             const double *col = X + (long long)kz * ny * ex + ix;     // stride ex along the row window
             double v;
@@ -190,7 +209,8 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
         __syncthreads();
         // z pass on the receiver box, write out
         for (int i = threadIdx.x; i < ex * ey * ez; i += blockDim.x) {
-            const int ix = i % ex, j = (i / ex) % ey, k = i / (ex * ey);
+            const int kx = (int)f_ex.div(i), ix = i - kx * ex;
+            const int k = (int)f_ey.div(kx), j = kx - k * ey;
             const int fz = z0 + k;
             const double *pl = XY + (long long)j * ex + ix;            // stride ex*ey along the plane window
             double v;
@@ -227,13 +247,16 @@ __device__ __forceinline__ df2 interp_df(const float2 *v, int stride, int first)
     return df_norm(df_pow2(acc, scale));
 }
 
+// One prediction patch by the whole CTA (sf: the CTA's dynamic shared
+// memory, cg components per pass). The coarse box is read through L2
+// (ld.global.cg): in the fused sync the restrictions of the same launch, run
+// by other CTAs, wrote some of it, and a line this SM's L1 held from before
+// could be stale. Every thread ends past a barrier, so the caller may reuse
+// sf at once.
+
 template <int NCOEF>
-__global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict__ patches, float2 *buf, BufGeo geo,
-                                                         int nc, int cg, const BlockDesc *desc, const TreeClock *clk) {
-    extern __shared__ float2 sf[];
-    const Patch p = patches[blockIdx.x];
-    // the receiver's stage input is anchored to its tree's quantum
-    const float M = clk[desc[p.dst].tree].anchor_M;
+__device__ __forceinline__ void predict_df_patch(const Patch &p, float2 *buf, BufGeo geo, int nc, int cg, float M,
+                                                 float2 *sf) {
     const int cx = p.shi[0] - p.slo[0] + 1, cy = p.shi[1] - p.slo[1] + 1, cz = p.shi[2] - p.slo[2] + 1;
     const int Fx = 2 * cx - 1, Fy = 2 * cy - 1, Fz = 2 * cz - 1;
     constexpr int h = NCOEF - 1;
@@ -248,21 +271,25 @@ __global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict
     const int ny = (yw1 - yw0) / 2 + 1, nz = (zw1 - zw0) / 2 + 1;
     const int ncp = cx * cy * cz, nX = ex * ny * nz, nXY = ex * ey * nz, nR = ex * ey * ez;
     const long long npts = geo.npts();
+    const FastDiv f_cx(cx), f_cy(cy), f_ex(ex), f_ey(ey), f_ny(ny);
+    const FastDiv f_ncp(ncp), f_nX(nX), f_nXY(nXY), f_nR(nR);
     for (int c0 = 0; c0 < nc; c0 += cg) {
         const int ncg = min(cg, nc - c0);
         float2 *C = sf;                      // ncg coarse boxes
         float2 *X = C + ncg * ncp;           // ncg x-pass windows
         float2 *XY = X + ncg * nX;           // ncg x-y windows
         for (int i = threadIdx.x; i < ncg * ncp; i += blockDim.x) {
-            const int c = i / ncp, k = i - c * ncp;
-            const int x = k % cx, y = (k / cx) % cy, z = k / (cx * cy);
-            C[i] = buf[((long long)p.src * nc + c0 + c) * npts +
-                       ((long long)(p.slo[2] + z) * geo.ny + (p.slo[1] + y)) * geo.nx + (p.slo[0] + x)];
+            const int c = (int)f_ncp.div(i), k = i - c * ncp;
+            const int kx = (int)f_cx.div(k), x = k - kx * cx;
+            const int z = (int)f_cy.div(kx), y = kx - z * cy;
+            C[i] = __ldcg(buf + ((long long)p.src * nc + c0 + c) * npts +
+                          ((long long)(p.slo[2] + z) * geo.ny + (p.slo[1] + y)) * geo.nx + (p.slo[0] + x));
         }
         __syncthreads();
         for (int i = threadIdx.x; i < ncg * nX; i += blockDim.x) {
-            const int c = i / nX, k = i - c * nX;
-            const int ix = k % ex, jy = (k / ex) % ny, kz = k / (ex * ny);
+            const int c = (int)f_nX.div(i), k = i - c * nX;
+            const int kx = (int)f_ex.div(k), ix = k - kx * ex;
+            const int kz = (int)f_ny.div(kx), jy = kx - kz * ny;
             const int fx = x0 + ix;
             const float2 *row = C + c * ncp + ((long long)((zw0 >> 1) + kz) * cy + (yw0 >> 1) + jy) * cx;
             float2 v;
@@ -276,8 +303,9 @@ __global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict
         }
         __syncthreads();
         for (int i = threadIdx.x; i < ncg * nXY; i += blockDim.x) {
-            const int c = i / nXY, k = i - c * nXY;
-            const int ix = k % ex, j = (k / ex) % ey, kz = k / (ex * ey);
+            const int c = (int)f_nXY.div(i), k = i - c * nXY;
+            const int kx = (int)f_ex.div(k), ix = k - kx * ex;
+            const int kz = (int)f_ey.div(kx), j = kx - kz * ey;
             const int fy = y0 + j;
             const float2 *col = X + c * nX + (long long)kz * ny * ex + ix;
             float2 v;
@@ -291,8 +319,9 @@ __global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict
         }
         __syncthreads();
         for (int i = threadIdx.x; i < ncg * nR; i += blockDim.x) {
-            const int c = i / nR, k = i - c * nR;
-            const int ix = k % ex, j = (k / ex) % ey, kk = k / (ex * ey);
+            const int c = (int)f_nR.div(i), k = i - c * nR;
+            const int kx = (int)f_ex.div(k), ix = k - kx * ex;
+            const int kk = (int)f_ey.div(kx), j = kx - kk * ey;
             const int fz = z0 + kk;
             const float2 *pl = XY + c * nXY + (long long)j * ex + ix;
             float2 v;
@@ -310,6 +339,118 @@ __global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict
         __syncthreads();
     }
 }
+
+template <int NCOEF>
+__global__ void __launch_bounds__(256) predict_df_kernel(const Patch *__restrict__ patches, float2 *buf, BufGeo geo,
+                                                         int nc, int cg, const BlockDesc *desc, const TreeClock *clk) {
+    extern __shared__ float2 sf[];
+    const Patch p = patches[blockIdx.x];
+    // the receiver's stage input is anchored to its tree's quantum
+    predict_df_patch<NCOEF>(p, buf, geo, nc, cg, clk[desc[p.dst].tree].anchor_M, sf);
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void red_release_add_u32(unsigned *p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long sync_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The per-step ghost sync of the FP32-pipe precision as one launch: the
+// restriction entries (gather form) and then the prediction patches, which
+// read coarse ghost nodes the restrictions fill. CTAs take work items in
+// order from a ticket counter: chunks of 512 restriction entries first, then
+// one prediction patch per ticket (largest first). A CTA holding a
+// prediction ticket waits until every restriction chunk is done; every chunk
+// was handed to a running CTA before that ticket, and chunks wait for
+// nothing, so the wait ends (bounded at one second all the same: then *err
+// is set and the CTA stops). ctr[0] is the ticket counter, ctr[1] the chunks
+// done, ctr[2] the CTAs that finished; the last CTA to finish sets all three
+// back to zero for the next launch.
+template <int NC, int NCOEF>
+__global__ void __launch_bounds__(256, 4) sync_df_fused_kernel(const uint2 *__restrict__ pairs, unsigned npairs,
+                                                            const Patch *__restrict__ patches, int npatch,
+                                                            float2 *buf, BufGeo geo, int cg, const BlockDesc *desc,
+                                                            const TreeClock *clk, unsigned *ctr, int *err) {
+    extern __shared__ float2 sf[];
+    __shared__ unsigned s_tk;
+    __shared__ int s_ok;
+    constexpr unsigned CHUNK = 512;
+    const unsigned ng = (npairs + CHUNK - 1) / CHUNK;
+    const unsigned nwork = ng + (unsigned)npatch;
+    const unsigned cs = (unsigned)geo.npts();
+    auto *b64 = reinterpret_cast<unsigned long long *>(buf);
+    bool ready = ng == 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_tk = atomicAdd(&ctr[0], 1u);
+        __syncthreads();
+        const unsigned tk = s_tk;
+        __syncthreads();   // every thread has the ticket before thread 0 takes the next
+        if (tk >= nwork) break;
+        if (tk < ng) {
+            const unsigned base = tk * CHUNK + threadIdx.x;
+            uint2 e[2];
+            unsigned long long v[2][NC];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const unsigned i = base + k * 256u;
+                e[k] = i < npairs ? __ldg(pairs + i) : make_uint2(0u, 0u);
+                if (i < npairs) {
+#pragma unroll
+                    for (int c = 0; c < NC; c++) v[k][c] = b64[e[k].y + c * cs];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                if (base + k * 256u < npairs) {
+#pragma unroll
+                    for (int c = 0; c < NC; c++) b64[e[k].x + c * cs] = v[k][c];
+                }
+            }
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0) red_release_add_u32(&ctr[1], 1u);
+            continue;
+        }
+        if (!ready) {
+            if (threadIdx.x == 0) {
+                s_ok = 1;
+                const unsigned long long t0 = sync_ns();
+                while (ld_acquire_u32(&ctr[1]) < ng) {
+                    if (sync_ns() - t0 > 1000000000ull) {
+                        s_ok = 0;
+                        atomicExch(err, 1);
+                        break;
+                    }
+                }
+            }
+            __syncthreads();
+            if (!s_ok) break;
+            ready = true;
+        }
+        const Patch p = patches[tk - ng];
+        predict_df_patch<NCOEF>(p, buf, geo, NC, cg, clk[desc[p.dst].tree].anchor_M, sf);
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&ctr[2], 1u) == gridDim.x - 1) {
+            ctr[0] = 0u;
+            ctr[1] = 0u;
+            ctr[2] = 0u;
+            __threadfence();
+        }
+    }
+}
+
 
 cudaError_t sync_init() { return cudaSuccess; }
 
@@ -370,6 +511,52 @@ cudaError_t launch_predict_df(const Patch *patches, int npatch, int max_smem_dou
         case 8: return go(predict_df_kernel<8>, 3);
         default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_sync_df_fused(const void *pairs, unsigned npairs, const Patch *patches, int npatch,
+                                 int max_smem_doubles, void *buf, BufGeo geo, int nc, int order_predictor,
+                                 const BlockDesc *desc, const TreeClock *clk, unsigned *ctr, int *err, cudaStream_t s,
+                                 int min_ctas) {
+    if (npairs == 0 && npatch <= 0) return cudaSuccess;
+    if (!ctr || !err || (npatch > 0 && !patches) || (npairs > 0 && !pairs)) return cudaErrorInvalidValue;
+    // components per prediction pass as in launch_predict_df
+    const size_t per = sizeof(float2) * (size_t)std::max(1, max_smem_doubles);
+    const size_t limit = 200 * 1024;
+    if (per > limit) return cudaErrorInvalidValue;
+    const size_t room = std::min<size_t>(limit, (size_t)(224 * 1024) / (size_t)std::max(1, min_ctas));
+    const int cg = (int)std::max<size_t>(1, std::min<size_t>((size_t)nc, room / per));
+    const size_t smem = npatch > 0 ? per * cg : 0;
+    const unsigned nwork = (npairs + 511u) / 512u + (unsigned)std::max(0, npatch);
+    auto go = [&](auto kern) -> cudaError_t {
+        cudaError_t e;
+        if (smem > 48 * 1024 &&
+            (e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+            return e;
+        int dev = 0, nsm = 0, occ = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, smem)) != cudaSuccess) return e;
+        const unsigned grid = std::min<unsigned>(nwork, (unsigned)std::max(1, nsm * std::max(1, occ)));
+        kern<<<grid, 256, smem, s>>>(reinterpret_cast<const uint2 *>(pairs), npairs, patches, npatch,
+                                     reinterpret_cast<float2 *>(buf), geo, cg, desc, clk, ctr, err);
+        return cudaGetLastError();
+    };
+    if (nc == 4) {
+        switch (order_predictor) {
+            case 2: return go(sync_df_fused_kernel<4, 2>);
+            case 4: return go(sync_df_fused_kernel<4, 4>);
+            case 6: return go(sync_df_fused_kernel<4, 6>);
+            case 8: return go(sync_df_fused_kernel<4, 8>);
+        }
+    } else if (nc == 3) {
+        switch (order_predictor) {
+            case 2: return go(sync_df_fused_kernel<3, 2>);
+            case 4: return go(sync_df_fused_kernel<3, 4>);
+            case 6: return go(sync_df_fused_kernel<3, 6>);
+            case 8: return go(sync_df_fused_kernel<3, 8>);
+        }
+    }
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_expand(const Patch *patches, const unsigned *first, int npatch, unsigned total, BufGeo geo,
