@@ -34,11 +34,26 @@ namespace wg {
 struct FastDiv {
     unsigned d;
     unsigned long long m;
-    __device__ __forceinline__ explicit FastDiv(unsigned dd) : d(dd), m(dd > 1u ? ~0ull / dd + 1ull : 0ull) {}
     __device__ __forceinline__ unsigned div(unsigned n) const {
         return d > 1u ? (unsigned)__umul64hi((unsigned long long)n, m) : n;
     }
 };
+
+__device__ __forceinline__ unsigned long long fastdiv_magic(unsigned d) { return d > 1u ? ~0ull / d + 1ull : 0ull; }
+
+// the multipliers of up to 9 divisors of a patch, formed once per CTA (a
+// 64-bit division each) into shared memory mag[]; every thread calls it,
+// and it ends past a barrier
+__device__ __forceinline__ void fastdiv_setup(unsigned long long *mag, const unsigned (&d)[9]) {
+    if (threadIdx.x < 9) {
+        unsigned v = d[0];
+#pragma unroll
+        for (int k = 1; k < 9; k++)
+            if ((int)threadIdx.x == k) v = d[k];
+        mag[threadIdx.x] = fastdiv_magic(v);
+    }
+    __syncthreads();
+}
 
 // Copy and restriction patches: one warp per patch, one lane per receiver
 // row (x fastest), so the index arithmetic is one division per row.
@@ -167,7 +182,10 @@ __global__ void __launch_bounds__(256) predict_kernel(const Patch *__restrict__ 
     zw1 -= zw1 & 1;
     const int ny = (yw1 - yw0) / 2 + 1, nz = (zw1 - zw0) / 2 + 1;
     const int ncp = cx * cy * cz;
-    const FastDiv f_cx(cx), f_cy(cy), f_ex(ex), f_ey(ey), f_ny(ny);
+    __shared__ unsigned long long mag[9];
+    fastdiv_setup(mag, {(unsigned)cx, (unsigned)cy, (unsigned)ex, (unsigned)ey, (unsigned)ny, 1u, 1u, 1u, 1u});
+    const FastDiv f_cx{(unsigned)cx, mag[0]}, f_cy{(unsigned)cy, mag[1]}, f_ex{(unsigned)ex, mag[2]},
+        f_ey{(unsigned)ey, mag[3]}, f_ny{(unsigned)ny, mag[4]};
     double *C = sm;                       // coarse box
     double *X = C + ncp;                  // ex * ny * nz
     double *XY = X + ex * ny * nz;        // ex * ey * nz
@@ -271,8 +289,13 @@ __device__ __forceinline__ void predict_df_patch(const Patch &p, float2 *buf, Bu
     const int ny = (yw1 - yw0) / 2 + 1, nz = (zw1 - zw0) / 2 + 1;
     const int ncp = cx * cy * cz, nX = ex * ny * nz, nXY = ex * ey * nz, nR = ex * ey * ez;
     const long long npts = geo.npts();
-    const FastDiv f_cx(cx), f_cy(cy), f_ex(ex), f_ey(ey), f_ny(ny);
-    const FastDiv f_ncp(ncp), f_nX(nX), f_nXY(nXY), f_nR(nR);
+    __shared__ unsigned long long mag[9];
+    fastdiv_setup(mag, {(unsigned)cx, (unsigned)cy, (unsigned)ex, (unsigned)ey, (unsigned)ny, (unsigned)ncp,
+                        (unsigned)nX, (unsigned)nXY, (unsigned)nR});
+    const FastDiv f_cx{(unsigned)cx, mag[0]}, f_cy{(unsigned)cy, mag[1]}, f_ex{(unsigned)ex, mag[2]},
+        f_ey{(unsigned)ey, mag[3]}, f_ny{(unsigned)ny, mag[4]};
+    const FastDiv f_ncp{(unsigned)ncp, mag[5]}, f_nX{(unsigned)nX, mag[6]}, f_nXY{(unsigned)nXY, mag[7]},
+        f_nR{(unsigned)nR, mag[8]};
     for (int c0 = 0; c0 < nc; c0 += cg) {
         const int ncg = min(cg, nc - c0);
         float2 *C = sf;                      // ncg coarse boxes
