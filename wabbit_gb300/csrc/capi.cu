@@ -240,6 +240,7 @@ struct wg_ctx {
     // wg_rk4_stream: stage 4 of the tree's step also writes u_n+1 into this
     // compact array (positions by block slot in d_pos), instead of a gather
     double *s4_out = nullptr;
+    int s4_keep = 1;                    // stage-4 mode of rk4_enqueue_df (launch_acm_stage_df keep_state)
     DevArray<int> d_pos;
     // set when a bounded device wait gave up (WG_ETIMEOUT): a bulk copy may
     // still have been landing in shared memory, so nothing the context holds
@@ -933,7 +934,7 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     prof_mark(ctx, 7);
     if ((st = run_sync(ctx, t, ctx->E, true, g_rhs, g_rhs, true, push))) return st;
     prof_mark(ctx, 8);
-    if ((st = stage_launch_df(ctx, t, 4, ctx->E, ctx->B, push))) return st;
+    if ((st = stage_launch_df(ctx, t, 4, ctx->E, ctx->B, push, ctx->s4_keep))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
     prof_mark(ctx, 9);
     return WG_OK;
@@ -3098,9 +3099,15 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
         t->shadow_valid = shadow;
         // the result buffer O[cur] is free once the result of step k-2 is out
         if (k >= 2) WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, d2h_done[cur], 0));
-        if (shadow) ctx->s4_out = O[cur];
+        // the result goes to O[cur]; except after the last step the next
+        // input replaces it, so it need not reach the state or its copy
+        if (shadow) {
+            ctx->s4_out = O[cur];
+            ctx->s4_keep = k + 1 < nsteps ? 2 : 1;
+        }
         st = rk4_enqueue(ctx, tree);
         ctx->s4_out = nullptr;
+        ctx->s4_keep = 1;
         if (st) return st;
         if (!shadow)
             WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[cur], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,

@@ -41,12 +41,13 @@ struct StageArgsDF {
     const float2 *in;      // stage input s_j (thin layout, ghosts synchronised)
     const float2 *u0;      // anchored copy of u_n = s1 (thin layout)
     const float2 *s2, *s3; // stage inputs 2 and 3 (thin layout; read by stage 4)
-    float2 *out;           // next stage input; at stage 4 the copy of u_{n+1}
+    float2 *out;           // next stage input; at stage 4 the copy of u_{n+1} (null: not stored)
     BufGeo gt;
     double *un;            // u_n, FP64 (full layout)
-    double *un_out;        // where stage 4 stores u_n+1 (un, or null when timing the stage)
+    double *un_out;        // where stage 4 stores u_n+1 (un, or null: not stored)
     double *cout;          // stage 4: u_n+1 also into a compact interior array (nblk, nc, Bz, By, Bx), or null
     const int *cpos;       // block slot -> its position in cout
+    int record;            // stage 4: merge max |u_n+1| into the tree's running max
     BufGeo gun;
     const float2 *mask;    // 5 words per point, interior only
     const int *push;       // same-level ghost copies pushed by the writer, or null
@@ -74,16 +75,17 @@ __device__ __forceinline__ df2 cf(const float c[2]) { return {c[0], c[1]}; }
 // fill those nodes later); dir = (dz+1)*9 + (dy+1)*3 + (dx+1) points from b
 // to the receiver. The host enables this only after checking that every copy
 // patch of the table is such a translation.
+// (row: the 27 receiver slots of the writer's block, in global or shared
+// memory)
 template <int DIM, int NV>
-__device__ __forceinline__ void push_ghosts(const int *push, int b, int ix, int iy, int iz, int Bs0, int Bs1,
-                                            int Bs2, BufGeo gt, float2 *out, long long cs, const float2 *v) {
+__device__ __forceinline__ void push_ghosts_row(const int *row, int ix, int iy, int iz, int Bs0, int Bs1, int Bs2,
+                                                BufGeo gt, float2 *out, long long cs, const float2 *v) {
     const int g = gt.gb;
     const int sx = ix < g ? -1 : (ix >= Bs0 - g ? 1 : 0);
     const int sy = iy < g ? -1 : (iy >= Bs1 - g ? 1 : 0);
     const int sz = DIM == 3 ? (iz < g ? -1 : (iz >= Bs2 - g ? 1 : 0)) : 0;
     const int near = (sx ? 1 : 0) | (sy ? 2 : 0) | (sz ? 4 : 0);
     if (!near) return;
-    const int *row = push + b * 27;
     // the point's offset inside a block; a receiver across (dx, dy, dz) sees
     // it shifted by -(dx Bs0 + dy Bs1 nx + dz Bs2 nx ny)
     const long long own = ((long long)(DIM == 3 ? iz + g : 0) * gt.ny + (iy + g)) * gt.nx + (ix + g);
@@ -95,6 +97,12 @@ __device__ __forceinline__ void push_ghosts(const int *push, int b, int ix, int 
 #pragma unroll
         for (int c = 0; c < NV; c++) o[c * cs] = v[c];
     }
+}
+
+template <int DIM, int NV>
+__device__ __forceinline__ void push_ghosts(const int *push, int b, int ix, int iy, int iz, int Bs0, int Bs1,
+                                            int Bs2, BufGeo gt, float2 *out, long long cs, const float2 *v) {
+    push_ghosts_row<DIM, NV>(push + b * 27, ix, iy, iz, Bs0, Bs1, Bs2, gt, out, cs, v);
 }
 
 // The per-block and per-tree constants of a stage, loaded once per thread:
@@ -306,16 +314,17 @@ __device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int ix, int
 
 // RK4 stage update of one point: stages 1-3 write the anchored next stage
 // input u_n + a dt k_j (a = 1/2, 1/2, 1), stage 4 writes u_n+1 to the FP64
-// state (unless un_out is null: a timing run) and its anchored copy, and
-// returns the largest |u_n+1| of the point in umax. ctr: the centre values of this stage's input (s1 = u_n at stage
-// 1, s4 at stage 4). (ix, iy, iz): interior coordinates; off: the point's
+// state (unless un_out is null), to cout (when given) and its anchored copy
+// (unless out is null), and returns the largest |u_n+1| of the point in
+// umax. ctr: the centre values of this stage's input (s1 = u_n at stage 1,
+// s4 at stage 4). (ix, iy, iz): interior coordinates; off: the point's
 // offset in the thin buffers (component 0).
 template <int DIM, int STAGE>
 __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, int b, int ix, int iy, int iz,
                                       long long off, const df2 r[DIM + 1], const df2 ctr[DIM + 1],
                                       const RkIn<DIM> &in, float &umax) {
     const long long cs = a.gt.npts();
-    float2 *o = a.out + off;
+    float2 *o = a.out ? a.out + off : nullptr;
     float2 ov[DIM + 1];
     if (STAGE < 4) {
 #pragma unroll
@@ -331,6 +340,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
                      ((long long)(iz + (DIM == 3 ? a.gun.gb : 0)) * a.gun.ny + (iy + a.gun.gb)) * a.gun.nx +
                      (ix + a.gun.gb);
         const df2 third = {a.third[0], a.third[1]};
+        float2 *const ob = a.out;
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
             const double u = f2_bits(in.c[c]);
@@ -346,11 +356,14 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
             if (a.cout)
                 a.cout[((long long)a.cpos[b] * (DIM + 1) + c) * a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1) +
                        ((DIM == 3 ? iz * a.Bs1 : 0) + iy) * a.Bs0 + ix] = v;
-            const df2 w = anchor(df_add_nr(ud, inc), k.M);
-            ov[c] = make_float2(w.hi, w.lo);
-            o[c * cs] = ov[c];
-            umax = fmaxf(umax, fabsf(w.hi));
+            if (ob) {   // the anchored copy of u_n+1 and its running maximum
+                const df2 w = anchor(df_add_nr(ud, inc), k.M);
+                ov[c] = make_float2(w.hi, w.lo);
+                o[c * cs] = ov[c];
+                umax = fmaxf(umax, fabsf(w.hi));
+            }
         }
+        if (!ob) return;   // the result went to cout alone
     }
     if (a.push) push_ghosts<DIM, DIM + 1>(a.push, b, ix, iy, iz, a.Bs0, a.Bs1, a.Bs2, a.gt, a.out, cs, ov);
 }
@@ -411,7 +424,7 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
             default: direct_point<DIM, 4>(a, k, u, cs, stv, m, npts_int, b, ix, iy, iz, off, umax); break;
         }
     }
-    if (a.stage == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
+    if (a.stage == 4 && a.record) merge_umax(umax, a.clk, d.tree);
 }
 
 // 3-D blocks of 16x16xBs2 points with 2 ghost layers (the stage-input
@@ -475,7 +488,7 @@ __global__ void __launch_bounds__(256, 2) acm_stage_df_tile(StageArgsDF a, const
                   ctr[3]);
         rk_df<3, STAGE>(a, kc, b, ix, iy, iz, off, r, ctr, cur, umax);
     }
-    if (STAGE == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
+    if (STAGE == 4 && a.record) merge_umax(umax, a.clk, d.tree);
 }
 
 // Whole-block form of the tile kernel ("march"): one CTA per 16x16x16
@@ -551,7 +564,7 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_march(StageArgsDF a, cons
             load_plane(k + 3);
         }
     }
-    if (STAGE == 4 && a.un_out) merge_umax(umax, a.clk, d.tree);
+    if (STAGE == 4 && a.record) merge_umax(umax, a.clk, d.tree);
 }
 
 // Persistent form of the tile kernel ("pipe"): one launch per RK stage for
@@ -629,7 +642,7 @@ __global__ void __launch_bounds__(512, 1) acm_stage_df_pipe(StageArgsDF a, const
         const int zs = (s % nsb) * ZT;      // first plane of the slab
         const int z0 = zs + 2 * half;       // first plane of this thread
         const BlockDesc &d = a.desc[b];
-        if (STAGE == 4 && a.un_out && d.tree != utree) {   // uniform over the CTA
+        if (STAGE == 4 && a.record && d.tree != utree) {   // uniform over the CTA
             if (utree >= 0) merge_umax(umax, a.clk, utree);
             umax = 0.f;
             utree = d.tree;
@@ -657,7 +670,7 @@ __global__ void __launch_bounds__(512, 1) acm_stage_df_pipe(StageArgsDF a, const
             issue(s + 2 * step, buf);
         }
     }
-    if (STAGE == 4 && a.un_out && utree >= 0) merge_umax(umax, a.clk, utree);
+    if (STAGE == 4 && a.record && utree >= 0) merge_umax(umax, a.clk, utree);
 }
 
 // slab height of the tile kernel (0: not applicable): 16x16 planes, two
@@ -686,8 +699,14 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.out = reinterpret_cast<float2 *>(out);
     a.gt = gt;
     a.un = un;
-    a.un_out = keep_state ? un : nullptr;
+    // keep_state 1: u_n+1 to the state, its copy to out, its maximum recorded
+    // (and to cout when given); 0 (timing): the copy to out only; 2: u_n+1
+    // to cout only (a result the next input replaces)
+    if (keep_state < 0 || keep_state > 2 || (keep_state == 2 && (stage != 4 || !cout))) return cudaErrorInvalidValue;
+    a.un_out = keep_state == 1 ? un : nullptr;
     a.cout = keep_state && stage == 4 ? cout : nullptr;
+    a.record = keep_state == 1;
+    if (keep_state == 2) a.out = nullptr;
     a.cpos = cpos;
     a.gun = gun;
     a.mask = reinterpret_cast<const float2 *>(maskdf);
@@ -803,10 +822,14 @@ __global__ void __launch_bounds__(256) shadow_kernel(const int *__restrict__ blk
 // row per (block, component), 32-bit index arithmetic. Towards the state it
 // also merges max |u| into the tree's running max (clk, when given), from
 // which the anchored copy of the FP32-pipe precision takes its quantum.
+// BS: the block edge when all edges equal it (index arithmetic by shifts),
+// 0 for the general case
+template <int BS>
 __global__ void __launch_bounds__(256) interior_xfer_kernel(const int *__restrict__ slots, double *compact, double *A,
-                                                            BufGeo ga, int nc, int Bx, int By, int Bz, int to_state,
+                                                            BufGeo ga, int nc, int Bx_, int By_, int Bz_, int to_state,
                                                             const BlockDesc *desc, TreeClock *clk, float2 *shadow,
                                                             BufGeo gs, const int *push) {
+    const int Bx = BS ? BS : Bx_, By = BS ? BS : By_, Bz = BS ? (Bz_ > 1 ? BS : 1) : Bz_;
     const int b = slots[blockIdx.x], c = blockIdx.y;
     const int nint = Bx * By * Bz;
     double *cp = compact + ((long long)blockIdx.x * nc + c) * nint;
@@ -838,6 +861,51 @@ __global__ void __launch_bounds__(256) interior_xfer_kernel(const int *__restric
         }
     }
     if (to_state && clk) merge_umax(umax, clk, desc[b].tree);
+}
+
+// The upload direction of interior_xfer_kernel for 3-D 16^3 blocks with the
+// double-float copy: one CTA per block, every thread moving all NV
+// components of its points (the compact rows of the components are read
+// side by side), the block's 27 push receivers staged in shared memory, one
+// merge of the maximum per block. Values and writes are those of
+// interior_xfer_kernel.
+template <int NV>
+__global__ void __launch_bounds__(256) interior_scatter_df_kernel(const int *__restrict__ slots,
+                                                                  const double *__restrict__ compact, double *A,
+                                                                  BufGeo ga, const BlockDesc *desc, TreeClock *clk,
+                                                                  float2 *shadow, BufGeo gs, const int *push) {
+    constexpr int BS = 16, NINT = BS * BS * BS;
+    __shared__ int prow[27];
+    const int b = slots[blockIdx.x];
+    if (push && threadIdx.x < 27) prow[threadIdx.x] = push[b * 27 + threadIdx.x];
+    __syncthreads();
+    const double *cp = compact + (long long)blockIdx.x * NV * NINT;
+    const long long na = ga.npts(), ns = gs.npts();
+    double *ab = A + (long long)b * NV * na;
+    float2 *db = shadow + (long long)b * NV * ns;
+    const float M = clk[desc[b].tree].anchor_M;
+    float umax = 0.f;
+#pragma unroll 1
+    for (int i = threadIdx.x; i < NINT; i += 256) {
+        const int ix = i & (BS - 1), iy = (i >> 4) & (BS - 1), iz = i >> 8;
+        double v[NV];
+#pragma unroll
+        for (int c = 0; c < NV; c++) v[c] = __ldcs(cp + c * NINT + i);
+        const long long oa = ((long long)(iz + ga.gb) * ga.ny + (iy + ga.gb)) * ga.nx + (ix + ga.gb);
+        const long long os = ((long long)(iz + gs.gb) * gs.ny + (iy + gs.gb)) * gs.nx + (ix + gs.gb);
+        float2 f[NV];
+#pragma unroll
+        for (int c = 0; c < NV; c++) {
+            ab[c * na + oa] = v[c];
+            const df2 sv = df_split(v[c]);
+            umax = fmaxf(umax, fabsf(sv.hi));
+            const df2 w = anchor(sv, M);
+            f[c] = make_float2(w.hi, w.lo);
+            db[c * ns + os] = f[c];
+        }
+        if (push) push_ghosts_row<3, NV>(prow, ix, iy, iz, BS, BS, BS, gs, shadow, ns, f);
+    }
+    merge_umax(umax, clk, desc[b].tree);
 }
 
 __global__ void anchor_check_kernel(TreeClock *clk, const int *trees, int ntrees) {
@@ -902,8 +970,14 @@ cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, do
                                  void *shadow, BufGeo gs, const int *push) {
     if (nblk <= 0) return cudaSuccess;
     if (shadow && (!to_state || !clk)) return cudaErrorInvalidValue;
-    interior_xfer_kernel<<<dim3(nblk, nc), 256, 0, s>>>(slots, compact, A, ga, nc, Bx, By, Bz, to_state, desc, clk,
-                                                         reinterpret_cast<float2 *>(shadow), gs, push);
+    const bool b16 = Bx == 16 && By == 16 && (Bz == 1 || Bz == 16);
+    if (shadow && nc == 4 && Bz == 16 && b16 && ga.nz > 1 && gs.nz > 1) {
+        interior_scatter_df_kernel<4><<<(unsigned)nblk, 256, 0, s>>>(slots, compact, A, ga, desc, clk,
+                                                                     reinterpret_cast<float2 *>(shadow), gs, push);
+        return cudaGetLastError();
+    }
+    (b16 ? interior_xfer_kernel<16> : interior_xfer_kernel<0>)<<<dim3(nblk, nc), 256, 0, s>>>(
+        slots, compact, A, ga, nc, Bx, By, Bz, to_state, desc, clk, reinterpret_cast<float2 *>(shadow), gs, push);
     return cudaGetLastError();
 }
 
