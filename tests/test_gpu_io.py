@@ -36,26 +36,32 @@ def test_interior_roundtrip_pinned_and_pageable(dim):
         assert np.array_equal(f.download(), full_pinned)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_rk4_stream_equals_upload_step_download(precision):
-    """wg_rk4_stream (overlapped transfers, two staging buffers) gives, step
-    by step, the same results as upload + wg_rk4_step + download."""
+@pytest.mark.parametrize("precision,scales", [(0, (1, 1, 1, 1)), (1, (1, 1, 1, 1)), (1, (1, 8, 0.25, 3, 3))])
+def test_rk4_stream_equals_upload_step_download(precision, scales):
+    """wg_rk4_stream (overlapped transfers, two staging buffers; with the
+    FP32-pipe precision the last stage of a step loads the next input) gives,
+    step by step, the same results as upload + wg_rk4_step + download, also
+    when the inputs' magnitudes change the anchoring quantum between steps,
+    and leaves the last result as the state."""
     cfg = small_cfg(3, "CDF44", Bs=16, jmin=1, jmax=2)
     cfg.rhs_precision = precision
     lv, co = grids.random_graded(3, cfg.Jmin, cfg.Jmax, seed=7, frac=0.5)
     rng = np.random.default_rng(9)
-    nsteps = 4
+    nsteps = len(scales)
     with Context(cfg, len(lv) + 4) as ctx:
         f = ctx.forest()
         f.set_grid(lv, co)
         shape = (len(lv),) + f.interior_shape
         ins = [torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(nsteps)]
-        for a in ins:
-            a[...] = 0.1 * rng.standard_normal(shape)
+        for a, sc in zip(ins, scales):
+            a[...] = 0.1 * sc * rng.standard_normal(shape)
         outs = [torch.zeros(shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(nsteps)]
         f.set_time(0.0)
         f.rk4_stream(ins, outs)
         t_stream = f.time()
+        assert np.array_equal(f.download_interior(), outs[-1])
+        f.timeStep_tree()
+        after = f.download_interior()
         f.set_time(0.0)
         for k in range(nsteps):
             f.upload_interior(ins[k])
@@ -63,3 +69,5 @@ def test_rk4_stream_equals_upload_step_download(precision):
             ref = f.download_interior()
             assert np.array_equal(outs[k], ref), k
         assert f.time() == t_stream
+        f.timeStep_tree()
+        assert np.array_equal(f.download_interior(), after)

@@ -241,6 +241,8 @@ struct wg_ctx {
     // compact array (positions by block slot in d_pos), instead of a gather
     double *s4_out = nullptr;
     int s4_keep = 1;                    // stage-4 mode of rk4_enqueue_df (launch_acm_stage_df keep_state)
+    const double *s4_next = nullptr;    // stage 4 (keep 3): the next step's compact input
+    cudaEvent_t s4_wait = nullptr;      // stage 4 waits for it (the copy of s4_next), or null
     DevArray<int> d_pos;
     // set when a bounded device wait gave up (WG_ETIMEOUT): a bulk copy may
     // still have been landing in shared memory, so nothing the context holds
@@ -272,7 +274,7 @@ struct wg_ctx {
     cudaStream_t d2h_stream = nullptr;  // results of wg_rk4_stream
     double *stream_buf = nullptr;       // wg_rk4_stream: two input and two output staging buffers
     size_t stream_buf_bytes = 0;
-    cudaEvent_t io_ev[8] = {};          // wg_rk4_stream: h2d done, d2h done, gathered, scattered (x2)
+    cudaEvent_t io_ev[10] = {};         // wg_rk4_stream: h2d done (x3), d2h done (x2), gathered (x2), consumed (x3)
     size_t staging_bytes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -746,7 +748,7 @@ static int stage_pair(wg_ctx *ctx, int stage, const int *plain, int nplain, cons
     auto go = [&](int msk, const int *blk, int n) {
         return launch_acm_stage_df(dim, stage, msk, blk, n, ctx->d_desc, ctx->d_tp, ctx->d_clk, in, ctx->B, ctx->C,
                                    ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0], Bs[1], Bs[2], tm,
-                                   march, ctx->d_err, ctx->stream, keep, ctx->s4_out, ctx->d_pos.p);
+                                   march, ctx->d_err, ctx->stream, keep, ctx->s4_out, ctx->d_pos.p, ctx->s4_next);
     };
     if (march == 2) {
         WG_CUDA_OK(go(nmasked, both, nplain + nmasked));
@@ -934,6 +936,7 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     prof_mark(ctx, 7);
     if ((st = run_sync(ctx, t, ctx->E, true, g_rhs, g_rhs, true, push))) return st;
     prof_mark(ctx, 8);
+    if (ctx->s4_wait) WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, ctx->s4_wait, 0));
     if ((st = stage_launch_df(ctx, t, 4, ctx->E, ctx->B, push, ctx->s4_keep))) return st;
     WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
     prof_mark(ctx, 9);
@@ -3041,15 +3044,15 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     const int nblk = (int)t->slots.size();
     const size_t per = (size_t)ctx->geo.nc * ctx->nint, bytes = sizeof(double) * per * nblk;
     int st;
-    if (ctx->stream_buf_bytes < 4 * bytes) {
+    if (ctx->stream_buf_bytes < 5 * bytes) {
         cudaFree(ctx->stream_buf);
         ctx->stream_buf = nullptr;
         ctx->stream_buf_bytes = 0;
-        if (cudaMalloc(&ctx->stream_buf, 4 * bytes) != cudaSuccess) {
+        if (cudaMalloc(&ctx->stream_buf, 5 * bytes) != cudaSuccess) {
             cudaGetLastError();
-            return fail(WG_ENOMEM, "staging buffers of 4 x %zu bytes do not fit", bytes);
+            return fail(WG_ENOMEM, "staging buffers of 5 x %zu bytes do not fit", bytes);
         }
-        ctx->stream_buf_bytes = 4 * bytes;
+        ctx->stream_buf_bytes = 5 * bytes;
     }
     if ((st = ensure_copy_stream(ctx, 1))) return st;
     if (!ctx->d2h_stream && cudaStreamCreateWithFlags(&ctx->d2h_stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -3058,17 +3061,23 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     }
     for (cudaEvent_t &ev : ctx->io_ev)
         if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return fail(WG_ECUDA, "cudaEventCreate failed");
-    // I[k & 1] receives step k's input, O[k & 1] its result: the copy in of
-    // step k+1 waits only for the scatter of step k-1, the copy out of step k
-    // only for its gather, so both directions use the link at once
-    cudaEvent_t *h2d_done = ctx->io_ev, *d2h_done = ctx->io_ev + 2, *gathered = ctx->io_ev + 4,
-                *scattered = ctx->io_ev + 6;
+    // I[k % 3] receives step k's input, O[k & 1] its result. FP32-pipe: the
+    // last stage of step k also loads input k+1 into the state and its
+    // anchored copy (the scatter of the next step), so an input is consumed
+    // either by the first scatter or by the stage 4 before its step. The
+    // copy in of step k+1 waits only for the consumption of input k-2 (three
+    // input buffers: the copies in run ahead of the steps, and a stage 4
+    // finds its next input on the device), the copy out of step k only for
+    // the end of step k, so both directions use the link at once
+    cudaEvent_t *h2d_done = ctx->io_ev, *d2h_done = ctx->io_ev + 3, *gathered = ctx->io_ev + 5,
+                *consumed = ctx->io_ev + 7;
     const bool shadow = ctx->precision == WG_RHS_FP32;
     bool push = false;
     if (shadow && (st = thin_plan(ctx, *t, &push))) return st;
     if ((st = autotune_stage_form(ctx, *t))) return st;
     const size_t pb = per * nblk;
-    double *I[2] = {ctx->stream_buf, ctx->stream_buf + pb}, *O[2] = {ctx->stream_buf + 2 * pb, ctx->stream_buf + 3 * pb};
+    double *I[3] = {ctx->stream_buf, ctx->stream_buf + pb, ctx->stream_buf + 2 * pb};
+    double *O[2] = {ctx->stream_buf + 3 * pb, ctx->stream_buf + 4 * pb};
     // FP32-pipe: the last stage writes the result into O directly
     if (shadow) {
         std::vector<int> pos(ctx->max_blocks, 0);
@@ -3078,44 +3087,61 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     WG_CUDA_OK(cudaMemcpyAsync(I[0], ins[0], bytes, cudaMemcpyDefault, ctx->copy_stream));
     WG_CUDA_OK(cudaEventRecord(h2d_done[0], ctx->copy_stream));
+    auto scatter = [&](double *in) -> int {   // input into the state (and its anchored copy)
+        if (shadow) WG_CUDA_OK(launch_umax_reset(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
+        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, in, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 1,
+                                        ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream,
+                                        shadow ? ctx->B : nullptr, ctx->gT, push ? ctx->d_push : nullptr));
+        return WG_OK;
+    };
+    auto reanchor = [&]() -> int {   // the quantum of the new state, the copy redone if it changed
+        WG_CUDA_OK(launch_anchor_check(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
+        WG_CUDA_OK(launch_shadow(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz,
+                                 push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream, 1));
+        return WG_OK;
+    };
     for (int k = 0; k < nsteps; k++) {
-        const int cur = k & 1, nxt = cur ^ 1;
+        const int cur = k % 3, nxt = (k + 1) % 3, oc = k & 1;
         if (k + 1 < nsteps) {
-            if (k >= 1) WG_CUDA_OK(cudaStreamWaitEvent(ctx->copy_stream, scattered[nxt], 0));
+            if (k >= 2) WG_CUDA_OK(cudaStreamWaitEvent(ctx->copy_stream, consumed[nxt], 0));
             WG_CUDA_OK(cudaMemcpyAsync(I[nxt], ins[k + 1], bytes, cudaMemcpyDefault, ctx->copy_stream));
             WG_CUDA_OK(cudaEventRecord(h2d_done[nxt], ctx->copy_stream));
         }
-        WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, h2d_done[cur], 0));
-        if (shadow) WG_CUDA_OK(launch_umax_reset(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
-        WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, I[cur], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 1,
-                                        ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream,
-                                        shadow ? ctx->B : nullptr, ctx->gT, push ? ctx->d_push : nullptr));
-        WG_CUDA_OK(cudaEventRecord(scattered[cur], ctx->stream));
-        if (shadow) {
-            WG_CUDA_OK(launch_anchor_check(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
-            WG_CUDA_OK(launch_shadow(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz,
-                                     push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream, 1));
+        // the input of step k: scattered here (the first step, or FP64),
+        // otherwise already loaded by the last stage of step k-1
+        if (k == 0 || !shadow) {
+            WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, h2d_done[cur], 0));
+            if ((st = scatter(I[cur]))) return st;
+            WG_CUDA_OK(cudaEventRecord(consumed[cur], ctx->stream));
+            if (shadow && (st = reanchor())) return st;
         }
         t->shadow_valid = shadow;
-        // the result buffer O[cur] is free once the result of step k-2 is out
-        if (k >= 2) WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, d2h_done[cur], 0));
-        // the result goes to O[cur]; except after the last step the next
-        // input replaces it, so it need not reach the state or its copy
+        // the result buffer O[oc] is free once the result of step k-2 is out
+        if (k >= 2) WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, d2h_done[oc], 0));
+        const bool chain = shadow && k + 1 < nsteps;
         if (shadow) {
-            ctx->s4_out = O[cur];
-            ctx->s4_keep = k + 1 < nsteps ? 2 : 1;
+            ctx->s4_out = O[oc];
+            ctx->s4_keep = chain ? 3 : 1;
+            ctx->s4_next = chain ? I[nxt] : nullptr;
+            ctx->s4_wait = chain ? h2d_done[nxt] : nullptr;
         }
         st = rk4_enqueue(ctx, tree);
         ctx->s4_out = nullptr;
         ctx->s4_keep = 1;
+        ctx->s4_next = nullptr;
+        ctx->s4_wait = nullptr;
         if (st) return st;
+        if (chain) {
+            WG_CUDA_OK(cudaEventRecord(consumed[nxt], ctx->stream));
+            if ((st = reanchor())) return st;
+        }
         if (!shadow)
-            WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[cur], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,
+            WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[oc], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,
                                             ctx->d_desc, nullptr, ctx->stream));
-        WG_CUDA_OK(cudaEventRecord(gathered[cur], ctx->stream));
-        WG_CUDA_OK(cudaStreamWaitEvent(ctx->d2h_stream, gathered[cur], 0));
-        WG_CUDA_OK(cudaMemcpyAsync(outs[k], O[cur], bytes, cudaMemcpyDefault, ctx->d2h_stream));
-        WG_CUDA_OK(cudaEventRecord(d2h_done[cur], ctx->d2h_stream));
+        WG_CUDA_OK(cudaEventRecord(gathered[oc], ctx->stream));
+        WG_CUDA_OK(cudaStreamWaitEvent(ctx->d2h_stream, gathered[oc], 0));
+        WG_CUDA_OK(cudaMemcpyAsync(outs[k], O[oc], bytes, cudaMemcpyDefault, ctx->d2h_stream));
+        WG_CUDA_OK(cudaEventRecord(d2h_done[oc], ctx->d2h_stream));
     }
     WG_CUDA_OK(cudaStreamSynchronize(ctx->d2h_stream));
     WG_CUDA_OK(cudaStreamSynchronize(ctx->copy_stream));

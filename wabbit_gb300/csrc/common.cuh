@@ -138,12 +138,13 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
                                 cudaStream_t s, int keep_state = 1, double *cout = nullptr,
-                                const int *cpos = nullptr);
+                                const int *cpos = nullptr, const double *nin = nullptr);
 // (march 0: tmap is a slab map and the tile kernel runs; 1: tmap is a map
 // with one-plane boxes and the whole-block ring kernel runs; 2: tmap is a
 // slab map and the persistent double-buffered slab kernel runs over masked
 // and unmasked blocks at once, masked then being the number of masked blocks
-// at the head of blk; keep_state 0 times stage 4 without storing u_n+1)
+// at the head of blk; keep_state: see launch_acm_stage_df in k_acm_df.cu,
+// 0 times stage 4 without storing u_n+1)
 // slab height of the TMA tile form of the double-float stage kernel (3-D,
 // Bs0*Bs1 = 256), 0 where it does not apply; tmap (a CUtensorMap over the
 // stage-input buffer: dims nx, ny, nz*nc*slots; box nx, ny, zt+4) selects it

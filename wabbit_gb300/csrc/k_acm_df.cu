@@ -46,8 +46,9 @@ struct StageArgsDF {
     double *un;            // u_n, FP64 (full layout)
     double *un_out;        // where stage 4 stores u_n+1 (un, or null: not stored)
     double *cout;          // stage 4: u_n+1 also into a compact interior array (nblk, nc, Bz, By, Bx), or null
-    const int *cpos;       // block slot -> its position in cout
-    int record;            // stage 4: merge max |u_n+1| into the tree's running max
+    const int *cpos;       // block slot -> its position in cout (and nin)
+    const double *nin;     // stage 4: the next step's input (compact like cout), which replaces the state, or null
+    int record;            // stage 4: merge the maximum of what it stores into the tree's running max
     BufGeo gun;
     const float2 *mask;    // 5 words per point, interior only
     const int *push;       // same-level ghost copies pushed by the writer, or null
@@ -352,10 +353,23 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
             const df2 sum = df_sub_nr({sh, sl}, df_pow2(ud, 4.f));
             const df2 inc = df_norm(df_add_nr(df_mul_nr(third, sum), df_mul_nr(k.db, df_norm(r[c]))));
             const double v = __dadd_rn(u, df_to_double(inc));
+            const long long ci = ((long long)(a.cout || a.nin ? a.cpos[b] : 0) * (DIM + 1) + c) * a.Bs0 * a.Bs1 *
+                                     (DIM == 3 ? a.Bs2 : 1) +
+                                 ((DIM == 3 ? iz * a.Bs1 : 0) + iy) * a.Bs0 + ix;
+            if (a.cout) a.cout[ci] = v;
+            if (a.nin) {   // the next input takes the place of u_n+1 in the state and its copy
+                const double x = __ldcs(a.nin + ci);
+                if (a.un_out) un[c * us] = x;
+                if (ob) {
+                    const df2 sx = df_split(x);
+                    const df2 w = anchor(sx, k.M);
+                    ov[c] = make_float2(w.hi, w.lo);
+                    o[c * cs] = ov[c];
+                    umax = fmaxf(umax, fabsf(sx.hi));
+                }
+                continue;
+            }
             if (a.un_out) un[c * us] = v;
-            if (a.cout)
-                a.cout[((long long)a.cpos[b] * (DIM + 1) + c) * a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1) +
-                       ((DIM == 3 ? iz * a.Bs1 : 0) + iy) * a.Bs0 + ix] = v;
             if (ob) {   // the anchored copy of u_n+1 and its running maximum
                 const df2 w = anchor(df_add_nr(ud, inc), k.M);
                 ov[c] = make_float2(w.hi, w.lo);
@@ -684,7 +698,7 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const TreeParams *tp, TreeClock *clk, const void *in, const void *u0, const void *s2,
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
-                                cudaStream_t s, int keep_state, double *cout, const int *cpos) {
+                                cudaStream_t s, int keep_state, double *cout, const int *cpos, const double *nin) {
     if (nblk <= 0) return cudaSuccess;
     if (stage < 1 || stage > 4) return cudaErrorInvalidValue;
     StageArgsDF a;
@@ -701,11 +715,16 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.un = un;
     // keep_state 1: u_n+1 to the state, its copy to out, its maximum recorded
     // (and to cout when given); 0 (timing): the copy to out only; 2: u_n+1
-    // to cout only (a result the next input replaces)
-    if (keep_state < 0 || keep_state > 2 || (keep_state == 2 && (stage != 4 || !cout))) return cudaErrorInvalidValue;
-    a.un_out = keep_state == 1 ? un : nullptr;
+    // to cout only (a result the next input replaces); 3: u_n+1 to cout, and
+    // the next step's input nin (compact like cout) into the state, its copy
+    // to out and its maximum recorded
+    if (keep_state < 0 || keep_state > 3 || (keep_state >= 2 && (stage != 4 || !cout || !cpos)) ||
+        (keep_state == 3 && !nin))
+        return cudaErrorInvalidValue;
+    a.un_out = keep_state == 1 || keep_state == 3 ? un : nullptr;
     a.cout = keep_state && stage == 4 ? cout : nullptr;
-    a.record = keep_state == 1;
+    a.nin = keep_state == 3 ? nin : nullptr;
+    a.record = keep_state == 1 || keep_state == 3;
     if (keep_state == 2) a.out = nullptr;
     a.cpos = cpos;
     a.gun = gun;
