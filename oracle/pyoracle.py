@@ -60,6 +60,9 @@ def lib():
         L.or_adapt.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.or_wc_threshold.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.or_refine_everywhere.argtypes = [ctypes.c_void_p]
+        L.or_refine_significant.argtypes = [ctypes.c_void_p]
+        L.or_set_coarse_extension.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.or_status.argtypes = [ctypes.c_void_p, _ip]
         L.or_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _dp]
         L.or_adapt_full_tree.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.or_run.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
@@ -283,6 +286,27 @@ class Oracle:
 
     def refine_everywhere(self):
         self.L.or_refine_everywhere(self.h)
+
+    def refine_significant(self):
+        """refine_tree with the "significant" indicator: the blocks the last
+        adaptation found significant (and, for gradedness, their coarser
+        neighbours) refine; returns the new block count."""
+        n = self.L.or_refine_significant(self.h)
+        if n < 0:
+            raise RuntimeError(f"or_refine_significant failed ({n})")
+        return n
+
+    def status(self):
+        """The leaves' refinement status after the last adaptation."""
+        n = self.L.or_status(self.h, None)
+        out = np.zeros(n, np.int32)
+        if n:
+            self.L.or_status(self.h, _p(out, ctypes.c_int))
+        return out
+
+    def set_coarse_extension(self, on=True):
+        """useCoarseExtension and useSecurityZone for any wavelet."""
+        self.L.or_set_coarse_extension(self.h, 1 if on else 0)
 
     def filter(self, which):
         lo, hi = ctypes.c_int(), ctypes.c_int()

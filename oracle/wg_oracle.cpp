@@ -143,6 +143,13 @@ struct Oracle {
     // full-tree adaptation: hvy_tmp, refinement status, family
     std::vector<double> tmp;
     std::vector<int> ref, mother, dau;   // dau: 8 per block, -1 where absent
+    // refinement status of the leaves after the last adaptation (0:
+    // significant, REF_UNSIGNIFICANT_STAY), read by the "significant"
+    // refinement indicator
+    std::vector<int> status;
+    // useCoarseExtension / useSecurityZone also for unlifted wavelets (an ini
+    // that sets them, ini_file_to_params.f90:543-546)
+    bool ce_force = false;
     // RK registers: slot 0 = u_n, 1..4 = k1..k4 (hvy_work), interior points
     // only (the only points the RK update reads or writes)
     std::vector<double> work;
@@ -1358,8 +1365,12 @@ static int threshold_block(const Oracle &o, int b, const double *eps_use, double
 }
 
 // refineBlock (LIB/MESH/refinementExecute.f90:4-116): predict the whole block
-// (incl. ghosts) and cut the 2^d daughters out of the fine array.
-static void refine_everywhere(Oracle &o) {
+// (incl. ghosts) and cut the 2^d daughters out of the fine array, for every
+// block with refine[b] != 0 (all blocks below Jmax when refine is empty).
+static void refine_blocks(Oracle &o, const std::vector<int> &refine);
+static void refine_everywhere(Oracle &o) { refine_blocks(o, {}); }
+
+static void refine_blocks(Oracle &o, const std::vector<int> &refine) {
     const wg_config &p = o.cfg;
     const int dim = p.dim, g = p.g;
     const int nblk = (int)o.blocks.size();
@@ -1373,9 +1384,10 @@ static void refine_everywhere(Oracle &o) {
     // daughters are appended in (block, k_daughter) order; blocks on Jmax stay
     // (respectJmaxJmin_tree) and keep their place and data
     std::vector<int> first(nblk);
+    auto stays = [&](int b) { return o.blocks[b].level >= p.Jmax || (!refine.empty() && !refine[b]); };
     for (int b = 0; b < nblk; b++) {
         first[b] = (int)nbl.size();
-        if (o.blocks[b].level >= p.Jmax) {
+        if (stays(b)) {
             nbl.push_back(o.blocks[b]);
             continue;
         }
@@ -1391,7 +1403,7 @@ static void refine_everywhere(Oracle &o) {
     }
     ndata.assign(nbl.size() * o.nc * o.npts, 0.0);
     for (int b = 0; b < nblk; b++) {
-        if (o.blocks[b].level >= p.Jmax) {
+        if (stays(b)) {
             std::copy(o.blk(b), o.blk(b) + size_t(o.nc) * o.npts, ndata.begin() + size_t(first[b]) * o.nc * o.npts);
             continue;
         }
@@ -2133,7 +2145,7 @@ static int adapt_lifted(Oracle &o, const double *eps_use, int everywhere) {
     const Wavelet &w = o.wav;
     const int dim = p.dim, g = p.g, Jmin = p.Jmin;
     const size_t bsz = size_t(o.nc) * o.npts;
-    const bool use_ce = w.lifted;
+    const bool use_ce = w.lifted || o.ce_force;
     bool leaf_first = true;
     for (int d = 0; d < dim; d++)
         if (p.Bs[d] < 3 * std::max(std::abs(w.HD.lo), std::abs(w.HD.hi))) leaf_first = false;
@@ -2305,6 +2317,9 @@ static int adapt_lifted(Oracle &o, const double *eps_use, int everywhere) {
             if (p.Bs[d] < w.Nreconl || p.Bs[d] < w.Nreconr) recon_nb = true;
         }
         if (recon_nb) return WG_ENOTSUP;   // sync_M2D not restated (Bs below Nrecon)
+        // the reconstruction marks blocks in the status; it is restored
+        // afterwards (adapt_tree.f90:721-722,978)
+        const std::vector<int> saved = o.ref;
         std::fill(o.ref.begin(), o.ref.end(), 0);
         for (int b = 0; b < n2; b++) {
             if (!blk_is_leaf(o, b, false)) continue;
@@ -2346,7 +2361,7 @@ static int adapt_lifted(Oracle &o, const double *eps_use, int everywhere) {
                     if (o.blocks[b].level == level) reconstruct(b);
             }
         }
-        std::fill(o.ref.begin(), o.ref.end(), 0);
+        o.ref = saved;
     }
     // prune_fulltree2leafs
     {
@@ -2354,6 +2369,7 @@ static int adapt_lifted(Oracle &o, const double *eps_use, int everywhere) {
         for (int b = 0; b < n2; b++) del[b] = !blk_is_leaf(o, b, false);
         erase_blocks(o, del);
     }
+    o.status = o.ref;
     clear_mask(o);
     update_neighbors(o, false);
     update_family(o, Jmin);
@@ -2576,11 +2592,13 @@ int or_wc_threshold(void *h, double *data, const double *thresh) {
     return WG_OK;
 }
 
-// adapt_tree (CDF X0): indicator 0 threshold-state-vector (eps_use per
-// component), 1 everywhere; returns the new block count or an error
+// adapt_tree: indicator 0 threshold-state-vector (eps_use per component), 1
+// everywhere; CDF X0 by decimation unless the coarse extension is forced,
+// otherwise through the full tree; returns the new block count or an error
 int or_adapt(void *h, const double *eps_use, int indicator) {
     Oracle &o = *(Oracle *)h;
-    const int st = o.wav.Y != 0 ? adapt_lifted(o, eps_use, indicator == 1) : adapt_unlifted(o, eps_use, indicator == 1);
+    const int st = o.wav.Y != 0 || o.ce_force ? adapt_lifted(o, eps_use, indicator == 1)
+                                              : adapt_unlifted(o, eps_use, indicator == 1);
     return st ? st : (int)o.blocks.size();
 }
 
@@ -2594,6 +2612,60 @@ int or_adapt_full_tree(void *h, const double *eps_use, int indicator) {
 
 int or_refine_everywhere(void *h) {
     refine_everywhere(*(Oracle *)h);
+    return WG_OK;
+}
+
+// refine_tree(..., "significant") (LIB/MESH/refine_tree.f90:1-100): the
+// leaves' status of the last adaptation becomes the refinement flag
+// (refinementIndicator_tree.f90:152-167: 0 -> +1, REF_UNSIGNIFICANT_STAY ->
+// 0), respectJmaxJmin_tree, then ensureGradedness_tree without daughters
+// (ensureGradedness_tree.f90: a block next to a finer block that refines
+// refines as well, repeated until nothing changes), then refineBlock of the
+// flagged blocks. Returns the new block count, or WG_EINVAL where a status
+// is -1 or +1 (the reference aborts) or no adaptation set the status.
+int or_refine_significant(void *h) {
+    Oracle &o = *(Oracle *)h;
+    const int n = (int)o.blocks.size();
+    if ((int)o.status.size() != n) return WG_EINVAL;
+    std::vector<int> f(o.status);
+    for (int b = 0; b < n; b++) {
+        if (f[b] == -1 || f[b] == 1) return WG_EINVAL;
+        if (f[b] == 0) f[b] = 1;
+        else if (f[b] == kRefUnsignificantStay) f[b] = 0;
+        if (f[b] == 1 && o.blocks[b].level >= o.cfg.Jmax) f[b] = 0;
+    }
+    for (bool changed = true; changed;) {
+        changed = false;
+        for (int b = 0; b < n; b++) {
+            if (f[b] != 0 && f[b] != kRefUnsignificantStay) continue;
+            for (int r = 0; r < 168; r++) {
+                const int nb = o.nb[size_t(b) * 168 + r];
+                if (nb >= 0 && o.blocks[nb].level == o.blocks[b].level + 1 && f[nb] == 1) {
+                    f[b] = 1;
+                    changed = true;
+                    break;
+                }
+            }
+        }
+    }
+    std::vector<int> refine(n, 0);
+    for (int b = 0; b < n; b++) refine[b] = f[b] == 1;
+    refine_blocks(o, refine);
+    o.status.clear();
+    return (int)o.blocks.size();
+}
+
+// the leaves' status after the last adaptation (out: nblk ints, or null);
+// returns its length (0 when no adaptation set it)
+int or_status(void *h, int *out) {
+    Oracle &o = *(Oracle *)h;
+    if (out) std::copy(o.status.begin(), o.status.end(), out);
+    return (int)o.status.size();
+}
+
+// useCoarseExtension and useSecurityZone for any wavelet (on != 0)
+int or_set_coarse_extension(void *h, int on) {
+    ((Oracle *)h)->ce_force = on != 0;
     return WG_OK;
 }
 

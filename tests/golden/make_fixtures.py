@@ -21,6 +21,9 @@ compare against them:
   (112 blocks, levels 2-5, Bs=32), the reference's refine-everywhere result
   with CDF40 (448 blocks) and its coarsen-everywhere results with CDF40 and
   CDF44.
+* vortex2d_adapt.npz -- TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40: the
+  adaptive 2-D loop (significant refinement, CDF4,0 with coarse extension and
+  security zone): the ini text and the states at t=10 and t=15.
 * acm_cyl.npz -- TESTING/acm/acm_CDF40 and acm_CDF44: 2-D ACM flow past a
   cylinder (convective FD_4th_central, penalisation with cosine smoothing,
   p-norm sponge, adaptation every step with mask thresholding and max-level
@@ -151,6 +154,22 @@ def acm_cyl(ref):
     np.savez_compressed(os.path.join(HERE, "acm_cyl.npz"), **out)
 
 
+def vortex2d_adapt(ref):
+    """TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40: the adaptive 2-D loop
+    (significant refinement, CDF4,0 with coarse extension and security zone)
+    from t=10 to t=15: the ini text and both saved states."""
+    folder = os.path.join(ref, "TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40")
+    out = {}
+    with open(os.path.join(folder, "PARAMS_3vortices.ini"), errors="ignore") as f:
+        out["ini"] = np.array(f.read())
+    for tag, key in [("000010000000", "t10"), ("000015000000", "t15")]:
+        d, u = _fields(folder, ["ux", "uy", "p"], tag)
+        lv, c, u = _sorted(d, u)
+        out.update({f"{key}_level": lv, f"{key}_coords": c, f"{key}_u": u, f"{key}_time": d["time"],
+                    f"{key}_iteration": d["iteration"]})
+    np.savez_compressed(os.path.join(HERE, "vortex2d_adapt.npz"), **out)
+
+
 def h5_files(ref):
     from wabbit_gb300.h5io import H5File
     out = {}
@@ -172,6 +191,7 @@ if __name__ == "__main__":
     tg3d(ref)
     wavelets(ref)
     acm_cyl(ref)
+    vortex2d_adapt(ref)
     h5_files(ref)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
