@@ -91,7 +91,12 @@ typedef struct wg_config {
     /* [Blocks] force_maxlevel_dealiasing: blocks on Jmax are flagged for
      * coarsening (coarseningIndicator_tree.f90:287-293) */
     int    force_maxlevel_dealiasing;
-    int    reserved[12];
+    /* [Blocks] useCoarseExtension (with useSecurityZone): the adaptation
+     * takes the coarse-extension path of the lifted wavelets also for an
+     * unlifted wavelet (ini_file_to_params.f90:543-546: the default is on
+     * for lifted wavelets only); lifted wavelets always take it */
+    int    use_coarse_extension;
+    int    reserved[11];
 } wg_config;
 
 /*
@@ -242,8 +247,9 @@ int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);
  * block count (wg_get_grid returns the new grid). Masks are redrawn from the
  * tree's geometry (wg_set_geometry), else dropped. Needs
  * free arena slots for the mothers (about nblk/(2^d-1)).
- * Unlifted wavelets (CDF X0): the original values are kept (decimation).
- * Lifted wavelets (CDF XY): the reference's coarse-extension algorithm --
+ * Unlifted wavelets (CDF X0) without use_coarse_extension: the original
+ * values are kept (decimation). Lifted wavelets (CDF XY), or any wavelet
+ * with use_coarse_extension: the reference's coarse-extension algorithm --
  * filtered ghost sync, level-by-level FWT of the full tree
  * (wavelet_decompose_full_tree), coarse extension, the indicator on the
  * decomposition, the security zone (addSecurityZone_CE_tree), and the
@@ -254,6 +260,13 @@ int wg_get_time(wg_ctx *ctx, int tree, double *time, double *dt);
 #define WG_ADAPT_THRESHOLD 0
 #define WG_ADAPT_EVERYWHERE 1
 int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *nblk_out);
+/* The refinement status the last adaptation left on the tree's blocks
+ * (lgt_block(:, IDX_REFINE_STS) after adapt_tree): 0 for a block the
+ * indicator (or the security zone) kept, 9 (REF_UNSIGNIFICANT_STAY,
+ * LIB/MODULE/module_globals.f90:28) for a block kept only for completeness,
+ * gradedness or Jmin. Writes min(cap, nblk) values in block order and
+ * returns the block count; WG_EINVAL if the grid changed otherwise since. */
+int wg_get_refinement_status(wg_ctx *ctx, int tree, int cap, int *status);
 /* Phase times of the last lifted adaptation in ms: [0] host planning, [1]
  * ghost syncs, [2] FWT, [3] coarse extension and D2M copies, [4] indicator and
  * security zone, [5] IWT, [6] hvy_tmp block copies, [7] total. enable 1 / 0
@@ -325,6 +338,14 @@ int wg_threshold_flags_noalloc(const wg_config *cfg, int nblk, const double *d_b
  * replaced, at its position, by its 2^d daughters (digit order y, x, z).
  * Ghosts must hold g synced layers. */
 int wg_refine_everywhere(wg_ctx *ctx, int tree);
+/* refine_tree(..., "significant") (LIB/MESH/refine_tree.f90:1-100): the
+ * blocks whose status from the last adaptation is 0 refine (the status
+ * translation of refinementIndicator_tree.f90:152-167), those on Jmax stay
+ * (respectJmaxJmin_tree), and a block next to a finer block that refines
+ * refines as well (ensureGradedness_tree.f90), then refineBlock for them;
+ * the others keep their place. The new block order is that of
+ * wg_refine_everywhere. WG_EINVAL if no adaptation set the status. */
+int wg_refine_significant(wg_ctx *ctx, int tree);
 
 /* ---- measurement -------------------------------------------------------- */
 /* Mean device time (ms) of one launch over reps launches, CUDA events on the

@@ -2145,7 +2145,7 @@ static int adapt_lifted(Oracle &o, const double *eps_use, int everywhere) {
     const Wavelet &w = o.wav;
     const int dim = p.dim, g = p.g, Jmin = p.Jmin;
     const size_t bsz = size_t(o.nc) * o.npts;
-    const bool use_ce = w.lifted || o.ce_force;
+    const bool use_ce = w.lifted || o.ce_force || p.use_coarse_extension;
     bool leaf_first = true;
     for (int d = 0; d < dim; d++)
         if (p.Bs[d] < 3 * std::max(std::abs(w.HD.lo), std::abs(w.HD.hi))) leaf_first = false;
@@ -2597,8 +2597,8 @@ int or_wc_threshold(void *h, double *data, const double *thresh) {
 // otherwise through the full tree; returns the new block count or an error
 int or_adapt(void *h, const double *eps_use, int indicator) {
     Oracle &o = *(Oracle *)h;
-    const int st = o.wav.Y != 0 || o.ce_force ? adapt_lifted(o, eps_use, indicator == 1)
-                                              : adapt_unlifted(o, eps_use, indicator == 1);
+    const int st = o.wav.Y != 0 || o.ce_force || o.cfg.use_coarse_extension ? adapt_lifted(o, eps_use, indicator == 1)
+                                                                            : adapt_unlifted(o, eps_use, indicator == 1);
     return st ? st : (int)o.blocks.size();
 }
 

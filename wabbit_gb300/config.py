@@ -47,7 +47,8 @@ class WgConfig(ctypes.Structure):
         ("rhs_precision", ctypes.c_int),
         ("threshold_mask", ctypes.c_int),
         ("force_maxlevel_dealiasing", ctypes.c_int),
-        ("reserved", ctypes.c_int * 12),
+        ("use_coarse_extension", ctypes.c_int),
+        ("reserved", ctypes.c_int * 11),
     ]
 
     def copy(self) -> "WgConfig":
@@ -215,6 +216,12 @@ def from_ini_text(text: str) -> WgConfig:
     c.tsave_stats = float(ts) if ts else 0.0
     c.threshold_mask = int(float(get("Blocks", "threshold_mask", 0)))
     c.force_maxlevel_dealiasing = int(float(get("Blocks", "force_maxlevel_dealiasing", 0)))
+    # useCoarseExtension / useSecurityZone: on by default for lifted wavelets
+    # only (ini_file_to_params.f90:543-546); either set for an unlifted one
+    # switches the coarse-extension path on
+    ce = get("Blocks", "useCoarseExtension")
+    sz = get("Blocks", "useSecurityZone")
+    c.use_coarse_extension = int(any(v is not None and str(v).strip() not in ("", "0") for v in (ce, sz)))
     return c
 
 

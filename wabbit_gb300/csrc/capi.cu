@@ -208,6 +208,7 @@ struct Tree {
     std::map<long long, std::unique_ptr<SyncPlan>> spare;  // plans of an earlier grid: device buffers to reuse
     double time = 0.0;
     bool shadow_valid = false;         // double-float copy of u_n in B is current
+    std::vector<int> status;           // refinement status the last adaptation left (0 or 9 per block)
     wg_geometry geom{};                // penalisation geometry the masks are drawn from
     bool has_geom = false;             // false: masks are set by the caller (wg_set_mask*)
 };
@@ -1357,6 +1358,7 @@ int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *co
     if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "%s", err.c_str());
     if (!t->forest.graded()) return fail(WG_EGRID, "grid is not graded (level jump > 1 between neighbours)");
     t->slots.resize(nblk);
+    t->status.clear();
     t->mask_slot.assign(nblk, -1);
     t->shadow_valid = false;
     // the lowest free slots in ascending order (contiguous copies)
@@ -2425,13 +2427,14 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     if (e != cudaSuccess) return fail_restore(e, WG_ECUDA);
     // install the new grid
     const int nn = (int)leaves.size();
-    std::vector<int> lv(nn), co(3 * nn), sl(nn);
+    std::vector<int> lv(nn), co(3 * nn), sl(nn), stat(nn);
     std::vector<char> kept(nt, 0);
     for (int i = 0; i < nn; i++) {
         const int b = leaves[i];
         lv[i] = L.ft.level[b];
         for (int a = 0; a < 3; a++) co[3 * i + a] = L.ft.coords[3 * b + a];
         sl[i] = L.slot[b];
+        stat[i] = flags[b];
         kept[b] = 1;
     }
     for (int b = 0; b < nt; b++)
@@ -2442,6 +2445,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "adapt produced an invalid grid: %s", err.c_str());
     if (!t->forest.graded()) return fail(WG_EGRID, "adapt produced a grid that is not graded");
     t->slots = sl;
+    t->status = stat;
     t->mask_slot.assign(nn, -1);
     drop_sync(*t);
     t->shadow_valid = false;
@@ -2476,7 +2480,8 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
         if (st0) return st0;
         eps_use = eps_own.data();
     }
-    if (ctx->wav.lifted) return adapt_lifted(ctx, t, tree, eps_use, indicator == WG_ADAPT_THRESHOLD, nblk_out);
+    if (ctx->wav.lifted || t->cfg.use_coarse_extension)
+        return adapt_lifted(ctx, t, tree, eps_use, indicator == WG_ADAPT_THRESHOLD, nblk_out);
     const int dim = ctx->cfg.dim, nc = ctx->geo.nc, g = ctx->cfg.g;
     const int *Bs = ctx->cfg.Bs;
     const int nb = t->forest.size();
@@ -2558,12 +2563,13 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
     adapt_decide(ft, flags, leaves);
     // install the new grid
     const int nn = (int)leaves.size();
-    std::vector<int> lv(nn), co(3 * nn), sl(nn);
+    std::vector<int> lv(nn), co(3 * nn), sl(nn), stat(nn);
     for (int i = 0; i < nn; i++) {
         const int b = leaves[i];
         lv[i] = ft.level[b];
         for (int a = 0; a < 3; a++) co[3 * i + a] = ft.coords[3 * b + a];
         sl[i] = slot[b];
+        stat[i] = flags[b];
     }
     give_back(leaves);
     for (int m : t->mask_slot)
@@ -2572,6 +2578,7 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
     if (!t->forest.update_neighbors(err)) return fail(WG_EGRID, "adapt produced an invalid grid: %s", err.c_str());
     if (!t->forest.graded()) return fail(WG_EGRID, "adapt produced a grid that is not graded");
     t->slots = sl;
+    t->status = stat;
     t->mask_slot.assign(nn, -1);
     drop_sync(*t);
     t->shadow_valid = false;
@@ -2642,15 +2649,15 @@ static int refine_patches(const wg_config &c, int g, int order, const std::vecto
     return need;
 }
 
-int wg_refine_everywhere(wg_ctx *ctx, int tree) {
-    Tree *t = get_tree(ctx, tree);
-    if (!t) return tree_err();
+// refineBlock for the blocks with refine[b] != 0 (refinementExecute.f90:
+// 4-116): each is replaced, at its position, by its 2^d daughters; the
+// others keep their place and data
+static int refine_blocks(wg_ctx *ctx, Tree *t, int tree, const std::vector<char> &refine) {
     const int dim = ctx->cfg.dim, nd = 1 << dim;
     const int nb = t->forest.size();
-    // blocks on Jmax stay (respectJmaxJmin_tree, LIB/MESH/respectJmaxJmin_tree.f90)
     std::vector<int> ref;
     for (int b = 0; b < nb; b++)
-        if (t->forest.level[b] < t->cfg.Jmax) ref.push_back(b);
+        if (refine[b]) ref.push_back(b);
     const int nr = (int)ref.size();
     if ((size_t)nr * nd > ctx->free_slots.size()) return fail(WG_ENOMEM, "refinement needs %d free slots", nr * nd);
     const int nn = nb + nr * (nd - 1);
@@ -2705,7 +2712,7 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
         if (e != cudaSuccess) {   // the grid is unchanged
             cudaStreamSynchronize(ctx->stream);
             for (int s2 : bases) ctx->free_slots.give(s2);
-            return cuda_fail(e, "wg_refine_everywhere", __FILE__, __LINE__);
+            return cuda_fail(e, "refineBlock", __FILE__, __LINE__);
         }
     }
     // swap the tree onto the new blocks
@@ -2713,6 +2720,7 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     for (int m : t->mask_slot)
         if (m >= 0) ctx->mask_free.push_back(m);
     t->slots = slots;
+    t->status.clear();
     t->mask_slot.assign(nn, -1);
     t->shadow_valid = false;
     drop_sync(*t);
@@ -2726,6 +2734,58 @@ int wg_refine_everywhere(wg_ctx *ctx, int tree) {
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     ctx->grid_version++;
     return WG_OK;
+}
+
+int wg_refine_everywhere(wg_ctx *ctx, int tree) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return tree_err();
+    // blocks on Jmax stay (respectJmaxJmin_tree, LIB/MESH/respectJmaxJmin_tree.f90)
+    std::vector<char> refine(t->forest.size(), 0);
+    for (int b = 0; b < t->forest.size(); b++) refine[b] = t->forest.level[b] < t->cfg.Jmax;
+    return refine_blocks(ctx, t, tree, refine);
+}
+
+int wg_refine_significant(wg_ctx *ctx, int tree) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return tree_err();
+    const int nb = t->forest.size();
+    if ((int)t->status.size() != nb) return fail(WG_EINVAL, "no refinement status: adapt the tree first");
+    // refinementIndicator_tree "significant": 0 -> +1, REF_UNSIGNIFICANT_STAY -> 0
+    std::vector<int> f(nb);
+    for (int b = 0; b < nb; b++) {
+        const int s0 = t->status[b];
+        if (s0 == 1 || s0 == -1) return fail(WG_EINVAL, "refinement status %d on block %d", s0, b);
+        f[b] = s0 == 0 ? 1 : s0 == kFlagUnsignificantStay ? 0 : s0;
+        if (f[b] == 1 && t->forest.level[b] >= t->cfg.Jmax) f[b] = 0;   // respectJmaxJmin_tree
+    }
+    // ensureGradedness_tree: a block next to a finer block that refines refines
+    for (bool changed = true; changed;) {
+        changed = false;
+        for (int b = 0; b < nb; b++) {
+            if (f[b] != 0) continue;
+            for (int r = 0; r < kNumRelations; r++) {
+                const int n = t->forest.nbr[(size_t)b * kNumRelations + r];
+                if (n >= 0 && t->forest.level[n] == t->forest.level[b] + 1 && f[n] == 1) {
+                    f[b] = 1;
+                    changed = true;
+                    break;
+                }
+            }
+        }
+    }
+    std::vector<char> refine(nb, 0);
+    for (int b = 0; b < nb; b++) refine[b] = f[b] == 1;
+    return refine_blocks(ctx, t, tree, refine);
+}
+
+int wg_get_refinement_status(wg_ctx *ctx, int tree, int cap, int *status) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return tree_err();
+    const int nb = t->forest.size();
+    if ((int)t->status.size() != nb) return fail(WG_EINVAL, "no refinement status: adapt the tree first");
+    if (status)
+        for (int b = 0; b < std::min(cap, nb); b++) status[b] = t->status[b];
+    return nb;
 }
 
 // patch table of the tree's ghost sync for inspection: returns the number of

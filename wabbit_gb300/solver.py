@@ -400,6 +400,19 @@ class Forest:
     def refine_everywhere(self):
         capi.check(self.L.wg_refine_everywhere(self.ctx.h, self.tree))
 
+    def refine_significant(self):
+        """refine_tree(..., "significant"): the blocks the last adaptation
+        found significant refine (and, for gradedness, their coarser
+        neighbours)."""
+        capi.check(self.L.wg_refine_significant(self.ctx.h, self.tree))
+
+    def refinement_status(self):
+        """The status the last adaptation left per block (0 or 9)."""
+        n = capi.check(self.L.wg_get_refinement_status(self.ctx.h, self.tree, 0, None))
+        out = np.zeros(n, np.int32)
+        capi.check(self.L.wg_get_refinement_status(self.ctx.h, self.tree, n, _p(out, ctypes.c_int)))
+        return out
+
     def sync_table(self, gminus, gplus, thin=False):
         n = capi.check(self.L.wg_sync_table(self.ctx.h, self.tree, gminus, gplus, 1 if thin else 0, 0, None))
         out = np.zeros((n, 19), np.int32)
