@@ -21,8 +21,8 @@ compare against them:
   (112 blocks, levels 2-5, Bs=32), the reference's refine-everywhere result
   with CDF40 (448 blocks) and its coarsen-everywhere results with CDF40 and
   CDF44.
-* vortex2d_adapt.npz -- TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40: the
-  adaptive 2-D loop (significant refinement, CDF4,0 with coarse extension and
+* vortex2d_adapt.npz -- TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40 and
+  _CDF42: the adaptive 2-D loop (significant refinement, coarse extension and
   security zone): the ini text and the states at t=10 and t=15.
 * acm_cyl.npz -- TESTING/acm/acm_CDF40 and acm_CDF44: 2-D ACM flow past a
   cylinder (convective FD_4th_central, penalisation with cosine smoothing,
@@ -155,18 +155,20 @@ def acm_cyl(ref):
 
 
 def vortex2d_adapt(ref):
-    """TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40: the adaptive 2-D loop
-    (significant refinement, CDF4,0 with coarse extension and security zone)
-    from t=10 to t=15: the ini text and both saved states."""
-    folder = os.path.join(ref, "TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40")
+    """TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40 (and _CDF42): the
+    adaptive 2-D loop (significant refinement, coarse extension and security
+    zone) from t=10 to t=15: the ini text and both saved states; the CDF4,2
+    case's entries carry the prefix CDF42_."""
     out = {}
-    with open(os.path.join(folder, "PARAMS_3vortices.ini"), errors="ignore") as f:
-        out["ini"] = np.array(f.read())
-    for tag, key in [("000010000000", "t10"), ("000015000000", "t15")]:
-        d, u = _fields(folder, ["ux", "uy", "p"], tag)
-        lv, c, u = _sorted(d, u)
-        out.update({f"{key}_level": lv, f"{key}_coords": c, f"{key}_u": u, f"{key}_time": d["time"],
-                    f"{key}_iteration": d["iteration"]})
+    for w, pre in [("CDF40", ""), ("CDF42", "CDF42_")]:
+        folder = os.path.join(ref, f"TESTING/acm/3vortices/3vorticesAdaptFD4_{w}")
+        with open(os.path.join(folder, "PARAMS_3vortices.ini"), errors="ignore") as f:
+            out[pre + "ini"] = np.array(f.read())
+        for tag, key in [("000010000000", "t10"), ("000015000000", "t15")]:
+            d, u = _fields(folder, ["ux", "uy", "p"], tag)
+            lv, c, u = _sorted(d, u)
+            out.update({f"{pre}{key}_level": lv, f"{pre}{key}_coords": c, f"{pre}{key}_u": u,
+                        f"{pre}{key}_time": d["time"], f"{pre}{key}_iteration": d["iteration"]})
     np.savez_compressed(os.path.join(HERE, "vortex2d_adapt.npz"), **out)
 
 

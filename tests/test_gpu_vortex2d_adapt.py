@@ -1,6 +1,7 @@
-"""The library on the reference's adaptive 2-D ACM run
-TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40: CDF4,0 with the coarse
-extension and security zone its ini switches on (use_coarse_extension),
+"""The library on the reference's adaptive 2-D ACM runs
+TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40 and _CDF42: CDF4,0 with the
+coarse extension and security zone its ini switches on
+(use_coarse_extension), or the lifted CDF4,2,
 refinement "significant" (wg_refine_significant on the status the last
 wg_adapt left), one RK4 step per grid, the main loop of
 LIB/MAIN/main.f90:293-427 after the adaptation of the state read at t=10.
@@ -11,6 +12,7 @@ import pytest
 
 from acm_cyl_case import reorder
 from pyoracle import Oracle, interior, pad_blocks
+from test_vortex2d_adapt import load_case
 from wabbit_gb300 import config
 
 pytestmark = pytest.mark.gpu
@@ -62,10 +64,11 @@ def _run_oracle(z, cfg, nit):
     return o.grid(), interior(cfg, o.data()), t, status0
 
 
-def test_adaptive_loop_strict_matches_oracle(golden):
+@pytest.mark.parametrize("wavelet", ["CDF40", "CDF42"])
+def test_adaptive_loop_strict_matches_oracle(golden, wavelet):
     """40 iterations: the same refinement status after the first
     adaptation, the same grids and bit-identical states and times."""
-    z = golden("vortex2d_adapt.npz")
+    z = load_case(golden, wavelet)
     cfg = _cfg(z)
     (glv, gco), u, it, t, s0 = _run_library(z, cfg, nit=40)
     (olv, oco), uo, to, so = _run_oracle(z, cfg, 40)
@@ -79,7 +82,7 @@ def test_adaptive_loop_strict_matches_oracle(golden):
 def test_refine_significant_needs_a_status(golden):
     from wabbit_gb300 import capi
     from wabbit_gb300.solver import Context
-    z = golden("vortex2d_adapt.npz")
+    z = load_case(golden)
     cfg = _cfg(z)
     with Context(cfg, 200) as ctx:
         f = ctx.forest()
@@ -89,10 +92,12 @@ def test_refine_significant_needs_a_status(golden):
 
 
 @pytest.mark.slow
-def test_adaptive_run_t10_to_t15_matches_reference(golden):
-    """The reference's 2281 iterations end on its 61-block grid; the
-    values agree to 1e-13 of the field maximum (the oracle's own agreement)."""
-    z = golden("vortex2d_adapt.npz")
+@pytest.mark.parametrize("wavelet", ["CDF40", "CDF42"])
+def test_adaptive_run_t10_to_t15_matches_reference(golden, wavelet):
+    """The reference's 2281 iterations end on its grid (61 / 58 blocks);
+    the values agree to 1e-13 of the field maximum (the oracle's own
+    agreement)."""
+    z = load_case(golden, wavelet)
     cfg = _cfg(z)
     (glv, gco), u, it, t, _ = _run_library(z, cfg)
     assert it == int(z["t15_iteration"] - z["t10_iteration"]) and t == float(z["t15_time"])
