@@ -342,6 +342,11 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
                      (ix + a.gun.gb);
         const df2 third = {a.third[0], a.third[1]};
         float2 *const ob = a.out;
+        // the point in the compact arrays cout / nin (their component stride)
+        const int nint = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
+        const long long cbase = a.cout || a.nin ? (long long)a.cpos[b] * (DIM + 1) * nint +
+                                                      ((DIM == 3 ? iz * a.Bs1 : 0) + iy) * a.Bs0 + ix
+                                                : 0;
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
             const double u = f2_bits(in.c[c]);
@@ -353,9 +358,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
             const df2 sum = df_sub_nr({sh, sl}, df_pow2(ud, 4.f));
             const df2 inc = df_norm(df_add_nr(df_mul_nr(third, sum), df_mul_nr(k.db, df_norm(r[c]))));
             const double v = __dadd_rn(u, df_to_double(inc));
-            const long long ci = ((long long)(a.cout || a.nin ? a.cpos[b] : 0) * (DIM + 1) + c) * a.Bs0 * a.Bs1 *
-                                     (DIM == 3 ? a.Bs2 : 1) +
-                                 ((DIM == 3 ? iz * a.Bs1 : 0) + iy) * a.Bs0 + ix;
+            const long long ci = cbase + (long long)c * nint;
             if (a.cout) a.cout[ci] = v;
             if (a.nin) {   // the next input takes the place of u_n+1 in the state and its copy
                 const double x = __ldcs(a.nin + ci);
