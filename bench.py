@@ -78,7 +78,8 @@ def parse():
     ap.add_argument("--adapt-every", type=int, default=5,
                     help="serving: adaptation cycle length in steps (0: no adaptation)")
     ap.add_argument("--stage-form", default="auto",
-                    help="FP32-pipe stage kernel form: auto (timed per RK stage), direct, tile, march, pipe, or four "
+                    help="FP32-pipe stage kernel form: auto (timed per RK stage), direct, tile, march, pipe, tile2, "
+                         "tile8, or four "
                          "comma-separated forms for RK stages 1-4")
     ap.add_argument("--traffic", choices=["auto", "off"], default="auto",
                     help="measure the stage kernels' DRAM bytes with a one-pass ncu capture (dram__bytes_read/"
@@ -245,7 +246,7 @@ def measure_traffic(args, forms):
         return None, "ncu not found"
     log = tempfile.NamedTemporaryFile(prefix="traffic", suffix=".csv", delete=False).name
     # launches per RK stage: unmasked and masked blocks, or one (pipe form)
-    per = [1 if fm == "pipe" else 2 for fm in forms]
+    per = [1 if fm == "pipe" else 2 for fm in forms]   # launches per RK stage
     ncmd = [ncu, "--metrics", "dram__bytes_read.sum,dram__bytes_write.sum", "--clock-control", "none",
             "-k", "regex:acm_stage_df", "-c", str(sum(per)), "--csv", "--print-units", "base", "--log-file", log] + cmd
     try:
@@ -451,7 +452,8 @@ def run_ours(args, rank, world):
     form = ctx.stage_forms() if cfg.rhs_precision else ["direct"] * 4
     kname = {"direct": "acm_stage_df_kernel", "tile": "acm_stage_df_tile (TMA slabs)",
              "march": "acm_stage_df_march (TMA plane ring)",
-             "pipe": "acm_stage_df_pipe (persistent TMA slab pipeline)"}
+             "pipe": "acm_stage_df_pipe (persistent TMA slab pipeline)",
+             "tile2": "acm_stage_df_tile<2> (TMA slabs of 2 planes)", "tile8": "acm_stage_df_tile<8> (TMA slabs of 8 planes)"}
     stage_kernel = ("acm_stage_kernel (FP64)" if cfg.rhs_precision == 0 else
                     ", ".join(kname[x] for x in dict.fromkeys(form)))
     traffic, traffic_src = None, "not measured (--traffic off)"

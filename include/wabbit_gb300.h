@@ -156,8 +156,9 @@ int wg_set_variant(wg_ctx *ctx, int fast);
  * memory by TMA (3-D, 16x16 planes, g_rhs = 2); WG_FORM_MARCH walks a whole
  * 16^3 block through a ring of 5 planes loaded by TMA; WG_FORM_PIPE is the
  * tile form as a persistent kernel (one CTA per SM walking its slabs with
- * two slab buffers, the next slab loading while one is computed). The forms
- * compute the same bits. wg_get_stage_form
+ * two slab buffers, the next slab loading while one is computed);
+ * WG_FORM_TILE2 / WG_FORM_TILE8 are the tile form with slabs of 2 / 8
+ * planes. The forms compute the same bits. wg_get_stage_form
  * returns the form of stage 2, wg_get_stage_forms the forms of stages 1-4
  * (the autotuner's choices once it has run). */
 #define WG_FORM_AUTO 0
@@ -165,10 +166,12 @@ int wg_set_variant(wg_ctx *ctx, int fast);
 #define WG_FORM_TILE 2
 #define WG_FORM_MARCH 3
 #define WG_FORM_PIPE 4
+#define WG_FORM_TILE2 5   /* the tile form with slabs of 2 interior planes  */
+#define WG_FORM_TILE8 6   /* ... of 8 interior planes (Bs2 a multiple of 8)  */
 int wg_set_stage_form(wg_ctx *ctx, int form);
 int wg_get_stage_form(wg_ctx *ctx, int *form);
 int wg_get_stage_forms(wg_ctx *ctx, int *forms);
-/* Fixes the forms of RK stages 1-4 (each WG_FORM_DIRECT, _TILE, _MARCH or _PIPE),
+/* Fixes the forms of RK stages 1-4 (each WG_FORM_DIRECT, _TILE, _MARCH, _PIPE, _TILE2 or _TILE8),
  * e.g. to reuse the autotuner's choice of one context in another. */
 int wg_set_stage_forms(wg_ctx *ctx, const int *forms);
 int wg_synchronize(wg_ctx *ctx);

@@ -276,8 +276,9 @@ def test_fp32_pipe_stage_forms_bit_identical():
     data = smooth_state(cfg, lv, co, 31)
     mask = sphere_mask(cfg, lv, co, [0.5, 0.6, 0.7], 0.3)
     out = []
-    for forms in (["direct"] * 4, ["tile"] * 4, ["march"] * 4, ["pipe"] * 4, ["march", "tile", "direct", "march"],
-                  ["pipe", "direct", "tile", "pipe"]):
+    for forms in (["direct"] * 4, ["tile"] * 4, ["march"] * 4, ["pipe"] * 4, ["tile2"] * 4, ["tile8"] * 4,
+                  ["march", "tile", "direct", "march"], ["pipe", "direct", "tile", "pipe"],
+                  ["tile2", "tile8", "pipe", "tile8"]):
         with Context(cfg, len(lv) + 4) as ctx:
             ctx.set_stage_forms(forms)
             f = ctx.forest()
@@ -301,7 +302,7 @@ def test_fp32_pipe_rejects_skew_symmetric():
         Context(cfg, 8)
 
 
-@pytest.mark.parametrize("form", ["direct", "tile", "march", "pipe", "auto"])
+@pytest.mark.parametrize("form", ["direct", "tile", "march", "pipe", "tile2", "tile8", "auto"])
 def test_fp32_pipe_stage_forms_16cubed(form):
     """3-D 16^3 blocks (the benchmark geometry): the direct-load stage
     kernel, the TMA-staged slab, plane-ring and persistent slab kernels, and the autotuner's
@@ -334,5 +335,6 @@ def test_fp32_pipe_stage_forms_16cubed(form):
             assert err < 1e-12, (form, step, err)
         forms = ctx.stage_forms()
         assert len(forms) == 4
-        assert all(x in (("direct", "tile", "march", "pipe") if form == "auto" else (form,)) for x in forms)
+        assert all(x in (("direct", "tile", "march", "pipe", "tile2", "tile8") if form == "auto" else (form,))
+                   for x in forms)
         assert ctx.stage_form() == forms[1]

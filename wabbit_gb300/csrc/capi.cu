@@ -231,7 +231,8 @@ struct wg_ctx {
     std::vector<int> h_push;
     CUtensorMap tm[4];                  // TMA maps over B, C, D, E (3-D FP32-pipe precision): slab boxes
     CUtensorMap tp[4];                  // ... one-plane boxes (march form)
-    bool have_tm = false, have_march = false;
+    CUtensorMap tm2[4], tm8[4];         // ... slab boxes of 2 and 8 interior planes (tile2, tile8 forms)
+    bool have_tm = false, have_march = false, have_slabs28 = false;
     int stage_form = WG_FORM_AUTO;      // requested form of the FP32-pipe stage kernel
     int tuned[4] = {0, 0, 0, 0};        // the autotuner's choice per RK stage (0: not tuned yet)
     // step profile (wg_step_profile): events recorded between the kernel
@@ -706,8 +707,8 @@ int stage_launch(wg_ctx *ctx, Tree &t, int stage, const double *in, BufGeo gin, 
 }
 
 // the TMA map over a thin stage buffer (slab or one-plane boxes)
-static const void *in_map(wg_ctx *ctx, const double *in, bool plane) {
-    const CUtensorMap *m = plane ? ctx->tp : ctx->tm;
+static const void *in_map(wg_ctx *ctx, const double *in, bool plane, int slab = 4) {
+    const CUtensorMap *m = plane ? ctx->tp : slab == 2 ? ctx->tm2 : slab == 8 ? ctx->tm8 : ctx->tm;
     return in == ctx->B ? &m[0] : in == ctx->C ? &m[1] : in == ctx->D ? &m[2] : in == ctx->E ? &m[3] : nullptr;
 }
 
@@ -730,6 +731,10 @@ static void form_args(wg_ctx *ctx, int stage, const double *in, const void **tm,
     if (form == WG_FORM_PIPE && ctx->have_tm) {
         *tm = in_map(ctx, in, false);
         *march = 2;
+    }
+    if ((form == WG_FORM_TILE2 || form == WG_FORM_TILE8) && ctx->have_tm) {
+        *tm = in_map(ctx, in, false, form == WG_FORM_TILE2 ? 2 : 8);
+        *march = form == WG_FORM_TILE2 ? 3 : 4;
     }
 }
 
@@ -789,19 +794,26 @@ int make_tensor_maps(wg_ctx *ctx) {
     const cuuint64_t strides[2] = {(cuuint64_t)g.nx * 8, (cuuint64_t)g.nx * g.ny * 8};
     const cuuint32_t box[3] = {(cuuint32_t)g.nx, (cuuint32_t)g.ny, (cuuint32_t)(zt + 4)};
     const cuuint32_t pbox[3] = {(cuuint32_t)g.nx, (cuuint32_t)g.ny, 1};
+    const cuuint32_t box2[3] = {(cuuint32_t)g.nx, (cuuint32_t)g.ny, 6};
+    const cuuint32_t box8[3] = {(cuuint32_t)g.nx, (cuuint32_t)g.ny, 12};
     const cuuint32_t estr[3] = {1, 1, 1};
     double *bufs[4] = {ctx->B, ctx->C, ctx->D, ctx->E};
     const bool march = ctx->cfg.Bs[2] == 16;   // the march kernel walks 16 planes
+    const bool slabs28 = ctx->cfg.Bs[2] % 8 == 0;   // slab heights 2 and 8 divide the block
     for (int i = 0; i < 4; i++) {
-        for (int k = 0; k < (march ? 2 : 1); k++) {
-            const CUresult r = reinterpret_cast<Encode>(fn)(k ? &ctx->tp[i] : &ctx->tm[i], CU_TENSOR_MAP_DATA_TYPE_UINT64,
-                                                            3, bufs[i], dims, strides, k ? pbox : box, estr,
-                                                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        for (int k = 0; k < 4; k++) {
+            if ((k == 1 && !march) || (k >= 2 && !slabs28)) continue;
+            CUtensorMap *dst = k == 0 ? &ctx->tm[i] : k == 1 ? &ctx->tp[i] : k == 2 ? &ctx->tm2[i] : &ctx->tm8[i];
+            const cuuint32_t *bx = k == 0 ? box : k == 1 ? pbox : k == 2 ? box2 : box8;
+            const CUresult r = reinterpret_cast<Encode>(fn)(dst, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, bufs[i], dims,
+                                                            strides, bx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                                            CU_TENSOR_MAP_SWIZZLE_NONE,
                                                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                                             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
             if (r != CUDA_SUCCESS) return fail(WG_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
         }
     }
+    ctx->have_slabs28 = slabs28;
     ctx->have_tm = true;
     ctx->have_march = march;
     return WG_OK;
@@ -862,6 +874,10 @@ int autotune_stage_form(wg_ctx *ctx, Tree &t) {
     if (ctx->have_tm && !t.slots.empty()) forms.push_back(WG_FORM_TILE);
     if (ctx->have_march && !t.slots.empty()) forms.push_back(WG_FORM_MARCH);
     if (ctx->have_tm && !t.slots.empty()) forms.push_back(WG_FORM_PIPE);
+    if (ctx->have_slabs28 && !t.slots.empty()) {
+        forms.push_back(WG_FORM_TILE2);
+        forms.push_back(WG_FORM_TILE8);
+    }
     if (forms.size() == 1) {
         for (int &f : ctx->tuned) f = WG_FORM_DIRECT;
         return WG_OK;
@@ -1927,9 +1943,9 @@ int wg_wavelet_threshold(wg_ctx *ctx, int tree, const double *thresh) {
 
 int wg_set_stage_form(wg_ctx *ctx, int form) {
     if (!ctx) return fail(WG_EINVAL, "null ctx");
-    if (form != WG_FORM_AUTO && form != WG_FORM_DIRECT && form != WG_FORM_TILE && form != WG_FORM_MARCH &&
-        form != WG_FORM_PIPE)
-        return fail(WG_EINVAL, "unknown stage form %d", form);
+    if (form < WG_FORM_AUTO || form > WG_FORM_TILE8) return fail(WG_EINVAL, "unknown stage form %d", form);
+    if ((form == WG_FORM_TILE2 || form == WG_FORM_TILE8) && !ctx->have_slabs28)
+        return fail(WG_ENOTSUP, "slabs of 2 and 8 planes need the tile form and Bs2 a multiple of 8");
     if ((form == WG_FORM_TILE || form == WG_FORM_PIPE) && !ctx->have_tm)
         return fail(WG_ENOTSUP, "the tile and pipe forms need 3-D 16x16 planes, g_rhs = 2 and the FP32-pipe precision");
     if (form == WG_FORM_MARCH && !ctx->have_march)
@@ -1943,10 +1959,11 @@ int wg_set_stage_form(wg_ctx *ctx, int form) {
 int wg_set_stage_forms(wg_ctx *ctx, const int *forms) {
     if (!ctx || !forms) return fail(WG_EINVAL, "bad arguments");
     for (int k = 0; k < 4; k++) {
-        if (forms[k] != WG_FORM_DIRECT && forms[k] != WG_FORM_TILE && forms[k] != WG_FORM_MARCH &&
-            forms[k] != WG_FORM_PIPE)
-            return fail(WG_EINVAL, "stage %d: form %d is not direct, tile, march or pipe", k + 1, forms[k]);
+        if (forms[k] < WG_FORM_DIRECT || forms[k] > WG_FORM_TILE8)
+            return fail(WG_EINVAL, "stage %d: form %d is not direct, tile, march, pipe, tile2 or tile8", k + 1,
+                        forms[k]);
         if (((forms[k] == WG_FORM_TILE || forms[k] == WG_FORM_PIPE) && !ctx->have_tm) ||
+            ((forms[k] == WG_FORM_TILE2 || forms[k] == WG_FORM_TILE8) && !ctx->have_slabs28) ||
             (forms[k] == WG_FORM_MARCH && !ctx->have_march))
             return fail(WG_ENOTSUP, "stage %d: form %d does not apply to this configuration", k + 1, forms[k]);
     }

@@ -139,7 +139,8 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
                                 cudaStream_t s, int keep_state = 1, double *cout = nullptr,
                                 const int *cpos = nullptr, const double *nin = nullptr);
-// (march 0: tmap is a slab map and the tile kernel runs; 1: tmap is a map
+// (march 0, 3, 4: tmap is a slab map of 4, 2 or 8 interior planes and the
+// tile kernel of that slab height runs; 1: tmap is a map
 // with one-plane boxes and the whole-block ring kernel runs; 2: tmap is a
 // slab map and the persistent double-buffered slab kernel runs over masked
 // and unmasked blocks at once, masked then being the number of masked blocks

@@ -446,7 +446,8 @@ __global__ void __launch_bounds__(256, 3) acm_stage_df_kernel(StageArgsDF a) {
 
 // 3-D blocks of 16x16xBs2 points with 2 ghost layers (the stage-input
 // layout of FD_4th_central): each CTA of 256 threads takes a slab of ZT
-// interior planes of one block. One elected thread loads the slab's stencil
+// interior planes of one block (ZT = 2, 4 or 8: 76.8, 102.4 or 153.6 KB of
+// shared memory). One elected thread loads the slab's stencil
 // input (ZT+4 planes of 20x20 points per component, ghosts included) with
 // one TMA box per component into shared memory; every thread then walks its
 // (x, y) column through the slab, reading all stencil values from shared
@@ -780,17 +781,29 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
         kern<<<(unsigned)nblk, 256, smem, s>>>(a, map, err);
         return cudaGetLastError();
     }
-    if (zt == 4 && gt.nx == 20 && gt.ny == 20) {
-        const int nslab = Bs2 / zt;
-        const size_t smem = sizeof(float2) * 4 * (size_t)(zt + 4) * gt.nx * gt.ny;
+    if ((march == 0 || march == 3 || march == 4) && zt == 4 && gt.nx == 20 && gt.ny == 20) {
+        // slab height: 4 (march 0), 2 (march 3) or 8 (march 4) interior
+        // planes per CTA; tmap's boxes hold that height plus four ghost planes
+        const int z = march == 3 ? 2 : march == 4 ? 8 : 4;
+        if (Bs2 % z) return cudaErrorInvalidValue;
+        const int nslab = Bs2 / z;
+        const size_t smem = sizeof(float2) * 4 * (size_t)(z + 4) * gt.nx * gt.ny;
         const CUtensorMap &map = *reinterpret_cast<const CUtensorMap *>(tmap);
         using K = void (*)(StageArgsDF, const CUtensorMap, int, int *);
-        static const K kerns[2][4] = {
-            {acm_stage_df_tile<4, 1, false>, acm_stage_df_tile<4, 2, false>, acm_stage_df_tile<4, 3, false>,
-             acm_stage_df_tile<4, 4, false>},
-            {acm_stage_df_tile<4, 1, true>, acm_stage_df_tile<4, 2, true>, acm_stage_df_tile<4, 3, true>,
-             acm_stage_df_tile<4, 4, true>}};
-        const K kern = kerns[masked ? 1 : 0][stage - 1];
+        static const K kerns[3][2][4] = {
+            {{acm_stage_df_tile<4, 1, false>, acm_stage_df_tile<4, 2, false>, acm_stage_df_tile<4, 3, false>,
+              acm_stage_df_tile<4, 4, false>},
+             {acm_stage_df_tile<4, 1, true>, acm_stage_df_tile<4, 2, true>, acm_stage_df_tile<4, 3, true>,
+              acm_stage_df_tile<4, 4, true>}},
+            {{acm_stage_df_tile<2, 1, false>, acm_stage_df_tile<2, 2, false>, acm_stage_df_tile<2, 3, false>,
+              acm_stage_df_tile<2, 4, false>},
+             {acm_stage_df_tile<2, 1, true>, acm_stage_df_tile<2, 2, true>, acm_stage_df_tile<2, 3, true>,
+              acm_stage_df_tile<2, 4, true>}},
+            {{acm_stage_df_tile<8, 1, false>, acm_stage_df_tile<8, 2, false>, acm_stage_df_tile<8, 3, false>,
+              acm_stage_df_tile<8, 4, false>},
+             {acm_stage_df_tile<8, 1, true>, acm_stage_df_tile<8, 2, true>, acm_stage_df_tile<8, 3, true>,
+              acm_stage_df_tile<8, 4, true>}}};
+        const K kern = kerns[march == 3 ? 1 : march == 4 ? 2 : 0][masked ? 1 : 0][stage - 1];
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         a.chunks = 0;

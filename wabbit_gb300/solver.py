@@ -61,7 +61,7 @@ class Context:
     def set_variant(self, fast: bool):
         capi.check(self.L.wg_set_variant(self.h, 1 if fast else 0))
 
-    FORMS = {"auto": 0, "direct": 1, "tile": 2, "march": 3, "pipe": 4}
+    FORMS = {"auto": 0, "direct": 1, "tile": 2, "march": 3, "pipe": 4, "tile2": 5, "tile8": 6}
 
     def set_stage_form(self, form: str):
         """Form of the FP32-pipe stage kernel: auto (each RK stage timed in
