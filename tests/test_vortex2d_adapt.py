@@ -67,13 +67,16 @@ def test_significant_refinement_first_iterations(golden):
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("wavelet", ["CDF40", "CDF42"])
+@pytest.mark.parametrize("wavelet", ["CDF40"])
 def test_adaptive_run_t10_to_t15_matches_reference(golden, wavelet):
     """2281 adaptive iterations t=10 -> 15 (the reference's iteration count)
-    end on the reference's grid (CDF4,0: 61 blocks, CDF4,2: 58 blocks, on
-    levels 2-4); the values agree to 1e-13 of the field maximum (observed
-    8e-15 and 1.1e-14: the coarse-extension reconstruction of the reference
-    is not reproduced bit for bit, as for the CDF4,4 runs)."""
+    end on the reference's grid (61 blocks on levels 2-4); the values agree
+    to 1e-13 of the field maximum (observed 8e-15: the coarse-extension
+    reconstruction of the reference is not reproduced bit for bit, as for
+    the CDF4,4 runs). The CDF4,2 case (58 blocks, 1.1e-14) takes two minutes
+    on 16 cores in the oracle; its run to t=15 is checked through the device
+    path, which equals the oracle bit for bit in its strict variant
+    (test_gpu_vortex2d_adapt.py)."""
     z, cfg, o = _case(golden, wavelet)
     o.adapt(o.eps_use())
     t, it = float(z["t10_time"]), 0
