@@ -270,6 +270,11 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
  * gradedness or Jmin. Writes min(cap, nblk) values in block order and
  * returns the block count; WG_EINVAL if the grid changed otherwise since. */
 int wg_get_refinement_status(wg_ctx *ctx, int tree, int cap, int *status);
+/* Sets that status for the tree's current blocks (nblk values in block
+ * order), as a run restarted from a field file reads it with its grid
+ * (readHDF5vct_tree(..., read_refinement_status), LIB/MESH/InputOutput.f90:
+ * 322); each value must be 0 or 9. */
+int wg_set_refinement_status(wg_ctx *ctx, int tree, int nblk, const int *status);
 /* Phase times of the last lifted adaptation in ms: [0] host planning, [1]
  * ghost syncs, [2] FWT, [3] coarse extension and D2M copies, [4] indicator and
  * security zone, [5] IWT, [6] hvy_tmp block copies, [7] total. enable 1 / 0

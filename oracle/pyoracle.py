@@ -63,6 +63,7 @@ def lib():
         L.or_refine_significant.argtypes = [ctypes.c_void_p]
         L.or_set_coarse_extension.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.or_status.argtypes = [ctypes.c_void_p, _ip]
+        L.or_set_status.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip]
         L.or_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _dp]
         L.or_adapt_full_tree.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.or_run.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
@@ -303,6 +304,12 @@ class Oracle:
         if n:
             self.L.or_status(self.h, _p(out, ctypes.c_int))
         return out
+
+    def set_status(self, st):
+        """The leaves' refinement status (as read from a field file)."""
+        st = np.ascontiguousarray(st, np.int32)
+        if self.L.or_set_status(self.h, len(st), _p(st, ctypes.c_int)) != 0:
+            raise RuntimeError("or_set_status: wrong length")
 
     def set_coarse_extension(self, on=True):
         """useCoarseExtension and useSecurityZone for any wavelet."""

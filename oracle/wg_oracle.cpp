@@ -2663,6 +2663,15 @@ int or_status(void *h, int *out) {
     return (int)o.status.size();
 }
 
+// the leaves' status as a restarted run reads it from its field file
+// (readHDF5vct_tree with read_refinement_status, InputOutput.f90:322)
+int or_set_status(void *h, int n, const int *st) {
+    Oracle &o = *(Oracle *)h;
+    if (n != (int)o.blocks.size()) return WG_EINVAL;
+    o.status.assign(st, st + n);
+    return WG_OK;
+}
+
 // useCoarseExtension and useSecurityZone for any wavelet (on != 0)
 int or_set_coarse_extension(void *h, int on) {
     ((Oracle *)h)->ce_force = on != 0;

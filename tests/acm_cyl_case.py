@@ -19,6 +19,12 @@ class Case:
         ini = str(self.z["ini"])
         self.cfg = config.from_ini_text(ini)
         self.geo = config.geometry_from_ini_text(ini, self.cfg)
+        kv = config._parse_ini(ini)
+        # refine_tree's indicator of the main loop (main.f90:309-330)
+        self.significant = kv.get(("Blocks", "refinement_indicator"), "everywhere").strip() == "significant"
+
+    def status(self, key):
+        return self.z[f"{key}_status"]
 
     def grid(self, key):
         return self.z[f"{key}_level"], self.z[f"{key}_coords"]
@@ -53,10 +59,15 @@ def run_oracle(case, tend, threads=1):
     lv, co = case.grid("t0")
     o.set_grid(lv, co, pad_blocks(cfg, case.state("t0")))
     o.set_geometry(case.geo)
+    if case.significant:   # the status the initial adaptation left, saved with the t=0 state
+        o.set_status(case.status("t0"))
     t, it = 0.0, 0
     while t < tend - 1e-12:
         o.sync(cfg.g, cfg.g, ignore_filter=True)
-        o.refine_everywhere()
+        if case.significant:
+            o.refine_significant()
+        else:
+            o.refine_everywhere()
         o.make_mask()
         t, _ = o.step(t)
         o.adapt(o.eps_use())
@@ -81,10 +92,15 @@ def run_library(case, tend, fast=False, precision=0, max_blocks=1200):
         f.upload(pad_blocks(cfg, case.state("t0")))
         f.set_geometry(case.geo)
         f.set_time(0.0)
+        if case.significant:
+            f.set_refinement_status(case.status("t0"))
         t, it = 0.0, 0
         while t < tend - 1e-12:
             f.sync_ghosts_tree()
-            f.refine_everywhere()
+            if case.significant:
+                f.refine_significant()
+            else:
+                f.refine_everywhere()
             t, _ = f.timeStep_tree()
             f.adapt()
             it += 1

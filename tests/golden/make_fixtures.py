@@ -24,13 +24,15 @@ compare against them:
 * vortex2d_adapt.npz -- TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40 and
   _CDF42: the adaptive 2-D loop (significant refinement, coarse extension and
   security zone): the ini text and the states at t=10 and t=15.
-* acm_cyl.npz -- TESTING/acm/acm_CDF40 and acm_CDF44: 2-D ACM flow past a
-  cylinder (convective FD_4th_central, penalisation with cosine smoothing,
-  p-norm sponge, adaptation every step with mask thresholding and max-level
-  dealiasing, Bs=26, Jmax=6): the text of acm_cyl.ini, the state at t=0
-  (input), 0.05 and 0.1 (outputs) with their iteration counts, and the
-  saved mask (chi) on the t=0, 0.05 and 0.1 grids. Each case is stored under
-  the prefix "CDF40_" / "CDF44_".
+* acm_cyl.npz -- TESTING/acm/acm_CDF40, acm_CDF44, acm_significant_CDF44
+  and acm_norm_CDF44: 2-D ACM flow past a cylinder (convective
+  FD_4th_central, penalisation with cosine smoothing, p-norm sponge,
+  adaptation every step with mask thresholding and max-level dealiasing,
+  Bs=26): the text of acm_cyl.ini, the state at t=0 (input) and the saved
+  outputs (t=0.05 and 0.1 for Jmax=6; t=0.2 for the Jmax=5 variants with
+  refinement "significant" and with the vector-group norm 2 2 1) with their
+  iteration counts, refinement status and saved mask (chi). Each case is
+  stored under the prefix "CDF40_" / "CDF44_" / "SIG44_" / "NORM44_".
 
 * h5_files.npz -- every dataset and every attribute of two field files as
   the reference's saveHDF5_tree wrote them (2-D: acm_CDF40/mask_000000000000
@@ -136,21 +138,35 @@ def wavelets(ref):
     np.savez_compressed(os.path.join(HERE, "wavelet_adaptive.npz"), **out)
 
 
+def _status(folder, tag, d):
+    """The refinement_status dataset of a field file, in the order _sorted
+    gives its blocks."""
+    from wabbit_gb300.h5io import H5File
+    st = H5File(os.path.join(folder, f"ux_{tag}.h5")).read("refinement_status").astype(np.int32)
+    c = _coords3(d)
+    return st[np.lexsort((c[:, 0], c[:, 1], c[:, 2], d["level"]))]
+
+
 def acm_cyl(ref):
     out = {}
-    for w in ["CDF40", "CDF44"]:
-        folder = os.path.join(ref, "TESTING/acm", f"acm_{w}")
+    cases = [("CDF40", "acm_CDF40", [("000000000000", "t0"), ("000000050000", "t1"), ("000000100000", "t2")]),
+             ("CDF44", "acm_CDF44", [("000000000000", "t0"), ("000000050000", "t1"), ("000000100000", "t2")]),
+             ("SIG44", "acm_significant_CDF44", [("000000000000", "t0"), ("000000200000", "t2")]),
+             ("NORM44", "acm_norm_CDF44", [("000000000000", "t0"), ("000000200000", "t2")])]
+    for w, sub, tags in cases:
+        folder = os.path.join(ref, "TESTING/acm", sub)
         with open(os.path.join(folder, "acm_cyl.ini"), errors="ignore") as f:
             out[f"{w}_ini"] = np.array(f.read())
-        for tag, key in [("000000000000", "t0"), ("000000050000", "t1"), ("000000100000", "t2")]:
+        for tag, key in tags:
             d, u = _fields(folder, ["ux", "uy", "p"], tag)
+            st = _status(folder, tag, d)
             lv, c, u = _sorted(d, u)
             dm = read_wabbit(os.path.join(folder, f"mask_{tag}.h5"))
             lvm, cm, m = _sorted(dm, _interior(dm)[:, None])
             assert np.array_equal(lv, lvm) and np.array_equal(c, cm)
             out.update({f"{w}_{key}_level": lv, f"{w}_{key}_coords": c, f"{w}_{key}_u": u,
                         f"{w}_{key}_chi": m[:, 0], f"{w}_{key}_time": d["time"],
-                        f"{w}_{key}_iteration": d["iteration"]})
+                        f"{w}_{key}_iteration": d["iteration"], f"{w}_{key}_status": st})
     np.savez_compressed(os.path.join(HERE, "acm_cyl.npz"), **out)
 
 

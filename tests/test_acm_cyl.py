@@ -76,6 +76,28 @@ def test_cdf44_run_matches_reference(golden):
     assert np.abs(u - ref).max() <= 1e-13 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("w", ["SIG44", "NORM44"])
+def test_jmax5_variants_match_reference(golden, w):
+    """The reference's Jmax=5 cylinder variants with CDF4,4, 151 iterations
+    to t=0.2: acm_significant_CDF44 (refinement "significant" from the
+    status saved with the t=0 state) and acm_norm_CDF44 (threshold
+    components 2 2 1: the velocity components share one detail, their
+    maximum). Grid identical (112 blocks), values within 1e-13 of the
+    maximum (observed 2.6e-14, as for the other CDF4,4 runs)."""
+    c = Case(golden, w)
+    assert c.significant == (w == "SIG44")
+    o, it, t = run_oracle(c, float(c.z["t2_time"]), threads())
+    assert it == c.iteration("t2") and t == float(c.z["t2_time"])
+    lv, co = o.grid()
+    perm = reorder(*c.grid("t2"), lv, co)
+    assert perm is not None, "adapted grid differs from the reference's"
+    u = interior(c.cfg, o.data())[perm].reshape(c.state("t2").shape)
+    ref = c.state("t2")
+    assert np.abs(u - ref).max() <= 1e-13 * np.abs(ref).max()
+    if c.significant:
+        assert np.array_equal(np.sort(o.status()), np.sort(c.status("t2")))
+
+
 def test_divergence_guard_in_oracle(golden):
     """|u| > 1e12 anywhere stops the RHS (rhs_ACM.f90:133-146)."""
     from pyoracle import pad_blocks

@@ -54,6 +54,26 @@ def test_cylinder_run_strict_matches_oracle_and_reference_grid(golden, w):
     assert np.abs(u[perm].reshape(ref.shape) - ref).max() <= 1e-13 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("w", ["SIG44", "NORM44"])
+def test_jmax5_variants_strict_match_oracle_and_reference(golden, w):
+    """acm_significant_CDF44 (wg_refine_significant from the status set with
+    the t=0 state) and acm_norm_CDF44 (threshold components 2 2 1), 151
+    iterations to t=0.2: the strict variant equals the oracle bit for bit
+    and ends on the reference's grid."""
+    c = Case(golden, w)
+    tend = float(c.z["t2_time"])
+    (glv, gco), u, it, t = run_library(c, tend, fast=False)
+    (olv, oco), uo, ito, to = oracle_result(c, tend)
+    assert it == ito == c.iteration("t2") and t == to == tend
+    perm = reorder(olv, oco, glv, gco)
+    assert perm is not None, "library grid differs from the oracle's"
+    assert np.array_equal(u[perm], uo), "strict state differs from the oracle"
+    perm = reorder(*c.grid("t2"), glv, gco)
+    assert perm is not None, "library grid differs from the reference's"
+    ref = c.state("t2")
+    assert np.abs(u[perm].reshape(ref.shape) - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
 def test_cylinder_run_fast_variant(golden):
     c = Case(golden, "CDF40")
     (glv, gco), u, it, _ = run_library(c, 0.05, fast=True)

@@ -32,6 +32,7 @@ EXPORTS = [
     "wg_wavelet_decompose", "wg_wavelet_reconstruct", "wg_wavelet_threshold", "wg_threshold_flags_wd",
     "wg_adapt", "wg_adapt_profile", "wg_rk4_stream", "wg_set_geometry", "wg_get_stage_forms",
     "wg_step_profile", "wg_set_stage_forms", "wg_refine_significant", "wg_get_refinement_status",
+    "wg_set_refinement_status",
 ]
 
 
@@ -86,6 +87,7 @@ _SIGS = {
     "wg_refine_everywhere": (_i, [_vp, _i]),
     "wg_refine_significant": (_i, [_vp, _i]),
     "wg_get_refinement_status": (_i, [_vp, _i, _i, _ip]),
+    "wg_set_refinement_status": (_i, [_vp, _i, _i, _ip]),
     "wg_sync_table": (_i, [_vp, _i, _i, _i, _i, _i, _ip]),
     "wg_block_slot": (_i, [_vp, _i, _i]),
     "wg_sync_table_host": (_i, [ctypes.POINTER(WgConfig), _i, _ip, _ip, _i, _i, _i, _i, _ip]),

@@ -2795,6 +2795,17 @@ int wg_refine_significant(wg_ctx *ctx, int tree) {
     return refine_blocks(ctx, t, tree, refine);
 }
 
+int wg_set_refinement_status(wg_ctx *ctx, int tree, int nblk, const int *status) {
+    Tree *t = get_tree(ctx, tree);
+    if (!t) return tree_err();
+    if (nblk != t->forest.size() || (nblk && !status)) return fail(WG_EINVAL, "status of %d blocks expected", t->forest.size());
+    for (int b = 0; b < nblk; b++)
+        if (status[b] != 0 && status[b] != kFlagUnsignificantStay)
+            return fail(WG_EINVAL, "refinement status %d on block %d (0 or 9 expected)", status[b], b);
+    t->status.assign(status, status + nblk);
+    return WG_OK;
+}
+
 int wg_get_refinement_status(wg_ctx *ctx, int tree, int cap, int *status) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return tree_err();

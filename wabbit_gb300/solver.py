@@ -406,6 +406,11 @@ class Forest:
         neighbours)."""
         capi.check(self.L.wg_refine_significant(self.ctx.h, self.tree))
 
+    def set_refinement_status(self, status):
+        """The status of the current blocks as a restarted run reads it."""
+        st = np.ascontiguousarray(status, np.int32)
+        capi.check(self.L.wg_set_refinement_status(self.ctx.h, self.tree, len(st), _p(st, ctypes.c_int)))
+
     def refinement_status(self):
         """The status the last adaptation left per block (0 or 9)."""
         n = capi.check(self.L.wg_get_refinement_status(self.ctx.h, self.tree, 0, None))
