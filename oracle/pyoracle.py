@@ -64,6 +64,7 @@ def lib():
         L.or_set_coarse_extension.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.or_status.argtypes = [ctypes.c_void_p, _ip]
         L.or_set_status.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip]
+        L.or_set_fd_stencil.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.or_filter.argtypes = [ctypes.c_void_p, ctypes.c_int, _ip, _ip, _dp]
         L.or_adapt_full_tree.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int]
         L.or_run.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
@@ -310,6 +311,11 @@ class Oracle:
         st = np.ascontiguousarray(st, np.int32)
         if self.L.or_set_status(self.h, len(st), _p(st, ctypes.c_int)) != 0:
             raise RuntimeError("or_set_status: wrong length")
+
+    def set_fd_stencil(self, n):
+        """The FD stencil half-width of the wavelet set-up (0: none)."""
+        if self.L.or_set_fd_stencil(self.h, int(n)) != 0:
+            raise RuntimeError("or_set_fd_stencil failed")
 
     def set_coarse_extension(self, on=True):
         """useCoarseExtension and useSecurityZone for any wavelet."""

@@ -2672,6 +2672,16 @@ int or_set_status(void *h, int n, const int *st) {
     return WG_OK;
 }
 
+// the FD stencil half-width the wavelet set-up widens the coarse-extension
+// zones to (module_wavelets.f90:1402-1417): 2 for FD_4th_central (the
+// default), 0 where no discretization is set (the reference's wavelet
+// post-processing tools)
+int or_set_fd_stencil(void *h, int n) {
+    Oracle &o = *(Oracle *)h;
+    if (n < 0 || !setup_wavelet(o.cfg.wavelet, n, o.wav)) return WG_EINVAL;
+    return WG_OK;
+}
+
 // useCoarseExtension and useSecurityZone for any wavelet (on != 0)
 int or_set_coarse_extension(void *h, int on) {
     ((Oracle *)h)->ce_force = on != 0;

@@ -18,9 +18,9 @@ compare against them:
 * tg3d_equi.npz -- TESTING/acm/taylorGreen/taylorGreenEqui_FD4_CDF40: 3-D ACM,
   Bs=20, 8 blocks on level 1, state at t=0 (input) and t=10 (output).
 * wavelet_adaptive.npz -- TESTING/wavelets: a 2-D adaptive vorticity field
-  (112 blocks, levels 2-5, Bs=32), the reference's refine-everywhere result
-  with CDF40 (448 blocks) and its coarsen-everywhere results with CDF40 and
-  CDF44.
+  (112 blocks, levels 2-5, Bs=32), the reference's refine-everywhere results
+  with CDF40, CDF20 and CDF60 (448 blocks) and its coarsen-everywhere
+  results with CDF20, CDF22, CDF40, CDF42, CDF44, CDF60 and CDF62.
 * vortex2d_adapt.npz -- TESTING/acm/3vortices/3vorticesAdaptFD4_CDF40 and
   _CDF42: the adaptive 2-D loop (significant refinement, coarse extension and
   security zone): the ini text and the states at t=10 and t=15.
@@ -131,7 +131,11 @@ def wavelets(ref):
     d = read_wabbit(os.path.join(folder, "adaptive_CDF40", "vor_00100.h5"))
     lv, c, u = _sorted(d, _interior(d)[:, None])
     out.update(refined_level=lv, refined_coords=c, refined_u=u)
-    for w in ["CDF40", "CDF44"]:
+    for w in ["CDF20", "CDF60"]:   # the refinement with the order-2 and order-6 predictors
+        d = read_wabbit(os.path.join(folder, f"adaptive_{w}", "vor_00100.h5"))
+        lv, c, u = _sorted(d, _interior(d)[:, None])
+        out.update({f"refined_{w}_level": lv, f"refined_{w}_coords": c, f"refined_{w}_u": u})
+    for w in ["CDF20", "CDF22", "CDF40", "CDF42", "CDF44", "CDF60", "CDF62"]:
         d = read_wabbit(os.path.join(folder, f"adaptive_{w}", "vor_00200.h5"))
         lv, c, u = _sorted(d, _interior(d)[:, None])
         out.update({f"coarsened_{w}_level": lv, f"coarsened_{w}_coords": c, f"coarsened_{w}_u": u})

@@ -22,28 +22,33 @@ def _sorted(lv, co, u):
     return lv[order], co[order], u[order]
 
 
-def test_coarsen_everywhere_golden_cdf40(golden):
+@pytest.mark.parametrize("w", ["CDF40", "CDF20", "CDF60"])
+def test_coarsen_everywhere_golden_cdf40(golden, w):
+    """The unlifted adaptation on the file refined with the wavelet's own
+    predictor against TESTING/wavelets/adaptive_<w>/vor_00200.h5, bit for
+    bit."""
     z = golden("wavelet_adaptive.npz")
     cfg = config.defaults(2)
     cfg.Bs[0] = cfg.Bs[1] = 32
     cfg.domain[0] = cfg.domain[1] = 6.283185307179586
-    cfg.wavelet = b"CDF40"
-    cfg.g, cfg.g_rhs = 3, 2
+    cfg.wavelet = w.encode()
+    cfg.g, cfg.g_rhs = max(3, config.wavelet_ghosts(w)[0]), 2
     cfg.Jmin, cfg.Jmax = 1, 7
-    u1 = z["refined_u"]                          # one component; the ACM state carries three copies
+    key = "refined" if w == "CDF40" else f"refined_{w}"
+    u1 = z[f"{key}_u"]                           # one component; the ACM state carries three copies
     u3 = np.repeat(u1, 3, axis=1)
     with Context(cfg, 2 * len(u1)) as ctx:
         f = ctx.forest()
-        f.set_grid(z["refined_level"], z["refined_coords"])
+        f.set_grid(z[f"{key}_level"], z[f"{key}_coords"])
         f.upload(pad_blocks(cfg, u3))
         n = f.adapt(everywhere=True)
         assert n == 112
         lv, co = f.grid()
         lv, co, u = _sorted(lv, co, interior(cfg, f.download()))
-    assert np.array_equal(lv, z["coarsened_CDF40_level"])
-    assert np.array_equal(co, z["coarsened_CDF40_coords"])
+    assert np.array_equal(lv, z[f"coarsened_{w}_level"])
+    assert np.array_equal(co, z[f"coarsened_{w}_coords"])
     for c in range(3):
-        assert np.array_equal(u[:, c:c + 1], z["coarsened_CDF40_u"])
+        assert np.array_equal(u[:, c:c + 1], z[f"coarsened_{w}_u"])
 
 
 @pytest.mark.parametrize("dim,wavelet,quantile,jmax", [(2, "CDF40", 0.5, 5), (2, "CDF20", 0.7, 5), (2, "CDF60", 0.4, 5),

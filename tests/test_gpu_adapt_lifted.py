@@ -23,32 +23,39 @@ def _sorted(lv, co, u):
     return lv[order], co[order], u[order]
 
 
-def test_coarsen_everywhere_cdf44_matches_oracle(golden):
+@pytest.mark.parametrize("w,src", [("CDF44", "CDF40"), ("CDF42", "CDF40"), ("CDF62", "CDF60")])
+def test_coarsen_everywhere_cdf44_matches_oracle(golden, w, src):
+    """The lifted adaptation everywhere on the file refined with the
+    wavelet's predictor: bit for bit the oracle's, and within 4e-15 of
+    TESTING/wavelets/adaptive_<w>/vor_00200.h5 (the CE zones of these
+    wavelets are wider than the FD stencil, so the widening the device's
+    set-up applies changes nothing)."""
     z = golden("wavelet_adaptive.npz")
     cfg = config.defaults(2)
     cfg.Bs[0] = cfg.Bs[1] = 32
     cfg.domain[0] = cfg.domain[1] = 6.283185307179586
-    cfg.wavelet = b"CDF44"
-    cfg.g, cfg.g_rhs = 6, 2
+    cfg.wavelet = w.encode()
+    cfg.g, cfg.g_rhs = config.wavelet_ghosts(w)[0], 2
     cfg.Jmin, cfg.Jmax = 1, 7
-    u1 = z["refined_u"]
+    key = "refined" if src == "CDF40" else f"refined_{src}"
+    u1 = z[f"{key}_u"]
     u3 = np.concatenate([u1, 0.5 * u1 ** 2, -u1], axis=1)
     data = pad_blocks(cfg, u3)
     o = Oracle(cfg)
-    o.set_grid(z["refined_level"], z["refined_coords"], data)
+    o.set_grid(z[f"{key}_level"], z[f"{key}_coords"], data)
     o.sync(cfg.g, cfg.g, ignore_filter=False)
     assert o.adapt(everywhere=True) == 112
     with Context(cfg, 2 * len(u1)) as ctx:
         f = ctx.forest()
-        f.set_grid(z["refined_level"], z["refined_coords"])
+        f.set_grid(z[f"{key}_level"], z[f"{key}_coords"])
         f.upload(data)
         assert f.adapt(everywhere=True) == 112
         b = _sorted(*f.grid(), f.download())
     a = _sorted(*o.grid(), o.data())
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert np.array_equal(a[2], b[2])
-    assert np.array_equal(a[0], z["coarsened_CDF44_level"])
-    assert np.abs(interior(cfg, b[2])[:, :1] - z["coarsened_CDF44_u"]).max() <= 4e-15
+    assert np.array_equal(a[0], z[f"coarsened_{w}_level"])
+    assert np.abs(interior(cfg, b[2])[:, :1] - z[f"coarsened_{w}_u"]).max() <= 4e-15
 
 
 @pytest.mark.parametrize("dim,Bs,jmin,jmax,quantile", [(2, 32, 1, 4, 0.6), (2, 16, 2, 5, 0.5), (3, 16, 1, 3, 0.8),

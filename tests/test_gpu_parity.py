@@ -175,15 +175,19 @@ def test_tg3d_reference_golden(golden):
     assert np.array_equal(u, z["u_out"])
 
 
-def test_refine_everywhere_reference_golden(golden):
+@pytest.mark.parametrize("w", ["CDF40", "CDF20", "CDF60"])
+def test_refine_everywhere_reference_golden(golden, w):
+    """refineBlock with the order-4, order-2 and order-6 predictors against
+    TESTING/wavelets/adaptive_<w>/vor_00100.h5, bit for bit."""
     z = golden("wavelet_adaptive.npz")
     c = config.defaults(2)
     c.Bs[0] = c.Bs[1] = 32
     c.domain[0] = c.domain[1] = 6.283185307179586
     c.neq = 3  # the context needs dim+1 components: the field goes in component 0
-    c.wavelet = b"CDF40"
-    c.g, c.g_rhs = 3, 2
+    c.wavelet = w.encode()
+    c.g, c.g_rhs = max(3, config.wavelet_ghosts(w)[0]), 2
     c.Jmin, c.Jmax = 1, 7
+    key = "refined" if w == "CDF40" else f"refined_{w}"
     u = np.zeros((len(z["in_level"]), 3) + z["in_u"].shape[2:])
     u[:, 0] = z["in_u"][:, 0]
     with Context(c, 600) as ctx:
@@ -195,9 +199,9 @@ def test_refine_everywhere_reference_golden(golden):
         lv, co = f.grid()
         got = interior(c, f.download())[:, :1]
     order = np.lexsort((co[:, 0], co[:, 1], co[:, 2], lv))
-    assert np.array_equal(lv[order], z["refined_level"])
-    assert np.array_equal(co[order], z["refined_coords"])
-    assert np.array_equal(got[order], z["refined_u"])
+    assert np.array_equal(lv[order], z[f"{key}_level"])
+    assert np.array_equal(co[order], z[f"{key}_coords"])
+    assert np.array_equal(got[order], z[f"{key}_u"])
 
 
 @pytest.mark.parametrize("dim,wavelet", [(2, "CDF40"), (3, "CDF40"), (2, "CDF44"), (3, "CDF44"), (2, "CDF22")])

@@ -126,6 +126,53 @@ def test_refine_everywhere_golden(golden):
     assert np.array_equal(u[order], z["refined_u"])
 
 
+@pytest.mark.parametrize("w", ["CDF20", "CDF60"])
+def test_refine_everywhere_golden_other_predictors(golden, w):
+    """refineBlock with the order-2 and order-6 predictors (TESTING/wavelets/
+    adaptive_CDF20, _CDF60 vor_00100.h5): bit for bit."""
+    z = golden("wavelet_adaptive.npz")
+    g, _ = config.wavelet_ghosts(w)
+    cfg = wavelet_cfg(w, g)
+    o = Oracle(cfg)
+    o.set_grid(z["in_level"], z["in_coords"], pad_blocks(cfg, z["in_u"]))
+    o.sync(cfg.g, cfg.g, ignore_filter=False)
+    o.refine_everywhere()
+    lv, co = o.grid()
+    u = interior(cfg, o.data())
+    order = np.lexsort((co[:, 0], co[:, 1], co[:, 2], lv))
+    assert np.array_equal(lv[order], z[f"refined_{w}_level"])
+    assert np.array_equal(co[order], z[f"refined_{w}_coords"])
+    assert np.array_equal(u[order], z[f"refined_{w}_u"])
+
+
+@pytest.mark.parametrize("w,src,tol", [("CDF20", "CDF20", 0.0), ("CDF60", "CDF60", 0.0), ("CDF22", "CDF20", 4e-15),
+                                       ("CDF42", "CDF40", 4e-15), ("CDF62", "CDF60", 4e-15)])
+def test_coarsen_everywhere_golden_other_wavelets(golden, w, src, tol):
+    """adapt_tree 'everywhere' on the file refined with the wavelet's
+    predictor (TESTING/wavelets/adaptive_<w>/vor_00200.h5): unlifted CDF2,0
+    and CDF6,0 bit for bit, lifted CDF2,2, CDF4,2, CDF6,2 with the grid
+    exact and the values within 4e-15 (as CDF4,4). The wavelet tools run
+    without a discretization, so the coarse-extension zones are not widened
+    to the FD stencil (module_wavelets.f90:1402-1417): set_fd_stencil(0);
+    CDF2,2 is the one wavelet whose zones that widening changes (0.033 away
+    from the file with it)."""
+    z = golden("wavelet_adaptive.npz")
+    g, _ = config.wavelet_ghosts(w)
+    cfg = wavelet_cfg(w, g)
+    o = Oracle(cfg)
+    o.set_fd_stencil(0)
+    pre = "refined" if src == "CDF40" else f"refined_{src}"
+    o.set_grid(z[f"{pre}_level"], z[f"{pre}_coords"], pad_blocks(cfg, z[f"{pre}_u"]))
+    assert o.adapt(everywhere=True) == 112
+    lv, co = o.grid()
+    u = interior(cfg, o.data())
+    order = np.lexsort((co[:, 0], co[:, 1], co[:, 2], lv))
+    assert np.array_equal(lv[order], z[f"coarsened_{w}_level"])
+    assert np.array_equal(co[order], z[f"coarsened_{w}_coords"])
+    d = np.abs(u[order] - z[f"coarsened_{w}_u"]).max()
+    assert d <= tol, d
+
+
 @pytest.mark.parametrize("w", ["CDF20", "CDF40", "CDF44", "CDF60", "CDF62"])
 def test_wavelet_filter_sums(w):
     """Filter-bank identities checked at start-up by the reference
