@@ -865,7 +865,8 @@ int ensure_shadow(wg_ctx *ctx, Tree &t) {
 // the previous one's output (B -> C -> D -> E), so the timed kernels see
 // realistic values. Nothing the next step reads changes: stages 1-3 write
 // the scratch stage buffers, and stage 4 writes its copy of u_n+1 to C (not
-// B) and neither stores u_n+1 nor records its maximum (keep = 0). The
+// B) and neither stores u_n+1 nor records its maximum (keep = 4: it writes
+// u_n back unchanged where u_n+1 would go, so its traffic is the real one). The
 // autotuner may therefore run between any two steps without changing a bit
 // of the results.
 int autotune_stage_form(wg_ctx *ctx, Tree &t) {
@@ -895,7 +896,7 @@ int autotune_stage_form(wg_ctx *ctx, Tree &t) {
         int best_form = WG_FORM_DIRECT;
         for (int form : forms) {
             ctx->tuned[stage - 1] = form;
-            const int keep = stage == 4 ? 0 : 1;
+            const int keep = stage == 4 ? 4 : 1;
             if ((st = stage_launch_df(ctx, t, stage, in[stage - 1], out[stage - 1], push, keep))) break;   // warm-up
             WG_CUDA_OK(cudaEventRecord(e0, ctx->stream));
             for (int r = 0; r < 3 && !st; r++) st = stage_launch_df(ctx, t, stage, in[stage - 1], out[stage - 1], push, keep);

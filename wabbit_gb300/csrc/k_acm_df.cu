@@ -49,6 +49,7 @@ struct StageArgsDF {
     const int *cpos;       // block slot -> its position in cout (and nin)
     const double *nin;     // stage 4: the next step's input (compact like cout), which replaces the state, or null
     int record;            // stage 4: merge the maximum of what it stores into the tree's running max
+    int rewrite;           // stage 4: store u_n (unchanged) where u_n+1 would go (timing with the state's traffic)
     BufGeo gun;
     const float2 *mask;    // 5 words per point, interior only
     const int *push;       // same-level ghost copies pushed by the writer, or null
@@ -372,7 +373,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
                 }
                 continue;
             }
-            if (a.un_out) un[c * us] = v;
+            if (a.un_out) un[c * us] = a.rewrite ? u : v;
             if (ob) {   // the anchored copy of u_n+1 and its running maximum
                 const df2 w = anchor(df_add_nr(ud, inc), k.M);
                 ov[c] = make_float2(w.hi, w.lo);
@@ -718,17 +719,19 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.gt = gt;
     a.un = un;
     // keep_state 1: u_n+1 to the state, its copy to out, its maximum recorded
-    // (and to cout when given); 0 (timing): the copy to out only; 2: u_n+1
-    // to cout only (a result the next input replaces); 3: u_n+1 to cout, and
-    // the next step's input nin (compact like cout) into the state, its copy
-    // to out and its maximum recorded
-    if (keep_state < 0 || keep_state > 3 || (keep_state >= 2 && (stage != 4 || !cout || !cpos)) ||
+    // (and to cout when given); 0 (timing): the copy to out only; 4 (timing
+    // with the state's traffic): as 0, and u_n written back unchanged where
+    // u_n+1 would go; 2: u_n+1 to cout only (a result the next input
+    // replaces); 3: u_n+1 to cout, and the next step's input nin (compact
+    // like cout) into the state, its copy to out and its maximum recorded
+    if (keep_state < 0 || keep_state > 4 || ((keep_state == 2 || keep_state == 3) && (stage != 4 || !cout || !cpos)) ||
         (keep_state == 3 && !nin))
         return cudaErrorInvalidValue;
-    a.un_out = keep_state == 1 || keep_state == 3 ? un : nullptr;
-    a.cout = keep_state && stage == 4 ? cout : nullptr;
+    a.un_out = keep_state == 1 || keep_state == 3 || keep_state == 4 ? un : nullptr;
+    a.cout = (keep_state == 1 || keep_state == 2 || keep_state == 3) && stage == 4 ? cout : nullptr;
     a.nin = keep_state == 3 ? nin : nullptr;
     a.record = keep_state == 1 || keep_state == 3;
+    a.rewrite = keep_state == 4;
     if (keep_state == 2) a.out = nullptr;
     a.cpos = cpos;
     a.gun = gun;
