@@ -271,7 +271,6 @@ __device__ __forceinline__ df2 interp_df(const float2 *v, int stride, int first)
 // by other CTAs, wrote some of it, and a line this SM's L1 held from before
 // could be stale. Every thread ends past a barrier, so the caller may reuse
 // sf at once.
-
 template <int NCOEF>
 __device__ __forceinline__ void predict_df_patch(const Patch &p, float2 *buf, BufGeo geo, int nc, int cg, float M,
                                                  float2 *sf) {
