@@ -244,6 +244,7 @@ struct wg_ctx {
     double *s4_out = nullptr;
     int s4_keep = 1;                    // stage-4 mode of rk4_enqueue_df (launch_acm_stage_df keep_state)
     const double *s4_next = nullptr;    // stage 4 (keep 3): the next step's compact input
+    const double *s4_usrc = nullptr;    // dt and stage 4 read u_n from this compact input (positions d_pos), or null
     cudaEvent_t s4_wait = nullptr;      // stage 4 waits for it (the copy of s4_next), or null
     DevArray<int> d_pos;
     // set when a bounded device wait gave up (WG_ETIMEOUT): a bulk copy may
@@ -754,7 +755,8 @@ static int stage_pair(wg_ctx *ctx, int stage, const int *plain, int nplain, cons
     auto go = [&](int msk, const int *blk, int n) {
         return launch_acm_stage_df(dim, stage, msk, blk, n, ctx->d_desc, ctx->d_tp, ctx->d_clk, in, ctx->B, ctx->C,
                                    ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0], Bs[1], Bs[2], tm,
-                                   march, ctx->d_err, ctx->stream, keep, ctx->s4_out, ctx->d_pos.p, ctx->s4_next);
+                                   march, ctx->d_err, ctx->stream, keep, ctx->s4_out, ctx->d_pos.p, ctx->s4_next,
+                                   stage == 4 ? ctx->s4_usrc : nullptr);
     };
     if (march == 2) {
         WG_CUDA_OK(go(nmasked, both, nplain + nmasked));
@@ -939,8 +941,15 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     // or the shadow copy) when push is on
     if ((st = run_sync(ctx, t, ctx->B, true, g_rhs, g_rhs, true, push))) return st;
     prof_mark(ctx, 1);
-    WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
-                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx), ctx->stream, 1));
+    if (ctx->s4_usrc) {   // u_n in the compact input of a streamed step
+        const BufGeo gc = {Bs[0], Bs[1], ctx->cfg.dim == 3 ? Bs[2] : 1, 0};
+        WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk,
+                             ctx->s4_usrc, gc, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx),
+                             ctx->stream, 1, ctx->d_pos.p));
+    } else {
+        WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
+                             ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx), ctx->stream, 1));
+    }
     prof_mark(ctx, 2);
     if ((st = stage_launch_df(ctx, t, 1, ctx->B, ctx->C, push))) return st;
     prof_mark(ctx, 3);
@@ -3151,13 +3160,14 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     for (cudaEvent_t &ev : ctx->io_ev)
         if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return fail(WG_ECUDA, "cudaEventCreate failed");
     // I[k % 3] receives step k's input, O[k & 1] its result. FP32-pipe: the
-    // last stage of step k also loads input k+1 into the state and its
-    // anchored copy (the scatter of the next step), so an input is consumed
-    // either by the first scatter or by the stage 4 before its step. The
-    // copy in of step k+1 waits only for the consumption of input k-2 (three
-    // input buffers: the copies in run ahead of the steps, and a stage 4
-    // finds its next input on the device), the copy out of step k only for
-    // the end of step k, so both directions use the link at once
+    // last stage of step k also writes the anchored copy of input k+1 (the
+    // scatter of the next step), and step k+1 reads its u_n (dt, last stage)
+    // from I directly, so the FP64 state is written only by the last step;
+    // an input is free again after its own step. The copy in of step k+1
+    // waits only for the end of step k-2 (three input buffers: the copies in
+    // run ahead of the steps, and a stage 4 finds its next input on the
+    // device), the copy out of step k only for the end of step k, so both
+    // directions use the link at once
     cudaEvent_t *h2d_done = ctx->io_ev, *d2h_done = ctx->io_ev + 3, *gathered = ctx->io_ev + 5,
                 *consumed = ctx->io_ev + 7;
     const bool shadow = ctx->precision == WG_RHS_FP32;
@@ -3183,10 +3193,14 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
                                         shadow ? ctx->B : nullptr, ctx->gT, push ? ctx->d_push : nullptr));
         return WG_OK;
     };
-    auto reanchor = [&]() -> int {   // the quantum of the new state, the copy redone if it changed
+    // the quantum of the new state, the copy redone if it changed: from the
+    // state after a scatter, from the compact input (src) after a stage 4
+    // that loaded it
+    auto reanchor = [&](const double *src) -> int {
         WG_CUDA_OK(launch_anchor_check(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
-        WG_CUDA_OK(launch_shadow(t->d_all.p, nblk, ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0], Bs[1], Bz,
-                                 push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream, 1));
+        WG_CUDA_OK(launch_shadow(t->d_all.p, nblk, src ? src : ctx->A, ctx->gA, ctx->B, ctx->gT, ctx->geo.nc, Bs[0],
+                                 Bs[1], Bz, push ? ctx->d_push : nullptr, ctx->d_desc, ctx->d_clk, ctx->stream, 1,
+                                 src ? ctx->d_pos.p : nullptr));
         return WG_OK;
     };
     for (int k = 0; k < nsteps; k++) {
@@ -3201,8 +3215,7 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
         if (k == 0 || !shadow) {
             WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, h2d_done[cur], 0));
             if ((st = scatter(I[cur]))) return st;
-            WG_CUDA_OK(cudaEventRecord(consumed[cur], ctx->stream));
-            if (shadow && (st = reanchor())) return st;
+            if (shadow && (st = reanchor(nullptr))) return st;
         }
         t->shadow_valid = shadow;
         // the result buffer O[oc] is free once the result of step k-2 is out
@@ -3213,17 +3226,17 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
             ctx->s4_keep = chain ? 3 : 1;
             ctx->s4_next = chain ? I[nxt] : nullptr;
             ctx->s4_wait = chain ? h2d_done[nxt] : nullptr;
+            ctx->s4_usrc = I[cur];
         }
         st = rk4_enqueue(ctx, tree);
         ctx->s4_out = nullptr;
         ctx->s4_keep = 1;
         ctx->s4_next = nullptr;
         ctx->s4_wait = nullptr;
+        ctx->s4_usrc = nullptr;
         if (st) return st;
-        if (chain) {
-            WG_CUDA_OK(cudaEventRecord(consumed[nxt], ctx->stream));
-            if ((st = reanchor())) return st;
-        }
+        if (chain && (st = reanchor(I[nxt]))) return st;
+        WG_CUDA_OK(cudaEventRecord(consumed[cur], ctx->stream));   // input k read for the last time
         if (!shadow)
             WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, O[oc], ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 0,
                                             ctx->d_desc, nullptr, ctx->stream));

@@ -138,7 +138,8 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
                                 cudaStream_t s, int keep_state = 1, double *cout = nullptr,
-                                const int *cpos = nullptr, const double *nin = nullptr);
+                                const int *cpos = nullptr, const double *nin = nullptr,
+                                const double *usrc = nullptr);
 // (march 0, 3, 4: tmap is a slab map of 4, 2 or 8 interior planes and the
 // tile kernel of that slab height runs; 1: tmap is a map
 // with one-plane boxes and the whole-block ring kernel runs; 2: tmap is a
@@ -152,10 +153,12 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
 int tile_slab(int dim, int Bs0, int Bs1, int Bs2, int g);
 // double-float copy of the interiors of the listed blocks of an FP64 buffer
 // (push: same-level ghost copies as in the stage kernel, or null)
-// (only_if_flagged: only blocks of trees whose TreeClock::reshadow is set)
+// (only_if_flagged: only blocks of trees whose TreeClock::reshadow is set;
+// cpos: src is a compact array (position, component, z, y, x), block b at
+// position cpos[b], and gs is not used)
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
                           int Bs0, int Bs1, int Bs2, const int *push, const BlockDesc *desc, const TreeClock *clk,
-                          cudaStream_t s, int only_if_flagged = 0);
+                          cudaStream_t s, int only_if_flagged = 0, const int *cpos = nullptr);
 // after an upload that wrote the anchored copy with the trees' current
 // constant: the constant from the merged running max, and reshadow set
 // where it differs from the one used
@@ -199,7 +202,10 @@ cudaError_t launch_sphere_fill(const int4 *cand, const int *slot, int n, const S
 // holds kDtStartBits between reductions
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
-                      const int *trees, unsigned *done, cudaStream_t s, int step_start = 0);
+                      const int *trees, unsigned *done, cudaStream_t s, int step_start = 0,
+                      const int *upos = nullptr);
+// (upos: u is indexed by upos[slot] instead of the slot, e.g. a compact
+// interior array with geo = {Bs0, Bs1, Bs2, 0})
 
 cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
 // max |u| per component over the interiors of the listed blocks (Bs2 = 1 in 2-D)

@@ -47,7 +47,8 @@ struct StageArgsDF {
     double *un_out;        // where stage 4 stores u_n+1 (un, or null: not stored)
     double *cout;          // stage 4: u_n+1 also into a compact interior array (nblk, nc, Bz, By, Bx), or null
     const int *cpos;       // block slot -> its position in cout (and nin)
-    const double *nin;     // stage 4: the next step's input (compact like cout), which replaces the state, or null
+    const double *nin;     // stage 4: the next step's input (compact like cout): its anchored copy to out, or null
+    const double *usrc;    // stage 4: u_n read from this compact array (positions cpos) instead of un, or null
     int record;            // stage 4: merge the maximum of what it stores into the tree's running max
     int rewrite;           // stage 4: store u_n (unchanged) where u_n+1 would go (timing with the state's traffic)
     BufGeo gun;
@@ -301,15 +302,22 @@ __device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int ix, int
 #pragma unroll
         for (int c = 0; c <= DIM; c++) in.a[c] = a.u0[off + c * cs];
     } else if (STAGE == 4) {
-        const long long us = a.gun.npts();
-        const double *un = a.un + (long long)b * (DIM + 1) * us +
-                           ((long long)(iz + (DIM == 3 ? a.gun.gb : 0)) * a.gun.ny + (iy + a.gun.gb)) * a.gun.nx +
-                           (ix + a.gun.gb);
+        long long us = a.gun.npts();
+        const double *un;
+        if (a.usrc) {   // compact: (position, component, z, y, x)
+            const int nint = a.Bs0 * a.Bs1 * (DIM == 3 ? a.Bs2 : 1);
+            us = nint;
+            un = a.usrc + (long long)a.cpos[b] * (DIM + 1) * nint + ((DIM == 3 ? iz * a.Bs1 : 0) + iy) * a.Bs0 + ix;
+        } else {
+            un = a.un + (long long)b * (DIM + 1) * us +
+                 ((long long)(iz + (DIM == 3 ? a.gun.gb : 0)) * a.gun.ny + (iy + a.gun.gb)) * a.gun.nx +
+                 (ix + a.gun.gb);
+        }
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
             in.a[c] = a.s2[off + c * cs];
             in.b[c] = a.s3[off + c * cs];
-            in.c[c] = bits_f2(un[c * us]);
+            in.c[c] = bits_f2(a.usrc ? __ldcs(un + c * us) : un[c * us]);
         }
     }
 }
@@ -361,9 +369,8 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
             const double v = __dadd_rn(u, df_to_double(inc));
             const long long ci = cbase + (long long)c * nint;
             if (a.cout) a.cout[ci] = v;
-            if (a.nin) {   // the next input takes the place of u_n+1 in the state and its copy
+            if (a.nin) {   // the next input takes the place of u_n+1 in the anchored copy
                 const double x = __ldcs(a.nin + ci);
-                if (a.un_out) un[c * us] = x;
                 if (ob) {
                     const df2 sx = df_split(x);
                     const df2 w = anchor(sx, k.M);
@@ -703,7 +710,8 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const TreeParams *tp, TreeClock *clk, const void *in, const void *u0, const void *s2,
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
-                                cudaStream_t s, int keep_state, double *cout, const int *cpos, const double *nin) {
+                                cudaStream_t s, int keep_state, double *cout, const int *cpos, const double *nin,
+                                const double *usrc) {
     if (nblk <= 0) return cudaSuccess;
     if (stage < 1 || stage > 4) return cudaErrorInvalidValue;
     StageArgsDF a;
@@ -722,12 +730,15 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     // (and to cout when given); 0 (timing): the copy to out only; 4 (timing
     // with the state's traffic): as 0, and u_n written back unchanged where
     // u_n+1 would go; 2: u_n+1 to cout only (a result the next input
-    // replaces); 3: u_n+1 to cout, and the next step's input nin (compact
-    // like cout) into the state, its copy to out and its maximum recorded
+    // replaces); 3: u_n+1 to cout, and the anchored copy of the next step's
+    // input nin (compact like cout) to out with its maximum recorded (the
+    // next step reads u_n from nin: usrc). usrc (stage 4, with cpos): u_n
+    // is read from that compact array instead of un.
     if (keep_state < 0 || keep_state > 4 || ((keep_state == 2 || keep_state == 3) && (stage != 4 || !cout || !cpos)) ||
-        (keep_state == 3 && !nin))
+        (keep_state == 3 && !nin) || (usrc && (stage != 4 || !cpos || keep_state == 4)))
         return cudaErrorInvalidValue;
-    a.un_out = keep_state == 1 || keep_state == 3 || keep_state == 4 ? un : nullptr;
+    a.un_out = keep_state == 1 || keep_state == 4 ? un : nullptr;
+    a.usrc = stage == 4 ? usrc : nullptr;
     a.cout = (keep_state == 1 || keep_state == 2 || keep_state == 3) && stage == 4 ? cout : nullptr;
     a.nin = keep_state == 3 ? nin : nullptr;
     a.record = keep_state == 1 || keep_state == 3;
@@ -833,19 +844,19 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
 __global__ void __launch_bounds__(256) shadow_kernel(const int *__restrict__ blk, const double *src, BufGeo gs,
                                                      float2 *dst, BufGeo gd, int nc, int Bx, int By, int Bz,
                                                      const int *push, const BlockDesc *desc, const TreeClock *clk,
-                                                     int only_if_flagged) {
+                                                     int only_if_flagged, const int *cpos) {
     // one CTA per (block, component), 32-bit index arithmetic within the block
     const int b = blk[blockIdx.x], c = blockIdx.y;
     if (only_if_flagged && !clk[desc[b].tree].reshadow) return;
     const int nint = Bx * By * Bz;
     const int zs = gs.nz > 1 ? gs.gb : 0, zd = gd.nz > 1 ? gd.gb : 0;
-    const double *sb = src + ((long long)b * nc + c) * gs.npts();
+    const double *sb = cpos ? src + ((long long)cpos[b] * nc + c) * nint : src + ((long long)b * nc + c) * gs.npts();
     float2 *dc = dst + (long long)c * gd.npts();
     float2 *db = dc + (long long)b * nc * gd.npts();
     const float M = clk[desc[b].tree].anchor_M;
     for (int i = threadIdx.x; i < nint; i += blockDim.x) {
         const int ix = i % Bx, iy = (i / Bx) % By, iz = i / (Bx * By);
-        const double v = sb[((iz + zs) * gs.ny + (iy + gs.gb)) * gs.nx + (ix + gs.gb)];
+        const double v = cpos ? sb[i] : sb[((iz + zs) * gs.ny + (iy + gs.gb)) * gs.nx + (ix + gs.gb)];
         const df2 w = anchor(df_split(v), M);
         const float2 f = make_float2(w.hi, w.lo);
         db[((iz + zd) * gd.ny + (iy + gd.gb)) * gd.nx + (ix + gd.gb)] = f;
@@ -1026,11 +1037,11 @@ cudaError_t launch_anchor_check(TreeClock *clk, const int *trees, int ntrees, cu
 
 cudaError_t launch_shadow(const int *blk, int nblk, const double *src, BufGeo gs, void *dst, BufGeo gd, int nc,
                           int Bs0, int Bs1, int Bs2, const int *push, const BlockDesc *desc, const TreeClock *clk,
-                          cudaStream_t s, int only_if_flagged) {
+                          cudaStream_t s, int only_if_flagged, const int *cpos) {
     if (nblk <= 0) return cudaSuccess;
     shadow_kernel<<<dim3((unsigned)nblk, (unsigned)nc), 256, 0, s>>>(blk, src, gs, reinterpret_cast<float2 *>(dst), gd,
                                                                      nc, Bs0, Bs1, Bs2, push, desc, clk,
-                                                                     only_if_flagged);
+                                                                     only_if_flagged, cpos);
     return cudaGetLastError();
 }
 

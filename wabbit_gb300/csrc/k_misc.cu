@@ -64,7 +64,7 @@ template <int DIM, int BS>
 __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc *desc, const TreeParams *tp,
                                                  TreeClock *clk, const double *u, BufGeo geo, int Bs0_, int Bs1_,
                                                  int Bs2_, const int *trees, int ntrees, int step_start,
-                                                 unsigned *done) {
+                                                 unsigned *done, const int *upos) {
     const int Bs0 = BS ? BS : Bs0_, Bs1 = BS ? BS : Bs1_, Bs2 = BS ? BS : Bs2_;
     __shared__ int s_last;
     constexpr int kCache = 4096;
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc
     const long long np = geo.npts();
     const int nint = Bs0 * Bs1 * (DIM == 3 ? Bs2 : 1);
     const bool cache = nint <= kCache;
-    const double *ub = u + (long long)b * (DIM + 1) * np;
+    const double *ub = u + (long long)(upos ? upos[b] : b) * (DIM + 1) * np;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     auto offset = [&](int q) {
         const int ix = q % Bs0, iy = (q / Bs0) % Bs1, iz = DIM == 3 ? q / (Bs0 * Bs1) : 0;
@@ -184,12 +184,12 @@ __global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntree
 
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
-                      const int *trees, unsigned *done, cudaStream_t s, int step_start) {
+                      const int *trees, unsigned *done, cudaStream_t s, int step_start, const int *upos) {
     if (!done) return cudaErrorInvalidValue;
     if (nblk > 0) {
         const bool b16 = Bs0 == 16 && Bs1 == 16 && (dim == 2 || Bs2 == 16);
         auto k = dim == 2 ? (b16 ? dt_kernel<2, 16> : dt_kernel<2, 0>) : (b16 ? dt_kernel<3, 16> : dt_kernel<3, 0>);
-        k<<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2, trees, ntrees, step_start, done);
+        k<<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2, trees, ntrees, step_start, done, upos);
     } else {
         dt_finalize_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(tp, clk, trees, ntrees, step_start);
     }
