@@ -202,8 +202,10 @@ int wg_download_interior(wg_ctx *ctx, int tree, double *host);
 /* nsteps RK4 steps with host buffers: for step k the interior state is set
  * from ins[k], one step is taken (as wg_rk4_step) and the interior result is
  * written to outs[k]. With page-locked buffers the copy of step k+1's input
- * and of step k's result run while step k / k+1 compute (two staging buffers
- * of the interior size). Returns after the last result is on the host. */
+ * and of step k's result run while step k / k+1 compute (five device
+ * staging buffers of the interior size: three inputs, two results). Returns
+ * after the last result is on the host; the context's state then holds the
+ * last step's result. */
 int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, double *const *outs);
 /* Penalisation mask in the layout of hvy_mask (..., 1:6, Nb): chi, usx,
  * usy, usz, colour, sponge (createMask_tree, LIB/MESH/createMask_tree.f90);

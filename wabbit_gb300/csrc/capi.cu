@@ -3125,11 +3125,11 @@ int wg_download_interior(wg_ctx *ctx, int tree, double *host) {
     return interior_transfer(ctx, t, host, 0);
 }
 
-// Streaming RK4 steps with host buffers: two staging buffers, the input of
+// Streaming RK4 steps with host buffers: five staging buffers, the input of
 // step k+1 copied in (copy stream) while step k computes, the result of step
-// k copied out (d2h stream) while step k+1 computes. Every step scatters its
-// input into the state (and the FP32-pipe copy), steps, and gathers the
-// result.
+// k copied out (d2h stream) while step k+1 computes. FP64 precision: every
+// step scatters its input into the state, steps, and gathers the result.
+// FP32-pipe precision: the loop below.
 int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, double *const *outs) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return tree_err();
