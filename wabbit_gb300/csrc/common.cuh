@@ -219,8 +219,6 @@ cudaError_t launch_norm_linf(const int *blk, int nblk, const double *u, BufGeo g
 cudaError_t launch_interior_xfer(const int *slots, int nblk, double *compact, double *A, BufGeo ga, int nc, int Bx,
                                  int By, int Bz, int to_state, const BlockDesc *desc, TreeClock *clk, cudaStream_t s,
                                  void *shadow = nullptr, BufGeo gs = BufGeo{0, 0, 0, 0}, const int *push = nullptr);
-cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
-                                 int Bx, int By, int Bz, int to_full, cudaStream_t s);
 cudaError_t launch_fwt_flags(int dim, const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1,
                              int Bs2, int nc, int wavelet_x, int wavelet_y, const double *eps_use,
                              const int *tsvc, int *flags, double *details, cudaStream_t s, int input_is_wd = 0);

@@ -22,8 +22,6 @@ __device__ __forceinline__ df2 df_from(double v) {
     return {h, l};
 }
 
-__device__ __forceinline__ double df_to(df2 a) { return (double)a.hi + (double)a.lo; }
-
 __device__ __forceinline__ df2 quick_two_sum(float a, float b) {
     const float s = a + b;
     const float e = b - (s - a);
@@ -37,23 +35,7 @@ __device__ __forceinline__ df2 two_sum(float a, float b) {
     return {s, e};
 }
 
-__device__ __forceinline__ df2 df_add(df2 a, df2 b) {
-    const df2 s = two_sum(a.hi, b.hi);
-    const float e = s.lo + (a.lo + b.lo);
-    return quick_two_sum(s.hi, e);
-}
-
 __device__ __forceinline__ df2 df_neg(df2 a) { return {-a.hi, -a.lo}; }
-
-__device__ __forceinline__ df2 df_sub(df2 a, df2 b) { return df_add(a, df_neg(b)); }
-
-__device__ __forceinline__ df2 df_mul(df2 a, df2 b) {
-    const float p = a.hi * b.hi;
-    float e = fmaf(a.hi, b.hi, -p);
-    e = fmaf(a.hi, b.lo, e);
-    e = fmaf(a.lo, b.hi, e);
-    return quick_two_sum(p, e);
-}
 
 // The same operations without the final renormalisation. Their results may
 // carry |lo| above ulp(hi)/2 (after cancellation even |lo| > |hi|); every
@@ -89,7 +71,6 @@ static __device__ __noinline__ df2 df_from_slow(double v) { return df_from(v); }
 static __device__ __noinline__ double df_to_double_slow(float hi, float lo) {
     return __dadd_rn((double)hi, (double)lo);
 }
-static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
 
 // double -> double-float by bit manipulation on the integer units: hi is v
 // truncated to 24 significant bits, lo the remainder truncated to 24 bits
@@ -171,18 +152,6 @@ __device__ __forceinline__ double df_to_double(df2 x) {
     const unsigned long long bits = ((unsigned long long)(hb >> 31) << 63) | ((unsigned long long)e << 52) |
                                     ((unsigned long long)S & 0xfffffffffffffULL);
     return __longlong_as_double((long long)bits);
-}
-
-// float -> double (exact) by bit manipulation; zero, subnormal, inf and nan
-// inputs go through the conversion unit
-__device__ __forceinline__ double f2d_bits(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned ex = (u >> 23) & 0xffu;
-    if (ex == 0u || ex == 0xffu) return f2d_slow(f);
-    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                 ((unsigned long long)(ex - 127 + 1023) << 52) |
-                                 ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)b);
 }
 
 }  // namespace wg

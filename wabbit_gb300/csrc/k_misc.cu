@@ -196,32 +196,6 @@ cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, 
     return cudaGetLastError();
 }
 
-// copy between a compact interior array (nblk, nc, Bz, By, Bx) and the
-// interiors of the listed block slots of a full-layout buffer
-__global__ void interior_copy_kernel(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
-                                     int Bx, int By, int Bz, int to_full) {
-    const long long nint = (long long)Bx * By * Bz;
-    const long long total = (long long)nblk * nc * nint;
-    const int gz = geo.nz > 1 ? geo.gb : 0;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
-        const long long r = q % nint;
-        const int c = (int)((q / nint) % nc);
-        const int b = (int)(q / (nint * nc));
-        const int ix = (int)(r % Bx), iy = (int)((r / Bx) % By), iz = (int)(r / ((long long)Bx * By));
-        double *f = full + ((long long)slots[b] * nc + c) * geo.npts() +
-                    ((long long)(iz + gz) * geo.ny + (iy + geo.gb)) * geo.nx + (ix + geo.gb);
-        if (to_full) *f = compact[q];
-        else compact[q] = *f;
-    }
-}
-
-cudaError_t launch_interior_copy(const int *slots, int nblk, double *full, BufGeo geo, double *compact, int nc,
-                                 int Bx, int By, int Bz, int to_full, cudaStream_t s) {
-    if (nblk <= 0) return cudaSuccess;
-    interior_copy_kernel<<<1024, 256, 0, s>>>(slots, nblk, full, geo, compact, nc, Bx, By, Bz, to_full);
-    return cudaGetLastError();
-}
-
 cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s) {
     clock_advance_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
     return cudaGetLastError();
