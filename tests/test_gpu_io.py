@@ -38,7 +38,7 @@ def test_interior_roundtrip_pinned_and_pageable(dim):
 
 @pytest.mark.parametrize("precision,scales", [(0, (1, 1, 1, 1)), (1, (1, 1, 1, 1)), (1, (1, 8, 0.25, 3, 3))])
 def test_rk4_stream_equals_upload_step_download(precision, scales):
-    """wg_rk4_stream (overlapped transfers, two staging buffers; with the
+    """wg_rk4_stream (overlapped transfers, five staging buffers; with the
     FP32-pipe precision the last stage of a step loads the next input) gives,
     step by step, the same results as upload + wg_rk4_step + download, also
     when the inputs' magnitudes change the anchoring quantum between steps,
@@ -71,3 +71,72 @@ def test_rk4_stream_equals_upload_step_download(precision, scales):
         assert f.time() == t_stream
         f.timeStep_tree()
         assert np.array_equal(f.download_interior(), after)
+
+
+@pytest.mark.parametrize("dim,penal", [(2, 0), (3, 0), (3, 1)])
+def test_dt_from_recorded_maxima_equals_state_scan(dim, penal):
+    """FP32-pipe precision: the dt reduction of a step reads the per-block
+    maxima of |u|^2 that the previous step's last stage recorded; steps
+    replayed from the graph give the same states and times, bit for bit, as
+    steps each preceded by wg_compute_dt (which scans the state, so that the
+    step's own reduction scans it too)."""
+    cfg = small_cfg(dim, "CDF44" if dim == 3 else "CDF40", Bs=16, jmin=1, jmax=2 if dim == 3 else 3, penal=penal)
+    cfg.rhs_precision = 1
+    lv, co = grids.random_graded(dim, cfg.Jmin, cfg.Jmax, seed=11, frac=0.5)
+    rng = np.random.default_rng(12)
+    shape = (len(lv), cfg.neq, cfg.Bs[2] if dim == 3 else 1, cfg.Bs[1], cfg.Bs[0])
+    u0 = 0.2 * rng.standard_normal(shape)
+    nsteps = 6
+    res = []
+    for scan in (False, True):
+        with Context(cfg, len(lv) + 4) as ctx:
+            f = ctx.forest()
+            f.set_grid(lv, co)
+            if penal:
+                f.set_mask_sphere((0.5, 0.6, 0.7), 0.3)
+            f.upload_interior(u0)
+            f.set_time(0.0)
+            if scan:
+                for _ in range(nsteps):
+                    f.calculate_time_step()
+                    f.timeStep_tree()
+            else:
+                f.run(nsteps, use_graph=True)
+            res.append((f.download_interior(), f.time()))
+    assert np.array_equal(res[0][0], res[1][0])
+    assert res[0][1] == res[1][1]
+
+
+def test_stream_divergence_guard_on_the_next_input():
+    """FP32-pipe stream: the divergence guard of a step's input is taken by
+    the previous step's last stage, which loads it; an input with a value
+    above 1e12 makes the tree report WG_EDIVERGED, as the same input uploaded
+    does."""
+    from wabbit_gb300 import capi
+
+    cfg = small_cfg(3, "CDF44", Bs=16, jmin=1, jmax=2)
+    cfg.rhs_precision = 1
+    lv, co = grids.random_graded(3, cfg.Jmin, cfg.Jmax, seed=7, frac=0.5)
+    rng = np.random.default_rng(13)
+    with Context(cfg, len(lv) + 4) as ctx:
+        f = ctx.forest()
+        f.set_grid(lv, co)
+        shape = (len(lv),) + f.interior_shape
+        ins = [torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+        for a in ins:
+            a[...] = 0.1 * rng.standard_normal(shape)
+        outs = [torch.zeros(shape, dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
+        f.set_time(0.0)
+        f.rk4_stream(ins, outs)
+        f.time()                                  # clean inputs: no flag
+        ins[1][2, 3, 5, 4, 1] = 1.0e13
+        f.set_time(0.0)
+        f.rk4_stream(ins, outs)
+        with pytest.raises(capi.WgError) as e:
+            f.time()
+        assert e.value.code == capi.ERRORS_BY_NAME["WG_EDIVERGED"]
+        f.upload_interior(ins[1])
+        f.set_time(0.0)
+        with pytest.raises(capi.WgError) as e:
+            f.timeStep_tree()
+        assert e.value.code == capi.ERRORS_BY_NAME["WG_EDIVERGED"]

@@ -260,6 +260,7 @@ struct wg_ctx {
     std::vector<BlockDesc> h_desc;
     TreeParams *d_tp = nullptr;
     TreeClock *d_clk = nullptr;
+    unsigned long long *d_usq = nullptr;   // per block slot: max |u|^2 the last RK stage stored (TreeClock::usq_ready)
     int max_trees = 64;
     std::vector<Tree> trees;
     SlotPool free_slots;
@@ -297,6 +298,15 @@ TreeClock fresh_clock(double t) {
     c.time = t;
     c.dt_min_bits = kDtStartBits;
     return c;
+}
+
+// the tree's state changed outside an RK step: neither the double-float
+// copy of u_n nor the per-block maxima of |u|^2 the last RK stage recorded
+// (TreeClock::usq_ready) describe it any longer
+static int state_changed(wg_ctx *ctx, Tree *t, int tree) {
+    t->shadow_valid = false;
+    WG_CUDA_OK(cudaMemsetAsync(&ctx->d_clk[tree].usq_ready, 0, sizeof(int), ctx->stream));
+    return WG_OK;
 }
 
 int check_cfg(const wg_config *c) {
@@ -756,7 +766,7 @@ static int stage_pair(wg_ctx *ctx, int stage, const int *plain, int nplain, cons
         return launch_acm_stage_df(dim, stage, msk, blk, n, ctx->d_desc, ctx->d_tp, ctx->d_clk, in, ctx->B, ctx->C,
                                    ctx->D, out, ctx->gT, ctx->A, ctx->gA, ctx->mask_df, pp, Bs[0], Bs[1], Bs[2], tm,
                                    march, ctx->d_err, ctx->stream, keep, ctx->s4_out, ctx->d_pos.p, ctx->s4_next,
-                                   stage == 4 ? ctx->s4_usrc : nullptr);
+                                   stage == 4 ? ctx->s4_usrc : nullptr, ctx->d_usq);
     };
     if (march == 2) {
         WG_CUDA_OK(go(nmasked, both, nplain + nmasked));
@@ -945,10 +955,11 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
         const BufGeo gc = {Bs[0], Bs[1], ctx->cfg.dim == 3 ? Bs[2] : 1, 0};
         WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk,
                              ctx->s4_usrc, gc, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx),
-                             ctx->stream, 1, ctx->d_pos.p));
+                             ctx->stream, 1, ctx->d_pos.p, ctx->d_usq));
     } else {
         WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
-                             ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx), ctx->stream, 1));
+                             ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx), ctx->stream, 1,
+                             nullptr, ctx->d_usq));
     }
     prof_mark(ctx, 2);
     if ((st = stage_launch_df(ctx, t, 1, ctx->B, ctx->C, push))) return st;
@@ -965,7 +976,10 @@ int rk4_enqueue_df(wg_ctx *ctx, int tree_id) {
     prof_mark(ctx, 8);
     if (ctx->s4_wait) WG_CUDA_OK(cudaStreamWaitEvent(ctx->stream, ctx->s4_wait, 0));
     if ((st = stage_launch_df(ctx, t, 4, ctx->E, ctx->B, push, ctx->s4_keep))) return st;
-    WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream));
+    // the last stage recorded the maxima of what it wrote (the state, or in
+    // a streamed step the next input) unless it ran for timing only
+    WG_CUDA_OK(launch_clock_advance(ctx->d_clk, ctx->d_tree_ids.p + tree_id, 1, ctx->stream,
+                                    ctx->s4_keep == 1 || ctx->s4_keep == 3));
     prof_mark(ctx, 9);
     return WG_OK;
 }
@@ -1100,7 +1114,8 @@ int rk4_enqueue_batch(wg_ctx *ctx) {
     if ((st = run_sync_batch(ctx, ctx->B))) return st;
     prof_mark(ctx, 1);
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, bp.all.p, bp.n_all, ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A, ctx->gA, Bs[0],
-                         Bs[1], Bs[2], (int)bp.trees.size(), bp.tree_ids.p, dt_done(ctx), ctx->stream, 1));
+                         Bs[1], Bs[2], (int)bp.trees.size(), bp.tree_ids.p, dt_done(ctx), ctx->stream, 1, nullptr,
+                         ctx->d_usq));
     prof_mark(ctx, 2);
     if ((st = stage_launch_batch(ctx, 1, ctx->B, ctx->C))) return st;
     prof_mark(ctx, 3);
@@ -1115,7 +1130,7 @@ int rk4_enqueue_batch(wg_ctx *ctx) {
     if ((st = run_sync_batch(ctx, ctx->E))) return st;
     prof_mark(ctx, 8);
     if ((st = stage_launch_batch(ctx, 4, ctx->E, ctx->B))) return st;
-    WG_CUDA_OK(launch_clock_advance(ctx->d_clk, bp.tree_ids.p, (int)bp.trees.size(), ctx->stream));
+    WG_CUDA_OK(launch_clock_advance(ctx->d_clk, bp.tree_ids.p, (int)bp.trees.size(), ctx->stream, 1));
     prof_mark(ctx, 9);
     return WG_OK;
 }
@@ -1131,7 +1146,8 @@ int rk4_enqueue(wg_ctx *ctx, int tree_id) {
     if ((st = run_sync(ctx, t, ctx->A, false, g_rhs, g_rhs))) return st;
     prof_mark(ctx, 1);
     WG_CUDA_OK(launch_dt(ctx->cfg.dim, t.d_all.p, (int)t.slots.size(), ctx->d_desc, ctx->d_tp, ctx->d_clk, ctx->A,
-                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx), ctx->stream));
+                         ctx->gA, Bs[0], Bs[1], Bs[2], 1, ctx->d_tree_ids.p + tree_id, dt_done(ctx), ctx->stream, 0,
+                         nullptr, ctx->d_usq));
     prof_mark(ctx, 2);
     if ((st = stage_launch(ctx, t, 1, ctx->A, ctx->gA, ctx->B, ctx->gT))) return st;
     prof_mark(ctx, 3);
@@ -1244,11 +1260,13 @@ int wg_ctx_create(const wg_config *cfg, int max_blocks, wg_ctx **out) {
     }
     if (cudaMalloc(&ctx->d_desc, sizeof(BlockDesc) * max_blocks) != cudaSuccess ||
         cudaMalloc(&ctx->d_tp, sizeof(TreeParams) * ctx->max_trees) != cudaSuccess ||
-        cudaMalloc(&ctx->d_clk, sizeof(TreeClock) * ctx->max_trees) != cudaSuccess) {
+        cudaMalloc(&ctx->d_clk, sizeof(TreeClock) * ctx->max_trees) != cudaSuccess ||
+        cudaMalloc(&ctx->d_usq, sizeof(unsigned long long) * max_blocks) != cudaSuccess) {
         cudaGetLastError();
         wg_ctx_destroy(ctx.release());
         return fail(WG_ENOMEM, "device allocation of descriptors failed");
     }
+    cudaMemsetAsync(ctx->d_usq, 0, sizeof(unsigned long long) * max_blocks, ctx->stream);
     cudaMemsetAsync(ctx->A, 0, bytesA, ctx->stream);
     cudaMemsetAsync(ctx->B, 0, bytesT, ctx->stream);
     cudaMemsetAsync(ctx->C, 0, bytesT, ctx->stream);
@@ -1312,6 +1330,7 @@ int wg_ctx_destroy(wg_ctx *ctx) {
     cudaFree(ctx->d_desc);
     cudaFree(ctx->d_tp);
     cudaFree(ctx->d_clk);
+    cudaFree(ctx->d_usq);
     for (cudaEvent_t ev : ctx->copy_ev) cudaEventDestroy(ev);
     for (cudaEvent_t ev : ctx->prof_ev)
         if (ev) cudaEventDestroy(ev);
@@ -1386,7 +1405,7 @@ int wg_set_grid(wg_ctx *ctx, int tree, int nblk, const int *level, const int *co
     t->slots.resize(nblk);
     t->status.clear();
     t->mask_slot.assign(nblk, -1);
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     // the lowest free slots in ascending order (contiguous copies)
     for (int b = 0; b < nblk; b++) t->slots[b] = ctx->free_slots.take();
     int st;
@@ -1427,7 +1446,7 @@ int wg_upload_state(wg_ctx *ctx, int tree, const double *host_blocks) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return tree_err();
     if (!host_blocks) return fail(WG_EINVAL, "bad arguments");
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     const size_t per = sizeof(double) * ctx->geo.nc * ctx->gA.npts();
     if (!t->slots.empty() && contiguous(t->slots)) {
         WG_CUDA_OK(cudaMemcpyAsync((char *)ctx->A + per * t->slots[0], host_blocks, per * t->slots.size(),
@@ -1922,7 +1941,7 @@ int wg_wavelet_decompose(wg_ctx *ctx, int tree) {
     const int *Bs = ctx->cfg.Bs;
     WG_CUDA_OK(launch_wavelet_decompose(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0], Bs[1],
                                         Bs[2], ctx->geo.nc, ctx->wav.X, ctx->wav.Y, ctx->stream));
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     return WG_OK;
 }
@@ -1933,7 +1952,7 @@ int wg_wavelet_reconstruct(wg_ctx *ctx, int tree) {
     const int *Bs = ctx->cfg.Bs;
     WG_CUDA_OK(launch_wavelet_reconstruct(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0],
                                           Bs[1], Bs[2], ctx->geo.nc, ctx->wav.X, ctx->wav.Y, ctx->stream));
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     return WG_OK;
 }
@@ -1946,7 +1965,7 @@ int wg_wavelet_threshold(wg_ctx *ctx, int tree, const double *thresh) {
     const int *Bs = ctx->cfg.Bs;
     WG_CUDA_OK(launch_wc_threshold(ctx->cfg.dim, t->d_all.p, (int)t->slots.size(), ctx->A, ctx->gA, Bs[0], Bs[1],
                                    Bs[2], ctx->geo.nc, thresh, t->cfg.threshold_state_vector_component, ctx->stream));
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     return WG_OK;
 }
@@ -2475,7 +2494,7 @@ static int adapt_lifted(wg_ctx *ctx, Tree *t, int tree, const double *eps_use, b
     t->status = stat;
     t->mask_slot.assign(nn, -1);
     drop_sync(*t);
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     int st;
     if ((st = upload_desc(ctx, *t, tree))) return st;
     if ((st = upload_lists(ctx, *t))) return st;
@@ -2608,7 +2627,7 @@ int wg_adapt(wg_ctx *ctx, int tree, const double *eps_use, int indicator, int *n
     t->status = stat;
     t->mask_slot.assign(nn, -1);
     drop_sync(*t);
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     if ((st = upload_desc(ctx, *t, tree))) return st;
     if ((st = upload_lists(ctx, *t))) return st;
     if ((st = regen_masks(ctx, t, tree))) return st;
@@ -2749,7 +2768,7 @@ static int refine_blocks(wg_ctx *ctx, Tree *t, int tree, const std::vector<char>
     t->slots = slots;
     t->status.clear();
     t->mask_slot.assign(nn, -1);
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     drop_sync(*t);
     t->forest.set(nn, lv.data(), co.data());
     std::string err;
@@ -3112,7 +3131,7 @@ int wg_upload_interior(wg_ctx *ctx, int tree, const double *host) {
     Tree *t = get_tree(ctx, tree);
     if (!t) return tree_err();
     if (!host) return fail(WG_EINVAL, "bad arguments");
-    t->shadow_valid = false;
+    if (const int sc = state_changed(ctx, t, tree)) return sc;
     // the staging buffer is free once the stream's earlier work is done
     WG_CUDA_OK(cudaStreamSynchronize(ctx->stream));
     return interior_transfer(ctx, t, const_cast<double *>(host), 1);
@@ -3187,6 +3206,7 @@ int wg_rk4_stream(wg_ctx *ctx, int tree, int nsteps, const double *const *ins, d
     WG_CUDA_OK(cudaMemcpyAsync(I[0], ins[0], bytes, cudaMemcpyDefault, ctx->copy_stream));
     WG_CUDA_OK(cudaEventRecord(h2d_done[0], ctx->copy_stream));
     auto scatter = [&](double *in) -> int {   // input into the state (and its anchored copy)
+        WG_CUDA_OK(cudaMemsetAsync(&ctx->d_clk[tree].usq_ready, 0, sizeof(int), ctx->stream));
         if (shadow) WG_CUDA_OK(launch_umax_reset(ctx->d_clk, ctx->d_tree_ids.p + tree, 1, ctx->stream));
         WG_CUDA_OK(launch_interior_xfer(t->d_all.p, nblk, in, ctx->A, ctx->gA, ctx->geo.nc, Bs[0], Bs[1], Bz, 1,
                                         ctx->d_desc, shadow ? ctx->d_clk : nullptr, ctx->stream,

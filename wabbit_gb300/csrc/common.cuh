@@ -42,6 +42,12 @@ struct TreeClock {
     // M is chosen.
     float  anchor_M;
     unsigned umax_f;
+    // usq_ready: the last RK stage recorded every block's max |u|^2 of the
+    // state it wrote (BlockUsq, per block slot) and its divergence guard
+    // (div_next), and nothing has changed the state since; the next dt
+    // reduction then reads those maxima instead of the state
+    int    usq_ready;
+    int    div_next;
 };
 
 // Per-block descriptor. k1, k2: first-derivative weights (2/3)/dx, (1/12)/dx;
@@ -139,7 +145,7 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
                                 cudaStream_t s, int keep_state = 1, double *cout = nullptr,
                                 const int *cpos = nullptr, const double *nin = nullptr,
-                                const double *usrc = nullptr);
+                                const double *usrc = nullptr, unsigned long long *usq = nullptr);
 // (march 0, 3, 4: tmap is a slab map of 4, 2 or 8 interior planes and the
 // tile kernel of that slab height runs; 1: tmap is a map
 // with one-plane boxes and the whole-block ring kernel runs; 2: tmap is a
@@ -203,11 +209,15 @@ cudaError_t launch_sphere_fill(const int4 *cand, const int *slot, int n, const S
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
                       const int *trees, unsigned *done, cudaStream_t s, int step_start = 0,
-                      const int *upos = nullptr);
+                      const int *upos = nullptr, unsigned long long *usq = nullptr);
 // (upos: u is indexed by upos[slot] instead of the slot, e.g. a compact
-// interior array with geo = {Bs0, Bs1, Bs2, 0})
+// interior array with geo = {Bs0, Bs1, Bs2, 0}; usq: the per-slot maxima
+// the last RK stage records: read instead of the state for the trees whose
+// TreeClock::usq_ready is set, set back to zero for every listed block)
 
-cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s);
+// time += dt for the listed trees; usq_ready: the step's last stage recorded
+// the per-block maxima of the state it wrote (TreeClock::usq_ready)
+cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s, int usq_ready = 0);
 // max |u| per component over the interiors of the listed blocks (Bs2 = 1 in 2-D)
 cudaError_t launch_norm_linf(const int *blk, int nblk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int nc,
                              double *out, cudaStream_t s);

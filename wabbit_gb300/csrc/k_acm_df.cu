@@ -30,6 +30,7 @@
 #include "common.cuh"
 #include "df.cuh"
 #include "tma.cuh"
+#include "umag.cuh"
 
 namespace wg {
 
@@ -50,6 +51,7 @@ struct StageArgsDF {
     const double *nin;     // stage 4: the next step's input (compact like cout): its anchored copy to out, or null
     const double *usrc;    // stage 4: u_n read from this compact array (positions cpos) instead of un, or null
     int record;            // stage 4: merge the maximum of what it stores into the tree's running max
+    unsigned long long *usq;   // stage 4 (recording): per block slot, max |u|^2 of what it stores (bits + 1), or null
     int rewrite;           // stage 4: store u_n (unchanged) where u_n+1 would go (timing with the state's traffic)
     BufGeo gun;
     const float2 *mask;    // 5 words per point, interior only
@@ -322,6 +324,34 @@ __device__ __forceinline__ void rk_load(const StageArgsDF &a, int b, int ix, int
     }
 }
 
+// The per-block maximum of |u|^2 that the next dt reduction needs
+// (k_misc.cu::dt_kernel), taken from the values the last stage stores: the
+// FP64 sum u*u + v*v (+ w*w) rounded in the reduction's order, and its
+// divergence guard on every component. usq_term adds component c.
+template <int DIM>
+__device__ __forceinline__ void usq_term(int c, double w, double &usq, bool &ok) {
+    ok &= within_guard(w);
+    if (c < DIM) {
+        const double p = __dmul_rn(w, w);
+        usq = c == 0 ? p : __dadd_rn(usq, p);
+    }
+}
+
+// merge of one point's |u|^2 into the block's maximum: the warp's maximum
+// (every warp of every stage form holds points of one block) by one atomic.
+// The reduction's fmax skips nan sums, so they do not count here either; a
+// value s >= 0 is kept as its bits + 1 (ordered like s), 0 meaning none.
+__device__ __forceinline__ void usq_merge(const StageArgsDF &a, int b, double usq, bool ok) {
+    unsigned long long e = (unsigned long long)__double_as_longlong(usq);
+    e = (e & 0x7fffffffffffffffull) > 0x7ff0000000000000ull ? 0ull : e + 1ull;
+    const unsigned am = __activemask();
+    const unsigned hi = __reduce_max_sync(am, (unsigned)(e >> 32));
+    const unsigned lo = __reduce_max_sync(am, (unsigned)(e >> 32) == hi ? (unsigned)e : 0u);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(am) - 1) && (hi | lo))
+        atomicMax(a.usq + b, ((unsigned long long)hi << 32) | lo);
+    if (!ok) atomicOr(&a.clk[a.desc[b].tree].div_next, 1);
+}
+
 // RK4 stage update of one point: stages 1-3 write the anchored next stage
 // input u_n + a dt k_j (a = 1/2, 1/2, 1), stage 4 writes u_n+1 to the FP64
 // state (unless un_out is null), to cout (when given) and its anchored copy
@@ -356,6 +386,8 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
         const long long cbase = a.cout || a.nin ? (long long)a.cpos[b] * (DIM + 1) * nint +
                                                       ((DIM == 3 ? iz * a.Bs1 : 0) + iy) * a.Bs0 + ix
                                                 : 0;
+        double usq = 0.0;   // |u|^2 of the stored velocity, in the order of the dt reduction
+        bool ok = true;     // every stored component within the divergence guard
 #pragma unroll
         for (int c = 0; c <= DIM; c++) {
             const double u = f2_bits(in.c[c]);
@@ -371,6 +403,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
             if (a.cout) a.cout[ci] = v;
             if (a.nin) {   // the next input takes the place of u_n+1 in the anchored copy
                 const double x = __ldcs(a.nin + ci);
+                if (a.usq) usq_term<DIM>(c, x, usq, ok);
                 if (ob) {
                     const df2 sx = df_split(x);
                     const df2 w = anchor(sx, k.M);
@@ -381,6 +414,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
                 continue;
             }
             if (a.un_out) un[c * us] = a.rewrite ? u : v;
+            if (a.usq) usq_term<DIM>(c, v, usq, ok);
             if (ob) {   // the anchored copy of u_n+1 and its running maximum
                 const df2 w = anchor(df_add_nr(ud, inc), k.M);
                 ov[c] = make_float2(w.hi, w.lo);
@@ -388,6 +422,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
                 umax = fmaxf(umax, fabsf(w.hi));
             }
         }
+        if (a.usq) usq_merge(a, b, usq, ok);
         if (!ob) return;   // the result went to cout alone
     }
     if (a.push) push_ghosts<DIM, DIM + 1>(a.push, b, ix, iy, iz, a.Bs0, a.Bs1, a.Bs2, a.gt, a.out, cs, ov);
@@ -711,7 +746,7 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
                                 const void *s3, void *out, BufGeo gt, double *un, BufGeo gun, const void *maskdf,
                                 const int *push, int Bs0, int Bs1, int Bs2, const void *tmap, int march, int *err,
                                 cudaStream_t s, int keep_state, double *cout, const int *cpos, const double *nin,
-                                const double *usrc) {
+                                const double *usrc, unsigned long long *usq) {
     if (nblk <= 0) return cudaSuccess;
     if (stage < 1 || stage > 4) return cudaErrorInvalidValue;
     StageArgsDF a;
@@ -742,6 +777,7 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.cout = (keep_state == 1 || keep_state == 2 || keep_state == 3) && stage == 4 ? cout : nullptr;
     a.nin = keep_state == 3 ? nin : nullptr;
     a.record = keep_state == 1 || keep_state == 3;
+    a.usq = a.record && stage == 4 ? usq : nullptr;
     a.rewrite = keep_state == 4;
     if (keep_state == 2) a.out = nullptr;
     a.cpos = cpos;

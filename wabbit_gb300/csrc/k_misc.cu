@@ -5,6 +5,8 @@
 // LIB/TIME/calculate_time_step.f90:28-48), then the output-time trimming of
 // calculate_time_step.f90:50-118 -- all on the device, so that a whole RK4
 // step can be captured in a CUDA graph.
+#include <algorithm>
+
 #include "common.cuh"
 #include "df.cuh"
 #include "exact.cuh"
@@ -35,11 +37,10 @@ __device__ __forceinline__ double usq_exact(const double *ub, long long np, long
     return s;
 }
 
-// GET_DT_BLOCK_ACM of one block from its max |u|^2, then the atomic min
-// over the blocks of its tree (calculate_time_step.f90:28-48)
+// GET_DT_BLOCK_ACM of one block from its max |u|^2 (u_mag; the callers
+// take the atomic min over the blocks of its tree, calculate_time_step.f90:28-48)
 template <int DIM>
-__device__ __forceinline__ void dt_of_block(const TreeParams &p, const BlockDesc &d, double u_mag,
-                                            TreeClock &c) {
+__device__ __forceinline__ double dt_of_block(const TreeParams &p, const BlockDesc &d, double u_mag) {
     const double u_eigen = __dadd_rn(sqrt(u_mag), sqrt(__dadd_rn(__dmul_rn(p.c0, p.c0), u_mag)));
     double dxmin = d.dx[0];
     for (int k = 1; k < DIM; k++) dxmin = fmin(dxmin, d.dx[k]);
@@ -48,31 +49,30 @@ __device__ __forceinline__ void dt_of_block(const TreeParams &p, const BlockDesc
     if (p.gamma_p > 0) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.gamma_p));
     if (p.penalization) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.C_eta));
     if (p.use_sponge) dt = fmin(dt, __dmul_rn(p.CFL_eta, p.C_sponge));
-    atomicMin(&c.dt_min_bits, (unsigned long long)__double_as_longlong(dt));
+    return dt;
 }
 
-// Per-block max |u|^2 over the interior (two passes, umag.cuh) -> per-block
-// dt -> atomic min per tree; a value outside the divergence guard sets the
-// tree's flag.
-// The last CTA to finish (counter *done, set back to zero by it) finalises
-// the listed trees, so the whole reduction is one launch.
+// dt_kernel: per block the max |u|^2 over the interior -- the maximum the
+// last RK stage recorded while it wrote the state (trees with
+// TreeClock::usq_ready), else from the state (two passes, umag.cuh) -> the
+// block's dt -> atomic min per tree; a value outside the divergence guard
+// sets the tree's flag. The last CTA to finish (counter *done, set back to
+// zero by it) finalises the listed trees, so the whole reduction is one
+// launch.
 __device__ void dt_finalize_tree(const TreeParams *tp, TreeClock *clk, int t, int step_start);
 
-// BS: the block edge when all edges equal it (index arithmetic by shifts),
-// 0 for the general case
+// the max |u|^2 of block b from its state (two passes, umag.cuh), its dt
+// merged into the tree's minimum, the divergence guard into its flag; every
+// thread of the CTA calls it
 template <int DIM, int BS>
-__global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc *desc, const TreeParams *tp,
-                                                 TreeClock *clk, const double *u, BufGeo geo, int Bs0_, int Bs1_,
-                                                 int Bs2_, const int *trees, int ntrees, int step_start,
-                                                 unsigned *done, const int *upos) {
+__device__ __forceinline__ void dt_scan_block(const BlockDesc &d, TreeClock *clk, const TreeParams *tp,
+                                              const double *u, BufGeo geo, int Bs0_, int Bs1_, int Bs2_,
+                                              const int *upos, int b) {
     const int Bs0 = BS ? BS : Bs0_, Bs1 = BS ? BS : Bs1_, Bs2 = BS ? BS : Bs2_;
-    __shared__ int s_last;
     constexpr int kCache = 4096;
     __shared__ float s32[kCache];
     __shared__ float red32[8];
     __shared__ double red64[8];
-    const int b = blk[blockIdx.x];
-    const BlockDesc &d = desc[b];
     const long long np = geo.npts();
     const int nint = Bs0 * Bs1 * (DIM == 3 ? Bs2 : 1);
     const bool cache = nint <= kCache;
@@ -111,7 +111,57 @@ __global__ void __launch_bounds__(256) dt_kernel(const int *blk, const BlockDesc
     if (threadIdx.x == 0) {
         double u_mag = red64[0];
         for (int w = 1; w < (int)(blockDim.x >> 5); w++) u_mag = fmax(u_mag, red64[w]);
-        dt_of_block<DIM>(tp[d.tree], d, u_mag, clk[d.tree]);
+        atomicMin(&clk[d.tree].dt_min_bits,
+                  (unsigned long long)__double_as_longlong(dt_of_block<DIM>(tp[d.tree], d, u_mag)));
+    }
+}
+
+// A grid of resident CTAs: the blocks whose tree's last RK stage recorded
+// their maxima take one thread each (their dt merged per warp and tree), the
+// others one CTA each in turn. BS: the block edge when all edges equal it
+// (index arithmetic by shifts), 0 for the general case.
+template <int DIM, int BS>
+__global__ void __launch_bounds__(256) dt_kernel(const int *blk, int nblk, const BlockDesc *desc,
+                                                 const TreeParams *tp, TreeClock *clk, const double *u, BufGeo geo,
+                                                 int Bs0, int Bs1, int Bs2, const int *trees, int ntrees,
+                                                 int step_start, unsigned *done, const int *upos,
+                                                 unsigned long long *usq) {
+    __shared__ int s_last;
+    // a tree's flag was set before this launch and is cleared only by the
+    // last CTA, after every CTA has read it
+    if (usq) {
+        const int span = (int)(gridDim.x * blockDim.x);
+        for (int j0 = (int)(blockIdx.x * blockDim.x); j0 < nblk; j0 += span) {   // uniform over the CTA
+            const int j = j0 + (int)threadIdx.x;
+            int tree = -1;
+            unsigned long long bits = ~0ull;
+            if (j < nblk) {
+                const int b = blk[j];
+                const BlockDesc &d = desc[b];
+                if (__ldcg(&clk[d.tree].usq_ready)) {
+                    const unsigned long long e = usq[b];
+                    usq[b] = 0ull;
+                    tree = d.tree;
+                    bits = (unsigned long long)__double_as_longlong(
+                        dt_of_block<DIM>(tp[tree], d, e ? __longlong_as_double((long long)(e - 1ull)) : -1.0));
+                }
+            }
+            // dt >= 0: the minimum of the bits is the minimum, per tree
+            const unsigned grp = __match_any_sync(0xffffffffu, tree);
+            const unsigned hi = __reduce_min_sync(grp, (unsigned)(bits >> 32));
+            const unsigned lo = __reduce_min_sync(grp, (unsigned)(bits >> 32) == hi ? (unsigned)bits : 0xffffffffu);
+            if (tree >= 0 && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1))
+                atomicMin(&clk[tree].dt_min_bits, ((unsigned long long)hi << 32) | lo);
+        }
+    }
+    for (int i = (int)blockIdx.x; i < nblk; i += (int)gridDim.x) {
+        const int b = blk[i];
+        const BlockDesc &d = desc[b];
+        if (usq && __ldcg(&clk[d.tree].usq_ready)) continue;   // uniform over the CTA
+        dt_scan_block<DIM, BS>(d, clk, tp, u, geo, Bs0, Bs1, Bs2, upos, b);
+        if (usq && threadIdx.x == 0) usq[b] = 0ull;
+    }
+    if (threadIdx.x == 0) {
         // acquire-release count of the finished CTAs: the last one sees every
         // other CTA's minimum (and flag) before it finalises
         unsigned n;
@@ -153,6 +203,11 @@ __device__ void dt_finalize_tree(const TreeParams *tp, TreeClock *clk, int t, in
     }
     if (__dadd_rn(time, dt) > p.time_max && time <= p.time_max) dt = __dsub_rn(p.time_max, time);
     c.dt = dt;
+    // the divergence guard the last RK stage took on the state it wrote, if
+    // this reduction used its maxima
+    if (c.usq_ready && c.div_next) c.diverged = 1;
+    c.usq_ready = 0;
+    c.div_next = 0;
     const df2 f1 = df_from(dt), f3 = df_from(__ddiv_rn(dt, 3.0)), f6 = df_from(__ddiv_rn(dt, 6.0));
     c.f_dt[0] = f1.hi;
     c.f_dt[1] = f1.lo;
@@ -174,30 +229,40 @@ __global__ void dt_finalize_kernel(const TreeParams *tp, TreeClock *clk, const i
     if (i < ntrees) dt_finalize_tree(tp, clk, trees[i], step_start);
 }
 
-__global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntrees) {
+__global__ void clock_advance_kernel(TreeClock *clk, const int *trees, int ntrees, int usq_ready) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < ntrees) {
         TreeClock &c = clk[trees[i]];
         c.time = __dadd_rn(c.time, c.dt);
+        c.usq_ready = usq_ready;
     }
 }
 
 cudaError_t launch_dt(int dim, const int *blk, int nblk, const BlockDesc *desc, const TreeParams *tp,
                       TreeClock *clk, const double *u, BufGeo geo, int Bs0, int Bs1, int Bs2, int ntrees,
-                      const int *trees, unsigned *done, cudaStream_t s, int step_start, const int *upos) {
+                      const int *trees, unsigned *done, cudaStream_t s, int step_start, const int *upos,
+                      unsigned long long *usq) {
     if (!done) return cudaErrorInvalidValue;
     if (nblk > 0) {
         const bool b16 = Bs0 == 16 && Bs1 == 16 && (dim == 2 || Bs2 == 16);
         auto k = dim == 2 ? (b16 ? dt_kernel<2, 16> : dt_kernel<2, 0>) : (b16 ? dt_kernel<3, 16> : dt_kernel<3, 0>);
-        k<<<nblk, 256, 0, s>>>(blk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2, trees, ntrees, step_start, done, upos);
+        // as many CTAs as are resident at once (every CTA loops)
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, 0);
+        if (e != cudaSuccess) return e;
+        const int grid = std::min(nblk, std::max(1, sms * per_sm));
+        k<<<grid, 256, 0, s>>>(blk, nblk, desc, tp, clk, u, geo, Bs0, Bs1, Bs2, trees, ntrees, step_start, done,
+                               upos, usq);
     } else {
         dt_finalize_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(tp, clk, trees, ntrees, step_start);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s) {
-    clock_advance_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees);
+cudaError_t launch_clock_advance(TreeClock *clk, const int *trees, int ntrees, cudaStream_t s, int usq_ready) {
+    clock_advance_kernel<<<(ntrees + 127) / 128, 128, 0, s>>>(clk, trees, ntrees, usq_ready);
     return cudaGetLastError();
 }
 
