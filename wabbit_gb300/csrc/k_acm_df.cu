@@ -51,7 +51,7 @@ struct StageArgsDF {
     const double *nin;     // stage 4: the next step's input (compact like cout): its anchored copy to out, or null
     const double *usrc;    // stage 4: u_n read from this compact array (positions cpos) instead of un, or null
     int record;            // stage 4: merge the maximum of what it stores into the tree's running max
-    unsigned long long *usq;   // stage 4 (recording): per block slot, max |u|^2 of what it stores (bits + 1), or null
+    unsigned long long *usq;   // stage 4: per block slot, max |u|^2 of what it stores (bits + 1), or null
     int rewrite;           // stage 4: store u_n (unchanged) where u_n+1 would go (timing with the state's traffic)
     BufGeo gun;
     const float2 *mask;    // 5 words per point, interior only
@@ -414,7 +414,7 @@ __device__ __forceinline__ void rk_df(const StageArgsDF &a, const DfConst &k, in
                 continue;
             }
             if (a.un_out) un[c * us] = a.rewrite ? u : v;
-            if (a.usq) usq_term<DIM>(c, v, usq, ok);
+            if (a.usq) usq_term<DIM>(c, a.rewrite ? u : v, usq, ok);
             if (ob) {   // the anchored copy of u_n+1 and its running maximum
                 const df2 w = anchor(df_add_nr(ud, inc), k.M);
                 ov[c] = make_float2(w.hi, w.lo);
@@ -777,7 +777,10 @@ cudaError_t launch_acm_stage_df(int dim, int stage, int masked, const int *blk, 
     a.cout = (keep_state == 1 || keep_state == 2 || keep_state == 3) && stage == 4 ? cout : nullptr;
     a.nin = keep_state == 3 ? nin : nullptr;
     a.record = keep_state == 1 || keep_state == 3;
-    a.usq = a.record && stage == 4 ? usq : nullptr;
+    // (timing with the state's traffic records the maxima of the state it
+    // rewrites, the values the recording of the last stage that wrote the
+    // state holds: the timed kernel does the same work as the real one)
+    a.usq = (a.record || keep_state == 4) && stage == 4 ? usq : nullptr;
     a.rewrite = keep_state == 4;
     if (keep_state == 2) a.out = nullptr;
     a.cpos = cpos;
