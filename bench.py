@@ -12,9 +12,12 @@ configuration at Jmax=6 (4,208 blocks).
 
 value: point-updates/s with the state resident in HBM, K steps replayed from
        a captured CUDA graph, timed with CUDA events on the solver's stream.
-e2e:   the same through the C ABI with host buffers: every step uploads the
-       interior state from pinned host memory, runs wg_rk4_step (which reads
-       back time and dt) and downloads the interior state.
+e2e:   the same through the C ABI with host buffers: wg_rk4_stream over a
+       stream of at least 40 steps, every step's input copied in from pinned
+       host memory and its result copied out to pinned host memory (the
+       copies of neighbouring steps overlap the step on the device);
+       e2e.sequential: wg_upload_interior + wg_rk4_step +
+       wg_download_interior one after another.
 plain_fp64: the plain per-solve FP64 path on the same grid and IC (one
        wg_rk4_step call per step, no graph), its speed and the relative L2
        difference of the two states after K steps.
